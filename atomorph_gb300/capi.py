@@ -1,0 +1,308 @@
+"""ctypes binding of the atomorph_gb300 C ABI (include/atomorph_gb300.h).
+
+This is thin glue for Python callers (tests, the benchmark); the
+reference-facing host API is the C++ class ``am::morph`` in
+include/atomorph_gb300.hpp.  The binding loads the in-tree CUDA library and
+raises if it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libatomorph_gb300.so")
+HEADER = os.path.join(HERE, "..", "include", "atomorph_gb300.h")
+
+AM_OK, AM_ERR_BUSY, AM_ERR_NOMEM, AM_ERR_CUDA, AM_ERR_TIMEOUT, AM_ERR_ARG, AM_ERR_STATE, AM_ERR_UNSUPPORTED, \
+    AM_ERR_NOT_FOUND = range(9)
+RGB, HSP, NONE, LINEAR, SPLINE, COSINE, PERLIN = range(7)
+STATE_BLOB_DETECTION, STATE_BLOB_UNIFICATION, STATE_BLOB_MATCHING, STATE_ATOM_MORPHING, STATE_DONE = range(5)
+PROPOSAL_RANDOM, PROPOSAL_LOCAL, PROPOSAL_LEARNED = range(3)
+
+u8p = C.POINTER(C.c_uint8)
+u64p = C.POINTER(C.c_uint64)
+i32p = C.POINTER(C.c_int32)
+f64p = C.POINTER(C.c_double)
+f32p = C.POINTER(C.c_float)
+vp = C.c_void_p
+
+_SIGS = {
+    "am_create": (C.c_int, [C.POINTER(vp)]),
+    "am_destroy": (None, [vp]),
+    "am_clear": (C.c_int, [vp]),
+    "am_last_error": (C.c_char_p, []),
+    "am_version": (C.c_char_p, []),
+    "am_add_pixel": (C.c_int, [vp, C.c_size_t, C.c_uint16, C.c_uint16, C.c_uint8, C.c_uint8, C.c_uint8, C.c_uint8]),
+    "am_add_pixels": (C.c_int, [vp, C.c_size_t, u8p, C.c_uint32, C.c_uint32]),
+    "am_add_frame": (C.c_int, [vp, C.c_size_t]),
+    "am_set_seed": (C.c_int, [vp, C.c_uint]),
+    "am_set_blob_delimiter": (C.c_int, [vp, C.c_uint]),
+    "am_set_blob_threshold": (C.c_int, [vp, C.c_double]),
+    "am_set_blob_max_size": (C.c_int, [vp, C.c_size_t]),
+    "am_set_blob_min_size": (C.c_int, [vp, C.c_size_t]),
+    "am_set_blob_box_grip": (C.c_int, [vp, C.c_uint16]),
+    "am_set_blob_box_samples": (C.c_int, [vp, C.c_size_t]),
+    "am_set_blob_number": (C.c_int, [vp, C.c_size_t]),
+    "am_set_blob_rgba_weight": (C.c_int, [vp, C.c_uint]),
+    "am_set_blob_size_weight": (C.c_int, [vp, C.c_uint]),
+    "am_set_blob_xy_weight": (C.c_int, [vp, C.c_uint]),
+    "am_set_degeneration": (C.c_int, [vp, C.c_size_t]),
+    "am_set_motion": (C.c_int, [vp, C.c_uint]),
+    "am_set_fading": (C.c_int, [vp, C.c_uint]),
+    "am_set_threads": (C.c_int, [vp, C.c_size_t]),
+    "am_set_cycle_length": (C.c_int, [vp, C.c_size_t]),
+    "am_set_feather": (C.c_int, [vp, C.c_size_t]),
+    "am_set_keep_background": (C.c_int, [vp, C.c_int]),
+    "am_set_finite": (C.c_int, [vp, C.c_int]),
+    "am_set_show_blobs": (C.c_int, [vp, C.c_uint]),
+    "am_set_fluid": (C.c_int, [vp, C.c_uint]),
+    "am_set_density": (C.c_int, [vp, C.c_uint16]),
+    "am_set_resolution": (C.c_int, [vp, C.c_uint16, C.c_uint16]),
+    "am_set_proposal": (C.c_int, [vp, C.c_uint]),
+    "am_set_sweeps": (C.c_int, [vp, C.c_size_t]),
+    "am_set_motion_noise": (C.c_int, [vp, C.c_double]),
+    "am_compute": (C.c_int, [vp]),
+    "am_iterate": (C.c_int, [vp, C.c_size_t]),
+    "am_compute_seconds": (C.c_int, [vp, C.c_double]),
+    "am_suspend": (C.c_int, [vp]),
+    "am_suspend_timeout": (C.c_int, [vp, C.c_double]),
+    "am_is_busy": (C.c_int, [vp]),
+    "am_synchronize": (C.c_int, [vp]),
+    "am_next_state": (C.c_int, [vp]),
+    "am_get_state": (C.c_uint, [vp]),
+    "am_get_energy": (C.c_double, [vp]),
+    "am_get_cost": (C.c_int, [vp, u64p, f64p]),
+    "am_get_blob_count": (C.c_size_t, [vp, C.c_size_t]),
+    "am_get_blob_count_total": (C.c_size_t, [vp]),
+    "am_get_pixel_count": (C.c_size_t, [vp, C.c_size_t]),
+    "am_get_frame_count": (C.c_size_t, [vp]),
+    "am_get_frame_key": (C.c_size_t, [vp, C.c_double]),
+    "am_get_width": (C.c_uint16, [vp]),
+    "am_get_height": (C.c_uint16, [vp]),
+    "am_get_time": (C.c_double, [vp, C.c_size_t, C.c_size_t]),
+    "am_get_average_pixel": (C.c_int, [vp, C.c_size_t, C.POINTER(C.c_uint16), u8p]),
+    "am_get_blob_average": (C.c_int, [vp, C.c_size_t, C.c_size_t, C.POINTER(C.c_uint16), u8p]),
+    "am_get_atom_count": (C.c_size_t, [vp]),
+    "am_get_chain_count": (C.c_size_t, [vp]),
+    "am_render": (C.c_int, [vp, C.c_double, vp, C.c_int]),
+    "am_render_many": (C.c_int, [vp, f64p, C.c_size_t, vp]),
+    "am_export_chains": (C.c_int, [vp, u64p, u64p, i32p]),
+    "am_import_chains": (C.c_int, [vp, C.c_size_t, C.c_size_t, u64p, u64p, i32p]),
+    "am_refine": (C.c_int, [vp, C.c_size_t, u64p]),
+    "am_get_stream": (vp, [vp]),
+    "am_launch_count": (C.c_uint64, []),
+    "am_device_sync": (C.c_int, [vp]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the CUDA library (built by atomorph_gb300.build); raises if it is
+    not there."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"atomorph_gb300 CUDA library not built: {LIB_PATH} (run __graft_entry__.build())")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    import re
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(am_[a-z_0-9]+)\s*\(", text)))
+
+
+class AmError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        msg = (load().am_last_error() or b"").decode(errors="replace")
+        super().__init__(f"{what} failed with status {code}: {msg}")
+        self.code = code
+
+
+def _check(rc: int, what: str) -> int:
+    if rc != AM_OK:
+        raise AmError(rc, what)
+    return rc
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+class Morph:
+    """One morph handle (the GB300 counterpart of am::morph)."""
+
+    def __init__(self):
+        self.lib = load()
+        h = vp()
+        _check(self.lib.am_create(C.byref(h)), "am_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.am_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- setters: morph.h:52-76 ---------------------------------------------
+    def set(self, **kw) -> "Morph":
+        for k, v in kw.items():
+            f = getattr(self.lib, "am_set_" + k)
+            if k == "resolution":
+                _check(f(self.h, *v), "am_set_" + k)
+            else:
+                _check(f(self.h, v), "am_set_" + k)
+        return self
+
+    def add_image(self, frame: int, img: np.ndarray) -> None:
+        img = np.ascontiguousarray(img, np.uint8)
+        _check(self.lib.am_add_pixels(self.h, frame, _p(img, u8p), img.shape[1], img.shape[0]), "am_add_pixels")
+
+    def add_pixel(self, frame, x, y, r, g, b, a) -> int:
+        return self.lib.am_add_pixel(self.h, frame, x, y, r, g, b, a)
+
+    def add_frame(self, frame) -> int:
+        return self.lib.am_add_frame(self.h, frame)
+
+    def load(self, frames, **settings) -> "Morph":
+        """Adds key frames 0..K-1 and sets the resolution to their extent, as
+        the reference demo's load_files does (demo/main.cpp:135-176)."""
+        self.set(**settings)
+        w = h = 0
+        for i, img in enumerate(frames):
+            self.add_image(i, img)
+            w, h = max(w, img.shape[1]), max(h, img.shape[0])
+        self.set(resolution=(w, h))
+        return self
+
+    # -- control -------------------------------------------------------------
+    def synchronize(self) -> int:
+        return self.lib.am_synchronize(self.h)
+
+    def iterate(self, n: int) -> None:
+        _check(self.lib.am_iterate(self.h, n), "am_iterate")
+
+    def compute(self) -> None:
+        _check(self.lib.am_compute(self.h), "am_compute")
+
+    def suspend(self, timeout: float | None = None) -> int:
+        if timeout is None:
+            return self.lib.am_suspend(self.h)
+        return self.lib.am_suspend_timeout(self.h, timeout)
+
+    def next_state(self) -> None:
+        self.lib.am_next_state(self.h)
+
+    def run_until(self, state: int, max_steps: int = 100000) -> int:
+        """Synchronous driver: synchronize, step, synchronize until the worker
+        reaches `state` (or max_steps)."""
+        _check(self.synchronize(), "am_synchronize")
+        steps = 0
+        while self.state < state and steps < max_steps:
+            self.iterate(1)
+            self.suspend()
+            _check(self.synchronize(), "am_synchronize")
+            steps += 1
+        return self.state
+
+    # -- readout -------------------------------------------------------------
+    @property
+    def state(self) -> int:
+        return self.lib.am_get_state(self.h)
+
+    @property
+    def energy(self) -> float:
+        return self.lib.am_get_energy(self.h)
+
+    def cost(self) -> int:
+        ex = C.c_uint64()
+        _check(self.lib.am_get_cost(self.h, C.byref(ex), None), "am_get_cost")
+        return ex.value
+
+    def blob_count(self, frame: int) -> int:
+        return self.lib.am_get_blob_count(self.h, frame)
+
+    def pixel_count(self, frame: int) -> int:
+        return self.lib.am_get_pixel_count(self.h, frame)
+
+    @property
+    def atoms(self) -> int:
+        return self.lib.am_get_atom_count(self.h)
+
+    @property
+    def chains(self) -> int:
+        return self.lib.am_get_chain_count(self.h)
+
+    @property
+    def width(self) -> int:
+        return self.lib.am_get_width(self.h)
+
+    @property
+    def height(self) -> int:
+        return self.lib.am_get_height(self.h)
+
+    def get_time(self, i: int, n: int) -> float:
+        return self.lib.am_get_time(self.h, i, n)
+
+    def render(self, t: float) -> np.ndarray:
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        _check(self.lib.am_render(self.h, t, out.ctypes.data, 0), "am_render")
+        return out
+
+    def render_device(self, t: float, dev_ptr: int) -> None:
+        _check(self.lib.am_render(self.h, t, dev_ptr, 1), "am_render")
+
+    def refine(self, sweeps: int, proposal: int | None = None) -> np.ndarray:
+        if proposal is not None:
+            self.set(proposal=proposal)
+        gains = np.zeros(max(sweeps, 1), np.uint64)
+        _check(self.lib.am_refine(self.h, sweeps, _p(gains, u64p)), "am_refine")
+        return gains[:sweeps]
+
+    def export_chains(self):
+        """(widths, pts[K*N], blob_order[K, C])."""
+        Cn = self.chains
+        N = self.atoms
+        K = self.lib.am_get_frame_count(self.h)
+        w = np.zeros(max(Cn, 1), np.uint64)
+        pts = np.zeros(max(K * N, 1), np.uint64)
+        order = np.zeros(max(K * Cn, 1), np.int32)
+        _check(self.lib.am_export_chains(self.h, _p(w, u64p), _p(pts, u64p), _p(order, i32p)), "am_export_chains")
+        return w[:Cn], pts[:K * N], order[:K * Cn].reshape(K, Cn)
+
+    def import_chains(self, widths, pts, order) -> None:
+        widths = np.ascontiguousarray(widths, np.uint64)
+        pts = np.ascontiguousarray(pts, np.uint64)
+        order = np.ascontiguousarray(order, np.int32)
+        K = order.shape[0]
+        _check(self.lib.am_import_chains(self.h, K, len(widths), _p(widths, u64p), _p(pts, u64p), _p(order, i32p)),
+               "am_import_chains")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.am_get_stream(self.h) or 0
+
+
+def launch_count() -> int:
+    return load().am_launch_count()

@@ -1,0 +1,293 @@
+// extern "C" entry points declared in include/atomorph_gb300.h.  Each one is
+// a thin wrapper over amg::Engine; the header names the reference member each
+// replaces.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+
+struct am_morph {
+    amg::Engine e;
+};
+
+namespace amg {
+const char *last_error();
+}
+
+using amg::Engine;
+
+#define H(m) (m)->e
+#define CHECK(m) \
+    if (!(m)) return AM_ERR_ARG
+
+extern "C" {
+
+const char *am_last_error(void) { return amg::last_error(); }
+const char *am_version(void) { return "atomorph_gb300 1.0 (reference API 1.0)"; }
+
+int am_create(am_morph **out) {
+    if (!out) return AM_ERR_ARG;
+    *out = new (std::nothrow) am_morph();
+    return *out ? AM_OK : AM_ERR_NOMEM;
+}
+void am_destroy(am_morph *m) { delete m; }
+int am_clear(am_morph *m) { CHECK(m); return H(m).clear(); }
+
+int am_add_pixel(am_morph *m, size_t frame, uint16_t x, uint16_t y, uint8_t r, uint8_t g, uint8_t b, uint8_t a) {
+    CHECK(m);
+    uint32_t c = r | (g << 8) | (b << 16) | ((uint32_t)a << 24);
+    return H(m).add_pixel(frame, x, y, c);
+}
+int am_add_pixels(am_morph *m, size_t frame, const uint8_t *rgba, uint32_t w, uint32_t h) {
+    CHECK(m);
+    return H(m).add_pixels(frame, rgba, w, h);
+}
+int am_add_frame(am_morph *m, size_t frame) { CHECK(m); return H(m).add_frame(frame); }
+
+// ---- parameters
+int am_set_seed(am_morph *m, unsigned s) { CHECK(m); H(m).set_seed(s); return AM_OK; }
+int am_set_blob_delimiter(am_morph *m, unsigned d) {
+    CHECK(m);
+    if (d != AM_RGB && d != AM_HSP) return AM_ERR_ARG;
+    H(m).front.delimiter = d;
+    return AM_OK;
+}
+int am_set_blob_threshold(am_morph *m, double t) { CHECK(m); H(m).front.threshold = t; return AM_OK; }
+int am_set_blob_max_size(am_morph *m, size_t s) { CHECK(m); H(m).front.max_size = s; return AM_OK; }
+int am_set_blob_min_size(am_morph *m, size_t s) { CHECK(m); H(m).front.min_size = s; return AM_OK; }
+int am_set_blob_box_grip(am_morph *m, uint16_t g) { CHECK(m); H(m).front.box_grip = g; return AM_OK; }
+int am_set_blob_box_samples(am_morph *m, size_t s) { CHECK(m); H(m).front.box_samples = s; return AM_OK; }
+int am_set_blob_number(am_morph *m, size_t n) { CHECK(m); H(m).front.blob_number = n; return AM_OK; }
+int am_set_blob_rgba_weight(am_morph *m, unsigned w) { CHECK(m); H(m).front.rgba_w = w & 255u; return AM_OK; }
+int am_set_blob_size_weight(am_morph *m, unsigned w) { CHECK(m); H(m).front.size_w = w & 255u; return AM_OK; }
+int am_set_blob_xy_weight(am_morph *m, unsigned w) { CHECK(m); H(m).front.xy_w = w & 255u; return AM_OK; }
+int am_set_degeneration(am_morph *m, size_t d) { CHECK(m); H(m).front.degeneration = d; return AM_OK; }
+int am_set_motion(am_morph *m, unsigned v) {
+    CHECK(m);
+    if (v != AM_NONE && v != AM_LINEAR && v != AM_SPLINE) return AM_ERR_ARG;
+    H(m).front.motion = v;
+    return AM_OK;
+}
+int am_set_fading(am_morph *m, unsigned v) {
+    CHECK(m);
+    if (v != AM_NONE && v != AM_LINEAR && v != AM_COSINE && v != AM_PERLIN) return AM_ERR_ARG;
+    H(m).front.fading = v;
+    return AM_OK;
+}
+int am_set_threads(am_morph *m, size_t t) { CHECK(m); H(m).front.threads = t; return AM_OK; }
+int am_set_cycle_length(am_morph *m, size_t c) { CHECK(m); H(m).front.cycle_length = c; return AM_OK; }
+int am_set_feather(am_morph *m, size_t f) {
+    CHECK(m);
+    if (f != 0) { amg::set_error("feather > 0 is not implemented on the GPU path"); return AM_ERR_UNSUPPORTED; }
+    H(m).front.feather = f;
+    return AM_OK;
+}
+int am_set_keep_background(am_morph *m, int k) {
+    CHECK(m);
+    if (k) { amg::set_error("keep_background is not implemented on the GPU path"); return AM_ERR_UNSUPPORTED; }
+    H(m).front.keep_background = false;
+    return AM_OK;
+}
+int am_set_finite(am_morph *m, int f) { CHECK(m); H(m).front.finite = f != 0; return AM_OK; }
+int am_set_show_blobs(am_morph *m, unsigned b) {
+    CHECK(m);
+    if (b != AM_TEXTURE) { amg::set_error("only TEXTURE blobs are implemented on the GPU path"); return AM_ERR_UNSUPPORTED; }
+    H(m).front.show_blobs = b;
+    return AM_OK;
+}
+// morph::set_fluid / set_density (morph.cpp:1553-1570): fluid forces density 1
+// and density > 1 turns the fluid off; density changes restart the morph.
+int am_set_fluid(am_morph *m, unsigned f) {
+    CHECK(m);
+    Engine &e = H(m);
+    if (e.front.fluidsteps != f) {
+        e.front.fluidsteps = f;
+        if (f > 0 && e.front.density > 1) { e.front.density = 1; e.identifier++; }
+    }
+    return AM_OK;
+}
+int am_set_density(am_morph *m, uint16_t d) {
+    CHECK(m);
+    Engine &e = H(m);
+    if (e.front.density != d) {
+        e.front.density = d;
+        e.identifier++;
+        if (e.front.fluidsteps != 0 && d > 1) e.front.fluidsteps = 0;
+    }
+    return AM_OK;
+}
+int am_set_resolution(am_morph *m, uint16_t w, uint16_t h) { CHECK(m); H(m).width = w; H(m).height = h; return AM_OK; }
+int am_set_proposal(am_morph *m, unsigned k) {
+    CHECK(m);
+    if (k > AM_PROPOSAL_LEARNED) return AM_ERR_ARG;
+    H(m).front.proposal = k;
+    H(m).active.proposal = k;
+    return AM_OK;
+}
+int am_set_sweeps(am_morph *m, size_t s) { CHECK(m); H(m).front.sweeps = s; H(m).active.sweeps = s; return AM_OK; }
+int am_set_motion_noise(am_morph *m, double a) {
+    CHECK(m);
+    if (!(a >= 0.0)) return AM_ERR_ARG;
+    H(m).front.motion_noise = a;
+    return AM_OK;
+}
+
+// ---- control
+int am_compute(am_morph *m) { CHECK(m); return H(m).compute(); }
+int am_iterate(am_morph *m, size_t n) { CHECK(m); return H(m).iterate(n); }
+int am_compute_seconds(am_morph *m, double s) { CHECK(m); return H(m).compute_seconds(s); }
+int am_suspend(am_morph *m) { CHECK(m); return H(m).suspend(-1.0); }
+int am_suspend_timeout(am_morph *m, double t) { CHECK(m); return H(m).suspend(t < 0 ? 0.0 : t); }
+int am_is_busy(const am_morph *m) { return m && m->e.is_busy() ? 1 : 0; }
+int am_synchronize(am_morph *m) { CHECK(m); return H(m).synchronize(); }
+int am_next_state(am_morph *m) { CHECK(m); H(m).skip_state = true; return AM_OK; }
+
+// ---- readout
+unsigned am_get_state(const am_morph *m) { return m ? m->e.f_state : 0u; }
+double am_get_energy(const am_morph *m) { return m ? m->e.f_energy : 0.0; }
+int am_get_cost(am_morph *m, uint64_t *exact, double *as_double) {
+    CHECK(m);
+    Engine &e = H(m);
+    if (e.is_busy()) return AM_ERR_BUSY;
+    uint64_t v = 0;
+    if (e.fN) {
+        int rc = e.compute_cost(&v);
+        if (rc) return rc;
+    }
+    if (exact) *exact = v;
+    if (as_double) *as_double = (double)v;
+    return AM_OK;
+}
+size_t am_get_frame_count(const am_morph *m) { return m ? m->e.frames.size() : 0; }
+static long frame_index(const Engine &e, size_t key) {
+    long i = 0;
+    for (auto &kv : e.frames) {
+        if (kv.first == key) return i;
+        ++i;
+    }
+    return -1;
+}
+size_t am_get_blob_count(const am_morph *m, size_t frame) {
+    if (!m) return 0;
+    long i = frame_index(m->e, frame);
+    if (i < 0 || (size_t)i >= m->e.f_blobs.size()) return 0;
+    return m->e.f_blobs[i].size();
+}
+size_t am_get_blob_count_total(const am_morph *m) {
+    if (!m) return 0;
+    size_t n = 0;
+    for (auto &b : m->e.f_blobs) n += b.size();
+    return n;
+}
+size_t am_get_pixel_count(const am_morph *m, size_t frame) {
+    if (!m) return 0;
+    auto it = m->e.frames.find(frame);
+    return it == m->e.frames.end() ? 0 : it->second.count;
+}
+// morph::get_frame_key (morph.cpp:404-423).
+size_t am_get_frame_key(const am_morph *m, double t) {
+    if (!m) return SIZE_MAX;
+    double integ;
+    t = std::modf(t, &integ);
+    if (t < 0.0) t += 1.0;
+    size_t f = (size_t)(t * m->e.frames.size());
+    size_t i = 0;
+    for (auto &kv : m->e.frames)
+        if (i++ == f) return kv.first;
+    return SIZE_MAX;
+}
+uint16_t am_get_width(const am_morph *m) { return m ? m->e.width : 0; }
+uint16_t am_get_height(const am_morph *m) { return m ? m->e.height : 0; }
+// morph::get_time (morph.cpp:1522-1538).
+double am_get_time(const am_morph *m, size_t i, size_t n) {
+    if (!m || n == 0) return 0.0;
+    size_t F = m->e.frames.size();
+    if (m->e.front.finite) {
+        if (n == 1) {
+            if (F == 0) return 0.0;
+            return (1.0 - (1.0 / double(F))) / 2.0;
+        }
+        double t = double(i) / double(n - 1);
+        t *= 1.0 - (1.0 / double(F));
+        return t;
+    }
+    return double(i) / double(n);
+}
+int am_get_average_pixel(const am_morph *m, size_t frame, uint16_t *xy, uint8_t *rgba) {
+    if (!m) return AM_ERR_ARG;
+    auto it = m->e.frames.find(frame);
+    if (it == m->e.frames.end()) return AM_ERR_NOT_FOUND;
+    if (xy) { xy[0] = (uint16_t)std::round(it->second.x); xy[1] = (uint16_t)std::round(it->second.y); }
+    if (rgba) {
+        long i = frame_index(m->e, frame);
+        double r = 0, g = 0, b = 0, a = 0, n = 0;
+        if (i >= 0 && (size_t)i < m->e.f_blobs.size())
+            for (auto &bl : m->e.f_blobs[i]) { r += bl.r * bl.size; g += bl.g * bl.size; b += bl.b * bl.size; a += bl.a * bl.size; n += bl.size; }
+        if (n > 0) { r /= n; g /= n; b /= n; a /= n; }
+        rgba[0] = (uint8_t)std::round(255.0 * r); rgba[1] = (uint8_t)std::round(255.0 * g);
+        rgba[2] = (uint8_t)std::round(255.0 * b); rgba[3] = (uint8_t)std::round(255.0 * a);
+    }
+    return AM_OK;
+}
+int am_get_blob_average(const am_morph *m, size_t frame, size_t blob, uint16_t *xy, uint8_t *rgba) {
+    if (!m) return AM_ERR_ARG;
+    long i = frame_index(m->e, frame);
+    if (i < 0 || (size_t)i >= m->e.f_blobs.size() || blob >= m->e.f_blobs[i].size()) return AM_ERR_NOT_FOUND;
+    const amg::Blob &b = m->e.f_blobs[i][blob];
+    if (xy) { xy[0] = (uint16_t)std::round(b.x); xy[1] = (uint16_t)std::round(b.y); }
+    if (rgba) {
+        rgba[0] = (uint8_t)std::round(255.0 * b.r); rgba[1] = (uint8_t)std::round(255.0 * b.g);
+        rgba[2] = (uint8_t)std::round(255.0 * b.b); rgba[3] = (uint8_t)std::round(255.0 * b.a);
+    }
+    return AM_OK;
+}
+size_t am_get_atom_count(const am_morph *m) { return m ? (size_t)m->e.fN : 0; }
+size_t am_get_chain_count(const am_morph *m) { return m ? (size_t)m->e.fC : 0; }
+
+int am_render(am_morph *m, double t, uint8_t *out, int on_dev) {
+    CHECK(m);
+    if (!out) return AM_ERR_ARG;
+    return H(m).render(t, out, on_dev != 0);
+}
+int am_render_many(am_morph *m, const double *ts, size_t n, uint8_t *out) {
+    CHECK(m);
+    if ((!ts || !out) && n) return AM_ERR_ARG;
+    size_t fsz = (size_t)H(m).width * H(m).height * 4;
+    for (size_t i = 0; i < n; ++i) {
+        int rc = H(m).render(ts[i], out + i * fsz, true);
+        if (rc) return rc;
+    }
+    return AM_OK;
+}
+
+int am_export_chains(am_morph *m, uint64_t *w, uint64_t *pts, int32_t *order) {
+    CHECK(m);
+    return H(m).export_chains(w, pts, order);
+}
+int am_import_chains(am_morph *m, size_t K, size_t C, const uint64_t *w, const uint64_t *pts, const int32_t *order) {
+    CHECK(m);
+    return H(m).import_chains(K, C, w, pts, order);
+}
+int am_refine(am_morph *m, size_t sweeps, uint64_t *gains) {
+    CHECK(m);
+    Engine &e = H(m);
+    if (e.is_busy()) return AM_ERR_BUSY;
+    if (e.state != AM_STATE_ATOM_MORPHING && e.state != AM_STATE_DONE) return AM_ERR_STATE;
+    e.active.proposal = e.front.proposal;
+    int rc = e.refine(sweeps, gains);
+    if (rc) return rc;
+    return e.publish_front();
+}
+
+// ---- runtime
+void *am_get_stream(am_morph *m) { return m ? (void *)m->e.rstream : nullptr; }
+uint64_t am_launch_count(void) { return amg::g_launches.load(); }
+int am_device_sync(am_morph *m) {
+    CHECK(m);
+    if (m->e.stream) { cudaError_t x = cudaStreamSynchronize(m->e.stream); if (x) return AM_ERR_CUDA; }
+    if (m->e.rstream) { cudaError_t x = cudaStreamSynchronize(m->e.rstream); if (x) return AM_ERR_CUDA; }
+    return AM_OK;
+}
+
+}  // extern "C"

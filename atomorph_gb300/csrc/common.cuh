@@ -1,0 +1,112 @@
+// Shared device/host helpers of the atomorph_gb300 CUDA library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+
+namespace amg {
+
+// ------------------------------------------------------------- errors -----
+void set_error(const std::string &msg);       // per-thread last error text
+extern std::atomic<uint64_t> g_launches;      // kernels launched by the library
+
+#define AMG_CUDA(call)                                                              \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            ::amg::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));   \
+            return AM_ERR_CUDA;                                                     \
+        }                                                                           \
+    } while (0)
+
+// Launch bookkeeping: every kernel launch goes through this so the process-wide
+// launch counter (am_launch_count) is exact.
+#define AMG_LAUNCH(kernel, grid, block, smem, stream, ...)                          \
+    do {                                                                            \
+        kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);                 \
+        ::amg::g_launches.fetch_add(1, std::memory_order_relaxed);                  \
+    } while (0)
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// ------------------------------------------------------------- points -----
+// The reference's 8-byte point word (atomorph.h:275-284), little-endian:
+// bits 0-15 x, 16-31 y, 32-39 x_fract, 40-47 y_fract, 48-55 flags.
+constexpr uint8_t kHasPixel = 1;
+constexpr uint8_t kHasFluid = 2;
+
+__host__ __device__ __forceinline__ int32_t pt_X(uint64_t w) {  // x in 1/256 px
+    return (int32_t)(((w & 0xFFFFu) << 8) | ((w >> 32) & 0xFFu));
+}
+__host__ __device__ __forceinline__ int32_t pt_Y(uint64_t w) {
+    return (int32_t)((((w >> 16) & 0xFFFFu) << 8) | ((w >> 40) & 0xFFu));
+}
+__host__ __device__ __forceinline__ uint32_t pt_x(uint64_t w) { return (uint32_t)(w & 0xFFFFu); }
+__host__ __device__ __forceinline__ uint32_t pt_y(uint64_t w) { return (uint32_t)((w >> 16) & 0xFFFFu); }
+__host__ __device__ __forceinline__ uint32_t pt_xf(uint64_t w) { return (uint32_t)((w >> 32) & 0xFFu); }
+__host__ __device__ __forceinline__ uint32_t pt_yf(uint64_t w) { return (uint32_t)((w >> 40) & 0xFFu); }
+__host__ __device__ __forceinline__ uint32_t pt_flags(uint64_t w) { return (uint32_t)((w >> 48) & 0xFFu); }
+__host__ __device__ __forceinline__ uint64_t pt_make(uint32_t x, uint32_t y, uint32_t xf, uint32_t yf,
+                                                     uint32_t flags) {
+    return (uint64_t)(x & 0xFFFFu) | ((uint64_t)(y & 0xFFFFu) << 16) | ((uint64_t)(xf & 0xFFu) << 32) |
+           ((uint64_t)(yf & 0xFFu) << 40) | ((uint64_t)(flags & 0xFFu) << 48);
+}
+// point_distance (atomorph.h:334-339): squared distance in 1/256 px, exact.
+__host__ __device__ __forceinline__ uint64_t pt_dist(uint64_t a, uint64_t b) {
+    int64_t dx = (int64_t)pt_X(a) - pt_X(b);
+    int64_t dy = (int64_t)pt_Y(a) - pt_Y(b);
+    return (uint64_t)(dx * dx + dy * dy);
+}
+
+// ------------------------------------------------------------ hashing -----
+// Counter-based randomness: every random choice is a pure function of
+// (seed, sweep, chain, frame, index), so a run is reproducible and a resumed
+// run continues the same stream.
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU;
+    x ^= x >> 15; x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27; x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31;
+    return x;
+}
+
+// Bijection of [0, n) (n <= 2^31) keyed by `key`: a 4-round balanced Feistel
+// network on the smallest even bit width covering n, with cycle walking.
+__device__ __forceinline__ uint32_t permute_index(uint32_t x, uint32_t n, uint32_t half_bits, uint64_t key) {
+    const uint32_t mask = (1u << half_bits) - 1u;
+    const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+    do {
+        uint32_t L = x >> half_bits, R = x & mask;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            uint32_t F = mix32(R ^ (r & 1 ? k1 : k0) ^ (0x9e3779b9u * (uint32_t)(r + 1))) & mask;
+            uint32_t nL = R;
+            R = L ^ F;
+            L = nL;
+        }
+        x = (L << half_bits) | R;
+    } while (x >= n);
+    return x;
+}
+__host__ __device__ __forceinline__ uint32_t half_bits_for(uint32_t n) {
+    uint32_t b = 1;
+    while ((1ull << b) < n) ++b;
+    return (b + 1) / 2;
+}
+
+// ------------------------------------------------------------ reductions --
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace amg

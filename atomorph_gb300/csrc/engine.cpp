@@ -1,0 +1,811 @@
+// Host engine and C ABI of atomorph_gb300.
+//
+// The handle mirrors the reference's split between the front-end am::morph
+// (key frames, settings, rendering from its own copy of the results) and the
+// worker am::thread (the pipeline state machine).  The worker runs on a host
+// std::thread like the reference's (thread.h:45-53, thread.cpp:173-206); every
+// step it takes enqueues CUDA kernels on the handle's stream and waits for
+// them, so a paused worker never has GPU work in flight.  synchronize()
+// publishes the worker's results to the front copy that rendering reads
+// (morph.cpp:102-269), so a frame can be rendered while the worker refines.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <string>
+
+namespace amg {
+
+std::atomic<uint64_t> g_launches{0};
+static thread_local std::string t_error;
+void set_error(const std::string &msg) { t_error = msg; }
+const char *last_error() { return t_error.c_str(); }
+
+// PerlinNoise(seed) permutation (perlin.cpp:11-17): 0..255 shuffled by
+// std::mt19937(seed), seed 0 replaced by the engine's default seed, repeated.
+static void perlin_perm(unsigned seed, int *p) {
+    if (seed == 0) seed = std::mt19937::default_seed;
+    std::iota(p, p + 256, 0);
+    std::shuffle(p, p + 256, std::mt19937(seed));
+    for (int i = 0; i < 256; ++i) p[256 + i] = p[i];
+}
+
+Engine::Engine() {
+    cudaGetDevice(&device);
+    // Default-constructed PerlinNoise maps use seed 1 (perlin.h:7, morph.h:136-137).
+    perlin_perm(1, perm_lag);
+    perlin_perm(1, perm_slope);
+}
+
+Engine::~Engine() {
+    if (running) {
+        signal_pause = true;
+        signal_stop = true;
+        if (th.joinable()) th.join();
+    }
+    if (rw) render_work_destroy(rw);
+    if (bw) blob_work_destroy(bw);
+    d_raw.release(); d_stored.release(); d_display.release(); d_present.release(); d_labels.release();
+    d_P.release(); d_Pf.release(); d_chain_off.release(); d_pair_off.release(); d_chain_off_f.release();
+    d_singles.release(); d_rank_f.release(); d_phase.release(); d_acc.release(); d_stats.release();
+    d_desc.release(); d_energy.release(); d_perm.release(); d_sorted.release(); d_keys.release();
+    d_tk.release(); d_tv.release(); d_hist.release(); d_bstart.release(); d_bsize.release(); d_volxy.release();
+    d_blob_of.release(); d_frame.release();
+    if (h_pinned) cudaFreeHost(h_pinned);
+    if (stream) cudaStreamDestroy(stream);
+    if (rstream) cudaStreamDestroy(rstream);
+}
+
+static int ensure_streams(Engine *e) {
+    if (e->stream) return AM_OK;
+    AMG_CUDA(cudaSetDevice(e->device));
+    AMG_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    AMG_CUDA(cudaStreamCreateWithFlags(&e->rstream, cudaStreamNonBlocking));
+    e->rw = render_work_create();
+    e->bw = blob_work_create();
+    int rc = render_set_perlin(e->rw, e->perm_lag, e->perm_slope);
+    return rc;
+}
+
+// ------------------------------------------------------------ ingestion --
+static void grow(HostFrame &f, uint32_t w, uint32_t h) {
+    if (w <= f.w && h <= f.h) return;
+    uint32_t nw = std::max(w, f.w), nh = std::max(h, f.h);
+    std::vector<uint32_t> raw((size_t)nw * nh, 0);
+    std::vector<uint8_t> pr((size_t)nw * nh, 0);
+    for (uint32_t y = 0; y < f.h; ++y) {
+        std::memcpy(&raw[(size_t)y * nw], &f.raw[(size_t)y * f.w], f.w * 4);
+        std::memcpy(&pr[(size_t)y * nw], &f.present[(size_t)y * f.w], f.w);
+    }
+    f.raw.swap(raw);
+    f.present.swap(pr);
+    f.w = nw;
+    f.h = nh;
+}
+
+int Engine::add_frame(size_t key) {
+    if (frames.count(key)) return AM_ERR_ARG;
+    HostFrame &f = frames[key];
+    f.x = bbox_x1 <= bbox_x2 ? (bbox_x1 + bbox_x2) / 2.0 : 0.0;
+    f.y = bbox_y1 <= bbox_y2 ? (bbox_y1 + bbox_y2) / 2.0 : 0.0;
+    identifier++;
+    return AM_OK;
+}
+
+int Engine::add_pixel(size_t key, uint16_t x, uint16_t y, uint32_t rgba) {
+    if (!frames.count(key)) add_frame(key);
+    HostFrame &f = frames[key];
+    grow(f, (uint32_t)x + 1, (uint32_t)y + 1);
+    size_t i = (size_t)y * f.w + x;
+    bool fresh = !f.present[i];
+    f.raw[i] = rgba;
+    f.present[i] = front.delimiter == AM_HSP ? 2 : 1;
+    if (fresh) f.count++;
+    identifier++;
+    bbox_x1 = std::min(bbox_x1, x); bbox_y1 = std::min(bbox_y1, y);
+    bbox_x2 = std::max(bbox_x2, x); bbox_y2 = std::max(bbox_y2, y);
+    if (f.count == 1 && fresh) { f.x = x; f.y = y; }
+    else {
+        double w = 1.0 / double(f.count);
+        f.x = (1.0 - w) * f.x + w * x;
+        f.y = (1.0 - w) * f.y + w * y;
+    }
+    return AM_OK;
+}
+
+int Engine::add_pixels(size_t key, const uint8_t *rgba, uint32_t w, uint32_t h) {
+    if (!rgba && (size_t)w * h) return AM_ERR_ARG;
+    if (w > 65536 || h > 65536) return AM_ERR_ARG;
+    if (!frames.count(key)) add_frame(key);
+    HostFrame &f = frames[key];
+    bool any = false;
+    const uint8_t mark = front.delimiter == AM_HSP ? 2 : 1;
+    for (uint32_t y = 0; y < h; ++y) {
+        for (uint32_t x = 0; x < w; ++x) {
+            const uint8_t *p = rgba + 4 * ((size_t)y * w + x);
+            if (p[3] == 0) continue;
+            if (!any) { grow(f, w, h); any = true; }
+            size_t i = (size_t)y * f.w + x;
+            bool fresh = !f.present[i];
+            uint32_t c;
+            std::memcpy(&c, p, 4);
+            f.raw[i] = c;
+            f.present[i] = mark;
+            if (fresh) f.count++;
+            bbox_x1 = std::min<uint16_t>(bbox_x1, (uint16_t)x); bbox_y1 = std::min<uint16_t>(bbox_y1, (uint16_t)y);
+            bbox_x2 = std::max<uint16_t>(bbox_x2, (uint16_t)x); bbox_y2 = std::max<uint16_t>(bbox_y2, (uint16_t)y);
+            if (f.count == 1 && fresh) { f.x = x; f.y = y; }
+            else {
+                double wt = 1.0 / double(f.count);
+                f.x = (1.0 - wt) * f.x + wt * x;
+                f.y = (1.0 - wt) * f.y + wt * y;
+            }
+        }
+    }
+    identifier++;
+    return AM_OK;
+}
+
+void Engine::set_seed(unsigned s) {
+    seed = s;
+    perlin_perm(s, perm_lag);
+    perlin_perm(s + 1, perm_slope);
+    if (rw) render_set_perlin(rw, perm_lag, perm_slope);
+}
+
+int Engine::clear() {
+    if (running) {
+        signal_pause = true;
+        signal_stop = true;
+        if (th.joinable()) th.join();
+        running = false;
+        paused = true;
+        signal_stop = false;
+        signal_pause = false;
+    }
+    frames.clear();
+    identifier = 0;
+    worker_identifier = SIZE_MAX;
+    bbox_x1 = bbox_y1 = UINT16_MAX;
+    bbox_x2 = bbox_y2 = 0;
+    state = AM_STATE_BLOB_DETECTION;
+    blobs.clear(); blob_real.clear(); perm.clear(); widths.clear();
+    Wb = C = 0; N = 0; match_started = false; cost_valid = false;
+    fK = fC = 0; fN = 0; f_widths.clear(); f_chain_off.clear(); f_rank.clear(); f_blobs.clear(); f_group.clear();
+    f_state = AM_STATE_BLOB_DETECTION;
+    f_energy = 0.0;
+    if (rw) render_invalidate(rw);
+    return AM_OK;
+}
+
+// -------------------------------------------------------------- worker ---
+void Engine::run() {
+    if (device >= 0) cudaSetDevice(device);
+    auto start = std::chrono::steady_clock::now();
+    while (!signal_stop) {
+        if (!signal_pause && !paused) {
+            step();
+            if (iterations > 0 && --iterations == 0) signal_pause = true;
+            if (seconds > 0.0) {
+                auto end = std::chrono::steady_clock::now();
+                if (std::chrono::duration<double>(end - start).count() > seconds) {
+                    signal_pause = true;
+                    seconds = 0.0;
+                }
+            }
+        } else {
+            paused = true;
+            signal_pause = false;
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+            start = std::chrono::steady_clock::now();
+        }
+    }
+    running = false;
+    signal_stop = false;
+    signal_pause = false;
+    paused = true;
+}
+
+void Engine::start_thread() {
+    if (th.joinable()) th.join();
+    running = true;
+    th = std::thread(&Engine::run, this);
+}
+
+int Engine::compute() {
+    if (is_busy()) return AM_ERR_BUSY;
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    if (!running) start_thread();
+    paused = false;
+    return AM_OK;
+}
+int Engine::iterate(size_t n) {
+    if (is_busy()) return AM_ERR_BUSY;
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    iterations = n;
+    if (!running) start_thread();
+    paused = false;
+    return AM_OK;
+}
+int Engine::compute_seconds(double s) {
+    if (is_busy()) return AM_ERR_BUSY;
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    seconds = s;
+    if (!running) start_thread();
+    paused = false;
+    return AM_OK;
+}
+int Engine::suspend(double timeout) {
+    auto t0 = std::chrono::steady_clock::now();
+    while (is_busy()) {
+        signal_pause = true;
+        if (paused) break;
+        if (timeout >= 0.0 &&
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > timeout)
+            return AM_ERR_TIMEOUT;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    return AM_OK;
+}
+
+void Engine::step() {
+    if (status != AM_OK) return;
+    int rc = AM_OK;
+    switch (state) {
+        case AM_STATE_BLOB_DETECTION:
+            rc = detect();
+            if (!rc) state = AM_STATE_BLOB_UNIFICATION;
+            break;
+        case AM_STATE_BLOB_UNIFICATION:
+            // In the component regime unify_frame leaves every blob as it is.
+            state = AM_STATE_BLOB_MATCHING;
+            break;
+        case AM_STATE_BLOB_MATCHING: {
+            bool done = false;
+            if (!match_started) {
+                rc = match_init();
+                if (!rc && worker_skip) done = true;
+            } else if (worker_skip || Wb <= 1) {
+                done = true;
+            } else {
+                rc = match_run(&done);
+            }
+            if (!rc && done) {
+                rc = build_chains();
+                if (!rc) state = (C == 0 || N == 0) ? AM_STATE_DONE : AM_STATE_ATOM_MORPHING;
+            }
+            break;
+        }
+        case AM_STATE_ATOM_MORPHING:
+            if (worker_skip) state = AM_STATE_DONE;
+            else rc = refine(active.sweeps, nullptr);
+            break;
+        default:
+            break;
+    }
+    worker_skip = false;
+    if (rc) status = rc;
+}
+
+// ------------------------------------------------------------- pipeline --
+int Engine::upload_frames() {
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    K = (uint32_t)frames.size();
+    CW = 1; CH = 1;
+    for (auto &kv : frames) { CW = std::max(CW, kv.second.w); CH = std::max(CH, kv.second.h); }
+    frame_keys.clear();
+    size_t fr = (size_t)CW * CH;
+    std::vector<uint32_t> raw(fr * std::max<uint32_t>(K, 1), 0);
+    std::vector<uint8_t> pr(fr * std::max<uint32_t>(K, 1), 0);
+    uint32_t k = 0;
+    for (auto &kv : frames) {
+        frame_keys.push_back(kv.first);
+        const HostFrame &f = kv.second;
+        for (uint32_t y = 0; y < f.h; ++y) {
+            std::memcpy(&raw[k * fr + (size_t)y * CW], &f.raw[(size_t)y * f.w], f.w * 4);
+            std::memcpy(&pr[k * fr + (size_t)y * CW], &f.present[(size_t)y * f.w], f.w);
+        }
+        ++k;
+    }
+    size_t n = fr * K;
+    if ((rc = d_raw.reserve(std::max<size_t>(n, 1)))) return rc;
+    if ((rc = d_present.reserve(std::max<size_t>(n, 1)))) return rc;
+    if ((rc = d_stored.reserve(std::max<size_t>(n, 1)))) return rc;
+    if ((rc = d_display.reserve(std::max<size_t>(n, 1)))) return rc;
+    if ((rc = d_labels.reserve(std::max<size_t>(n, 1)))) return rc;
+    if (n) {
+        AMG_CUDA(cudaMemcpyAsync(d_raw.p, raw.data(), n * 4, cudaMemcpyHostToDevice, stream));
+        AMG_CUDA(cudaMemcpyAsync(d_present.p, pr.data(), n, cudaMemcpyHostToDevice, stream));
+    }
+    rc = launch_colour(d_raw.p, d_present.p, d_stored.p, d_display.p, n, front.delimiter == AM_HSP, stream);
+    if (rc) return rc;
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    return AM_OK;
+}
+
+int Engine::detect() {
+    blobs.assign(K, {});
+    blob_real.assign(K, 0);
+    size_t fr = (size_t)CW * CH;
+    for (uint32_t k = 0; k < K; ++k) {
+        uint32_t nb = 0;
+        int rc = label_components(bw, d_present.p + k * fr, d_stored.p + k * fr, CW, CH, d_labels.p + k * fr, &nb,
+                                  stream);
+        if (rc) return rc;
+        if ((rc = d_stats.reserve(std::max<size_t>((size_t)nb * 7, 7)))) return rc;
+        rc = blob_stats(bw, d_labels.p + k * fr, d_stored.p + k * fr, CW, CH, nb, d_stats.p, stream);
+        if (rc) return rc;
+        std::vector<unsigned long long> st((size_t)nb * 7);
+        if (nb) AMG_CUDA(cudaMemcpyAsync(st.data(), d_stats.p, st.size() * 8, cudaMemcpyDeviceToHost, stream));
+        AMG_CUDA(cudaStreamSynchronize(stream));
+        std::vector<Blob> &bl = blobs[k];
+        bl.resize(nb);
+        for (uint32_t b = 0; b < nb; ++b) {
+            const unsigned long long *s = &st[(size_t)b * 7];
+            double c = (double)s[0];
+            bl[b].size = s[0];
+            bl[b].x = s[1] / c; bl[b].y = s[2] / c;
+            bl[b].r = s[3] / c / 255.0; bl[b].g = s[4] / c / 255.0;
+            bl[b].b = s[5] / c / 255.0; bl[b].a = s[6] / c / 255.0;
+        }
+        blob_real[k] = nb;
+    }
+    return AM_OK;
+}
+
+int Engine::match_init() {
+    match_started = true;
+    Wb = 0;
+    for (auto &b : blobs) Wb = std::max<uint32_t>(Wb, (uint32_t)b.size());
+    // Pad every frame with empty "volatile" blobs (thread.cpp:636-647) placed
+    // at the frame's mean, colour of the frame's mean.
+    uint32_t k = 0;
+    for (auto &kv : frames) {
+        const HostFrame &f = kv.second;
+        Blob v;
+        v.size = 0;
+        if (f.count) {
+            v.x = f.x; v.y = f.y;
+            double r = 0, g = 0, b = 0, a = 0, n = 0;
+            for (auto &bb : blobs[k]) { r += bb.r * bb.size; g += bb.g * bb.size; b += bb.b * bb.size; a += bb.a * bb.size; n += bb.size; }
+            if (n > 0) { v.r = r / n; v.g = g / n; v.b = b / n; v.a = a / n; }
+        } else {
+            v.x = bbox_x1 <= bbox_x2 ? (bbox_x1 + bbox_x2) / 2.0 : 0.0;
+            v.y = bbox_y1 <= bbox_y2 ? (bbox_y1 + bbox_y2) / 2.0 : 0.0;
+        }
+        while (blobs[k].size() < Wb) blobs[k].push_back(v);
+        ++k;
+    }
+    // Random initial groups, as the reference shuffles each frame's blobs
+    // (thread.cpp:649-657).
+    perm.assign((size_t)K * Wb, 0);
+    std::mt19937_64 rng(0x9e3779b97f4a7c15ULL ^ active_seed_mix());
+    for (uint32_t kk = 0; kk < K; ++kk) {
+        int32_t *row = &perm[(size_t)kk * Wb];
+        std::iota(row, row + Wb, 0);
+        std::shuffle(row, row + Wb, rng);
+    }
+    match_step = 0;
+    match_energy = -1.0;
+    if (Wb == 0) return AM_OK;
+    int rc;
+    if ((rc = d_desc.reserve((size_t)K * Wb * 7))) return rc;
+    if ((rc = d_perm.reserve((size_t)K * Wb))) return rc;
+    if ((rc = d_energy.reserve(1))) return rc;
+    std::vector<double> desc((size_t)K * Wb * 7);
+    for (uint32_t kk = 0; kk < K; ++kk)
+        for (uint32_t b = 0; b < Wb; ++b) {
+            const Blob &x = blobs[kk][b];
+            double *d = &desc[((size_t)kk * Wb + b) * 7];
+            d[0] = (double)x.size; d[1] = x.x; d[2] = x.y; d[3] = x.r; d[4] = x.g; d[5] = x.b; d[6] = x.a;
+        }
+    AMG_CUDA(cudaMemcpyAsync(d_desc.p, desc.data(), desc.size() * 8, cudaMemcpyHostToDevice, stream));
+    AMG_CUDA(cudaMemcpyAsync(d_perm.p, perm.data(), perm.size() * 4, cudaMemcpyHostToDevice, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    return AM_OK;
+}
+
+unsigned Engine::active_seed_mix() const { return seed; }
+
+int Engine::match_run(bool *done) {
+    *done = false;
+    MatchArgs a;
+    a.desc = d_desc.p;
+    a.perm = d_perm.p;
+    a.Wb = Wb;
+    a.K = K;
+    int dx = (int)bbox_x2 - (int)bbox_x1, dy = (int)bbox_y2 - (int)bbox_y1;
+    a.bbox_d = bbox_x1 <= bbox_x2 ? (double)(dx * dx + dy * dy) : 0.0;
+    if (a.bbox_d <= 0.0) a.bbox_d = 1.0;
+    double sum = (double)(active.rgba_w * active.rgba_w + active.size_w * active.size_w + active.xy_w * active.xy_w);
+    if (sum > 0) {
+        a.w_rgba = (active.rgba_w * active.rgba_w) / sum;
+        a.w_size = (active.size_w * active.size_w) / sum;
+        a.w_xy = 1.0 - (a.w_rgba + a.w_size);
+    } else {
+        a.w_rgba = 0.33; a.w_size = 0.33; a.w_xy = 0.34;
+    }
+    a.sweeps = 64;
+    a.key = mix64(((uint64_t)seed << 32) ^ (match_step + 1));
+    a.degenerate = active.degeneration;
+    a.energy_out = d_energy.p;
+    int rc = launch_blob_match(a, stream);
+    if (rc) return rc;
+    double e = 0;
+    AMG_CUDA(cudaMemcpyAsync(&e, d_energy.p, 8, cudaMemcpyDeviceToHost, stream));
+    AMG_CUDA(cudaMemcpyAsync(perm.data(), d_perm.p, perm.size() * 4, cudaMemcpyDeviceToHost, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    ++match_step;
+    // Converged when a whole step of sweeps no longer lowers the energy
+    // (the reference stops at zero energy or when told to, thread.cpp:735).
+    if (match_energy >= 0.0 && e >= match_energy) *done = true;
+    if (e == 0.0 || match_step >= 256) *done = true;
+    match_energy = e;
+    return AM_OK;
+}
+
+static std::vector<std::vector<uint32_t>> phases_for(uint32_t K) {
+    std::vector<std::vector<uint32_t>> ph;
+    if (K == 0) return ph;
+    if (K == 1) return {{0}};
+    if (K == 2) return {{0}, {1}};
+    std::vector<uint32_t> ev, od, last;
+    for (uint32_t y = 0; y < K; ++y) {
+        if (K % 2 == 1 && y == K - 1) last.push_back(y);
+        else if (y % 2 == 0) ev.push_back(y);
+        else od.push_back(y);
+    }
+    ph.push_back(ev);
+    ph.push_back(od);
+    if (!last.empty()) ph.push_back(last);
+    return ph;
+}
+
+int Engine::set_chain_layout(const std::vector<uint64_t> &w) {
+    widths = w;
+    C = (uint32_t)w.size();
+    chain_off.assign(C + 1, 0);
+    pair_off.assign(C + 1, 0);
+    singles.clear();
+    for (uint32_t c = 0; c < C; ++c) {
+        chain_off[c + 1] = chain_off[c] + w[c];
+        pair_off[c + 1] = pair_off[c] + w[c] / 2;
+        if (w[c] == 1) singles.push_back(chain_off[c]);
+    }
+    N = chain_off[C];
+    int rc;
+    if ((rc = d_P.reserve(std::max<uint64_t>(N * K, 1)))) return rc;
+    if ((rc = d_chain_off.reserve(C + 1))) return rc;
+    if ((rc = d_pair_off.reserve(C + 1))) return rc;
+    if ((rc = d_singles.reserve(std::max<size_t>(singles.size(), 1)))) return rc;
+    if ((rc = d_phase.reserve(std::max<uint32_t>(K, 1)))) return rc;
+    AMG_CUDA(cudaMemcpyAsync(d_chain_off.p, chain_off.data(), (C + 1) * 8, cudaMemcpyHostToDevice, stream));
+    AMG_CUDA(cudaMemcpyAsync(d_pair_off.p, pair_off.data(), (C + 1) * 8, cudaMemcpyHostToDevice, stream));
+    if (!singles.empty())
+        AMG_CUDA(cudaMemcpyAsync(d_singles.p, singles.data(), singles.size() * 8, cudaMemcpyHostToDevice, stream));
+    std::vector<uint32_t> ph;
+    for (auto &p : phases_for(K)) ph.insert(ph.end(), p.begin(), p.end());
+    if (!ph.empty()) AMG_CUDA(cudaMemcpyAsync(d_phase.p, ph.data(), ph.size() * 4, cudaMemcpyHostToDevice, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    return AM_OK;
+}
+
+int Engine::build_chains() {
+    if (!match_started) {
+        int rc = match_init();
+        if (rc) return rc;
+    }
+    C = 0;
+    N = 0;
+    if (Wb == 0 || K == 0) return AM_OK;
+    // Empty blobs take positions interpolated between the group's non-empty
+    // neighbours (fix_volatiles, thread.cpp:1187-1233).
+    std::vector<uint32_t> volxy((size_t)K * Wb, 0);
+    std::vector<int32_t> blob_of((size_t)K * Wb, -1);
+    std::vector<uint64_t> w(Wb, 0);
+    for (uint32_t g = 0; g < Wb; ++g) {
+        std::vector<Blob *> col(K);
+        for (uint32_t k = 0; k < K; ++k) col[k] = &blobs[k][perm[(size_t)k * Wb + g]];
+        if (K > 1) {
+            uint32_t i = 0;
+            bool started = false;
+            std::vector<Blob *> vol;
+            Blob *first = nullptr, *prev = nullptr;
+            while (true) {
+                i = (i + 1) % K;
+                Blob *bl = col[i];
+                bool empty = bl->size == 0;
+                if (!started) {
+                    if (empty) { if (i == 0) break; continue; }
+                    started = true; first = prev = bl; continue;
+                }
+                if (empty) { vol.push_back(bl); continue; }
+                for (size_t v = 0; v < vol.size(); ++v) {
+                    double t = (v + 1.0) / double(vol.size() + 1.0);
+                    vol[v]->x = t * bl->x + (1.0 - t) * prev->x;
+                    vol[v]->y = t * bl->y + (1.0 - t) * prev->y;
+                }
+                vol.clear();
+                prev = bl;
+                if (prev == first) break;
+            }
+        }
+        uint64_t mx = 0;
+        for (uint32_t k = 0; k < K; ++k) {
+            int32_t b = perm[(size_t)k * Wb + g];
+            const Blob &bl = blobs[k][b];
+            mx = std::max<uint64_t>(mx, bl.size);
+            if ((size_t)b < blob_real[k] && bl.size > 0) blob_of[(size_t)k * Wb + g] = b;
+            uint32_t vx = (uint32_t)(uint16_t)std::round(bl.x), vy = (uint32_t)(uint16_t)std::round(bl.y);
+            volxy[(size_t)k * Wb + g] = vx | (vy << 16);
+        }
+        w[g] = mx * active.density;
+    }
+    int rc = set_chain_layout(w);
+    if (rc) return rc;
+    // Sort each frame's pixels by (blob, row-major position).
+    size_t fr = (size_t)CW * CH;
+    uint32_t maxb = 1;
+    for (uint32_t k = 0; k < K; ++k) maxb = std::max<uint32_t>(maxb, (uint32_t)blob_real[k]);
+    if ((rc = d_sorted.reserve(fr * K))) return rc;
+    if ((rc = d_keys.reserve(fr))) return rc;
+    if ((rc = d_tk.reserve(fr))) return rc;
+    if ((rc = d_tv.reserve(fr))) return rc;
+    if ((rc = d_hist.reserve(radix_hist_words(fr)))) return rc;
+    if ((rc = d_bstart.reserve((size_t)K * maxb))) return rc;
+    if ((rc = d_bsize.reserve((size_t)K * maxb))) return rc;
+    if ((rc = d_volxy.reserve((size_t)K * Wb))) return rc;
+    if ((rc = d_blob_of.reserve((size_t)K * Wb))) return rc;
+    std::vector<uint32_t> bstart((size_t)K * maxb, 0), bsize((size_t)K * maxb, 0);
+    std::vector<uint32_t> iota_px(fr);
+    std::iota(iota_px.begin(), iota_px.end(), 0u);
+    for (uint32_t k = 0; k < K; ++k) {
+        uint32_t nb = (uint32_t)blob_real[k];
+        uint32_t acc = 0;
+        for (uint32_t b = 0; b < nb; ++b) {
+            bstart[(size_t)k * maxb + b] = acc;
+            bsize[(size_t)k * maxb + b] = (uint32_t)blobs[k][b].size;
+            acc += (uint32_t)blobs[k][b].size;
+        }
+        // keys = labels with absent pixels mapped past the last blob.
+        int bits = 1;
+        while ((1ull << bits) < (uint64_t)nb + 1) ++bits;
+        rc = labels_to_keys(d_labels.p + k * fr, d_keys.p, fr, nb, stream);
+        if (rc) return rc;
+        AMG_CUDA(cudaMemcpyAsync(d_sorted.p + k * fr, iota_px.data(), fr * 4, cudaMemcpyHostToDevice, stream));
+        rc = radix_sort_pairs(d_keys.p, d_sorted.p + k * fr, d_tk.p, d_tv.p, d_hist.p, fr, bits, stream);
+        if (rc) return rc;
+    }
+    AMG_CUDA(cudaMemcpyAsync(d_bstart.p, bstart.data(), bstart.size() * 4, cudaMemcpyHostToDevice, stream));
+    AMG_CUDA(cudaMemcpyAsync(d_bsize.p, bsize.data(), bsize.size() * 4, cudaMemcpyHostToDevice, stream));
+    AMG_CUDA(cudaMemcpyAsync(d_volxy.p, volxy.data(), volxy.size() * 4, cudaMemcpyHostToDevice, stream));
+    AMG_CUDA(cudaMemcpyAsync(d_blob_of.p, blob_of.data(), blob_of.size() * 4, cudaMemcpyHostToDevice, stream));
+    ChainBuildArgs cb;
+    cb.P = d_P.p; cb.N = N; cb.K = K; cb.C = C; cb.chain_off = d_chain_off.p; cb.blob_of = d_blob_of.p;
+    cb.blob_start = d_bstart.p; cb.blob_size = d_bsize.p; cb.maxb = maxb; cb.sorted = d_sorted.p;
+    cb.npx = (uint32_t)fr; cb.CW = CW; cb.vol_xy = d_volxy.p;
+    cb.seed = mix64(((uint64_t)seed << 16) ^ 0xC4A1);
+    rc = launch_chain_build(cb, stream);
+    if (rc) return rc;
+    uint64_t ex = 0;
+    rc = compute_cost(&ex);
+    if (rc) return rc;
+    cost_exact = ex;
+    cost_valid = true;
+    return AM_OK;
+}
+
+int Engine::compute_cost(uint64_t *exact) {
+    int rc;
+    if ((rc = d_acc.reserve(8))) return rc;
+    if (N == 0 || K == 0) { *exact = 0; return AM_OK; }
+    rc = launch_cost(d_P.p, N, K, d_singles.p, (uint32_t)singles.size(), d_acc.p + 2, stream);
+    if (rc) return rc;
+    unsigned long long v = 0;
+    AMG_CUDA(cudaMemcpyAsync(&v, d_acc.p + 2, 8, cudaMemcpyDeviceToHost, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    *exact = v;
+    return AM_OK;
+}
+
+int Engine::refine(size_t sweeps, uint64_t *gains) {
+    if (N == 0 || K == 0 || sweeps == 0) return AM_OK;
+    if (active.proposal != AM_PROPOSAL_RANDOM) {
+        int rc = refine_guided(sweeps, gains);
+        return rc;
+    }
+    int rc;
+    if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * sweeps + 4)))) return rc;
+    AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * sweeps * 8, stream));
+    auto ph = phases_for(K);
+    for (size_t s = 0; s < sweeps; ++s) {
+        uint32_t pofs = 0;
+        for (size_t p = 0; p < ph.size(); ++p) {
+            SweepArgs a;
+            a.P = d_P.p; a.N = N; a.K = K; a.C = C; a.chain_off = d_chain_off.p; a.pair_off = d_pair_off.p;
+            a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
+            a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p);
+            a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
+            if (pair_off[C] > 0) {
+                rc = launch_sweep_random(a, stream);
+                if (rc) return rc;
+            }
+            pofs += (uint32_t)ph[p].size();
+        }
+        ++sweep_counter;
+    }
+    std::vector<unsigned long long> acc(2 * sweeps);
+    AMG_CUDA(cudaMemcpyAsync(acc.data(), d_acc.p + 4, acc.size() * 8, cudaMemcpyDeviceToHost, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    for (size_t s = 0; s < sweeps; ++s) {
+        cost_exact -= acc[2 * s];
+        if (gains) gains[s] = acc[2 * s];
+    }
+    return AM_OK;
+}
+
+int Engine::publish_front() {
+    fK = K; fC = C; fN = N;
+    f_widths = widths; f_chain_off = chain_off; f_keys = frame_keys;
+    f_blobs = blobs;
+    f_group.assign(K, {});
+    f_rank.assign((size_t)K * C, 0);
+    for (uint32_t k = 0; k < K && k < blobs.size(); ++k) {
+        f_group[k].assign(blobs[k].size(), 0);
+        for (uint32_t g = 0; g < Wb && (size_t)k * Wb + g < perm.size(); ++g) {
+            int32_t b = perm[(size_t)k * Wb + g];
+            if ((size_t)b < f_group[k].size()) f_group[k][b] = (int32_t)g;
+            if (g < C) f_rank[(size_t)k * C + g] = b;
+        }
+    }
+    f_state = state;
+    if (state == AM_STATE_BLOB_MATCHING) f_energy = match_energy;
+    else if (state == AM_STATE_ATOM_MORPHING || state == AM_STATE_DONE) f_energy = cost_valid ? (double)cost_exact : 0.0;
+    else f_energy = -1.0;
+    if (N && K) {
+        int rc;
+        if ((rc = d_Pf.reserve(N * K))) return rc;
+        if ((rc = d_chain_off_f.reserve(C + 1))) return rc;
+        if ((rc = d_rank_f.reserve((size_t)K * C))) return rc;
+        AMG_CUDA(cudaMemcpyAsync(d_Pf.p, d_P.p, N * K * 8, cudaMemcpyDeviceToDevice, stream));
+        AMG_CUDA(cudaMemcpyAsync(d_chain_off_f.p, chain_off.data(), (C + 1) * 8, cudaMemcpyHostToDevice, stream));
+        AMG_CUDA(cudaMemcpyAsync(d_rank_f.p, f_rank.data(), f_rank.size() * 4, cudaMemcpyHostToDevice, stream));
+        AMG_CUDA(cudaStreamSynchronize(stream));
+    }
+    if (rw) render_invalidate(rw);
+    return AM_OK;
+}
+
+int Engine::synchronize() {
+    if (is_busy()) return AM_ERR_BUSY;
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    if (status) {
+        int s = status;
+        status = AM_OK;
+        return s;
+    }
+    active = front;
+    if (identifier != worker_identifier) {
+        state = AM_STATE_BLOB_DETECTION;
+        blobs.clear(); blob_real.clear(); perm.clear(); widths.clear();
+        Wb = C = 0; N = 0; match_started = false; cost_valid = false; sweep_counter = 0;
+        rc = upload_frames();
+        if (rc) return rc;
+        worker_identifier = identifier;
+    }
+    rc = publish_front();
+    if (rc) return rc;
+    if (skip_state) {
+        worker_skip = true;
+        skip_state = false;
+    }
+    return AM_OK;
+}
+
+int Engine::render(double time, uint8_t *out, bool out_dev) {
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    size_t bytes = (size_t)width * height * 4;
+    if (bytes == 0) return AM_OK;
+    uint8_t *dst = out;
+    if (!out_dev) {
+        if ((rc = d_frame.reserve(bytes))) return rc;
+        dst = d_frame.p;
+    }
+    double integ;
+    double t = std::modf(time, &integ);
+    if (t < 0.0) t += 1.0;
+    if (fN == 0 || fK == 0) {
+        // No chains yet: the key frame's blob pixels as they are
+        // (morph.cpp:469-475), or nothing before blobs exist.
+        AMG_CUDA(cudaMemsetAsync(dst, 0, bytes, rstream));
+        size_t f = (size_t)(t * fK);
+        bool have_blobs = f < f_blobs.size() && !f_blobs[f].empty();
+        if (fK && f < fK && have_blobs) {
+            rc = copy_keyframe(f, dst);
+            if (rc) return rc;
+        }
+    } else {
+        RenderScene sc;
+        sc.K = fK; sc.C = fC; sc.N = fN; sc.CW = CW; sc.CH = CH; sc.width = width; sc.height = height;
+        sc.bbox[0] = bbox_x1; sc.bbox[1] = bbox_y1; sc.bbox[2] = bbox_x2; sc.bbox[3] = bbox_y2;
+        sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
+        sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
+        size_t f = (size_t)(t * fK);
+        uint64_t key = f < f_keys.size() ? f_keys[f] : 0;
+        rc = render_frame(rw, sc, t, key, dst, rstream);
+        if (rc) return rc;
+    }
+    if (!out_dev) AMG_CUDA(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, rstream));
+    AMG_CUDA(cudaStreamSynchronize(rstream));
+    return AM_OK;
+}
+
+int Engine::import_chains(size_t k_, size_t c_, const uint64_t *w, const uint64_t *pts, const int32_t *order) {
+    if (is_busy()) return AM_ERR_BUSY;
+    if (k_ != frames.size() || !w || (!pts && c_)) return AM_ERR_ARG;
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    active = front;
+    if (identifier != worker_identifier) {
+        rc = upload_frames();
+        if (rc) return rc;
+        worker_identifier = identifier;
+    }
+    K = (uint32_t)k_;
+    Wb = (uint32_t)c_;
+    perm.assign((size_t)K * Wb, 0);
+    blobs.assign(K, std::vector<Blob>(Wb));
+    blob_real.assign(K, Wb);
+    for (uint32_t k = 0; k < K; ++k)
+        for (uint32_t b = 0; b < Wb; ++b) {
+            int32_t g = order ? order[(size_t)k * Wb + b] : (int32_t)b;
+            if (g < 0 || (uint32_t)g >= Wb) return AM_ERR_ARG;
+            perm[(size_t)k * Wb + g] = (int32_t)b;
+        }
+    match_started = true;
+    rc = set_chain_layout(std::vector<uint64_t>(w, w + c_));
+    if (rc) return rc;
+    if (N * K) AMG_CUDA(cudaMemcpyAsync(d_P.p, pts, N * K * 8, cudaMemcpyHostToDevice, stream));
+    uint64_t ex = 0;
+    rc = compute_cost(&ex);
+    if (rc) return rc;
+    cost_exact = ex;
+    cost_valid = true;
+    state = AM_STATE_ATOM_MORPHING;
+    return publish_front();
+}
+
+int Engine::export_chains(uint64_t *w, uint64_t *pts, int32_t *order) {
+    if (w) for (uint32_t c = 0; c < fC; ++c) w[c] = f_widths[c];
+    if (pts && fN * fK) {
+        AMG_CUDA(cudaMemcpyAsync(pts, d_Pf.p, fN * fK * 8, cudaMemcpyDeviceToHost, rstream));
+        AMG_CUDA(cudaStreamSynchronize(rstream));
+    }
+    if (order)
+        for (uint32_t k = 0; k < fK; ++k)
+            for (uint32_t g = 0; g < fC; ++g) order[(size_t)k * fC + f_rank[(size_t)k * fC + g]] = (int32_t)g;
+    return AM_OK;
+}
+
+int Engine::copy_keyframe(size_t f, uint8_t *dst) {
+    size_t fr = (size_t)CW * CH;
+    return launch_keyframe_copy(d_display.p + f * fr, d_present.p + f * fr, CW, CH, width, height, dst, rstream);
+}
+
+int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
+    (void)sweeps;
+    (void)gains;
+    set_error("proposal kind not available in this build");
+    return AM_ERR_UNSUPPORTED;
+}
+
+}  // namespace amg

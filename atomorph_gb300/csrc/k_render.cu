@@ -1,0 +1,663 @@
+// Frame render (the atom path of morph::get_pixels(t), morph.cpp:452-678 and
+// 1302-1421) as tile-binned CUDA kernels.
+//
+// Per key-frame pair (prepared once, reused by every output frame of the
+// transition):
+//   k_pair_prep    per atom: endpoints in 1/256 px, both colours with the
+//                  alpha-0 substitution for a missing side (morph.cpp:500-522),
+//                  Perlin lag/slope (morph.cpp:537-545, FP32), composite rank
+//                  of its chain; keyed by the tile of the path midpoint.
+//   radix sort + k_pair_gather   records reordered by that tile, so a warp's
+//                  atoms land in few output tiles at any time of the pair.
+// Per output frame:
+//   k_frame_splat  exact position (LINEAR: the reference's double formula
+//                  morph.cpp:1501-1515; SPLINE: the cyclic Catmull-Rom
+//                  morph.cpp:526-531, spline.cpp:29-57, both evaluated with
+//                  round-to-nearest FP64 operations and no fused multiply-add),
+//                  colour fade, the four bilinear corners with the reference's
+//                  bbox/size rules (morph.cpp:552-588), per-tile histogram.
+//   scan           tile offsets.
+//   k_frame_scatter  16-byte records into their tiles (a corner in a
+//                  neighbouring tile duplicates the record there).
+//   k_frame_resolve  one CTA per 32x32 tile: for each chain present, in the
+//                  key frame's blob order, exact integer weighted means of the
+//                  corners (weights (255-xf)(255-yf) etc. are integers, so the
+//                  reference's per-pixel mean morph.cpp:593-623 is computed as
+//                  an exactly rounded rational), then the ordered "over"
+//                  composite morph.cpp:1348-1402 in FP64; 16-byte RGBA8 stores.
+#include "common.cuh"
+#include "kernels.h"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace amg {
+
+constexpr int kTile = 32;
+constexpr uint32_t kInactive = 0xFFFFFFFFu;
+
+struct RenderWork {
+    int pair_f = -1;
+    uint64_t cap = 0;       // atom capacity of the buffers below
+    uint64_t active = 0;    // active atoms of the prepared pair (sorted first)
+    uint32_t motion = 0, fading = 0;
+    int4 *pa = nullptr, *pb = nullptr;   // endpoints / spline control points
+    uint2 *col = nullptr;
+    float2 *ls = nullptr;
+    uint32_t *rank = nullptr, *idx = nullptr;
+    int4 *pa2 = nullptr, *pb2 = nullptr;
+    uint2 *col2 = nullptr;
+    float2 *ls2 = nullptr;
+    uint32_t *rank2 = nullptr, *idx2 = nullptr;
+    uint32_t *keys = nullptr, *vals = nullptr, *tkeys = nullptr, *tvals = nullptr, *hist = nullptr;
+    uint32_t *d_active = nullptr;
+    uint4 *spl = nullptr;
+    uint4 *rec = nullptr;
+    uint64_t rec_cap = 0;
+    uint32_t *tile_cnt = nullptr, *tile_off = nullptr, *tile_cur = nullptr;
+    uint32_t ntiles_cap = 0;
+    int *perm = nullptr;    // [2][512] Perlin permutations on the device
+    bool perm_set = false;
+};
+
+RenderWork *render_work_create() { return new RenderWork(); }
+
+static void rw_free(RenderWork *w) {
+    void *ps[] = {w->pa, w->pb, w->col, w->ls, w->rank, w->idx, w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2,
+                  w->keys, w->vals, w->tkeys, w->tvals, w->hist, w->spl, w->d_active};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    w->pa = w->pb = w->pa2 = w->pb2 = nullptr;
+    w->col = w->col2 = nullptr;
+    w->ls = w->ls2 = nullptr;
+    w->rank = w->idx = w->rank2 = w->idx2 = w->keys = w->vals = w->tkeys = w->tvals = w->hist = w->d_active = nullptr;
+    w->spl = nullptr;
+    w->cap = 0;
+}
+
+void render_work_destroy(RenderWork *w) {
+    if (!w) return;
+    rw_free(w);
+    if (w->rec) cudaFree(w->rec);
+    if (w->tile_cnt) cudaFree(w->tile_cnt);
+    if (w->tile_off) cudaFree(w->tile_off);
+    if (w->tile_cur) cudaFree(w->tile_cur);
+    if (w->perm) cudaFree(w->perm);
+    delete w;
+}
+
+void render_invalidate(RenderWork *w) { w->pair_f = -1; }
+
+int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope) {
+    if (!w->perm) AMG_CUDA(cudaMalloc(&w->perm, 1024 * sizeof(int)));
+    std::vector<int> h(1024);
+    std::memcpy(h.data(), perm_lag, 512 * sizeof(int));
+    std::memcpy(h.data() + 512, perm_slope, 512 * sizeof(int));
+    AMG_CUDA(cudaMemcpy(w->perm, h.data(), 1024 * sizeof(int), cudaMemcpyHostToDevice));
+    w->perm_set = true;
+    w->pair_f = -1;
+    return AM_OK;
+}
+
+static int rw_reserve(RenderWork *w, uint64_t n) {
+    if (n <= w->cap) return AM_OK;
+    rw_free(w);
+    uint64_t c = n + n / 8 + 1024;
+    AMG_CUDA(cudaMalloc(&w->pa, c * sizeof(int4)));
+    AMG_CUDA(cudaMalloc(&w->pb, c * sizeof(int4)));
+    AMG_CUDA(cudaMalloc(&w->col, c * sizeof(uint2)));
+    AMG_CUDA(cudaMalloc(&w->ls, c * sizeof(float2)));
+    AMG_CUDA(cudaMalloc(&w->rank, c * 4));
+    AMG_CUDA(cudaMalloc(&w->idx, c * 4));
+    AMG_CUDA(cudaMalloc(&w->pa2, c * sizeof(int4)));
+    AMG_CUDA(cudaMalloc(&w->pb2, c * sizeof(int4)));
+    AMG_CUDA(cudaMalloc(&w->col2, c * sizeof(uint2)));
+    AMG_CUDA(cudaMalloc(&w->ls2, c * sizeof(float2)));
+    AMG_CUDA(cudaMalloc(&w->rank2, c * 4));
+    AMG_CUDA(cudaMalloc(&w->idx2, c * 4));
+    AMG_CUDA(cudaMalloc(&w->keys, c * 4));
+    AMG_CUDA(cudaMalloc(&w->vals, c * 4));
+    AMG_CUDA(cudaMalloc(&w->tkeys, c * 4));
+    AMG_CUDA(cudaMalloc(&w->tvals, c * 4));
+    AMG_CUDA(cudaMalloc(&w->hist, radix_hist_words(c) * 4));
+    AMG_CUDA(cudaMalloc(&w->spl, c * sizeof(uint4)));
+    AMG_CUDA(cudaMalloc(&w->d_active, 4));
+    w->cap = c;
+    return AM_OK;
+}
+
+namespace {
+
+__device__ __forceinline__ uint32_t find_chain_r(const uint64_t *__restrict__ off, uint32_t C, uint64_t r) {
+    uint32_t lo = 0, hi = C;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= r) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// ----------------------------------------------------------- Perlin FP32 --
+// Improved Perlin noise at z = 0 (perlin.cpp:19-43; the z terms vanish since
+// fade(0) = 0), 8 octaves (perlin.cpp:57-69), on a permutation in smem.
+__device__ __forceinline__ float pgrad(int hash, float x, float y) {
+    int h = hash & 15;
+    float u = h < 8 ? x : y, v = h < 4 ? y : (h == 12 || h == 14 ? x : 0.f);
+    return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
+}
+__device__ __forceinline__ float pfade(float t) { return t * t * t * (t * (t * 6.f - 15.f) + 10.f); }
+__device__ float pnoise(const int *p, float x, float y) {
+    float fx = floorf(x), fy = floorf(y);
+    int X = (int)fx & 255, Y = (int)fy & 255;
+    x -= fx; y -= fy;
+    float u = pfade(x), v = pfade(y);
+    int A = p[X] + Y, AA = p[A], AB = p[A + 1];
+    int B = p[X + 1] + Y, BA = p[B], BB = p[B + 1];
+    float l1 = pgrad(p[AA], x, y) + u * (pgrad(p[BA], x - 1.f, y) - pgrad(p[AA], x, y));
+    float l2 = pgrad(p[AB], x, y - 1.f) + u * (pgrad(p[BB], x - 1.f, y - 1.f) - pgrad(p[AB], x, y - 1.f));
+    return l1 + v * (l2 - l1);
+}
+__device__ float poctave(const int *p, float x, float y) {
+    float r = 0.f, amp = 1.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        r += pnoise(p, x, y) * amp;
+        x *= 2.f; y *= 2.f; amp *= 0.5f;
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, const int *__restrict__ perm,
+                                                    int4 *pa, int4 *pb, uint2 *col, float2 *ls, uint32_t *rank,
+                                                    uint32_t *keys, uint32_t *vals, uint32_t tiles_x,
+                                                    uint32_t inactive_key) {
+    __shared__ int sp[1024];
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x) sp[i] = perm ? perm[i] : 0;
+    __syncthreads();
+    const uint32_t y = f, yn = (f + 1) % sc.K;
+    const float bw = (float)(sc.bbox[2] - sc.bbox[0] + 1), bh = (float)(sc.bbox[3] - sc.bbox[1] + 1);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < sc.N; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t w1 = sc.P[(uint64_t)y * sc.N + i], w2 = sc.P[(uint64_t)yn * sc.N + i];
+        bool h1 = pt_flags(w1) & kHasPixel, h2 = pt_flags(w2) & kHasPixel;
+        vals[i] = (uint32_t)i;
+        if (!h1 && !h2) {
+            rank[i] = kInactive;
+            keys[i] = inactive_key;
+            continue;
+        }
+        uint32_t c = find_chain_r(sc.chain_off, sc.C, i);
+        uint32_t c1 = 0, c2 = 0;
+        const size_t fr = (size_t)sc.CH * sc.CW;
+        if (h1) c1 = sc.display[(size_t)y * fr + (size_t)pt_y(w1) * sc.CW + pt_x(w1)];
+        if (h2) c2 = sc.display[(size_t)yn * fr + (size_t)pt_y(w2) * sc.CW + pt_x(w2)];
+        if (h1 && !h2) c2 = c1 & 0x00FFFFFFu;
+        if (h2 && !h1) c1 = c2 & 0x00FFFFFFu;
+        int32_t X1 = pt_X(w1), Y1 = pt_Y(w1), X2 = pt_X(w2), Y2 = pt_Y(w2);
+        if (sc.motion == AM_SPLINE) {
+            uint32_t K = sc.K;
+            uint32_t s0 = (f + K - 1) % K, s2 = (f + 1) % K, s3 = (f + 2) % K;
+            uint64_t q0 = sc.P[(uint64_t)s0 * sc.N + i], q2 = sc.P[(uint64_t)s2 * sc.N + i],
+                     q3 = sc.P[(uint64_t)s3 * sc.N + i];
+            pa[i] = make_int4(pt_X(q0), pt_Y(q0), X1, Y1);
+            pb[i] = make_int4(pt_X(q2), pt_Y(q2), pt_X(q3), pt_Y(q3));
+        } else {
+            pa[i] = make_int4(X1, Y1, X2, Y2);
+        }
+        col[i] = make_uint2(c1, c2);
+        float lag = 0.5f, slope = 0.5f;
+        if (sc.fading == AM_PERLIN) {
+            // morph.cpp:540-545: pt1 normalised by the bbox, frequency 8.
+            float px = ((float)((int)pt_x(w1) - (int)sc.bbox[0]) * 256.f + (float)pt_xf(w1)) / (bw * 256.f) * 8.f;
+            float py = ((float)((int)pt_y(w1) - (int)sc.bbox[1]) * 256.f + (float)pt_yf(w1)) / (bh * 256.f) * 8.f;
+            lag = poctave(sp, px, py) * 0.5f + 0.5f;
+            slope = poctave(sp + 512, px, py) * 0.5f + 0.5f;
+        }
+        ls[i] = make_float2(lag, slope);
+        rank[i] = (uint32_t)sc.rank[(size_t)f * sc.C + c];
+        int mx = ((X1 + X2) >> 9), my = ((Y1 + Y2) >> 9);
+        mx = min(max(mx, 0), (int)sc.width - 1);
+        my = min(max(my, 0), (int)sc.height - 1);
+        keys[i] = (uint32_t)((my / kTile) * tiles_x + (mx / kTile));
+    }
+}
+
+__global__ void k_pair_gather(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ order, uint64_t n,
+                              const int4 *pa, const int4 *pb, const uint2 *col, const float2 *ls,
+                              const uint32_t *rank, int4 *pa2, int4 *pb2, uint2 *col2, float2 *ls2,
+                              uint32_t *rank2, uint32_t *idx2, int spline, uint32_t *active) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t i = order[j];
+        uint32_t r = rank[i];
+        rank2[j] = r;
+        idx2[j] = i;
+        if (r == kInactive) {
+            if (j == 0 || rank[order[j - 1]] != kInactive) *active = (uint32_t)j;
+            continue;
+        }
+        pa2[j] = pa[i];
+        if (spline) pb2[j] = pb[i];
+        col2[j] = col[i];
+        ls2[j] = ls[i];
+        if (j + 1 == n) *active = (uint32_t)n;
+    }
+}
+
+struct FrameArgs {
+    double w1, w2;          // LINEAR: weight of pt1 and 1 - that weight
+    double b[4];            // SPLINE basis at the frame's local time
+    uint32_t seg_ok;        // 1 when the spline segment is the prepared one
+    int32_t seg[4];         // control frames when seg_ok == 0
+    float str;              // colour weight of the earlier key frame, 1 - t
+    uint32_t tiles_x, ntiles;
+};
+
+// Exact double formula of morph::interpolate(point) (morph.cpp:1504-1512)
+// with round-to-nearest operations: floor(w1*X1 + w2*X2) in 1/256 px.
+__device__ __forceinline__ int32_t lin_fixed(double w1, double w2, int32_t a, int32_t b) {
+    double v = __dadd_rn(__dmul_rn(w1, (double)a), __dmul_rn(w2, (double)b));
+    return (int32_t)v;  // v >= 0: truncation is floor
+}
+// Catmull-Rom value at the prepared basis, then the reference's modf /
+// round(fract * 255) split (morph.cpp:528-530).  Returns the 1/256 grid
+// position as (integer part << 8) | fract byte with the integer part taken
+// modulo 2^16 like the x86 build's double -> uint16 conversion.
+__device__ __forceinline__ uint32_t spl_fixed(const double *b, int32_t q0, int32_t q1, int32_t q2, int32_t q3) {
+    double v0 = (double)(q0 >> 8) + (double)(q0 & 255) / 256.0;
+    double v1 = (double)(q1 >> 8) + (double)(q1 & 255) / 256.0;
+    double v2 = (double)(q2 >> 8) + (double)(q2 & 255) / 256.0;
+    double v3 = (double)(q3 >> 8) + (double)(q3 & 255) / 256.0;
+    double v = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, b[0]), __dmul_rn(v1, b[1])), __dmul_rn(v2, b[2])),
+                         __dmul_rn(v3, b[3]));
+    double ip = trunc(v);
+    double fr = __dsub_rn(v, ip);
+    uint32_t xi = (uint32_t)(int)ip & 0xFFFFu;
+    uint32_t xf = (uint32_t)(int)round(__dmul_rn(fr, 255.0)) & 0xFFu;
+    return (xi << 8) | xf;
+}
+
+// Colour fade of one atom (morph.cpp:537-550, 1467-1488) in FP32.
+__device__ __forceinline__ uint32_t fade_colour(uint32_t fading, uint32_t c1, uint32_t c2, float lag, float slope,
+                                                float str) {
+    if (fading == AM_PERLIN || fading == AM_COSINE) {
+        const float pi = 3.14159265358f;
+        float s = (slope + 0.1f) / 1.1f;
+        float l = (1.f - s) * lag;
+        if (str <= l) str = 0.f;
+        else if (str >= l + s) str = 1.f;
+        else str = (-cosf((str - l) * (pi / s)) + 1.f) * 0.5f;
+    }
+    uint32_t o = 0;
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+        float a = (float)((c1 >> (8 * ch)) & 255u), b = (float)((c2 >> (8 * ch)) & 255u);
+        float v = str * a + (1.f - str) * b;
+        o |= ((uint32_t)(int)roundf(v) & 255u) << (8 * ch);
+    }
+    return o;
+}
+
+// Up to four distinct tiles touched by the valid corners of base pixel
+// (px, py); returns the count.
+__device__ __forceinline__ int corner_tiles(uint32_t px, uint32_t py, uint32_t valid, uint32_t tiles_x,
+                                            uint32_t *t) {
+    int n = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!(valid & (1u << k))) continue;
+        uint32_t cx = px + (k & 1), cy = py + (k >> 1);
+        uint32_t tt = (cy / kTile) * tiles_x + cx / kTile;
+        bool dup = false;
+        for (int j = 0; j < n; ++j) dup |= t[j] == tt;
+        if (!dup) t[n++] = tt;
+    }
+    return n;
+}
+
+__global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs fa, uint64_t n,
+                                                      const int4 *__restrict__ pa, const int4 *__restrict__ pb,
+                                                      const uint2 *__restrict__ col, const float2 *__restrict__ ls,
+                                                      const uint32_t *__restrict__ rank,
+                                                      const uint32_t *__restrict__ idx, uint4 *spl,
+                                                      uint32_t *tile_cnt) {
+    extern __shared__ uint32_t hist[];
+    const bool smem_hist = fa.ntiles <= 8192;
+    if (smem_hist) {
+        for (uint32_t i = threadIdx.x; i < fa.ntiles; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+    }
+    const uint32_t bx1 = sc.bbox[0], by1 = sc.bbox[1], bx2 = sc.bbox[2], by2 = sc.bbox[3];
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t r = rank[i];
+        uint32_t X, Y;
+        int4 a = pa[i];
+        if (sc.motion == AM_LINEAR) {
+            X = (uint32_t)lin_fixed(fa.w1, fa.w2, a.x, a.z);
+            Y = (uint32_t)lin_fixed(fa.w1, fa.w2, a.y, a.w);
+        } else if (sc.motion == AM_SPLINE) {
+            int4 b;
+            if (fa.seg_ok) {
+                b = pb[i];
+            } else {
+                uint64_t o = idx[i];
+                uint64_t q0 = sc.P[(uint64_t)fa.seg[0] * sc.N + o], q1 = sc.P[(uint64_t)fa.seg[1] * sc.N + o];
+                uint64_t q2 = sc.P[(uint64_t)fa.seg[2] * sc.N + o], q3 = sc.P[(uint64_t)fa.seg[3] * sc.N + o];
+                a = make_int4(pt_X(q0), pt_Y(q0), pt_X(q1), pt_Y(q1));
+                b = make_int4(pt_X(q2), pt_Y(q2), pt_X(q3), pt_Y(q3));
+            }
+            X = spl_fixed(fa.b, a.x, a.z, b.x, b.z);
+            Y = spl_fixed(fa.b, a.y, a.w, b.y, b.w);
+        } else {
+            X = (uint32_t)a.x;
+            Y = (uint32_t)a.y;
+        }
+        uint32_t px = X >> 8, py = Y >> 8, xf = X & 255u, yf = Y & 255u;
+        uint2 c = col[i];
+        float2 q = ls[i];
+        uint32_t colour = fade_colour(sc.fading, c.x, c.y, q.x, q.y, fa.str);
+        uint32_t valid = 0;
+        bool skip = (px >= sc.width || py >= sc.height) && (px > bx2 || px < bx1 || py > by2 || py < by1);
+        if (!skip) {
+            if (xf < 255u && yf < 255u) valid |= 1u;
+            if ((px < bx2 || px + 1 < sc.width) && xf > 0u && yf < 255u) valid |= 2u;
+            if ((py < by2 || py + 1 < sc.height) && xf < 255u && yf > 0u) valid |= 4u;
+            if (xf > 0u && yf > 0u && ((py < by2 && px < bx2) || (py + 1 < sc.height && px + 1 < sc.width)))
+                valid |= 8u;
+            // Corners outside the output are dropped (they only arise when the
+            // resolution is smaller than the key frames' bounding box).
+            if (px >= sc.width || py >= sc.height) valid &= ~1u;
+            if (px + 1 >= sc.width || py >= sc.height) valid &= ~2u;
+            if (px >= sc.width || py + 1 >= sc.height) valid &= ~4u;
+            if (px + 1 >= sc.width || py + 1 >= sc.height) valid &= ~8u;
+        }
+        spl[i] = make_uint4(px | (py << 16), xf | (yf << 8) | (valid << 16), colour, r);
+        if (valid) {
+            uint32_t t[4];
+            int nt = corner_tiles(px, py, valid, fa.tiles_x, t);
+            for (int k = 0; k < nt; ++k) {
+                if (smem_hist) atomicAdd(&hist[t[k]], 1u);
+                else atomicAdd(&tile_cnt[t[k]], 1u);
+            }
+        }
+    }
+    if (smem_hist) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < fa.ntiles; i += blockDim.x)
+            if (hist[i]) atomicAdd(&tile_cnt[i], hist[i]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_frame_scatter(const uint4 *__restrict__ spl, uint64_t n,
+                                                        uint32_t tiles_x, uint32_t *tile_cur, uint4 *rec) {
+    const int lane = threadIdx.x & 31;
+    for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = base + threadIdx.x;
+        uint4 s = i < n ? spl[i] : make_uint4(0, 0, 0, 0);
+        uint32_t valid = i < n ? (s.y >> 16) & 15u : 0u;
+        uint32_t t[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+        int nt = valid ? corner_tiles(s.x & 0xFFFFu, s.x >> 16, valid, tiles_x, t) : 0;
+        // Warp-aggregated slot reservation per distinct tile.
+        for (int k = 0; k < 4; ++k) {
+            uint32_t tt = k < nt ? t[k] : 0xFFFFFFFFu;
+            unsigned act = __ballot_sync(0xffffffffu, k < nt);
+            if (!act) break;
+            unsigned peers = __match_any_sync(0xffffffffu, tt);
+            if (k < nt) {
+                int leader = __ffs(peers) - 1;
+                uint32_t slot = 0;
+                if (lane == leader) slot = atomicAdd(&tile_cur[tt], (uint32_t)__popc(peers));
+                slot = __shfl_sync(peers, slot, leader);
+                slot += __popc(peers & ((1u << lane) - 1u));
+                rec[slot] = s;
+            }
+        }
+    }
+}
+
+// Exactly rounded (half away from zero) quotient num/den, both >= 0, den > 0.
+__device__ __forceinline__ uint32_t round_div(unsigned long long num, unsigned long long den) {
+    return (uint32_t)((2ull * num + den) / (2ull * den));
+}
+
+__global__ void __launch_bounds__(256) k_frame_resolve(const uint4 *__restrict__ rec,
+                                                        const uint32_t *__restrict__ tile_off, uint32_t tiles_x,
+                                                        uint32_t width, uint32_t height, uint32_t density,
+                                                        uint8_t *out) {
+    __shared__ unsigned long long sW[kTile * kTile], sC[4][kTile * kTile];
+    __shared__ uint32_t sN[kTile * kTile];
+    __shared__ uint32_t red[8];
+    const uint32_t tile = blockIdx.x;
+    const uint32_t tx0 = (tile % tiles_x) * kTile, ty0 = (tile / tiles_x) * kTile;
+    const uint32_t beg = tile_off[tile], end = tile_off[tile + 1];
+    for (int i = threadIdx.x; i < kTile * kTile; i += 256) {
+        sW[i] = 0; sC[0][i] = 0; sC[1][i] = 0; sC[2][i] = 0; sC[3][i] = 0; sN[i] = 0;
+    }
+    const uint32_t lr = threadIdx.x >> 3, lc0 = (threadIdx.x & 7) * 4;
+    int n[4] = {0, 0, 0, 0};
+    uint32_t c0[4] = {0, 0, 0, 0};
+    double R[4], G[4], B[4], A[4];
+    // First chain rank present.
+    uint32_t mn = 0xFFFFFFFFu;
+    for (uint32_t j = beg + threadIdx.x; j < end; j += 256) mn = min(mn, rec[j].w);
+    for (int o = 16; o; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
+    __syncthreads();
+    uint32_t cur = red[0];
+    for (int k = 1; k < 8; ++k) cur = min(cur, red[k]);
+    while (cur != 0xFFFFFFFFu) {
+        __syncthreads();
+        uint32_t nxt = 0xFFFFFFFFu;
+        for (uint32_t j = beg + threadIdx.x; j < end; j += 256) {
+            uint4 s = rec[j];
+            if (s.w != cur) {
+                if (s.w > cur) nxt = min(nxt, s.w);
+                continue;
+            }
+            uint32_t px = s.x & 0xFFFFu, py = s.x >> 16;
+            uint32_t xf = s.y & 255u, yf = (s.y >> 8) & 255u, valid = (s.y >> 16) & 15u;
+            uint32_t wx[2] = {255u - xf, xf}, wy[2] = {255u - yf, yf};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!(valid & (1u << k))) continue;
+                uint32_t cx = px + (k & 1) - tx0, cy = py + (k >> 1) - ty0;
+                if (cx >= (uint32_t)kTile || cy >= (uint32_t)kTile) continue;
+                uint32_t li = cy * kTile + cx;
+                unsigned long long W = (unsigned long long)(wx[k & 1] * wy[k >> 1]);
+                atomicAdd(&sW[li], W);
+                atomicAdd(&sC[0][li], W * (s.z & 255u));
+                atomicAdd(&sC[1][li], W * ((s.z >> 8) & 255u));
+                atomicAdd(&sC[2][li], W * ((s.z >> 16) & 255u));
+                atomicAdd(&sC[3][li], W * (s.z >> 24));
+                atomicAdd(&sN[li], 1u);
+            }
+        }
+        for (int o = 16; o; o >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, o));
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nxt;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint32_t li = lr * kTile + lc0 + q;
+            uint32_t cnt = sN[li];
+            if (!cnt) continue;
+            unsigned long long W = sW[li];
+            uint32_t r = round_div(sC[0][li], W), g = round_div(sC[1][li], W), b = round_div(sC[2][li], W);
+            uint32_t a;
+            if (cnt >= density) a = round_div(sC[3][li], W);
+            else a = round_div((unsigned long long)cnt * sC[3][li], (unsigned long long)density * W);
+            sW[li] = 0; sC[0][li] = 0; sC[1][li] = 0; sC[2][li] = 0; sC[3][li] = 0; sN[li] = 0;
+            if (a == 0) continue;  // draw_atoms skips transparent blob pixels
+            uint32_t cc = r | (g << 8) | (b << 16) | (a << 24);
+            if (n[q] == 0) {
+                c0[q] = cc;
+            } else {
+                if (n[q] == 1) {
+                    R[q] = (c0[q] & 255u) / 255.0; G[q] = ((c0[q] >> 8) & 255u) / 255.0;
+                    B[q] = ((c0[q] >> 16) & 255u) / 255.0; A[q] = (c0[q] >> 24) / 255.0;
+                }
+                double sr = r / 255.0, sg = g / 255.0, sb = b / 255.0, sa = a / 255.0;
+                double om = __dsub_rn(1.0, sa);
+                R[q] = __dadd_rn(__dmul_rn(sa, sr), __dmul_rn(om, R[q]));
+                G[q] = __dadd_rn(__dmul_rn(sa, sg), __dmul_rn(om, G[q]));
+                B[q] = __dadd_rn(__dmul_rn(sa, sb), __dmul_rn(om, B[q]));
+                A[q] = __dadd_rn(A[q], __dmul_rn(__dsub_rn(1.0, A[q]), a / 255.0));
+            }
+            n[q]++;
+        }
+        __syncthreads();
+        cur = red[0];
+        for (int k = 1; k < 8; ++k) cur = min(cur, red[k]);
+    }
+    uint32_t gy = ty0 + lr, gx = tx0 + lc0;
+    if (gy >= height || gx >= width) return;
+    uint32_t o[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (n[q] == 0) o[q] = 0;
+        else if (n[q] == 1) o[q] = c0[q];
+        else {
+            auto cb = [](double v) { return (uint32_t)(int)round(__dmul_rn(v, 255.0)) & 255u; };
+            o[q] = cb(R[q]) | (cb(G[q]) << 8) | (cb(B[q]) << 16) | (cb(A[q]) << 24);
+        }
+    }
+    uint8_t *dst = out + ((size_t)gy * width + gx) * 4;
+    if (gx + 4 <= width && (((uintptr_t)dst & 15u) == 0)) {
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(o[0], o[1], o[2], o[3]);
+    } else {
+        for (int q = 0; q < 4 && gx + q < width; ++q) reinterpret_cast<uint32_t *>(dst)[q] = o[q];
+    }
+}
+
+__global__ void k_keyframe_copy(const uint32_t *__restrict__ display, const uint8_t *__restrict__ present,
+                                uint32_t CW, uint32_t CH, uint32_t width, uint32_t height, uint32_t *out) {
+    size_t n = (size_t)width * height;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        uint32_t x = (uint32_t)(i % width), y = (uint32_t)(i / width);
+        uint32_t c = 0;
+        if (x < CW && y < CH) {
+            size_t j = (size_t)y * CW + x;
+            if (present[j] && (display[j] >> 24)) c = display[j];
+        }
+        out[i] = c;
+    }
+}
+
+}  // namespace
+
+int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32_t CW, uint32_t CH, uint32_t width,
+                         uint32_t height, uint8_t *out, cudaStream_t s) {
+    size_t n = (size_t)width * height;
+    if (!n) return AM_OK;
+    unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)kSMs * 16);
+    AMG_LAUNCH(k_keyframe_copy, grid, 256, 0, s, display, present, CW, CH, width, height, (uint32_t *)out);
+    AMG_CUDA(cudaGetLastError());
+    return AM_OK;
+}
+
+static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStream_t s) {
+    int rc = rw_reserve(w, sc.N);
+    if (rc) return rc;
+    uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
+    unsigned grid = (unsigned)std::min<uint64_t>((sc.N + 255) / 256, (uint64_t)kSMs * 8);
+    AMG_LAUNCH(k_pair_prep, grid, 256, 0, s, sc, f, w->perm_set ? w->perm : nullptr, w->pa, w->pb, w->col, w->ls,
+               w->rank, w->keys, w->vals, tiles_x, tiles_x * tiles_y);
+    // Inactive atoms carry key ntiles so a sort on the tile bits orders them last.
+    int bits = 1;
+    while ((1ull << bits) < (uint64_t)tiles_x * tiles_y + 1) ++bits;
+    rc = radix_sort_pairs(w->keys, w->vals, w->tkeys, w->tvals, w->hist, sc.N, bits, s);
+    if (rc) return rc;
+    AMG_CUDA(cudaMemsetAsync(w->d_active, 0, 4, s));
+    AMG_LAUNCH(k_pair_gather, grid, 256, 0, s, w->keys, w->vals, sc.N, w->pa, w->pb, w->col, w->ls, w->rank,
+               w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2, (int)(sc.motion == AM_SPLINE), w->d_active);
+    uint32_t act = 0;
+    AMG_CUDA(cudaMemcpyAsync(&act, w->d_active, 4, cudaMemcpyDeviceToHost, s));
+    AMG_CUDA(cudaStreamSynchronize(s));
+    w->active = act;
+    w->pair_f = (int)f;
+    w->motion = sc.motion;
+    w->fading = sc.fading;
+    return AM_OK;
+}
+
+int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, uint8_t *out,
+                 cudaStream_t s) {
+    const size_t bytes = (size_t)sc.width * sc.height * 4;
+    if (sc.K == 0 || sc.C == 0 || sc.N == 0) {
+        AMG_CUDA(cudaMemsetAsync(out, 0, bytes, s));
+        return AM_OK;
+    }
+    size_t f = (size_t)(time * sc.K);
+    if (f >= sc.K) {
+        AMG_CUDA(cudaMemsetAsync(out, 0, bytes, s));
+        return AM_OK;
+    }
+    double dt = 1.0 / double(sc.K);
+    double t = std::max(0.0, (time - (double)(frame_key * dt)) / dt);
+    if (w->pair_f != (int)f || w->motion != sc.motion || w->fading != sc.fading) {
+        int rc = prep_pair(w, sc, (uint32_t)f, s);
+        if (rc) return rc;
+    }
+    uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
+    uint32_t ntiles = tiles_x * tiles_y;
+    if (ntiles + 1 > w->ntiles_cap) {
+        if (w->tile_cnt) cudaFree(w->tile_cnt);
+        if (w->tile_off) cudaFree(w->tile_off);
+        if (w->tile_cur) cudaFree(w->tile_cur);
+        AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
+        AMG_CUDA(cudaMalloc(&w->tile_off, (ntiles + 1) * 4));
+        AMG_CUDA(cudaMalloc(&w->tile_cur, (ntiles + 1) * 4));
+        w->ntiles_cap = ntiles + 1;
+    }
+    uint64_t need = w->active * 4 + 16;
+    if (need > w->rec_cap) {
+        if (w->rec) cudaFree(w->rec);
+        w->rec_cap = need + need / 4;
+        AMG_CUDA(cudaMalloc(&w->rec, w->rec_cap * sizeof(uint4)));
+    }
+    FrameArgs fa;
+    std::memset(&fa, 0, sizeof(fa));
+    fa.w1 = 1.0 - t;
+    fa.w2 = 1.0 - fa.w1;
+    fa.str = (float)(1.0 - t);
+    fa.tiles_x = tiles_x;
+    fa.ntiles = ntiles;
+    fa.seg_ok = 1;
+    if (sc.motion == AM_SPLINE) {
+        // GetInterpolatedSplinePoint(time) (spline.cpp:45-57) basis.
+        int n = (int)sc.K;
+        double delta_t = 1.0 / n;
+        int p = (int)(time / delta_t);
+        auto wrap = [n](int i) { return i < 0 ? n - 1 : (i >= n ? i - n : i); };
+        double lt = (time - delta_t * (double)p) / delta_t;
+        double t2 = lt * lt, t3 = t2 * lt;
+        fa.b[0] = 0.5 * (-t3 + 2.0 * t2 - lt);
+        fa.b[1] = 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
+        fa.b[2] = 0.5 * (-3.0 * t3 + 4.0 * t2 + lt);
+        fa.b[3] = 0.5 * (t3 - t2);
+        fa.seg[0] = wrap(p - 1); fa.seg[1] = wrap(p); fa.seg[2] = wrap(p + 1); fa.seg[3] = wrap(p + 2);
+        fa.seg_ok = (p == (int)f) ? 1u : 0u;
+    }
+    AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
+    uint64_t n = w->active;
+    if (n) {
+        unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 4);
+        size_t smem = ntiles <= 8192 ? ntiles * 4 : 0;
+        AMG_LAUNCH(k_frame_splat, grid, 256, smem, s, sc, fa, n, w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2,
+                   w->spl, w->tile_cnt);
+    }
+    AMG_CUDA(cudaMemcpyAsync(w->tile_off, w->tile_cnt, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
+    {
+        int rc = launch_scan_u32(w->tile_off, (size_t)ntiles + 1, nullptr, s);
+        if (rc) return rc;
+    }
+    AMG_CUDA(cudaMemcpyAsync(w->tile_cur, w->tile_off, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
+    if (n) {
+        unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 4);
+        AMG_LAUNCH(k_frame_scatter, grid, 256, 0, s, w->spl, n, tiles_x, w->tile_cur, w->rec);
+    }
+    AMG_LAUNCH(k_frame_resolve, ntiles, 256, 0, s, w->rec, w->tile_off, tiles_x, sc.width, sc.height,
+               sc.density ? sc.density : 1u, out);
+    AMG_CUDA(cudaGetLastError());
+    return AM_OK;
+}
+
+}  // namespace amg

@@ -1,0 +1,130 @@
+// Host-callable launch wrappers of the atomorph_gb300 kernels.  Every wrapper
+// enqueues on the given stream and returns an AM_* status.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "../../include/atomorph_gb300.h"
+
+namespace amg {
+
+// ---- k_colour.cu
+int launch_colour(const uint32_t *raw, const uint8_t *present, uint32_t *stored, uint32_t *display, size_t n,
+                  int display_hsp, cudaStream_t s);
+int launch_hsp_probe(const uint32_t *in, uint32_t *out, size_t n, int dir, cudaStream_t s);
+
+// ---- k_chains.cu
+// Exact atom cost: out += sum over atoms i, frames j of
+// d(P[j][i], P[(j+1)%K][i]) (thread.cpp:1109-1125), atoms of width-1 chains
+// excluded via the `single` list.
+int launch_cost(const uint64_t *P, uint64_t N, uint32_t K, const uint64_t *single, uint32_t nsingle,
+                unsigned long long *out, cudaStream_t s);
+
+struct SweepArgs {
+    uint64_t *P;                 // [K][N] chain points
+    uint64_t N;
+    uint32_t K;
+    uint32_t C;                  // chains
+    const uint64_t *chain_off;   // [C+1] atom offsets of the chains
+    const uint64_t *pair_off;    // [C+1] prefix sums of floor(width/2)
+    const uint32_t *frames;      // frames updated by this phase
+    uint32_t nframes;
+    uint64_t key;                // random key of this (sweep, phase)
+    unsigned long long *gain;    // += exact cost decrease
+    unsigned long long *accepted;
+};
+// One phase of the plain refinement: for every chain and every frame of the
+// phase, a uniformly random perfect matching of the chain's columns; each pair
+// is swapped when the reference's criterion c1 >= c2 holds
+// (thread.cpp:1014-1039).
+int launch_sweep_random(const SweepArgs &a, cudaStream_t s);
+
+// Stable LSD radix sort of (key, value) u32 pairs on the low `bits` key bits.
+// tmp buffers must hold n elements each; hist needs radix_hist_words(n).
+size_t radix_hist_words(size_t n);
+int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals, uint32_t *hist,
+                     size_t n, int bits, cudaStream_t s);
+// keys[i] = labels[i] >= 0 ? labels[i] : nb (absent pixels sort last).
+int labels_to_keys(const int32_t *labels, uint32_t *keys, size_t n, uint32_t nb, cudaStream_t s);
+// Exclusive scan of n u32 in place (single CTA; setup-sized arrays).
+int launch_scan_u32(uint32_t *a, size_t n, uint32_t *total, cudaStream_t s);
+
+struct ChainBuildArgs {
+    uint64_t *P;                  // [K][N] output
+    uint64_t N;
+    uint32_t K;
+    uint32_t C;
+    const uint64_t *chain_off;    // [C+1]
+    const int32_t *blob_of;       // [K][C] blob index (within frame) of group g, -1 = volatile
+    const uint32_t *blob_start;   // [K][maxb] start of blob b's pixels in sorted[k]
+    const uint32_t *blob_size;    // [K][maxb]
+    uint32_t maxb;
+    const uint32_t *sorted;       // [K][npx] pixel indices sorted by (blob, row-major)
+    uint32_t npx;                 // pixels per frame canvas
+    uint32_t CW;                  // canvas width
+    const uint32_t *vol_xy;       // [K][C] rounded centre of volatile blobs (x | y << 16)
+    uint64_t seed;
+};
+// init_morph (thread.cpp:770-848): surface points in row-major order,
+// duplicates drawn from a random permutation with random fractions.
+int launch_chain_build(const ChainBuildArgs &a, cudaStream_t s);
+
+// ---- k_render.cu
+struct RenderScene {
+    uint32_t K, C;
+    uint64_t N;
+    uint32_t CW, CH;              // key-frame canvas
+    uint32_t width, height;       // output resolution
+    uint32_t bbox[4];
+    uint32_t motion, fading, density;
+    const uint64_t *P;            // [K][N]
+    const uint64_t *chain_off;    // [C+1]
+    const uint32_t *display;      // [K][CH][CW] RGB colour read by get_pixel
+    const int32_t *rank;          // [K][C] composite rank of group g in frame k
+};
+struct RenderWork;                // per-handle scratch (k_render.cu)
+RenderWork *render_work_create();
+void render_work_destroy(RenderWork *w);
+// Uploads the two Perlin permutations (lag map seed, slope map seed+1).
+int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope);
+// Renders the frame at normalised time `time` into out (device, width*height*4).
+int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, uint8_t *out,
+                 cudaStream_t s);
+// Writes key frame colours (display[CH][CW]) of present, non-transparent
+// pixels into a width*height RGBA8 frame (rendering before chains exist).
+int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32_t CW, uint32_t CH,
+                         uint32_t width, uint32_t height, uint8_t *out, cudaStream_t s);
+// Drops cached per-key-frame-pair data (chains or settings changed).
+void render_invalidate(RenderWork *w);
+
+// ---- k_blobs.cu
+struct BlobWork;
+BlobWork *blob_work_create();
+void blob_work_destroy(BlobWork *w);
+// 4-connected components of one key frame's present pixels: labels (blob
+// index by first pixel in row-major order, -1 absent) and per-blob exact sums
+// {count, sum x, sum y, sum r, sum g, sum b, sum a} of the stored colour.
+int label_components(BlobWork *w, const uint8_t *present, const uint32_t *stored, uint32_t CW, uint32_t CH,
+                     int32_t *labels, uint32_t *nblobs, cudaStream_t s);
+int blob_stats(BlobWork *w, const int32_t *labels, const uint32_t *stored, uint32_t CW, uint32_t CH,
+               uint32_t nblobs, unsigned long long *stats, cudaStream_t s);
+
+struct MatchArgs {
+    const double *desc;   // [K][Wb][7] blob descriptors (size, x, y, r, g, b, a)
+    int32_t *perm;        // [K][Wb] blob of group g in frame k (in/out)
+    uint32_t Wb, K;
+    double bbox_d, w_rgba, w_size, w_xy;
+    uint32_t sweeps;
+    uint64_t key;
+    size_t degenerate;
+    double *energy_out;   // device double
+};
+// Blob matching (thread.cpp:669-737): disjoint random group pairs per frame,
+// swapped when the blob-distance criterion c1 >= c2 holds.  One CTA.
+int launch_blob_match(const MatchArgs &a, cudaStream_t s);
+
+}  // namespace amg

@@ -1,0 +1,173 @@
+/*
+ * atomorph_gb300 — C ABI of the GB300 (sm_103a) morph pipeline.
+ *
+ * This is the drop-in boundary for the atomorph morph path.  Every entry point
+ * replaces one member of the reference's C++ class am::morph (morph.h:9-145)
+ * or one step the reference's demo performs around it; the comment on each
+ * declaration names the reference interface it replaces as file:line.  The
+ * C++ class am::morph in include/atomorph_gb300.hpp maps these calls back to
+ * the reference's own signatures (bool / no-op conventions).
+ *
+ * Conventions
+ *   - Functions returning int return an AM_* status.  Queries return their
+ *     value directly, with the reference's "missing" value (0, SIZE_MAX, ...).
+ *   - Pointers are plain host pointers unless a parameter says "device".
+ *   - A handle is used by one host thread at a time; its GPU work runs on
+ *     the handle's own CUDA stream (am_get_stream).
+ */
+#ifndef ATOMORPH_GB300_H
+#define ATOMORPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference's bool/nullptr conventions, made explicit) */
+#define AM_OK              0
+#define AM_ERR_BUSY        1  /* worker running: reference no-ops (morph.cpp:53,60,66,103) */
+#define AM_ERR_NOMEM       2  /* device or host allocation failed (reference: new(std::nothrow)) */
+#define AM_ERR_CUDA        3  /* a CUDA call failed; am_last_error() has the text */
+#define AM_ERR_TIMEOUT     4  /* suspend(timeout) expired (morph.cpp:80-100) / bounded wait expired */
+#define AM_ERR_ARG         5  /* invalid argument */
+#define AM_ERR_STATE       6  /* call not valid in the current pipeline state */
+#define AM_ERR_UNSUPPORTED 7  /* setting outside what the GPU path implements */
+#define AM_ERR_NOT_FOUND   8  /* frame / blob does not exist */
+
+/* ---- constants, same values as atomorph.h:235-248, 304-306 */
+#define AM_RGB     0
+#define AM_HSP     1
+#define AM_NONE    2
+#define AM_LINEAR  3
+#define AM_SPLINE  4
+#define AM_COSINE  5
+#define AM_PERLIN  6
+#define AM_STATE_BLOB_DETECTION   0
+#define AM_STATE_BLOB_UNIFICATION 1
+#define AM_STATE_BLOB_MATCHING    2
+#define AM_STATE_ATOM_MORPHING    3
+#define AM_STATE_DONE             4
+#define AM_HAS_PIXEL 1
+#define AM_HAS_FLUID 2
+#define AM_TEXTURE  0
+#define AM_AVERAGE  1
+#define AM_DISTINCT 2
+
+/* ---- swap proposal kinds (new; the reference has only uniform random pairs) */
+#define AM_PROPOSAL_RANDOM  0  /* disjoint uniform random pairs: the plain method */
+#define AM_PROPOSAL_LOCAL   1  /* spatially local candidates, exact gain, greedy disjoint matching */
+#define AM_PROPOSAL_LEARNED 2  /* local candidates ranked by the trained MLP, exact gain decides */
+
+typedef struct am_morph am_morph;
+
+/* ---- lifetime */
+int  am_create(am_morph **out);          /* morph::morph()  morph.cpp:9-12 */
+void am_destroy(am_morph *m);            /* morph::~morph() morph.cpp:14-16 */
+int  am_clear(am_morph *m);              /* morph::clear()  morph.cpp:18-50 */
+const char *am_last_error(void);         /* text of the last AM_ERR_CUDA / AM_ERR_ARG in this thread */
+const char *am_version(void);            /* am::get_version atomorph.cpp:1015-1017 */
+
+/* ---- key-frame ingestion */
+/* morph::add_pixel (morph.cpp:298-337): stores the pixel (HSP-converted when
+ * the delimiter is HSP), updates bbox and running frame means. */
+int am_add_pixel(am_morph *m, size_t frame, uint16_t x, uint16_t y,
+                 uint8_t r, uint8_t g, uint8_t b, uint8_t a);
+/* Bulk form of the demo's fill_morph (demo/main.cpp:96-127): every pixel of
+ * a w*h RGBA8 image with alpha > 0 is added in row-major order; an image
+ * with no such pixel adds an empty frame. */
+int am_add_pixels(am_morph *m, size_t frame, const uint8_t *rgba, uint32_t w, uint32_t h);
+int am_add_frame(am_morph *m, size_t frame);           /* morph::add_frame morph.cpp:287-296; AM_ERR_ARG if it exists */
+
+/* ---- parameters (morph.h:52-76, morph.cpp:436-444, 1517-1570) */
+int am_set_seed(am_morph *m, unsigned seed);                 /* morph::set_seed morph.cpp:436 */
+int am_set_blob_delimiter(am_morph *m, unsigned d);          /* morph.h:52 */
+int am_set_blob_threshold(am_morph *m, double t);            /* morph.h:53 */
+int am_set_blob_max_size(am_morph *m, size_t s);             /* morph.h:54 */
+int am_set_blob_min_size(am_morph *m, size_t s);             /* morph.h:55 */
+int am_set_blob_box_grip(am_morph *m, uint16_t g);           /* morph.h:56 */
+int am_set_blob_box_samples(am_morph *m, size_t s);          /* morph.h:57 */
+int am_set_blob_number(am_morph *m, size_t n);               /* morph.h:58 */
+int am_set_blob_rgba_weight(am_morph *m, unsigned w);        /* morph.h:59 */
+int am_set_blob_size_weight(am_morph *m, unsigned w);        /* morph.h:60 */
+int am_set_blob_xy_weight(am_morph *m, unsigned w);          /* morph.h:61 */
+int am_set_degeneration(am_morph *m, size_t d);              /* morph.h:62 */
+int am_set_motion(am_morph *m, unsigned motion);             /* morph.h:63 */
+int am_set_fading(am_morph *m, unsigned fading);             /* morph.h:64 */
+int am_set_threads(am_morph *m, size_t t);                   /* morph.h:65 (accepted; GPU width is automatic) */
+int am_set_cycle_length(am_morph *m, size_t c);              /* morph.h:66 (proposals per atom step, see DESIGN) */
+int am_set_feather(am_morph *m, size_t f);                   /* morph.h:67 */
+int am_set_keep_background(am_morph *m, int k);              /* morph.h:68 */
+int am_set_finite(am_morph *m, int f);                       /* morph.h:69 */
+int am_set_show_blobs(am_morph *m, unsigned b);              /* morph.h:70 */
+int am_set_fluid(am_morph *m, unsigned steps);               /* morph::set_fluid morph.cpp:1553-1560 */
+int am_set_density(am_morph *m, uint16_t d);                 /* morph::set_density morph.cpp:1562-1570 */
+int am_set_resolution(am_morph *m, uint16_t w, uint16_t h);  /* morph::set_resolution morph.cpp:1517-1520 */
+/* New knobs (no reference counterpart): swap proposal kind, sweeps per
+ * atom-morphing step, and the Perlin motion amplitude in pixels (0 = off). */
+int am_set_proposal(am_morph *m, unsigned kind);
+int am_set_sweeps(am_morph *m, size_t sweeps_per_step);
+int am_set_motion_noise(am_morph *m, double amplitude_px);
+
+/* ---- control (morph.h:40-49, morph.cpp:52-100, 102-269) */
+int am_compute(am_morph *m);                          /* morph::compute() morph.cpp:52-57 */
+int am_iterate(am_morph *m, size_t iterations);       /* morph::iterate morph.cpp:59-63 */
+int am_compute_seconds(am_morph *m, double seconds);  /* morph::compute(double) morph.cpp:65-70 */
+int am_suspend(am_morph *m);                          /* morph::suspend() morph.cpp:72-78 */
+int am_suspend_timeout(am_morph *m, double timeout);  /* morph::suspend(double) morph.cpp:80-100; AM_ERR_TIMEOUT on expiry */
+int am_is_busy(const am_morph *m);                    /* morph::is_busy morph.h:49; 1 or 0 */
+int am_synchronize(am_morph *m);                      /* morph::synchronize morph.cpp:102-269; AM_ERR_BUSY while running */
+int am_next_state(am_morph *m);                       /* morph::next_state morph.h:39 */
+
+/* ---- readout */
+unsigned am_get_state(const am_morph *m);                   /* morph.h:38 */
+double   am_get_energy(const am_morph *m);                  /* morph.h:41; the TRUE cost (see am_get_cost) */
+/* Exact atom cost: sum over chains of thread::get_energy(chain*)
+ * (thread.cpp:1109-1125), as an exact integer and as a double. */
+int      am_get_cost(am_morph *m, uint64_t *exact, double *as_double);
+size_t   am_get_blob_count(const am_morph *m, size_t frame);  /* morph::get_blob_count(f) morph.cpp:399-402 */
+size_t   am_get_blob_count_total(const am_morph *m);          /* morph::get_blob_count() morph.cpp:425-434 */
+size_t   am_get_pixel_count(const am_morph *m, size_t frame); /* morph::get_pixel_count morph.cpp:394-397 */
+size_t   am_get_frame_count(const am_morph *m);               /* morph.h:37 */
+size_t   am_get_frame_key(const am_morph *m, double t);       /* morph::get_frame_key morph.cpp:404-423 */
+uint16_t am_get_width(const am_morph *m);                     /* morph.h:35 */
+uint16_t am_get_height(const am_morph *m);                    /* morph.h:36 */
+double   am_get_time(const am_morph *m, size_t i, size_t n);  /* morph::get_time morph.cpp:1522-1538 */
+/* morph::get_average_pixel(f) morph.cpp:339-354: x, y, r, g, b, a (RGB). */
+int      am_get_average_pixel(const am_morph *m, size_t frame, uint16_t *xy, uint8_t *rgba);
+/* morph::get_average_pixel(f, b) morph.cpp:356-376. */
+int      am_get_blob_average(const am_morph *m, size_t frame, size_t blob, uint16_t *xy, uint8_t *rgba);
+size_t   am_get_atom_count(const am_morph *m);                /* total chain width (atoms per key frame) */
+size_t   am_get_chain_count(const am_morph *m);               /* chains = blob groups */
+
+/* Renders the frame at time t (morph::get_pixels(t, vec) morph.cpp:1405-1421)
+ * as width*height RGBA8, row-major.  out is a host pointer, or a device
+ * pointer when out_on_device != 0. */
+int am_render(am_morph *m, double t, uint8_t *out, int out_on_device);
+/* Renders n frames at times ts[0..n) into n consecutive device frames. */
+int am_render_many(am_morph *m, const double *ts, size_t n, uint8_t *out_device);
+
+/* ---- chains (reference chain = points[width][height], atomorph.h:286-298)
+ * pts is frame-major: pts[k * N + off_c + x] = point x of chain c at key
+ * frame k, as the reference's 8-byte point word (atomorph.h:275-284, padding
+ * byte zero).  blob_order[k * C + b] = group of the b-th blob of key frame k
+ * (composite order in draw_atoms, morph.cpp:1309). */
+int am_export_chains(am_morph *m, uint64_t *widths, uint64_t *pts, int32_t *blob_order);
+int am_import_chains(am_morph *m, size_t K, size_t C, const uint64_t *widths,
+                     const uint64_t *pts, const int32_t *blob_order);
+/* Runs n refinement sweeps now on the handle's stream with the current
+ * proposal kind (the synchronous form of the atom-morphing step,
+ * thread.cpp:1043-1068).  gains (optional, n entries) receive the exact cost
+ * decrease of each sweep. */
+int am_refine(am_morph *m, size_t sweeps, uint64_t *gains);
+
+/* ---- runtime */
+void    *am_get_stream(am_morph *m);        /* cudaStream_t of the handle */
+uint64_t am_launch_count(void);             /* kernels launched by this library, process-wide */
+int      am_device_sync(am_morph *m);       /* waits for the handle's stream */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

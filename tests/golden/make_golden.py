@@ -1,0 +1,109 @@
+"""Generates the golden fixtures in this directory from the UNMODIFIED
+reference library (oracle/_ref/libamref.so, built from the reference sources
+by oracle/Makefile).  Run it where the reference sources are present:
+
+    python tests/golden/make_golden.py
+
+Fixtures (all small, seeded):
+  hsp.npz         RGB->HSP and HSP->RGB byte conversions (color.cpp:64-92)
+  perlin.npz      8-octave Perlin noise samples (perlin.cpp:57-69)
+  spline.npz      cyclic Catmull-Rom samples (spline.cpp:45-57)
+  ellipses64.npz  64x64, 2 key frames: reference blobs, chains, cost, 20
+                  refinement sweeps, rendered frames (LINEAR, PERLIN, HSP)
+  spline48.npz    48x48, 3 key frames: chains and frames (SPLINE, COSINE, RGB,
+                  density 2)
+  fluid.npz       FluidModel::step on 300 particles for 8 steps
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+from atomorph_gb300 import synth  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+RENDER_TS = [0.0, 0.1, 0.37, 0.5, 0.8, 0.99]
+
+
+def morph_case(R, frames, *, seed, motion, fading, delimiter, density, sweeps, sweep_seed):
+    R.new(frames, seed=seed, motion=motion, fading=fading, delimiter=delimiter, density=density)
+    R.prepare()
+    w, K = R.widths()
+    st = R.state(seed, motion, fading, delimiter, density, frames)
+    out = dict(frames=np.stack(frames), seed=seed, motion=motion, fading=fading, delimiter=delimiter,
+               density=density, K=K, widths=w, pts0=st["pts"], blob_order=st["blob_order"], bbox=st["bbox"],
+               colors=st["colors"], present=st["present"], width=st["width"], height=st["height"],
+               blob_counts=np.array([R.blob_count(f) for f in range(K)]),
+               real_blob_sizes=np.array([sorted(s for g_, s, xy in R.blobs(f) if s > 0) + [0] * (
+                   R.blob_count(f) - sum(1 for g_, s, xy in R.blobs(f) if s > 0)) for f in range(K)]),
+               pixel_counts=np.array([R.pixel_count(f) for f in range(K)]),
+               energy0=R.energy())
+    R.sweeps(sweeps, sweep_seed)
+    out.update(sweeps=sweeps, sweep_seed=sweep_seed, pts=R.points(), energy=R.energy(), ts=np.array(RENDER_TS),
+               renders=np.stack([R.render(t) for t in RENDER_TS]))
+    return out
+
+
+def main():
+    orc.build(with_ref=True)
+    R = orc.Reference()
+    L = R.lib
+    rng = np.random.default_rng(2024)
+    rgb = rng.integers(0, 2**32, 4096, dtype=np.uint64).astype(np.uint32)
+    np.savez_compressed(os.path.join(HERE, "hsp.npz"), rgb=rgb,
+                        hsp=np.array([L.ref_rgb_to_hsp(int(c)) for c in rgb], np.uint32),
+                        back=np.array([L.ref_hsp_to_rgb(int(c)) for c in rgb], np.uint32))
+    xy = rng.uniform(0, 9, (512, 2))
+    seeds = np.array([1, 7, 8, 12345])
+    noise = np.array([[L.ref_octave_noise(int(s), x, y, 8) for x, y in xy] for s in seeds])
+    np.savez_compressed(os.path.join(HERE, "perlin.npz"), xy=xy, seeds=seeds, noise=noise)
+    pts = rng.uniform(0, 60, (5, 2))
+    ts = np.linspace(0, 0.999, 97)
+    sp = []
+    for t in ts:
+        o = np.zeros(2)
+        L.ref_spline_eval(pts.ctypes.data_as(orc.f64p), len(pts), t, o.ctypes.data_as(orc.f64p))
+        sp.append(o)
+    np.savez_compressed(os.path.join(HERE, "spline.npz"), pts=pts, ts=ts, values=np.array(sp))
+
+    frames = synth.workload("ellipses64")
+    np.savez_compressed(os.path.join(HERE, "ellipses64.npz"),
+                        **morph_case(R, frames, seed=7, motion=3, fading=6, delimiter=1, density=1, sweeps=20,
+                                     sweep_seed=123))
+    r3 = np.random.default_rng(48)
+    frames3 = [synth.ellipses_frame(48, 3, 4.0, 12.0, r3) for _ in range(3)]
+    np.savez_compressed(os.path.join(HERE, "spline48.npz"),
+                        **morph_case(R, frames3, seed=3, motion=4, fading=5, delimiter=0, density=2, sweeps=5,
+                                     sweep_seed=9))
+
+    n, gsx, gsy = 300, 40, 36
+    P = np.zeros((18, n))
+    P[0] = rng.uniform(6, 33, n); P[1] = rng.uniform(6, 29, n)
+    P[4] = P[0] + rng.normal(0, 2, n); P[5] = P[1] + rng.normal(0, 2, n)
+    P[6] = 1.0; P[7] = 1.0; P[8] = rng.random(n) < 0.7; P[9] = rng.choice([0.1, 1.0], n)
+    P[10:14] = rng.random((4, n)); P[14:18] = rng.random((4, n)); P[7][::13] = 0
+    h = L.ref_fluid_new(gsx, gsy, n)
+    q = np.zeros((n, 20)); q[:, :18] = P.T
+    L.ref_fluid_set(h, q.ctypes.data_as(orc.f64p), n)
+    steps = []
+    for s in range(8):
+        L.ref_fluid_step(h, 7 - s, 4.0, 0.25)
+        L.ref_fluid_get(h, q.ctypes.data_as(orc.f64p), n)
+        steps.append(q[:, :18].T.copy())
+    L.ref_fluid_free(h)
+    np.savez_compressed(os.path.join(HERE, "fluid.npz"), init=P, gsx=gsx, gsy=gsy, freedom=4.0,
+                        step1=steps[0], step8=steps[-1])
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

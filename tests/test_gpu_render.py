@@ -1,0 +1,84 @@
+"""Frame render parity: the CUDA renderer against frames the reference itself
+rendered (tests/golden) and against the oracle on larger seeded cases, from
+identical atom positions.  Tolerance: at most 1 LSB per channel (the CUDA
+path rounds exact rational weighted means where the reference rounds a
+double sum; they can differ only at exact .5 ties, and FP32 colour fades can
+move a value across a rounding boundary by one)."""
+import numpy as np
+import pytest
+
+from atomorph_gb300 import synth
+from conftest import golden, golden_state, morph_from_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _lsb(a, b):
+    d = np.abs(a.astype(np.int32) - b.astype(np.int32))
+    return int(d.max()), int((d > 0).sum())
+
+
+@pytest.mark.parametrize("case", ["ellipses64", "spline48"])
+def test_render_matches_reference_frames(capi, case):
+    g = golden(case)
+    m = morph_from_golden(capi, g)
+    for t, ref in zip(g["ts"], g["renders"]):
+        got = m.render(float(t))
+        worst, ndiff = _lsb(got, ref)
+        assert worst <= 1, f"t={t}: {ndiff} channels differ, worst {worst}"
+        assert ndiff <= max(4, ref.size // 500), f"t={t}: {ndiff} channels differ"
+
+
+@pytest.mark.parametrize("motion,fading,delimiter,density", [
+    (3, 6, 1, 1),   # LINEAR, PERLIN, HSP
+    (4, 5, 0, 1),   # SPLINE, COSINE, RGB
+    (4, 6, 1, 2),   # SPLINE, PERLIN, density 2
+    (2, 3, 0, 1),   # NONE, LINEAR
+])
+def test_render_matches_oracle_on_gpu_built_chains(capi, oracle, motion, fading, delimiter, density):
+    frames = synth.workload("shapes256")
+    m = capi.Morph()
+    m.load(frames, seed=11, blob_delimiter=delimiter, motion=motion, fading=fading, density=density)
+    assert m.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+    m.refine(20)
+    w, pts, order = m.export_chains()
+    from oracle.oracle import stored_frames
+    colors, present = stored_frames(frames, delimiter, oracle)
+    st = dict(K=len(frames), width=m.width, height=m.height, bbox=_bbox(frames), seed=11, motion=motion,
+              fading=fading, delimiter=delimiter, density=density, colors=colors, present=present, widths=w,
+              pts=pts, blob_order=order, frame_keys=np.arange(len(frames), dtype=np.uint64))
+    for t in (0.0, 0.13, 0.5, 0.77, 0.96):
+        ref = oracle.render(st, t)
+        got = m.render(t)
+        worst, ndiff = _lsb(got, ref)
+        assert worst <= 1, f"t={t}: worst {worst}, {ndiff} channels differ"
+        assert ndiff <= ref.size // 200
+
+
+def _bbox(frames):
+    xs, ys = [], []
+    for f in frames:
+        y, x = np.nonzero(f[..., 3])
+        xs += [x.min(), x.max()]
+        ys += [y.min(), y.max()]
+    return np.array([min(xs), min(ys), max(xs), max(ys)], np.uint32)
+
+
+def test_render_before_chains_shows_key_frame(capi):
+    frames = synth.workload("ellipses64")
+    m = capi.Morph()
+    m.load(frames, blob_delimiter=0)
+    m.run_until(capi.STATE_BLOB_MATCHING)
+    got = m.render(0.0)
+    exp = np.where(frames[0][..., 3:4] > 0, frames[0], 0)
+    assert np.array_equal(got, exp)
+
+
+def test_render_device_output_matches_host(capi):
+    torch = pytest.importorskip("torch")
+    g = golden("ellipses64")
+    m = morph_from_golden(capi, g)
+    buf = torch.zeros((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    for t in (0.2, 0.6):
+        m.render_device(t, buf.data_ptr())
+        assert np.array_equal(buf.cpu().numpy(), m.render(t))
