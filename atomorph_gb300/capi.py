@@ -93,6 +93,8 @@ _SIGS = {
     "am_import_chains": (C.c_int, [vp, C.c_size_t, C.c_size_t, u64p, u64p, i32p]),
     "am_refine": (C.c_int, [vp, C.c_size_t, u64p]),
     "am_get_stream": (vp, [vp]),
+    "am_profile_enable": (C.c_int, [vp, C.c_int]),
+    "am_profile_read": (C.c_size_t, [vp, C.POINTER(C.c_char_p), f64p, u64p, C.c_size_t]),
     "am_launch_count": (C.c_uint64, []),
     "am_device_sync": (C.c_int, [vp]),
 }
@@ -214,6 +216,17 @@ class Morph:
     def next_state(self) -> None:
         self.lib.am_next_state(self.h)
 
+    def wait(self, timeout: float = 600.0) -> None:
+        """Waits, without interrupting it, until the worker has used up its
+        iteration budget and paused (callers of the reference poll is_busy()
+        the same way; suspend() would cut the budget short)."""
+        import time
+        t0 = time.time()
+        while self.lib.am_is_busy(self.h):
+            if time.time() - t0 > timeout:
+                raise TimeoutError("worker still busy")
+            time.sleep(0.0005)
+
     def run_until(self, state: int, max_steps: int = 100000) -> int:
         """Synchronous driver: synchronize, step, synchronize until the worker
         reaches `state` (or max_steps)."""
@@ -221,7 +234,7 @@ class Morph:
         steps = 0
         while self.state < state and steps < max_steps:
             self.iterate(1)
-            self.suspend()
+            self.wait()
             _check(self.synchronize(), "am_synchronize")
             steps += 1
         return self.state
@@ -298,6 +311,16 @@ class Morph:
         K = order.shape[0]
         _check(self.lib.am_import_chains(self.h, K, len(widths), _p(widths, u64p), _p(pts, u64p), _p(order, i32p)),
                "am_import_chains")
+
+    def profile(self, on: bool) -> None:
+        _check(self.lib.am_profile_enable(self.h, 1 if on else 0), "am_profile_enable")
+
+    def profile_read(self) -> dict:
+        names = (C.c_char_p * 16)()
+        ms = np.zeros(16)
+        n = np.zeros(16, np.uint64)
+        k = self.lib.am_profile_read(self.h, names, _p(ms, f64p), _p(n, u64p), 16)
+        return {names[i].decode(): (float(ms[i]), int(n[i])) for i in range(k)}
 
     @property
     def stream(self) -> int:

@@ -281,6 +281,23 @@ int am_refine(am_morph *m, size_t sweeps, uint64_t *gains) {
 }
 
 // ---- runtime
+int am_profile_enable(am_morph *m, int on) {
+    CHECK(m);
+    m->e.prof.on = on != 0;
+    m->e.prof.reset();
+    return AM_OK;
+}
+size_t am_profile_read(am_morph *m, const char **names, double *ms, uint64_t *launches, size_t cap) {
+    if (!m) return 0;
+    m->e.prof.collect();
+    size_t n = 0;
+    for (int i = 0; i < amg::PROF_COUNT && n < cap; ++i, ++n) {
+        if (names) names[n] = amg::kProfNames[i];
+        if (ms) ms[n] = m->e.prof.ms[i];
+        if (launches) launches[n] = m->e.prof.launches[i];
+    }
+    return n;
+}
 void *am_get_stream(am_morph *m) { return m ? (void *)m->e.rstream : nullptr; }
 uint64_t am_launch_count(void) { return amg::g_launches.load(); }
 int am_device_sync(am_morph *m) {

@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <string>
+#include <vector>
 
 namespace amg {
 
@@ -31,6 +32,61 @@ extern std::atomic<uint64_t> g_launches;      // kernels launched by the library
     } while (0)
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// Opt-in per-kernel timing with CUDA events recorded on the launching stream
+// around each launch; read back (and waited for) by collect().
+enum ProfId {
+    PROF_SPLAT, PROF_SCAN, PROF_SCATTER, PROF_RESOLVE, PROF_PAIR, PROF_SWEEP_RANDOM, PROF_SWEEP_LOCAL,
+    PROF_MLP, PROF_FLUID, PROF_COUNT
+};
+struct Prof {
+    bool on = false;
+    struct Span { int id; cudaEvent_t a, b; };
+    std::vector<Span> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[PROF_COUNT] = {};
+    uint64_t launches[PROF_COUNT] = {};
+    cudaEvent_t open_ev = nullptr;
+    cudaEvent_t take() {
+        cudaEvent_t e = nullptr;
+        if (pool.empty()) cudaEventCreate(&e);
+        else { e = pool.back(); pool.pop_back(); }
+        return e;
+    }
+    void open(cudaStream_t s) {
+        if (!on) return;
+        open_ev = take();
+        cudaEventRecord(open_ev, s);
+    }
+    void close(int id, cudaStream_t s) {
+        if (!on || !open_ev) return;
+        cudaEvent_t b = take();
+        cudaEventRecord(b, s);
+        pending.push_back({id, open_ev, b});
+        open_ev = nullptr;
+    }
+    void collect() {
+        for (auto &sp : pending) {
+            float t = 0.f;
+            cudaEventSynchronize(sp.b);
+            cudaEventElapsedTime(&t, sp.a, sp.b);
+            ms[sp.id] += t;
+            launches[sp.id] += 1;
+            pool.push_back(sp.a);
+            pool.push_back(sp.b);
+        }
+        pending.clear();
+    }
+    void reset() {
+        collect();
+        for (int i = 0; i < PROF_COUNT; ++i) { ms[i] = 0; launches[i] = 0; }
+    }
+    ~Prof() {
+        for (auto &sp : pending) { cudaEventDestroy(sp.a); cudaEventDestroy(sp.b); }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+extern const char *const kProfNames[PROF_COUNT];
 
 // ------------------------------------------------------------- points -----
 // The reference's 8-byte point word (atomorph.h:275-284), little-endian:

@@ -20,6 +20,8 @@
 namespace amg {
 
 std::atomic<uint64_t> g_launches{0};
+const char *const kProfNames[PROF_COUNT] = {"k_frame_splat", "k_scan_u32",   "k_frame_scatter", "k_frame_resolve",
+                                            "pair_prep",     "k_sweep_random", "k_sweep_local", "mlp", "fluid"};
 static thread_local std::string t_error;
 void set_error(const std::string &msg) { t_error = msg; }
 const char *last_error() { return t_error.c_str(); }
@@ -66,6 +68,7 @@ static int ensure_streams(Engine *e) {
     AMG_CUDA(cudaStreamCreateWithFlags(&e->rstream, cudaStreamNonBlocking));
     e->rw = render_work_create();
     e->bw = blob_work_create();
+    render_set_prof(e->rw, &e->prof);
     int rc = render_set_perlin(e->rw, e->perm_lag, e->perm_slope);
     return rc;
 }
@@ -634,8 +637,10 @@ int Engine::refine(size_t sweeps, uint64_t *gains) {
             a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p);
             a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
             if (pair_off[C] > 0) {
+                prof.open(stream);
                 rc = launch_sweep_random(a, stream);
                 if (rc) return rc;
+                prof.close(PROF_SWEEP_RANDOM, stream);
             }
             pofs += (uint32_t)ph[p].size();
         }
@@ -744,8 +749,14 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         rc = render_frame(rw, sc, t, key, dst, rstream);
         if (rc) return rc;
     }
-    if (!out_dev) AMG_CUDA(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, rstream));
-    AMG_CUDA(cudaStreamSynchronize(rstream));
+    // A device frame is left in flight on the render stream (am_get_stream);
+    // a host frame is copied out and waited for.
+    if (!out_dev) {
+        AMG_CUDA(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, rstream));
+        AMG_CUDA(cudaStreamSynchronize(rstream));
+    } else {
+        AMG_CUDA(cudaGetLastError());
+    }
     return AM_OK;
 }
 

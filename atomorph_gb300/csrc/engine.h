@@ -148,6 +148,7 @@ class Engine {
     DBuf<uint32_t> d_sorted, d_keys, d_tk, d_tv, d_hist, d_bstart, d_bsize, d_volxy;
     DBuf<int32_t> d_blob_of;
     DBuf<uint8_t> d_frame;                 // host-output staging frame
+    Prof prof;
     RenderWork *rw = nullptr;
     BlobWork *bw = nullptr;
     uint8_t *h_pinned = nullptr;

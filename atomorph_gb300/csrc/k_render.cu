@@ -59,7 +59,10 @@ struct RenderWork {
     uint32_t ntiles_cap = 0;
     int *perm = nullptr;    // [2][512] Perlin permutations on the device
     bool perm_set = false;
+    Prof *prof = nullptr;   // optional per-kernel timing
 };
+
+void render_set_prof(RenderWork *w, Prof *p) { w->prof = p; }
 
 RenderWork *render_work_create() { return new RenderWork(); }
 
@@ -593,8 +596,10 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     double dt = 1.0 / double(sc.K);
     double t = std::max(0.0, (time - (double)(frame_key * dt)) / dt);
     if (w->pair_f != (int)f || w->motion != sc.motion || w->fading != sc.fading) {
+        if (w->prof) w->prof->open(s);
         int rc = prep_pair(w, sc, (uint32_t)f, s);
         if (rc) return rc;
+        if (w->prof) w->prof->close(PROF_PAIR, s);
     }
     uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
     uint32_t ntiles = tiles_x * tiles_y;
@@ -641,21 +646,29 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     if (n) {
         unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 4);
         size_t smem = ntiles <= 8192 ? ntiles * 4 : 0;
+        if (w->prof) w->prof->open(s);
         AMG_LAUNCH(k_frame_splat, grid, 256, smem, s, sc, fa, n, w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2,
                    w->spl, w->tile_cnt);
+        if (w->prof) w->prof->close(PROF_SPLAT, s);
     }
     AMG_CUDA(cudaMemcpyAsync(w->tile_off, w->tile_cnt, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
     {
+        if (w->prof) w->prof->open(s);
         int rc = launch_scan_u32(w->tile_off, (size_t)ntiles + 1, nullptr, s);
         if (rc) return rc;
+        if (w->prof) w->prof->close(PROF_SCAN, s);
     }
     AMG_CUDA(cudaMemcpyAsync(w->tile_cur, w->tile_off, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
     if (n) {
         unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 4);
+        if (w->prof) w->prof->open(s);
         AMG_LAUNCH(k_frame_scatter, grid, 256, 0, s, w->spl, n, tiles_x, w->tile_cur, w->rec);
+        if (w->prof) w->prof->close(PROF_SCATTER, s);
     }
+    if (w->prof) w->prof->open(s);
     AMG_LAUNCH(k_frame_resolve, ntiles, 256, 0, s, w->rec, w->tile_off, tiles_x, sc.width, sc.height,
                sc.density ? sc.density : 1u, out);
+    if (w->prof) w->prof->close(PROF_RESOLVE, s);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }

@@ -12,6 +12,8 @@
 
 namespace amg {
 
+struct Prof;
+
 // ---- k_colour.cu
 int launch_colour(const uint32_t *raw, const uint8_t *present, uint32_t *stored, uint32_t *display, size_t n,
                   int display_hsp, cudaStream_t s);
@@ -89,6 +91,7 @@ struct RenderScene {
 struct RenderWork;                // per-handle scratch (k_render.cu)
 RenderWork *render_work_create();
 void render_work_destroy(RenderWork *w);
+void render_set_prof(RenderWork *w, Prof *p);
 // Uploads the two Perlin permutations (lag map seed, slope map seed+1).
 int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope);
 // Renders the frame at normalised time `time` into out (device, width*height*4).

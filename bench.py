@@ -1,0 +1,468 @@
+"""Benchmark of the morph hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (N=1): ``shapes1024`` — 8 seeded 1024x1024 RGBA8 key frames of 40-80
+overlapping ellipses/rectangles (~1M atoms per key frame), SPLINE motion,
+PERLIN colour fading, HSP blob delimiter.  Setup (untimed) runs the whole
+pipeline on the GPU: blobs, matching, chains, refinement.  One step renders
+the full morph cycle, 240 output frames at t = i/240, into device memory;
+``value`` is frames/s with everything resident in HBM.  ``e2e`` renders the
+same frames through the C ABI into pinned HOST memory (device->host copy of
+every frame inside the timed region).  ``time_to_cost`` reports the
+refinement side of the metric (plain random-pair sweeps vs the guided
+proposal) on the same chains.
+
+--impl reference times the reference's CPU implementation of the render on
+this machine's host cores: the oracle restatement (the reference itself is
+not built on this machine), every host thread rendering its own frames.
+Under torchrun every rank renders its own cycle (replicas, weak scaling, no
+collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s at 1024²"
+UNIT = "frames/s"
+WORKLOAD = "shapes1024"
+FRAMES_PER_STEP = 240
+SETTINGS = dict(seed=5, blob_delimiter=1, motion=4, fading=6, density=1)
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, path):
+        self.path = path
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self, gpu_index=0):
+        try:
+            rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = [r for r in rows if len(r) >= 9 and r[0].strip() == str(gpu_index)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "samples": len(rows),
+                "reasons": sorted(reasons)}
+
+
+def setup_morph(capi, frames, refine_sweeps):
+    m = capi.Morph()
+    m.load(frames, **SETTINGS)
+    st = m.run_until(capi.STATE_ATOM_MORPHING)
+    if st != capi.STATE_ATOM_MORPHING:
+        raise RuntimeError(f"pipeline stopped in state {st}")
+    if refine_sweeps:
+        m.refine(refine_sweeps)
+    return m
+
+
+def render_roofline(m, frames_ts, torch, stream):
+    """Per-kernel live CUDA-event timing over one extra cycle, and the
+    algorithmic bytes of the dominant kernel."""
+    m.profile(True)
+    buf = torch.empty((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    for t in frames_ts:
+        m.render_device(float(t), buf.data_ptr())
+    stream.synchronize()
+    prof = m.profile_read()
+    m.profile(False)
+    return prof
+
+
+def bench_ours(args, rank, world):
+    import torch
+    from atomorph_gb300 import capi, synth
+
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    frames = synth.workload(WORKLOAD)
+    atoms_per_frame = int(np.mean([synth.opaque_count(f) for f in frames]))
+    m = setup_morph(capi, frames, refine_sweeps=args.refine_sweeps)
+    N, K = m.atoms, len(frames)
+    stream = torch.cuda.ExternalStream(m.stream)
+    ts = [m.get_time(i, FRAMES_PER_STEP) for i in range(FRAMES_PER_STEP)]
+    out = torch.empty((FRAMES_PER_STEP, m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    fb = m.height * m.width * 4
+
+    def step():
+        base = out.data_ptr()
+        for i, t in enumerate(ts):
+            m.render_device(float(t), base + i * fb)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = capi.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                             f"clocks_rank{rank}.csv")) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = capi.launch_count() - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    total_frames = FRAMES_PER_STEP * args.steps * world
+    value = total_frames / (ms / 1e3)
+
+    # e2e: same frames through the C ABI into pinned host memory
+    host = torch.empty((8, m.height, m.width, 4), dtype=torch.uint8).pin_memory()
+    hp = host.data_ptr()
+    for i in range(min(16, len(ts))):
+        m.lib.am_render(m.h, float(ts[i]), hp + (i % 8) * fb, 0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for i, t in enumerate(ts):
+            rc = m.lib.am_render(m.h, float(t), hp + (i % 8) * fb, 0)
+            assert rc == 0
+    e2e_s = time.perf_counter() - t0
+    e2e = FRAMES_PER_STEP * args.steps * world / e2e_s
+
+    # roofline of the dominant kernel from a profiled cycle
+    prof = render_roofline(m, ts, torch, stream)
+    per_frame = {k: v for k, v in prof.items() if v[1] > 0}
+    dom = max(per_frame.items(), key=lambda kv: kv[1][0])
+    hbm, peak_kind = _peaks()
+    # Algorithmic bytes per frame (spline path): per active atom the four
+    # control points (32 B) + two colours (8 B) + lag/slope (8 B) + chain rank
+    # (4 B) + original index (4 B) = 56 B read once, plus 4 B per output pixel.
+    frame_bytes = N * 56 + m.width * m.height * 4
+    frame_ms_profiled = sum(v[0] for v in per_frame.values() if True) / FRAMES_PER_STEP
+    dom_name, (dom_ms, dom_n) = dom[0], dom[1]
+    dom_avg_ms = dom_ms / dom_n
+    # Algorithmic bytes attributed to the dominant kernel (roofline)
+    kernel_bytes = {
+        "k_frame_splat": N * 56,
+        "k_frame_scatter": N * 16 * 2,
+        "k_frame_resolve": N * 16 + m.width * m.height * 4,
+        "pair_prep": N * 8 * 4,
+        "k_scan_u32": 4 * 1024 * 2,
+    }.get(dom_name, frame_bytes)
+    achieved = kernel_bytes / (dom_avg_ms / 1e3) / 1e9
+    roof = {"kernel": dom_name, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "peak_kind": peak_kind, "traffic": None,
+            "algorithmic_bytes_per_launch": int(kernel_bytes), "avg_launch_ms": round(dom_avg_ms, 5),
+            "frame": {"algorithmic_bytes": int(frame_bytes), "profiled_ms": round(frame_ms_profiled, 5),
+                      "achieved_gbs": round(frame_bytes / (frame_ms_profiled / 1e3) / 1e9, 1),
+                      "frac": round(frame_bytes / (frame_ms_profiled / 1e3) / 1e9 / hbm, 4)},
+            "kernels_ms_per_frame": {k: round(v[0] / FRAMES_PER_STEP, 5) for k, v in per_frame.items()}}
+
+    ttc = None
+    if rank == 0 and args.time_to_cost:
+        ttc = time_to_cost(capi, frames, args)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(m, frames, ts, args)
+
+    res = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/int32 fixed-point (exact integer means)",
+        "data": "synthetic seeded key frames (no public dataset exists for this path)",
+        "config": {"workload": WORKLOAD, "key_frames": K, "resolution": [m.width, m.height],
+                   "atoms_per_key_frame": atoms_per_frame, "chain_atoms": N, "chains": m.chains,
+                   "frames_per_step": FRAMES_PER_STEP, "motion": "spline", "fading": "perlin",
+                   "refine_sweeps_before_render": args.refine_sweeps,
+                   "l2": "per-step working set > L2 (240 output frames, 960 MB, written each step)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": FRAMES_PER_STEP * fb},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "clocks": clk.summary(),
+    }
+    if ttc is not None:
+        res["time_to_cost"] = ttc
+    if cpu is not None:
+        res["cpu_baseline"] = cpu
+    return res
+
+
+def time_to_cost(capi, frames, args):
+    """Refinement half of the metric on the same workload: sweeps and wall
+    time of the plain random-pair refinement to its converged cost, and the
+    time for each proposal kind to get within 0.5% of it."""
+    out = {}
+    m = setup_morph(capi, frames, refine_sweeps=0)
+    w, pts0, order = m.export_chains()
+    c0 = m.cost()
+    # plain to convergence: stop when a block of sweeps gains < 1e-5 of cost
+    block = 50
+    t0 = time.perf_counter()
+    trace = [(0, 0.0, c0)]
+    sweeps = 0
+    while sweeps < args.plain_max_sweeps:
+        g = m.refine(block, capi.PROPOSAL_RANDOM)
+        sweeps += block
+        c = trace[-1][2] - int(g.sum())
+        trace.append((sweeps, time.perf_counter() - t0, c))
+        if g.sum() < 1e-5 * c:
+            break
+    c_plain = trace[-1][2]
+    target = 1.005 * c_plain
+    hit = next((tr for tr in trace if tr[2] <= target), trace[-1])
+    out["plain"] = {"converged_cost": int(c_plain), "converged_sweeps": sweeps,
+                    "converged_s": round(trace[-1][1], 3), "sweeps_to_target": hit[0],
+                    "s_to_target": round(hit[1], 4)}
+    out["initial_cost"] = int(c0)
+    out["target_cost"] = int(target)
+    for kind, name in ((capi.PROPOSAL_LOCAL, "local"), (capi.PROPOSAL_LEARNED, "learned")):
+        try:
+            m.import_chains(w, pts0, order)
+            t0 = time.perf_counter()
+            sweeps, c = 0, c0
+            while c > target and sweeps < args.plain_max_sweeps:
+                g = m.refine(5, kind)
+                sweeps += 5
+                c -= int(g.sum())
+            out[name] = {"sweeps_to_target": sweeps, "s_to_target": round(time.perf_counter() - t0, 4),
+                         "cost": int(c), "reached": bool(c <= target)}
+        except Exception as e:  # proposal kind not available
+            out[name] = {"unavailable": str(e).splitlines()[0][:160]}
+    if "s_to_target" in out.get("learned", {}) and out["learned"]["reached"]:
+        out["speedup_learned_vs_plain"] = round(out["plain"]["s_to_target"] / max(out["learned"]["s_to_target"], 1e-9), 2)
+    m.close()
+    return out
+
+
+def cpu_baseline(m, frames, ts, args):
+    """The oracle restatement of the reference render, timed on one host
+    thread on a bounded sample of the same frames and chains."""
+    from oracle import oracle as orc
+    O = orc.Oracle()
+    w, pts, order = m.export_chains()
+    st = _oracle_state(O, m, frames, w, pts, order)
+    sample = [ts[i] for i in (37, 150)][: args.cpu_frames]
+    t0 = time.perf_counter()
+    O.render_many(st, sample, threads=1)
+    dt = time.perf_counter() - t0
+    return {"value": round(len(sample) / dt, 5), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{len(sample)} frames of {WORKLOAD} (t={', '.join(f'{t:.4f}' for t in sample)}), same chains"}
+
+
+def _oracle_state(O, m, frames, w, pts, order):
+    from oracle import oracle as orc
+    colors, present = orc.stored_frames(frames, SETTINGS["blob_delimiter"], O)
+    xs, ys = [], []
+    for f in frames:
+        y, x = np.nonzero(f[..., 3])
+        xs += [int(x.min()), int(x.max())]
+        ys += [int(y.min()), int(y.max())]
+    return dict(K=len(frames), width=m.width, height=m.height, bbox=np.array([min(xs), min(ys), max(xs), max(ys)]),
+                seed=SETTINGS["seed"], motion=SETTINGS["motion"], fading=SETTINGS["fading"],
+                delimiter=SETTINGS["blob_delimiter"], density=SETTINGS["density"], colors=colors, present=present,
+                widths=w, pts=pts, blob_order=order, frame_keys=np.arange(len(frames), dtype=np.uint64))
+
+
+def bench_reference(args, rank, world):
+    """CPU reference arm: chains built on the CPU by the oracle (components,
+    blob matching, chain construction, a few reference sweeps), then every
+    step renders one frame per host thread with the oracle renderer."""
+    if rank != 0:
+        return None
+    from atomorph_gb300 import synth
+    from oracle import oracle as orc
+    O = orc.Oracle()
+    frames = synth.workload(WORKLOAD)
+    K = len(frames)
+    st = cpu_pipeline(O, frames)
+    threads = os.cpu_count() or 1
+    ts = [i / FRAMES_PER_STEP for i in range(FRAMES_PER_STEP)]
+    per_step = threads
+    cursor = [0]
+
+    def step():
+        sample = [ts[(cursor[0] + j * 17) % FRAMES_PER_STEP] for j in range(per_step)]
+        cursor[0] += 1
+        O.render_many(st, sample, threads=threads)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = per_step * args.steps / dt
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference arithmetic)",
+        "data": "synthetic seeded key frames",
+        "config": {"workload": WORKLOAD, "key_frames": K, "resolution": [1024, 1024],
+                   "chain_atoms": int(np.sum(st["widths"])), "frames_per_step": per_step,
+                   "parallelism": f"{threads} host threads, one frame each"},
+        "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{per_step} frames per step of {WORKLOAD}, one per host thread"},
+        "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def cpu_pipeline(O, frames):
+    """CPU restatement of the reference pipeline up to chains: components,
+    blob matching, chain construction (oracle/oracle.cpp)."""
+    import ctypes as C
+    from oracle import oracle as orc
+    K = len(frames)
+    delim = SETTINGS["blob_delimiter"]
+    colors, present = orc.stored_frames(frames, delim, O)
+    descs, labels_all = [], []
+    for k, img in enumerate(frames):
+        st_img = colors[k].view(np.uint8).reshape(img.shape)
+        lab, stats = O.components(img, st_img)
+        labels_all.append(lab)
+        d = np.zeros((len(stats), 7))
+        d[:, 0] = stats[:, 0]
+        d[:, 1:3] = stats[:, 1:3] / stats[:, :1]
+        d[:, 3:7] = stats[:, 3:7] / stats[:, :1] / 255.0
+        descs.append(d)
+    Wb = max(len(d) for d in descs)
+    desc = np.zeros((K, Wb, 7))
+    for k, d in enumerate(descs):
+        desc[k, :len(d)] = d
+        desc[k, len(d):, 1:3] = d[:, 1:3].mean(0) if len(d) else 0
+    perm = np.tile(np.arange(Wb, dtype=np.int32), (K, 1))
+    xs, ys = [], []
+    for f in frames:
+        y, x = np.nonzero(f[..., 3])
+        xs += [int(x.min()), int(x.max())]
+        ys += [int(y.min()), int(y.max())]
+    bbox = np.array([min(xs), min(ys), max(xs), max(ys)])
+    bbox_d = float((bbox[2] - bbox[0]) ** 2 + (bbox[3] - bbox[1]) ** 2)
+    wr, ws, wx = orc.blob_weights(1, 1, 1)
+    O.lib.orc_blob_match(desc.ctypes.data_as(orc.f64p), perm.ctypes.data_as(orc.i32p), Wb, K, 20000, 1, bbox_d,
+                         wr, ws, wx)
+    widths, chains = [], []
+    for g in range(Wb):
+        surfs, keep = [], []
+        cnt = np.zeros(K, np.uint64)
+        cx = np.zeros(K)
+        cy = np.zeros(K)
+        colk = np.zeros((K, 7))
+        for k in range(K):
+            b = perm[k, g]
+            colk[k] = desc[k, b]
+            if b < len(descs[k]):
+                ys_, xs_ = np.nonzero(labels_all[k] == b)
+                pos = (ys_.astype(np.uint64) * 65536 + xs_.astype(np.uint64))
+                pos.sort()
+            else:
+                pos = np.zeros(0, np.uint64)
+            keep.append(pos)
+            cnt[k] = len(pos)
+        O.lib.orc_fix_volatiles(colk.ctypes.data_as(orc.f64p), K)
+        cx[:] = colk[:, 1]
+        cy[:] = colk[:, 2]
+        ptrs = (orc.u64p * K)(*[p.ctypes.data_as(orc.u64p) for p in keep])
+        wdt = O.lib.orc_chain_build(ptrs, cnt.ctypes.data_as(orc.u64p), cx.ctypes.data_as(orc.f64p),
+                                    cy.ctypes.data_as(orc.f64p), K, SETTINGS["density"], g, None, 0)
+        buf = np.zeros(int(wdt) * K, np.uint64)
+        O.lib.orc_chain_build(ptrs, cnt.ctypes.data_as(orc.u64p), cx.ctypes.data_as(orc.f64p),
+                              cy.ctypes.data_as(orc.f64p), K, SETTINGS["density"], g,
+                              buf.ctypes.data_as(orc.u64p), int(wdt))
+        widths.append(int(wdt))
+        chains.append(buf.reshape(K, int(wdt)))
+    widths = np.array(widths, np.uint64)
+    pts = np.concatenate(chains, axis=1).reshape(-1)
+    order = np.zeros((K, Wb), np.int32)
+    for k in range(K):
+        for g in range(Wb):
+            order[k, perm[k, g]] = g
+    return dict(K=K, width=1024, height=1024, bbox=bbox, seed=SETTINGS["seed"], motion=SETTINGS["motion"],
+                fading=SETTINGS["fading"], delimiter=delim, density=SETTINGS["density"], colors=colors,
+                present=present, widths=widths, pts=pts, blob_order=order,
+                frame_keys=np.arange(K, dtype=np.uint64))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--refine-sweeps", type=int, default=100)
+    ap.add_argument("--time-to-cost", type=int, default=1)
+    ap.add_argument("--plain-max-sweeps", type=int, default=3000)
+    ap.add_argument("--cpu-frames", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        res = bench_reference(args, rank, world)
+    else:
+        res = bench_ours(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -162,8 +162,14 @@ int am_import_chains(am_morph *m, size_t K, size_t C, const uint64_t *widths,
  * decrease of each sweep. */
 int am_refine(am_morph *m, size_t sweeps, uint64_t *gains);
 
-/* ---- runtime */
-void    *am_get_stream(am_morph *m);        /* cudaStream_t of the handle */
+/* ---- runtime (no reference counterpart) */
+void    *am_get_stream(am_morph *m);        /* cudaStream_t that renders run on */
+/* Per-kernel timing: when enabled, CUDA events are recorded on the launching
+ * stream around every render / refinement kernel; am_profile_read waits for
+ * them and returns, per kernel kind, the name, total milliseconds and launch
+ * count (up to cap kinds; returns the number written). */
+int      am_profile_enable(am_morph *m, int on);
+size_t   am_profile_read(am_morph *m, const char **names, double *ms, uint64_t *launches, size_t cap);
 uint64_t am_launch_count(void);             /* kernels launched by this library, process-wide */
 int      am_device_sync(am_morph *m);       /* waits for the handle's stream */
 

@@ -87,6 +87,6 @@ def test_worker_thread_runs_and_suspends(capi):
     m.next_state()
     assert m.synchronize() == capi.AM_OK
     m.iterate(1)
-    m.suspend()
+    m.wait()
     m.synchronize()
     assert m.state == capi.STATE_DONE
