@@ -30,7 +30,10 @@ UNITS = [
     ("k_chains.cu", []),
     ("k_render.cu", []),
     ("k_blobs.cu", []),
+    ("k_local.cu", []),
+    ("k_mlp.cu", []),
     ("engine.cpp", ["-x", "cu"]),
+    ("engine_mlp.cpp", ["-x", "cu"]),
     ("capi.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
 ]
 

@@ -92,6 +92,13 @@ _SIGS = {
     "am_export_chains": (C.c_int, [vp, u64p, u64p, i32p]),
     "am_import_chains": (C.c_int, [vp, C.c_size_t, C.c_size_t, u64p, u64p, i32p]),
     "am_refine": (C.c_int, [vp, C.c_size_t, u64p]),
+    "am_record_swaps": (C.c_int, [vp, C.c_size_t]),
+    "am_recorded_swaps": (C.c_size_t, [vp, f32p, f32p, C.c_size_t]),
+    "am_train_proposal": (C.c_int, [vp, f32p, f32p, C.c_size_t, C.c_size_t, C.c_double, f32p]),
+    "am_get_proposal_weights": (C.c_int, [vp, f32p, C.c_size_t]),
+    "am_set_proposal_weights": (C.c_int, [vp, f32p, C.c_size_t]),
+    "am_proposal_forward": (C.c_int, [vp, f32p, C.c_size_t, f32p]),
+    "am_proposal_grad": (C.c_int, [vp, f32p, f32p, C.c_size_t, f32p, f32p]),
     "am_get_stream": (vp, [vp]),
     "am_profile_enable": (C.c_int, [vp, C.c_int]),
     "am_profile_read": (C.c_size_t, [vp, C.POINTER(C.c_char_p), f64p, u64p, C.c_size_t]),
@@ -311,6 +318,48 @@ class Morph:
         K = order.shape[0]
         _check(self.lib.am_import_chains(self.h, K, len(widths), _p(widths, u64p), _p(pts, u64p), _p(order, i32p)),
                "am_import_chains")
+
+    # -- learned proposal -----------------------------------------------------
+    def record_swaps(self, cap: int) -> None:
+        _check(self.lib.am_record_swaps(self.h, cap), "am_record_swaps")
+
+    def recorded_swaps(self, cap: int):
+        f = np.zeros((cap, 10), np.float32)
+        t = np.zeros(cap, np.float32)
+        n = self.lib.am_recorded_swaps(self.h, _p(f, f32p), _p(t, f32p), cap)
+        return f[:n], t[:n]
+
+    def train_proposal(self, feats, targets, epochs: int = 3, lr: float = 1e-3) -> float:
+        feats = np.ascontiguousarray(feats, np.float32)
+        targets = np.ascontiguousarray(targets, np.float32)
+        loss = C.c_float()
+        _check(self.lib.am_train_proposal(self.h, _p(feats, f32p), _p(targets, f32p), len(targets), epochs, lr,
+                                          C.byref(loss)), "am_train_proposal")
+        return loss.value
+
+    def proposal_weights(self, w=None):
+        if w is None:
+            out = np.zeros(4929, np.float32)
+            _check(self.lib.am_get_proposal_weights(self.h, _p(out, f32p), 4929), "am_get_proposal_weights")
+            return out
+        w = np.ascontiguousarray(w, np.float32)
+        _check(self.lib.am_set_proposal_weights(self.h, _p(w, f32p), len(w)), "am_set_proposal_weights")
+        return w
+
+    def proposal_forward(self, feats):
+        feats = np.ascontiguousarray(feats, np.float32)
+        out = np.zeros(len(feats), np.float32)
+        _check(self.lib.am_proposal_forward(self.h, _p(feats, f32p), len(feats), _p(out, f32p)), "am_proposal_forward")
+        return out
+
+    def proposal_grad(self, feats, targets):
+        feats = np.ascontiguousarray(feats, np.float32)
+        targets = np.ascontiguousarray(targets, np.float32)
+        g = np.zeros(4929, np.float32)
+        loss = C.c_float()
+        _check(self.lib.am_proposal_grad(self.h, _p(feats, f32p), _p(targets, f32p), len(targets), _p(g, f32p),
+                                         C.byref(loss)), "am_proposal_grad")
+        return g, loss.value
 
     def profile(self, on: bool) -> None:
         _check(self.lib.am_profile_enable(self.h, 1 if on else 0), "am_profile_enable")

@@ -280,6 +280,33 @@ int am_refine(am_morph *m, size_t sweeps, uint64_t *gains) {
     return e.publish_front();
 }
 
+// ---- learned proposal
+int am_record_swaps(am_morph *m, size_t cap) { CHECK(m); return H(m).record_swaps(cap); }
+size_t am_recorded_swaps(am_morph *m, float *f, float *t, size_t cap) { return m ? m->e.recorded_swaps(f, t, cap) : 0; }
+int am_train_proposal(am_morph *m, const float *f, const float *t, size_t n, size_t epochs, double lr, float *loss) {
+    CHECK(m);
+    if (H(m).is_busy()) return AM_ERR_BUSY;
+    return H(m).train_proposal(f, t, n, epochs, lr, loss);
+}
+int am_get_proposal_weights(am_morph *m, float *w, size_t count) {
+    CHECK(m);
+    return H(m).proposal_weights(w, count, false);
+}
+int am_set_proposal_weights(am_morph *m, const float *w, size_t count) {
+    CHECK(m);
+    return H(m).proposal_weights(const_cast<float *>(w), count, true);
+}
+int am_proposal_forward(am_morph *m, const float *f, size_t n, float *out) {
+    CHECK(m);
+    if ((!f || !out) && n) return AM_ERR_ARG;
+    return H(m).proposal_forward(f, n, out);
+}
+int am_proposal_grad(am_morph *m, const float *f, const float *t, size_t n, float *grad, float *loss) {
+    CHECK(m);
+    if (!grad || ((!f || !t) && n)) return AM_ERR_ARG;
+    return H(m).proposal_grad(f, t, n, grad, loss);
+}
+
 // ---- runtime
 int am_profile_enable(am_morph *m, int on) {
     CHECK(m);

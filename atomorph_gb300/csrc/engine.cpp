@@ -73,6 +73,8 @@ static int ensure_streams(Engine *e) {
     return rc;
 }
 
+int Engine::ensure_streams_public() { return ensure_streams(this); }
+
 // ------------------------------------------------------------ ingestion --
 static void grow(HostFrame &f, uint32_t w, uint32_t h) {
     if (w <= f.w && h <= f.h) return;
@@ -472,6 +474,7 @@ static std::vector<std::vector<uint32_t>> phases_for(uint32_t K) {
 }
 
 int Engine::set_chain_layout(const std::vector<uint64_t> &w) {
+    local_valid = false;
     widths = w;
     C = (uint32_t)w.size();
     chain_off.assign(C + 1, 0);
@@ -624,6 +627,7 @@ int Engine::refine(size_t sweeps, uint64_t *gains) {
         int rc = refine_guided(sweeps, gains);
         return rc;
     }
+    local_valid = false;  // plain sweeps move points without the guided index
     int rc;
     if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * sweeps + 4)))) return rc;
     AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * sweeps * 8, stream));
@@ -812,11 +816,90 @@ int Engine::copy_keyframe(size_t f, uint8_t *dst) {
     return launch_keyframe_copy(d_display.p + f * fr, d_present.p + f * fr, CW, CH, width, height, dst, rstream);
 }
 
+int Engine::ensure_local_index() {
+    if (local_valid) return AM_OK;
+    int rc;
+    uint32_t ncells = ((CW + 1) / 2) * ((CH + 1) / 2);
+    size_t maxph = 0;
+    for (auto &p : phases_for(K)) maxph = std::max(maxph, p.size());
+    if ((rc = d_slot_pt.reserve(N * K))) return rc;
+    if ((rc = d_col.reserve(N * K))) return rc;
+    if ((rc = d_slot_of.reserve(N * K))) return rc;
+    if ((rc = d_cell_start.reserve((size_t)K * (ncells + 1)))) return rc;
+    if ((rc = d_chain_id.reserve(N))) return rc;
+    if ((rc = d_chain_w1.reserve(std::max<uint32_t>(C, 1)))) return rc;
+    if ((rc = d_claim.reserve(N * maxph))) return rc;
+    if ((rc = d_pgain.reserve(N * maxph))) return rc;
+    if ((rc = d_lprop.reserve(N * maxph))) return rc;
+    if ((rc = d_lk.reserve(N))) return rc;
+    if ((rc = d_lv.reserve(N))) return rc;
+    if ((rc = d_tk.reserve(N))) return rc;
+    if ((rc = d_tv.reserve(N))) return rc;
+    if ((rc = d_hist.reserve(radix_hist_words(N)))) return rc;
+    std::vector<uint8_t> w1(std::max<uint32_t>(C, 1), 0);
+    for (uint32_t c = 0; c < C; ++c) w1[c] = widths[c] <= 1;
+    AMG_CUDA(cudaMemcpyAsync(d_chain_w1.p, w1.data(), w1.size(), cudaMemcpyHostToDevice, stream));
+    lix.slot_pt = d_slot_pt.p; lix.col = d_col.p; lix.slot_of = d_slot_of.p; lix.cell_start = d_cell_start.p;
+    lix.chain_id = d_chain_id.p; lix.chain_w1 = d_chain_w1.p;
+    rc = local_index_build(lix, d_P.p, N, K, CW, CH, d_chain_off.p, C, d_lk.p, d_lv.p, d_tk.p, d_tv.p, d_hist.p,
+                           stream);
+    if (rc) return rc;
+    local_valid = true;
+    return AM_OK;
+}
+
 int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
-    (void)sweeps;
-    (void)gains;
-    set_error("proposal kind not available in this build");
-    return AM_ERR_UNSUPPORTED;
+    if (active.proposal == AM_PROPOSAL_LEARNED && !mlp_ready()) {
+        set_error("the learned proposal needs a trained network (am_train_proposal / am_set_proposal_weights)");
+        return AM_ERR_STATE;
+    }
+    int rc = ensure_local_index();
+    if (rc) return rc;
+    if (active.proposal == AM_PROPOSAL_LEARNED) {
+        if ((rc = mlp_init())) return rc;
+        size_t maxph = 0;
+        for (auto &p : phases_for(K)) maxph = std::max(maxph, p.size());
+        if ((rc = d_cost_cache.reserve(N * maxph))) return rc;
+    }
+    if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * sweeps + 4)))) return rc;
+    AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * sweeps * 8, stream));
+    auto ph = phases_for(K);
+    for (size_t s = 0; s < sweeps; ++s) {
+        uint32_t pofs = 0;
+        for (size_t p = 0; p < ph.size(); ++p) {
+            LocalArgs a;
+            a.P = d_P.p; a.N = N; a.K = K; a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
+            a.slot_pt = lix.slot_pt; a.col = lix.col; a.slot_of = lix.slot_of; a.cell_start = lix.cell_start;
+            a.ncx = lix.ncx; a.ncy = lix.ncy; a.ncells = lix.ncells; a.chain_id = lix.chain_id;
+            a.chain_w1 = lix.chain_w1; a.cap = 16;
+            a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p ^ 0x5bd1e995ULL);
+            a.claim = d_claim.p; a.prop = d_lprop.p; a.pgain = d_pgain.p;
+            a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
+            if (active.proposal == AM_PROPOSAL_LEARNED) {
+                a.mlp = d_mlp_dep.p; a.cost_cache = d_cost_cache.p; a.display = d_display.p;
+                a.CW = CW; a.CH = CH; a.topk = 2; a.err = d_err.p;
+                if (recording) {
+                    a.rec_feat = d_rec_feat.p; a.rec_gain = d_rec_gain.p; a.rec_count = d_rec_count.p;
+                    a.rec_cap = rec_cap;
+                }
+            }
+            prof.open(stream);
+            if (active.proposal == AM_PROPOSAL_LEARNED) rc = launch_learned_phase(a, stream);
+            else rc = launch_local_phase(a, stream);
+            if (rc) return rc;
+            prof.close(active.proposal == AM_PROPOSAL_LEARNED ? PROF_MLP : PROF_SWEEP_LOCAL, stream);
+            pofs += (uint32_t)ph[p].size();
+        }
+        ++sweep_counter;
+    }
+    std::vector<unsigned long long> acc(2 * sweeps);
+    AMG_CUDA(cudaMemcpyAsync(acc.data(), d_acc.p + 4, acc.size() * 8, cudaMemcpyDeviceToHost, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    for (size_t s = 0; s < sweeps; ++s) {
+        cost_exact -= acc[2 * s];
+        if (gains) gains[s] = acc[2 * s];
+    }
+    return AM_OK;
 }
 
 }  // namespace amg

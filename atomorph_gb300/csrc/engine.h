@@ -148,6 +148,15 @@ class Engine {
     DBuf<uint32_t> d_sorted, d_keys, d_tk, d_tv, d_hist, d_bstart, d_bsize, d_volxy;
     DBuf<int32_t> d_blob_of;
     DBuf<uint8_t> d_frame;                 // host-output staging frame
+    // guided refinement index (valid while only guided sweeps touch P)
+    LocalIndex lix;
+    bool local_valid = false;
+    DBuf<uint64_t> d_slot_pt;
+    DBuf<uint32_t> d_col, d_slot_of, d_cell_start, d_chain_id, d_lprop, d_lk, d_lv;
+    DBuf<uint8_t> d_chain_w1;
+    DBuf<unsigned long long> d_claim, d_pgain;
+    int ensure_local_index();
+
     Prof prof;
     RenderWork *rw = nullptr;
     BlobWork *bw = nullptr;
@@ -172,6 +181,25 @@ class Engine {
     int copy_keyframe(size_t f, uint8_t *dst);
     unsigned active_seed_mix() const;
     int status = AM_OK;                    // first failure inside the worker
+    bool mlp_ready() const { return mlp_trained || recording; }
+    bool mlp_trained = false;
+
+    // proposal network (engine_mlp.cpp)
+    DBuf<float> d_mlp_master, d_mlp_dep, d_mlp_grad, d_adam_m, d_adam_v, d_mlp_loss, d_rec_feat, d_rec_gain;
+    DBuf<float> d_io_a, d_io_b;
+    DBuf<unsigned long long> d_rec_count, d_cost_cache;
+    DBuf<int> d_err;
+    uint64_t rec_cap = 0, adam_t = 0;
+    bool recording = false;
+    int mlp_init();
+    int record_swaps(size_t cap);
+    size_t recorded_swaps(float *feat, float *gains, size_t cap);
+    int train_proposal(const float *feat, const float *gains, size_t n, size_t epochs, double lr, float *loss_out);
+    int proposal_weights(float *w, size_t count, bool set);
+    int proposal_forward(const float *feat, size_t n, float *out);
+    int proposal_grad(const float *feat, const float *target, size_t n, float *grad, float *loss);
+    int check_err();
+    int ensure_streams_public();
 
   private:
     void run();

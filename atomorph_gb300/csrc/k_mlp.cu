@@ -1,0 +1,701 @@
+// The learned swap proposal: a 10 -> 64 -> 64 -> 1 ReLU network with BF16
+// weights and FP32 accumulation, run and trained on the 5th-generation tensor
+// cores (tcgen05.mma, accumulators in tensor memory) from hand-written PTX.
+//
+// Operands live in shared memory in the canonical no-swizzle K-major layout:
+// 8x16-byte core matrices, the byte offset of element (r, k) being
+//   (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2
+// (LBO = 128 B between core matrices along K, SBO between 8-row groups).
+// One elected thread issues the MMAs; tcgen05.commit arrives on an mbarrier
+// every thread waits on with a bounded number of tries (a failed wait sets
+// the error flag instead of spinning); each warp reads its own 32 TMEM lanes
+// with tcgen05.ld.
+//
+// Features of a candidate pair (column x1 at key frame y, candidate column x2
+// holding point a2), S = 16 px in 1/256 units:
+//   0,1  (a2 - m1) / S, m1 = midpoint of x1's points at the neighbouring frames
+//   2-5  (colour(a2) - colour(a1)) / 255, RGBA of the key frame's pixels
+//   6,7  log1p(cost of column x1 / S^2), same for column x2
+//   8    parity of the chain (blob group) id
+//   9    log1p(|a1 - a2|^2 / S^2)
+// Target: sign(g) * log1p(|g| / S^2) with g the exact swap gain.
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace amg {
+namespace {
+
+constexpr float kS = 4096.f;             // 16 px in 1/256 px
+constexpr float kS2 = 4096.f * 4096.f;
+constexpr int kTM = 128;                 // rows per MMA tile
+// deployed layout offsets (floats)
+constexpr int kOffW1 = 0, kOffW2 = 512, kOffB1 = 2560, kOffB2 = 2624, kOffW3 = 2688, kOffB3 = 2752;
+// master layout offsets (floats)
+constexpr int kMW1 = 0, kMB1 = 640, kMW2 = 704, kMB2 = 4800, kMW3 = 4864, kMB3 = 4928;
+
+// ------------------------------------------------------------------ PTX ---
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t make_desc(const void *base, uint32_t sbo) {
+    uint32_t a = smem_u32(base);
+    return (uint64_t)((a >> 4) & 0x3FFFu) | ((uint64_t)((128u >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t M, uint32_t N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+__device__ __forceinline__ int kmaj(int r, int k, int sbo) {
+    return (r >> 3) * sbo + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+__device__ __forceinline__ void put_bf16(uint8_t *base, int off, float v) {
+    *reinterpret_cast<__nv_bfloat16 *>(base + off) = __float2bfloat16_rn(v);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Bounded wait: gives up after ~1M tries and flags the error.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+    for (uint32_t it = 0; it < (1u << 20); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    if (err) atomicExch(err, 1);
+    return false;
+}
+// 16 consecutive fp32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Loads W1 (B operand [64][16]) and W2 (B operand [64][64]) from the deployed
+// parameters into shared memory; W2T ([i][o]) too when wanted.
+__device__ void load_weights(const float *dep, uint8_t *B1, uint8_t *B2, uint8_t *B2T) {
+    const __nv_bfloat16 *w1 = reinterpret_cast<const __nv_bfloat16 *>(dep + kOffW1);
+    const __nv_bfloat16 *w2 = reinterpret_cast<const __nv_bfloat16 *>(dep + kOffW2);
+    for (int e = threadIdx.x; e < 64 * 16; e += blockDim.x) {
+        int n = e >> 4, k = e & 15;
+        *reinterpret_cast<__nv_bfloat16 *>(B1 + kmaj(n, k, 256)) = w1[e];
+    }
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+        int o = e >> 6, i = e & 63;
+        *reinterpret_cast<__nv_bfloat16 *>(B2 + kmaj(o, i, 1024)) = w2[e];
+        if (B2T) *reinterpret_cast<__nv_bfloat16 *>(B2T + kmaj(i, o, 1024)) = w2[e];
+    }
+}
+
+struct FwdSmem {
+    uint8_t A1[kTM * 16 * 2];   // features [128][16]
+    uint8_t A2[kTM * 64 * 2];   // hidden 1 [128][64]
+    uint8_t B1[64 * 16 * 2];
+    uint8_t B2[64 * 64 * 2];
+    float b1[64], b2[64], w3[64];
+    float b3;
+    uint64_t bar;
+    uint32_t tmem;
+};
+
+// Forward of one 128-row tile whose features are in s.A1: returns this
+// thread's score (row = threadIdx.x).  Whole CTA of 128 threads.
+__device__ float forward_tile(FwdSmem &s, uint32_t &phase, int *err) {
+    const int warp = threadIdx.x >> 5;
+    const uint32_t lane_base = s.tmem + ((uint32_t)(32 * warp) << 16);
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        fence_after();
+        mma(s.tmem, make_desc(s.A1, 256), make_desc(s.B1, 256), idesc_bf16(128, 64), 0);
+        mma_commit(&s.bar);
+    }
+    bool ok = mbar_wait(&s.bar, phase, err);
+    phase ^= 1;
+    fence_after();
+    float v[16];
+    const int r = threadIdx.x;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        tmem_ld16(lane_base + 16 * c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            int i = 16 * c + j;
+            float h = ok ? fmaxf(v[j] + s.b1[i], 0.f) : 0.f;
+            put_bf16(s.A2, kmaj(r, i, 1024), h);
+        }
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        fence_after();
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            mma(s.tmem + 64, make_desc(s.A2 + 256 * k, 1024), make_desc(s.B2 + 256 * k, 1024), idesc_bf16(128, 64),
+                k > 0);
+        mma_commit(&s.bar);
+    }
+    ok = mbar_wait(&s.bar, phase, err) && ok;
+    phase ^= 1;
+    fence_after();
+    float out = s.b3;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        tmem_ld16(lane_base + 64 + 16 * c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            int i = 16 * c + j;
+            out += fmaxf(v[j] + s.b2[i], 0.f) * s.w3[i];
+        }
+    }
+    fence_before();
+    return ok ? out : 0.f;
+}
+
+__device__ void fwd_setup(FwdSmem &s, const float *dep) {
+    load_weights(dep, s.B1, s.B2, nullptr);
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+        s.b1[i] = dep[kOffB1 + i];
+        s.b2[i] = dep[kOffB2 + i];
+        s.w3[i] = dep[kOffW3 + i];
+    }
+    if (threadIdx.x == 0) {
+        s.b3 = dep[kOffB3];
+        mbar_init(&s.bar);
+    }
+    if (threadIdx.x < 32) tmem_alloc(&s.tmem, 128);
+    fence_before();
+    __syncthreads();
+    fence_after();
+}
+__device__ void fwd_teardown(FwdSmem &s) {
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (threadIdx.x < 32) tmem_dealloc(s.tmem, 128);
+}
+
+__device__ __forceinline__ void write_features(uint8_t *A1, int r, const float *f) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) put_bf16(A1, kmaj(r, k, 256), k < kMlpIn ? f[k] : 0.f);
+}
+
+// ------------------------------------------------------- forward kernel --
+__global__ void __launch_bounds__(128) k_mlp_forward(const float *__restrict__ feat, uint64_t n,
+                                                     const float *__restrict__ dep, float *out, int *err) {
+    extern __shared__ __align__(1024) uint8_t smraw[];
+    FwdSmem &s = *reinterpret_cast<FwdSmem *>(smraw);
+    fwd_setup(s, dep);
+    uint32_t phase = 0;
+    for (uint64_t base = (uint64_t)blockIdx.x * kTM; base < n; base += (uint64_t)gridDim.x * kTM) {
+        uint64_t row = base + threadIdx.x;
+        float f[kMlpIn];
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) f[k] = row < n ? feat[row * kMlpIn + k] : 0.f;
+        write_features(s.A1, threadIdx.x, f);
+        float o = forward_tile(s, phase, err);
+        if (row < n) out[row] = o;
+    }
+    fwd_teardown(s);
+}
+
+// ----------------------------------------------------- training kernel ---
+struct TrainSmem {
+    uint8_t A1[kTM * 16 * 2];        // X [b][16]
+    uint8_t A2[kTM * 64 * 2];        // H1 [b][64]
+    uint8_t G2[kTM * 64 * 2];        // dZ2 [b][64]
+    uint8_t G2T[kTM * kTM * 2];      // dZ2^T [o pad 128][b 128]
+    uint8_t H1T[64 * kTM * 2];       // H1^T [i 64][b 128]
+    uint8_t G1T[kTM * kTM * 2];      // dZ1^T [o pad 128][b 128]
+    uint8_t XT[16 * kTM * 2];        // X^T [i 16][b 128]
+    uint8_t B1[64 * 16 * 2];
+    uint8_t B2[64 * 64 * 2];
+    uint8_t B2T[64 * 64 * 2];
+    float b1[64], b2[64], w3[64];
+    float gb1[64], gb2[64], gw3[64];
+    float b3, gb3, loss;
+    uint64_t bar;
+    uint32_t tmem;
+};
+
+__global__ void __launch_bounds__(128) k_mlp_train(const float *__restrict__ feat, const float *__restrict__ target,
+                                                   uint64_t n, const float *__restrict__ dep, float *grad,
+                                                   float *loss_sum, int *err) {
+    extern __shared__ __align__(1024) uint8_t smraw[];
+    TrainSmem &s = *reinterpret_cast<TrainSmem *>(smraw);
+    const int r = threadIdx.x, warp = r >> 5;
+    load_weights(dep, s.B1, s.B2, s.B2T);
+    for (int i = r; i < 64; i += 128) {
+        s.b1[i] = dep[kOffB1 + i]; s.b2[i] = dep[kOffB2 + i]; s.w3[i] = dep[kOffW3 + i];
+        s.gb1[i] = 0.f; s.gb2[i] = 0.f; s.gw3[i] = 0.f;
+    }
+    // Padding rows 64..127 of the transposed gradient operands stay zero.
+    for (int e = r; e < kTM * kTM; e += 128) {
+        int o = e / kTM, b = e % kTM;
+        if (o >= 64) { put_bf16(s.G2T, kmaj(o, b, 2048), 0.f); put_bf16(s.G1T, kmaj(o, b, 2048), 0.f); }
+    }
+    if (r == 0) { s.b3 = dep[kOffB3]; s.gb3 = 0.f; s.loss = 0.f; mbar_init(&s.bar); }
+    if (r < 32) tmem_alloc(&s.tmem, 256);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t lb = s.tmem + ((uint32_t)(32 * warp) << 16);
+    const uint32_t tD1 = s.tmem, tD2 = s.tmem + 64, tW2 = s.tmem + 128, tW1 = s.tmem + 192;
+    uint32_t phase = 0;
+    const float inv_n = 1.f / (float)n;
+    int tiles = 0;
+    bool ok = true;
+    for (uint64_t base = (uint64_t)blockIdx.x * kTM; base < n; base += (uint64_t)gridDim.x * kTM, ++tiles) {
+        uint64_t row = base + r;
+        bool valid = row < n;
+        float f[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            float x = (valid && k < kMlpIn) ? feat[row * kMlpIn + k] : 0.f;
+            f[k] = x;
+            put_bf16(s.A1, kmaj(r, k, 256), x);
+            put_bf16(s.XT, kmaj(k, r, 2048), x);
+        }
+        float tgt = valid ? target[row] : 0.f;
+        // layer 1
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (r == 0) {
+            fence_after();
+            mma(tD1, make_desc(s.A1, 256), make_desc(s.B1, 256), idesc_bf16(128, 64), 0);
+            mma_commit(&s.bar);
+        }
+        ok = mbar_wait(&s.bar, phase, err) && ok;
+        phase ^= 1;
+        fence_after();
+        uint32_t act1[2] = {0u, 0u};
+        float v[16];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tmem_ld16(lb + tD1 - s.tmem + 16 * c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                int i = 16 * c + j;
+                float z = v[j] + s.b1[i];
+                float h = (valid && z > 0.f) ? z : 0.f;
+                if (z > 0.f) act1[i >> 5] |= 1u << (i & 31);
+                put_bf16(s.A2, kmaj(r, i, 1024), h);
+                put_bf16(s.H1T, kmaj(i, r, 2048), h);
+            }
+        }
+        // layer 2
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (r == 0) {
+            fence_after();
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                mma(tD2, make_desc(s.A2 + 256 * k, 1024), make_desc(s.B2 + 256 * k, 1024), idesc_bf16(128, 64), k > 0);
+            mma_commit(&s.bar);
+        }
+        ok = mbar_wait(&s.bar, phase, err) && ok;
+        phase ^= 1;
+        fence_after();
+        float z2[64];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tmem_ld16(lb + 64 + 16 * c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) z2[16 * c + j] = v[j] + s.b2[16 * c + j];
+        }
+        float out = s.b3;
+#pragma unroll
+        for (int i = 0; i < 64; ++i) out += fmaxf(z2[i], 0.f) * s.w3[i];
+        float e = valid ? out - tgt : 0.f;
+        float dout = 2.f * e * inv_n;
+        atomicAdd(&s.loss, e * e);
+        atomicAdd(&s.gb3, dout);
+#pragma unroll
+        for (int i = 0; i < 64; ++i) {
+            float h2 = fmaxf(z2[i], 0.f);
+            float g = z2[i] > 0.f ? dout * s.w3[i] : 0.f;
+            if (h2 != 0.f) atomicAdd(&s.gw3[i], dout * h2);
+            if (g != 0.f) atomicAdd(&s.gb2[i], g);
+            put_bf16(s.G2, kmaj(r, i, 1024), g);
+            put_bf16(s.G2T, kmaj(i, r, 2048), g);
+        }
+        // dH1 = dZ2 W2  and  dW2 += dZ2^T H1
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (r == 0) {
+            fence_after();
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                mma(tD1, make_desc(s.G2 + 256 * k, 1024), make_desc(s.B2T + 256 * k, 1024), idesc_bf16(128, 64),
+                    k > 0);
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                mma(tW2, make_desc(s.G2T + 256 * k, 2048), make_desc(s.H1T + 256 * k, 2048), idesc_bf16(128, 64),
+                    (tiles > 0 || k > 0) ? 1u : 0u);
+            mma_commit(&s.bar);
+        }
+        ok = mbar_wait(&s.bar, phase, err) && ok;
+        phase ^= 1;
+        fence_after();
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tmem_ld16(lb + 16 * c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                int i = 16 * c + j;
+                float g = (act1[i >> 5] >> (i & 31)) & 1u ? v[j] : 0.f;
+                if (!valid) g = 0.f;
+                if (g != 0.f) atomicAdd(&s.gb1[i], g);
+                put_bf16(s.G1T, kmaj(i, r, 2048), g);
+            }
+        }
+        // dW1 += dZ1^T X
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (r == 0) {
+            fence_after();
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                mma(tW1, make_desc(s.G1T + 256 * k, 2048), make_desc(s.XT + 256 * k, 2048), idesc_bf16(128, 16),
+                    (tiles > 0 || k > 0) ? 1u : 0u);
+            mma_commit(&s.bar);
+        }
+        ok = mbar_wait(&s.bar, phase, err) && ok;
+        phase ^= 1;
+        fence_after();
+    }
+    // Reduce the accumulated weight gradients (rows 0..63 live in warps 0-1).
+    fence_before();
+    __syncthreads();
+    fence_after();
+    ok = __all_sync(0xffffffffu, ok);
+    if (tiles > 0 && warp < 2 && ok) {
+        float v[16];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            tmem_ld16(lb + 128 + 16 * c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) atomicAdd(grad + kMW2 + r * 64 + 16 * c + j, v[j]);
+        }
+        tmem_ld16(lb + 192, v);
+#pragma unroll
+        for (int j = 0; j < kMlpIn; ++j) atomicAdd(grad + kMW1 + r * kMlpIn + j, v[j]);
+    }
+    __syncthreads();
+    if (r < 64) {
+        atomicAdd(grad + kMB1 + r, s.gb1[r]);
+        atomicAdd(grad + kMB2 + r, s.gb2[r]);
+        atomicAdd(grad + kMW3 + r, s.gw3[r]);
+    }
+    if (r == 0) {
+        atomicAdd(grad + kMB3, s.gb3);
+        if (loss_sum) atomicAdd(loss_sum, s.loss);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (r < 32) tmem_dealloc(s.tmem, 256);
+}
+
+__global__ void k_mlp_deploy(const float *__restrict__ m, float *dep) {
+    __nv_bfloat16 *w1 = reinterpret_cast<__nv_bfloat16 *>(dep + kOffW1);
+    __nv_bfloat16 *w2 = reinterpret_cast<__nv_bfloat16 *>(dep + kOffW2);
+    for (int e = threadIdx.x; e < 64 * 16; e += blockDim.x) {
+        int o = e >> 4, i = e & 15;
+        w1[e] = __float2bfloat16_rn(i < kMlpIn ? m[kMW1 + o * kMlpIn + i] : 0.f);
+    }
+    for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) w2[e] = __float2bfloat16_rn(m[kMW2 + e]);
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+        dep[kOffB1 + i] = m[kMB1 + i];
+        dep[kOffB2 + i] = m[kMB2 + i];
+        dep[kOffW3 + i] = m[kMW3 + i];
+    }
+    if (threadIdx.x == 0) dep[kOffB3] = m[kMB3];
+}
+
+__global__ void k_adam(float *p, const float *g, float *m, float *v, int n, float lr, float c1, float c2) {
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float gi = g[i];
+        m[i] = b1 * m[i] + (1.f - b1) * gi;
+        v[i] = b2 * v[i] + (1.f - b2) * gi * gi;
+        p[i] -= lr * (m[i] / c1) / (sqrtf(v[i] / c2) + eps);
+    }
+}
+
+// ----------------------------------------------- learned proposal kernel --
+__global__ void __launch_bounds__(256) k_cost_cache(LocalArgs a) {
+    const uint64_t N = a.N, total = N * a.nframes;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t fi = (uint32_t)(t / N);
+        uint64_t x = t - (uint64_t)fi * N;
+        uint32_t y = a.frames[fi];
+        uint32_t yn = y + 1 == a.K ? 0 : y + 1, yp = y == 0 ? a.K - 1 : y - 1;
+        uint64_t p = a.P[(uint64_t)yp * N + x], c = a.P[(uint64_t)y * N + x], q = a.P[(uint64_t)yn * N + x];
+        a.cost_cache[t] = pt_dist(p, c) + pt_dist(c, q);
+    }
+}
+
+__device__ __forceinline__ float slog1p(float x) { return x >= 0.f ? log1pf(x) : -log1pf(-x); }
+
+struct PropSmem {
+    FwdSmem f;
+};
+
+// One warp per column, 32 candidates per column from the 3x3 cells around
+// the column's target; 4 columns = one 128-row MMA tile.
+__global__ void __launch_bounds__(128) k_learned_propose(LocalArgs a) {
+    extern __shared__ __align__(1024) uint8_t smraw[];
+    PropSmem &s = *reinterpret_cast<PropSmem *>(smraw);
+    fwd_setup(s.f, a.mlp);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t N = a.N, total = N * a.nframes;
+    const uint64_t ntiles = (total + 3) / 4;
+    uint32_t phase = 0;
+    const size_t fr = (size_t)a.CW * a.CH;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint64_t t = tile * 4 + warp;
+        bool colok = t < total;
+        uint32_t fi = 0, x1 = 0, y = 0, yp = 0, yn = 0, c = 0;
+        uint64_t a1 = 0, p1 = 0, n1 = 0;
+        bool cand = false;
+        uint32_t x2 = 0xFFFFFFFFu, s2 = 0;
+        float feats[kMlpIn];
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) feats[k] = 0.f;
+        if (colok) {
+            fi = (uint32_t)(t / N);
+            x1 = (uint32_t)(t - (uint64_t)fi * N);
+            y = a.frames[fi];
+            yn = y + 1 == a.K ? 0 : y + 1;
+            yp = y == 0 ? a.K - 1 : y - 1;
+            c = a.chain_id[x1];
+            if (lane == 0) a.prop[t] = 0xFFFFFFFFu;
+            if (!a.chain_w1[c]) {
+                a1 = a.P[(uint64_t)y * N + x1];
+                p1 = a.P[(uint64_t)yp * N + x1];
+                n1 = a.P[(uint64_t)yn * N + x1];
+                int32_t mx = (pt_X(p1) + pt_X(n1)) >> 1, my = (pt_Y(p1) + pt_Y(n1)) >> 1;
+                int cx = (int)min((uint32_t)max(mx, 0) >> 9, a.ncx - 1);
+                int cy = (int)min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
+                const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
+                // cell k of the 3x3 window, centre first
+                uint32_t beg = 0, cnt = 0;
+                if (lane < 9) {
+                    int kk = lane == 0 ? 4 : (lane <= 4 ? lane - 1 : lane);
+                    int qx = cx + (kk % 3) - 1, qy = cy + (kk / 3) - 1;
+                    if (qx >= 0 && qy >= 0 && qx < (int)a.ncx && qy < (int)a.ncy) {
+                        uint32_t cell = (uint32_t)qy * a.ncx + (uint32_t)qx;
+                        beg = cs[cell];
+                        cnt = cs[cell + 1] - beg;
+                    }
+                }
+                // inclusive prefix of the counts over lanes 0..8
+                uint32_t pre = cnt;
+#pragma unroll
+                for (int o = 1; o < 16; o <<= 1) {
+                    uint32_t u = __shfl_up_sync(0xffffffffu, pre, o);
+                    if (lane >= o) pre += u;
+                }
+                // candidate `lane`: first cell whose inclusive prefix exceeds it
+                uint32_t my_cell = 9;
+                for (int k = 8; k >= 0; --k) {
+                    uint32_t pk = __shfl_sync(0xffffffffu, pre, k);
+                    if ((uint32_t)lane < pk) my_cell = (uint32_t)k;
+                }
+                uint32_t bk = __shfl_sync(0xffffffffu, beg, my_cell < 9 ? my_cell : 0);
+                bool has_prev = my_cell > 0 && my_cell < 9;
+                uint32_t pk_raw = __shfl_sync(0xffffffffu, pre, has_prev ? my_cell - 1 : 0);
+                uint32_t pk_prev = has_prev ? pk_raw : 0u;
+                if (my_cell < 9) {
+                    s2 = bk + ((uint32_t)lane - pk_prev);
+                    x2 = a.col[(uint64_t)y * N + s2];
+                    cand = x2 != x1 && a.chain_id[x2] == c;
+                }
+                if (cand) {
+                    uint64_t a2 = a.slot_pt[(uint64_t)y * N + s2];
+                    uint32_t col1 = a.display[(size_t)y * fr + (size_t)pt_y(a1) * a.CW + pt_x(a1)];
+                    uint32_t col2 = a.display[(size_t)y * fr + (size_t)pt_y(a2) * a.CW + pt_x(a2)];
+                    float c1 = (float)a.cost_cache[(uint64_t)fi * N + x1];
+                    float c2 = (float)a.cost_cache[(uint64_t)fi * N + x2];
+                    feats[0] = fminf(fmaxf((float)(pt_X(a2) - mx) / kS, -8.f), 8.f);
+                    feats[1] = fminf(fmaxf((float)(pt_Y(a2) - my) / kS, -8.f), 8.f);
+#pragma unroll
+                    for (int ch = 0; ch < 4; ++ch)
+                        feats[2 + ch] = ((float)((col2 >> (8 * ch)) & 255u) - (float)((col1 >> (8 * ch)) & 255u)) / 255.f;
+                    feats[6] = log1pf(c1 / kS2);
+                    feats[7] = log1pf(c2 / kS2);
+                    feats[8] = (float)(c & 1u);
+                    feats[9] = log1pf((float)pt_dist(a1, a2) / kS2);
+                }
+            }
+        }
+        write_features(s.f.A1, threadIdx.x, feats);
+        float score = forward_tile(s.f, phase, a.err);
+        if (!cand) score = -INFINITY;
+        // Optional sample log: exact gain of every candidate.
+        if (a.rec_count && cand) {
+            int64_t g = 0;
+            {
+                uint64_t a2 = a.slot_pt[(uint64_t)y * N + s2];
+                uint64_t p2 = a.P[(uint64_t)yp * N + x2], n2 = a.P[(uint64_t)yn * N + x2];
+                uint64_t cc1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
+                uint64_t cc2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);
+                g = (int64_t)cc1 - (int64_t)cc2;
+            }
+            unsigned long long slot = atomicAdd(a.rec_count, 1ull);
+            if (slot < a.rec_cap) {
+#pragma unroll
+                for (int k = 0; k < kMlpIn; ++k) a.rec_feat[slot * kMlpIn + k] = feats[k];
+                a.rec_gain[slot] = slog1p((float)g / kS2);
+            }
+        }
+        // Top-k by score, then the exact criterion decides.
+        int64_t best = 0;
+        uint32_t bx = 0xFFFFFFFFu;
+        float sc = score;
+        for (uint32_t k = 0; k < a.topk; ++k) {
+            float m = sc;
+            int ml = lane;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                float om = __shfl_xor_sync(0xffffffffu, m, o);
+                int ol = __shfl_xor_sync(0xffffffffu, ml, o);
+                if (om > m || (om == m && ol < ml)) { m = om; ml = ol; }
+            }
+            if (m == -INFINITY) break;
+            int64_t g = 0;
+            if (lane == ml) {
+                uint64_t a2 = a.slot_pt[(uint64_t)y * N + s2];
+                uint64_t p2 = a.P[(uint64_t)yp * N + x2], n2 = a.P[(uint64_t)yn * N + x2];
+                uint64_t cc1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
+                uint64_t cc2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);
+                g = (int64_t)cc1 - (int64_t)cc2;
+                sc = -INFINITY;
+            }
+            g = __shfl_sync(0xffffffffu, g, ml);
+            uint32_t gx = __shfl_sync(0xffffffffu, x2, ml);
+            if (g > best) { best = g; bx = gx; }
+        }
+        if (colok && lane == 0 && bx != 0xFFFFFFFFu) {
+            float gf = (float)best;
+            unsigned long long k = ((unsigned long long)__float_as_uint(gf) << 32) | x1;
+            a.prop[t] = bx;
+            a.pgain[t] = (unsigned long long)best;
+            atomicMax(a.claim + (uint64_t)fi * N + x1, k);
+            atomicMax(a.claim + (uint64_t)fi * N + bx, k);
+        }
+    }
+    fwd_teardown(s.f);
+}
+
+}  // namespace
+
+static int set_smem(const void *fn, size_t bytes) {
+    AMG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return AM_OK;
+}
+
+int mlp_deploy(const float *master, float *deployed, cudaStream_t s) {
+    AMG_LAUNCH(k_mlp_deploy, 1, 256, 0, s, master, deployed);
+    AMG_CUDA(cudaGetLastError());
+    return AM_OK;
+}
+
+int mlp_forward(const float *feat, uint64_t n, const float *deployed, float *out, int *err, cudaStream_t s) {
+    if (!n) return AM_OK;
+    // >= 56 KB of shared memory keeps at most 4 CTAs (4 x 128 TMEM columns) per SM.
+    size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 56 * 1024);
+    int rc = set_smem((const void *)k_mlp_forward, smem);
+    if (rc) return rc;
+    unsigned grid = (unsigned)std::min<uint64_t>((n + kTM - 1) / kTM, (uint64_t)kSMs * 4);
+    AMG_LAUNCH(k_mlp_forward, grid, 128, smem, s, feat, n, deployed, out, err);
+    AMG_CUDA(cudaGetLastError());
+    return AM_OK;
+}
+
+int mlp_grad(const float *feat, const float *target, uint64_t n, const float *deployed, float *grad, float *loss_sum,
+             int *err, cudaStream_t s) {
+    AMG_CUDA(cudaMemsetAsync(grad, 0, kMlpMasterParams * sizeof(float), s));
+    if (loss_sum) AMG_CUDA(cudaMemsetAsync(loss_sum, 0, sizeof(float), s));
+    if (!n) return AM_OK;
+    size_t smem = sizeof(TrainSmem) + 1024;
+    int rc = set_smem((const void *)k_mlp_train, smem);
+    if (rc) return rc;
+    unsigned grid = (unsigned)std::min<uint64_t>((n + kTM - 1) / kTM, (uint64_t)kSMs);
+    AMG_LAUNCH(k_mlp_train, grid, 128, smem, s, feat, target, n, deployed, grad, loss_sum, err);
+    AMG_CUDA(cudaGetLastError());
+    return AM_OK;
+}
+
+int mlp_train_step(const float *feat, const float *target, uint64_t n, float *master, float *deployed, float *grad,
+                   float *adam_m, float *adam_v, uint64_t t, float lr, float *loss_sum, int *err, cudaStream_t s) {
+    int rc = mlp_grad(feat, target, n, deployed, grad, loss_sum, err, s);
+    if (rc) return rc;
+    float c1 = 1.f - powf(0.9f, (float)t), c2 = 1.f - powf(0.999f, (float)t);
+    AMG_LAUNCH(k_adam, (kMlpMasterParams + 255) / 256, 256, 0, s, master, grad, adam_m, adam_v, kMlpMasterParams, lr,
+               c1, c2);
+    return mlp_deploy(master, deployed, s);
+}
+
+int launch_learned_phase(const LocalArgs &a, cudaStream_t s) {
+    uint64_t total = a.N * a.nframes;
+    if (!total) return AM_OK;
+    AMG_CUDA(cudaMemsetAsync(a.claim, 0, total * sizeof(unsigned long long), s));
+    unsigned g1 = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)kSMs * 8);
+    AMG_LAUNCH(k_cost_cache, g1, 256, 0, s, a);
+    size_t smem = std::max<size_t>(sizeof(PropSmem) + 1024, 56 * 1024);
+    int rc = set_smem((const void *)k_learned_propose, smem);
+    if (rc) return rc;
+    unsigned g2 = (unsigned)std::min<uint64_t>((total + 3) / 4, (uint64_t)kSMs * 4);
+    AMG_LAUNCH(k_learned_propose, g2, 128, smem, s, a);
+    return launch_local_apply(a, s);
+}
+
+}  // namespace amg

@@ -45,6 +45,74 @@ struct SweepArgs {
 // (thread.cpp:1014-1039).
 int launch_sweep_random(const SweepArgs &a, cudaStream_t s);
 
+// ---- k_local.cu: guided refinement (spatially local candidates)
+struct LocalIndex {
+    uint32_t ncx = 0, ncy = 0, ncells = 0;   // 2x2-pixel cells over the canvas
+    uint64_t *slot_pt = nullptr;             // [K][N] points sorted by cell (static)
+    uint32_t *col = nullptr;                 // [K][N] column holding slot s
+    uint32_t *slot_of = nullptr;             // [K][N] slot held by column x
+    uint32_t *cell_start = nullptr;          // [K][ncells+1]
+    uint32_t *chain_id = nullptr;            // [N]
+    uint8_t *chain_w1 = nullptr;             // [C] 1 for width-1 chains
+};
+struct LocalArgs {
+    uint64_t *P;
+    uint64_t N;
+    uint32_t K;
+    const uint32_t *frames;
+    uint32_t nframes;
+    const uint64_t *slot_pt;
+    uint32_t *col, *slot_of;
+    const uint32_t *cell_start;
+    uint32_t ncx, ncy, ncells;
+    const uint32_t *chain_id;
+    const uint8_t *chain_w1;
+    uint32_t cap;                            // candidates examined per cell
+    uint64_t key;                            // random key of this (sweep, phase)
+    unsigned long long *claim;               // [nframes][N]
+    uint32_t *prop;                          // [nframes][N] proposed partner
+    unsigned long long *pgain;               // [nframes][N] exact gain of the proposal
+    unsigned long long *gain, *accepted;
+    // learned proposal only
+    const float *mlp = nullptr;              // deployed network (MlpLayout)
+    unsigned long long *cost_cache = nullptr;// [nframes][N] current cost of each column
+    const uint32_t *display = nullptr;       // [K][CH][CW] key-frame colours
+    uint32_t CW = 0, CH = 0;
+    uint32_t topk = 2;                       // best-scored candidates checked exactly
+    float *rec_feat = nullptr;               // optional sample log: features [cap][10]
+    float *rec_gain = nullptr;               //   and exact gains [cap]
+    unsigned long long *rec_count = nullptr;
+    uint64_t rec_cap = 0;
+    int *err = nullptr;                      // bounded-wait failure flag
+};
+
+// ---- k_mlp.cu: the proposal network 10 -> 64 -> 64 -> 1 (ReLU)
+// Deployed layout (floats): W1 bf16 [64][16] as 512 floats, W2 bf16 [64][64]
+// as 2048 floats, b1[64], b2[64], w3[64], b3 — see MlpLayout.
+constexpr int kMlpIn = 10, kMlpHid = 64;
+constexpr int kMlpMasterParams = kMlpHid * kMlpIn + kMlpHid + kMlpHid * kMlpHid + kMlpHid + kMlpHid + 1;  // 4929
+constexpr int kMlpDeployedFloats = 512 + 2048 + 64 + 64 + 64 + 4;
+// Packs fp32 master parameters (W1[64][10], b1, W2[64][64], b2, w3, b3) into
+// the deployed bf16/fp32 layout.
+int mlp_deploy(const float *master, float *deployed, cudaStream_t s);
+// One optimisation step over n samples: forward + backward on tensor cores,
+// gradients reduced into grad (kMlpMasterParams floats), Adam on master.
+int mlp_train_step(const float *feat, const float *target, uint64_t n, float *master, float *deployed, float *grad,
+                   float *adam_m, float *adam_v, uint64_t t, float lr, float *loss_sum, int *err, cudaStream_t s);
+// Forward only (scores for n samples), for tests and the gradient check.
+int mlp_forward(const float *feat, uint64_t n, const float *deployed, float *out, int *err, cudaStream_t s);
+// Gradient of the mean squared error over n samples (no update).
+int mlp_grad(const float *feat, const float *target, uint64_t n, const float *deployed, float *grad,
+             float *loss_sum, int *err, cudaStream_t s);
+int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K, uint32_t CW, uint32_t CH,
+                      const uint64_t *chain_off, uint32_t C, uint32_t *keys, uint32_t *vals, uint32_t *tk,
+                      uint32_t *tv, uint32_t *hist, cudaStream_t s);
+int launch_local_phase(const LocalArgs &a, cudaStream_t s);
+int launch_local_apply(const LocalArgs &a, cudaStream_t s);
+// Learned proposal phase: candidates from a wider window scored by the MLP
+// on tensor cores, the best-scored ones checked exactly (k_mlp.cu).
+int launch_learned_phase(const LocalArgs &a, cudaStream_t s);
+
 // Stable LSD radix sort of (key, value) u32 pairs on the low `bits` key bits.
 // tmp buffers must hold n elements each; hist needs radix_hist_words(n).
 size_t radix_hist_words(size_t n);

@@ -162,6 +162,28 @@ int am_import_chains(am_morph *m, size_t K, size_t C, const uint64_t *widths,
  * decrease of each sweep. */
 int am_refine(am_morph *m, size_t sweeps, uint64_t *gains);
 
+/* ---- learned swap proposal (no reference counterpart; the reference only
+ * draws uniform random pairs, thread.cpp:1000-1005).  The network maps 10
+ * pair features to a score; its fp32 master parameters are exchanged as
+ * AM_PROPOSAL_PARAMS floats: W1[64][10], b1[64], W2[64][64], b2[64], w3[64], b3. */
+#define AM_PROPOSAL_FEATURES 10
+#define AM_PROPOSAL_PARAMS 4929
+/* Makes the next learned-proposal sweeps log up to cap candidate pairs: their
+ * features and target sign(g)*log1p(|g|/S^2) of the exact swap gain g. */
+int    am_record_swaps(am_morph *m, size_t cap);
+size_t am_recorded_swaps(am_morph *m, float *features, float *targets, size_t cap);
+/* Trains the network on the GPU (tensor-core forward/backward, Adam) on n
+ * samples for `epochs` passes; loss_out gets the last epoch's mean loss. */
+int    am_train_proposal(am_morph *m, const float *features, const float *targets, size_t n, size_t epochs,
+                         double lr, float *loss_out);
+int    am_get_proposal_weights(am_morph *m, float *w, size_t count);
+int    am_set_proposal_weights(am_morph *m, const float *w, size_t count);
+/* Scores of n feature rows, and the gradient of the mean squared error of n
+ * (feature, target) rows with respect to the master parameters. */
+int    am_proposal_forward(am_morph *m, const float *features, size_t n, float *scores);
+int    am_proposal_grad(am_morph *m, const float *features, const float *targets, size_t n, float *grad,
+                        float *loss_sum);
+
 /* ---- runtime (no reference counterpart) */
 void    *am_get_stream(am_morph *m);        /* cudaStream_t that renders run on */
 /* Per-kernel timing: when enabled, CUDA events are recorded on the launching

@@ -66,3 +66,38 @@ def test_refine_requires_chains(capi):
     m.load(synth.workload("ellipses64"))
     with pytest.raises(capi.AmError):
         m.refine(1)
+
+
+def test_local_proposal_invariants_and_speed(capi, oracle):
+    """Guided (spatially local) proposals keep every invariant of the plain
+    refinement and reach the plain method's 2000-sweep cost in fewer sweeps."""
+    frames = synth.workload("shapes256")
+    m = capi.Morph()
+    m.load(frames, seed=3, blob_delimiter=0, motion=capi.LINEAR, fading=capi.LINEAR)
+    assert m.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+    w, pts0, order = m.export_chains()
+    K = len(frames)
+    c0 = m.cost()
+    g = m.refine(2000, capi.PROPOSAL_RANDOM)
+    c_plain = m.cost()
+    assert c_plain == c0 - int(g.sum())
+    m.import_chains(w, pts0, order)
+    total, sweeps = 0, 0
+    while sweeps < 2000:
+        gl = m.refine(10, capi.PROPOSAL_LOCAL)
+        total += int(gl.sum())
+        sweeps += 10
+        if c0 - total <= c_plain:
+            break
+    c_local = m.cost()
+    assert c_local == c0 - total
+    _, pts, _ = m.export_chains()
+    assert _columns_are_permutations(pts0, pts, w, K)
+    assert oracle.energy(pts, w, K)[1] == c_local
+    assert c_local <= 1.005 * c_plain, (c_local, c_plain)
+    assert sweeps < 2000
+    # switching back to random sweeps after guided ones stays consistent
+    g2 = m.refine(5, capi.PROPOSAL_RANDOM)
+    assert m.cost() == c_local - int(g2.sum())
+    gl2 = m.refine(5, capi.PROPOSAL_LOCAL)
+    assert m.cost() == c_local - int(g2.sum()) - int(gl2.sum())

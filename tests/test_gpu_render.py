@@ -26,7 +26,12 @@ def test_render_matches_reference_frames(capi, case):
         got = m.render(float(t))
         worst, ndiff = _lsb(got, ref)
         assert worst <= 1, f"t={t}: {ndiff} channels differ, worst {worst}"
-        assert ndiff <= max(4, ref.size // 500), f"t={t}: {ndiff} channels differ"
+        # COSINE fading at local time 0.5 puts every fading atom exactly on a
+        # rounding tie (the ramp is cos(pi/2): +6e-17 in FP64, -4e-8 in FP32),
+        # so odd colour sums may round the other way there; elsewhere the
+        # frames agree except for rare ties.
+        tie_frame = int(g["fading"]) == 5 and abs(float(t) * int(g["K"]) % 1 - 0.5) < 1e-9
+        assert ndiff <= (ref.size // 20 if tie_frame else max(4, ref.size // 500)), f"t={t}: {ndiff} differ"
 
 
 @pytest.mark.parametrize("motion,fading,delimiter,density", [
@@ -81,4 +86,5 @@ def test_render_device_output_matches_host(capi):
     buf = torch.zeros((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
     for t in (0.2, 0.6):
         m.render_device(t, buf.data_ptr())
+        assert m.lib.am_device_sync(m.h) == capi.AM_OK  # device frames are left in flight
         assert np.array_equal(buf.cpu().numpy(), m.render(t))
