@@ -126,6 +126,20 @@ int am_set_proposal(am_morph *m, unsigned k) {
     return AM_OK;
 }
 int am_set_sweeps(am_morph *m, size_t s) { CHECK(m); H(m).front.sweeps = s; H(m).active.sweeps = s; return AM_OK; }
+int am_set_tuning(am_morph *m, const char *name, double value) {
+    CHECK(m);
+    if (!name || !(value >= 0.0) || value > 1024.0) return AM_ERR_ARG;
+    amg::Params *ps[2] = {&H(m).front, &H(m).active};
+    std::string n(name);
+    for (amg::Params *p : ps) {
+        if (n == "local_self") p->local_self = (uint32_t)value;
+        else if (n == "local_target") p->local_target = (uint32_t)value;
+        else if (n == "local_random") p->local_random = (uint32_t)value;
+        else if (n == "learned_topk") p->learned_topk = std::max<uint32_t>(1, std::min<uint32_t>(8, (uint32_t)value));
+        else return AM_ERR_ARG;
+    }
+    return AM_OK;
+}
 int am_set_motion_noise(am_morph *m, double a) {
     CHECK(m);
     if (!(a >= 0.0)) return AM_ERR_ARG;

@@ -871,13 +871,14 @@ int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
             a.P = d_P.p; a.N = N; a.K = K; a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
             a.slot_pt = lix.slot_pt; a.col = lix.col; a.slot_of = lix.slot_of; a.cell_start = lix.cell_start;
             a.ncx = lix.ncx; a.ncy = lix.ncy; a.ncells = lix.ncells; a.chain_id = lix.chain_id;
-            a.chain_w1 = lix.chain_w1; a.cap = 16;
+            a.chain_w1 = lix.chain_w1; a.cap = active.local_target;
+            a.self_cap = active.local_self; a.nrandom = active.local_random; a.chain_off = d_chain_off.p;
             a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p ^ 0x5bd1e995ULL);
             a.claim = d_claim.p; a.prop = d_lprop.p; a.pgain = d_pgain.p;
             a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
             if (active.proposal == AM_PROPOSAL_LEARNED) {
                 a.mlp = d_mlp_dep.p; a.cost_cache = d_cost_cache.p; a.display = d_display.p;
-                a.CW = CW; a.CH = CH; a.topk = 2; a.err = d_err.p;
+                a.CW = CW; a.CH = CH; a.topk = active.learned_topk; a.err = d_err.p;
                 if (recording) {
                     a.rec_feat = d_rec_feat.p; a.rec_gain = d_rec_gain.p; a.rec_count = d_rec_count.p;
                     a.rec_cap = rec_cap;

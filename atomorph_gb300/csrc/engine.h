@@ -30,6 +30,8 @@ struct Params {  // defaults of morph.h:97-119
     unsigned motion = AM_SPLINE, fading = AM_PERLIN;
     unsigned proposal = AM_PROPOSAL_RANDOM;
     size_t sweeps = 1;
+    // guided-refinement tunables (am_set_tuning; chosen by the autotuner)
+    uint32_t local_self = 12, local_target = 8, local_random = 2, learned_topk = 2;
     double motion_noise = 0.0;
 };
 

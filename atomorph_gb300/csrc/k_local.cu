@@ -12,7 +12,8 @@
 //   slot_of[y][x]   slot currently held by column x
 // A column x1 at frame y costs d(p1,a1)+d(a1,n1) with p1/n1 its points at the
 // neighbouring frames; it is cheapest where its point sits at m1 = (p1+n1)/2.
-// Candidates are the columns holding points in the cell of m1; every
+// Candidates come from the column's own neighbourhood, the cell of m1 and a
+// few uniform random columns (k_local_propose); every
 // candidate's gain is the reference's exact six-point criterion
 // (thread.cpp:1014-1022) in integers.  Each column proposes its best strictly
 // improving partner and claims both columns with atomicMax on
@@ -75,6 +76,34 @@ __device__ __forceinline__ unsigned long long claim_key(int64_t gain, uint32_t x
     return ((unsigned long long)__float_as_uint(g) << 32) | x1;
 }
 
+// Scans up to `cap` slots of cell (qx, qy) starting at a hashed offset and
+// keeps the best strictly improving partner.
+__device__ __forceinline__ void scan_cell(const LocalArgs &a, const uint32_t *cs, const uint64_t *spt,
+                                          const uint32_t *col, const uint64_t *Pp, const uint64_t *Pn, int qx, int qy,
+                                          uint32_t cap, uint32_t h, uint32_t x1, uint32_t c, uint64_t p1,
+                                          uint64_t a1, uint64_t n1, int64_t &best, uint32_t &bx) {
+    if (qx < 0 || qy < 0 || qx >= (int)a.ncx || qy >= (int)a.ncy || cap == 0) return;
+    uint32_t cell = (uint32_t)qy * a.ncx + (uint32_t)qx;
+    uint32_t beg = cs[cell], n = cs[cell + 1] - beg;
+    if (n == 0) return;
+    uint32_t take = min(n, cap), start = n > cap ? h % n : 0;
+    for (uint32_t j = 0; j < take; ++j) {
+        uint32_t s = beg + (start + j) % n;
+        uint32_t x2 = col[s];
+        if (x2 == x1 || a.chain_id[x2] != c) continue;
+        int64_t g = swap_gain(p1, a1, n1, Pp[x2], spt[s], Pn[x2]);
+        if (g > best) { best = g; bx = x2; }
+    }
+}
+
+// Candidates of column x1 at frame y, all checked with the exact criterion:
+//   * the column's own neighbourhood (the cell of its point a1 and the four
+//     cells around it): resolves the local crossings left after the coarse
+//     transport is right, which uniform pairs almost never sample at large N;
+//   * the cell of its target m1: moves a column straight to where its
+//     neighbours in the other key frames pull it;
+//   * a few uniform random columns of the same chain: the reference's own
+//     proposal, for the coarse, long-range part.
 __global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
     const uint64_t N = a.N;
     const uint64_t total = N * a.nframes;
@@ -88,35 +117,40 @@ __global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
         uint32_t c = a.chain_id[x1];
         if (a.chain_w1[c]) continue;  // width-1 chains do not refine (thread.cpp:1045)
         uint64_t a1 = Py[x1], p1 = Pp[x1], n1 = Pn[x1];
-        int32_t mx = (pt_X(p1) + pt_X(n1)) >> 1, my = (pt_Y(p1) + pt_Y(n1)) >> 1;
-        uint32_t cx = min((uint32_t)max(mx, 0) >> 9, a.ncx - 1), cy = min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
         const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
         const uint64_t *spt = a.slot_pt + (uint64_t)y * N;
         const uint32_t *col = a.col + (uint64_t)y * N;
         int64_t best = 0;
         uint32_t bx = 0xFFFFFFFFu;
-        // The target cell, then (when it holds fewer than the cap) one
-        // neighbouring cell chosen by a counter hash.
         uint32_t h = mix32((uint32_t)a.key ^ mix32(x1 * 0x9E3779B1u + y));
-        for (int pass = 0; pass < 2; ++pass) {
-            uint32_t qx = cx, qy = cy;
-            if (pass == 1) {
-                int dx = (int)(h % 3u) - 1, dy = (int)((h / 3u) % 3u) - 1;
-                if (dx == 0 && dy == 0) dx = 1;
-                qx = (uint32_t)min(max((int)cx + dx, 0), (int)a.ncx - 1);
-                qy = (uint32_t)min(max((int)cy + dy, 0), (int)a.ncy - 1);
+        // own neighbourhood: centre cell, then the 4-neighbour cells
+        int ax = (int)min((uint32_t)pt_X(a1) >> 9, a.ncx - 1), ay = (int)min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1);
+        if (a.self_cap) {
+            uint32_t per = max(1u, a.self_cap / 3u);
+            scan_cell(a, cs, spt, col, Pp, Pn, ax, ay, per, h, x1, c, p1, a1, n1, best, bx);
+            const int dx4[4] = {1, -1, 0, 0}, dy4[4] = {0, 0, 1, -1};
+            uint32_t r0 = h >> 28;
+            for (int k = 0; k < 2; ++k) {
+                int d = (int)((r0 + 2u * k) & 3u);
+                scan_cell(a, cs, spt, col, Pp, Pn, ax + dx4[d], ay + dy4[d], per, h >> 3, x1, c, p1, a1, n1, best, bx);
             }
-            uint32_t cell = qy * a.ncx + qx;
-            uint32_t beg = cs[cell], end = cs[cell + 1];
-            uint32_t n = end - beg;
-            if (n == 0) continue;
-            uint32_t take = min(n, a.cap);
-            uint32_t start = n > a.cap ? (h >> 8) % n : 0;
-            for (uint32_t j = 0; j < take; ++j) {
-                uint32_t s = beg + (start + j) % n;
-                uint32_t x2 = col[s];
-                if (x2 == x1 || a.chain_id[x2] != c) continue;
-                int64_t g = swap_gain(p1, a1, n1, Pp[x2], spt[s], Pn[x2]);
+        }
+        // target cell
+        if (a.cap) {
+            int32_t mx = (pt_X(p1) + pt_X(n1)) >> 1, my = (pt_Y(p1) + pt_Y(n1)) >> 1;
+            int cx = (int)min((uint32_t)max(mx, 0) >> 9, a.ncx - 1), cy = (int)min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
+            scan_cell(a, cs, spt, col, Pp, Pn, cx, cy, a.cap, h >> 5, x1, c, p1, a1, n1, best, bx);
+        }
+        // uniform random partners in the same chain
+        if (a.nrandom) {
+            uint64_t off = a.chain_off[c];
+            uint32_t w = (uint32_t)(a.chain_off[c + 1] - off);
+            uint32_t r = h;
+            for (uint32_t k = 0; k < a.nrandom; ++k) {
+                r = mix32(r + 0x68E31DA4u);
+                uint32_t x2 = (uint32_t)off + r % w;
+                if (x2 == x1) continue;
+                int64_t g = swap_gain(p1, a1, n1, Pp[x2], Py[x2], Pn[x2]);
                 if (g > best) { best = g; bx = x2; }
             }
         }

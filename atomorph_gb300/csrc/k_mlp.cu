@@ -484,6 +484,46 @@ __global__ void __launch_bounds__(256) k_cost_cache(LocalArgs a) {
 
 __device__ __forceinline__ float slog1p(float x) { return x >= 0.f ? log1pf(x) : -log1pf(-x); }
 
+// Warp-collective: lanes [lo, hi) each take one slot of the 5-cell window
+// (centre and its 4 neighbours) around cell (cx, cy); when the window holds
+// more slots than lanes, the start rotates by `rot`.  Returns whether the
+// calling lane got a slot.
+__device__ __forceinline__ bool window_slot(const uint32_t *cs, int cx, int cy, uint32_t ncx, uint32_t ncy, int lane,
+                                            int lo, int hi, uint32_t rot, uint32_t *slot) {
+    uint32_t beg = 0, cnt = 0;
+    if (lane < 5) {
+        int qx = cx + (lane == 1 ? 1 : (lane == 2 ? -1 : 0));
+        int qy = cy + (lane == 3 ? 1 : (lane == 4 ? -1 : 0));
+        if (qx >= 0 && qy >= 0 && qx < (int)ncx && qy < (int)ncy) {
+            uint32_t cell = (uint32_t)qy * ncx + (uint32_t)qx;
+            beg = cs[cell];
+            cnt = cs[cell + 1] - beg;
+        }
+    }
+    uint32_t pre = cnt;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        uint32_t u = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += u;
+    }
+    uint32_t total = __shfl_sync(0xffffffffu, pre, 4);
+    uint32_t j = (uint32_t)(lane - lo);
+    bool mine = lane >= lo && lane < hi && j < total;
+    if (total > (uint32_t)(hi - lo) && total) j = (j + rot % total) % total;
+    uint32_t ksel = 5;
+#pragma unroll
+    for (int k = 4; k >= 0; --k) {
+        uint32_t pk = __shfl_sync(0xffffffffu, pre, k);
+        if (j < pk) ksel = (uint32_t)k;
+    }
+    uint32_t src = ksel < 5 ? ksel : 0u;
+    uint32_t bk = __shfl_sync(0xffffffffu, beg, src);
+    uint32_t pprev = __shfl_sync(0xffffffffu, pre, src > 0 ? src - 1 : 0);
+    if (src == 0) pprev = 0;
+    *slot = bk + (j - pprev);
+    return mine && ksel < 5;
+}
+
 struct PropSmem {
     FwdSmem f;
 };
@@ -506,6 +546,7 @@ __global__ void __launch_bounds__(128) k_learned_propose(LocalArgs a) {
         uint64_t a1 = 0, p1 = 0, n1 = 0;
         bool cand = false;
         uint32_t x2 = 0xFFFFFFFFu, s2 = 0;
+        uint64_t a2w = 0;
         float feats[kMlpIn];
 #pragma unroll
         for (int k = 0; k < kMlpIn; ++k) feats[k] = 0.f;
@@ -522,44 +563,29 @@ __global__ void __launch_bounds__(128) k_learned_propose(LocalArgs a) {
                 p1 = a.P[(uint64_t)yp * N + x1];
                 n1 = a.P[(uint64_t)yn * N + x1];
                 int32_t mx = (pt_X(p1) + pt_X(n1)) >> 1, my = (pt_Y(p1) + pt_Y(n1)) >> 1;
-                int cx = (int)min((uint32_t)max(mx, 0) >> 9, a.ncx - 1);
-                int cy = (int)min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
+                int tx = (int)min((uint32_t)max(mx, 0) >> 9, a.ncx - 1);
+                int ty = (int)min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
+                int ox = (int)min((uint32_t)pt_X(a1) >> 9, a.ncx - 1);
+                int oy = (int)min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1);
                 const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
-                // cell k of the 3x3 window, centre first
-                uint32_t beg = 0, cnt = 0;
-                if (lane < 9) {
-                    int kk = lane == 0 ? 4 : (lane <= 4 ? lane - 1 : lane);
-                    int qx = cx + (kk % 3) - 1, qy = cy + (kk / 3) - 1;
-                    if (qx >= 0 && qy >= 0 && qx < (int)a.ncx && qy < (int)a.ncy) {
-                        uint32_t cell = (uint32_t)qy * a.ncx + (uint32_t)qx;
-                        beg = cs[cell];
-                        cnt = cs[cell + 1] - beg;
-                    }
-                }
-                // inclusive prefix of the counts over lanes 0..8
-                uint32_t pre = cnt;
-#pragma unroll
-                for (int o = 1; o < 16; o <<= 1) {
-                    uint32_t u = __shfl_up_sync(0xffffffffu, pre, o);
-                    if (lane >= o) pre += u;
-                }
-                // candidate `lane`: first cell whose inclusive prefix exceeds it
-                uint32_t my_cell = 9;
-                for (int k = 8; k >= 0; --k) {
-                    uint32_t pk = __shfl_sync(0xffffffffu, pre, k);
-                    if ((uint32_t)lane < pk) my_cell = (uint32_t)k;
-                }
-                uint32_t bk = __shfl_sync(0xffffffffu, beg, my_cell < 9 ? my_cell : 0);
-                bool has_prev = my_cell > 0 && my_cell < 9;
-                uint32_t pk_raw = __shfl_sync(0xffffffffu, pre, has_prev ? my_cell - 1 : 0);
-                uint32_t pk_prev = has_prev ? pk_raw : 0u;
-                if (my_cell < 9) {
-                    s2 = bk + ((uint32_t)lane - pk_prev);
+                uint32_t hh = mix32((uint32_t)a.key ^ mix32(x1 * 0x9E3779B1u + y));
+                // lanes 0-15: own neighbourhood, 16-27: target window, 28-31: random
+                uint32_t sA, sB;
+                bool vA = window_slot(cs, ox, oy, a.ncx, a.ncy, lane, 0, 16, hh, &sA);
+                bool vB = window_slot(cs, tx, ty, a.ncx, a.ncy, lane, 16, 28, hh >> 7, &sB);
+                if (vA || vB) {
+                    s2 = vA ? sA : sB;
                     x2 = a.col[(uint64_t)y * N + s2];
-                    cand = x2 != x1 && a.chain_id[x2] == c;
+                    a2w = a.slot_pt[(uint64_t)y * N + s2];
+                } else if (lane >= 28) {
+                    uint64_t off = a.chain_off[c];
+                    uint32_t w = (uint32_t)(a.chain_off[c + 1] - off);
+                    x2 = (uint32_t)off + mix32(hh + (uint32_t)lane * 0x68E31DA4u) % w;
+                    a2w = a.P[(uint64_t)y * N + x2];
                 }
+                cand = x2 != 0xFFFFFFFFu && x2 != x1 && a.chain_id[x2] == c;
                 if (cand) {
-                    uint64_t a2 = a.slot_pt[(uint64_t)y * N + s2];
+                    uint64_t a2 = a2w;
                     uint32_t col1 = a.display[(size_t)y * fr + (size_t)pt_y(a1) * a.CW + pt_x(a1)];
                     uint32_t col2 = a.display[(size_t)y * fr + (size_t)pt_y(a2) * a.CW + pt_x(a2)];
                     float c1 = (float)a.cost_cache[(uint64_t)fi * N + x1];
@@ -583,7 +609,7 @@ __global__ void __launch_bounds__(128) k_learned_propose(LocalArgs a) {
         if (a.rec_count && cand) {
             int64_t g = 0;
             {
-                uint64_t a2 = a.slot_pt[(uint64_t)y * N + s2];
+                uint64_t a2 = a2w;
                 uint64_t p2 = a.P[(uint64_t)yp * N + x2], n2 = a.P[(uint64_t)yn * N + x2];
                 uint64_t cc1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
                 uint64_t cc2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);
@@ -612,7 +638,7 @@ __global__ void __launch_bounds__(128) k_learned_propose(LocalArgs a) {
             if (m == -INFINITY) break;
             int64_t g = 0;
             if (lane == ml) {
-                uint64_t a2 = a.slot_pt[(uint64_t)y * N + s2];
+                uint64_t a2 = a2w;
                 uint64_t p2 = a.P[(uint64_t)yp * N + x2], n2 = a.P[(uint64_t)yn * N + x2];
                 uint64_t cc1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
                 uint64_t cc2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);

@@ -249,11 +249,56 @@ __global__ void k_pair_gather(const uint32_t *__restrict__ keys, const uint32_t 
 struct FrameArgs {
     double w1, w2;          // LINEAR: weight of pt1 and 1 - that weight
     double b[4];            // SPLINE basis at the frame's local time
+    long long w1q;          // round(w1 * 2^38)
+    long long bq[4];        // round(b[i] * 2^38)
+    uint32_t lin_mode;      // 0 general, 1 w1 == 1 (X = X1), 2 w1 == 0 (X = X2)
+    uint32_t key_mode;      // 1 when the spline basis is exactly (0, 1, 0, 0)
     uint32_t seg_ok;        // 1 when the spline segment is the prepared one
     int32_t seg[4];         // control frames when seg_ok == 0
     float str;              // colour weight of the earlier key frame, 1 - t
     uint32_t tiles_x, ntiles;
 };
+
+// Fast exact positions.  The reference evaluates its interpolation in
+// double; its result differs from the exact real value of the same formula
+// by far less than 2^-21 px.  The kernels evaluate that real value in 64-bit
+// fixed point (weights quantised to 2^-38, error below 2^-21 px as well) and
+// take its floor / rounded fraction, which equals the reference's unless the
+// value lies within the combined error bound of a rounding boundary; those
+// rare atoms re-run the reference's own double formula (lin_fixed /
+// spl_fixed below).  Returns false when the fallback is needed.
+__device__ __forceinline__ bool lin_fast(const FrameArgs &fa, int32_t a, int32_t b, int32_t *out) {
+    if (fa.lin_mode == 1) { *out = a; return true; }
+    if (fa.lin_mode == 2) { *out = b; return true; }
+    long long V = ((long long)b << 38) + fa.w1q * (long long)(a - b);  // units of 2^-38 (1/256 px)
+    const long long one = 1ll << 38, tol = 1ll << 24;                    // 2^-14 (1/256 px)
+    long long r = V & (one - 1);
+    if (r < tol || one - r < tol) return false;
+    *out = (int32_t)(V >> 38);
+    return true;
+}
+__device__ __forceinline__ bool spl_fast(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
+                                         uint32_t *out) {
+    if ((abs(q0 - q1) | abs(q2 - q1) | abs(q3 - q1)) >= (1 << 22)) return false;  // keeps V in 63 bits
+    long long V = ((long long)q1 << 38) + fa.bq[0] * (long long)(q0 - q1) + fa.bq[2] * (long long)(q2 - q1) +
+                  fa.bq[3] * (long long)(q3 - q1);  // units of 2^-46 px
+    unsigned long long A = V >= 0 ? (unsigned long long)V : (unsigned long long)(-V);
+    const unsigned long long one = 1ull << 46;
+    unsigned long long I = A >> 46, F = A & (one - 1);
+    if (!fa.key_mode) {
+        const unsigned long long tol = 1ull << 26;  // 2^-20 px
+        if (F < tol || one - F < tol) return false;
+        unsigned long long h = (F * 255ull) & (one - 1);
+        unsigned long long d = h > (one >> 1) ? h - (one >> 1) : (one >> 1) - h;
+        if (d < 255ull * tol) return false;
+    }
+    unsigned long long xf = (F * 255ull + (one >> 1)) >> 46;  // round half away on |fraction|
+    int sign = V < 0 ? -1 : 1;
+    uint32_t xi = (uint32_t)(sign * (long long)I) & 0xFFFFu;
+    uint32_t xb = (uint32_t)(sign * (long long)xf) & 0xFFu;
+    *out = (xi << 8) | xb;
+    return true;
+}
 
 // Exact double formula of morph::interpolate(point) (morph.cpp:1504-1512)
 // with round-to-nearest operations: floor(w1*X1 + w2*X2) in 1/256 px.
@@ -335,8 +380,9 @@ __global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs f
         uint32_t X, Y;
         int4 a = pa[i];
         if (sc.motion == AM_LINEAR) {
-            X = (uint32_t)lin_fixed(fa.w1, fa.w2, a.x, a.z);
-            Y = (uint32_t)lin_fixed(fa.w1, fa.w2, a.y, a.w);
+            int32_t xx, yy;
+            X = lin_fast(fa, a.x, a.z, &xx) ? (uint32_t)xx : (uint32_t)lin_fixed(fa.w1, fa.w2, a.x, a.z);
+            Y = lin_fast(fa, a.y, a.w, &yy) ? (uint32_t)yy : (uint32_t)lin_fixed(fa.w1, fa.w2, a.y, a.w);
         } else if (sc.motion == AM_SPLINE) {
             int4 b;
             if (fa.seg_ok) {
@@ -348,8 +394,8 @@ __global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs f
                 a = make_int4(pt_X(q0), pt_Y(q0), pt_X(q1), pt_Y(q1));
                 b = make_int4(pt_X(q2), pt_Y(q2), pt_X(q3), pt_Y(q3));
             }
-            X = spl_fixed(fa.b, a.x, a.z, b.x, b.z);
-            Y = spl_fixed(fa.b, a.y, a.w, b.y, b.w);
+            if (!spl_fast(fa, a.x, a.z, b.x, b.z, &X)) X = spl_fixed(fa.b, a.x, a.z, b.x, b.z);
+            if (!spl_fast(fa, a.y, a.w, b.y, b.w, &Y)) Y = spl_fixed(fa.b, a.y, a.w, b.y, b.w);
         } else {
             X = (uint32_t)a.x;
             Y = (uint32_t)a.y;
@@ -622,6 +668,8 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     std::memset(&fa, 0, sizeof(fa));
     fa.w1 = 1.0 - t;
     fa.w2 = 1.0 - fa.w1;
+    fa.w1q = llround(std::ldexp(fa.w1, 38));
+    fa.lin_mode = fa.w1 == 1.0 ? 1u : (fa.w1 == 0.0 ? 2u : 0u);
     fa.str = (float)(1.0 - t);
     fa.tiles_x = tiles_x;
     fa.ntiles = ntiles;
@@ -640,6 +688,8 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         fa.b[3] = 0.5 * (t3 - t2);
         fa.seg[0] = wrap(p - 1); fa.seg[1] = wrap(p); fa.seg[2] = wrap(p + 1); fa.seg[3] = wrap(p + 2);
         fa.seg_ok = (p == (int)f) ? 1u : 0u;
+        for (int i = 0; i < 4; ++i) fa.bq[i] = llround(std::ldexp(fa.b[i], 38));
+        fa.key_mode = (fa.b[0] == 0.0 && fa.b[1] == 1.0 && fa.b[2] == 0.0 && fa.b[3] == 0.0) ? 1u : 0u;
     }
     AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
     uint64_t n = w->active;

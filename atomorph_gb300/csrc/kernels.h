@@ -67,7 +67,10 @@ struct LocalArgs {
     uint32_t ncx, ncy, ncells;
     const uint32_t *chain_id;
     const uint8_t *chain_w1;
-    uint32_t cap;                            // candidates examined per cell
+    uint32_t cap;                            // candidates from the target cell
+    uint32_t self_cap = 12;                  // candidates from the column's own neighbourhood
+    uint32_t nrandom = 2;                    // uniform random candidates of the same chain
+    const uint64_t *chain_off = nullptr;     // [C+1]
     uint64_t key;                            // random key of this (sweep, phase)
     unsigned long long *claim;               // [nframes][N]
     uint32_t *prop;                          // [nframes][N] proposed partner

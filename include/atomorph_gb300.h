@@ -109,6 +109,11 @@ int am_set_resolution(am_morph *m, uint16_t w, uint16_t h);  /* morph::set_resol
 int am_set_proposal(am_morph *m, unsigned kind);
 int am_set_sweeps(am_morph *m, size_t sweeps_per_step);
 int am_set_motion_noise(am_morph *m, double amplitude_px);
+/* Guided-refinement tunables (the autotuner sets these): "local_self",
+ * "local_target", "local_random" (candidates per column from the column's own
+ * neighbourhood, its target cell, and uniform random columns) and
+ * "learned_topk" (network-ranked candidates checked exactly). */
+int am_set_tuning(am_morph *m, const char *name, double value);
 
 /* ---- control (morph.h:40-49, morph.cpp:52-100, 102-269) */
 int am_compute(am_morph *m);                          /* morph::compute() morph.cpp:52-57 */
