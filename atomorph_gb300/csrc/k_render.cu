@@ -463,98 +463,161 @@ __global__ void __launch_bounds__(256) k_frame_scatter(const uint4 *__restrict__
     }
 }
 
-// Exactly rounded (half away from zero) quotient num/den, both >= 0, den > 0.
+// Exactly rounded (half away from zero) quotient num/den, both >= 0, den > 0,
+// for quotients below 2^24: a float estimate corrected in exact integers.
 __device__ __forceinline__ uint32_t round_div(unsigned long long num, unsigned long long den) {
-    return (uint32_t)((2ull * num + den) / (2ull * den));
+    unsigned long long a = 2ull * num + den, b = 2ull * den;
+    long long q = (long long)__fdividef((float)a, (float)b);
+    long long r = (long long)a - q * (long long)b;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (r < 0) { --q; r += (long long)b; }
+        else if (r >= (long long)b) { ++q; r -= (long long)b; }
+    }
+    return (uint32_t)q;
 }
+
+constexpr int kRecCache = 2048;   // records of a tile kept in shared memory (32 KB)
+constexpr uint32_t kPackMax = 258; // contributions per pixel for which packed 32-bit sums cannot overflow
+
+// Shared memory of the resolve kernel, two layouts over one buffer:
+//  packed: WN[1024] (W sum low 40 bits | count << 40), RG[1024], BA[1024]
+//          (two 32-bit channel sums each), then the record cache;
+//  exact:  W, R, G, B, A as 64-bit sums and N as 32-bit counts.
+constexpr size_t kResolveSmem = 3 * 8 * 1024 + kRecCache * 16;
 
 __global__ void __launch_bounds__(256) k_frame_resolve(const uint4 *__restrict__ rec,
                                                         const uint32_t *__restrict__ tile_off, uint32_t tiles_x,
                                                         uint32_t width, uint32_t height, uint32_t density,
                                                         uint8_t *out) {
-    __shared__ unsigned long long sW[kTile * kTile], sC[4][kTile * kTile];
-    __shared__ uint32_t sN[kTile * kTile];
+    extern __shared__ __align__(16) unsigned char sm[];
     __shared__ uint32_t red[8];
+    __shared__ int s_over;
+    unsigned long long *WN = reinterpret_cast<unsigned long long *>(sm);
+    unsigned long long *RG = WN + 1024, *BA = WN + 2048;
+    uint4 *cache = reinterpret_cast<uint4 *>(sm + 3 * 8 * 1024);
+    unsigned long long *xW = WN, *xR = WN + 1024, *xG = WN + 2048, *xB = WN + 3072, *xA = WN + 4096;
+    uint32_t *xN = reinterpret_cast<uint32_t *>(WN + 5120);
     const uint32_t tile = blockIdx.x;
     const uint32_t tx0 = (tile % tiles_x) * kTile, ty0 = (tile / tiles_x) * kTile;
     const uint32_t beg = tile_off[tile], end = tile_off[tile + 1];
-    for (int i = threadIdx.x; i < kTile * kTile; i += 256) {
-        sW[i] = 0; sC[0][i] = 0; sC[1][i] = 0; sC[2][i] = 0; sC[3][i] = 0; sN[i] = 0;
-    }
+    const uint32_t nrec = end - beg;
     const uint32_t lr = threadIdx.x >> 3, lc0 = (threadIdx.x & 7) * 4;
-    int n[4] = {0, 0, 0, 0};
-    uint32_t c0[4] = {0, 0, 0, 0};
+    int n[4];
+    uint32_t c0[4];
     double R[4], G[4], B[4], A[4];
-    // First chain rank present.
-    uint32_t mn = 0xFFFFFFFFu;
-    for (uint32_t j = beg + threadIdx.x; j < end; j += 256) mn = min(mn, rec[j].w);
-    for (int o = 16; o; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
-    __syncthreads();
-    uint32_t cur = red[0];
-    for (int k = 1; k < 8; ++k) cur = min(cur, red[k]);
-    while (cur != 0xFFFFFFFFu) {
-        __syncthreads();
-        uint32_t nxt = 0xFFFFFFFFu;
-        for (uint32_t j = beg + threadIdx.x; j < end; j += 256) {
-            uint4 s = rec[j];
-            if (s.w != cur) {
-                if (s.w > cur) nxt = min(nxt, s.w);
-                continue;
-            }
-            uint32_t px = s.x & 0xFFFFu, py = s.x >> 16;
-            uint32_t xf = s.y & 255u, yf = (s.y >> 8) & 255u, valid = (s.y >> 16) & 15u;
-            uint32_t wx[2] = {255u - xf, xf}, wy[2] = {255u - yf, yf};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!(valid & (1u << k))) continue;
-                uint32_t cx = px + (k & 1) - tx0, cy = py + (k >> 1) - ty0;
-                if (cx >= (uint32_t)kTile || cy >= (uint32_t)kTile) continue;
-                uint32_t li = cy * kTile + cx;
-                unsigned long long W = (unsigned long long)(wx[k & 1] * wy[k >> 1]);
-                atomicAdd(&sW[li], W);
-                atomicAdd(&sC[0][li], W * (s.z & 255u));
-                atomicAdd(&sC[1][li], W * ((s.z >> 8) & 255u));
-                atomicAdd(&sC[2][li], W * ((s.z >> 16) & 255u));
-                atomicAdd(&sC[3][li], W * (s.z >> 24));
-                atomicAdd(&sN[li], 1u);
-            }
+    for (int mode = 0; mode < 2; ++mode) {
+        const bool packed = mode == 0;
+        const bool cached = packed && nrec <= (uint32_t)kRecCache;
+        if (packed) {
+            for (int i = threadIdx.x; i < 3 * 1024; i += 256) WN[i] = 0ull;
+            if (cached)
+                for (uint32_t j = threadIdx.x; j < nrec; j += 256) cache[j] = rec[beg + j];
+        } else {
+            for (int i = threadIdx.x; i < 5 * 1024; i += 256) WN[i] = 0ull;
+            for (int i = threadIdx.x; i < 1024; i += 256) xN[i] = 0u;
         }
-        for (int o = 16; o; o >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, o));
-        __syncthreads();
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nxt;
+        if (threadIdx.x == 0) s_over = 0;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            uint32_t li = lr * kTile + lc0 + q;
-            uint32_t cnt = sN[li];
-            if (!cnt) continue;
-            unsigned long long W = sW[li];
-            uint32_t r = round_div(sC[0][li], W), g = round_div(sC[1][li], W), b = round_div(sC[2][li], W);
-            uint32_t a;
-            if (cnt >= density) a = round_div(sC[3][li], W);
-            else a = round_div((unsigned long long)cnt * sC[3][li], (unsigned long long)density * W);
-            sW[li] = 0; sC[0][li] = 0; sC[1][li] = 0; sC[2][li] = 0; sC[3][li] = 0; sN[li] = 0;
-            if (a == 0) continue;  // draw_atoms skips transparent blob pixels
-            uint32_t cc = r | (g << 8) | (b << 16) | (a << 24);
-            if (n[q] == 0) {
-                c0[q] = cc;
-            } else {
-                if (n[q] == 1) {
-                    R[q] = (c0[q] & 255u) / 255.0; G[q] = ((c0[q] >> 8) & 255u) / 255.0;
-                    B[q] = ((c0[q] >> 16) & 255u) / 255.0; A[q] = (c0[q] >> 24) / 255.0;
-                }
-                double sr = r / 255.0, sg = g / 255.0, sb = b / 255.0, sa = a / 255.0;
-                double om = __dsub_rn(1.0, sa);
-                R[q] = __dadd_rn(__dmul_rn(sa, sr), __dmul_rn(om, R[q]));
-                G[q] = __dadd_rn(__dmul_rn(sa, sg), __dmul_rn(om, G[q]));
-                B[q] = __dadd_rn(__dmul_rn(sa, sb), __dmul_rn(om, B[q]));
-                A[q] = __dadd_rn(A[q], __dmul_rn(__dsub_rn(1.0, A[q]), a / 255.0));
-            }
-            n[q]++;
-        }
+        for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; }
         __syncthreads();
-        cur = red[0];
+        uint32_t mn = 0xFFFFFFFFu;
+        for (uint32_t j = threadIdx.x; j < nrec; j += 256) mn = min(mn, cached ? cache[j].w : rec[beg + j].w);
+        for (int o = 16; o; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
+        __syncthreads();
+        uint32_t cur = red[0];
         for (int k = 1; k < 8; ++k) cur = min(cur, red[k]);
+        bool over = false;
+        while (cur != 0xFFFFFFFFu) {
+            __syncthreads();
+            uint32_t nxt = 0xFFFFFFFFu;
+            for (uint32_t j = threadIdx.x; j < nrec; j += 256) {
+                uint4 s = cached ? cache[j] : rec[beg + j];
+                if (s.w != cur) {
+                    if (s.w > cur) nxt = min(nxt, s.w);
+                    continue;
+                }
+                uint32_t px = s.x & 0xFFFFu, py = s.x >> 16;
+                uint32_t xf = s.y & 255u, yf = (s.y >> 8) & 255u, valid = (s.y >> 16) & 15u;
+                uint32_t wx[2] = {255u - xf, xf}, wy[2] = {255u - yf, yf};
+                uint32_t cr = s.z & 255u, cg = (s.z >> 8) & 255u, cb = (s.z >> 16) & 255u, ca = s.z >> 24;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (!(valid & (1u << k))) continue;
+                    uint32_t cx = px + (k & 1) - tx0, cy = py + (k >> 1) - ty0;
+                    if (cx >= (uint32_t)kTile || cy >= (uint32_t)kTile) continue;
+                    uint32_t li = cy * kTile + cx;
+                    uint32_t W = wx[k & 1] * wy[k >> 1];
+                    if (packed) {
+                        atomicAdd(&WN[li], (unsigned long long)W | (1ull << 40));
+                        atomicAdd(&RG[li], (unsigned long long)(W * cr) | ((unsigned long long)(W * cg) << 32));
+                        atomicAdd(&BA[li], (unsigned long long)(W * cb) | ((unsigned long long)(W * ca) << 32));
+                    } else {
+                        atomicAdd(&xW[li], (unsigned long long)W);
+                        atomicAdd(&xR[li], (unsigned long long)(W * cr));
+                        atomicAdd(&xG[li], (unsigned long long)(W * cg));
+                        atomicAdd(&xB[li], (unsigned long long)(W * cb));
+                        atomicAdd(&xA[li], (unsigned long long)(W * ca));
+                        atomicAdd(&xN[li], 1u);
+                    }
+                }
+            }
+            for (int o = 16; o; o >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, o));
+            __syncthreads();
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nxt;
+            if (packed) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if ((WN[lr * kTile + lc0 + q] >> 40) > kPackMax) s_over = 1;
+                __syncthreads();
+                if (s_over) { over = true; break; }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                uint32_t li = lr * kTile + lc0 + q;
+                unsigned long long W, sr, sg, sb, sa;
+                uint32_t cnt;
+                if (packed) {
+                    unsigned long long wn = WN[li], rg = RG[li], ba = BA[li];
+                    cnt = (uint32_t)(wn >> 40);
+                    W = wn & ((1ull << 40) - 1);
+                    sr = rg & 0xFFFFFFFFull; sg = rg >> 32; sb = ba & 0xFFFFFFFFull; sa = ba >> 32;
+                    WN[li] = 0ull; RG[li] = 0ull; BA[li] = 0ull;
+                } else {
+                    cnt = xN[li];
+                    W = xW[li]; sr = xR[li]; sg = xG[li]; sb = xB[li]; sa = xA[li];
+                    xW[li] = 0; xR[li] = 0; xG[li] = 0; xB[li] = 0; xA[li] = 0; xN[li] = 0;
+                }
+                if (!cnt) continue;
+                uint32_t r, g, b, a;
+                r = round_div(sr, W); g = round_div(sg, W); b = round_div(sb, W);
+                a = cnt >= density ? round_div(sa, W)
+                                   : round_div((unsigned long long)cnt * sa, (unsigned long long)density * W);
+                if (a == 0) continue;  // draw_atoms skips transparent blob pixels
+                uint32_t cc = r | (g << 8) | (b << 16) | (a << 24);
+                if (n[q] == 0) {
+                    c0[q] = cc;
+                } else {
+                    if (n[q] == 1) {
+                        R[q] = (c0[q] & 255u) / 255.0; G[q] = ((c0[q] >> 8) & 255u) / 255.0;
+                        B[q] = ((c0[q] >> 16) & 255u) / 255.0; A[q] = (c0[q] >> 24) / 255.0;
+                    }
+                    double sr_ = r / 255.0, sg_ = g / 255.0, sb_ = b / 255.0, sa_ = a / 255.0;
+                    double om = __dsub_rn(1.0, sa_);
+                    R[q] = __dadd_rn(__dmul_rn(sa_, sr_), __dmul_rn(om, R[q]));
+                    G[q] = __dadd_rn(__dmul_rn(sa_, sg_), __dmul_rn(om, G[q]));
+                    B[q] = __dadd_rn(__dmul_rn(sa_, sb_), __dmul_rn(om, B[q]));
+                    A[q] = __dadd_rn(A[q], __dmul_rn(__dsub_rn(1.0, A[q]), a / 255.0));
+                }
+                n[q]++;
+            }
+            __syncthreads();
+            cur = red[0];
+            for (int k = 1; k < 8; ++k) cur = min(cur, red[k]);
+        }
+        if (!over) break;
+        __syncthreads();
     }
     uint32_t gy = ty0 + lr, gx = tx0 + lc0;
     if (gy >= height || gx >= width) return;
@@ -716,7 +779,15 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         if (w->prof) w->prof->close(PROF_SCATTER, s);
     }
     if (w->prof) w->prof->open(s);
-    AMG_LAUNCH(k_frame_resolve, ntiles, 256, 0, s, w->rec, w->tile_off, tiles_x, sc.width, sc.height,
+    {
+        static bool attr = false;
+        if (!attr) {
+            AMG_CUDA(cudaFuncSetAttribute(k_frame_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kResolveSmem));
+            attr = true;
+        }
+    }
+    AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem, s, w->rec, w->tile_off, tiles_x, sc.width, sc.height,
                sc.density ? sc.density : 1u, out);
     if (w->prof) w->prof->close(PROF_RESOLVE, s);
     AMG_CUDA(cudaGetLastError());
