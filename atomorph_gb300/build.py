@@ -34,7 +34,9 @@ UNITS = [
     ("k_mlp.cu", []),
     ("engine.cpp", ["-x", "cu"]),
     ("engine_mlp.cpp", ["-x", "cu"]),
+    ("k_fluid.cu", []),
     ("capi.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
+    ("capi_fluid.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
 ]
 
 

@@ -99,6 +99,14 @@ _SIGS = {
     "am_set_proposal_weights": (C.c_int, [vp, f32p, C.c_size_t]),
     "am_proposal_forward": (C.c_int, [vp, f32p, C.c_size_t, f32p]),
     "am_proposal_grad": (C.c_int, [vp, f32p, f32p, C.c_size_t, f32p, f32p]),
+    "am_fluid_create": (C.c_int, [C.POINTER(vp), C.c_uint32, C.c_uint32, C.c_uint32]),
+    "am_fluid_destroy": (None, [vp]),
+    "am_fluid_set_particles": (C.c_int, [vp, f64p]),
+    "am_fluid_get_particles": (C.c_int, [vp, f64p]),
+    "am_fluid_step": (C.c_int, [vp, C.c_size_t, C.c_double]),
+    "am_fluid_steps": (C.c_int, [vp, C.c_size_t, C.c_double]),
+    "am_fluid_stream": (vp, [vp]),
+    "am_set_tuning": (C.c_int, [vp, C.c_char_p, C.c_double]),
     "am_get_stream": (vp, [vp]),
     "am_profile_enable": (C.c_int, [vp, C.c_int]),
     "am_profile_read": (C.c_size_t, [vp, C.POINTER(C.c_char_p), f64p, u64p, C.c_size_t]),
@@ -378,3 +386,42 @@ class Morph:
 
 def launch_count() -> int:
     return load().am_launch_count()
+
+
+class Fluid:
+    """The FP32 GPU fluid solver (counterpart of the reference's FluidModel)."""
+
+    FIELDS = 18
+
+    def __init__(self, gsx: int, gsy: int, n: int):
+        self.lib = load()
+        h = vp()
+        _check(self.lib.am_fluid_create(C.byref(h), gsx, gsy, n), "am_fluid_create")
+        self.h, self.n = h, n
+
+    def close(self):
+        if self.h:
+            self.lib.am_fluid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, P: np.ndarray) -> None:
+        """P: [18, n] fields (oracle order)."""
+        q = np.ascontiguousarray(np.asarray(P, np.float64).T)
+        _check(self.lib.am_fluid_set_particles(self.h, _p(q, f64p)), "am_fluid_set_particles")
+
+    def get(self) -> np.ndarray:
+        q = np.zeros((self.n, 18))
+        _check(self.lib.am_fluid_get_particles(self.h, _p(q, f64p)), "am_fluid_get_particles")
+        return q.T.copy()
+
+    def step(self, steps_left: int, freedom_radius: float) -> None:
+        _check(self.lib.am_fluid_step(self.h, steps_left, freedom_radius), "am_fluid_step")
+
+    def steps(self, n: int, freedom_radius: float) -> None:
+        _check(self.lib.am_fluid_steps(self.h, n, freedom_radius), "am_fluid_steps")

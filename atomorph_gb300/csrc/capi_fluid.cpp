@@ -1,0 +1,66 @@
+// extern "C" entry points of the standalone fluid solver (the GB300
+// counterpart of the reference's FluidModel, fluidmodel.h:103-142).
+#include "engine.h"
+
+struct am_fluid {
+    amg::FluidDev *f = nullptr;
+    cudaStream_t s = nullptr;
+};
+
+extern "C" {
+
+int am_fluid_create(am_fluid **out, uint32_t gsx, uint32_t gsy, uint32_t n) {
+    if (!out || gsx < 8 || gsy < 8) return AM_ERR_ARG;
+    am_fluid *h = new (std::nothrow) am_fluid();
+    if (!h) return AM_ERR_NOMEM;
+    if (cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        amg::set_error("cudaStreamCreate failed");
+        return AM_ERR_CUDA;
+    }
+    h->f = amg::fluid_create(gsx, gsy, n);
+    if (!h->f) {
+        cudaStreamDestroy(h->s);
+        delete h;
+        return AM_ERR_NOMEM;
+    }
+    *out = h;
+    return AM_OK;
+}
+
+void am_fluid_destroy(am_fluid *h) {
+    if (!h) return;
+    amg::fluid_destroy(h->f);
+    if (h->s) cudaStreamDestroy(h->s);
+    delete h;
+}
+
+int am_fluid_set_particles(am_fluid *h, const double *state) {
+    if (!h || !state) return AM_ERR_ARG;
+    return amg::fluid_set(h->f, state, h->s);
+}
+
+int am_fluid_get_particles(am_fluid *h, double *state) {
+    if (!h || !state) return AM_ERR_ARG;
+    return amg::fluid_get(h->f, state, h->s);
+}
+
+int am_fluid_step(am_fluid *h, size_t steps_left, double freedom_radius) {
+    if (!h) return AM_ERR_ARG;
+    int rc = amg::fluid_step(h->f, steps_left, freedom_radius, h->s, nullptr);
+    if (rc) return rc;
+    return cudaStreamSynchronize(h->s) == cudaSuccess ? AM_OK : AM_ERR_CUDA;
+}
+
+int am_fluid_steps(am_fluid *h, size_t n, double freedom_radius) {
+    if (!h) return AM_ERR_ARG;
+    for (size_t i = 0; i < n; ++i) {
+        int rc = amg::fluid_step(h->f, n - (i + 1), freedom_radius, h->s, nullptr);
+        if (rc) return rc;
+    }
+    return cudaStreamSynchronize(h->s) == cudaSuccess ? AM_OK : AM_ERR_CUDA;
+}
+
+void *am_fluid_stream(am_fluid *h) { return h ? (void *)h->s : nullptr; }
+
+}  // extern "C"

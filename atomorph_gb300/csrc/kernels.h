@@ -175,6 +175,14 @@ int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32
 // Drops cached per-key-frame-pair data (chains or settings changed).
 void render_invalidate(RenderWork *w);
 
+// ---- k_fluid.cu: FluidModel::step in FP32
+struct FluidDev;
+FluidDev *fluid_create(uint32_t gsx, uint32_t gsy, uint32_t n);
+void fluid_destroy(FluidDev *f);
+int fluid_set(FluidDev *f, const double *state, cudaStream_t s);  // n x 18 doubles (oracle order)
+int fluid_get(FluidDev *f, double *state, cudaStream_t s);
+int fluid_step(FluidDev *f, uint64_t steps_left, double freedom_radius, cudaStream_t s, Prof *prof);
+
 // ---- k_blobs.cu
 struct BlobWork;
 BlobWork *blob_work_create();

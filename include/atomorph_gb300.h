@@ -189,6 +189,20 @@ int    am_proposal_forward(am_morph *m, const float *features, size_t n, float *
 int    am_proposal_grad(am_morph *m, const float *features, const float *targets, size_t n, float *grad,
                         float *loss_sum);
 
+/* ---- fluid solver (the reference's FluidModel, fluidmodel.h:103-142), FP32.
+ * Particle state is exchanged as 18 doubles per particle in this order:
+ * x y u v gravity_x gravity_y freedom_r active mature strength R G B A r g b a
+ * (Particle, fluidmodel.h:33-79; positions in grid units). */
+typedef struct am_fluid am_fluid;
+int  am_fluid_create(am_fluid **out, uint32_t gsize_x, uint32_t gsize_y, uint32_t particles); /* FluidModel::FluidModel fluidmodel.cpp:107-148 */
+void am_fluid_destroy(am_fluid *f);                                             /* FluidModel::~FluidModel fluidmodel.cpp:151-162 */
+int  am_fluid_set_particles(am_fluid *f, const double *state);
+int  am_fluid_get_particles(am_fluid *f, double *state);                        /* FluidModel::getParticles fluidmodel.cpp:595-597 */
+int  am_fluid_step(am_fluid *f, size_t steps_left, double freedom_radius);      /* FluidModel::step fluidmodel.cpp:165-580 */
+/* n steps with steps_left = n-1 .. 0, as morph::step_fluid runs them (morph.cpp:1054). */
+int  am_fluid_steps(am_fluid *f, size_t n, double freedom_radius);
+void *am_fluid_stream(am_fluid *f);
+
 /* ---- runtime (no reference counterpart) */
 void    *am_get_stream(am_morph *m);        /* cudaStream_t that renders run on */
 /* Per-kernel timing: when enabled, CUDA events are recorded on the launching

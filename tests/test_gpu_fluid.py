@@ -1,0 +1,67 @@
+"""FP32 GPU fluid solver against the FP64 oracle (the reference's
+FluidModel::step restated bit-exactly, tests/test_oracle_pin.py).
+
+Stated tolerance (FP32 vs FP64): after the steps below, every particle
+position is within 0.02 grid units and every velocity within 0.02 grid
+units/step of the FP64 result; colours within 0.01.  Errors are printed per
+config."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_oracle(oracle, P, gsx, gsy, steps, freedom):
+    P = P.copy()
+    grid = np.zeros(13 * gsx * gsy)
+    touched = np.zeros(gsx * gsy, np.uint8)
+    for s in range(steps):
+        oracle.fluid_step(P, gsx, gsy, grid, touched, steps - 1 - s, freedom)
+    return P
+
+
+def _errors(a, b):
+    act = a[7] != 0
+    return dict(pos=float(np.abs(a[0:2, act] - b[0:2, act]).max()),
+                vel=float(np.abs(a[2:4, act] - b[2:4, act]).max()),
+                col=float(np.abs(a[14:18, act] - b[14:18, act]).max()))
+
+
+def test_fluid_matches_reference_golden(capi):
+    g = golden("fluid")
+    gsx, gsy = int(g["gsx"]), int(g["gsy"])
+    f = capi.Fluid(gsx, gsy, g["init"].shape[1])
+    f.set(g["init"])
+    for s in range(8):
+        f.step(7 - s, float(g["freedom"]))
+    got = f.get()
+    e = _errors(got, g["step8"])
+    print("fluid golden 40x36, 300 particles, 8 steps:", e)
+    assert np.array_equal(got[7], g["step8"][7]) and np.array_equal(got[8], g["step8"][8])
+    assert e["pos"] <= 0.02 and e["vel"] <= 0.02 and e["col"] <= 0.01, e
+
+
+@pytest.mark.parametrize("gs,n,steps", [(128, 20000, 10), (512, 200000, 10)])
+def test_fluid_matches_oracle_at_scale(capi, oracle, gs, n, steps):
+    r = np.random.default_rng(gs + n)
+    P = np.zeros((18, n))
+    P[0] = r.uniform(12, gs - 12, n)
+    P[1] = r.uniform(12, gs - 12, n)
+    P[4] = np.clip(P[0] + r.normal(0, 3, n), 10, gs - 10)
+    P[5] = np.clip(P[1] + r.normal(0, 3, n), 10, gs - 10)
+    P[6] = 1.0
+    P[7] = (r.random(n) < 0.95)
+    P[8] = (r.random(n) < 0.8)
+    P[9] = r.choice([0.1, 1.0], n)
+    P[10:14] = r.random((4, n))
+    P[14:18] = r.random((4, n))
+    ref = _run_oracle(oracle, P, gs, gs, steps, 4.0)
+    f = capi.Fluid(gs, gs, n)
+    f.set(P)
+    f.steps(steps, 4.0)
+    got = f.get()
+    e = _errors(got, ref)
+    print(f"fluid {gs}x{gs}, {n} particles, {steps} steps:", e)
+    assert e["pos"] <= 0.02 and e["vel"] <= 0.02 and e["col"] <= 0.01, e
