@@ -136,6 +136,7 @@ int am_set_tuning(am_morph *m, const char *name, double value) {
         else if (n == "local_target") p->local_target = (uint32_t)value;
         else if (n == "local_random") p->local_random = (uint32_t)value;
         else if (n == "learned_topk") p->learned_topk = std::max<uint32_t>(1, std::min<uint32_t>(8, (uint32_t)value));
+        else if (n == "guided_switch") p->guided_switch = value;
         else return AM_ERR_ARG;
     }
     return AM_OK;

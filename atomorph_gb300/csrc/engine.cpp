@@ -475,6 +475,7 @@ static std::vector<std::vector<uint32_t>> phases_for(uint32_t K) {
 
 int Engine::set_chain_layout(const std::vector<uint64_t> &w) {
     local_valid = false;
+    guided_on = false;
     widths = w;
     C = (uint32_t)w.size();
     chain_off.assign(C + 1, 0);
@@ -621,12 +622,29 @@ int Engine::compute_cost(uint64_t *exact) {
     return AM_OK;
 }
 
+// Guided and learned refinement start with the plain method's cheap uniform
+// sweeps, which fix the coarse transport quickly, and switch (once per set of
+// chains) to guided sweeps when a block of plain sweeps gains less than
+// `guided_switch` of the cost per sweep; from then on the guided proposals
+// resolve the local crossings uniform pairs almost never sample.
 int Engine::refine(size_t sweeps, uint64_t *gains) {
     if (N == 0 || K == 0 || sweeps == 0) return AM_OK;
-    if (active.proposal != AM_PROPOSAL_RANDOM) {
-        int rc = refine_guided(sweeps, gains);
-        return rc;
+    if (active.proposal == AM_PROPOSAL_RANDOM) return refine_plain(sweeps, gains);
+    size_t done = 0;
+    while (!guided_on && done < sweeps) {
+        size_t b = std::min<size_t>(50, sweeps - done);
+        uint64_t before = cost_exact;
+        int rc = refine_plain(b, gains ? gains + done : nullptr);
+        if (rc) return rc;
+        done += b;
+        double g = (double)(before - cost_exact);
+        if (g < active.guided_switch * (double)b * (double)cost_exact) guided_on = true;
     }
+    if (done < sweeps) return refine_guided(sweeps - done, gains ? gains + done : nullptr);
+    return AM_OK;
+}
+
+int Engine::refine_plain(size_t sweeps, uint64_t *gains) {
     local_valid = false;  // plain sweeps move points without the guided index
     int rc;
     if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * sweeps + 4)))) return rc;

@@ -32,6 +32,7 @@ struct Params {  // defaults of morph.h:97-119
     size_t sweeps = 1;
     // guided-refinement tunables (am_set_tuning; chosen by the autotuner)
     uint32_t local_self = 12, local_target = 8, local_random = 2, learned_topk = 2;
+    double guided_switch = 1e-4;  // plain -> guided when a plain sweep gains less than this fraction
     double motion_noise = 0.0;
 };
 
@@ -180,6 +181,8 @@ class Engine {
     int export_chains(uint64_t *w, uint64_t *pts, int32_t *order);
     int set_chain_layout(const std::vector<uint64_t> &w);
     int refine_guided(size_t sweeps, uint64_t *gains);
+    int refine_plain(size_t sweeps, uint64_t *gains);
+    bool guided_on = false;                // the guided phase of the current chains has started
     int copy_keyframe(size_t f, uint8_t *dst);
     unsigned active_seed_mix() const;
     int status = AM_OK;                    // first failure inside the worker

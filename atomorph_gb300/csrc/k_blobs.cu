@@ -77,9 +77,19 @@ __global__ void k_cc_merge(const uint8_t *__restrict__ present, int32_t *L, uint
     }
 }
 
-__global__ void k_cc_flatten(int32_t *L, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        if (L[i] >= 0) L[i] = cc_find(L, (int32_t)i);
+// Every label becomes its root.  No path compression here: with merging
+// finished, the only values written are roots, so a thread walking through a
+// pixel another thread just rewrote still reaches the same root (with
+// compression, a stale halving write could replace a root by an ancestor).
+__global__ void k_cc_flatten(int32_t *L, size_t n, int *err) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int32_t x = L[i];
+        if (x < 0) continue;
+        int it = 0;
+        for (int32_t p = L[x]; p != x && it < (1 << 24); p = L[x], ++it) x = p;
+        if (L[x] != x) atomicExch(err, 1);
+        L[i] = x;
+    }
 }
 
 // Roots per scan tile.
@@ -126,18 +136,24 @@ __global__ void __launch_bounds__(256) k_root_rank(const int32_t *__restrict__ L
     }
 }
 
+// Roots were ranked by k_root_rank and every present pixel's label is a root
+// after k_cc_flatten; when flattening flagged a failure the host discards the
+// labels, and k_blob_stats ignores any label outside [0, nblobs).
 __global__ void k_relabel(int32_t *L, const int32_t *__restrict__ rank, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        if (L[i] >= 0) L[i] = rank[L[i]];
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int32_t r = L[i];
+        if (r >= 0) L[i] = rank[r];
+    }
 }
 
 // Exact per-blob sums; lanes with the same label reduce together first.
 __global__ void k_blob_stats(const int32_t *__restrict__ L, const uint32_t *__restrict__ stored, uint32_t W,
-                             size_t n, unsigned long long *stats) {
+                             size_t n, unsigned long long *stats, uint32_t nblobs) {
     const int lane = threadIdx.x & 31;
     for (size_t base = blockIdx.x * (size_t)blockDim.x; base < n; base += (size_t)gridDim.x * blockDim.x) {
         size_t i = base + threadIdx.x;
         int32_t l = i < n ? L[i] : -1;
+        if (l >= (int32_t)nblobs) l = -1;  // never written out of range
         unsigned peers = __match_any_sync(0xffffffffu, l);
         uint32_t c = i < n ? stored[i] : 0u;
         uint32_t v[7] = {1u, (uint32_t)(i % W), (uint32_t)(i / W), c & 255u, (c >> 8) & 255u, (c >> 16) & 255u,
@@ -260,7 +276,7 @@ int label_components(BlobWork *w, const uint8_t *present, const uint32_t *stored
     unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)kSMs * 16);
     AMG_LAUNCH(k_cc_init, grid, 256, 0, s, present, labels, n);
     AMG_LAUNCH(k_cc_merge, grid, 256, 0, s, present, labels, CW, CH, w->err);
-    AMG_LAUNCH(k_cc_flatten, grid, 256, 0, s, labels, n);
+    AMG_LAUNCH(k_cc_flatten, grid, 256, 0, s, labels, n, w->err);
     AMG_LAUNCH(k_root_count, (unsigned)ntiles, 256, 0, s, labels, n, w->tile_cnt);
     AMG_CUDA(cudaMemsetAsync(w->tile_cnt + ntiles, 0, 4, s));
     int rc = launch_scan_u32(w->tile_cnt, ntiles + 1, nullptr, s);
@@ -287,7 +303,7 @@ int blob_stats(BlobWork *w, const int32_t *labels, const uint32_t *stored, uint3
     AMG_CUDA(cudaMemsetAsync(stats, 0, (size_t)nblobs * 7 * sizeof(unsigned long long), s));
     if (!n || !nblobs) return AM_OK;
     unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)kSMs * 16);
-    AMG_LAUNCH(k_blob_stats, grid, 256, 0, s, labels, stored, CW, n, stats);
+    AMG_LAUNCH(k_blob_stats, grid, 256, 0, s, labels, stored, CW, n, stats, nblobs);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }

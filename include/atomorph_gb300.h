@@ -111,8 +111,10 @@ int am_set_sweeps(am_morph *m, size_t sweeps_per_step);
 int am_set_motion_noise(am_morph *m, double amplitude_px);
 /* Guided-refinement tunables (the autotuner sets these): "local_self",
  * "local_target", "local_random" (candidates per column from the column's own
- * neighbourhood, its target cell, and uniform random columns) and
- * "learned_topk" (network-ranked candidates checked exactly). */
+ * neighbourhood, its target cell, and uniform random columns),
+ * "learned_topk" (network-ranked candidates checked exactly) and
+ * "guided_switch" (guided/learned refinement runs plain sweeps until one gains
+ * less than this fraction of the cost per sweep; 0 = guided from the start). */
 int am_set_tuning(am_morph *m, const char *name, double value);
 
 /* ---- control (morph.h:40-49, morph.cpp:52-100, 102-269) */

@@ -55,6 +55,15 @@ inline pixel create_pixel(uint16_t x, uint16_t y, unsigned char r, unsigned char
 inline pixel create_pixel(uint16_t x, uint16_t y, color c) { return create_pixel(x, y, c.r, c.g, c.b, c.a); }
 inline size_t xy2pos(uint16_t x, uint16_t y) { return (size_t)y * (UINT16_MAX + 1) + x; }
 inline const char *get_version() { return "1.0"; }
+// atomorph.h:300-302, 355-357: build warnings and the OpenCV variant flag.
+const size_t WARN_POINTER_SIZE = 1, WARN_PIXEL_SIZE = 2, WARN_POINT_SIZE = 3;
+inline size_t get_warning() {
+    size_t flags = 0;
+    if (sizeof(void *) < 8) flags |= WARN_POINTER_SIZE;
+    if (sizeof(pixel) > 8) flags |= WARN_PIXEL_SIZE;
+    return flags;
+}
+inline bool uses_opencv() { return false; }
 
 class morph {
   public:
