@@ -35,6 +35,7 @@ UNITS = [
     ("engine.cpp", ["-x", "cu"]),
     ("engine_mlp.cpp", ["-x", "cu"]),
     ("k_fluid.cu", []),
+    ("noalloc.cu", []),
     ("capi.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
     ("capi_fluid.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
 ]

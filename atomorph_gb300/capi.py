@@ -75,6 +75,7 @@ _SIGS = {
     "am_get_state": (C.c_uint, [vp]),
     "am_get_energy": (C.c_double, [vp]),
     "am_get_cost": (C.c_int, [vp, u64p, f64p]),
+    "am_get_cost_noalloc": (C.c_int, [vp, u64p]),
     "am_get_blob_count": (C.c_size_t, [vp, C.c_size_t]),
     "am_get_blob_count_total": (C.c_size_t, [vp]),
     "am_get_pixel_count": (C.c_size_t, [vp, C.c_size_t]),

@@ -174,6 +174,19 @@ int am_get_cost(am_morph *m, uint64_t *exact, double *as_double) {
     if (as_double) *as_double = (double)v;
     return AM_OK;
 }
+int am_get_cost_noalloc(am_morph *m, uint64_t *exact) {
+    CHECK(m);
+    if (!exact) return AM_ERR_ARG;
+    Engine &e = H(m);
+    if (e.is_busy()) return AM_ERR_BUSY;
+    uint64_t v = 0;
+    if (e.fN) {
+        int rc = e.compute_cost_noalloc(&v);
+        if (rc) return rc;
+    }
+    *exact = v;
+    return AM_OK;
+}
 size_t am_get_frame_count(const am_morph *m) { return m ? m->e.frames.size() : 0; }
 static long frame_index(const Engine &e, size_t key) {
     long i = 0;

@@ -175,6 +175,7 @@ class Engine {
     int build_chains();
     int refine(size_t sweeps, uint64_t *gains);
     int compute_cost(uint64_t *exact);
+    int compute_cost_noalloc(uint64_t *exact);  // noalloc.cu: static scratch, no device allocation
     int publish_front();
     int render(double t, uint8_t *out, bool out_dev);
     int import_chains(size_t K, size_t C, const uint64_t *w, const uint64_t *pts, const int32_t *order);

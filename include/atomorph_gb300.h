@@ -133,6 +133,15 @@ double   am_get_energy(const am_morph *m);                  /* morph.h:41; the T
 /* Exact atom cost: sum over chains of thread::get_energy(chain*)
  * (thread.cpp:1109-1125), as an exact integer and as a double. */
 int      am_get_cost(am_morph *m, uint64_t *exact, double *as_double);
+/* The exact cost of am_get_cost without allocating device memory (no
+ * counterpart in the reference): for callers that must not allocate while
+ * other work is on the device, since cudaMalloc/cudaFree may synchronise it.
+ * Scratch is one static device array shared by all calls in the process, so
+ * calls that overlap in time race and must be serialised by the caller.
+ * Accepts chains of at most 2^27 columns (atoms x key frames); larger ones
+ * return AM_ERR_ARG.  The first call on a device looks up the array's
+ * address: make it before any stream capture begins. */
+int      am_get_cost_noalloc(am_morph *m, uint64_t *exact);
 size_t   am_get_blob_count(const am_morph *m, size_t frame);  /* morph::get_blob_count(f) morph.cpp:399-402 */
 size_t   am_get_blob_count_total(const am_morph *m);          /* morph::get_blob_count() morph.cpp:425-434 */
 size_t   am_get_pixel_count(const am_morph *m, size_t frame); /* morph::get_pixel_count morph.cpp:394-397 */
