@@ -36,6 +36,9 @@ UNITS = [
     ("engine_mlp.cpp", ["-x", "cu"]),
     ("k_fluid.cu", []),
     ("noalloc.cu", []),
+    ("k_batch.cu", []),
+    ("engine_batch.cpp", ["-x", "cu"]),
+    ("capi_batch.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
     ("capi.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
     ("capi_fluid.cpp", ["-x", "cu", "-Xcompiler", "-fvisibility=default"]),
 ]

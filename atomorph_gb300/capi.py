@@ -108,6 +108,13 @@ _SIGS = {
     "am_fluid_steps": (C.c_int, [vp, C.c_size_t, C.c_double]),
     "am_fluid_stream": (vp, [vp]),
     "am_set_tuning": (C.c_int, [vp, C.c_char_p, C.c_double]),
+    "am_batch_create": (C.c_int, [C.POINTER(vp), C.POINTER(vp), C.c_size_t]),
+    "am_batch_destroy": (None, [vp]),
+    "am_batch_refine": (C.c_int, [vp, C.c_size_t, u64p]),
+    "am_batch_tune": (C.c_int, [vp, C.c_size_t]),
+    "am_batch_get_tuning": (C.c_int, [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32)]),
+    "am_batch_set_tuning": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
     "am_get_stream": (vp, [vp]),
     "am_profile_enable": (C.c_int, [vp, C.c_int]),
     "am_profile_read": (C.c_size_t, [vp, C.POINTER(C.c_char_p), f64p, u64p, C.c_size_t]),
@@ -191,6 +198,13 @@ class Morph:
                 _check(f(self.h, *v), "am_set_" + k)
             else:
                 _check(f(self.h, v), "am_set_" + k)
+        return self
+
+    def tune(self, **kw) -> "Morph":
+        """Guided-refinement tunables (am_set_tuning): local_self,
+        local_target, local_random, learned_keep, guided_switch."""
+        for k, v in kw.items():
+            _check(self.lib.am_set_tuning(self.h, k.encode(), float(v)), "am_set_tuning " + k)
         return self
 
     def add_image(self, frame: int, img: np.ndarray) -> None:
@@ -332,6 +346,9 @@ class Morph:
     def record_swaps(self, cap: int) -> None:
         _check(self.lib.am_record_swaps(self.h, cap), "am_record_swaps")
 
+    def recorded_count(self) -> int:
+        return int(self.lib.am_recorded_swaps(self.h, None, None, 1 << 62))
+
     def recorded_swaps(self, cap: int):
         f = np.zeros((cap, 10), np.float32)
         t = np.zeros(cap, np.float32)
@@ -426,3 +443,45 @@ class Fluid:
 
     def steps(self, n: int, freedom_radius: float) -> None:
         _check(self.lib.am_fluid_steps(self.h, n, freedom_radius), "am_fluid_steps")
+
+
+class Batch:
+    """Batched refinement of many morph jobs (am_batch_*)."""
+
+    def __init__(self, jobs):
+        self.lib = load()
+        self.jobs = list(jobs)  # keeps the handles alive
+        arr = (vp * len(self.jobs))(*[j.h for j in self.jobs])
+        h = vp()
+        _check(self.lib.am_batch_create(C.byref(h), arr, len(self.jobs)), "am_batch_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.am_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def refine(self, sweeps: int) -> np.ndarray:
+        """Runs `sweeps` plain sweeps of every job; returns gains [jobs, sweeps]."""
+        g = np.zeros((len(self.jobs), sweeps), np.uint64)
+        _check(self.lib.am_batch_refine(self.h, sweeps, _p(g, u64p)), "am_batch_refine")
+        return g
+
+    def tune(self, trial_sweeps: int = 3) -> dict:
+        _check(self.lib.am_batch_tune(self.h, trial_sweeps), "am_batch_tune")
+        return self.tuning
+
+    @property
+    def tuning(self) -> dict:
+        v = [C.c_uint32(0) for _ in range(4)]
+        _check(self.lib.am_batch_get_tuning(self.h, *[C.byref(x) for x in v]), "am_batch_get_tuning")
+        return dict(threads=v[0].value, ctas_per_sm=v[1].value, chunk=v[2].value, order=v[3].value)
+
+    def set_tuning(self, threads: int, ctas_per_sm: int, chunk: int, order: int) -> None:
+        _check(self.lib.am_batch_set_tuning(self.h, threads, ctas_per_sm, chunk, order), "am_batch_set_tuning")

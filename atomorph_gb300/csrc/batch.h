@@ -1,0 +1,56 @@
+// Host side of a batch of morph jobs refined together (am_batch_*): one
+// persistent cooperative launch per call, captured once into a CUDA graph
+// and replayed, with a launch shape and work schedule picked by an
+// autotuner that times real sweeps on a snapshot of the jobs' chains.
+#pragma once
+
+#include <map>
+#include <vector>
+
+#include "engine.h"
+
+namespace amg {
+
+struct BatchTuning {
+    uint32_t threads = 256;      // threads per CTA
+    uint32_t ctas_per_sm = 4;    // co-resident CTAs per SM (<= occupancy limit)
+    uint32_t chunk = 4096;       // pairs per chunk (a CTA's unit of work)
+    uint32_t order = 0;          // 0: each job's chunks together; 1: jobs interleaved chunk by chunk
+};
+
+class Batch {
+  public:
+    explicit Batch(std::vector<Engine *> jobs);
+    ~Batch();
+    int init();
+    int refine(size_t sweeps, uint64_t *gains);  // gains: [njobs][sweeps] or null
+    int tune(size_t trial_sweeps);
+    BatchTuning tuning;
+    size_t njobs() const { return jobs_.size(); }
+
+  private:
+    int sync_layout();                 // rebuild chunks when any job's chain layout changed
+    int run(size_t sweeps, const BatchTuning &t, bool graph, float *ms);
+    void drop_graphs();
+    std::vector<Engine *> jobs_;
+    std::vector<uint64_t> versions_;
+    int device_ = 0, sms_ = 0;
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    uint32_t nphase_ = 0;
+    DBuf<BatchJob> d_jobs_;
+    BatchJob *h_jobs_ = nullptr;       // pinned mirror, copied in by the graph
+    DBuf<uint32_t> d_ch_job_, d_ch_count_;
+    DBuf<uint64_t> d_ch_start_;
+    uint32_t ch_off_[4] = {};
+    DBuf<unsigned long long> d_gains_;
+    unsigned long long *h_gains_ = nullptr;  // pinned, filled by the graph
+    size_t h_gains_n_ = 0;
+    DBuf<unsigned> d_bar_;
+    DBuf<int> d_err_;
+    uint32_t chunk_built_ = 0, order_built_ = UINT32_MAX;
+    struct Graph { cudaGraphExec_t exec = nullptr; BatchTuning t; };
+    std::map<size_t, Graph> graphs_;   // by sweeps per call
+};
+
+}  // namespace amg

@@ -5,11 +5,7 @@
 #include <cstring>
 #include <new>
 
-#include "engine.h"
-
-struct am_morph {
-    amg::Engine e;
-};
+#include "handle.h"
 
 namespace amg {
 const char *last_error();
@@ -135,7 +131,10 @@ int am_set_tuning(am_morph *m, const char *name, double value) {
         if (n == "local_self") p->local_self = (uint32_t)value;
         else if (n == "local_target") p->local_target = (uint32_t)value;
         else if (n == "local_random") p->local_random = (uint32_t)value;
-        else if (n == "learned_topk") p->learned_topk = std::max<uint32_t>(1, std::min<uint32_t>(8, (uint32_t)value));
+        else if (n == "learned_keep") {
+            if (!(value > 0.0 && value <= 1.0)) return AM_ERR_ARG;
+            p->learned_keep = value;
+        }
         else if (n == "guided_switch") p->guided_switch = value;
         else return AM_ERR_ARG;
     }

@@ -117,6 +117,26 @@ __host__ __device__ __forceinline__ uint64_t pt_dist(uint64_t a, uint64_t b) {
     return (uint64_t)(dx * dx + dy * dy);
 }
 
+// Target sum s = p + n of a column (its points at the two neighbouring key
+// frames), 1/256 px, x in the low word and y in the high word.
+__host__ __device__ __forceinline__ uint64_t sums_pack(int32_t sx, int32_t sy) {
+    return (uint64_t)(uint32_t)sx | ((uint64_t)(uint32_t)sy << 32);
+}
+__host__ __device__ __forceinline__ int32_t sums_x(uint64_t s) { return (int32_t)(uint32_t)s; }
+__host__ __device__ __forceinline__ int32_t sums_y(uint64_t s) { return (int32_t)(uint32_t)(s >> 32); }
+
+// Gain of exchanging the points a1, a2 of two columns at one key frame, in
+// the reference's six-point criterion (thread.cpp:1014-1022):
+//   c1 - c2 = d(p1,a1)+d(a1,n1)+d(p2,a2)+d(a2,n2) - d(p2,a1)-d(a1,n2)-d(p1,a2)-d(a2,n1)
+//           = 2 (a1 - a2) . (s2 - s1),   s = p + n,
+// since every squared norm appears once on each side.  Exact in int64:
+// |a1 - a2| < 2^24 and |s2 - s1| < 2^25 per axis.
+__host__ __device__ __forceinline__ int64_t pair_gain(uint64_t a1, uint64_t S1, uint64_t a2, uint64_t S2) {
+    int64_t dx = (int64_t)pt_X(a1) - pt_X(a2), dy = (int64_t)pt_Y(a1) - pt_Y(a2);
+    int64_t ex = (int64_t)sums_x(S2) - sums_x(S1), ey = (int64_t)sums_y(S2) - sums_y(S1);
+    return 2 * (dx * ex + dy * ey);
+}
+
 // ------------------------------------------------------------ hashing -----
 // Counter-based randomness: every random choice is a pure function of
 // (seed, sweep, chain, frame, index), so a run is reproducible and a resumed
@@ -152,6 +172,13 @@ __device__ __forceinline__ uint32_t permute_index(uint32_t x, uint32_t n, uint32
     } while (x >= n);
     return x;
 }
+// Key of one (sweep, phase) of a job's plain refinement: a pure function of
+// the job's seed and sweep counter, so batched and per-job sweeps draw the
+// same pairs.
+__host__ __device__ __forceinline__ uint64_t sweep_key(unsigned seed, uint64_t sweep, uint32_t phase) {
+    return mix64(((uint64_t)seed << 40) ^ (sweep << 4) ^ phase);
+}
+
 __host__ __device__ __forceinline__ uint32_t half_bits_for(uint32_t n) {
     uint32_t b = 1;
     while ((1ull << b) < n) ++b;

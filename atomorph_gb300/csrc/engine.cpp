@@ -456,7 +456,7 @@ int Engine::match_run(bool *done) {
     return AM_OK;
 }
 
-static std::vector<std::vector<uint32_t>> phases_for(uint32_t K) {
+std::vector<std::vector<uint32_t>> phases_for(uint32_t K) {
     std::vector<std::vector<uint32_t>> ph;
     if (K == 0) return ph;
     if (K == 1) return {{0}};
@@ -474,6 +474,7 @@ static std::vector<std::vector<uint32_t>> phases_for(uint32_t K) {
 }
 
 int Engine::set_chain_layout(const std::vector<uint64_t> &w) {
+    ++layout_version;
     local_valid = false;
     guided_on = false;
     widths = w;
@@ -631,6 +632,7 @@ int Engine::refine(size_t sweeps, uint64_t *gains) {
     if (N == 0 || K == 0 || sweeps == 0) return AM_OK;
     if (active.proposal == AM_PROPOSAL_RANDOM) return refine_plain(sweeps, gains);
     size_t done = 0;
+    if (active.guided_switch <= 0.0) guided_on = true;
     while (!guided_on && done < sweeps) {
         size_t b = std::min<size_t>(50, sweeps - done);
         uint64_t before = cost_exact;
@@ -656,7 +658,7 @@ int Engine::refine_plain(size_t sweeps, uint64_t *gains) {
             SweepArgs a;
             a.P = d_P.p; a.N = N; a.K = K; a.C = C; a.chain_off = d_chain_off.p; a.pair_off = d_pair_off.p;
             a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
-            a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p);
+            a.key = sweep_key(seed, sweep_counter, (uint32_t)p);
             a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
             if (pair_off[C] > 0) {
                 prof.open(stream);
@@ -849,6 +851,9 @@ int Engine::ensure_local_index() {
     if ((rc = d_claim.reserve(N * maxph))) return rc;
     if ((rc = d_pgain.reserve(N * maxph))) return rc;
     if ((rc = d_lprop.reserve(N * maxph))) return rc;
+    if ((rc = d_sv.reserve(N * K))) return rc;
+    if ((rc = d_hot.reserve(N * K))) return rc;
+    AMG_CUDA(cudaMemsetAsync(d_hot.p, 0, N * K, stream));
     if ((rc = d_lk.reserve(N))) return rc;
     if ((rc = d_lv.reserve(N))) return rc;
     if ((rc = d_tk.reserve(N))) return rc;
@@ -858,7 +863,7 @@ int Engine::ensure_local_index() {
     for (uint32_t c = 0; c < C; ++c) w1[c] = widths[c] <= 1;
     AMG_CUDA(cudaMemcpyAsync(d_chain_w1.p, w1.data(), w1.size(), cudaMemcpyHostToDevice, stream));
     lix.slot_pt = d_slot_pt.p; lix.col = d_col.p; lix.slot_of = d_slot_of.p; lix.cell_start = d_cell_start.p;
-    lix.chain_id = d_chain_id.p; lix.chain_w1 = d_chain_w1.p;
+    lix.chain_id = d_chain_id.p; lix.chain_w1 = d_chain_w1.p; lix.sv = d_sv.p;
     rc = local_index_build(lix, d_P.p, N, K, CW, CH, d_chain_off.p, C, d_lk.p, d_lv.p, d_tk.p, d_tv.p, d_hist.p,
                            stream);
     if (rc) return rc;
@@ -873,11 +878,13 @@ int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
     }
     int rc = ensure_local_index();
     if (rc) return rc;
+    size_t maxph = 0;
+    for (auto &p : phases_for(K)) maxph = std::max(maxph, p.size());
     if (active.proposal == AM_PROPOSAL_LEARNED) {
         if ((rc = mlp_init())) return rc;
-        size_t maxph = 0;
-        for (auto &p : phases_for(K)) maxph = std::max(maxph, p.size());
-        if ((rc = d_cost_cache.reserve(N * maxph))) return rc;
+        if ((rc = d_sel.reserve(N * maxph))) return rc;
+        if ((rc = d_nsel.reserve(1))) return rc;
+        if (recording && (rc = d_rec_idx.reserve(N * maxph))) return rc;
     }
     if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * sweeps + 4)))) return rc;
     AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * sweeps * 8, stream));
@@ -892,14 +899,16 @@ int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
             a.chain_w1 = lix.chain_w1; a.cap = active.local_target;
             a.self_cap = active.local_self; a.nrandom = active.local_random; a.chain_off = d_chain_off.p;
             a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p ^ 0x5bd1e995ULL);
-            a.claim = d_claim.p; a.prop = d_lprop.p; a.pgain = d_pgain.p;
+            a.claim = d_claim.p; a.prop = d_lprop.p; a.pgain = d_pgain.p; a.sv = d_sv.p; a.hot = d_hot.p;
+            a.single_chain = C == 1;
             a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
             if (active.proposal == AM_PROPOSAL_LEARNED) {
-                a.mlp = d_mlp_dep.p; a.cost_cache = d_cost_cache.p; a.display = d_display.p;
-                a.CW = CW; a.CH = CH; a.topk = active.learned_topk; a.err = d_err.p;
+                a.mlp = d_mlp_dep.p; a.keep = (float)active.learned_keep; a.err = d_err.p;
+                a.cost_scale = log1pf((float)((double)cost_exact / ((double)N * K) / kGainScale));
+                a.sel_out = d_sel.p; a.nsel_out = d_nsel.p;
                 if (recording) {
                     a.rec_feat = d_rec_feat.p; a.rec_gain = d_rec_gain.p; a.rec_count = d_rec_count.p;
-                    a.rec_cap = rec_cap;
+                    a.rec_cap = rec_cap; a.rec_idx = d_rec_idx.p;
                 }
             }
             prof.open(stream);

@@ -31,8 +31,9 @@ struct Params {  // defaults of morph.h:97-119
     unsigned proposal = AM_PROPOSAL_RANDOM;
     size_t sweeps = 1;
     // guided-refinement tunables (am_set_tuning; chosen by the autotuner)
-    uint32_t local_self = 12, local_target = 8, local_random = 2, learned_topk = 2;
-    double guided_switch = 1e-4;  // plain -> guided when a plain sweep gains less than this fraction
+    uint32_t local_self = 12, local_target = 8, local_random = 2;
+    double learned_keep = 0.25;  // fraction of slots the learned gate lets scan
+    double guided_switch = 1e-3;  // plain -> guided when a plain sweep gains less than this fraction
     double motion_noise = 0.0;
 };
 
@@ -53,6 +54,10 @@ template <class T>
 struct DBuf {
     T *p = nullptr;
     size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
     int reserve(size_t count) {
         if (count <= n) return AM_OK;
         if (p) cudaFree(p);
@@ -74,6 +79,10 @@ struct DBuf {
         n = 0;
     }
 };
+
+// Frames refined together (never adjacent): K=2 {0},{1}; even K evens, odds;
+// odd K evens except the last, odds, the last.
+std::vector<std::vector<uint32_t>> phases_for(uint32_t K);
 
 class Engine {
   public:
@@ -122,6 +131,7 @@ class Engine {
     uint64_t N = 0;
     std::vector<uint64_t> widths, chain_off, pair_off, singles;
     uint64_t sweep_counter = 0;
+    uint64_t layout_version = 0;           // bumped whenever the chain layout changes
     uint64_t cost_exact = 0;               // exact cost after the last refinement step
     bool cost_valid = false;
 
@@ -157,7 +167,10 @@ class Engine {
     DBuf<uint64_t> d_slot_pt;
     DBuf<uint32_t> d_col, d_slot_of, d_cell_start, d_chain_id, d_lprop, d_lk, d_lv;
     DBuf<uint8_t> d_chain_w1;
-    DBuf<unsigned long long> d_claim, d_pgain;
+    DBuf<unsigned long long> d_claim, d_pgain, d_nsel;
+    DBuf<uint64_t> d_sv;
+    DBuf<uint8_t> d_hot;
+    DBuf<uint32_t> d_sel, d_rec_idx;
     int ensure_local_index();
 
     Prof prof;
@@ -193,7 +206,7 @@ class Engine {
     // proposal network (engine_mlp.cpp)
     DBuf<float> d_mlp_master, d_mlp_dep, d_mlp_grad, d_adam_m, d_adam_v, d_mlp_loss, d_rec_feat, d_rec_gain;
     DBuf<float> d_io_a, d_io_b;
-    DBuf<unsigned long long> d_rec_count, d_cost_cache;
+    DBuf<unsigned long long> d_rec_count;
     DBuf<int> d_err;
     uint64_t rec_cap = 0, adam_t = 0;
     bool recording = false;

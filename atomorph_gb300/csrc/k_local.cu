@@ -12,13 +12,16 @@
 //   slot_of[y][x]   slot currently held by column x
 // A column x1 at frame y costs d(p1,a1)+d(a1,n1) with p1/n1 its points at the
 // neighbouring frames; it is cheapest where its point sits at m1 = (p1+n1)/2.
+// The index also holds s = p + n of the column at every slot, in slot order
+// (k_slot_sums once, then kept current by the apply kernel); the six-point
+// criterion (thread.cpp:1014-1022) of a swap is exactly
+// 2 (a1 - a2) . (s2 - s1) (pair_gain), so a candidate costs two reads from
+// the same slot-ordered arrays its cell window lives in.
 // Candidates come from the column's own neighbourhood, the cell of m1 and a
-// few uniform random columns (k_local_propose); every
-// candidate's gain is the reference's exact six-point criterion
-// (thread.cpp:1014-1022) in integers.  Each column proposes its best strictly
-// improving partner and claims both columns with atomicMax on
-// (gain, proposer); a proposal is applied when it holds the claim of both
-// columns, so applied swaps are disjoint and every applied gain is exact.
+// few uniform random columns (k_local_propose).  Each slot proposes its best
+// strictly improving partner slot and claims both with atomicMax on
+// (gain, proposer slot); a proposal is applied when it holds the claim of
+// both slots, so applied swaps are disjoint and every applied gain is exact.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -62,26 +65,51 @@ __global__ void k_chain_ids(const uint64_t *__restrict__ off, uint32_t C, uint64
     }
 }
 
-__device__ __forceinline__ int64_t swap_gain(uint64_t p1, uint64_t a1, uint64_t n1, uint64_t p2, uint64_t a2,
-                                             uint64_t n2) {
-    uint64_t c1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
-    uint64_t c2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);
-    return (int64_t)c1 - (int64_t)c2;
+// Target sums of the columns holding the slots: sv[y][s] = p + n for the
+// column x at slot s of frame y, with p, n its points at frames y-1 and y+1
+// (1/256 px; x in the low word, y in the high word).  Built once with the
+// index; afterwards k_local_apply keeps it current: a swap at frame y moves
+// the two columns' sums at frame y to their new slots and changes the two
+// columns' sums at frames y-1 and y+1 by the exchanged points' difference.
+__global__ void __launch_bounds__(256) k_slot_sums(const uint64_t *__restrict__ P, const uint32_t *__restrict__ col,
+                                                   uint64_t N, uint32_t K, uint64_t *sv) {
+    const uint64_t total = N * K;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t y = (uint32_t)(t / N);
+        uint32_t yn = y + 1 == K ? 0 : y + 1, yp = y == 0 ? K - 1 : y - 1;
+        uint32_t x = col[t];
+        uint64_t p = P[(uint64_t)yp * N + x], n = P[(uint64_t)yn * N + x];
+        sv[t] = sums_pack(pt_X(p) + pt_X(n), pt_Y(p) + pt_Y(n));
+    }
+}
+
+// sv[i] += (dx, dy) with one 32-bit atomic per half: two frames of one phase
+// (y-1 and y+1 around a frame y) may update the same entry concurrently.
+__device__ __forceinline__ void sums_add(uint64_t *sv, uint64_t i, int32_t dx, int32_t dy) {
+    unsigned *w = reinterpret_cast<unsigned *>(sv + i);
+    if (dx) atomicAdd(w, (unsigned)dx);
+    if (dy) atomicAdd(w + 1, (unsigned)dy);
 }
 
 // Monotone key: positive gains order like their float value; ties broken by
-// the proposer's index.
-__device__ __forceinline__ unsigned long long claim_key(int64_t gain, uint32_t x1) {
+// the proposer's slot.
+__device__ __forceinline__ unsigned long long claim_key(int64_t gain, uint32_t s1) {
     float g = (float)gain;
-    return ((unsigned long long)__float_as_uint(g) << 32) | x1;
+    return ((unsigned long long)__float_as_uint(g) << 32) | s1;
 }
 
+struct Col {        // the proposing column
+    uint32_t s1;    // its slot
+    uint64_t a1;    // its point
+    uint64_t S1;    // its target sum
+    uint64_t lo, hi;// its chain's column range
+};
+
 // Scans up to `cap` slots of cell (qx, qy) starting at a hashed offset and
-// keeps the best strictly improving partner.
+// keeps the best strictly improving partner slot.
 __device__ __forceinline__ void scan_cell(const LocalArgs &a, const uint32_t *cs, const uint64_t *spt,
-                                          const uint32_t *col, const uint64_t *Pp, const uint64_t *Pn, int qx, int qy,
-                                          uint32_t cap, uint32_t h, uint32_t x1, uint32_t c, uint64_t p1,
-                                          uint64_t a1, uint64_t n1, int64_t &best, uint32_t &bx) {
+                                          const uint32_t *col, const uint64_t *sv, int qx, int qy, uint32_t cap,
+                                          uint32_t h, const Col &c, int64_t &best, uint32_t &bs) {
     if (qx < 0 || qy < 0 || qx >= (int)a.ncx || qy >= (int)a.ncy || cap == 0) return;
     uint32_t cell = (uint32_t)qy * a.ncx + (uint32_t)qx;
     uint32_t beg = cs[cell], n = cs[cell + 1] - beg;
@@ -89,103 +117,145 @@ __device__ __forceinline__ void scan_cell(const LocalArgs &a, const uint32_t *cs
     uint32_t take = min(n, cap), start = n > cap ? h % n : 0;
     for (uint32_t j = 0; j < take; ++j) {
         uint32_t s = beg + (start + j) % n;
+        if (s == c.s1) continue;
         uint32_t x2 = col[s];
-        if (x2 == x1 || a.chain_id[x2] != c) continue;
-        int64_t g = swap_gain(p1, a1, n1, Pp[x2], spt[s], Pn[x2]);
-        if (g > best) { best = g; bx = x2; }
+        if (x2 < c.lo || x2 >= c.hi) continue;
+        int64_t g = pair_gain(c.a1, c.S1, spt[s], sv[s]);
+        if (g > best) { best = g; bs = s; }
     }
 }
 
-// Candidates of column x1 at frame y, all checked with the exact criterion:
-//   * the column's own neighbourhood (the cell of its point a1 and the four
-//     cells around it): resolves the local crossings left after the coarse
-//     transport is right, which uniform pairs almost never sample at large N;
-//   * the cell of its target m1: moves a column straight to where its
+// Candidates of the column at slot s1 of frame y, all checked with the exact
+// criterion:
+//   * the column's own neighbourhood (the cell of its point a1 and two of the
+//     four cells around it): resolves the local crossings left after the
+//     coarse transport is right, which uniform pairs almost never sample at
+//     large N;
+//   * the cell of its target m1 = S1/2: moves a column straight to where its
 //     neighbours in the other key frames pull it;
 //   * a few uniform random columns of the same chain: the reference's own
 //     proposal, for the coarse, long-range part.
+// Slot-major: a column reads its own point and target sum, and those of its
+// cell-window candidates, from slot-ordered arrays (coalesced, L2-resident
+// windows); only the random candidates are scattered loads.  With `sel` set
+// only the listed slots propose (the learned gate's choice).
 __global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
     const uint64_t N = a.N;
-    const uint64_t total = N * a.nframes;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t total = a.sel ? (uint64_t)*a.nsel : N * a.nframes;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t t = a.sel ? (uint64_t)a.sel[i] : i;
         uint32_t fi = (uint32_t)(t / N);
-        uint32_t x1 = (uint32_t)(t - (uint64_t)fi * N);
+        Col c;
+        c.s1 = (uint32_t)(t - (uint64_t)fi * N);
         uint32_t y = a.frames[fi];
-        uint32_t yn = y + 1 == a.K ? 0 : y + 1, yp = y == 0 ? a.K - 1 : y - 1;
-        const uint64_t *Py = a.P + (uint64_t)y * N, *Pp = a.P + (uint64_t)yp * N, *Pn = a.P + (uint64_t)yn * N;
-        a.prop[t] = 0xFFFFFFFFu;
-        uint32_t c = a.chain_id[x1];
-        if (a.chain_w1[c]) continue;  // width-1 chains do not refine (thread.cpp:1045)
-        uint64_t a1 = Py[x1], p1 = Pp[x1], n1 = Pn[x1];
-        const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
         const uint64_t *spt = a.slot_pt + (uint64_t)y * N;
         const uint32_t *col = a.col + (uint64_t)y * N;
+        const uint64_t *sv = a.sv + (uint64_t)y * N;
+        a.prop[t] = 0xFFFFFFFFu;
+        uint32_t x1 = col[c.s1];
+        uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
+        if (a.chain_w1[ch]) continue;  // width-1 chains do not refine (thread.cpp:1045)
+        c.a1 = spt[c.s1];
+        c.S1 = sv[c.s1];
+        c.lo = a.single_chain ? 0ull : a.chain_off[ch];
+        c.hi = a.single_chain ? N : a.chain_off[ch + 1];
+        const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
         int64_t best = 0;
-        uint32_t bx = 0xFFFFFFFFu;
-        uint32_t h = mix32((uint32_t)a.key ^ mix32(x1 * 0x9E3779B1u + y));
-        // own neighbourhood: centre cell, then the 4-neighbour cells
-        int ax = (int)min((uint32_t)pt_X(a1) >> 9, a.ncx - 1), ay = (int)min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1);
+        uint32_t bs = 0xFFFFFFFFu;
+        uint32_t h = mix32((uint32_t)a.key ^ mix32(c.s1 * 0x9E3779B1u + y));
+        // own neighbourhood: centre cell, then two of the 4-neighbour cells
+        int ax = (int)min((uint32_t)pt_X(c.a1) >> 9, a.ncx - 1), ay = (int)min((uint32_t)pt_Y(c.a1) >> 9, a.ncy - 1);
         if (a.self_cap) {
             uint32_t per = max(1u, a.self_cap / 3u);
-            scan_cell(a, cs, spt, col, Pp, Pn, ax, ay, per, h, x1, c, p1, a1, n1, best, bx);
-            const int dx4[4] = {1, -1, 0, 0}, dy4[4] = {0, 0, 1, -1};
+            scan_cell(a, cs, spt, col, sv, ax, ay, per, h, c, best, bs);
             uint32_t r0 = h >> 28;
+#pragma unroll
             for (int k = 0; k < 2; ++k) {
-                int d = (int)((r0 + 2u * k) & 3u);
-                scan_cell(a, cs, spt, col, Pp, Pn, ax + dx4[d], ay + dy4[d], per, h >> 3, x1, c, p1, a1, n1, best, bx);
+                int d = (int)((r0 + 2u * k) & 3u);  // 0..3: +x, -x, +y, -y
+                int dx = d == 0 ? 1 : (d == 1 ? -1 : 0), dy = d == 2 ? 1 : (d == 3 ? -1 : 0);
+                scan_cell(a, cs, spt, col, sv, ax + dx, ay + dy, per, h >> 3, c, best, bs);
             }
         }
         // target cell
         if (a.cap) {
-            int32_t mx = (pt_X(p1) + pt_X(n1)) >> 1, my = (pt_Y(p1) + pt_Y(n1)) >> 1;
+            int32_t mx = sums_x(c.S1) >> 1, my = sums_y(c.S1) >> 1;
             int cx = (int)min((uint32_t)max(mx, 0) >> 9, a.ncx - 1), cy = (int)min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
-            scan_cell(a, cs, spt, col, Pp, Pn, cx, cy, a.cap, h >> 5, x1, c, p1, a1, n1, best, bx);
+            scan_cell(a, cs, spt, col, sv, cx, cy, a.cap, h >> 5, c, best, bs);
         }
         // uniform random partners in the same chain
         if (a.nrandom) {
-            uint64_t off = a.chain_off[c];
-            uint32_t w = (uint32_t)(a.chain_off[c + 1] - off);
+            uint32_t w = (uint32_t)(c.hi - c.lo);
+            const uint32_t *slot_of = a.slot_of + (uint64_t)y * N;
             uint32_t r = h;
             for (uint32_t k = 0; k < a.nrandom; ++k) {
                 r = mix32(r + 0x68E31DA4u);
-                uint32_t x2 = (uint32_t)off + r % w;
+                uint32_t x2 = (uint32_t)c.lo + r % w;
                 if (x2 == x1) continue;
-                int64_t g = swap_gain(p1, a1, n1, Pp[x2], Py[x2], Pn[x2]);
-                if (g > best) { best = g; bx = x2; }
+                uint32_t s = slot_of[x2];
+                int64_t g = pair_gain(c.a1, c.S1, spt[s], sv[s]);
+                if (g > best) { best = g; bs = s; }
             }
         }
-        if (bx != 0xFFFFFFFFu) {
-            unsigned long long k = claim_key(best, x1);
-            a.prop[t] = bx;
+        if (a.hot) a.hot[(uint64_t)y * N + c.s1] = gain_bucket(best);
+        if (a.rec_idx) {
+            uint32_t j = a.rec_idx[t];
+            if (j != 0xFFFFFFFFu) a.rec_gain[j] = log1pf((float)best / kGainScale);
+        }
+        if (bs != 0xFFFFFFFFu) {
+            unsigned long long k = claim_key(best, c.s1);
+            a.prop[t] = bs;
             a.pgain[t] = (unsigned long long)best;
-            atomicMax(a.claim + (uint64_t)fi * N + x1, k);
-            atomicMax(a.claim + (uint64_t)fi * N + bx, k);
+            atomicMax(a.claim + (uint64_t)fi * N + c.s1, k);
+            atomicMax(a.claim + (uint64_t)fi * N + bs, k);
         }
     }
 }
 
+// A proposal (s1 -> s2) is applied when it holds the claim of both slots:
+// applied swaps are then disjoint, so the columns at s1 and s2 are read and
+// written by this thread alone.
 __global__ void __launch_bounds__(256) k_local_apply(LocalArgs a) {
     const uint64_t N = a.N;
-    const uint64_t total = N * a.nframes;
+    const uint64_t total = a.sel ? (uint64_t)*a.nsel : N * a.nframes;
     unsigned long long gain = 0, acc = 0;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t x2 = a.prop[t];
-        if (x2 == 0xFFFFFFFFu) continue;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t t = a.sel ? (uint64_t)a.sel[i] : i;
+        uint32_t s2 = a.prop[t];
+        if (s2 == 0xFFFFFFFFu) continue;
         uint32_t fi = (uint32_t)(t / N);
-        uint32_t x1 = (uint32_t)(t - (uint64_t)fi * N);
-        unsigned long long k1 = a.claim[(uint64_t)fi * N + x1], k2 = a.claim[(uint64_t)fi * N + x2];
-        if (k1 != k2 || (uint32_t)k1 != x1) continue;
+        uint32_t s1 = (uint32_t)(t - (uint64_t)fi * N);
+        unsigned long long k1 = a.claim[(uint64_t)fi * N + s1], k2 = a.claim[(uint64_t)fi * N + s2];
+        if (k1 != k2 || (uint32_t)k1 != s1) continue;
         uint32_t y = a.frames[fi];
         uint64_t *Py = a.P + (uint64_t)y * N;
         uint32_t *slot_of = a.slot_of + (uint64_t)y * N, *col = a.col + (uint64_t)y * N;
+        uint32_t x1 = col[s1], x2 = col[s2];
         uint64_t w1 = Py[x1], w2 = Py[x2];
         Py[x1] = w2;
         Py[x2] = w1;
-        uint32_t s1 = slot_of[x1], s2 = slot_of[x2];
         slot_of[x1] = s2;
         slot_of[x2] = s1;
         col[s1] = x2;
         col[s2] = x1;
+        // The sums at frame y follow their columns to the other slot (no
+        // other thread touches slots s1, s2 of frame y in this phase).
+        uint64_t *svy = a.sv + (uint64_t)y * N;
+        const uint64_t t1 = svy[s1];
+        svy[s1] = svy[s2];
+        svy[s2] = t1;
+        // x1 now holds w2 and x2 holds w1 at frame y: their target sums at the
+        // neighbouring frames move by the difference (twice for K = 2, where
+        // y-1 and y+1 are the same frame and s = 2 p).
+        if (a.K > 1) {
+            const int32_t dx = pt_X(w2) - pt_X(w1), dy = pt_Y(w2) - pt_Y(w1);
+            const uint32_t yn = y + 1 == a.K ? 0 : y + 1, yp = y == 0 ? a.K - 1 : y - 1;
+            for (int side = 0; side < 2; ++side) {
+                const uint64_t yy = side ? yn : yp;
+                const uint32_t *so = a.slot_of + yy * N;
+                sums_add(a.sv, yy * N + so[x1], dx, dy);
+                sums_add(a.sv, yy * N + so[x2], -dx, -dy);
+            }
+        }
         gain += a.pgain[t];
         acc += 1;
     }
@@ -221,7 +291,17 @@ int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K,
         if (rc) return rc;
     }
     AMG_LAUNCH(k_chain_ids, grid, 256, 0, s, chain_off, C, N, ix.chain_id);
+    unsigned g2 = (unsigned)std::min<uint64_t>((N * K + 255) / 256, (uint64_t)kSMs * 8);
+    AMG_LAUNCH(k_slot_sums, g2, 256, 0, s, P, ix.col, N, K, ix.sv);
     AMG_CUDA(cudaGetLastError());
+    return AM_OK;
+}
+
+int launch_local_propose(const LocalArgs &a, cudaStream_t s) {
+    uint64_t total = a.N * a.nframes;
+    if (!total) return AM_OK;
+    unsigned grid = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)kSMs * 8);
+    AMG_LAUNCH(k_local_propose, grid, 256, 0, s, a);
     return AM_OK;
 }
 
@@ -238,11 +318,9 @@ int launch_local_phase(const LocalArgs &a, cudaStream_t s) {
     uint64_t total = a.N * a.nframes;
     if (!total) return AM_OK;
     AMG_CUDA(cudaMemsetAsync(a.claim, 0, total * sizeof(unsigned long long), s));
-    unsigned grid = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)kSMs * 8);
-    AMG_LAUNCH(k_local_propose, grid, 256, 0, s, a);
-    AMG_LAUNCH(k_local_apply, grid, 256, 0, s, a);
-    AMG_CUDA(cudaGetLastError());
-    return AM_OK;
+    int rc = launch_local_propose(a, s);
+    if (!rc) rc = launch_local_apply(a, s);
+    return rc;
 }
 
 }  // namespace amg

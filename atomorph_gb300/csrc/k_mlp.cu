@@ -11,14 +11,13 @@
 // the error flag instead of spinning); each warp reads its own 32 TMEM lanes
 // with tcgen05.ld.
 //
-// Features of a candidate pair (column x1 at key frame y, candidate column x2
-// holding point a2), S = 16 px in 1/256 units:
-//   0,1  (a2 - m1) / S, m1 = midpoint of x1's points at the neighbouring frames
-//   2-5  (colour(a2) - colour(a1)) / 255, RGBA of the key frame's pixels
-//   6,7  log1p(cost of column x1 / S^2), same for column x2
-//   8    parity of the chain (blob group) id
-//   9    log1p(|a1 - a2|^2 / S^2)
-// Target: sign(g) * log1p(|g| / S^2) with g the exact swap gain.
+// As a swap proposal the network is a gate in front of the guided candidate
+// scan (k_local.cu): it scores every column of a phase from features of the
+// column alone (gate_features below), and only the best-scored fraction of
+// each 32-column group runs the scan.  Its training target is
+// log1p(g / S^2), g the best exact gain the full scan found for the column,
+// S = 16 px in 1/256 px units; samples come from the refinement itself
+// (am_record_swaps).
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -469,196 +468,100 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, int n, floa
     }
 }
 
-// ----------------------------------------------- learned proposal kernel --
-__global__ void __launch_bounds__(256) k_cost_cache(LocalArgs a) {
-    const uint64_t N = a.N, total = N * a.nframes;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t fi = (uint32_t)(t / N);
-        uint64_t x = t - (uint64_t)fi * N;
-        uint32_t y = a.frames[fi];
-        uint32_t yn = y + 1 == a.K ? 0 : y + 1, yp = y == 0 ? a.K - 1 : y - 1;
-        uint64_t p = a.P[(uint64_t)yp * N + x], c = a.P[(uint64_t)y * N + x], q = a.P[(uint64_t)yn * N + x];
-        a.cost_cache[t] = pt_dist(p, c) + pt_dist(c, q);
-    }
+// ----------------------------------------------- learned proposal gate --
+// Features of the column at slot s1 of frame y, from data the guided scan
+// reads anyway (coalesced, slot order) — no candidate is touched:
+//   0,1  displacement of its point from its target m1 = S1/2, /16 px (clamped)
+//   2    log1p(|a1 - m1|^2 / (16 px)^2)
+//   3,4  log1p(points in its own cell), log1p(points in its target cell)
+//   5    1 when the target cell is its own cell
+//   6    gain bucket of the slot's last scan (log2 of the best gain) / 16
+//   7    log1p(mean column cost / (16 px)^2): how far refinement has come
+//   8    log1p(chain width) / 16
+//   9    0 (spare)
+__device__ __forceinline__ bool gate_features(const LocalArgs &a, uint64_t t, float *f) {
+    const uint64_t N = a.N;
+    uint32_t fi = (uint32_t)(t / N);
+    uint32_t s1 = (uint32_t)(t - (uint64_t)fi * N);
+    uint32_t y = a.frames[fi];
+    uint32_t x1 = a.col[(uint64_t)y * N + s1];
+    uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
+    if (a.chain_w1[ch]) return false;
+    uint64_t a1 = a.slot_pt[(uint64_t)y * N + s1], S1 = a.sv[(uint64_t)y * N + s1];
+    float dx = (float)pt_X(a1) - 0.5f * (float)sums_x(S1), dy = (float)pt_Y(a1) - 0.5f * (float)sums_y(S1);
+    f[0] = fminf(fmaxf(dx / kS, -8.f), 8.f);
+    f[1] = fminf(fmaxf(dy / kS, -8.f), 8.f);
+    f[2] = log1pf((dx * dx + dy * dy) / kS2);
+    const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
+    uint32_t ax = min((uint32_t)pt_X(a1) >> 9, a.ncx - 1), ay = min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1);
+    int32_t mx = sums_x(S1) >> 1, my = sums_y(S1) >> 1;
+    uint32_t tx = min((uint32_t)max(mx, 0) >> 9, a.ncx - 1), ty = min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
+    uint32_t own = ay * a.ncx + ax, tgt = ty * a.ncx + tx;
+    f[3] = log1pf((float)(cs[own + 1] - cs[own]));
+    f[4] = log1pf((float)(cs[tgt + 1] - cs[tgt]));
+    f[5] = own == tgt ? 1.f : 0.f;
+    f[6] = (float)a.hot[(uint64_t)y * N + s1] * (1.f / 16.f);
+    f[7] = a.cost_scale;
+    f[8] = log1pf((float)(a.chain_off[ch + 1] - a.chain_off[ch])) * (1.f / 16.f);
+    f[9] = 0.f;
+    return true;
 }
 
-__device__ __forceinline__ float slog1p(float x) { return x >= 0.f ? log1pf(x) : -log1pf(-x); }
-
-// Warp-collective: lanes [lo, hi) each take one slot of the 5-cell window
-// (centre and its 4 neighbours) around cell (cx, cy); when the window holds
-// more slots than lanes, the start rotates by `rot`.  Returns whether the
-// calling lane got a slot.
-__device__ __forceinline__ bool window_slot(const uint32_t *cs, int cx, int cy, uint32_t ncx, uint32_t ncy, int lane,
-                                            int lo, int hi, uint32_t rot, uint32_t *slot) {
-    uint32_t beg = 0, cnt = 0;
-    if (lane < 5) {
-        int qx = cx + (lane == 1 ? 1 : (lane == 2 ? -1 : 0));
-        int qy = cy + (lane == 3 ? 1 : (lane == 4 ? -1 : 0));
-        if (qx >= 0 && qy >= 0 && qx < (int)ncx && qy < (int)ncy) {
-            uint32_t cell = (uint32_t)qy * ncx + (uint32_t)qx;
-            beg = cs[cell];
-            cnt = cs[cell + 1] - beg;
-        }
-    }
-    uint32_t pre = cnt;
-#pragma unroll
-    for (int o = 1; o < 8; o <<= 1) {
-        uint32_t u = __shfl_up_sync(0xffffffffu, pre, o);
-        if (lane >= o) pre += u;
-    }
-    uint32_t total = __shfl_sync(0xffffffffu, pre, 4);
-    uint32_t j = (uint32_t)(lane - lo);
-    bool mine = lane >= lo && lane < hi && j < total;
-    if (total > (uint32_t)(hi - lo) && total) j = (j + rot % total) % total;
-    uint32_t ksel = 5;
-#pragma unroll
-    for (int k = 4; k >= 0; --k) {
-        uint32_t pk = __shfl_sync(0xffffffffu, pre, k);
-        if (j < pk) ksel = (uint32_t)k;
-    }
-    uint32_t src = ksel < 5 ? ksel : 0u;
-    uint32_t bk = __shfl_sync(0xffffffffu, beg, src);
-    uint32_t pprev = __shfl_sync(0xffffffffu, pre, src > 0 ? src - 1 : 0);
-    if (src == 0) pprev = 0;
-    *slot = bk + (j - pprev);
-    return mine && ksel < 5;
-}
-
-struct PropSmem {
-    FwdSmem f;
-};
-
-// One warp per column, 32 candidates per column from the 3x3 cells around
-// the column's target; 4 columns = one 128-row MMA tile.
-__global__ void __launch_bounds__(128) k_learned_propose(LocalArgs a) {
+// One CTA scores 128 consecutive slots per tile (one MMA tile; four warps of
+// 32 slots).  Each warp lists its `keep` best-scored eligible slots; while
+// recording, every eligible slot is listed and its features logged.
+__global__ void __launch_bounds__(128) k_learned_gate(LocalArgs a) {
     extern __shared__ __align__(1024) uint8_t smraw[];
-    PropSmem &s = *reinterpret_cast<PropSmem *>(smraw);
-    fwd_setup(s.f, a.mlp);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint64_t N = a.N, total = N * a.nframes;
-    const uint64_t ntiles = (total + 3) / 4;
+    FwdSmem &s = *reinterpret_cast<FwdSmem *>(smraw);
+    fwd_setup(s, a.mlp);
+    const int lane = threadIdx.x & 31;
+    const uint64_t total = a.N * a.nframes;
+    const uint64_t ntiles = (total + kTM - 1) / kTM;
+    const int kk = max(1, min(32, (int)ceilf(a.keep * 32.f)));
+    const bool rec = a.rec_idx != nullptr;
     uint32_t phase = 0;
-    const size_t fr = (size_t)a.CW * a.CH;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        uint64_t t = tile * 4 + warp;
-        bool colok = t < total;
-        uint32_t fi = 0, x1 = 0, y = 0, yp = 0, yn = 0, c = 0;
-        uint64_t a1 = 0, p1 = 0, n1 = 0;
-        bool cand = false;
-        uint32_t x2 = 0xFFFFFFFFu, s2 = 0;
-        uint64_t a2w = 0;
-        float feats[kMlpIn];
+        uint64_t t = tile * kTM + threadIdx.x;
+        float f[kMlpIn];
 #pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) feats[k] = 0.f;
-        if (colok) {
-            fi = (uint32_t)(t / N);
-            x1 = (uint32_t)(t - (uint64_t)fi * N);
-            y = a.frames[fi];
-            yn = y + 1 == a.K ? 0 : y + 1;
-            yp = y == 0 ? a.K - 1 : y - 1;
-            c = a.chain_id[x1];
-            if (lane == 0) a.prop[t] = 0xFFFFFFFFu;
-            if (!a.chain_w1[c]) {
-                a1 = a.P[(uint64_t)y * N + x1];
-                p1 = a.P[(uint64_t)yp * N + x1];
-                n1 = a.P[(uint64_t)yn * N + x1];
-                int32_t mx = (pt_X(p1) + pt_X(n1)) >> 1, my = (pt_Y(p1) + pt_Y(n1)) >> 1;
-                int tx = (int)min((uint32_t)max(mx, 0) >> 9, a.ncx - 1);
-                int ty = (int)min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
-                int ox = (int)min((uint32_t)pt_X(a1) >> 9, a.ncx - 1);
-                int oy = (int)min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1);
-                const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
-                uint32_t hh = mix32((uint32_t)a.key ^ mix32(x1 * 0x9E3779B1u + y));
-                // lanes 0-15: own neighbourhood, 16-27: target window, 28-31: random
-                uint32_t sA, sB;
-                bool vA = window_slot(cs, ox, oy, a.ncx, a.ncy, lane, 0, 16, hh, &sA);
-                bool vB = window_slot(cs, tx, ty, a.ncx, a.ncy, lane, 16, 28, hh >> 7, &sB);
-                if (vA || vB) {
-                    s2 = vA ? sA : sB;
-                    x2 = a.col[(uint64_t)y * N + s2];
-                    a2w = a.slot_pt[(uint64_t)y * N + s2];
-                } else if (lane >= 28) {
-                    uint64_t off = a.chain_off[c];
-                    uint32_t w = (uint32_t)(a.chain_off[c + 1] - off);
-                    x2 = (uint32_t)off + mix32(hh + (uint32_t)lane * 0x68E31DA4u) % w;
-                    a2w = a.P[(uint64_t)y * N + x2];
+        for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
+        bool elig = t < total && gate_features(a, t, f);
+        write_features(s.A1, threadIdx.x, f);
+        float score = forward_tile(s, phase, a.err);
+        bool keep;
+        if (rec) {
+            keep = elig;
+            if (t < total) {
+                uint32_t j = 0xFFFFFFFFu;
+                if (elig) {
+                    unsigned long long r = atomicAdd(a.rec_count, 1ull);
+                    if (r < a.rec_cap) {
+                        j = (uint32_t)r;
+#pragma unroll
+                        for (int k = 0; k < kMlpIn; ++k) a.rec_feat[r * kMlpIn + k] = f[k];
+                    }
                 }
-                cand = x2 != 0xFFFFFFFFu && x2 != x1 && a.chain_id[x2] == c;
-                if (cand) {
-                    uint64_t a2 = a2w;
-                    uint32_t col1 = a.display[(size_t)y * fr + (size_t)pt_y(a1) * a.CW + pt_x(a1)];
-                    uint32_t col2 = a.display[(size_t)y * fr + (size_t)pt_y(a2) * a.CW + pt_x(a2)];
-                    float c1 = (float)a.cost_cache[(uint64_t)fi * N + x1];
-                    float c2 = (float)a.cost_cache[(uint64_t)fi * N + x2];
-                    feats[0] = fminf(fmaxf((float)(pt_X(a2) - mx) / kS, -8.f), 8.f);
-                    feats[1] = fminf(fmaxf((float)(pt_Y(a2) - my) / kS, -8.f), 8.f);
-#pragma unroll
-                    for (int ch = 0; ch < 4; ++ch)
-                        feats[2 + ch] = ((float)((col2 >> (8 * ch)) & 255u) - (float)((col1 >> (8 * ch)) & 255u)) / 255.f;
-                    feats[6] = log1pf(c1 / kS2);
-                    feats[7] = log1pf(c2 / kS2);
-                    feats[8] = (float)(c & 1u);
-                    feats[9] = log1pf((float)pt_dist(a1, a2) / kS2);
-                }
+                a.rec_idx[t] = j;
             }
+        } else {
+            if (!elig) score = -INFINITY;
+            int rank = 0;
+#pragma unroll 8
+            for (int j = 0; j < 32; ++j) {
+                float o = __shfl_sync(0xffffffffu, score, j);
+                rank += (o > score) || (o == score && j < lane);
+            }
+            keep = elig && rank < kk;
         }
-        write_features(s.f.A1, threadIdx.x, feats);
-        float score = forward_tile(s.f, phase, a.err);
-        if (!cand) score = -INFINITY;
-        // Optional sample log: exact gain of every candidate.
-        if (a.rec_count && cand) {
-            int64_t g = 0;
-            {
-                uint64_t a2 = a2w;
-                uint64_t p2 = a.P[(uint64_t)yp * N + x2], n2 = a.P[(uint64_t)yn * N + x2];
-                uint64_t cc1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
-                uint64_t cc2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);
-                g = (int64_t)cc1 - (int64_t)cc2;
-            }
-            unsigned long long slot = atomicAdd(a.rec_count, 1ull);
-            if (slot < a.rec_cap) {
-#pragma unroll
-                for (int k = 0; k < kMlpIn; ++k) a.rec_feat[slot * kMlpIn + k] = feats[k];
-                a.rec_gain[slot] = slog1p((float)g / kS2);
-            }
-        }
-        // Top-k by score, then the exact criterion decides.
-        int64_t best = 0;
-        uint32_t bx = 0xFFFFFFFFu;
-        float sc = score;
-        for (uint32_t k = 0; k < a.topk; ++k) {
-            float m = sc;
-            int ml = lane;
-#pragma unroll
-            for (int o = 16; o; o >>= 1) {
-                float om = __shfl_xor_sync(0xffffffffu, m, o);
-                int ol = __shfl_xor_sync(0xffffffffu, ml, o);
-                if (om > m || (om == m && ol < ml)) { m = om; ml = ol; }
-            }
-            if (m == -INFINITY) break;
-            int64_t g = 0;
-            if (lane == ml) {
-                uint64_t a2 = a2w;
-                uint64_t p2 = a.P[(uint64_t)yp * N + x2], n2 = a.P[(uint64_t)yn * N + x2];
-                uint64_t cc1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
-                uint64_t cc2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);
-                g = (int64_t)cc1 - (int64_t)cc2;
-                sc = -INFINITY;
-            }
-            g = __shfl_sync(0xffffffffu, g, ml);
-            uint32_t gx = __shfl_sync(0xffffffffu, x2, ml);
-            if (g > best) { best = g; bx = gx; }
-        }
-        if (colok && lane == 0 && bx != 0xFFFFFFFFu) {
-            float gf = (float)best;
-            unsigned long long k = ((unsigned long long)__float_as_uint(gf) << 32) | x1;
-            a.prop[t] = bx;
-            a.pgain[t] = (unsigned long long)best;
-            atomicMax(a.claim + (uint64_t)fi * N + x1, k);
-            atomicMax(a.claim + (uint64_t)fi * N + bx, k);
+        unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (m) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(a.nsel_out, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (keep) a.sel_out[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)t;
         }
     }
-    fwd_teardown(s.f);
+    fwd_teardown(s);
 }
 
 }  // namespace
@@ -713,15 +616,23 @@ int mlp_train_step(const float *feat, const float *target, uint64_t n, float *ma
 int launch_learned_phase(const LocalArgs &a, cudaStream_t s) {
     uint64_t total = a.N * a.nframes;
     if (!total) return AM_OK;
+    if (total >= 0xFFFFFFFFull) {
+        set_error("the learned gate lists slots as 32-bit indices: too many columns in one phase");
+        return AM_ERR_ARG;
+    }
     AMG_CUDA(cudaMemsetAsync(a.claim, 0, total * sizeof(unsigned long long), s));
-    unsigned g1 = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)kSMs * 8);
-    AMG_LAUNCH(k_cost_cache, g1, 256, 0, s, a);
-    size_t smem = std::max<size_t>(sizeof(PropSmem) + 1024, 56 * 1024);
-    int rc = set_smem((const void *)k_learned_propose, smem);
-    if (rc) return rc;
-    unsigned g2 = (unsigned)std::min<uint64_t>((total + 3) / 4, (uint64_t)kSMs * 4);
-    AMG_LAUNCH(k_learned_propose, g2, 128, smem, s, a);
-    return launch_local_apply(a, s);
+    AMG_CUDA(cudaMemsetAsync(a.nsel_out, 0, sizeof(unsigned long long), s));
+    int rc;
+    // >= 56 KB of shared memory keeps at most 4 CTAs (4 x 128 TMEM columns) per SM.
+    size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 56 * 1024);
+    if ((rc = set_smem((const void *)k_learned_gate, smem))) return rc;
+    unsigned g = (unsigned)std::min<uint64_t>((total + kTM - 1) / kTM, (uint64_t)kSMs * 4);
+    AMG_LAUNCH(k_learned_gate, g, 128, smem, s, a);
+    LocalArgs b = a;
+    b.sel = a.sel_out;
+    b.nsel = a.nsel_out;
+    if ((rc = launch_local_propose(b, s))) return rc;
+    return launch_local_apply(b, s);
 }
 
 }  // namespace amg

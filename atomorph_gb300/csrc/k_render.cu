@@ -248,9 +248,9 @@ __global__ void k_pair_gather(const uint32_t *__restrict__ keys, const uint32_t 
 
 struct FrameArgs {
     double w1, w2;          // LINEAR: weight of pt1 and 1 - that weight
-    double b[4];            // SPLINE basis at the frame's local time
+    double b0, b1, b2, b3;  // SPLINE basis at the frame's local time
     long long w1q;          // round(w1 * 2^38)
-    long long bq[4];        // round(b[i] * 2^38)
+    long long bq0, bq2, bq3;// round(b_i * 2^38) (b1 enters through the q1 term)
     uint32_t lin_mode;      // 0 general, 1 w1 == 1 (X = X1), 2 w1 == 0 (X = X2)
     uint32_t key_mode;      // 1 when the spline basis is exactly (0, 1, 0, 0)
     uint32_t seg_ok;        // 1 when the spline segment is the prepared one
@@ -280,8 +280,8 @@ __device__ __forceinline__ bool lin_fast(const FrameArgs &fa, int32_t a, int32_t
 __device__ __forceinline__ bool spl_fast(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
                                          uint32_t *out) {
     if ((abs(q0 - q1) | abs(q2 - q1) | abs(q3 - q1)) >= (1 << 22)) return false;  // keeps V in 63 bits
-    long long V = ((long long)q1 << 38) + fa.bq[0] * (long long)(q0 - q1) + fa.bq[2] * (long long)(q2 - q1) +
-                  fa.bq[3] * (long long)(q3 - q1);  // units of 2^-46 px
+    long long V = ((long long)q1 << 38) + fa.bq0 * (long long)(q0 - q1) + fa.bq2 * (long long)(q2 - q1) +
+                  fa.bq3 * (long long)(q3 - q1);  // units of 2^-46 px
     unsigned long long A = V >= 0 ? (unsigned long long)V : (unsigned long long)(-V);
     const unsigned long long one = 1ull << 46;
     unsigned long long I = A >> 46, F = A & (one - 1);
@@ -310,13 +310,13 @@ __device__ __forceinline__ int32_t lin_fixed(double w1, double w2, int32_t a, in
 // round(fract * 255) split (morph.cpp:528-530).  Returns the 1/256 grid
 // position as (integer part << 8) | fract byte with the integer part taken
 // modulo 2^16 like the x86 build's double -> uint16 conversion.
-__device__ __forceinline__ uint32_t spl_fixed(const double *b, int32_t q0, int32_t q1, int32_t q2, int32_t q3) {
+__device__ __forceinline__ uint32_t spl_fixed(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3) {
     double v0 = (double)(q0 >> 8) + (double)(q0 & 255) / 256.0;
     double v1 = (double)(q1 >> 8) + (double)(q1 & 255) / 256.0;
     double v2 = (double)(q2 >> 8) + (double)(q2 & 255) / 256.0;
     double v3 = (double)(q3 >> 8) + (double)(q3 & 255) / 256.0;
-    double v = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, b[0]), __dmul_rn(v1, b[1])), __dmul_rn(v2, b[2])),
-                         __dmul_rn(v3, b[3]));
+    double v = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, fa.b0), __dmul_rn(v1, fa.b1)), __dmul_rn(v2, fa.b2)),
+                         __dmul_rn(v3, fa.b3));
     double ip = trunc(v);
     double fr = __dsub_rn(v, ip);
     uint32_t xi = (uint32_t)(int)ip & 0xFFFFu;
@@ -394,8 +394,8 @@ __global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs f
                 a = make_int4(pt_X(q0), pt_Y(q0), pt_X(q1), pt_Y(q1));
                 b = make_int4(pt_X(q2), pt_Y(q2), pt_X(q3), pt_Y(q3));
             }
-            if (!spl_fast(fa, a.x, a.z, b.x, b.z, &X)) X = spl_fixed(fa.b, a.x, a.z, b.x, b.z);
-            if (!spl_fast(fa, a.y, a.w, b.y, b.w, &Y)) Y = spl_fixed(fa.b, a.y, a.w, b.y, b.w);
+            if (!spl_fast(fa, a.x, a.z, b.x, b.z, &X)) X = spl_fixed(fa, a.x, a.z, b.x, b.z);
+            if (!spl_fast(fa, a.y, a.w, b.y, b.w, &Y)) Y = spl_fixed(fa, a.y, a.w, b.y, b.w);
         } else {
             X = (uint32_t)a.x;
             Y = (uint32_t)a.y;
@@ -421,11 +421,21 @@ __global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs f
         }
         spl[i] = make_uint4(px | (py << 16), xf | (yf << 8) | (valid << 16), colour, r);
         if (valid) {
-            uint32_t t[4];
-            int nt = corner_tiles(px, py, valid, fa.tiles_x, t);
-            for (int k = 0; k < nt; ++k) {
-                if (smem_hist) atomicAdd(&hist[t[k]], 1u);
-                else atomicAdd(&tile_cnt[t[k]], 1u);
+            // Distinct tiles of the valid corners, in registers: corner k sits
+            // at (px + (k & 1), py + (k >> 1)); count a tile at the first
+            // valid corner that lands in it.
+            uint32_t tk[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) tk[k] = ((py + (k >> 1)) / kTile) * fa.tiles_x + (px + (k & 1)) / kTile;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!(valid & (1u << k))) continue;
+                bool dup = false;
+#pragma unroll
+                for (int j = 0; j < k; ++j) dup |= (valid & (1u << j)) && tk[j] == tk[k];
+                if (dup) continue;
+                if (smem_hist) atomicAdd(&hist[tk[k]], 1u);
+                else atomicAdd(&tile_cnt[tk[k]], 1u);
             }
         }
     }
@@ -745,14 +755,16 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         auto wrap = [n](int i) { return i < 0 ? n - 1 : (i >= n ? i - n : i); };
         double lt = (time - delta_t * (double)p) / delta_t;
         double t2 = lt * lt, t3 = t2 * lt;
-        fa.b[0] = 0.5 * (-t3 + 2.0 * t2 - lt);
-        fa.b[1] = 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
-        fa.b[2] = 0.5 * (-3.0 * t3 + 4.0 * t2 + lt);
-        fa.b[3] = 0.5 * (t3 - t2);
+        fa.b0 = 0.5 * (-t3 + 2.0 * t2 - lt);
+        fa.b1 = 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
+        fa.b2 = 0.5 * (-3.0 * t3 + 4.0 * t2 + lt);
+        fa.b3 = 0.5 * (t3 - t2);
         fa.seg[0] = wrap(p - 1); fa.seg[1] = wrap(p); fa.seg[2] = wrap(p + 1); fa.seg[3] = wrap(p + 2);
         fa.seg_ok = (p == (int)f) ? 1u : 0u;
-        for (int i = 0; i < 4; ++i) fa.bq[i] = llround(std::ldexp(fa.b[i], 38));
-        fa.key_mode = (fa.b[0] == 0.0 && fa.b[1] == 1.0 && fa.b[2] == 0.0 && fa.b[3] == 0.0) ? 1u : 0u;
+        fa.bq0 = llround(std::ldexp(fa.b0, 38));
+        fa.bq2 = llround(std::ldexp(fa.b2, 38));
+        fa.bq3 = llround(std::ldexp(fa.b3, 38));
+        fa.key_mode = (fa.b0 == 0.0 && fa.b1 == 1.0 && fa.b2 == 0.0 && fa.b3 == 0.0) ? 1u : 0u;
     }
     AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
     uint64_t n = w->active;

@@ -45,6 +45,35 @@ struct SweepArgs {
 // (thread.cpp:1014-1039).
 int launch_sweep_random(const SweepArgs &a, cudaStream_t s);
 
+// ---- k_batch.cu: many jobs' plain sweeps in one persistent launch
+struct BatchJob {
+    uint64_t *P;                 // the job's [K][N] chain points
+    uint64_t N;
+    uint32_t K, C;
+    const uint64_t *chain_off, *pair_off;
+    const uint32_t *frames;      // the job's phase frames, phases concatenated
+    uint32_t ph_off[3], ph_n[3]; // per phase: offset into frames and frame count (0 = no such phase)
+    unsigned seed;
+    uint64_t sweep0;             // the job's sweep counter when the launch starts
+    uint64_t pairs;              // pair_off[C]
+};
+struct BatchArgs {
+    const BatchJob *jobs;
+    uint32_t njobs;
+    const uint32_t *ch_job;      // chunk -> job
+    const uint64_t *ch_start;    // first pair index (t of sweep_pair) of the chunk
+    const uint32_t *ch_count;    // pairs in the chunk
+    uint32_t ch_off[4];          // chunks of phase p: [ch_off[p], ch_off[p+1])
+    uint32_t nphase;             // phases of the longest schedule (<= 3)
+    uint32_t sweeps;
+    unsigned long long *gains;   // [njobs][sweeps] exact cost decrease, zeroed before the launch
+    unsigned *bar;               // [0] arrivals, [1] generation, [2] abort; zeroed before the launch
+    int *err;
+};
+int batch_max_ctas_per_sm(uint32_t threads, int *out);
+// Cooperative launch of `grid` CTAs (all co-resident) running b.sweeps sweeps.
+int launch_batch_sweeps(const BatchArgs &b, uint32_t grid, uint32_t threads, cudaStream_t s);
+
 // ---- k_local.cu: guided refinement (spatially local candidates)
 struct LocalIndex {
     uint32_t ncx = 0, ncy = 0, ncells = 0;   // 2x2-pixel cells over the canvas
@@ -52,6 +81,7 @@ struct LocalIndex {
     uint32_t *col = nullptr;                 // [K][N] column holding slot s
     uint32_t *slot_of = nullptr;             // [K][N] slot held by column x
     uint32_t *cell_start = nullptr;          // [K][ncells+1]
+    uint64_t *sv = nullptr;                  // [K][N] target sum p + n of the column at slot s
     uint32_t *chain_id = nullptr;            // [N]
     uint8_t *chain_w1 = nullptr;             // [C] 1 for width-1 chains
 };
@@ -72,22 +102,43 @@ struct LocalArgs {
     uint32_t nrandom = 2;                    // uniform random candidates of the same chain
     const uint64_t *chain_off = nullptr;     // [C+1]
     uint64_t key;                            // random key of this (sweep, phase)
-    unsigned long long *claim;               // [nframes][N]
-    uint32_t *prop;                          // [nframes][N] proposed partner
+    uint64_t *sv = nullptr;                  // [K][N] target sum of the column at each slot (kept current)
+    bool single_chain = false;               // C == 1: no chain lookups
+    unsigned long long *claim;               // [nframes][N] by slot
+    uint32_t *prop;                          // [nframes][N] proposed partner slot, by proposer slot
     unsigned long long *pgain;               // [nframes][N] exact gain of the proposal
     unsigned long long *gain, *accepted;
+    uint8_t *hot = nullptr;                  // [K][N] gain bucket of each slot's last scan
+    const uint32_t *sel = nullptr;           // proposing slots (t = fi*N + s) when gated
+    const unsigned long long *nsel = nullptr;//   and their count
     // learned proposal only
     const float *mlp = nullptr;              // deployed network (MlpLayout)
-    unsigned long long *cost_cache = nullptr;// [nframes][N] current cost of each column
-    const uint32_t *display = nullptr;       // [K][CH][CW] key-frame colours
-    uint32_t CW = 0, CH = 0;
-    uint32_t topk = 2;                       // best-scored candidates checked exactly
+    float keep = 0.25f;                      // fraction of each 32-slot group the network lets scan
+    float cost_scale = 0.f;                  // log1p(mean column cost / kGainScale)
+    uint32_t *sel_out = nullptr;             // gate output list
+    unsigned long long *nsel_out = nullptr;
     float *rec_feat = nullptr;               // optional sample log: features [cap][10]
-    float *rec_gain = nullptr;               //   and exact gains [cap]
+    float *rec_gain = nullptr;               //   and the best gain the full scan found [cap]
+    uint32_t *rec_idx = nullptr;             // [nframes][N] record row of each slot or ~0
     unsigned long long *rec_count = nullptr;
     uint64_t rec_cap = 0;
     int *err = nullptr;                      // bounded-wait failure flag
 };
+
+// Gains enter the network and its targets as log1p(gain / kGainScale):
+// kGainScale = (16 px)^2 in (1/256 px)^2.
+constexpr float kGainScale = 4096.f * 4096.f;
+// log2 bucket of a gain (0 = no improving partner found), 1..63.
+__host__ __device__ __forceinline__ uint8_t gain_bucket(int64_t g) {
+    if (g <= 0) return 0;
+#ifdef __CUDA_ARCH__
+    return (uint8_t)(64 - __clzll(g));
+#else
+    int b = 0;
+    while (g) { ++b; g >>= 1; }
+    return (uint8_t)b;
+#endif
+}
 
 // ---- k_mlp.cu: the proposal network 10 -> 64 -> 64 -> 1 (ReLU)
 // Deployed layout (floats): W1 bf16 [64][16] as 512 floats, W2 bf16 [64][64]
@@ -110,10 +161,14 @@ int mlp_grad(const float *feat, const float *target, uint64_t n, const float *de
 int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K, uint32_t CW, uint32_t CH,
                       const uint64_t *chain_off, uint32_t C, uint32_t *keys, uint32_t *vals, uint32_t *tk,
                       uint32_t *tv, uint32_t *hist, cudaStream_t s);
+// One guided phase: proposals of every slot, disjoint apply.
 int launch_local_phase(const LocalArgs &a, cudaStream_t s);
+int launch_local_propose(const LocalArgs &a, cudaStream_t s);  // a.sel/a.nsel: listed slots only
 int launch_local_apply(const LocalArgs &a, cudaStream_t s);
-// Learned proposal phase: candidates from a wider window scored by the MLP
-// on tensor cores, the best-scored ones checked exactly (k_mlp.cu).
+// Learned proposal phase (k_mlp.cu): the network scores every slot from its
+// own cheap features on tensor cores, the best-scored `keep` fraction of each
+// 32-slot group is listed, and only listed slots run the guided candidate
+// scan (exact gains, disjoint apply as above).
 int launch_learned_phase(const LocalArgs &a, cudaStream_t s);
 
 // Stable LSD radix sort of (key, value) u32 pairs on the low `bits` key bits.

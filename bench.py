@@ -212,6 +212,9 @@ def bench_ours(args, rank, world):
     ttc = None
     if rank == 0 and args.time_to_cost:
         ttc = time_to_cost(capi, frames, args)
+    bat = None
+    if rank == 0 and args.batch_jobs:
+        bat = batch_bench(capi, args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -236,55 +239,143 @@ def bench_ours(args, rank, world):
     }
     if ttc is not None:
         res["time_to_cost"] = ttc
+    if bat is not None:
+        res["batch"] = bat
     if cpu is not None:
         res["cpu_baseline"] = cpu
     return res
 
 
+def _twin(capi, frames, w, pts, order):
+    """A fresh handle with the same key frames and settings holding the given
+    chains (sweep counter 0, as the original's was when they were exported)."""
+    t = capi.Morph()
+    t.load(frames, **SETTINGS)
+    t.import_chains(w, pts, order)
+    return t
+
+
 def time_to_cost(capi, frames, args):
-    """Refinement half of the metric on the same workload: sweeps and wall
-    time of the plain random-pair refinement to its converged cost, and the
-    time for each proposal kind to get within 0.5% of it."""
+    """Refinement half of the metric on the same workload.  The plain
+    random-pair refinement runs until the last `plain_window` sweeps gain
+    less than `plain_conv` of the cost (or `plain_max_s` seconds): that cost
+    is its converged cost C_plain.  Then each proposal kind starts from the
+    same initial chains (a fresh twin handle, same seed and sweep counter) and
+    runs until its cost is <= 1.005 C_plain.  All forms refine in blocks of
+    `block` sweeps per am_refine call (each call also publishes the chains
+    for rendering).  The learned form records its first guided sweeps, trains
+    its network on them on the GPU, and continues gated; recording and
+    training are inside its wall time."""
     out = {}
+    B = args.block
     m = setup_morph(capi, frames, refine_sweeps=0)
     w, pts0, order = m.export_chains()
     c0 = m.cost()
-    # plain to convergence: stop when a block of sweeps gains < 1e-5 of cost
-    block = 50
     t0 = time.perf_counter()
     trace = [(0, 0.0, c0)]
-    sweeps = 0
-    while sweeps < args.plain_max_sweeps:
-        g = m.refine(block, capi.PROPOSAL_RANDOM)
-        sweeps += block
-        c = trace[-1][2] - int(g.sum())
+    sweeps, c = 0, c0
+    while True:
+        g = m.refine(B, capi.PROPOSAL_RANDOM)
+        sweeps += B
+        c -= int(g.sum())
         trace.append((sweeps, time.perf_counter() - t0, c))
-        if g.sum() < 1e-5 * c:
+        back = next((tr for tr in reversed(trace) if tr[0] <= sweeps - args.plain_window), None)
+        if back is not None and back[2] - c < args.plain_conv * c:
             break
+        if trace[-1][1] > args.plain_max_s:
+            break
+    m.close()
     c_plain = trace[-1][2]
     target = 1.005 * c_plain
-    hit = next((tr for tr in trace if tr[2] <= target), trace[-1])
+    hit = next(tr for tr in trace if tr[2] <= target)
     out["plain"] = {"converged_cost": int(c_plain), "converged_sweeps": sweeps,
                     "converged_s": round(trace[-1][1], 3), "sweeps_to_target": hit[0],
-                    "s_to_target": round(hit[1], 4)}
+                    "s_to_target": round(hit[1], 4),
+                    "ms_per_sweep": round(1e3 * trace[-1][1] / max(sweeps, 1), 4)}
     out["initial_cost"] = int(c0)
     out["target_cost"] = int(target)
+    out["block"] = B
     for kind, name in ((capi.PROPOSAL_LOCAL, "local"), (capi.PROPOSAL_LEARNED, "learned")):
-        try:
-            m.import_chains(w, pts0, order)
-            t0 = time.perf_counter()
-            sweeps, c = 0, c0
-            while c > target and sweeps < args.plain_max_sweeps:
-                g = m.refine(5, kind)
-                sweeps += 5
-                c -= int(g.sum())
-            out[name] = {"sweeps_to_target": sweeps, "s_to_target": round(time.perf_counter() - t0, 4),
-                         "cost": int(c), "reached": bool(c <= target)}
-        except Exception as e:  # proposal kind not available
-            out[name] = {"unavailable": str(e).splitlines()[0][:160]}
-    if "s_to_target" in out.get("learned", {}) and out["learned"]["reached"]:
-        out["speedup_learned_vs_plain"] = round(out["plain"]["s_to_target"] / max(out["learned"]["s_to_target"], 1e-9), 2)
-    m.close()
+        t = _twin(capi, frames, w, pts0, order)
+        info = {}
+        t0 = time.perf_counter()
+        sweeps, c = 0, c0
+        if kind == capi.PROPOSAL_LEARNED:
+            t.tune(learned_keep=args.learned_keep)
+            t.record_swaps(args.learned_samples)
+            recording = True
+        while c > target and time.perf_counter() - t0 < args.proposal_max_s:
+            g = t.refine(B, kind)
+            sweeps += B
+            c -= int(g.sum())
+            if kind == capi.PROPOSAL_LEARNED and recording and t.recorded_count() >= args.learned_samples // 2:
+                t1 = time.perf_counter()
+                f, y = t.recorded_swaps(args.learned_samples)
+                loss = t.train_proposal(f, y, epochs=2, lr=2e-3)
+                t.record_swaps(0)
+                recording = False
+                info.update(trained_at_sweep=sweeps, samples=int(len(y)),
+                            train_s=round(time.perf_counter() - t1, 4), loss=round(float(loss), 5))
+        info.update(sweeps_to_target=sweeps, s_to_target=round(time.perf_counter() - t0, 4), cost=int(c),
+                    reached=bool(c <= target))
+        out[name] = info
+        t.close()
+    for name in ("local", "learned"):
+        if out[name].get("reached"):
+            out[f"speedup_{name}_vs_plain"] = round(out["plain"]["s_to_target"] / max(out[name]["s_to_target"], 1e-9), 2)
+    return out
+
+
+def batch_bench(capi, args):
+    """Batching workload: 32 jobs (atoms log-uniform 2k-200k, 3-8 key frames,
+    128/256/512 canvases).  Each job refines `batch_sweeps` plain sweeps,
+    once job by job (one am_refine per job) and once as one batch (one
+    persistent launch in a replayed CUDA graph, autotuned); both start from
+    the same chains with the same sweep counters, so every job's cost must
+    come out identical.  Each form runs twice; the second run is timed."""
+    from atomorph_gb300 import synth
+    n, S = args.batch_jobs, args.batch_sweeps
+    solo, twin = [], []
+    t0 = time.perf_counter()
+    for j in range(n):
+        frames = synth.workload("batch", j)
+        a = capi.Morph()
+        a.load(frames, seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+        if a.run_until(capi.STATE_ATOM_MORPHING) != capi.STATE_ATOM_MORPHING:
+            raise RuntimeError(f"batch job {j}: pipeline stopped early")
+        b = capi.Morph()
+        b.load(frames, seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+        b.import_chains(*a.export_chains())
+        solo.append(a)
+        twin.append(b)
+    setup_s = time.perf_counter() - t0
+    atoms = [a.atoms for a in solo]
+    keys = [a.export_chains()[2].shape[0] for a in solo]
+    seq_s = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        for a in solo:
+            a.refine(S, capi.PROPOSAL_RANDOM)
+        seq_s.append(time.perf_counter() - t0)
+    batch = capi.Batch(twin)
+    t0 = time.perf_counter()
+    tuning = batch.tune(3)
+    tune_s = time.perf_counter() - t0
+    bat_s = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        batch.refine(S)
+        bat_s.append(time.perf_counter() - t0)
+    equal = all(a.cost() == b.cost() for a, b in zip(solo, twin))
+    out = {"workload": f"batch ({n} jobs)", "atoms_min": min(atoms), "atoms_max": max(atoms),
+           "atoms_total": int(sum(atoms)), "key_frames": sorted(set(keys)), "sweeps_per_job": S,
+           "setup_s": round(setup_s, 2), "sequential_s": round(seq_s[1], 4), "batched_s": round(bat_s[1], 4),
+           "first_batched_call_s": round(bat_s[0], 4), "tune_s": round(tune_s, 3), "tuning": tuning,
+           "jobs_per_s_sequential": round(n / seq_s[1], 2), "jobs_per_s_batched": round(n / bat_s[1], 2),
+           "speedup": round(seq_s[1] / bat_s[1], 2), "per_job_cost_identical": bool(equal)}
+    batch.close()
+    for m in solo + twin:
+        m.close()
     return out
 
 
@@ -444,8 +535,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--refine-sweeps", type=int, default=100)
     ap.add_argument("--time-to-cost", type=int, default=1)
-    ap.add_argument("--plain-max-sweeps", type=int, default=3000)
+    ap.add_argument("--block", type=int, default=20)
+    ap.add_argument("--plain-window", type=int, default=2000)
+    ap.add_argument("--plain-conv", type=float, default=2e-5)
+    ap.add_argument("--plain-max-s", type=float, default=60.0)
+    ap.add_argument("--proposal-max-s", type=float, default=30.0)
+    ap.add_argument("--learned-keep", type=float, default=0.25)
+    ap.add_argument("--learned-samples", type=int, default=4_000_000)
     ap.add_argument("--cpu-frames", type=int, default=2)
+    ap.add_argument("--batch-jobs", type=int, default=32)
+    ap.add_argument("--batch-sweeps", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

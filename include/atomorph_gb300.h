@@ -58,7 +58,7 @@ extern "C" {
 /* ---- swap proposal kinds (new; the reference has only uniform random pairs) */
 #define AM_PROPOSAL_RANDOM  0  /* disjoint uniform random pairs: the plain method */
 #define AM_PROPOSAL_LOCAL   1  /* spatially local candidates, exact gain, greedy disjoint matching */
-#define AM_PROPOSAL_LEARNED 2  /* local candidates ranked by the trained MLP, exact gain decides */
+#define AM_PROPOSAL_LEARNED 2  /* the trained MLP picks which columns run the local scan */
 
 typedef struct am_morph am_morph;
 
@@ -112,7 +112,8 @@ int am_set_motion_noise(am_morph *m, double amplitude_px);
 /* Guided-refinement tunables (the autotuner sets these): "local_self",
  * "local_target", "local_random" (candidates per column from the column's own
  * neighbourhood, its target cell, and uniform random columns),
- * "learned_topk" (network-ranked candidates checked exactly) and
+ * "learned_keep" (fraction of columns, 0 < f <= 1, that the learned gate lets
+ * run the guided candidate scan in each sweep) and
  * "guided_switch" (guided/learned refinement runs plain sweeps until one gains
  * less than this fraction of the cost per sweep; 0 = guided from the start). */
 int am_set_tuning(am_morph *m, const char *name, double value);
@@ -180,12 +181,15 @@ int am_refine(am_morph *m, size_t sweeps, uint64_t *gains);
 
 /* ---- learned swap proposal (no reference counterpart; the reference only
  * draws uniform random pairs, thread.cpp:1000-1005).  The network maps 10
- * pair features to a score; its fp32 master parameters are exchanged as
+ * features of a column to a predicted gain of scanning it; its fp32 master
+ * parameters are exchanged as
  * AM_PROPOSAL_PARAMS floats: W1[64][10], b1[64], W2[64][64], b2[64], w3[64], b3. */
 #define AM_PROPOSAL_FEATURES 10
 #define AM_PROPOSAL_PARAMS 4929
-/* Makes the next learned-proposal sweeps log up to cap candidate pairs: their
- * features and target sign(g)*log1p(|g|/S^2) of the exact swap gain g. */
+/* Makes the next learned-proposal sweeps scan every column and log up to cap
+ * of them: the column's features and the target log1p(g/S^2) of the best
+ * exact swap gain g its full candidate scan found (0 when none improves);
+ * S = 16 px in 1/256 px units. */
 int    am_record_swaps(am_morph *m, size_t cap);
 size_t am_recorded_swaps(am_morph *m, float *features, float *targets, size_t cap);
 /* Trains the network on the GPU (tensor-core forward/backward, Adam) on n
@@ -213,6 +217,29 @@ int  am_fluid_step(am_fluid *f, size_t steps_left, double freedom_radius);      
 /* n steps with steps_left = n-1 .. 0, as morph::step_fluid runs them (morph.cpp:1054). */
 int  am_fluid_steps(am_fluid *f, size_t n, double freedom_radius);
 void *am_fluid_stream(am_fluid *f);
+
+/* ---- batched refinement (no reference counterpart: the reference refines
+ * one morph per worker thread, thread.cpp:173-206).  A batch refines many
+ * jobs (morph handles whose chains are built) with one persistent cooperative
+ * launch per call that runs every sweep of every job, captured once into a
+ * CUDA graph and replayed.  Each job draws the same random pairs as its own
+ * am_refine with AM_PROPOSAL_RANDOM would, so results are bit-identical to
+ * refining the jobs one by one, and each job's cost, sweep counter and
+ * rendered front copy advance as after am_refine.  All jobs must be on one
+ * device and idle (not computing) during batch calls. */
+typedef struct am_batch am_batch;
+int  am_batch_create(am_batch **out, am_morph *const *jobs, size_t n);
+void am_batch_destroy(am_batch *b);
+/* n plain sweeps of every job; gains (optional, [jobs][sweeps]) receive the
+ * exact cost decrease of each job's sweeps. */
+int  am_batch_refine(am_batch *b, size_t sweeps, uint64_t *gains);
+/* Autotuner: times trial_sweeps real sweeps of all jobs under each candidate
+ * launch shape (threads per CTA, CTAs per SM) and work schedule (pairs per
+ * chunk, job-major or interleaved chunk order) on a snapshot of the jobs'
+ * chains, keeps the fastest, and leaves the chains as they were. */
+int  am_batch_tune(am_batch *b, size_t trial_sweeps);
+int  am_batch_get_tuning(const am_batch *b, uint32_t *threads, uint32_t *ctas_per_sm, uint32_t *chunk, uint32_t *order);
+int  am_batch_set_tuning(am_batch *b, uint32_t threads, uint32_t ctas_per_sm, uint32_t chunk, uint32_t order);
 
 /* ---- runtime (no reference counterpart) */
 void    *am_get_stream(am_morph *m);        /* cudaStream_t that renders run on */

@@ -1,6 +1,10 @@
 """The learned swap proposal: tensor-core forward/backward against the numpy
-restatement, training, and what the trained network gains over the same
-candidate search without it."""
+restatement, training, and what the trained network gains.
+
+The network gates the guided candidate scan: it scores every column from
+cheap features of the column itself, and only the best-scored fraction of
+each 32-column group runs the scan.  Trained on the best gains the full scan
+found, it should pick the columns where improving swaps are."""
 import numpy as np
 import pytest
 
@@ -70,34 +74,72 @@ def _chains(capi, frames, **kw):
     return m
 
 
+def test_learned_gate_keep_all_equals_guided(capi):
+    """With every column kept, the gated path runs exactly the guided sweeps:
+    same proposals, same claims, same applied swaps, bit for bit.  Two
+    handles with the same frames, seed and chains (sweep counters at 0)."""
+    frames = synth.workload("shapes256")
+    kw = dict(seed=3, blob_delimiter=0, motion=capi.LINEAR, fading=capi.LINEAR)
+    a = _chains(capi, frames, **kw)
+    b = capi.Morph()
+    b.load(frames, **kw)
+    b.import_chains(*a.export_chains())
+    c0 = a.cost()
+    assert b.cost() == c0
+    a.tune(guided_switch=0)
+    b.tune(guided_switch=0, learned_keep=1.0)
+    b.proposal_weights(_rand_params(9))
+    g_local = a.refine(12, capi.PROPOSAL_LOCAL)
+    g_learned = b.refine(12, capi.PROPOSAL_LEARNED)
+    assert np.array_equal(g_local, g_learned)
+    assert np.array_equal(a.export_chains()[1], b.export_chains()[1])
+    assert b.cost() == c0 - int(g_learned.sum())
+
+
 def test_learned_proposal_end_to_end(capi, oracle):
-    """Record swap outcomes, train on the GPU, refine with the network: exact
-    invariants hold, and the trained network beats the same candidate search
-    ranked by an untrained network (what the training gains)."""
+    """Record the full scan's outcomes, train on the GPU, refine with the
+    gate: exact invariants hold, and at the same scan budget (a quarter of the
+    columns) the trained gate gains more than an untrained one."""
     frames = synth.workload("shapes256")
     m = _chains(capi, frames, seed=3, blob_delimiter=0, motion=capi.LINEAR, fading=capi.LINEAR)
+    m.tune(guided_switch=0)  # guided from the first sweep: every sweep records
     w, pts0, order = m.export_chains()
     K = len(frames)
     c0 = m.cost()
-    m.record_swaps(400000)
-    gains = m.refine(20, capi.PROPOSAL_LEARNED)
-    feats, targets = m.recorded_swaps(400000)
+    m.record_swaps(1 << 20)
+    gains = m.refine(10, capi.PROPOSAL_LEARNED)
+    feats, targets = m.recorded_swaps(1 << 20)
     assert len(targets) > 100000
-    assert np.isfinite(feats).all() and np.isfinite(targets).all()
+    assert np.isfinite(feats).all() and np.isfinite(targets).all() and (targets >= 0).all()
     assert m.cost() == c0 - int(gains.sum())
     untrained = m.proposal_weights()
     perm = np.random.default_rng(0).permutation(len(targets))
-    loss = m.train_proposal(feats[perm], targets[perm], epochs=4, lr=2e-3)
+    loss = m.train_proposal(feats[perm], targets[perm], epochs=6, lr=2e-3)
     assert np.isfinite(loss)
     trained = m.proposal_weights()
-    sweeps = 30
+    m.proposal_weights(untrained)
+    pred_u = m.proposal_forward(feats[:50000])
+    m.proposal_weights(trained)
+    pred_t = m.proposal_forward(feats[:50000])
+    mse_u = float(np.mean((pred_u - targets[:50000]) ** 2))
+    mse_t = float(np.mean((pred_t - targets[:50000]) ** 2))
+    print("gate regression mse untrained %.4f trained %.4f" % (mse_u, mse_t))
+    assert mse_t < 0.5 * mse_u
+    sweeps = 20
     results = {}
     for name, wts in (("untrained", untrained), ("trained", trained)):
-        m.import_chains(w, pts0, order)
-        m.proposal_weights(wts)
-        g = m.refine(sweeps, capi.PROPOSAL_LEARNED)
-        results[name] = m.cost()
+        # a fresh twin per arm: same frames, seed, chains and sweep counter,
+        # so both arms draw the same random candidates
+        t = capi.Morph()
+        t.load(frames, seed=3, blob_delimiter=0, motion=capi.LINEAR, fading=capi.LINEAR)
+        t.import_chains(w, pts0, order)
+        t.tune(guided_switch=0, learned_keep=0.25)
+        t.proposal_weights(wts)
+        g = t.refine(sweeps, capi.PROPOSAL_LEARNED)
+        results[name] = t.cost()
         assert results[name] == c0 - int(g.sum())
-        _, pts, _ = m.export_chains()
+        _, pts, _ = t.export_chains()
         assert oracle.energy(pts, w, K)[1] == results[name]
+        t.close()
+    print("cost after %d gated sweeps (keep 1/4):" % sweeps, results, "start", c0)
     assert results["trained"] < results["untrained"], results
