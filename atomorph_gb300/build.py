@@ -19,7 +19,10 @@ OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libatomorph_gb300.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code keeps every double operation separately rounded (no FMA
+# contraction), as the reference's x86 build evaluates it.
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+          "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
 
 # (source, extra flags).  Colour conversion must round every multiply and add

@@ -40,7 +40,7 @@ class Batch {
     uint32_t nphase_ = 0;
     DBuf<BatchJob> d_jobs_;
     BatchJob *h_jobs_ = nullptr;       // pinned mirror, copied in by the graph
-    DBuf<uint32_t> d_ch_job_, d_ch_count_;
+    DBuf<uint32_t> d_ch_job_, d_ch_count_, d_ch_fi_;
     DBuf<uint64_t> d_ch_start_;
     uint32_t ch_off_[4] = {};
     DBuf<unsigned long long> d_gains_;

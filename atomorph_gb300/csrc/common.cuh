@@ -37,7 +37,7 @@ constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
 // around each launch; read back (and waited for) by collect().
 enum ProfId {
     PROF_SPLAT, PROF_SCAN, PROF_SCATTER, PROF_RESOLVE, PROF_PAIR, PROF_SWEEP_RANDOM, PROF_SWEEP_LOCAL,
-    PROF_MLP, PROF_FLUID, PROF_COUNT
+    PROF_MLP, PROF_FLUID, PROF_BIN, PROF_COUNT
 };
 struct Prof {
     bool on = false;
@@ -111,10 +111,13 @@ __host__ __device__ __forceinline__ uint64_t pt_make(uint32_t x, uint32_t y, uin
            ((uint64_t)(yf & 0xFFu) << 40) | ((uint64_t)(flags & 0xFFu) << 48);
 }
 // point_distance (atomorph.h:334-339): squared distance in 1/256 px, exact.
+// Coordinates are below 2^24, so differences fit in 32 bits and every
+// product is a 32 x 32 -> 64-bit multiply (64 x 64-bit integer multiplies
+// are slow on GB300).
 __host__ __device__ __forceinline__ uint64_t pt_dist(uint64_t a, uint64_t b) {
-    int64_t dx = (int64_t)pt_X(a) - pt_X(b);
-    int64_t dy = (int64_t)pt_Y(a) - pt_Y(b);
-    return (uint64_t)(dx * dx + dy * dy);
+    const int32_t dx = pt_X(a) - pt_X(b);
+    const int32_t dy = pt_Y(a) - pt_Y(b);
+    return (uint64_t)((int64_t)dx * dx + (int64_t)dy * dy);
 }
 
 // Target sum s = p + n of a column (its points at the two neighbouring key
@@ -132,9 +135,9 @@ __host__ __device__ __forceinline__ int32_t sums_y(uint64_t s) { return (int32_t
 // since every squared norm appears once on each side.  Exact in int64:
 // |a1 - a2| < 2^24 and |s2 - s1| < 2^25 per axis.
 __host__ __device__ __forceinline__ int64_t pair_gain(uint64_t a1, uint64_t S1, uint64_t a2, uint64_t S2) {
-    int64_t dx = (int64_t)pt_X(a1) - pt_X(a2), dy = (int64_t)pt_Y(a1) - pt_Y(a2);
-    int64_t ex = (int64_t)sums_x(S2) - sums_x(S1), ey = (int64_t)sums_y(S2) - sums_y(S1);
-    return 2 * (dx * ex + dy * ey);
+    const int32_t dx = pt_X(a1) - pt_X(a2), dy = pt_Y(a1) - pt_Y(a2);
+    const int32_t ex = sums_x(S2) - sums_x(S1), ey = sums_y(S2) - sums_y(S1);
+    return 2 * ((int64_t)dx * ex + (int64_t)dy * ey);
 }
 
 // ------------------------------------------------------------ hashing -----

@@ -59,37 +59,39 @@ int Batch::init() {
     return sync_layout();
 }
 
-// Chunk tables: for each phase p, every job's pairs x frames of its phase p
-// cut into chunks of at most tuning.chunk pairs.
+// Chunk tables: for each phase p and each frame of every job's phase p, the
+// job's pairs cut into chunks of at most tuning.chunk pairs.
 int Batch::sync_layout() {
     bool changed = tuning.chunk != chunk_built_ || tuning.order != order_built_;
     for (size_t j = 0; j < jobs_.size(); ++j) changed |= versions_[j] != jobs_[j]->layout_version;
     if (!changed) return AM_OK;
-    std::vector<uint32_t> job[3], cnt[3];
+    struct Ch { uint64_t start; uint32_t count, fi; };
+    std::vector<uint32_t> job[3], cnt[3], fis[3];
     std::vector<uint64_t> start[3];
     nphase_ = 0;
     for (uint32_t p = 0; p < 3; ++p) {
-        std::vector<std::vector<std::pair<uint64_t, uint32_t>>> per(jobs_.size());
+        std::vector<std::vector<Ch>> per(jobs_.size());
         for (size_t j = 0; j < jobs_.size(); ++j) {
             Engine *e = jobs_[j];
             auto ph = phases_for(e->K);
             nphase_ = std::max<uint32_t>(nphase_, (uint32_t)ph.size());
             if (p >= ph.size() || e->pair_off.empty()) continue;
-            uint64_t items = e->pair_off[e->C] * ph[p].size();
-            for (uint64_t s = 0; s < items; s += tuning.chunk)
-                per[j].push_back({s, (uint32_t)std::min<uint64_t>(tuning.chunk, items - s)});
+            const uint64_t pairs = e->pair_off[e->C];
+            for (uint32_t fi = 0; fi < (uint32_t)ph[p].size(); ++fi)
+                for (uint64_t s = 0; s < pairs; s += tuning.chunk)
+                    per[j].push_back({s, (uint32_t)std::min<uint64_t>(tuning.chunk, pairs - s), fi});
         }
+        auto put = [&](size_t j, const Ch &c) {
+            job[p].push_back((uint32_t)j); start[p].push_back(c.start); cnt[p].push_back(c.count); fis[p].push_back(c.fi);
+        };
         if (tuning.order == 0) {
             for (size_t j = 0; j < per.size(); ++j)
-                for (auto &c : per[j]) { job[p].push_back((uint32_t)j); start[p].push_back(c.first); cnt[p].push_back(c.second); }
+                for (auto &c : per[j]) put(j, c);
         } else {
             for (size_t k = 0;; ++k) {
                 bool any = false;
                 for (size_t j = 0; j < per.size(); ++j)
-                    if (k < per[j].size()) {
-                        any = true;
-                        job[p].push_back((uint32_t)j); start[p].push_back(per[j][k].first); cnt[p].push_back(per[j][k].second);
-                    }
+                    if (k < per[j].size()) { any = true; put(j, per[j][k]); }
                 if (!any) break;
             }
         }
@@ -98,23 +100,26 @@ int Batch::sync_layout() {
     if (total > UINT32_MAX) { set_error("am_batch: too many chunks"); return AM_ERR_ARG; }
     ch_off_[0] = 0;
     for (int p = 0; p < 3; ++p) ch_off_[p + 1] = ch_off_[p] + (uint32_t)job[p].size();
-    std::vector<uint32_t> J, Cn;
+    std::vector<uint32_t> J, Cn, F;
     std::vector<uint64_t> S;
     for (int p = 0; p < 3; ++p) {
         J.insert(J.end(), job[p].begin(), job[p].end());
         Cn.insert(Cn.end(), cnt[p].begin(), cnt[p].end());
+        F.insert(F.end(), fis[p].begin(), fis[p].end());
         S.insert(S.end(), start[p].begin(), start[p].end());
     }
-    uint32_t *oj = d_ch_job_.p, *oc = d_ch_count_.p;
+    uint32_t *oj = d_ch_job_.p, *oc = d_ch_count_.p, *of = d_ch_fi_.p;
     uint64_t *os = d_ch_start_.p;
     int rc;
     if ((rc = d_ch_job_.reserve(std::max<size_t>(total, 1)))) return rc;
     if ((rc = d_ch_count_.reserve(std::max<size_t>(total, 1)))) return rc;
+    if ((rc = d_ch_fi_.reserve(std::max<size_t>(total, 1)))) return rc;
     if ((rc = d_ch_start_.reserve(std::max<size_t>(total, 1)))) return rc;
-    if (oj != d_ch_job_.p || oc != d_ch_count_.p || os != d_ch_start_.p) drop_graphs();
+    if (oj != d_ch_job_.p || oc != d_ch_count_.p || os != d_ch_start_.p || of != d_ch_fi_.p) drop_graphs();
     if (total) {
         AMG_CUDA(cudaMemcpyAsync(d_ch_job_.p, J.data(), total * 4, cudaMemcpyHostToDevice, stream_));
         AMG_CUDA(cudaMemcpyAsync(d_ch_count_.p, Cn.data(), total * 4, cudaMemcpyHostToDevice, stream_));
+        AMG_CUDA(cudaMemcpyAsync(d_ch_fi_.p, F.data(), total * 4, cudaMemcpyHostToDevice, stream_));
         AMG_CUDA(cudaMemcpyAsync(d_ch_start_.p, S.data(), total * 8, cudaMemcpyHostToDevice, stream_));
     }
     AMG_CUDA(cudaStreamSynchronize(stream_));
@@ -148,7 +153,7 @@ int Batch::run(size_t sweeps, const BatchTuning &t, bool graph, float *ms) {
     uint32_t grid = std::min<uint32_t>(t.ctas_per_sm, (uint32_t)occ) * (uint32_t)sms_;
     BatchArgs a;
     a.jobs = d_jobs_.p; a.njobs = (uint32_t)nj;
-    a.ch_job = d_ch_job_.p; a.ch_start = d_ch_start_.p; a.ch_count = d_ch_count_.p;
+    a.ch_job = d_ch_job_.p; a.ch_start = d_ch_start_.p; a.ch_count = d_ch_count_.p; a.ch_fi = d_ch_fi_.p;
     std::memcpy(a.ch_off, ch_off_, sizeof(ch_off_));
     a.nphase = nphase_; a.sweeps = (uint32_t)sweeps; a.gains = d_gains_.p; a.bar = d_bar_.p; a.err = d_err_.p;
     auto enqueue = [&]() -> int {

@@ -74,8 +74,9 @@ __global__ void k_batch_sweeps(BatchArgs b) {
                 a.frames = J.frames + J.ph_off[p]; a.nframes = J.ph_n[p];
                 a.key = sweep_key(J.seed, J.sweep0 + s, (uint32_t)p);
                 const uint64_t start = b.ch_start[ch], end = start + b.ch_count[ch];
+                const uint32_t fi = b.ch_fi[ch];
                 unsigned long long gain = 0, acc = 0;
-                for (uint64_t t = start + threadIdx.x; t < end; t += blockDim.x) sweep_pair(a, J.pairs, t, gain, acc);
+                for (uint64_t r = start + threadIdx.x; r < end; r += blockDim.x) sweep_pair(a, fi, r, gain, acc);
                 gain = warp_sum_u64(gain);
                 if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = gain;
                 __syncthreads();

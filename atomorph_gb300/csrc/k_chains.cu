@@ -16,13 +16,10 @@ namespace {
 // ---------------------------------------------------------------- cost ----
 __global__ void k_cost(const uint64_t *__restrict__ P, uint64_t N, uint32_t K, unsigned long long *out) {
     unsigned long long acc = 0;
-    const uint64_t total = N * K;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t j = (uint32_t)(t / N);
-        uint64_t i = t - (uint64_t)j * N;
-        uint32_t jn = j + 1 == K ? 0 : j + 1;
-        acc += pt_dist(__ldg(P + (uint64_t)j * N + i), __ldg(P + (uint64_t)jn * N + i));
+    for (uint32_t j = 0; j < K; ++j) {
+        const uint32_t jn = j + 1 == K ? 0 : j + 1;
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += (uint64_t)gridDim.x * blockDim.x)
+            acc += pt_dist(__ldg(P + (uint64_t)j * N + i), __ldg(P + (uint64_t)jn * N + i));
     }
     acc = warp_sum_u64(acc);
     __shared__ unsigned long long part[32];
@@ -49,11 +46,11 @@ __global__ void k_cost_sub(const uint64_t *__restrict__ P, uint64_t N, uint32_t 
 // ------------------------------------------------------- random sweep ----
 __global__ void __launch_bounds__(256) k_sweep_random(SweepArgs a) {
     const uint64_t pairs = __ldg(a.pair_off + a.C);
-    const uint64_t total = pairs * a.nframes;
     unsigned long long gain = 0, acc = 0;
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
-         t += (uint64_t)gridDim.x * blockDim.x)
-        sweep_pair(a, pairs, t, gain, acc);
+    for (uint32_t fi = 0; fi < a.nframes; ++fi)
+        for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < pairs;
+             r += (uint64_t)gridDim.x * blockDim.x)
+            sweep_pair(a, fi, r, gain, acc);
     gain = warp_sum_u64(gain);
     acc = warp_sum_u64(acc);
     if ((threadIdx.x & 31) == 0) {

@@ -139,14 +139,12 @@ __device__ __forceinline__ void scan_cell(const LocalArgs &a, const uint32_t *cs
 // cell-window candidates, from slot-ordered arrays (coalesced, L2-resident
 // windows); only the random candidates are scattered loads.  With `sel` set
 // only the listed slots propose (the learned gate's choice).
-__global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
+__device__ __forceinline__ void propose_one(const LocalArgs &a, uint32_t fi, uint32_t s1) {
     const uint64_t N = a.N;
-    const uint64_t total = a.sel ? (uint64_t)*a.nsel : N * a.nframes;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t t = a.sel ? (uint64_t)a.sel[i] : i;
-        uint32_t fi = (uint32_t)(t / N);
+    const uint64_t t = (uint64_t)fi * N + s1;
+    {
         Col c;
-        c.s1 = (uint32_t)(t - (uint64_t)fi * N);
+        c.s1 = s1;
         uint32_t y = a.frames[fi];
         const uint64_t *spt = a.slot_pt + (uint64_t)y * N;
         const uint32_t *col = a.col + (uint64_t)y * N;
@@ -154,7 +152,7 @@ __global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
         a.prop[t] = 0xFFFFFFFFu;
         uint32_t x1 = col[c.s1];
         uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
-        if (a.chain_w1[ch]) continue;  // width-1 chains do not refine (thread.cpp:1045)
+        if (a.chain_w1[ch]) return;  // width-1 chains do not refine (thread.cpp:1045)
         c.a1 = spt[c.s1];
         c.S1 = sv[c.s1];
         c.lo = a.single_chain ? 0ull : a.chain_off[ch];
@@ -211,21 +209,42 @@ __global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
     }
 }
 
+// Slot t of a gated list: t = fi * N + s < 2^32 (the host checks), so a
+// 32-bit division splits it.
+__device__ __forceinline__ void split_slot(uint32_t t, uint32_t n32, uint32_t &fi, uint32_t &s) {
+    fi = t / n32;
+    s = t - fi * n32;
+}
+
+__global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
+    if (a.sel) {
+        const uint64_t total = *a.nsel;
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+             i += (uint64_t)gridDim.x * blockDim.x) {
+            uint32_t fi, s1;
+            split_slot(a.sel[i], (uint32_t)a.N, fi, s1);
+            propose_one(a, fi, s1);
+        }
+    } else {
+        for (uint32_t fi = 0; fi < a.nframes; ++fi)
+            for (uint64_t s1 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s1 < a.N;
+                 s1 += (uint64_t)gridDim.x * blockDim.x)
+                propose_one(a, fi, (uint32_t)s1);
+    }
+}
+
 // A proposal (s1 -> s2) is applied when it holds the claim of both slots:
 // applied swaps are then disjoint, so the columns at s1 and s2 are read and
 // written by this thread alone.
-__global__ void __launch_bounds__(256) k_local_apply(LocalArgs a) {
+__device__ __forceinline__ void apply_one(const LocalArgs &a, uint32_t fi, uint32_t s1, unsigned long long &gain,
+                                          unsigned long long &acc) {
     const uint64_t N = a.N;
-    const uint64_t total = a.sel ? (uint64_t)*a.nsel : N * a.nframes;
-    unsigned long long gain = 0, acc = 0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t t = a.sel ? (uint64_t)a.sel[i] : i;
+    const uint64_t t = (uint64_t)fi * N + s1;
+    {
         uint32_t s2 = a.prop[t];
-        if (s2 == 0xFFFFFFFFu) continue;
-        uint32_t fi = (uint32_t)(t / N);
-        uint32_t s1 = (uint32_t)(t - (uint64_t)fi * N);
+        if (s2 == 0xFFFFFFFFu) return;
         unsigned long long k1 = a.claim[(uint64_t)fi * N + s1], k2 = a.claim[(uint64_t)fi * N + s2];
-        if (k1 != k2 || (uint32_t)k1 != s1) continue;
+        if (k1 != k2 || (uint32_t)k1 != s1) return;
         uint32_t y = a.frames[fi];
         uint64_t *Py = a.P + (uint64_t)y * N;
         uint32_t *slot_of = a.slot_of + (uint64_t)y * N, *col = a.col + (uint64_t)y * N;
@@ -258,6 +277,24 @@ __global__ void __launch_bounds__(256) k_local_apply(LocalArgs a) {
         }
         gain += a.pgain[t];
         acc += 1;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_local_apply(LocalArgs a) {
+    unsigned long long gain = 0, acc = 0;
+    if (a.sel) {
+        const uint64_t total = *a.nsel;
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+             i += (uint64_t)gridDim.x * blockDim.x) {
+            uint32_t fi, s1;
+            split_slot(a.sel[i], (uint32_t)a.N, fi, s1);
+            apply_one(a, fi, s1, gain, acc);
+        }
+    } else {
+        for (uint32_t fi = 0; fi < a.nframes; ++fi)
+            for (uint64_t s1 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s1 < a.N;
+                 s1 += (uint64_t)gridDim.x * blockDim.x)
+                apply_one(a, fi, (uint32_t)s1, gain, acc);
     }
     gain = warp_sum_u64(gain);
     acc = warp_sum_u64(acc);

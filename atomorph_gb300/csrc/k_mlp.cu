@@ -481,8 +481,9 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, int n, floa
 //   9    0 (spare)
 __device__ __forceinline__ bool gate_features(const LocalArgs &a, uint64_t t, float *f) {
     const uint64_t N = a.N;
-    uint32_t fi = (uint32_t)(t / N);
-    uint32_t s1 = (uint32_t)(t - (uint64_t)fi * N);
+    // t < 2^32 (the host checks): a 32-bit division splits it
+    const uint32_t fi = (uint32_t)t / (uint32_t)N;
+    const uint32_t s1 = (uint32_t)t - fi * (uint32_t)N;
     uint32_t y = a.frames[fi];
     uint32_t x1 = a.col[(uint64_t)y * N + s1];
     uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];

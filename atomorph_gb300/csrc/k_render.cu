@@ -57,6 +57,10 @@ struct RenderWork {
     uint64_t rec_cap = 0;
     uint32_t *tile_cnt = nullptr, *tile_off = nullptr, *tile_cur = nullptr;
     uint32_t ntiles_cap = 0;
+    uint32_t *stab = nullptr;  // per-frame spline table of static integer coordinates
+    uint32_t stab_cap = 0;
+    unsigned *bar = nullptr;   // grid barrier of the fused splat + binning launch
+    int *err = nullptr;        // its bounded-wait failure flag
     int *perm = nullptr;    // [2][512] Perlin permutations on the device
     bool perm_set = false;
     Prof *prof = nullptr;   // optional per-kernel timing
@@ -87,6 +91,9 @@ void render_work_destroy(RenderWork *w) {
     if (w->tile_off) cudaFree(w->tile_off);
     if (w->tile_cur) cudaFree(w->tile_cur);
     if (w->perm) cudaFree(w->perm);
+    if (w->bar) cudaFree(w->bar);
+    if (w->stab) cudaFree(w->stab);
+    if (w->err) cudaFree(w->err);
     delete w;
 }
 
@@ -251,6 +258,18 @@ struct FrameArgs {
     double b0, b1, b2, b3;  // SPLINE basis at the frame's local time
     long long w1q;          // round(w1 * 2^38)
     long long bq0, bq2, bq3;// round(b_i * 2^38) (b1 enters through the q1 term)
+    // The same weights split as hi * 2^19 + lo (lo in [0, 2^19)), so every
+    // product with a 32-bit coordinate difference is a 32 x 32 -> 64-bit
+    // multiply: 64 x 64-bit integer multiplies are slow on this part.
+    int32_t w1h, w1l, bh0, bl0, bh2, bl2, bh3, bl3;
+    // SPLINE: the reference's double result for a coordinate that sits on
+    // the integer pixel p in all four control frames (an atom that does not
+    // move along that axis): stab[p] for p < stab_n.  The fixed-point value
+    // of such a coordinate is exactly an integer, i.e. on a rounding
+    // boundary, so without the table every such atom would need the FP64
+    // evaluation.
+    const uint32_t *stab;
+    uint32_t stab_n;
     uint32_t lin_mode;      // 0 general, 1 w1 == 1 (X = X1), 2 w1 == 0 (X = X2)
     uint32_t key_mode;      // 1 when the spline basis is exactly (0, 1, 0, 0)
     uint32_t seg_ok;        // 1 when the spline segment is the prepared one
@@ -260,18 +279,24 @@ struct FrameArgs {
 };
 
 // Fast exact positions.  The reference evaluates its interpolation in
-// double; its result differs from the exact real value of the same formula
-// by far less than 2^-21 px.  The kernels evaluate that real value in 64-bit
-// fixed point (weights quantised to 2^-38, error below 2^-21 px as well) and
-// take its floor / rounded fraction, which equals the reference's unless the
-// value lies within the combined error bound of a rounding boundary; those
-// rare atoms re-run the reference's own double formula (lin_fixed /
-// spl_fixed below).  Returns false when the fallback is needed.
+// double.  The kernels evaluate the same formula's real value in 64-bit fixed
+// point (weights quantised to 2^-38) and take its floor / rounded fraction,
+// which equals the reference's unless the value lies within the combined
+// error bound of a rounding boundary; those rare atoms re-run the reference's
+// own double formula (lin_fixed / spl_fixed below).  The bound is per atom:
+// quantising a weight moves the value by at most half a unit of 2^-38 per
+// unit of the coordinate difference it multiplies, i.e. |d| / 2 fixed-point
+// units in total, and the reference's double rounding (a handful of
+// operations on values below 2^16 px, plus its weights summing to 1 only
+// within a few ulps) stays below 2^13 units of 2^-46 px.  Returns false when
+// the fallback is needed.
 __device__ __forceinline__ bool lin_fast(const FrameArgs &fa, int32_t a, int32_t b, int32_t *out) {
     if (fa.lin_mode == 1) { *out = a; return true; }
     if (fa.lin_mode == 2) { *out = b; return true; }
-    long long V = ((long long)b << 38) + fa.w1q * (long long)(a - b);  // units of 2^-38 (1/256 px)
-    const long long one = 1ll << 38, tol = 1ll << 24;                    // 2^-14 (1/256 px)
+    const int32_t d = a - b;
+    long long V = ((long long)b << 38) + (long long)fa.w1h * d * (1ll << 19) + (long long)fa.w1l * d;  // 2^-38 (1/256 px)
+    const long long one = 1ll << 38;
+    const long long tol = (long long)((uint32_t)abs(d) >> 1) + (1ll << 13);
     long long r = V & (one - 1);
     if (r < tol || one - r < tol) return false;
     *out = (int32_t)(V >> 38);
@@ -280,29 +305,31 @@ __device__ __forceinline__ bool lin_fast(const FrameArgs &fa, int32_t a, int32_t
 __device__ __forceinline__ bool spl_fast(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
                                          uint32_t *out) {
     if ((abs(q0 - q1) | abs(q2 - q1) | abs(q3 - q1)) >= (1 << 22)) return false;  // keeps V in 63 bits
-    long long V = ((long long)q1 << 38) + fa.bq0 * (long long)(q0 - q1) + fa.bq2 * (long long)(q2 - q1) +
-                  fa.bq3 * (long long)(q3 - q1);  // units of 2^-46 px
+    const int32_t d0 = q0 - q1, d2 = q2 - q1, d3 = q3 - q1;
+    long long V = ((long long)q1 << 38) +
+                  ((long long)fa.bh0 * d0 + (long long)fa.bh2 * d2 + (long long)fa.bh3 * d3) * (1ll << 19) +
+                  (long long)fa.bl0 * d0 + (long long)fa.bl2 * d2 + (long long)fa.bl3 * d3;  // units of 2^-46 px
     unsigned long long A = V >= 0 ? (unsigned long long)V : (unsigned long long)(-V);
     const unsigned long long one = 1ull << 46;
     unsigned long long I = A >> 46, F = A & (one - 1);
     if (!fa.key_mode) {
-        const unsigned long long tol = 1ull << 26;  // 2^-20 px
+        const unsigned long long tol =
+            (unsigned long long)(((uint32_t)abs(d0) + (uint32_t)abs(d2) + (uint32_t)abs(d3)) >> 1) + (1ull << 14);
         if (F < tol || one - F < tol) return false;
-        unsigned long long h = (F * 255ull) & (one - 1);
-        unsigned long long d = h > (one >> 1) ? h - (one >> 1) : (one >> 1) - h;
-        if (d < 255ull * tol) return false;
+        unsigned long long h = ((F << 8) - F) & (one - 1);  // F * 255 mod one
+        unsigned long long dd = h > (one >> 1) ? h - (one >> 1) : (one >> 1) - h;
+        if (dd < 255ull * tol) return false;
     }
-    unsigned long long xf = (F * 255ull + (one >> 1)) >> 46;  // round half away on |fraction|
-    int sign = V < 0 ? -1 : 1;
-    uint32_t xi = (uint32_t)(sign * (long long)I) & 0xFFFFu;
-    uint32_t xb = (uint32_t)(sign * (long long)xf) & 0xFFu;
+    unsigned long long xf = ((F << 8) - F + (one >> 1)) >> 46;  // round(F * 255), half away on |fraction|
+    uint32_t xi = (uint32_t)I & 0xFFFFu, xb = (uint32_t)xf & 0xFFu;
+    if (V < 0) { xi = (0u - xi) & 0xFFFFu; xb = (0u - xb) & 0xFFu; }
     *out = (xi << 8) | xb;
     return true;
 }
 
-// Exact double formula of morph::interpolate(point) (morph.cpp:1504-1512)
-// with round-to-nearest operations: floor(w1*X1 + w2*X2) in 1/256 px.
-__device__ __forceinline__ int32_t lin_fixed(double w1, double w2, int32_t a, int32_t b) {
+// The FP64 fallbacks are out of line on purpose: inlined, the compiler may
+// evaluate them under a predicate for every atom, and FP64 throughput is low.
+__device__ __noinline__ int32_t lin_fixed(double w1, double w2, int32_t a, int32_t b) {
     double v = __dadd_rn(__dmul_rn(w1, (double)a), __dmul_rn(w2, (double)b));
     return (int32_t)v;  // v >= 0: truncation is floor
 }
@@ -310,18 +337,27 @@ __device__ __forceinline__ int32_t lin_fixed(double w1, double w2, int32_t a, in
 // round(fract * 255) split (morph.cpp:528-530).  Returns the 1/256 grid
 // position as (integer part << 8) | fract byte with the integer part taken
 // modulo 2^16 like the x86 build's double -> uint16 conversion.
-__device__ __forceinline__ uint32_t spl_fixed(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3) {
+__device__ __noinline__ uint32_t spl_fixed(double b0, double b1, double b2, double b3, int32_t q0, int32_t q1,
+                                           int32_t q2, int32_t q3) {
     double v0 = (double)(q0 >> 8) + (double)(q0 & 255) / 256.0;
     double v1 = (double)(q1 >> 8) + (double)(q1 & 255) / 256.0;
     double v2 = (double)(q2 >> 8) + (double)(q2 & 255) / 256.0;
     double v3 = (double)(q3 >> 8) + (double)(q3 & 255) / 256.0;
-    double v = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, fa.b0), __dmul_rn(v1, fa.b1)), __dmul_rn(v2, fa.b2)),
-                         __dmul_rn(v3, fa.b3));
+    double v = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, b0), __dmul_rn(v1, b1)), __dmul_rn(v2, b2)),
+                         __dmul_rn(v3, b3));
     double ip = trunc(v);
     double fr = __dsub_rn(v, ip);
     uint32_t xi = (uint32_t)(int)ip & 0xFFFFu;
     uint32_t xf = (uint32_t)(int)round(__dmul_rn(fr, 255.0)) & 0xFFu;
     return (xi << 8) | xf;
+}
+
+__global__ void k_spline_table(double b0, double b1, double b2, double b3, uint32_t n, uint32_t *tab) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) {
+        const int32_t q = (int32_t)(p << 8);
+        tab[p] = spl_fixed(b0, b1, b2, b3, q, q, q, q);
+    }
 }
 
 // Colour fade of one atom (morph.cpp:537-550, 1467-1488) in FP32.
@@ -362,87 +398,330 @@ __device__ __forceinline__ int corner_tiles(uint32_t px, uint32_t py, uint32_t v
     return n;
 }
 
-__global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs fa, uint64_t n,
-                                                      const int4 *__restrict__ pa, const int4 *__restrict__ pb,
-                                                      const uint2 *__restrict__ col, const float2 *__restrict__ ls,
-                                                      const uint32_t *__restrict__ rank,
-                                                      const uint32_t *__restrict__ idx, uint4 *spl,
-                                                      uint32_t *tile_cnt) {
+// A coordinate on the same integer pixel in all four control frames: the
+// per-frame table holds the reference's double result.
+__device__ __forceinline__ bool spl_static(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
+                                           uint32_t *out) {
+    if (fa.key_mode || q0 != q1 || q2 != q1 || q3 != q1 || (q1 & 255) || q1 < 0) return false;
+    const uint32_t p = (uint32_t)q1 >> 8;
+    if (p >= fa.stab_n) return false;
+    *out = __ldg(fa.stab + p);
+    return true;
+}
+
+struct SplatIn {
+    const int4 *pa, *pb;
+    const uint2 *col;
+    const float2 *ls;
+    const uint32_t *rank, *idx;
+};
+
+// One atom at the frame's time: exact position, faded colour and the valid
+// bilinear corners (morph.cpp:523-588), packed as the 16-byte splat record
+// {px | py << 16, xf | yf << 8 | valid << 16, colour, rank}.
+// Control coordinates of atom i for the frame: LINEAR/none use a = pa[i]
+// (x1, y1, x2, y2); SPLINE uses a = (q0.x, q0.y, q1.x, q1.y) and
+// b = (q2.x, q2.y, q3.x, q3.y).
+__device__ __forceinline__ void atom_controls(const RenderScene &sc, const FrameArgs &fa, const SplatIn &in,
+                                              uint64_t i, int4 &a, int4 &b) {
+    a = in.pa[i];
+    b = make_int4(0, 0, 0, 0);
+    if (sc.motion == AM_SPLINE) {
+        if (fa.seg_ok) {
+            b = in.pb[i];
+        } else {
+            uint64_t o = in.idx[i];
+            uint64_t q0 = sc.P[(uint64_t)fa.seg[0] * sc.N + o], q1 = sc.P[(uint64_t)fa.seg[1] * sc.N + o];
+            uint64_t q2 = sc.P[(uint64_t)fa.seg[2] * sc.N + o], q3 = sc.P[(uint64_t)fa.seg[3] * sc.N + o];
+            a = make_int4(pt_X(q0), pt_Y(q0), pt_X(q1), pt_Y(q1));
+            b = make_int4(pt_X(q2), pt_Y(q2), pt_X(q3), pt_Y(q3));
+        }
+    }
+}
+
+// Position of one axis by the exact integer paths; false when the value sits
+// too close to a rounding boundary and the reference's double formula must
+// decide (axis_fixed).
+__device__ __forceinline__ bool axis_fast(const RenderScene &sc, const FrameArgs &fa, int axis, const int4 &a,
+                                          const int4 &b, uint32_t *out) {
+    const int32_t c0 = axis ? a.y : a.x, c1 = axis ? a.w : a.z, c2 = axis ? b.y : b.x, c3 = axis ? b.w : b.z;
+    if (sc.motion == AM_LINEAR) {
+        int32_t v;
+        if (!lin_fast(fa, c0, c1, &v)) return false;
+        *out = (uint32_t)v;
+        return true;
+    }
+    if (sc.motion == AM_SPLINE) return spl_static(fa, c0, c1, c2, c3, out) || spl_fast(fa, c0, c1, c2, c3, out);
+    *out = (uint32_t)c0;
+    return true;
+}
+__device__ __forceinline__ uint32_t axis_fixed(const RenderScene &sc, const FrameArgs &fa, int axis, const int4 &a,
+                                               const int4 &b) {
+    const int32_t c0 = axis ? a.y : a.x, c1 = axis ? a.w : a.z, c2 = axis ? b.y : b.x, c3 = axis ? b.w : b.z;
+    if (sc.motion == AM_LINEAR) return (uint32_t)lin_fixed(fa.w1, fa.w2, c0, c1);
+    return spl_fixed(fa.b0, fa.b1, fa.b2, fa.b3, c0, c1, c2, c3);
+}
+
+// The splat record of an atom at 1/256-px position (X, Y): base pixel,
+// fractions and the valid bilinear corners with the reference's bbox/size
+// rules (morph.cpp:552-588), packed as
+// {px | py << 16, xf | yf << 8 | valid << 16, colour, rank}.
+__device__ __forceinline__ uint4 finish_record(const RenderScene &sc, uint32_t X, uint32_t Y, uint32_t colour,
+                                               uint32_t r) {
+    uint32_t px = X >> 8, py = Y >> 8, xf = X & 255u, yf = Y & 255u;
+    uint32_t valid = 0;
+    const uint32_t bx1 = sc.bbox[0], by1 = sc.bbox[1], bx2 = sc.bbox[2], by2 = sc.bbox[3];
+    bool skip = (px >= sc.width || py >= sc.height) && (px > bx2 || px < bx1 || py > by2 || py < by1);
+    if (!skip) {
+        if (xf < 255u && yf < 255u) valid |= 1u;
+        if ((px < bx2 || px + 1 < sc.width) && xf > 0u && yf < 255u) valid |= 2u;
+        if ((py < by2 || py + 1 < sc.height) && xf < 255u && yf > 0u) valid |= 4u;
+        if (xf > 0u && yf > 0u && ((py < by2 && px < bx2) || (py + 1 < sc.height && px + 1 < sc.width)))
+            valid |= 8u;
+        // Corners outside the output are dropped (they only arise when the
+        // resolution is smaller than the key frames' bounding box).
+        if (px >= sc.width || py >= sc.height) valid &= ~1u;
+        if (px + 1 >= sc.width || py >= sc.height) valid &= ~2u;
+        if (px >= sc.width || py + 1 >= sc.height) valid &= ~4u;
+        if (px + 1 >= sc.width || py + 1 >= sc.height) valid &= ~8u;
+    }
+    return make_uint4(px | (py << 16), xf | (yf << 8) | (valid << 16), colour, r);
+}
+
+// One atom at the frame's time: exact position, faded colour (morph.cpp:
+// 523-588) and its splat record, FP64 fallback inline.
+__device__ __forceinline__ uint4 splat_atom(const RenderScene &sc, const FrameArgs &fa, const SplatIn &in,
+                                            uint64_t i) {
+    int4 a, b;
+    atom_controls(sc, fa, in, i, a, b);
+    uint32_t X, Y;
+    if (!axis_fast(sc, fa, 0, a, b, &X)) X = axis_fixed(sc, fa, 0, a, b);
+    if (!axis_fast(sc, fa, 1, a, b, &Y)) Y = axis_fixed(sc, fa, 1, a, b);
+    uint2 c = in.col[i];
+    float2 q = in.ls[i];
+    return finish_record(sc, X, Y, fade_colour(sc.fading, c.x, c.y, q.x, q.y, fa.str), in.rank[i]);
+}
+
+// Tiles of the valid corners of a splat record, each distinct tile once:
+// bit k of the returned mask marks corner k as the first valid corner in its
+// tile; tk[k] is that corner's tile.  Registers only.
+__device__ __forceinline__ uint32_t record_tiles(uint4 s, uint32_t tiles_x, uint32_t *tk) {
+    const uint32_t px = s.x & 0xFFFFu, py = s.x >> 16, valid = (s.y >> 16) & 15u;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) tk[k] = ((py + (k >> 1)) / kTile) * tiles_x + (px + (k & 1)) / kTile;
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!(valid & (1u << k))) continue;
+        bool dup = false;
+#pragma unroll
+        for (int j = 0; j < k; ++j) dup |= (valid & (1u << j)) && tk[j] == tk[k];
+        if (!dup) m |= 1u << k;
+    }
+    return m;
+}
+
+__global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs fa, uint64_t n, SplatIn in,
+                                                      uint4 *spl, uint32_t *tile_cnt) {
     extern __shared__ uint32_t hist[];
     const bool smem_hist = fa.ntiles <= 8192;
     if (smem_hist) {
         for (uint32_t i = threadIdx.x; i < fa.ntiles; i += blockDim.x) hist[i] = 0;
         __syncthreads();
     }
-    const uint32_t bx1 = sc.bbox[0], by1 = sc.bbox[1], bx2 = sc.bbox[2], by2 = sc.bbox[3];
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t r = rank[i];
-        uint32_t X, Y;
-        int4 a = pa[i];
-        if (sc.motion == AM_LINEAR) {
-            int32_t xx, yy;
-            X = lin_fast(fa, a.x, a.z, &xx) ? (uint32_t)xx : (uint32_t)lin_fixed(fa.w1, fa.w2, a.x, a.z);
-            Y = lin_fast(fa, a.y, a.w, &yy) ? (uint32_t)yy : (uint32_t)lin_fixed(fa.w1, fa.w2, a.y, a.w);
-        } else if (sc.motion == AM_SPLINE) {
-            int4 b;
-            if (fa.seg_ok) {
-                b = pb[i];
-            } else {
-                uint64_t o = idx[i];
-                uint64_t q0 = sc.P[(uint64_t)fa.seg[0] * sc.N + o], q1 = sc.P[(uint64_t)fa.seg[1] * sc.N + o];
-                uint64_t q2 = sc.P[(uint64_t)fa.seg[2] * sc.N + o], q3 = sc.P[(uint64_t)fa.seg[3] * sc.N + o];
-                a = make_int4(pt_X(q0), pt_Y(q0), pt_X(q1), pt_Y(q1));
-                b = make_int4(pt_X(q2), pt_Y(q2), pt_X(q3), pt_Y(q3));
-            }
-            if (!spl_fast(fa, a.x, a.z, b.x, b.z, &X)) X = spl_fixed(fa, a.x, a.z, b.x, b.z);
-            if (!spl_fast(fa, a.y, a.w, b.y, b.w, &Y)) Y = spl_fixed(fa, a.y, a.w, b.y, b.w);
-        } else {
-            X = (uint32_t)a.x;
-            Y = (uint32_t)a.y;
-        }
-        uint32_t px = X >> 8, py = Y >> 8, xf = X & 255u, yf = Y & 255u;
-        uint2 c = col[i];
-        float2 q = ls[i];
-        uint32_t colour = fade_colour(sc.fading, c.x, c.y, q.x, q.y, fa.str);
-        uint32_t valid = 0;
-        bool skip = (px >= sc.width || py >= sc.height) && (px > bx2 || px < bx1 || py > by2 || py < by1);
-        if (!skip) {
-            if (xf < 255u && yf < 255u) valid |= 1u;
-            if ((px < bx2 || px + 1 < sc.width) && xf > 0u && yf < 255u) valid |= 2u;
-            if ((py < by2 || py + 1 < sc.height) && xf < 255u && yf > 0u) valid |= 4u;
-            if (xf > 0u && yf > 0u && ((py < by2 && px < bx2) || (py + 1 < sc.height && px + 1 < sc.width)))
-                valid |= 8u;
-            // Corners outside the output are dropped (they only arise when the
-            // resolution is smaller than the key frames' bounding box).
-            if (px >= sc.width || py >= sc.height) valid &= ~1u;
-            if (px + 1 >= sc.width || py >= sc.height) valid &= ~2u;
-            if (px >= sc.width || py + 1 >= sc.height) valid &= ~4u;
-            if (px + 1 >= sc.width || py + 1 >= sc.height) valid &= ~8u;
-        }
-        spl[i] = make_uint4(px | (py << 16), xf | (yf << 8) | (valid << 16), colour, r);
-        if (valid) {
-            // Distinct tiles of the valid corners, in registers: corner k sits
-            // at (px + (k & 1), py + (k >> 1)); count a tile at the first
-            // valid corner that lands in it.
-            uint32_t tk[4];
+        uint4 rec = splat_atom(sc, fa, in, i);
+        spl[i] = rec;
+        uint32_t tk[4];
+        uint32_t m = record_tiles(rec, fa.tiles_x, tk);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) tk[k] = ((py + (k >> 1)) / kTile) * fa.tiles_x + (px + (k & 1)) / kTile;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!(valid & (1u << k))) continue;
-                bool dup = false;
-#pragma unroll
-                for (int j = 0; j < k; ++j) dup |= (valid & (1u << j)) && tk[j] == tk[k];
-                if (dup) continue;
-                if (smem_hist) atomicAdd(&hist[tk[k]], 1u);
-                else atomicAdd(&tile_cnt[tk[k]], 1u);
-            }
+        for (int k = 0; k < 4; ++k) {
+            if (!(m & (1u << k))) continue;
+            if (smem_hist) atomicAdd(&hist[tk[k]], 1u);
+            else atomicAdd(&tile_cnt[tk[k]], 1u);
         }
     }
     if (smem_hist) {
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < fa.ntiles; i += blockDim.x)
             if (hist[i]) atomicAdd(&tile_cnt[i], hist[i]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused splat + binning: one cooperative launch per frame.  Each CTA splats
+// a contiguous chunk of `per` x 256 atoms (the pair records are sorted by
+// the tile of the path midpoint, so a chunk touches few tiles), keeps the
+// records in shared memory, counts them per tile in a shared histogram and
+// reserves its share of every tile it touches with one global atomic per
+// tile (the returned count is its offset inside the tile).  After a grid
+// barrier — whose last arriving CTA turns the tile counts into tile offsets
+// and clears the counts for the next frame — every CTA writes its records
+// straight to their tiles.  No splat buffer, no separate scan kernel.
+// The barrier waits are bounded (kBinBarrierTries polls): a CTA that gives
+// up sets the error flag and the abort flag and every CTA leaves.
+constexpr int kBinThreads = 256;
+constexpr uint32_t kBinMaxTiles = 2048;
+constexpr uint32_t kBinBarrierTries = 1u << 24;
+
+struct BinArgs {
+    RenderScene sc;
+    FrameArgs fa;
+    uint64_t n;
+    uint32_t per;           // atoms per thread (records kept in shared memory)
+    SplatIn in;
+    uint4 *rec;
+    uint32_t *tile_cnt;     // [ntiles] zero on entry, zero again on exit
+    uint32_t *tile_off;     // [ntiles + 1] out: exclusive scan of the counts
+    unsigned *bar;          // [0] arrivals, [1] generation, [2] abort
+    int *err;
+};
+
+// Dynamic shared memory of k_frame_bin: records [per][256] uint4, tile
+// histogram and CTA bases [ntiles] u32 each, fallback list [per][512] u16.
+inline size_t bin_smem(uint32_t per, uint32_t ntiles) {
+    return (size_t)per * kBinThreads * 16 + (size_t)ntiles * 8 + (size_t)per * kBinThreads * 2 * 2;
+}
+
+constexpr uint32_t kNoAtom = 0xFFFFFFFFu;  // X of a record slot past the last atom
+
+__global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(BinArgs b) {
+    extern __shared__ __align__(16) unsigned char bsm[];
+    const uint32_t ntiles = b.fa.ntiles, tid = threadIdx.x, per = b.per;
+    uint4 *srec = reinterpret_cast<uint4 *>(bsm);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(bsm + (size_t)per * kBinThreads * 16);
+    uint32_t *base = hist + ntiles;
+    uint16_t *fix = reinterpret_cast<uint16_t *>(base + ntiles);
+    __shared__ uint32_t warp_sum[kBinThreads / 32];
+    __shared__ uint32_t nfix;
+    __shared__ int s_last, s_ok;
+    for (uint32_t t = tid; t < ntiles; t += kBinThreads) hist[t] = 0;
+    if (tid == 0) nfix = 0;
+    __syncthreads();
+    const uint64_t chunk0 = (uint64_t)blockIdx.x * per * kBinThreads;
+    // ---- positions by the integer paths.  Axes that need the reference's
+    // double formula are listed and evaluated together afterwards, so the
+    // slow FP64 work runs in full warps instead of holding up every warp
+    // that contains one such atom.
+    for (uint32_t r = 0; r < per; ++r) {
+        const uint32_t slot = r * kBinThreads + tid;
+        const uint64_t i = chunk0 + slot;
+        uint4 v = make_uint4(kNoAtom, 0, 0, 0);
+        uint32_t need = 0;
+        if (i < b.n) {
+            int4 a, c;
+            atom_controls(b.sc, b.fa, b.in, i, a, c);
+            if (!axis_fast(b.sc, b.fa, 0, a, c, &v.x)) need |= 1u;
+            if (!axis_fast(b.sc, b.fa, 1, a, c, &v.y)) need |= 2u;
+            const uint2 col = b.in.col[i];
+            const float2 q = b.in.ls[i];
+            v.z = fade_colour(b.sc.fading, col.x, col.y, q.x, q.y, b.fa.str);
+            v.w = b.in.rank[i];
+        }
+        srec[slot] = v;
+        const uint32_t k = __popc(need);
+        if (k) {
+            const uint32_t at = atomicAdd(&nfix, k);
+            uint32_t e = 0;
+            if (need & 1u) fix[at + e++] = (uint16_t)(slot * 2);
+            if (need & 2u) fix[at + e] = (uint16_t)(slot * 2 + 1);
+        }
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < nfix; j += kBinThreads) {
+        const uint32_t e = fix[j], slot = e >> 1, axis = e & 1u;
+        int4 a, c;
+        atom_controls(b.sc, b.fa, b.in, chunk0 + slot, a, c);
+        const uint32_t v = axis_fixed(b.sc, b.fa, (int)axis, a, c);
+        if (axis) srec[slot].y = v;
+        else srec[slot].x = v;
+    }
+    __syncthreads();
+    for (uint32_t r = 0; r < per; ++r) {
+        const uint32_t slot = r * kBinThreads + tid;
+        const uint4 v = srec[slot];
+        const uint4 rec = v.x == kNoAtom ? make_uint4(0, 0, 0, 0) : finish_record(b.sc, v.x, v.y, v.z, v.w);
+        srec[slot] = rec;
+        uint32_t tk[4];
+        uint32_t m = record_tiles(rec, b.fa.tiles_x, tk);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (m & (1u << k)) atomicAdd(&hist[tk[k]], 1u);
+    }
+    __syncthreads();
+    for (uint32_t t = tid; t < ntiles; t += kBinThreads) {
+        uint32_t h = hist[t];
+        base[t] = h ? atomicAdd(&b.tile_cnt[t], h) : 0u;
+    }
+    // ---- grid barrier; the last CTA scans the counts into offsets
+    __syncthreads();
+    if (tid == 0) {
+        s_ok = 1;
+        __threadfence();
+        s_last = atomicAdd(b.bar, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        uint32_t carry = 0;
+        for (uint32_t t0 = 0; t0 <= ntiles; t0 += kBinThreads) {
+            const uint32_t t = t0 + tid;
+            const uint32_t v = t < ntiles ? *((volatile uint32_t *)b.tile_cnt + t) : 0u;
+            uint32_t x = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if ((tid & 31) >= (uint32_t)o) x += y;
+            }
+            if ((tid & 31) == 31) warp_sum[tid >> 5] = x;
+            __syncthreads();
+            uint32_t wbase = 0;
+            for (uint32_t w = 0; w < (tid >> 5); ++w) wbase += warp_sum[w];
+            uint32_t total = 0;
+            for (uint32_t w = 0; w < kBinThreads / 32; ++w) total += warp_sum[w];
+            if (t <= ntiles) b.tile_off[t] = carry + wbase + x - v;
+            if (t < ntiles) b.tile_cnt[t] = 0u;
+            carry += total;
+            __syncthreads();
+        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            atomicExch(b.bar, 0u);
+            __threadfence();
+            atomicAdd(b.bar + 1, 1u);
+        }
+    } else if (tid == 0) {
+        // The barrier words are zeroed before every launch and this is the
+        // launch's only barrier: wait for the generation to leave 0.
+        volatile unsigned *gen = b.bar + 1;
+        volatile int *abort_flag = (volatile int *)(b.bar + 2);
+        uint32_t tries = 0;
+        while (*gen == 0u) {
+            if (*abort_flag) { s_ok = 0; break; }
+            if (++tries > kBinBarrierTries) {
+                atomicExch(b.err, AM_ERR_TIMEOUT);
+                atomicExch((int *)(b.bar + 2), 1);
+                s_ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    // ---- records to their tiles
+    for (uint32_t t = tid; t < ntiles; t += kBinThreads)
+        if (hist[t]) hist[t] = __ldcg(b.tile_off + t) + base[t];
+    __syncthreads();
+    for (uint32_t r = 0; r < per; ++r) {
+        const uint4 rec = srec[r * kBinThreads + tid];
+        uint32_t tk[4];
+        uint32_t m = record_tiles(rec, b.fa.tiles_x, tk);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (m & (1u << k)) b.rec[atomicAdd(&hist[tk[k]], 1u)] = rec;
     }
 }
 
@@ -487,7 +766,22 @@ __device__ __forceinline__ uint32_t round_div(unsigned long long num, unsigned l
     return (uint32_t)q;
 }
 
-constexpr int kRecCache = 2048;   // records of a tile kept in shared memory (32 KB)
+// round_div for 32-bit sums: den < 2^24, quotient < 256 (packed path).
+// No 64-bit conversion or 64 x 64 multiply (both are slow on this part).
+__device__ __forceinline__ uint32_t round_div32(uint32_t num, uint32_t den) {
+    float qf = __fdividef(__uint2float_rn(num), __uint2float_rn(den)) + 0.5f;
+    uint32_t q = __float2uint_rz(qf);
+    const unsigned long long a = 2ull * num + den, b = 2ull * den;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const unsigned long long lo = (unsigned long long)(2u * q) * den;  // 32 x 32 -> 64
+        if (a < lo) --q;
+        else if (a >= lo + b) ++q;
+    }
+    return q;
+}
+
+constexpr int kRecCache = 1920;   // records of a tile kept in shared memory (30 KB; 4 CTAs per SM fit)
 constexpr uint32_t kPackMax = 258; // contributions per pixel for which packed 32-bit sums cannot overflow
 
 // Shared memory of the resolve kernel, two layouts over one buffer:
@@ -496,7 +790,31 @@ constexpr uint32_t kPackMax = 258; // contributions per pixel for which packed 3
 //  exact:  W, R, G, B, A as 64-bit sums and N as 32-bit counts.
 constexpr size_t kResolveSmem = 3 * 8 * 1024 + kRecCache * 16;
 
-__global__ void __launch_bounds__(256) k_frame_resolve(const uint4 *__restrict__ rec,
+// Ordered "over" of one more blob's colour onto a pixel (morph.cpp:1357-1380)
+// in FP64 with round-to-nearest operations; `first` seeds the state from the
+// pixel's first blob colour c0.  Out of line and on local memory: only pixels
+// covered by two or more blobs get here.
+__device__ __noinline__ void over_blob(double *st, bool first, uint32_t c0, uint32_t cc) {
+    if (first) {
+        st[0] = (c0 & 255u) / 255.0; st[1] = ((c0 >> 8) & 255u) / 255.0;
+        st[2] = ((c0 >> 16) & 255u) / 255.0; st[3] = (c0 >> 24) / 255.0;
+    }
+    const double sr = (cc & 255u) / 255.0, sg = ((cc >> 8) & 255u) / 255.0, sb = ((cc >> 16) & 255u) / 255.0,
+                 sa = (cc >> 24) / 255.0;
+    const double om = __dsub_rn(1.0, sa);
+    st[0] = __dadd_rn(__dmul_rn(sa, sr), __dmul_rn(om, st[0]));
+    st[1] = __dadd_rn(__dmul_rn(sa, sg), __dmul_rn(om, st[1]));
+    st[2] = __dadd_rn(__dmul_rn(sa, sb), __dmul_rn(om, st[2]));
+    st[3] = __dadd_rn(st[3], __dmul_rn(__dsub_rn(1.0, st[3]), sa));
+}
+// create_color's round(x * 255) of the composite (atomorph.h color rules).
+__device__ __noinline__ uint32_t over_bytes(const double *st) {
+    uint32_t o = 0;
+    for (int k = 0; k < 4; ++k) o |= ((uint32_t)(int)round(__dmul_rn(st[k], 255.0)) & 255u) << (8 * k);
+    return o;
+}
+
+__global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restrict__ rec,
                                                         const uint32_t *__restrict__ tile_off, uint32_t tiles_x,
                                                         uint32_t width, uint32_t height, uint32_t density,
                                                         uint8_t *out) {
@@ -515,7 +833,7 @@ __global__ void __launch_bounds__(256) k_frame_resolve(const uint4 *__restrict__
     const uint32_t lr = threadIdx.x >> 3, lc0 = (threadIdx.x & 7) * 4;
     int n[4];
     uint32_t c0[4];
-    double R[4], G[4], B[4], A[4];
+    double st[4][4];  // FP64 "over" state (R, G, B, A) of pixels with 2+ blobs; local memory, rarely touched
     for (int mode = 0; mode < 2; ++mode) {
         const bool packed = mode == 0;
         const bool cached = packed && nrec <= (uint32_t)kRecCache;
@@ -601,25 +919,21 @@ __global__ void __launch_bounds__(256) k_frame_resolve(const uint4 *__restrict__
                 }
                 if (!cnt) continue;
                 uint32_t r, g, b, a;
-                r = round_div(sr, W); g = round_div(sg, W); b = round_div(sb, W);
-                a = cnt >= density ? round_div(sa, W)
-                                   : round_div((unsigned long long)cnt * sa, (unsigned long long)density * W);
+                if (packed) {
+                    const uint32_t w32 = (uint32_t)W;
+                    r = round_div32((uint32_t)sr, w32); g = round_div32((uint32_t)sg, w32);
+                    b = round_div32((uint32_t)sb, w32);
+                    a = cnt >= density ? round_div32((uint32_t)sa, w32)
+                                       : round_div((unsigned long long)cnt * sa, (unsigned long long)density * W);
+                } else {
+                    r = round_div(sr, W); g = round_div(sg, W); b = round_div(sb, W);
+                    a = cnt >= density ? round_div(sa, W)
+                                       : round_div((unsigned long long)cnt * sa, (unsigned long long)density * W);
+                }
                 if (a == 0) continue;  // draw_atoms skips transparent blob pixels
                 uint32_t cc = r | (g << 8) | (b << 16) | (a << 24);
-                if (n[q] == 0) {
-                    c0[q] = cc;
-                } else {
-                    if (n[q] == 1) {
-                        R[q] = (c0[q] & 255u) / 255.0; G[q] = ((c0[q] >> 8) & 255u) / 255.0;
-                        B[q] = ((c0[q] >> 16) & 255u) / 255.0; A[q] = (c0[q] >> 24) / 255.0;
-                    }
-                    double sr_ = r / 255.0, sg_ = g / 255.0, sb_ = b / 255.0, sa_ = a / 255.0;
-                    double om = __dsub_rn(1.0, sa_);
-                    R[q] = __dadd_rn(__dmul_rn(sa_, sr_), __dmul_rn(om, R[q]));
-                    G[q] = __dadd_rn(__dmul_rn(sa_, sg_), __dmul_rn(om, G[q]));
-                    B[q] = __dadd_rn(__dmul_rn(sa_, sb_), __dmul_rn(om, B[q]));
-                    A[q] = __dadd_rn(A[q], __dmul_rn(__dsub_rn(1.0, A[q]), a / 255.0));
-                }
+                if (n[q] == 0) c0[q] = cc;
+                else over_blob(st[q], n[q] == 1, c0[q], cc);
                 n[q]++;
             }
             __syncthreads();
@@ -633,14 +947,7 @@ __global__ void __launch_bounds__(256) k_frame_resolve(const uint4 *__restrict__
     if (gy >= height || gx >= width) return;
     uint32_t o[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        if (n[q] == 0) o[q] = 0;
-        else if (n[q] == 1) o[q] = c0[q];
-        else {
-            auto cb = [](double v) { return (uint32_t)(int)round(__dmul_rn(v, 255.0)) & 255u; };
-            o[q] = cb(R[q]) | (cb(G[q]) << 8) | (cb(B[q]) << 16) | (cb(A[q]) << 24);
-        }
-    }
+    for (int q = 0; q < 4; ++q) o[q] = n[q] == 0 ? 0u : (n[q] == 1 ? c0[q] : over_bytes(st[q]));
     uint8_t *dst = out + ((size_t)gy * width + gx) * 4;
     if (gx + 4 <= width && (((uintptr_t)dst & 15u) == 0)) {
         *reinterpret_cast<uint4 *>(dst) = make_uint4(o[0], o[1], o[2], o[3]);
@@ -673,6 +980,34 @@ int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32
     AMG_LAUNCH(k_keyframe_copy, grid, 256, 0, s, display, present, CW, CH, width, height, (uint32_t *)out);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
+}
+
+// Atoms per thread of the fused launch: the smallest count (1..8) whose
+// co-resident grid covers n atoms; 0 when even 8 does not.
+static uint32_t bin_per(uint64_t n, uint32_t ntiles) {
+    static int occ[9];
+    static uint32_t occ_tiles = UINT32_MAX;
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    if (occ_tiles != ntiles) {
+        for (int p = 0; p < 9; ++p) occ[p] = -1;
+        occ_tiles = ntiles;
+    }
+    for (uint32_t p = 1; p <= 8; ++p) {
+        if (occ[p] < 0) {
+            size_t smem = bin_smem(p, ntiles);
+            cudaFuncSetAttribute(k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            int o = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_frame_bin, kBinThreads, smem) != cudaSuccess) o = 0;
+            occ[p] = o;
+        }
+        if ((uint64_t)occ[p] * sms * kBinThreads * p >= n) return p;
+    }
+    return 0;
 }
 
 static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStream_t s) {
@@ -729,7 +1064,13 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
         AMG_CUDA(cudaMalloc(&w->tile_off, (ntiles + 1) * 4));
         AMG_CUDA(cudaMalloc(&w->tile_cur, (ntiles + 1) * 4));
+        AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
         w->ntiles_cap = ntiles + 1;
+    }
+    if (!w->bar) {
+        AMG_CUDA(cudaMalloc(&w->bar, 4 * sizeof(unsigned)));
+        AMG_CUDA(cudaMalloc(&w->err, sizeof(int)));
+        AMG_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), s));
     }
     uint64_t need = w->active * 4 + 16;
     if (need > w->rec_cap) {
@@ -742,6 +1083,11 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     fa.w1 = 1.0 - t;
     fa.w2 = 1.0 - fa.w1;
     fa.w1q = llround(std::ldexp(fa.w1, 38));
+    auto split = [](long long q, int32_t *h, int32_t *l) {
+        *h = (int32_t)(q >> 19);  // arithmetic shift: floor division
+        *l = (int32_t)(q & ((1ll << 19) - 1));
+    };
+    split(fa.w1q, &fa.w1h, &fa.w1l);
     fa.lin_mode = fa.w1 == 1.0 ? 1u : (fa.w1 == 0.0 ? 2u : 0u);
     fa.str = (float)(1.0 - t);
     fa.tiles_x = tiles_x;
@@ -764,31 +1110,64 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         fa.bq0 = llround(std::ldexp(fa.b0, 38));
         fa.bq2 = llround(std::ldexp(fa.b2, 38));
         fa.bq3 = llround(std::ldexp(fa.b3, 38));
+        split(fa.bq0, &fa.bh0, &fa.bl0);
+        split(fa.bq2, &fa.bh2, &fa.bl2);
+        split(fa.bq3, &fa.bh3, &fa.bl3);
         fa.key_mode = (fa.b0 == 0.0 && fa.b1 == 1.0 && fa.b2 == 0.0 && fa.b3 == 0.0) ? 1u : 0u;
+        if (!fa.key_mode) {
+            const uint32_t tn = std::max(std::max(sc.CW, sc.CH), std::max(sc.width, sc.height)) + 1;
+            if (tn > w->stab_cap) {
+                if (w->stab) cudaFree(w->stab);
+                w->stab = nullptr;
+                w->stab_cap = 0;
+                AMG_CUDA(cudaMalloc(&w->stab, (size_t)tn * 4));
+                w->stab_cap = tn;
+            }
+            AMG_LAUNCH(k_spline_table, (tn + 255) / 256, 256, 0, s, fa.b0, fa.b1, fa.b2, fa.b3, tn, w->stab);
+            fa.stab = w->stab;
+            fa.stab_n = tn;
+        }
     }
-    AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
     uint64_t n = w->active;
-    if (n) {
-        unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 4);
-        size_t smem = ntiles <= 8192 ? ntiles * 4 : 0;
+    SplatIn in{w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2};
+    uint32_t per = n && ntiles <= kBinMaxTiles ? bin_per(n, ntiles) : 0;
+    if (n && ntiles <= kBinMaxTiles && per) {
+        // fused splat + binning (one cooperative launch)
+        BinArgs b;
+        b.sc = sc; b.fa = fa; b.n = n; b.per = per; b.in = in; b.rec = w->rec;
+        b.tile_cnt = w->tile_cnt; b.tile_off = w->tile_off; b.bar = w->bar; b.err = w->err;
+        AMG_CUDA(cudaMemsetAsync(w->bar, 0, 4 * sizeof(unsigned), s));
+        unsigned grid = (unsigned)((n + (uint64_t)per * kBinThreads - 1) / ((uint64_t)per * kBinThreads));
+        void *params[] = {&b};
         if (w->prof) w->prof->open(s);
-        AMG_LAUNCH(k_frame_splat, grid, 256, smem, s, sc, fa, n, w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2,
-                   w->spl, w->tile_cnt);
-        if (w->prof) w->prof->close(PROF_SPLAT, s);
-    }
-    AMG_CUDA(cudaMemcpyAsync(w->tile_off, w->tile_cnt, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
-    {
-        if (w->prof) w->prof->open(s);
-        int rc = launch_scan_u32(w->tile_off, (size_t)ntiles + 1, nullptr, s);
-        if (rc) return rc;
-        if (w->prof) w->prof->close(PROF_SCAN, s);
-    }
-    AMG_CUDA(cudaMemcpyAsync(w->tile_cur, w->tile_off, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
-    if (n) {
-        unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 4);
-        if (w->prof) w->prof->open(s);
-        AMG_LAUNCH(k_frame_scatter, grid, 256, 0, s, w->spl, n, tiles_x, w->tile_cur, w->rec);
-        if (w->prof) w->prof->close(PROF_SCATTER, s);
+        AMG_CUDA(cudaLaunchCooperativeKernel((const void *)k_frame_bin, dim3(grid), dim3(kBinThreads), params,
+                                             bin_smem(per, ntiles), s));
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (w->prof) w->prof->close(PROF_BIN, s);
+    } else {
+        AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
+        if (n) {
+            unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 8);
+            size_t smem = ntiles <= 8192 ? ntiles * 4 : 0;
+            if (w->prof) w->prof->open(s);
+            AMG_LAUNCH(k_frame_splat, grid, 256, smem, s, sc, fa, n, in, w->spl, w->tile_cnt);
+            if (w->prof) w->prof->close(PROF_SPLAT, s);
+        }
+        AMG_CUDA(cudaMemcpyAsync(w->tile_off, w->tile_cnt, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
+        {
+            if (w->prof) w->prof->open(s);
+            int rc = launch_scan_u32(w->tile_off, (size_t)ntiles + 1, nullptr, s);
+            if (rc) return rc;
+            if (w->prof) w->prof->close(PROF_SCAN, s);
+        }
+        AMG_CUDA(cudaMemcpyAsync(w->tile_cur, w->tile_off, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
+        if (n) {
+            unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 8);
+            if (w->prof) w->prof->open(s);
+            AMG_LAUNCH(k_frame_scatter, grid, 256, 0, s, w->spl, n, tiles_x, w->tile_cur, w->rec);
+            if (w->prof) w->prof->close(PROF_SCATTER, s);
+        }
+        AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));  // the fused path expects zero counts
     }
     if (w->prof) w->prof->open(s);
     {

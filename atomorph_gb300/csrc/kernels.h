@@ -61,8 +61,9 @@ struct BatchArgs {
     const BatchJob *jobs;
     uint32_t njobs;
     const uint32_t *ch_job;      // chunk -> job
-    const uint64_t *ch_start;    // first pair index (t of sweep_pair) of the chunk
+    const uint64_t *ch_start;    // first pair of the chunk (within its frame)
     const uint32_t *ch_count;    // pairs in the chunk
+    const uint32_t *ch_fi;       // the chunk's frame within the job's phase
     uint32_t ch_off[4];          // chunks of phase p: [ch_off[p], ch_off[p+1])
     uint32_t nphase;             // phases of the longest schedule (<= 3)
     uint32_t sweeps;

@@ -18,14 +18,12 @@ __device__ __forceinline__ uint32_t find_chain(const uint64_t *__restrict__ off,
     return lo;
 }
 
-// Pair t of a phase (t = fi * pairs + r): frame y = frames[fi], pair r of the
-// chains' disjoint random pairs (a keyed Feistel permutation of each chain's
+// Pair r of phase frame fi: frame y = frames[fi], pair r of the chains'
+// disjoint random pairs (a keyed Feistel permutation of each chain's
 // columns, consecutive positions paired).  The reference's criterion
 // (thread.cpp:1014-1022), exact in integers: swap when c1 >= c2.
-__device__ __forceinline__ void sweep_pair(const SweepArgs &a, uint64_t pairs, uint64_t t, unsigned long long &gain,
+__device__ __forceinline__ void sweep_pair(const SweepArgs &a, uint32_t fi, uint64_t r, unsigned long long &gain,
                                            unsigned long long &acc) {
-    uint32_t fi = (uint32_t)(t / pairs);
-    uint64_t r = t - (uint64_t)fi * pairs;
     uint32_t y = __ldg(a.frames + fi);
     uint32_t yn = y + 1 == a.K ? 0 : y + 1;
     uint32_t yp = y == 0 ? a.K - 1 : y - 1;

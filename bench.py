@@ -194,6 +194,7 @@ def bench_ours(args, rank, world):
     dom_avg_ms = dom_ms / dom_n
     # Algorithmic bytes attributed to the dominant kernel (roofline)
     kernel_bytes = {
+        "k_frame_bin": N * 56 + N * 16,
         "k_frame_splat": N * 56,
         "k_frame_scatter": N * 16 * 2,
         "k_frame_resolve": N * 16 + m.width * m.height * 4,
