@@ -785,10 +785,10 @@ constexpr int kRecCache = 1920;   // records of a tile kept in shared memory (30
 constexpr uint32_t kPackMax = 258; // contributions per pixel for which packed 32-bit sums cannot overflow
 
 // Shared memory of the resolve kernel, two layouts over one buffer:
-//  packed: WN[1024] (W sum low 40 bits | count << 40), RG[1024], BA[1024]
-//          (two 32-bit channel sums each), then the record cache;
+//  packed: W, N, R, G, B, A as 32-bit sums [1024] each (exact while a pixel
+//          has at most kPackMax contributions), then the record cache;
 //  exact:  W, R, G, B, A as 64-bit sums and N as 32-bit counts.
-constexpr size_t kResolveSmem = 3 * 8 * 1024 + kRecCache * 16;
+constexpr size_t kResolveSmem = 6 * 4 * 1024 + kRecCache * 16;
 
 // Ordered "over" of one more blob's colour onto a pixel (morph.cpp:1357-1380)
 // in FP64 with round-to-nearest operations; `first` seeds the state from the
@@ -821,36 +821,45 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ uint32_t red[8];
     __shared__ int s_over;
-    unsigned long long *WN = reinterpret_cast<unsigned long long *>(sm);
-    unsigned long long *RG = WN + 1024, *BA = WN + 2048;
-    uint4 *cache = reinterpret_cast<uint4 *>(sm + 3 * 8 * 1024);
-    unsigned long long *xW = WN, *xR = WN + 1024, *xG = WN + 2048, *xB = WN + 3072, *xA = WN + 4096;
-    uint32_t *xN = reinterpret_cast<uint32_t *>(WN + 5120);
+    // packed mode: six 32-bit accumulators per pixel (a warp's 32-bit
+    // atomics spread over 32 banks); exact mode: 64-bit sums and a count
+    uint32_t *pW = reinterpret_cast<uint32_t *>(sm), *pN = pW + 1024, *pR = pW + 2048, *pG = pW + 3072,
+             *pB = pW + 4096, *pA = pW + 5120;
+    uint4 *cache = reinterpret_cast<uint4 *>(sm + 6 * 4 * 1024);
+    unsigned long long *xW = reinterpret_cast<unsigned long long *>(sm), *xR = xW + 1024, *xG = xW + 2048,
+                       *xB = xW + 3072, *xA = xW + 4096;
+    uint32_t *xN = reinterpret_cast<uint32_t *>(xW + 5120);
     const uint32_t tile = blockIdx.x;
     const uint32_t tx0 = (tile % tiles_x) * kTile, ty0 = (tile / tiles_x) * kTile;
     const uint32_t beg = tile_off[tile], end = tile_off[tile + 1];
     const uint32_t nrec = end - beg;
-    const uint32_t lr = threadIdx.x >> 3, lc0 = (threadIdx.x & 7) * 4;
+    // thread t owns pixels t, t + 256, t + 512, t + 768 of the tile (rows
+    // t/32 + 8q): a warp reads 32 consecutive accumulators and stores 32
+    // consecutive output pixels
     int n[4];
     uint32_t c0[4];
     double st[4][4];  // FP64 "over" state (R, G, B, A) of pixels with 2+ blobs; local memory, rarely touched
     for (int mode = 0; mode < 2; ++mode) {
         const bool packed = mode == 0;
         const bool cached = packed && nrec <= (uint32_t)kRecCache;
+        uint32_t mn = 0xFFFFFFFFu;
         if (packed) {
-            for (int i = threadIdx.x; i < 3 * 1024; i += 256) WN[i] = 0ull;
+            for (int i = threadIdx.x; i < 6 * 1024; i += 256) pW[i] = 0u;
             if (cached)
-                for (uint32_t j = threadIdx.x; j < nrec; j += 256) cache[j] = rec[beg + j];
+                for (uint32_t j = threadIdx.x; j < nrec; j += 256) {
+                    const uint4 v = rec[beg + j];
+                    cache[j] = v;
+                    mn = min(mn, v.w);
+                }
         } else {
-            for (int i = threadIdx.x; i < 5 * 1024; i += 256) WN[i] = 0ull;
+            for (int i = threadIdx.x; i < 5 * 1024; i += 256) xW[i] = 0ull;
             for (int i = threadIdx.x; i < 1024; i += 256) xN[i] = 0u;
         }
         if (threadIdx.x == 0) s_over = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; }
-        __syncthreads();
-        uint32_t mn = 0xFFFFFFFFu;
-        for (uint32_t j = threadIdx.x; j < nrec; j += 256) mn = min(mn, cached ? cache[j].w : rec[beg + j].w);
+        if (!cached)
+            for (uint32_t j = threadIdx.x; j < nrec; j += 256) mn = min(mn, rec[beg + j].w);
         for (int o = 16; o; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
         __syncthreads();
@@ -878,9 +887,12 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
                     uint32_t li = cy * kTile + cx;
                     uint32_t W = wx[k & 1] * wy[k >> 1];
                     if (packed) {
-                        atomicAdd(&WN[li], (unsigned long long)W | (1ull << 40));
-                        atomicAdd(&RG[li], (unsigned long long)(W * cr) | ((unsigned long long)(W * cg) << 32));
-                        atomicAdd(&BA[li], (unsigned long long)(W * cb) | ((unsigned long long)(W * ca) << 32));
+                        atomicAdd(&pW[li], W);
+                        atomicAdd(&pN[li], 1u);
+                        atomicAdd(&pR[li], W * cr);
+                        atomicAdd(&pG[li], W * cg);
+                        atomicAdd(&pB[li], W * cb);
+                        atomicAdd(&pA[li], W * ca);
                     } else {
                         atomicAdd(&xW[li], (unsigned long long)W);
                         atomicAdd(&xR[li], (unsigned long long)(W * cr));
@@ -895,23 +907,22 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
             __syncthreads();
             if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nxt;
             if (packed) {
+                // more than kPackMax contributions could have wrapped a 32-bit sum
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    if ((WN[lr * kTile + lc0 + q] >> 40) > kPackMax) s_over = 1;
+                    if (pN[threadIdx.x + 256 * q] > kPackMax) s_over = 1;
                 __syncthreads();
                 if (s_over) { over = true; break; }
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                uint32_t li = lr * kTile + lc0 + q;
+                const uint32_t li = threadIdx.x + 256 * q;
                 unsigned long long W, sr, sg, sb, sa;
                 uint32_t cnt;
                 if (packed) {
-                    unsigned long long wn = WN[li], rg = RG[li], ba = BA[li];
-                    cnt = (uint32_t)(wn >> 40);
-                    W = wn & ((1ull << 40) - 1);
-                    sr = rg & 0xFFFFFFFFull; sg = rg >> 32; sb = ba & 0xFFFFFFFFull; sa = ba >> 32;
-                    WN[li] = 0ull; RG[li] = 0ull; BA[li] = 0ull;
+                    cnt = pN[li];
+                    W = pW[li]; sr = pR[li]; sg = pG[li]; sb = pB[li]; sa = pA[li];
+                    pW[li] = 0u; pN[li] = 0u; pR[li] = 0u; pG[li] = 0u; pB[li] = 0u; pA[li] = 0u;
                 } else {
                     cnt = xN[li];
                     W = xW[li]; sr = xR[li]; sg = xG[li]; sb = xB[li]; sa = xA[li];
@@ -943,16 +954,13 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
         if (!over) break;
         __syncthreads();
     }
-    uint32_t gy = ty0 + lr, gx = tx0 + lc0;
-    if (gy >= height || gx >= width) return;
-    uint32_t o[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) o[q] = n[q] == 0 ? 0u : (n[q] == 1 ? c0[q] : over_bytes(st[q]));
-    uint8_t *dst = out + ((size_t)gy * width + gx) * 4;
-    if (gx + 4 <= width && (((uintptr_t)dst & 15u) == 0)) {
-        *reinterpret_cast<uint4 *>(dst) = make_uint4(o[0], o[1], o[2], o[3]);
-    } else {
-        for (int q = 0; q < 4 && gx + q < width; ++q) reinterpret_cast<uint32_t *>(dst)[q] = o[q];
+    for (int q = 0; q < 4; ++q) {
+        const uint32_t li = threadIdx.x + 256 * q;
+        const uint32_t gy = ty0 + (li >> 5), gx = tx0 + (li & 31u);
+        if (gy >= height || gx >= width) continue;
+        const uint32_t o = n[q] == 0 ? 0u : (n[q] == 1 ? c0[q] : over_bytes(st[q]));
+        reinterpret_cast<uint32_t *>(out)[(size_t)gy * width + gx] = o;
     }
 }
 
