@@ -37,22 +37,29 @@ namespace amg {
 constexpr int kTile = 32;
 constexpr uint32_t kInactive = 0xFFFFFFFFu;
 
-struct RenderWork {
-    int pair_f = -1;
-    uint64_t cap = 0;       // atom capacity of the buffers below
-    uint64_t active = 0;    // active atoms of the prepared pair (sorted first)
-    uint32_t motion = 0, fading = 0;
+// Prepared records of one key-frame pair (sorted by the tile of the path
+// midpoint); kept per pair while the chains do not change, so a cycle of
+// frames prepares each pair once.
+struct PairData {
+    int f = -1;                          // key frame of the pair held (-1: none)
+    uint32_t motion = 0, fading = 0, width = 0, height = 0;
+    uint64_t cap = 0;
     int4 *pa = nullptr, *pb = nullptr;   // endpoints / spline control points
     uint2 *col = nullptr;
     float2 *ls = nullptr;
     uint32_t *rank = nullptr, *idx = nullptr;
-    int4 *pa2 = nullptr, *pb2 = nullptr;
-    uint2 *col2 = nullptr;
-    float2 *ls2 = nullptr;
-    uint32_t *rank2 = nullptr, *idx2 = nullptr;
+    uint32_t *d_active = nullptr;        // active (sorted first) atoms, on the device
+};
+
+struct RenderWork {
+    uint64_t cap = 0;       // atom capacity of the prep scratch below
+    int4 *pa = nullptr, *pb = nullptr;   // unsorted prep output (scratch)
+    uint2 *col = nullptr;
+    float2 *ls = nullptr;
+    uint32_t *rank = nullptr;
     uint32_t *keys = nullptr, *vals = nullptr, *tkeys = nullptr, *tvals = nullptr, *hist = nullptr;
-    uint32_t *d_active = nullptr;
     uint4 *spl = nullptr;
+    std::vector<PairData> pairs;         // cache slots
     uint4 *rec = nullptr;
     uint64_t rec_cap = 0;
     uint32_t *tile_cnt = nullptr, *tile_off = nullptr, *tile_cur = nullptr;
@@ -66,21 +73,34 @@ struct RenderWork {
     Prof *prof = nullptr;   // optional per-kernel timing
 };
 
+// Device memory the pair cache may hold (beyond one pair, which is always
+// kept): all K pairs of a 1M-atom, 8-key-frame morph take 450 MB.
+constexpr uint64_t kPairCacheBytes = 8ull << 30;
+constexpr uint64_t kPairBytesPerAtom = 16 + 16 + 8 + 8 + 4 + 4;
+
 void render_set_prof(RenderWork *w, Prof *p) { w->prof = p; }
 
 RenderWork *render_work_create() { return new RenderWork(); }
 
-static void rw_free(RenderWork *w) {
-    void *ps[] = {w->pa, w->pb, w->col, w->ls, w->rank, w->idx, w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2,
-                  w->keys, w->vals, w->tkeys, w->tvals, w->hist, w->spl, w->d_active};
+static void pair_free(PairData &d) {
+    void *ps[] = {d.pa, d.pb, d.col, d.ls, d.rank, d.idx, d.d_active};
     for (void *p : ps)
         if (p) cudaFree(p);
-    w->pa = w->pb = w->pa2 = w->pb2 = nullptr;
-    w->col = w->col2 = nullptr;
-    w->ls = w->ls2 = nullptr;
-    w->rank = w->idx = w->rank2 = w->idx2 = w->keys = w->vals = w->tkeys = w->tvals = w->hist = w->d_active = nullptr;
+    d = PairData();
+}
+
+static void rw_free(RenderWork *w) {
+    void *ps[] = {w->pa, w->pb, w->col, w->ls, w->rank, w->keys, w->vals, w->tkeys, w->tvals, w->hist, w->spl};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    w->pa = w->pb = nullptr;
+    w->col = nullptr;
+    w->ls = nullptr;
+    w->rank = w->keys = w->vals = w->tkeys = w->tvals = w->hist = nullptr;
     w->spl = nullptr;
     w->cap = 0;
+    for (auto &d : w->pairs) pair_free(d);
+    w->pairs.clear();
 }
 
 void render_work_destroy(RenderWork *w) {
@@ -97,7 +117,9 @@ void render_work_destroy(RenderWork *w) {
     delete w;
 }
 
-void render_invalidate(RenderWork *w) { w->pair_f = -1; }
+void render_invalidate(RenderWork *w) {
+    for (auto &d : w->pairs) d.f = -1;
+}
 
 int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope) {
     if (!w->perm) AMG_CUDA(cudaMalloc(&w->perm, 1024 * sizeof(int)));
@@ -106,7 +128,7 @@ int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope)
     std::memcpy(h.data() + 512, perm_slope, 512 * sizeof(int));
     AMG_CUDA(cudaMemcpy(w->perm, h.data(), 1024 * sizeof(int), cudaMemcpyHostToDevice));
     w->perm_set = true;
-    w->pair_f = -1;
+    render_invalidate(w);
     return AM_OK;
 }
 
@@ -119,21 +141,27 @@ static int rw_reserve(RenderWork *w, uint64_t n) {
     AMG_CUDA(cudaMalloc(&w->col, c * sizeof(uint2)));
     AMG_CUDA(cudaMalloc(&w->ls, c * sizeof(float2)));
     AMG_CUDA(cudaMalloc(&w->rank, c * 4));
-    AMG_CUDA(cudaMalloc(&w->idx, c * 4));
-    AMG_CUDA(cudaMalloc(&w->pa2, c * sizeof(int4)));
-    AMG_CUDA(cudaMalloc(&w->pb2, c * sizeof(int4)));
-    AMG_CUDA(cudaMalloc(&w->col2, c * sizeof(uint2)));
-    AMG_CUDA(cudaMalloc(&w->ls2, c * sizeof(float2)));
-    AMG_CUDA(cudaMalloc(&w->rank2, c * 4));
-    AMG_CUDA(cudaMalloc(&w->idx2, c * 4));
     AMG_CUDA(cudaMalloc(&w->keys, c * 4));
     AMG_CUDA(cudaMalloc(&w->vals, c * 4));
     AMG_CUDA(cudaMalloc(&w->tkeys, c * 4));
     AMG_CUDA(cudaMalloc(&w->tvals, c * 4));
     AMG_CUDA(cudaMalloc(&w->hist, radix_hist_words(c) * 4));
     AMG_CUDA(cudaMalloc(&w->spl, c * sizeof(uint4)));
-    AMG_CUDA(cudaMalloc(&w->d_active, 4));
     w->cap = c;
+    return AM_OK;
+}
+
+static int pair_reserve(PairData &d, uint64_t c) {
+    if (d.cap >= c) return AM_OK;
+    pair_free(d);
+    AMG_CUDA(cudaMalloc(&d.pa, c * sizeof(int4)));
+    AMG_CUDA(cudaMalloc(&d.pb, c * sizeof(int4)));
+    AMG_CUDA(cudaMalloc(&d.col, c * sizeof(uint2)));
+    AMG_CUDA(cudaMalloc(&d.ls, c * sizeof(float2)));
+    AMG_CUDA(cudaMalloc(&d.rank, c * 4));
+    AMG_CUDA(cudaMalloc(&d.idx, c * 4));
+    AMG_CUDA(cudaMalloc(&d.d_active, 4));
+    d.cap = c;
     return AM_OK;
 }
 
@@ -521,8 +549,9 @@ __device__ __forceinline__ uint32_t record_tiles(uint4 s, uint32_t tiles_x, uint
     return m;
 }
 
-__global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs fa, uint64_t n, SplatIn in,
-                                                      uint4 *spl, uint32_t *tile_cnt) {
+__global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs fa, const uint32_t *n_dev,
+                                                      SplatIn in, uint4 *spl, uint32_t *tile_cnt) {
+    const uint64_t n = *n_dev;
     extern __shared__ uint32_t hist[];
     const bool smem_hist = fa.ntiles <= 8192;
     if (smem_hist) {
@@ -567,7 +596,7 @@ constexpr uint32_t kBinBarrierTries = 1u << 24;
 struct BinArgs {
     RenderScene sc;
     FrameArgs fa;
-    uint64_t n;
+    const uint32_t *n;      // atoms of the pair (device; the grid covers an upper bound)
     uint32_t per;           // atoms per thread (records kept in shared memory)
     SplatIn in;
     uint4 *rec;
@@ -599,6 +628,7 @@ __global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(BinArgs b) {
     if (tid == 0) nfix = 0;
     __syncthreads();
     const uint64_t chunk0 = (uint64_t)blockIdx.x * per * kBinThreads;
+    const uint64_t n_atoms = *b.n;
     // ---- positions by the integer paths.  Axes that need the reference's
     // double formula are listed and evaluated together afterwards, so the
     // slow FP64 work runs in full warps instead of holding up every warp
@@ -608,7 +638,7 @@ __global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(BinArgs b) {
         const uint64_t i = chunk0 + slot;
         uint4 v = make_uint4(kNoAtom, 0, 0, 0);
         uint32_t need = 0;
-        if (i < b.n) {
+        if (i < n_atoms) {
             int4 a, c;
             atom_controls(b.sc, b.fa, b.in, i, a, c);
             if (!axis_fast(b.sc, b.fa, 0, a, c, &v.x)) need |= 1u;
@@ -725,8 +755,9 @@ __global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(BinArgs b) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_frame_scatter(const uint4 *__restrict__ spl, uint64_t n,
+__global__ void __launch_bounds__(256) k_frame_scatter(const uint4 *__restrict__ spl, const uint32_t *n_dev,
                                                         uint32_t tiles_x, uint32_t *tile_cur, uint4 *rec) {
+    const uint64_t n = *n_dev;
     const int lane = threadIdx.x & 31;
     for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t i = base + threadIdx.x;
@@ -1018,9 +1049,23 @@ static uint32_t bin_per(uint64_t n, uint32_t ntiles) {
     return 0;
 }
 
-static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStream_t s) {
+// The cache slot holding pair f (prepared now when it is not there yet).
+static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStream_t s, PairData **out) {
     int rc = rw_reserve(w, sc.N);
     if (rc) return rc;
+    uint64_t per_pair = w->cap * kPairBytesPerAtom;
+    size_t slots = (size_t)std::max<uint64_t>(1, std::min<uint64_t>(sc.K, kPairCacheBytes / std::max<uint64_t>(per_pair, 1)));
+    if (w->pairs.size() != slots) {
+        for (auto &d : w->pairs) pair_free(d);
+        w->pairs.assign(slots, PairData());
+    }
+    PairData &d = w->pairs[f % slots];
+    *out = &d;
+    if (d.f == (int)f && d.motion == sc.motion && d.fading == sc.fading && d.width == sc.width &&
+        d.height == sc.height)
+        return AM_OK;
+    if ((rc = pair_reserve(d, w->cap))) return rc;
+    if (w->prof) w->prof->open(s);
     uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
     unsigned grid = (unsigned)std::min<uint64_t>((sc.N + 255) / 256, (uint64_t)kSMs * 8);
     AMG_LAUNCH(k_pair_prep, grid, 256, 0, s, sc, f, w->perm_set ? w->perm : nullptr, w->pa, w->pb, w->col, w->ls,
@@ -1030,16 +1075,16 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
     while ((1ull << bits) < (uint64_t)tiles_x * tiles_y + 1) ++bits;
     rc = radix_sort_pairs(w->keys, w->vals, w->tkeys, w->tvals, w->hist, sc.N, bits, s);
     if (rc) return rc;
-    AMG_CUDA(cudaMemsetAsync(w->d_active, 0, 4, s));
-    AMG_LAUNCH(k_pair_gather, grid, 256, 0, s, w->keys, w->vals, sc.N, w->pa, w->pb, w->col, w->ls, w->rank,
-               w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2, (int)(sc.motion == AM_SPLINE), w->d_active);
-    uint32_t act = 0;
-    AMG_CUDA(cudaMemcpyAsync(&act, w->d_active, 4, cudaMemcpyDeviceToHost, s));
-    AMG_CUDA(cudaStreamSynchronize(s));
-    w->active = act;
-    w->pair_f = (int)f;
-    w->motion = sc.motion;
-    w->fading = sc.fading;
+    AMG_CUDA(cudaMemsetAsync(d.d_active, 0, 4, s));
+    AMG_LAUNCH(k_pair_gather, grid, 256, 0, s, w->keys, w->vals, sc.N, w->pa, w->pb, w->col, w->ls, w->rank, d.pa,
+               d.pb, d.col, d.ls, d.rank, d.idx, (int)(sc.motion == AM_SPLINE), d.d_active);
+    AMG_CUDA(cudaGetLastError());
+    if (w->prof) w->prof->close(PROF_PAIR, s);
+    d.f = (int)f;
+    d.motion = sc.motion;
+    d.fading = sc.fading;
+    d.width = sc.width;
+    d.height = sc.height;
     return AM_OK;
 }
 
@@ -1057,11 +1102,10 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     }
     double dt = 1.0 / double(sc.K);
     double t = std::max(0.0, (time - (double)(frame_key * dt)) / dt);
-    if (w->pair_f != (int)f || w->motion != sc.motion || w->fading != sc.fading) {
-        if (w->prof) w->prof->open(s);
-        int rc = prep_pair(w, sc, (uint32_t)f, s);
+    PairData *pd = nullptr;
+    {
+        int rc = prep_pair(w, sc, (uint32_t)f, s, &pd);
         if (rc) return rc;
-        if (w->prof) w->prof->close(PROF_PAIR, s);
     }
     uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
     uint32_t ntiles = tiles_x * tiles_y;
@@ -1080,7 +1124,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         AMG_CUDA(cudaMalloc(&w->err, sizeof(int)));
         AMG_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), s));
     }
-    uint64_t need = w->active * 4 + 16;
+    uint64_t need = sc.N * 4 + 16;  // an atom has records in at most 4 tiles
     if (need > w->rec_cap) {
         if (w->rec) cudaFree(w->rec);
         w->rec_cap = need + need / 4;
@@ -1136,13 +1180,14 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
             fa.stab_n = tn;
         }
     }
-    uint64_t n = w->active;
-    SplatIn in{w->pa2, w->pb2, w->col2, w->ls2, w->rank2, w->idx2};
+    // atoms of the pair: at most N; the active count stays on the device
+    uint64_t n = sc.N;
+    SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx};
     uint32_t per = n && ntiles <= kBinMaxTiles ? bin_per(n, ntiles) : 0;
     if (n && ntiles <= kBinMaxTiles && per) {
         // fused splat + binning (one cooperative launch)
         BinArgs b;
-        b.sc = sc; b.fa = fa; b.n = n; b.per = per; b.in = in; b.rec = w->rec;
+        b.sc = sc; b.fa = fa; b.n = pd->d_active; b.per = per; b.in = in; b.rec = w->rec;
         b.tile_cnt = w->tile_cnt; b.tile_off = w->tile_off; b.bar = w->bar; b.err = w->err;
         AMG_CUDA(cudaMemsetAsync(w->bar, 0, 4 * sizeof(unsigned), s));
         unsigned grid = (unsigned)((n + (uint64_t)per * kBinThreads - 1) / ((uint64_t)per * kBinThreads));
@@ -1158,7 +1203,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
             unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 8);
             size_t smem = ntiles <= 8192 ? ntiles * 4 : 0;
             if (w->prof) w->prof->open(s);
-            AMG_LAUNCH(k_frame_splat, grid, 256, smem, s, sc, fa, n, in, w->spl, w->tile_cnt);
+            AMG_LAUNCH(k_frame_splat, grid, 256, smem, s, sc, fa, pd->d_active, in, w->spl, w->tile_cnt);
             if (w->prof) w->prof->close(PROF_SPLAT, s);
         }
         AMG_CUDA(cudaMemcpyAsync(w->tile_off, w->tile_cnt, (ntiles + 1) * 4, cudaMemcpyDeviceToDevice, s));
@@ -1172,7 +1217,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         if (n) {
             unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 8);
             if (w->prof) w->prof->open(s);
-            AMG_LAUNCH(k_frame_scatter, grid, 256, 0, s, w->spl, n, tiles_x, w->tile_cur, w->rec);
+            AMG_LAUNCH(k_frame_scatter, grid, 256, 0, s, w->spl, pd->d_active, tiles_x, w->tile_cur, w->rec);
             if (w->prof) w->prof->close(PROF_SCATTER, s);
         }
         AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));  // the fused path expects zero counts
