@@ -38,6 +38,7 @@ UNITS = [
     ("engine.cpp", ["-x", "cu"]),
     ("engine_mlp.cpp", ["-x", "cu"]),
     ("k_fluid.cu", []),
+    ("k_fluid_morph.cu", []),
     ("noalloc.cu", []),
     ("k_batch.cu", []),
     ("engine_batch.cpp", ["-x", "cu"]),

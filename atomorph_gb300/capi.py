@@ -107,6 +107,9 @@ _SIGS = {
     "am_fluid_step": (C.c_int, [vp, C.c_size_t, C.c_double]),
     "am_fluid_steps": (C.c_int, [vp, C.c_size_t, C.c_double]),
     "am_fluid_stream": (vp, [vp]),
+    "am_fluid_render": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_double, C.POINTER(C.c_uint32), C.c_double, u8p]),
+    "am_set_fluid_sparseness": (C.c_int, [vp, C.c_double]),
+    "am_get_fluid_particles": (C.c_size_t, [vp, f64p, C.c_size_t]),
     "am_set_tuning": (C.c_int, [vp, C.c_char_p, C.c_double]),
     "am_batch_create": (C.c_int, [C.POINTER(vp), C.POINTER(vp), C.c_size_t]),
     "am_batch_destroy": (None, [vp]),
@@ -199,6 +202,14 @@ class Morph:
             else:
                 _check(f(self.h, v), "am_set_" + k)
         return self
+
+    def fluid_particles(self) -> np.ndarray:
+        """[18, n] particle fields of the morph's fluid (oracle order)."""
+        n = self.lib.am_get_fluid_particles(self.h, None, 0)
+        q = np.zeros((max(n, 1), 18))
+        if n:
+            self.lib.am_get_fluid_particles(self.h, _p(q, f64p), n)
+        return q[:n].T.copy()
 
     def tune(self, **kw) -> "Morph":
         """Guided-refinement tunables (am_set_tuning): local_self,
@@ -443,6 +454,12 @@ class Fluid:
 
     def steps(self, n: int, freedom_radius: float) -> None:
         _check(self.lib.am_fluid_steps(self.h, n, freedom_radius), "am_fluid_steps")
+
+    def render(self, width: int, height: int, sparseness: float, bbox, t: float) -> np.ndarray:
+        out = np.zeros((height, width, 4), np.uint8)
+        bb = (C.c_uint32 * 4)(*[int(v) for v in bbox])
+        _check(self.lib.am_fluid_render(self.h, width, height, sparseness, bb, t, _p(out, u8p)), "am_fluid_render")
+        return out
 
 
 class Batch:

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <new>
 
+#include "fluid.cuh"
 #include "handle.h"
 
 namespace amg {
@@ -139,6 +140,18 @@ int am_set_tuning(am_morph *m, const char *name, double value) {
         else return AM_ERR_ARG;
     }
     return AM_OK;
+}
+int am_set_fluid_sparseness(am_morph *m, double v) {
+    CHECK(m);
+    if (!(v > 0.0 && v <= 64.0)) return AM_ERR_ARG;
+    H(m).front.fluid_sparseness = v;
+    return AM_OK;
+}
+size_t am_get_fluid_particles(am_morph *m, double *state, size_t cap) {
+    if (!m || !m->e.fluid) return 0;
+    const size_t n = m->e.fluid->n;
+    if (state && cap >= n && amg::fluid_get(m->e.fluid, state, m->e.rstream) != AM_OK) return 0;
+    return n;
 }
 int am_set_motion_noise(am_morph *m, double a) {
     CHECK(m);

@@ -63,4 +63,19 @@ int am_fluid_steps(am_fluid *h, size_t n, double freedom_radius) {
 
 void *am_fluid_stream(am_fluid *h) { return h ? (void *)h->s : nullptr; }
 
+int am_fluid_render(am_fluid *h, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox, double t,
+                    uint8_t *rgba_out) {
+    if (!h || !bbox || !rgba_out || !width || !height || !(sparseness > 0.0)) return AM_ERR_ARG;
+    uint8_t *d = nullptr;
+    const size_t bytes = (size_t)width * height * 4;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+        amg::set_error("cudaMalloc failed");
+        return AM_ERR_NOMEM;
+    }
+    int rc = amg::fluid_render_only(h->f, width, height, sparseness, bbox, t, d, h->s);
+    if (!rc && cudaMemcpy(rgba_out, d, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = AM_ERR_CUDA;
+    cudaFree(d);
+    return rc;
+}
+
 }  // extern "C"

@@ -9,6 +9,7 @@
 // publishes the worker's results to the front copy that rendering reads
 // (morph.cpp:102-269), so a frame can be rendered while the worker refines.
 #include "engine.h"
+#include "fluid.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -51,6 +52,8 @@ Engine::~Engine() {
     }
     if (rw) render_work_destroy(rw);
     if (bw) blob_work_destroy(bw);
+    if (fluid) fluid_destroy(fluid);
+    if (fmorph) fluid_morph_destroy(fmorph);
     d_raw.release(); d_stored.release(); d_display.release(); d_present.release(); d_labels.release();
     d_P.release(); d_Pf.release(); d_chain_off.release(); d_pair_off.release(); d_chain_off_f.release();
     d_singles.release(); d_rank_f.release(); d_phase.release(); d_acc.release(); d_stats.release();
@@ -682,6 +685,7 @@ int Engine::refine_plain(size_t sweeps, uint64_t *gains) {
 }
 
 int Engine::publish_front() {
+    ++publish_count;
     fK = K; fC = C; fN = N;
     f_widths = widths; f_chain_off = chain_off; f_keys = frame_keys;
     f_blobs = blobs;
@@ -763,6 +767,9 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
             rc = copy_keyframe(f, dst);
             if (rc) return rc;
         }
+    } else if (front.fluidsteps > 0) {
+        rc = render_fluid(t, dst);
+        if (rc) return rc;
     } else {
         RenderScene sc;
         sc.K = fK; sc.C = fC; sc.N = fN; sc.CW = CW; sc.CH = CH; sc.width = width; sc.height = height;
@@ -783,6 +790,59 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         AMG_CUDA(cudaGetLastError());
     }
     return AM_OK;
+}
+
+// The fluid frame (morph::get_pixels with fluid steps, morph.cpp:1417): the
+// particles are stepped to time t and drawn.  Like the reference, every call
+// advances the simulation, so frames are meant to be rendered in order.
+int Engine::render_fluid(double t, uint8_t *dst) {
+    const double sp = front.fluid_sparseness;
+    const uint32_t gsx = (uint32_t)std::lround(width * sp) + 20, gsy = (uint32_t)std::lround(height * sp) + 20;
+    if (!fluid || fluid->n != fN || fluid_gsx != gsx || fluid_gsy != gsy) {
+        // particle count = sum of the chains' maximum surfaces = N at density 1
+        // (morph.cpp:234-260); a new count or grid restarts the simulation
+        if (fluid) fluid_destroy(fluid);
+        if (fmorph) fluid_morph_destroy(fmorph);
+        fluid = fluid_create(gsx, gsy, (uint32_t)fN);
+        fmorph = fluid_morph_create();
+        if (!fluid || !fmorph) { set_error("fluid: out of device memory"); return AM_ERR_NOMEM; }
+        fluid_gsx = gsx;
+        fluid_gsy = gsy;
+        fluid_front = UINT64_MAX;
+    }
+    int rc;
+    if (fluid_front != publish_count) {
+        if ((rc = d_fchain_id.reserve(std::max<uint64_t>(fN, 1)))) return rc;
+        if ((rc = launch_chain_ids(d_chain_off_f.p, fC, fN, d_fchain_id.p, rstream))) return rc;
+        // surface of each chain's blob per key frame (blob_before/after ->surface.size())
+        surf_host.assign((size_t)fK * fC, 0);
+        for (uint32_t k = 0; k < fK && k < f_blobs.size(); ++k)
+            for (uint32_t c = 0; c < fC; ++c) {
+                const int32_t b = f_rank[(size_t)k * fC + c];
+                if (b >= 0 && (size_t)b < f_blobs[k].size()) surf_host[(size_t)k * fC + c] = (uint32_t)f_blobs[k][b].size;
+            }
+        if ((rc = d_surf.reserve(std::max<size_t>(surf_host.size(), 1)))) return rc;
+        AMG_CUDA(cudaMemcpyAsync(d_surf.p, surf_host.data(), surf_host.size() * 4, cudaMemcpyHostToDevice, rstream));
+        fluid_front = publish_count;
+    }
+    FluidFrame fr;
+    fr.sc.K = fK; fr.sc.C = fC; fr.sc.N = fN; fr.sc.CW = CW; fr.sc.CH = CH; fr.sc.width = width; fr.sc.height = height;
+    fr.sc.bbox[0] = bbox_x1; fr.sc.bbox[1] = bbox_y1; fr.sc.bbox[2] = bbox_x2; fr.sc.bbox[3] = bbox_y2;
+    fr.sc.motion = front.motion; fr.sc.fading = front.fading; fr.sc.density = front.density;
+    fr.sc.P = d_Pf.p; fr.sc.chain_off = d_chain_off_f.p; fr.sc.display = d_display.p; fr.sc.rank = d_rank_f.p;
+    const size_t f = std::min<size_t>((size_t)(t * fK), fK - 1);
+    fr.time = t;
+    fr.frame_key = f < f_keys.size() ? f_keys[f] : f;
+    fr.sparseness = sp;
+    fr.chain_id = d_fchain_id.p;
+    fr.surf = d_surf.p;
+    fr.surf_host = surf_host.data();
+    fr.chain_off_host = f_chain_off.data();
+    fr.perm = render_perm(rw);
+    fr.fluidsteps = front.fluidsteps;
+    fr.seed_key = mix64((uint64_t)seed << 24 ^ 0x666c7569ull);
+    fr.rw = rw;
+    return fluid_morph_frame(fmorph, fluid, fr, dst, rstream);
 }
 
 int Engine::import_chains(size_t k_, size_t c_, const uint64_t *w, const uint64_t *pts, const int32_t *order) {

@@ -35,6 +35,7 @@ struct Params {  // defaults of morph.h:97-119
     double learned_keep = 0.25;  // fraction of slots the learned gate lets scan
     double guided_switch = 1e-3;  // plain -> guided when a plain sweep gains less than this fraction
     double motion_noise = 0.0;
+    double fluid_sparseness = 1.0;  // solver grid units per pixel (the reference's sparseness)
 };
 
 struct HostFrame {
@@ -175,6 +176,14 @@ class Engine {
 
     Prof prof;
     RenderWork *rw = nullptr;
+    // fluid path of the render (step_fluid + draw_fluid)
+    FluidDev *fluid = nullptr;
+    FluidMorph *fmorph = nullptr;
+    uint32_t fluid_gsx = 0, fluid_gsy = 0;
+    uint64_t publish_count = 0, fluid_front = UINT64_MAX;
+    DBuf<uint32_t> d_fchain_id, d_surf;
+    std::vector<uint32_t> surf_host;
+    int render_fluid(double t, uint8_t *dst);
     BlobWork *bw = nullptr;
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_n = 0;

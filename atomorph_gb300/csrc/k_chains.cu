@@ -226,8 +226,85 @@ int launch_sweep_random(const SweepArgs &a, cudaStream_t s) {
 
 size_t radix_hist_words(size_t n) { return 256 * ((n + kRsTile - 1) / kRsTile) + 1; }
 
+// Multi-CTA exclusive scan for large arrays: block sums of kScanBlock
+// elements, a single-CTA scan of the sums, then each block's scan with its
+// offset.
+constexpr uint32_t kScanBlock = 4096;  // 1024 threads x 4
+
+__device__ __forceinline__ uint32_t block_excl_scan_1024(uint32_t v, uint32_t *warp_tot, uint32_t *block_total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    const uint32_t excl = (warp ? warp_tot[warp - 1] : 0u) + x - v;
+    if (block_total) *block_total = warp_tot[31];
+    __syncthreads();
+    return excl;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(const uint32_t *__restrict__ a, size_t n, uint32_t *sums) {
+    __shared__ uint32_t warp_tot[32];
+    const size_t base = (size_t)blockIdx.x * kScanBlock + (size_t)threadIdx.x * 4;
+    uint32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (base + k < n) v += a[base + k];
+    uint32_t tot = 0;
+    block_excl_scan_1024(v, warp_tot, &tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_apply(uint32_t *a, size_t n, const uint32_t *__restrict__ offs) {
+    __shared__ uint32_t warp_tot[32];
+    const size_t base = (size_t)blockIdx.x * kScanBlock + (size_t)threadIdx.x * 4;
+    uint32_t v[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = base + k < n ? a[base + k] : 0u;
+        sum += v[k];
+    }
+    uint32_t run = block_excl_scan_1024(sum, warp_tot, nullptr) + offs[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) a[base + k] = run;
+        run += v[k];
+    }
+}
+
 int launch_scan_u32(uint32_t *a, size_t n, uint32_t *total, cudaStream_t s) {
-    AMG_LAUNCH(k_scan_u32, 1, 1024, 0, s, a, n, total);
+    if (n <= 8 * (size_t)kScanBlock) {
+        AMG_LAUNCH(k_scan_u32, 1, 1024, 0, s, a, n, total);
+        AMG_CUDA(cudaGetLastError());
+        return AM_OK;
+    }
+    static thread_local uint32_t *sums = nullptr;
+    static thread_local size_t sums_cap = 0;
+    const size_t nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb + 1 > sums_cap) {
+        if (sums) cudaFree(sums);
+        sums = nullptr;
+        sums_cap = 0;
+        AMG_CUDA(cudaMalloc(&sums, (nb + 1) * sizeof(uint32_t)));
+        sums_cap = nb + 1;
+    }
+    AMG_LAUNCH(k_scan_sums, (unsigned)nb, 1024, 0, s, a, n, sums);
+    AMG_LAUNCH(k_scan_u32, 1, 1024, 0, s, sums, nb, total);
+    AMG_LAUNCH(k_scan_apply, (unsigned)nb, 1024, 0, s, a, n, sums);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }
@@ -241,7 +318,8 @@ int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tk, uint32_t *tv,
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
         AMG_LAUNCH(k_rs_hist, ntiles, kRsThreads, 0, s, ki, n, shift, hist, ntiles);
-        AMG_LAUNCH(k_scan_u32, 1, 1024, 0, s, hist, (size_t)256 * ntiles, (uint32_t *)nullptr);
+        int rc = launch_scan_u32(hist, (size_t)256 * ntiles, nullptr, s);
+        if (rc) return rc;
         AMG_LAUNCH(k_rs_scatter, ntiles, kRsThreads, 0, s, ki, vi, ko, vo, n, shift, hist, ntiles);
         std::swap(ki, ko);
         std::swap(vi, vo);

@@ -22,25 +22,15 @@
 // Grid clearing replaces the reference's active-node list: every node a step
 // touches is zero before the next step either way.
 #include "common.cuh"
+#include "fluid.cuh"
 #include "kernels.h"
 
 #include <vector>
 
 namespace amg {
 
-struct FluidDev {
-    uint32_t gsx = 0, gsy = 0, n = 0;
-    float *P = nullptr;      // [kFlFields][n]
-    uint8_t *flags = nullptr;// [n] bit0 active, bit1 mature
-    int2 *cell = nullptr;    // [n] stencil origin
-    float *G = nullptr;      // [kFlNode][gsx*gsy]
-    uint64_t step = 0;
-};
-
 namespace {
 
-enum { PX, PY, PU, PV, PGX, PGY, PFR, PSTR, PR_, PG_, PB_, PA_, Pr, Pg, Pb, Pa, kFlFields };
-enum { NM, ND, NGX, NGY, NAX, NAY, NU, NV, NW, NR, NG, NB, NA, kFlNode };
 
 struct Stencil {
     int cx, cy;

@@ -334,6 +334,14 @@ int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K,
     return AM_OK;
 }
 
+int launch_chain_ids(const uint64_t *chain_off, uint32_t C, uint64_t N, uint32_t *out, cudaStream_t s) {
+    if (!N) return AM_OK;
+    unsigned grid = (unsigned)std::min<uint64_t>((N + 255) / 256, (uint64_t)kSMs * 8);
+    AMG_LAUNCH(k_chain_ids, grid, 256, 0, s, chain_off, C, N, out);
+    AMG_CUDA(cudaGetLastError());
+    return AM_OK;
+}
+
 int launch_local_propose(const LocalArgs &a, cudaStream_t s) {
     uint64_t total = a.N * a.nframes;
     if (!total) return AM_OK;

@@ -27,6 +27,7 @@
 //                  composite morph.cpp:1348-1402 in FP64; 16-byte RGBA8 stores.
 #include "common.cuh"
 #include "kernels.h"
+#include "render_math.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -117,6 +118,8 @@ void render_work_destroy(RenderWork *w) {
     delete w;
 }
 
+const int *render_perm(RenderWork *w) { return w->perm_set ? w->perm : nullptr; }
+
 void render_invalidate(RenderWork *w) {
     for (auto &d : w->pairs) d.f = -1;
 }
@@ -174,36 +177,6 @@ __device__ __forceinline__ uint32_t find_chain_r(const uint64_t *__restrict__ of
         if (__ldg(off + mid) <= r) lo = mid; else hi = mid;
     }
     return lo;
-}
-
-// ----------------------------------------------------------- Perlin FP32 --
-// Improved Perlin noise at z = 0 (perlin.cpp:19-43; the z terms vanish since
-// fade(0) = 0), 8 octaves (perlin.cpp:57-69), on a permutation in smem.
-__device__ __forceinline__ float pgrad(int hash, float x, float y) {
-    int h = hash & 15;
-    float u = h < 8 ? x : y, v = h < 4 ? y : (h == 12 || h == 14 ? x : 0.f);
-    return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
-}
-__device__ __forceinline__ float pfade(float t) { return t * t * t * (t * (t * 6.f - 15.f) + 10.f); }
-__device__ float pnoise(const int *p, float x, float y) {
-    float fx = floorf(x), fy = floorf(y);
-    int X = (int)fx & 255, Y = (int)fy & 255;
-    x -= fx; y -= fy;
-    float u = pfade(x), v = pfade(y);
-    int A = p[X] + Y, AA = p[A], AB = p[A + 1];
-    int B = p[X + 1] + Y, BA = p[B], BB = p[B + 1];
-    float l1 = pgrad(p[AA], x, y) + u * (pgrad(p[BA], x - 1.f, y) - pgrad(p[AA], x, y));
-    float l2 = pgrad(p[AB], x, y - 1.f) + u * (pgrad(p[BB], x - 1.f, y - 1.f) - pgrad(p[AB], x, y - 1.f));
-    return l1 + v * (l2 - l1);
-}
-__device__ float poctave(const int *p, float x, float y) {
-    float r = 0.f, amp = 1.f;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        r += pnoise(p, x, y) * amp;
-        x *= 2.f; y *= 2.f; amp *= 0.5f;
-    }
-    return r;
 }
 
 __global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, const int *__restrict__ perm,
@@ -281,132 +254,12 @@ __global__ void k_pair_gather(const uint32_t *__restrict__ keys, const uint32_t 
     }
 }
 
-struct FrameArgs {
-    double w1, w2;          // LINEAR: weight of pt1 and 1 - that weight
-    double b0, b1, b2, b3;  // SPLINE basis at the frame's local time
-    long long w1q;          // round(w1 * 2^38)
-    long long bq0, bq2, bq3;// round(b_i * 2^38) (b1 enters through the q1 term)
-    // The same weights split as hi * 2^19 + lo (lo in [0, 2^19)), so every
-    // product with a 32-bit coordinate difference is a 32 x 32 -> 64-bit
-    // multiply: 64 x 64-bit integer multiplies are slow on this part.
-    int32_t w1h, w1l, bh0, bl0, bh2, bl2, bh3, bl3;
-    // SPLINE: the reference's double result for a coordinate that sits on
-    // the integer pixel p in all four control frames (an atom that does not
-    // move along that axis): stab[p] for p < stab_n.  The fixed-point value
-    // of such a coordinate is exactly an integer, i.e. on a rounding
-    // boundary, so without the table every such atom would need the FP64
-    // evaluation.
-    const uint32_t *stab;
-    uint32_t stab_n;
-    uint32_t lin_mode;      // 0 general, 1 w1 == 1 (X = X1), 2 w1 == 0 (X = X2)
-    uint32_t key_mode;      // 1 when the spline basis is exactly (0, 1, 0, 0)
-    uint32_t seg_ok;        // 1 when the spline segment is the prepared one
-    int32_t seg[4];         // control frames when seg_ok == 0
-    float str;              // colour weight of the earlier key frame, 1 - t
-    uint32_t tiles_x, ntiles;
-};
-
-// Fast exact positions.  The reference evaluates its interpolation in
-// double.  The kernels evaluate the same formula's real value in 64-bit fixed
-// point (weights quantised to 2^-38) and take its floor / rounded fraction,
-// which equals the reference's unless the value lies within the combined
-// error bound of a rounding boundary; those rare atoms re-run the reference's
-// own double formula (lin_fixed / spl_fixed below).  The bound is per atom:
-// quantising a weight moves the value by at most half a unit of 2^-38 per
-// unit of the coordinate difference it multiplies, i.e. |d| / 2 fixed-point
-// units in total, and the reference's double rounding (a handful of
-// operations on values below 2^16 px, plus its weights summing to 1 only
-// within a few ulps) stays below 2^13 units of 2^-46 px.  Returns false when
-// the fallback is needed.
-__device__ __forceinline__ bool lin_fast(const FrameArgs &fa, int32_t a, int32_t b, int32_t *out) {
-    if (fa.lin_mode == 1) { *out = a; return true; }
-    if (fa.lin_mode == 2) { *out = b; return true; }
-    const int32_t d = a - b;
-    long long V = ((long long)b << 38) + (long long)fa.w1h * d * (1ll << 19) + (long long)fa.w1l * d;  // 2^-38 (1/256 px)
-    const long long one = 1ll << 38;
-    const long long tol = (long long)((uint32_t)abs(d) >> 1) + (1ll << 13);
-    long long r = V & (one - 1);
-    if (r < tol || one - r < tol) return false;
-    *out = (int32_t)(V >> 38);
-    return true;
-}
-__device__ __forceinline__ bool spl_fast(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
-                                         uint32_t *out) {
-    if ((abs(q0 - q1) | abs(q2 - q1) | abs(q3 - q1)) >= (1 << 22)) return false;  // keeps V in 63 bits
-    const int32_t d0 = q0 - q1, d2 = q2 - q1, d3 = q3 - q1;
-    long long V = ((long long)q1 << 38) +
-                  ((long long)fa.bh0 * d0 + (long long)fa.bh2 * d2 + (long long)fa.bh3 * d3) * (1ll << 19) +
-                  (long long)fa.bl0 * d0 + (long long)fa.bl2 * d2 + (long long)fa.bl3 * d3;  // units of 2^-46 px
-    unsigned long long A = V >= 0 ? (unsigned long long)V : (unsigned long long)(-V);
-    const unsigned long long one = 1ull << 46;
-    unsigned long long I = A >> 46, F = A & (one - 1);
-    if (!fa.key_mode) {
-        const unsigned long long tol =
-            (unsigned long long)(((uint32_t)abs(d0) + (uint32_t)abs(d2) + (uint32_t)abs(d3)) >> 1) + (1ull << 14);
-        if (F < tol || one - F < tol) return false;
-        unsigned long long h = ((F << 8) - F) & (one - 1);  // F * 255 mod one
-        unsigned long long dd = h > (one >> 1) ? h - (one >> 1) : (one >> 1) - h;
-        if (dd < 255ull * tol) return false;
-    }
-    unsigned long long xf = ((F << 8) - F + (one >> 1)) >> 46;  // round(F * 255), half away on |fraction|
-    uint32_t xi = (uint32_t)I & 0xFFFFu, xb = (uint32_t)xf & 0xFFu;
-    if (V < 0) { xi = (0u - xi) & 0xFFFFu; xb = (0u - xb) & 0xFFu; }
-    *out = (xi << 8) | xb;
-    return true;
-}
-
-// The FP64 fallbacks are out of line on purpose: inlined, the compiler may
-// evaluate them under a predicate for every atom, and FP64 throughput is low.
-__device__ __noinline__ int32_t lin_fixed(double w1, double w2, int32_t a, int32_t b) {
-    double v = __dadd_rn(__dmul_rn(w1, (double)a), __dmul_rn(w2, (double)b));
-    return (int32_t)v;  // v >= 0: truncation is floor
-}
-// Catmull-Rom value at the prepared basis, then the reference's modf /
-// round(fract * 255) split (morph.cpp:528-530).  Returns the 1/256 grid
-// position as (integer part << 8) | fract byte with the integer part taken
-// modulo 2^16 like the x86 build's double -> uint16 conversion.
-__device__ __noinline__ uint32_t spl_fixed(double b0, double b1, double b2, double b3, int32_t q0, int32_t q1,
-                                           int32_t q2, int32_t q3) {
-    double v0 = (double)(q0 >> 8) + (double)(q0 & 255) / 256.0;
-    double v1 = (double)(q1 >> 8) + (double)(q1 & 255) / 256.0;
-    double v2 = (double)(q2 >> 8) + (double)(q2 & 255) / 256.0;
-    double v3 = (double)(q3 >> 8) + (double)(q3 & 255) / 256.0;
-    double v = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, b0), __dmul_rn(v1, b1)), __dmul_rn(v2, b2)),
-                         __dmul_rn(v3, b3));
-    double ip = trunc(v);
-    double fr = __dsub_rn(v, ip);
-    uint32_t xi = (uint32_t)(int)ip & 0xFFFFu;
-    uint32_t xf = (uint32_t)(int)round(__dmul_rn(fr, 255.0)) & 0xFFu;
-    return (xi << 8) | xf;
-}
-
 __global__ void k_spline_table(double b0, double b1, double b2, double b3, uint32_t n, uint32_t *tab) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < n) {
         const int32_t q = (int32_t)(p << 8);
         tab[p] = spl_fixed(b0, b1, b2, b3, q, q, q, q);
     }
-}
-
-// Colour fade of one atom (morph.cpp:537-550, 1467-1488) in FP32.
-__device__ __forceinline__ uint32_t fade_colour(uint32_t fading, uint32_t c1, uint32_t c2, float lag, float slope,
-                                                float str) {
-    if (fading == AM_PERLIN || fading == AM_COSINE) {
-        const float pi = 3.14159265358f;
-        float s = (slope + 0.1f) / 1.1f;
-        float l = (1.f - s) * lag;
-        if (str <= l) str = 0.f;
-        else if (str >= l + s) str = 1.f;
-        else str = (-cosf((str - l) * (pi / s)) + 1.f) * 0.5f;
-    }
-    uint32_t o = 0;
-#pragma unroll
-    for (int ch = 0; ch < 4; ++ch) {
-        float a = (float)((c1 >> (8 * ch)) & 255u), b = (float)((c2 >> (8 * ch)) & 255u);
-        float v = str * a + (1.f - str) * b;
-        o |= ((uint32_t)(int)roundf(v) & 255u) << (8 * ch);
-    }
-    return o;
 }
 
 // Up to four distinct tiles touched by the valid corners of base pixel
@@ -424,17 +277,6 @@ __device__ __forceinline__ int corner_tiles(uint32_t px, uint32_t py, uint32_t v
         if (!dup) t[n++] = tt;
     }
     return n;
-}
-
-// A coordinate on the same integer pixel in all four control frames: the
-// per-frame table holds the reference's double result.
-__device__ __forceinline__ bool spl_static(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
-                                           uint32_t *out) {
-    if (fa.key_mode || q0 != q1 || q2 != q1 || q3 != q1 || (q1 & 255) || q1 < 0) return false;
-    const uint32_t p = (uint32_t)q1 >> 8;
-    if (p >= fa.stab_n) return false;
-    *out = __ldg(fa.stab + p);
-    return true;
 }
 
 struct SplatIn {
@@ -1088,6 +930,63 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
     return AM_OK;
 }
 
+// Position / colour arithmetic of the frame at global time `time` (local
+// time t in pair f): linear weights, the spline basis of
+// GetInterpolatedSplinePoint (spline.cpp:45-57) and its fixed-point split,
+// and the per-frame table of static spline coordinates.
+int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, double t, FrameArgs *out,
+               cudaStream_t s) {
+    FrameArgs &fa = *out;
+    std::memset(&fa, 0, sizeof(fa));
+    fa.w1 = 1.0 - t;
+    fa.w2 = 1.0 - fa.w1;
+    fa.w1q = llround(std::ldexp(fa.w1, 38));
+    auto split = [](long long q, int32_t *h, int32_t *l) {
+        *h = (int32_t)(q >> 19);  // arithmetic shift: floor division
+        *l = (int32_t)(q & ((1ll << 19) - 1));
+    };
+    split(fa.w1q, &fa.w1h, &fa.w1l);
+    fa.lin_mode = fa.w1 == 1.0 ? 1u : (fa.w1 == 0.0 ? 2u : 0u);
+    fa.str = (float)(1.0 - t);
+    fa.seg_ok = 1;
+    if (sc.motion == AM_SPLINE) {
+        // GetInterpolatedSplinePoint(time) (spline.cpp:45-57) basis.
+        int n = (int)sc.K;
+        double delta_t = 1.0 / n;
+        int p = (int)(time / delta_t);
+        auto wrap = [n](int i) { return i < 0 ? n - 1 : (i >= n ? i - n : i); };
+        double lt = (time - delta_t * (double)p) / delta_t;
+        double t2 = lt * lt, t3 = t2 * lt;
+        fa.b0 = 0.5 * (-t3 + 2.0 * t2 - lt);
+        fa.b1 = 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
+        fa.b2 = 0.5 * (-3.0 * t3 + 4.0 * t2 + lt);
+        fa.b3 = 0.5 * (t3 - t2);
+        fa.seg[0] = wrap(p - 1); fa.seg[1] = wrap(p); fa.seg[2] = wrap(p + 1); fa.seg[3] = wrap(p + 2);
+        fa.seg_ok = (p == (int)f) ? 1u : 0u;
+        fa.bq0 = llround(std::ldexp(fa.b0, 38));
+        fa.bq2 = llround(std::ldexp(fa.b2, 38));
+        fa.bq3 = llround(std::ldexp(fa.b3, 38));
+        split(fa.bq0, &fa.bh0, &fa.bl0);
+        split(fa.bq2, &fa.bh2, &fa.bl2);
+        split(fa.bq3, &fa.bh3, &fa.bl3);
+        fa.key_mode = (fa.b0 == 0.0 && fa.b1 == 1.0 && fa.b2 == 0.0 && fa.b3 == 0.0) ? 1u : 0u;
+        if (!fa.key_mode) {
+            const uint32_t tn = std::max(std::max(sc.CW, sc.CH), std::max(sc.width, sc.height)) + 1;
+            if (tn > w->stab_cap) {
+                if (w->stab) cudaFree(w->stab);
+                w->stab = nullptr;
+                w->stab_cap = 0;
+                AMG_CUDA(cudaMalloc(&w->stab, (size_t)tn * 4));
+                w->stab_cap = tn;
+            }
+            AMG_LAUNCH(k_spline_table, (tn + 255) / 256, 256, 0, s, fa.b0, fa.b1, fa.b2, fa.b3, tn, w->stab);
+            fa.stab = w->stab;
+            fa.stab_n = tn;
+        }
+    }
+    return AM_OK;
+}
+
 int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, uint8_t *out,
                  cudaStream_t s) {
     const size_t bytes = (size_t)sc.width * sc.height * 4;
@@ -1131,55 +1030,12 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         AMG_CUDA(cudaMalloc(&w->rec, w->rec_cap * sizeof(uint4)));
     }
     FrameArgs fa;
-    std::memset(&fa, 0, sizeof(fa));
-    fa.w1 = 1.0 - t;
-    fa.w2 = 1.0 - fa.w1;
-    fa.w1q = llround(std::ldexp(fa.w1, 38));
-    auto split = [](long long q, int32_t *h, int32_t *l) {
-        *h = (int32_t)(q >> 19);  // arithmetic shift: floor division
-        *l = (int32_t)(q & ((1ll << 19) - 1));
-    };
-    split(fa.w1q, &fa.w1h, &fa.w1l);
-    fa.lin_mode = fa.w1 == 1.0 ? 1u : (fa.w1 == 0.0 ? 2u : 0u);
-    fa.str = (float)(1.0 - t);
+    {
+        int rc = frame_args(w, sc, time, (uint32_t)f, t, &fa, s);
+        if (rc) return rc;
+    }
     fa.tiles_x = tiles_x;
     fa.ntiles = ntiles;
-    fa.seg_ok = 1;
-    if (sc.motion == AM_SPLINE) {
-        // GetInterpolatedSplinePoint(time) (spline.cpp:45-57) basis.
-        int n = (int)sc.K;
-        double delta_t = 1.0 / n;
-        int p = (int)(time / delta_t);
-        auto wrap = [n](int i) { return i < 0 ? n - 1 : (i >= n ? i - n : i); };
-        double lt = (time - delta_t * (double)p) / delta_t;
-        double t2 = lt * lt, t3 = t2 * lt;
-        fa.b0 = 0.5 * (-t3 + 2.0 * t2 - lt);
-        fa.b1 = 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
-        fa.b2 = 0.5 * (-3.0 * t3 + 4.0 * t2 + lt);
-        fa.b3 = 0.5 * (t3 - t2);
-        fa.seg[0] = wrap(p - 1); fa.seg[1] = wrap(p); fa.seg[2] = wrap(p + 1); fa.seg[3] = wrap(p + 2);
-        fa.seg_ok = (p == (int)f) ? 1u : 0u;
-        fa.bq0 = llround(std::ldexp(fa.b0, 38));
-        fa.bq2 = llround(std::ldexp(fa.b2, 38));
-        fa.bq3 = llround(std::ldexp(fa.b3, 38));
-        split(fa.bq0, &fa.bh0, &fa.bl0);
-        split(fa.bq2, &fa.bh2, &fa.bl2);
-        split(fa.bq3, &fa.bh3, &fa.bl3);
-        fa.key_mode = (fa.b0 == 0.0 && fa.b1 == 1.0 && fa.b2 == 0.0 && fa.b3 == 0.0) ? 1u : 0u;
-        if (!fa.key_mode) {
-            const uint32_t tn = std::max(std::max(sc.CW, sc.CH), std::max(sc.width, sc.height)) + 1;
-            if (tn > w->stab_cap) {
-                if (w->stab) cudaFree(w->stab);
-                w->stab = nullptr;
-                w->stab_cap = 0;
-                AMG_CUDA(cudaMalloc(&w->stab, (size_t)tn * 4));
-                w->stab_cap = tn;
-            }
-            AMG_LAUNCH(k_spline_table, (tn + 255) / 256, 256, 0, s, fa.b0, fa.b1, fa.b2, fa.b3, tn, w->stab);
-            fa.stab = w->stab;
-            fa.stab_n = tn;
-        }
-    }
     // atoms of the pair: at most N; the active count stays on the device
     uint64_t n = sc.N;
     SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx};

@@ -239,6 +239,33 @@ int fluid_set(FluidDev *f, const double *state, cudaStream_t s);  // n x 18 doub
 int fluid_get(FluidDev *f, double *state, cudaStream_t s);
 int fluid_step(FluidDev *f, uint64_t steps_left, double freedom_radius, cudaStream_t s, Prof *prof);
 
+// ---- k_fluid_morph.cu: the morph's fluid path (step_fluid + draw_fluid)
+struct FluidMorph;
+struct FluidFrame {
+    RenderScene sc;                   // published chains, key frames, output
+    double time;                      // normalised global time
+    uint64_t frame_key;               // index of the pair's first key frame
+    double sparseness;                // solver grid units per pixel
+    const uint32_t *chain_id;         // [N] chain of each column (device)
+    const uint32_t *surf;             // [K][C] surface of each chain's blob (device)
+    const uint32_t *surf_host;        // the same on the host
+    const uint64_t *chain_off_host;   // [C+1]
+    const int *perm;                  // Perlin lag / slope permutations (device)
+    uint32_t fluidsteps;
+    uint64_t seed_key;
+    RenderWork *rw;                   // frame arithmetic tables
+};
+FluidMorph *fluid_morph_create();
+void fluid_morph_destroy(FluidMorph *m);
+// Steps the particles to the frame (management, update, solver) and draws
+// it into out (device, width * height RGBA8).
+int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr, uint8_t *out, cudaStream_t s);
+// draw_fluid of the particles as they are (tests and the standalone solver).
+int fluid_render_only(FluidDev *fl, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
+                      double t, uint8_t *out, cudaStream_t s);
+int launch_chain_ids(const uint64_t *chain_off, uint32_t C, uint64_t N, uint32_t *out, cudaStream_t s);
+const int *render_perm(RenderWork *w);
+
 // ---- k_blobs.cu
 struct BlobWork;
 BlobWork *blob_work_create();

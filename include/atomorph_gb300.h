@@ -109,6 +109,12 @@ int am_set_resolution(am_morph *m, uint16_t w, uint16_t h);  /* morph::set_resol
 int am_set_proposal(am_morph *m, unsigned kind);
 int am_set_sweeps(am_morph *m, size_t sweeps_per_step);
 int am_set_motion_noise(am_morph *m, double amplitude_px);
+/* Fluid solver grid units per pixel (the reference's sparseness, fixed at 1
+ * there): the grid is (width * s + 20) x (height * s + 20). */
+int am_set_fluid_sparseness(am_morph *m, double s);
+/* The morph's fluid particles (fields as am_fluid_get_particles) after the
+ * last fluid frame; returns the particle count, writes when cap >= it. */
+size_t am_get_fluid_particles(am_morph *m, double *state, size_t cap);
 /* Guided-refinement tunables (the autotuner sets these): "local_self",
  * "local_target", "local_random" (candidates per column from the column's own
  * neighbourhood, its target cell, and uniform random columns),
@@ -217,6 +223,12 @@ int  am_fluid_step(am_fluid *f, size_t steps_left, double freedom_radius);      
 /* n steps with steps_left = n-1 .. 0, as morph::step_fluid runs them (morph.cpp:1054). */
 int  am_fluid_steps(am_fluid *f, size_t n, double freedom_radius);
 void *am_fluid_stream(am_fluid *f);
+/* draw_fluid (morph.cpp:1081-1204) of the particles as they are: colour
+ * correction at local time t (written back to the particles, which also
+ * mature), bilinear splat, per-pixel rounded means into rgba_out (host,
+ * width x height RGBA8); bbox = x1, y1, x2, y2 of the key frames. */
+int  am_fluid_render(am_fluid *f, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
+                     double t, uint8_t *rgba_out);
 
 /* ---- batched refinement (no reference counterpart: the reference refines
  * one morph per worker thread, thread.cpp:173-206).  A batch refines many

@@ -722,6 +722,63 @@ void orc_fluid_step(double *P, uint32_t n, uint32_t gsx, uint32_t gsy, double *g
 }
 void orc_srand(unsigned s) { srand(s); }
 
+// draw_fluid's colour correction and splat (morph.cpp:1081-1204) of the
+// particles P[18][n] (fields as orc_fluid_step) into out (RGBA8 width x
+// height, zero where no particle lands).  feather = 0, keep_background off.
+// Corners outside the output are dropped like the GPU path (the reference
+// would wrap them into the next row).
+void orc_draw_fluid(double *P, uint32_t n, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
+                    double t, uint8_t *out) {
+    auto F = [&](int f, uint32_t i) -> double & { return P[(size_t)f * n + i]; };
+    const size_t npx = (size_t)width * height;
+    std::vector<double> W(npx, 0.0), R(npx, 0.0), G(npx, 0.0), B(npx, 0.0), A(npx, 0.0);
+    std::vector<uint8_t> any(npx, 0);
+    auto cc = [](double v) { return (uint32_t)(int)std::round(v * 255.0) & 255u; };  // create_color
+    for (uint32_t i = 0; i < n; ++i) {
+        if (F(FACT, i) == 0.0) continue;
+        const double st = F(FSTR, i), d = t - (1.0 * (1.0 - st));
+        const double w = (1.0 / (100.0 * std::pow(d, 2.0) + 1.0)) * std::pow(st, 2.0);
+        F(Fr, i) = (w * F(FR_, i)) + (1.0 - w) * F(Fr, i);
+        F(Fg, i) = (w * F(FG_, i)) + (1.0 - w) * F(Fg, i);
+        F(Fb, i) = (w * F(FB_, i)) + (1.0 - w) * F(Fb, i);
+        F(Fa, i) = (w * F(FA_, i)) + (1.0 - w) * F(Fa, i);
+        double px, py;
+        if (F(FX, i) <= 10.0) px = 0.0;
+        else if (F(FX, i) >= width * sparseness + 10.0) px = (double)(width - 1);
+        else px = (F(FX, i) - 10.0) / sparseness;
+        if (F(FY, i) <= 10.0) py = 0.0;
+        else if (F(FY, i) >= height * sparseness + 10.0) py = (double)(height - 1);
+        else py = (F(FY, i) - 10.0) / sparseness;
+        const uint32_t x = (uint32_t)std::min((int)px, (int)width - 1), y = (uint32_t)std::min((int)py, (int)height - 1);
+        F(FMAT, i) = 1.0;
+        double ipx, ipy;
+        const double xf = std::modf(px, &ipx), yf = std::modf(py, &ipy);
+        if (ipx >= width || ipy >= height) {
+            if (ipx > bbox[2] || ipx < bbox[0] || ipy > bbox[3] || ipy < bbox[1]) continue;
+        }
+        const double w11 = (1.0 - xf) * (1.0 - yf), w21 = xf * (1.0 - yf), w12 = (1.0 - xf) * yf, w22 = xf * yf;
+        const uint32_t r = cc(F(Fr, i)), g = cc(F(Fg, i)), b = cc(F(Fb, i)), a = cc(F(Fa, i));
+        auto put = [&](uint32_t cx, uint32_t cy, double wt) {
+            if (cx >= width || cy >= height) return;
+            const size_t q = (size_t)cy * width + cx;
+            W[q] += wt; R[q] += r * wt; G[q] += g * wt; B[q] += b * wt; A[q] += a * wt;
+            any[q] = 1;
+        };
+        if (w11 > 0.0) put(x, y, w11);
+        if ((x < bbox[2] || x + 1 < width) && w21 > 0.0) put(x + 1, y, w21);
+        if ((y < bbox[3] || y + 1 < height) && w12 > 0.0) put(x, y + 1, w12);
+        if (w22 > 0.0 && ((y < bbox[3] && x < bbox[2]) || (y + 1 < height && x + 1 < width))) put(x + 1, y + 1, w22);
+    }
+    for (size_t q = 0; q < npx; ++q) {
+        uint8_t *o = out + 4 * q;
+        if (!any[q]) { o[0] = o[1] = o[2] = o[3] = 0; continue; }
+        o[0] = (uint8_t)std::round(R[q] / W[q]);
+        o[1] = (uint8_t)std::round(G[q] / W[q]);
+        o[2] = (uint8_t)std::round(B[q] / W[q]);
+        o[3] = (uint8_t)std::round(A[q] / W[q]);
+    }
+}
+
 // --------------------------------------------------------------- blobs -----
 // 4-connected components of the present pixels of one key frame: the blobs
 // blobify_frame (thread.cpp:225-412) converges to when blob_threshold >= 1,

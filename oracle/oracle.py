@@ -107,6 +107,7 @@ class Oracle:
         L.orc_render_many.argtypes = [C.POINTER(Scene), f64p, C.c_uint32, u8p, C.c_uint32]
         L.orc_fluid_step.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, f64p, u8p, C.c_uint64, C.c_double]
         L.orc_srand.argtypes = [C.c_uint]
+        L.orc_draw_fluid.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, u32p, C.c_double, u8p]
         L.orc_components.restype = C.c_uint32
         L.orc_components.argtypes = [u8p, u32p, C.c_uint32, C.c_uint32, i32p, f64p, C.c_uint32]
         L.orc_blob_energy.restype = C.c_double
@@ -179,6 +180,15 @@ class Oracle:
         n = P.shape[1]
         self.lib.orc_fluid_step(_p(P, f64p), n, gsx, gsy, _p(grid, f64p), _p(touched, u8p), steps_left,
                                 freedom_radius)
+
+    def draw_fluid(self, P: np.ndarray, width: int, height: int, sparseness: float, bbox, t: float) -> np.ndarray:
+        """draw_fluid of particles P[18, n] (modified like the reference's:
+        colours corrected, particles matured); returns the RGBA8 frame."""
+        n = P.shape[1]
+        out = np.zeros((height, width, 4), np.uint8)
+        bb = np.ascontiguousarray(bbox, np.uint32)
+        self.lib.orc_draw_fluid(_p(P, f64p), n, width, height, sparseness, _p(bb, u32p), t, _p(out, u8p))
+        return out
 
     def srand(self, s: int) -> None:
         self.lib.orc_srand(s)
