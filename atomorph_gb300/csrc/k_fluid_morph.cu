@@ -324,7 +324,7 @@ __global__ void k_fm_update(FmArgs a) {
             lag = poctave(sp, px, py) * 0.5f + 0.5f;
             slope = poctave(sp + 512, px, py) * 0.5f + 0.5f;
         }
-        const uint32_t col = fade_colour(a.fading, c1, c2, lag, slope, 1.f - a.t);
+        const uint32_t col = fade_colour(a.fading, c1, c2, fade_params(lag, slope), 1.f - a.t);
         // attractor: the source column's trajectory point at this time
         uint32_t X = (uint32_t)pt_X(pt1), Y = (uint32_t)pt_Y(pt1);
         if (a.motion == AM_LINEAR) {
@@ -334,11 +334,9 @@ __global__ void k_fm_update(FmArgs a) {
         } else if (a.motion == AM_SPLINE) {
             const uint64_t q0 = a.P[(uint64_t)a.fa.seg[0] * a.N + src_x], q1 = a.P[(uint64_t)a.fa.seg[1] * a.N + src_x];
             const uint64_t q2 = a.P[(uint64_t)a.fa.seg[2] * a.N + src_x], q3 = a.P[(uint64_t)a.fa.seg[3] * a.N + src_x];
-            if (!spl_static(a.fa, pt_X(q0), pt_X(q1), pt_X(q2), pt_X(q3), &X) &&
-                !spl_fast(a.fa, pt_X(q0), pt_X(q1), pt_X(q2), pt_X(q3), &X))
+            if (!spl_fast(a.fa, pt_X(q0), pt_X(q1), pt_X(q2), pt_X(q3), &X))
                 X = spl_fixed(a.fa.b0, a.fa.b1, a.fa.b2, a.fa.b3, pt_X(q0), pt_X(q1), pt_X(q2), pt_X(q3));
-            if (!spl_static(a.fa, pt_Y(q0), pt_Y(q1), pt_Y(q2), pt_Y(q3), &Y) &&
-                !spl_fast(a.fa, pt_Y(q0), pt_Y(q1), pt_Y(q2), pt_Y(q3), &Y))
+            if (!spl_fast(a.fa, pt_Y(q0), pt_Y(q1), pt_Y(q2), pt_Y(q3), &Y))
                 Y = spl_fixed(a.fa.b0, a.fa.b1, a.fa.b2, a.fa.b3, pt_Y(q0), pt_Y(q1), pt_Y(q2), pt_Y(q3));
         }
         const float ptx = (float)(X >> 8) + (float)(X & 255u) / 256.f;

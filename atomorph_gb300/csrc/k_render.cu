@@ -65,8 +65,6 @@ struct RenderWork {
     uint64_t rec_cap = 0;
     uint32_t *tile_cnt = nullptr, *tile_off = nullptr, *tile_cur = nullptr;
     uint32_t ntiles_cap = 0;
-    uint32_t *stab = nullptr;  // per-frame spline table of static integer coordinates
-    uint32_t stab_cap = 0;
     unsigned *bar = nullptr;   // grid barrier of the fused splat + binning launch
     int *err = nullptr;        // its bounded-wait failure flag
     int *perm = nullptr;    // [2][512] Perlin permutations on the device
@@ -113,7 +111,6 @@ void render_work_destroy(RenderWork *w) {
     if (w->tile_cur) cudaFree(w->tile_cur);
     if (w->perm) cudaFree(w->perm);
     if (w->bar) cudaFree(w->bar);
-    if (w->stab) cudaFree(w->stab);
     if (w->err) cudaFree(w->err);
     delete w;
 }
@@ -224,7 +221,7 @@ __global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, c
             lag = poctave(sp, px, py) * 0.5f + 0.5f;
             slope = poctave(sp + 512, px, py) * 0.5f + 0.5f;
         }
-        ls[i] = make_float2(lag, slope);
+        ls[i] = fade_params(lag, slope);
         rank[i] = (uint32_t)sc.rank[(size_t)f * sc.C + c];
         int mx = ((X1 + X2) >> 9), my = ((Y1 + Y2) >> 9);
         mx = min(max(mx, 0), (int)sc.width - 1);
@@ -251,14 +248,6 @@ __global__ void k_pair_gather(const uint32_t *__restrict__ keys, const uint32_t 
         col2[j] = col[i];
         ls2[j] = ls[i];
         if (j + 1 == n) *active = (uint32_t)n;
-    }
-}
-
-__global__ void k_spline_table(double b0, double b1, double b2, double b3, uint32_t n, uint32_t *tab) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < n) {
-        const int32_t q = (int32_t)(p << 8);
-        tab[p] = spl_fixed(b0, b1, b2, b3, q, q, q, q);
     }
 }
 
@@ -321,7 +310,7 @@ __device__ __forceinline__ bool axis_fast(const RenderScene &sc, const FrameArgs
         *out = (uint32_t)v;
         return true;
     }
-    if (sc.motion == AM_SPLINE) return spl_static(fa, c0, c1, c2, c3, out) || spl_fast(fa, c0, c1, c2, c3, out);
+    if (sc.motion == AM_SPLINE) return spl_fast(fa, c0, c1, c2, c3, out);
     *out = (uint32_t)c0;
     return true;
 }
@@ -369,7 +358,7 @@ __device__ __forceinline__ uint4 splat_atom(const RenderScene &sc, const FrameAr
     if (!axis_fast(sc, fa, 1, a, b, &Y)) Y = axis_fixed(sc, fa, 1, a, b);
     uint2 c = in.col[i];
     float2 q = in.ls[i];
-    return finish_record(sc, X, Y, fade_colour(sc.fading, c.x, c.y, q.x, q.y, fa.str), in.rank[i]);
+    return finish_record(sc, X, Y, fade_colour(sc.fading, c.x, c.y, q, fa.str), in.rank[i]);
 }
 
 // Tiles of the valid corners of a splat record, each distinct tile once:
@@ -487,7 +476,7 @@ __global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(BinArgs b) {
             if (!axis_fast(b.sc, b.fa, 1, a, c, &v.y)) need |= 2u;
             const uint2 col = b.in.col[i];
             const float2 q = b.in.ls[i];
-            v.z = fade_colour(b.sc.fading, col.x, col.y, q.x, q.y, b.fa.str);
+            v.z = fade_colour(b.sc.fading, col.x, col.y, q, b.fa.str);
             v.w = b.in.rank[i];
         }
         srec[slot] = v;
@@ -970,19 +959,6 @@ int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, do
         split(fa.bq2, &fa.bh2, &fa.bl2);
         split(fa.bq3, &fa.bh3, &fa.bl3);
         fa.key_mode = (fa.b0 == 0.0 && fa.b1 == 1.0 && fa.b2 == 0.0 && fa.b3 == 0.0) ? 1u : 0u;
-        if (!fa.key_mode) {
-            const uint32_t tn = std::max(std::max(sc.CW, sc.CH), std::max(sc.width, sc.height)) + 1;
-            if (tn > w->stab_cap) {
-                if (w->stab) cudaFree(w->stab);
-                w->stab = nullptr;
-                w->stab_cap = 0;
-                AMG_CUDA(cudaMalloc(&w->stab, (size_t)tn * 4));
-                w->stab_cap = tn;
-            }
-            AMG_LAUNCH(k_spline_table, (tn + 255) / 256, 256, 0, s, fa.b0, fa.b1, fa.b2, fa.b3, tn, w->stab);
-            fa.stab = w->stab;
-            fa.stab_n = tn;
-        }
     }
     return AM_OK;
 }

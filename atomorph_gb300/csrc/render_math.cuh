@@ -47,14 +47,6 @@ struct FrameArgs {
     // product with a 32-bit coordinate difference is a 32 x 32 -> 64-bit
     // multiply: 64 x 64-bit integer multiplies are slow on this part.
     int32_t w1h, w1l, bh0, bl0, bh2, bl2, bh3, bl3;
-    // SPLINE: the reference's double result for a coordinate that sits on
-    // the integer pixel p in all four control frames (an atom that does not
-    // move along that axis): stab[p] for p < stab_n.  The fixed-point value
-    // of such a coordinate is exactly an integer, i.e. on a rounding
-    // boundary, so without the table every such atom would need the FP64
-    // evaluation.
-    const uint32_t *stab;
-    uint32_t stab_n;
     uint32_t lin_mode;      // 0 general, 1 w1 == 1 (X = X1), 2 w1 == 0 (X = X2)
     uint32_t key_mode;      // 1 when the spline basis is exactly (0, 1, 0, 0)
     uint32_t seg_ok;        // 1 when the spline segment is the prepared one
@@ -142,16 +134,22 @@ static __device__ __noinline__ uint32_t spl_fixed(double b0, double b1, double b
     return (xi << 8) | xf;
 }
 
-// Colour fade of one atom (morph.cpp:537-550, 1467-1488) in FP32.
-__device__ __forceinline__ uint32_t fade_colour(uint32_t fading, uint32_t c1, uint32_t c2, float lag, float slope,
-                                                float str) {
+// Colour fade of one atom (morph.cpp:537-550, 1467-1488) in FP32.  The
+// PERLIN / COSINE ramp of an atom depends on its lag and slope only, so its
+// parameters are prepared once per key-frame pair: fade_params gives
+// (l, pi / s) with s = (slope + 0.1) / 1.1 and l = (1 - s) lag, and the
+// frame's weight of the earlier colour is 0 before l, 1 after l + s and the
+// cosine ramp between.
+__device__ __forceinline__ float2 fade_params(float lag, float slope) {
+    const float s = (slope + 0.1f) / 1.1f;
+    return make_float2((1.f - s) * lag, 3.14159265358f / s);
+}
+__device__ __forceinline__ uint32_t fade_colour(uint32_t fading, uint32_t c1, uint32_t c2, float2 fp, float str) {
     if (fading == AM_PERLIN || fading == AM_COSINE) {
-        const float pi = 3.14159265358f;
-        float s = (slope + 0.1f) / 1.1f;
-        float l = (1.f - s) * lag;
-        if (str <= l) str = 0.f;
-        else if (str >= l + s) str = 1.f;
-        else str = (-cosf((str - l) * (pi / s)) + 1.f) * 0.5f;
+        const float x = (str - fp.x) * fp.y;
+        if (x <= 0.f) str = 0.f;
+        else if (x >= 3.14159265358f) str = 1.f;
+        else str = (1.f - __cosf(x)) * 0.5f;  // x in (0, pi): the intrinsic's error is far below 1/255
     }
     uint32_t o = 0;
 #pragma unroll
@@ -163,15 +161,5 @@ __device__ __forceinline__ uint32_t fade_colour(uint32_t fading, uint32_t c1, ui
     return o;
 }
 
-// A coordinate on the same integer pixel in all four control frames: the
-// per-frame table holds the reference's double result.
-__device__ __forceinline__ bool spl_static(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
-                                           uint32_t *out) {
-    if (fa.key_mode || q0 != q1 || q2 != q1 || q3 != q1 || (q1 & 255) || q1 < 0) return false;
-    const uint32_t p = (uint32_t)q1 >> 8;
-    if (p >= fa.stab_n) return false;
-    *out = __ldg(fa.stab + p);
-    return true;
-}
 
 }  // namespace amg
