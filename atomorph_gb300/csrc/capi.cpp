@@ -137,6 +137,7 @@ int am_set_tuning(am_morph *m, const char *name, double value) {
             p->learned_keep = value;
         }
         else if (n == "guided_switch") p->guided_switch = value;
+        else if (n == "learned_adaptive") p->learned_adaptive = value != 0.0;
         else return AM_ERR_ARG;
     }
     return AM_OK;

@@ -481,6 +481,7 @@ int Engine::set_chain_layout(const std::vector<uint64_t> &w) {
     ++layout_version;
     local_valid = false;
     guided_on = false;
+    lg_state = LG_MEASURE_FULL;
     widths = w;
     C = (uint32_t)w.size();
     chain_off.assign(C + 1, 0);
@@ -932,6 +933,28 @@ int Engine::ensure_local_index() {
     return AM_OK;
 }
 
+// The learned form runs its gate only while it pays: a gated sweep scans a
+// quarter of the regions (default keep) and costs about three quarters of a
+// full guided sweep, so it must keep at least that share of a full sweep's
+// gain.  The policy alternates one measured full block and one measured
+// gated block, then runs four blocks of the better one, and measures again.
+void Engine::learned_gate_next(double gain_per_sweep) {
+    constexpr double kGatedCost = 0.75;  // gated / full sweep time, measured at 1M atoms, keep 1/4
+    switch (lg_state) {
+    case LG_MEASURE_FULL:
+        lg_full_rate = gain_per_sweep;
+        lg_state = LG_MEASURE_GATED;
+        break;
+    case LG_MEASURE_GATED:
+        lg_state = gain_per_sweep >= kGatedCost * lg_full_rate ? LG_GATED : LG_FULL;
+        lg_left = 4;
+        break;
+    default:
+        if (--lg_left <= 0) lg_state = LG_MEASURE_FULL;
+        break;
+    }
+}
+
 int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
     if (active.proposal == AM_PROPOSAL_LEARNED && !mlp_ready()) {
         set_error("the learned proposal needs a trained network (am_train_proposal / am_set_proposal_weights)");
@@ -945,48 +968,62 @@ int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
         if ((rc = mlp_init())) return rc;
         if ((rc = d_sel.reserve(N * maxph))) return rc;
         if ((rc = d_nsel.reserve(1))) return rc;
-        if (recording && (rc = d_rec_idx.reserve(N * maxph))) return rc;
+        if (recording && (rc = d_rec_idx.reserve((N * maxph + 31) / 32 + 1))) return rc;
     }
-    if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * sweeps + 4)))) return rc;
-    AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * sweeps * 8, stream));
+    // Sweeps run in blocks; the learned form decides per block whether its
+    // gate runs (see learned_gate_next).
+    constexpr size_t kBlock = 10;
+    if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * kBlock + 4)))) return rc;
     auto ph = phases_for(K);
-    for (size_t s = 0; s < sweeps; ++s) {
-        uint32_t pofs = 0;
-        for (size_t p = 0; p < ph.size(); ++p) {
-            LocalArgs a;
-            a.P = d_P.p; a.N = N; a.K = K; a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
-            a.slot_pt = lix.slot_pt; a.col = lix.col; a.slot_of = lix.slot_of; a.cell_start = lix.cell_start;
-            a.ncx = lix.ncx; a.ncy = lix.ncy; a.ncells = lix.ncells; a.chain_id = lix.chain_id;
-            a.chain_w1 = lix.chain_w1; a.cap = active.local_target;
-            a.self_cap = active.local_self; a.nrandom = active.local_random; a.chain_off = d_chain_off.p;
-            a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p ^ 0x5bd1e995ULL);
-            a.claim = d_claim.p; a.prop = d_lprop.p; a.pgain = d_pgain.p; a.sv = d_sv.p; a.hot = d_hot.p;
-            a.single_chain = C == 1;
-            a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
-            if (active.proposal == AM_PROPOSAL_LEARNED) {
-                a.mlp = d_mlp_dep.p; a.keep = (float)active.learned_keep; a.err = d_err.p;
-                a.cost_scale = log1pf((float)((double)cost_exact / ((double)N * K) / kGainScale));
-                a.sel_out = d_sel.p; a.nsel_out = d_nsel.p;
-                if (recording) {
-                    a.rec_feat = d_rec_feat.p; a.rec_gain = d_rec_gain.p; a.rec_count = d_rec_count.p;
-                    a.rec_cap = rec_cap; a.rec_idx = d_rec_idx.p;
+    const bool learned = active.proposal == AM_PROPOSAL_LEARNED;
+    for (size_t done = 0; done < sweeps;) {
+        const size_t nb = std::min(kBlock, sweeps - done);
+        const bool gated = learned && (recording || !active.learned_adaptive || lg_state == LG_MEASURE_GATED ||
+                                       lg_state == LG_GATED);
+        AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * nb * 8, stream));
+        for (size_t s = 0; s < nb; ++s) {
+            uint32_t pofs = 0;
+            for (size_t p = 0; p < ph.size(); ++p) {
+                LocalArgs a;
+                a.P = d_P.p; a.N = N; a.K = K; a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
+                a.slot_pt = lix.slot_pt; a.col = lix.col; a.slot_of = lix.slot_of; a.cell_start = lix.cell_start;
+                a.ncx = lix.ncx; a.ncy = lix.ncy; a.ncells = lix.ncells; a.chain_id = lix.chain_id;
+                a.chain_w1 = lix.chain_w1; a.cap = active.local_target;
+                a.self_cap = active.local_self; a.nrandom = active.local_random; a.chain_off = d_chain_off.p;
+                a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p ^ 0x5bd1e995ULL);
+                a.claim = d_claim.p; a.prop = d_lprop.p; a.pgain = d_pgain.p; a.sv = d_sv.p; a.hot = d_hot.p;
+                a.single_chain = C == 1;
+                a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
+                if (gated) {
+                    a.mlp = d_mlp_dep.p; a.keep = (float)active.learned_keep; a.err = d_err.p;
+                    a.cost_scale = log1pf((float)((double)cost_exact / ((double)N * K) / kGainScale));
+                    a.sel_out = d_sel.p; a.nsel_out = d_nsel.p;
+                    a.explore = (uint32_t)mix64(sweep_counter ^ (uint64_t)p);
+                    if (recording) {
+                        a.rec_feat = d_rec_feat.p; a.rec_gain = d_rec_gain.p; a.rec_count = d_rec_count.p;
+                        a.rec_cap = rec_cap; a.rec_idx = d_rec_idx.p;
+                    }
                 }
+                prof.open(stream);
+                if (gated) rc = launch_learned_phase(a, stream);
+                else rc = launch_local_phase(a, stream);
+                if (rc) return rc;
+                prof.close(gated ? PROF_MLP : PROF_SWEEP_LOCAL, stream);
+                pofs += (uint32_t)ph[p].size();
             }
-            prof.open(stream);
-            if (active.proposal == AM_PROPOSAL_LEARNED) rc = launch_learned_phase(a, stream);
-            else rc = launch_local_phase(a, stream);
-            if (rc) return rc;
-            prof.close(active.proposal == AM_PROPOSAL_LEARNED ? PROF_MLP : PROF_SWEEP_LOCAL, stream);
-            pofs += (uint32_t)ph[p].size();
+            ++sweep_counter;
         }
-        ++sweep_counter;
-    }
-    std::vector<unsigned long long> acc(2 * sweeps);
-    AMG_CUDA(cudaMemcpyAsync(acc.data(), d_acc.p + 4, acc.size() * 8, cudaMemcpyDeviceToHost, stream));
-    AMG_CUDA(cudaStreamSynchronize(stream));
-    for (size_t s = 0; s < sweeps; ++s) {
-        cost_exact -= acc[2 * s];
-        if (gains) gains[s] = acc[2 * s];
+        std::vector<unsigned long long> acc(2 * nb);
+        AMG_CUDA(cudaMemcpyAsync(acc.data(), d_acc.p + 4, acc.size() * 8, cudaMemcpyDeviceToHost, stream));
+        AMG_CUDA(cudaStreamSynchronize(stream));
+        double block_gain = 0.0;
+        for (size_t s = 0; s < nb; ++s) {
+            cost_exact -= acc[2 * s];
+            block_gain += (double)acc[2 * s];
+            if (gains) gains[done + s] = acc[2 * s];
+        }
+        if (learned && !recording) learned_gate_next(block_gain / (double)nb);
+        done += nb;
     }
     return AM_OK;
 }

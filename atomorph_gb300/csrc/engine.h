@@ -32,7 +32,8 @@ struct Params {  // defaults of morph.h:97-119
     size_t sweeps = 1;
     // guided-refinement tunables (am_set_tuning; chosen by the autotuner)
     uint32_t local_self = 12, local_target = 8, local_random = 2;
-    double learned_keep = 0.25;  // fraction of slots the learned gate lets scan
+    double learned_keep = 0.25;  // fraction of regions the learned gate lets scan
+    bool learned_adaptive = true;  // run the gate only while it pays (learned_gate_next)
     double guided_switch = 1e-3;  // plain -> guided when a plain sweep gains less than this fraction
     double motion_noise = 0.0;
     double fluid_sparseness = 1.0;  // solver grid units per pixel (the reference's sparseness)
@@ -206,6 +207,11 @@ class Engine {
     int refine_guided(size_t sweeps, uint64_t *gains);
     int refine_plain(size_t sweeps, uint64_t *gains);
     bool guided_on = false;                // the guided phase of the current chains has started
+    // learned form: when its gate runs (learned_gate_next)
+    enum { LG_MEASURE_FULL, LG_MEASURE_GATED, LG_GATED, LG_FULL };
+    int lg_state = LG_MEASURE_FULL, lg_left = 0;
+    double lg_full_rate = 0.0;
+    void learned_gate_next(double gain_per_sweep);
     int copy_keyframe(size_t f, uint8_t *dst);
     unsigned active_seed_mix() const;
     int status = AM_OK;                    // first failure inside the worker

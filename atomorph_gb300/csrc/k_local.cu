@@ -139,7 +139,8 @@ __device__ __forceinline__ void scan_cell(const LocalArgs &a, const uint32_t *cs
 // cell-window candidates, from slot-ordered arrays (coalesced, L2-resident
 // windows); only the random candidates are scattered loads.  With `sel` set
 // only the listed slots propose (the learned gate's choice).
-__device__ __forceinline__ void propose_one(const LocalArgs &a, uint32_t fi, uint32_t s1) {
+// Returns the best gain found (0 when no improving partner).
+__device__ __forceinline__ int64_t propose_one(const LocalArgs &a, uint32_t fi, uint32_t s1) {
     const uint64_t N = a.N;
     const uint64_t t = (uint64_t)fi * N + s1;
     {
@@ -152,7 +153,7 @@ __device__ __forceinline__ void propose_one(const LocalArgs &a, uint32_t fi, uin
         a.prop[t] = 0xFFFFFFFFu;
         uint32_t x1 = col[c.s1];
         uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
-        if (a.chain_w1[ch]) return;  // width-1 chains do not refine (thread.cpp:1045)
+        if (a.chain_w1[ch]) return 0;  // width-1 chains do not refine (thread.cpp:1045)
         c.a1 = spt[c.s1];
         c.S1 = sv[c.s1];
         c.lo = a.single_chain ? 0ull : a.chain_off[ch];
@@ -195,10 +196,6 @@ __device__ __forceinline__ void propose_one(const LocalArgs &a, uint32_t fi, uin
             }
         }
         if (a.hot) a.hot[(uint64_t)y * N + c.s1] = gain_bucket(best);
-        if (a.rec_idx) {
-            uint32_t j = a.rec_idx[t];
-            if (j != 0xFFFFFFFFu) a.rec_gain[j] = log1pf((float)best / kGainScale);
-        }
         if (bs != 0xFFFFFFFFu) {
             unsigned long long k = claim_key(best, c.s1);
             a.prop[t] = bs;
@@ -206,6 +203,7 @@ __device__ __forceinline__ void propose_one(const LocalArgs &a, uint32_t fi, uin
             atomicMax(a.claim + (uint64_t)fi * N + c.s1, k);
             atomicMax(a.claim + (uint64_t)fi * N + bs, k);
         }
+        return best;
     }
 }
 
@@ -217,7 +215,31 @@ __device__ __forceinline__ void split_slot(uint32_t t, uint32_t n32, uint32_t &f
 }
 
 __global__ void __launch_bounds__(256) k_local_propose(LocalArgs a) {
-    if (a.sel) {
+    if (a.sel && a.sel_groups) {
+        // listed 32-slot regions, one warp each; while recording, the region's
+        // summed best gain is its training target
+        const uint64_t total = a.N * a.nframes, nsel = *a.nsel;
+        const int lane = threadIdx.x & 31;
+        const uint64_t w0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+        const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+        for (uint64_t i = w0; i < nsel; i += nw) {
+            const uint32_t g = a.sel[i];
+            const uint64_t t = (uint64_t)g * 32 + lane;
+            int64_t best = 0;
+            if (t < total) {
+                uint32_t fi, s1;
+                split_slot((uint32_t)t, (uint32_t)a.N, fi, s1);
+                best = propose_one(a, fi, s1);
+            }
+            if (a.rec_idx) {
+                float sum = (float)best;
+#pragma unroll
+                for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                const uint32_t j = a.rec_idx[g];
+                if (lane == 0 && j != 0xFFFFFFFFu) a.rec_gain[j] = log1pf(sum / kGainScale);
+            }
+        }
+    } else if (a.sel) {
         const uint64_t total = *a.nsel;
         for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
              i += (uint64_t)gridDim.x * blockDim.x) {
@@ -282,7 +304,20 @@ __device__ __forceinline__ void apply_one(const LocalArgs &a, uint32_t fi, uint3
 
 __global__ void __launch_bounds__(256) k_local_apply(LocalArgs a) {
     unsigned long long gain = 0, acc = 0;
-    if (a.sel) {
+    if (a.sel && a.sel_groups) {
+        const uint64_t total = a.N * a.nframes, nsel = *a.nsel;
+        const int lane = threadIdx.x & 31;
+        const uint64_t w0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+        const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+        for (uint64_t i = w0; i < nsel; i += nw) {
+            const uint64_t t = (uint64_t)a.sel[i] * 32 + lane;
+            if (t < total) {
+                uint32_t fi, s1;
+                split_slot((uint32_t)t, (uint32_t)a.N, fi, s1);
+                apply_one(a, fi, s1, gain, acc);
+            }
+        }
+    } else if (a.sel) {
         const uint64_t total = *a.nsel;
         for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
              i += (uint64_t)gridDim.x * blockDim.x) {

@@ -12,12 +12,12 @@
 // with tcgen05.ld.
 //
 // As a swap proposal the network is a gate in front of the guided candidate
-// scan (k_local.cu): it scores every column of a phase from features of the
-// column alone (gate_features below), and only the best-scored fraction of
-// each 32-column group runs the scan.  Its training target is
-// log1p(g / S^2), g the best exact gain the full scan found for the column,
-// S = 16 px in 1/256 px units; samples come from the refinement itself
-// (am_record_swaps).
+// scan (k_local.cu): it scores every 32-slot region of a phase (a compact
+// patch of the frame, since slots are sorted by cell) from features of the
+// region's slots, and only the best-scored fraction of the regions runs the
+// scan.  Its training target is log1p(G / S^2), G the sum of the best exact
+// gains the full scan found in the region, S = 16 px in 1/256 px units;
+// samples come from the refinement itself (am_record_swaps).
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -469,70 +469,122 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, int n, floa
 }
 
 // ----------------------------------------------- learned proposal gate --
-// Features of the column at slot s1 of frame y, from data the guided scan
-// reads anyway (coalesced, slot order) — no candidate is touched:
-//   0,1  displacement of its point from its target m1 = S1/2, /16 px (clamped)
-//   2    log1p(|a1 - m1|^2 / (16 px)^2)
-//   3,4  log1p(points in its own cell), log1p(points in its target cell)
-//   5    1 when the target cell is its own cell
-//   6    gain bucket of the slot's last scan (log2 of the best gain) / 16
-//   7    log1p(mean column cost / (16 px)^2): how far refinement has come
-//   8    log1p(chain width) / 16
-//   9    0 (spare)
-__device__ __forceinline__ bool gate_features(const LocalArgs &a, uint64_t t, float *f) {
-    const uint64_t N = a.N;
-    // t < 2^32 (the host checks): a 32-bit division splits it
-    const uint32_t fi = (uint32_t)t / (uint32_t)N;
-    const uint32_t s1 = (uint32_t)t - fi * (uint32_t)N;
-    uint32_t y = a.frames[fi];
-    uint32_t x1 = a.col[(uint64_t)y * N + s1];
-    uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
-    if (a.chain_w1[ch]) return false;
-    uint64_t a1 = a.slot_pt[(uint64_t)y * N + s1], S1 = a.sv[(uint64_t)y * N + s1];
-    float dx = (float)pt_X(a1) - 0.5f * (float)sums_x(S1), dy = (float)pt_Y(a1) - 0.5f * (float)sums_y(S1);
-    f[0] = fminf(fmaxf(dx / kS, -8.f), 8.f);
-    f[1] = fminf(fmaxf(dy / kS, -8.f), 8.f);
-    f[2] = log1pf((dx * dx + dy * dy) / kS2);
-    const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
-    uint32_t ax = min((uint32_t)pt_X(a1) >> 9, a.ncx - 1), ay = min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1);
-    int32_t mx = sums_x(S1) >> 1, my = sums_y(S1) >> 1;
-    uint32_t tx = min((uint32_t)max(mx, 0) >> 9, a.ncx - 1), ty = min((uint32_t)max(my, 0) >> 9, a.ncy - 1);
-    uint32_t own = ay * a.ncx + ax, tgt = ty * a.ncx + tx;
-    f[3] = log1pf((float)(cs[own + 1] - cs[own]));
-    f[4] = log1pf((float)(cs[tgt + 1] - cs[tgt]));
-    f[5] = own == tgt ? 1.f : 0.f;
-    f[6] = (float)a.hot[(uint64_t)y * N + s1] * (1.f / 16.f);
-    f[7] = a.cost_scale;
-    f[8] = log1pf((float)(a.chain_off[ch + 1] - a.chain_off[ch])) * (1.f / 16.f);
-    f[9] = 0.f;
-    return true;
+// The network gates regions, not single columns: slots are sorted by 2x2-px
+// cell, so 32 consecutive slots of a frame are a compact patch of the frame,
+// and late in refinement the improving swaps left are concentrated in a few
+// unsettled patches.  A region's features come from data the scan reads
+// anyway (coalesced, one warp per region), one network row scores a region,
+// and only the best-scored `keep` fraction of each 128-region tile is scanned
+// (by full warps).  Features of region g (slots 32g .. 32g+31 of the phase's
+// frames), S = 16 px:
+//   0,1  mean and max of log1p(|a - m|^2 / S^2), a the slot's point, m its
+//        column's target (p + n) / 2
+//   2,3  mean and max gain bucket of the slots' last scans / 16
+//   4    fraction of slots whose last scan found an improving partner
+//   5,6  mean |a - m| along x and along y / S
+//   7    log1p(mean column cost / S^2): how far refinement has come
+//   8    fraction of slots whose target lies in their own cell
+//   9    fraction of slots that can refine (chain wider than 1)
+// Target: log1p(sum of the best gains the full scan found in the region / S^2).
+struct GroupFeat {
+    float f[kMlpIn];
+    bool elig;
+};
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
 }
 
-// One CTA scores 128 consecutive slots per tile (one MMA tile; four warps of
-// 32 slots).  Each warp lists its `keep` best-scored eligible slots; while
-// recording, every eligible slot is listed and its features logged.
+// Warp-collective: features of region g (every lane gets them).
+__device__ __forceinline__ GroupFeat group_features(const LocalArgs &a, uint64_t g, uint64_t total) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t t = g * 32 + lane;
+    float lg = 0.f, hb = 0.f, hit = 0.f, ax = 0.f, ay = 0.f, same = 0.f, ok = 0.f;
+    if (t < total) {
+        const uint32_t N32 = (uint32_t)a.N;
+        const uint32_t fi = (uint32_t)t / N32, s1 = (uint32_t)t - fi * N32;  // t < 2^32 (host-checked)
+        const uint32_t y = a.frames[fi];
+        const uint64_t base = (uint64_t)y * a.N + s1;
+        const uint32_t x1 = a.col[base];
+        const uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
+        if (!a.chain_w1[ch]) {
+            ok = 1.f;
+            const uint64_t a1 = a.slot_pt[base], S1 = a.sv[base];
+            const float dx = (float)pt_X(a1) - 0.5f * (float)sums_x(S1), dy = (float)pt_Y(a1) - 0.5f * (float)sums_y(S1);
+            lg = log1pf((dx * dx + dy * dy) / kS2);
+            const uint8_t h = a.hot[base];
+            hb = (float)h * (1.f / 16.f);
+            hit = h ? 1.f : 0.f;
+            ax = fabsf(dx) / kS;
+            ay = fabsf(dy) / kS;
+            const int32_t mx = sums_x(S1) >> 1, my = sums_y(S1) >> 1;
+            const uint32_t own = (min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1)) * a.ncx + min((uint32_t)pt_X(a1) >> 9, a.ncx - 1);
+            const uint32_t tgt = (min((uint32_t)max(my, 0) >> 9, a.ncy - 1)) * a.ncx + min((uint32_t)max(mx, 0) >> 9, a.ncx - 1);
+            same = own == tgt ? 1.f : 0.f;
+        }
+    }
+    GroupFeat r;
+    const float n = warp_sum_f(ok);
+    const float inv = n > 0.f ? 1.f / n : 0.f;
+    r.f[0] = warp_sum_f(lg) * inv;
+    r.f[1] = warp_max_f(lg);
+    r.f[2] = warp_sum_f(hb) * inv;
+    r.f[3] = warp_max_f(hb);
+    r.f[4] = warp_sum_f(hit) * inv;
+    r.f[5] = fminf(warp_sum_f(ax) * inv, 8.f);
+    r.f[6] = fminf(warp_sum_f(ay) * inv, 8.f);
+    r.f[7] = a.cost_scale;
+    r.f[8] = warp_sum_f(same) * inv;
+    r.f[9] = n * (1.f / 32.f);
+    r.elig = n > 0.f;
+    return r;
+}
+
+// One CTA scores 128 regions per tile (one MMA tile): warp w computes the
+// features of regions 32w .. 32w+31 of the tile, lane r keeps region
+// 32w + r's row.  While recording, every eligible region is listed and its
+// features logged.
 __global__ void __launch_bounds__(128) k_learned_gate(LocalArgs a) {
     extern __shared__ __align__(1024) uint8_t smraw[];
     FwdSmem &s = *reinterpret_cast<FwdSmem *>(smraw);
+    __shared__ float sc[kTM];
     fwd_setup(s, a.mlp);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t total = a.N * a.nframes;
-    const uint64_t ntiles = (total + kTM - 1) / kTM;
-    const int kk = max(1, min(32, (int)ceilf(a.keep * 32.f)));
+    const uint64_t ngroups = (total + 31) / 32;
+    const uint64_t ntiles = (ngroups + kTM - 1) / kTM;
+    const int kk = max(1, min(kTM, (int)ceilf(a.keep * (float)kTM)));
     const bool rec = a.rec_idx != nullptr;
     uint32_t phase = 0;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        uint64_t t = tile * kTM + threadIdx.x;
         float f[kMlpIn];
 #pragma unroll
         for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
-        bool elig = t < total && gate_features(a, t, f);
+        bool elig = false;
+        for (int r = 0; r < 32; ++r) {
+            const uint64_t g = tile * kTM + warp * 32 + r;
+            if (g >= ngroups) break;  // uniform across the warp
+            const GroupFeat gf = group_features(a, g, total);
+            if (lane == r) {
+#pragma unroll
+                for (int k = 0; k < kMlpIn; ++k) f[k] = gf.f[k];
+                elig = gf.elig;
+            }
+        }
+        const uint64_t g = tile * kTM + threadIdx.x;
         write_features(s.A1, threadIdx.x, f);
         float score = forward_tile(s, phase, a.err);
         bool keep;
         if (rec) {
             keep = elig;
-            if (t < total) {
+            if (g < ngroups) {
                 uint32_t j = 0xFFFFFFFFu;
                 if (elig) {
                     unsigned long long r = atomicAdd(a.rec_count, 1ull);
@@ -542,24 +594,29 @@ __global__ void __launch_bounds__(128) k_learned_gate(LocalArgs a) {
                         for (int k = 0; k < kMlpIn; ++k) a.rec_feat[r * kMlpIn + k] = f[k];
                     }
                 }
-                a.rec_idx[t] = j;
+                a.rec_idx[g] = j;
             }
         } else {
-            if (!elig) score = -INFINITY;
+            sc[threadIdx.x] = elig ? score : -INFINITY;
+            __syncthreads();
             int rank = 0;
-#pragma unroll 8
-            for (int j = 0; j < 32; ++j) {
-                float o = __shfl_sync(0xffffffffu, score, j);
-                rank += (o > score) || (o == score && j < lane);
+            const float me = sc[threadIdx.x];
+            for (int j = 0; j < kTM; ++j) {
+                const float o = sc[j];
+                rank += (o > me) || (o == me && j < (int)threadIdx.x);
             }
-            keep = elig && rank < kk;
+            __syncthreads();
+            // exploration: one region in eight is scanned whatever its score,
+            // in a rotation, so a region the network ranks low is still
+            // rescanned every few sweeps
+            keep = elig && (rank < kk || (((uint32_t)g + a.explore) & 7u) == 0u);
         }
         unsigned m = __ballot_sync(0xffffffffu, keep);
         if (m) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(a.nsel_out, (unsigned long long)__popc(m));
             base = __shfl_sync(0xffffffffu, base, 0);
-            if (keep) a.sel_out[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)t;
+            if (keep) a.sel_out[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)g;
         }
     }
     fwd_teardown(s);
@@ -627,11 +684,13 @@ int launch_learned_phase(const LocalArgs &a, cudaStream_t s) {
     // >= 56 KB of shared memory keeps at most 4 CTAs (4 x 128 TMEM columns) per SM.
     size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 56 * 1024);
     if ((rc = set_smem((const void *)k_learned_gate, smem))) return rc;
-    unsigned g = (unsigned)std::min<uint64_t>((total + kTM - 1) / kTM, (uint64_t)kSMs * 4);
+    const uint64_t ngroups = (total + 31) / 32;
+    unsigned g = (unsigned)std::min<uint64_t>((ngroups + kTM - 1) / kTM, (uint64_t)kSMs * 4);
     AMG_LAUNCH(k_learned_gate, g, 128, smem, s, a);
     LocalArgs b = a;
     b.sel = a.sel_out;
     b.nsel = a.nsel_out;
+    b.sel_groups = true;
     if ((rc = launch_local_propose(b, s))) return rc;
     return launch_local_apply(b, s);
 }

@@ -110,17 +110,19 @@ struct LocalArgs {
     unsigned long long *pgain;               // [nframes][N] exact gain of the proposal
     unsigned long long *gain, *accepted;
     uint8_t *hot = nullptr;                  // [K][N] gain bucket of each slot's last scan
-    const uint32_t *sel = nullptr;           // proposing slots (t = fi*N + s) when gated
-    const unsigned long long *nsel = nullptr;//   and their count
+    const uint32_t *sel = nullptr;           // proposing slots (t = fi*N + s) when gated,
+    const unsigned long long *nsel = nullptr;//   their count,
+    bool sel_groups = false;                 //   and whether entries are 32-slot regions (t / 32)
     // learned proposal only
     const float *mlp = nullptr;              // deployed network (MlpLayout)
-    float keep = 0.25f;                      // fraction of each 32-slot group the network lets scan
+    float keep = 0.25f;                      // fraction of the regions of each 128-region tile the network lets scan
+    uint32_t explore = 0;                    // rotates the regions scanned regardless of score (1 in 8)
     float cost_scale = 0.f;                  // log1p(mean column cost / kGainScale)
     uint32_t *sel_out = nullptr;             // gate output list
     unsigned long long *nsel_out = nullptr;
     float *rec_feat = nullptr;               // optional sample log: features [cap][10]
-    float *rec_gain = nullptr;               //   and the best gain the full scan found [cap]
-    uint32_t *rec_idx = nullptr;             // [nframes][N] record row of each slot or ~0
+    float *rec_gain = nullptr;               //   and the summed best gains the full scan found [cap]
+    uint32_t *rec_idx = nullptr;             // [nframes*N/32] record row of each region or ~0
     unsigned long long *rec_count = nullptr;
     uint64_t rec_cap = 0;
     int *err = nullptr;                      // bounded-wait failure flag
@@ -166,10 +168,10 @@ int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K,
 int launch_local_phase(const LocalArgs &a, cudaStream_t s);
 int launch_local_propose(const LocalArgs &a, cudaStream_t s);  // a.sel/a.nsel: listed slots only
 int launch_local_apply(const LocalArgs &a, cudaStream_t s);
-// Learned proposal phase (k_mlp.cu): the network scores every slot from its
-// own cheap features on tensor cores, the best-scored `keep` fraction of each
-// 32-slot group is listed, and only listed slots run the guided candidate
-// scan (exact gains, disjoint apply as above).
+// Learned proposal phase (k_mlp.cu): the network scores every 32-slot region
+// from cheap features of its slots on tensor cores, the best-scored `keep`
+// fraction of each 128-region tile is listed, and only listed regions run the
+// guided candidate scan (exact gains, disjoint apply as above).
 int launch_learned_phase(const LocalArgs &a, cudaStream_t s);
 
 // Stable LSD radix sort of (key, value) u32 pairs on the low `bits` key bits.

@@ -118,8 +118,10 @@ size_t am_get_fluid_particles(am_morph *m, double *state, size_t cap);
 /* Guided-refinement tunables (the autotuner sets these): "local_self",
  * "local_target", "local_random" (candidates per column from the column's own
  * neighbourhood, its target cell, and uniform random columns),
- * "learned_keep" (fraction of columns, 0 < f <= 1, that the learned gate lets
- * run the guided candidate scan in each sweep) and
+ * "learned_keep" (fraction of 32-slot regions, 0 < f <= 1, that the learned
+ * gate lets run the guided candidate scan in a gated sweep),
+ * "learned_adaptive" (1, the default: the learned form runs its gate only in
+ * blocks of sweeps where gated sweeps keep up with full ones; 0: always) and
  * "guided_switch" (guided/learned refinement runs plain sweeps until one gains
  * less than this fraction of the cost per sweep; 0 = guided from the start). */
 int am_set_tuning(am_morph *m, const char *name, double value);
