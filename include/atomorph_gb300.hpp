@@ -16,6 +16,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <iostream>  // callers of the reference rely on its header pulling in the iostreams
 #include <stdexcept>
 #include <vector>
 
@@ -57,10 +58,24 @@ inline size_t xy2pos(uint16_t x, uint16_t y) { return (size_t)y * (UINT16_MAX + 
 inline const char *get_version() { return "1.0"; }
 // atomorph.h:300-302, 355-357: build warnings and the OpenCV variant flag.
 const size_t WARN_POINTER_SIZE = 1, WARN_PIXEL_SIZE = 2, WARN_POINT_SIZE = 3;
+// The 8-byte atom word (atomorph.h:275-284): the layout the chains use on
+// the GPU and in am_export_chains / am_import_chains.
+typedef union key_point {
+    struct {
+        uint16_t x;
+        uint16_t y;
+        uint8_t x_fract;
+        uint8_t y_fract;
+        uint8_t flags;
+    } s;
+    uint64_t word;
+} point;
+
 inline size_t get_warning() {
     size_t flags = 0;
     if (sizeof(void *) < 8) flags |= WARN_POINTER_SIZE;
     if (sizeof(pixel) > 8) flags |= WARN_PIXEL_SIZE;
+    if (sizeof(point) > 8) flags |= WARN_POINT_SIZE;
     return flags;
 }
 inline bool uses_opencv() { return false; }
