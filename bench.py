@@ -122,6 +122,23 @@ def render_roofline(m, frames_ts, torch, stream):
     return prof
 
 
+def max_over_ranks(ms, world, device="cuda"):
+    """Slowest rank's timed region: the whole job's throughput is measured
+    against it (replicas render their own cycles, so this is the only
+    collective of a multi-GPU run)."""
+    if world == 1:
+        return float(ms)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(frames_per_rank, world, ms):
+    """Whole-job frames/s: frames all ranks rendered over the slowest rank's time."""
+    return frames_per_rank * world / (ms / 1e3)
+
+
 def bench_ours(args, rank, world):
     import torch
     from atomorph_gb300 import capi, synth
@@ -160,12 +177,8 @@ def bench_ours(args, rank, world):
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     launches = capi.launch_count() - launches0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    total_frames = FRAMES_PER_STEP * args.steps * world
-    value = total_frames / (ms / 1e3)
+    ms = max_over_ranks(ms, world)
+    value = job_value(FRAMES_PER_STEP * args.steps, world, ms)
 
     # e2e: same frames through the C ABI into pinned host memory
     host = torch.empty((8, m.height, m.width, 4), dtype=torch.uint8).pin_memory()
