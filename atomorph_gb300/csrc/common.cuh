@@ -37,7 +37,7 @@ constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
 // around each launch; read back (and waited for) by collect().
 enum ProfId {
     PROF_SPLAT, PROF_SCAN, PROF_SCATTER, PROF_RESOLVE, PROF_PAIR, PROF_SWEEP_RANDOM, PROF_SWEEP_LOCAL,
-    PROF_MLP, PROF_FLUID, PROF_BIN, PROF_COUNT
+    PROF_MLP, PROF_FLUID, PROF_BIN, PROF_FLUID_MANAGE, PROF_FLUID_DRAW, PROF_COUNT
 };
 struct Prof {
     bool on = false;

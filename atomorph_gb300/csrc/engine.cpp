@@ -22,8 +22,8 @@ namespace amg {
 
 std::atomic<uint64_t> g_launches{0};
 const char *const kProfNames[PROF_COUNT] = {"k_frame_splat", "k_scan_u32",   "k_frame_scatter", "k_frame_resolve",
-                                            "pair_prep",     "k_sweep_random", "k_sweep_local", "mlp", "fluid",
-                                            "k_frame_bin"};
+                                            "pair_prep",     "k_sweep_random", "k_sweep_local", "mlp", "fluid_step",
+                                            "k_frame_bin",   "fluid_manage", "fluid_draw"};
 static thread_local std::string t_error;
 void set_error(const std::string &msg) { t_error = msg; }
 const char *last_error() { return t_error.c_str(); }

@@ -588,6 +588,8 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
     AMG_CUDA(cudaMemsetAsync(m->src_any, 0, canvas * 8, s));
     AMG_CUDA(cudaMemsetAsync(m->chain_cnt, 0, (size_t)sc.C * 4, s));
     AMG_CUDA(cudaMemsetAsync(m->phase1, 0, (size_t)sc.C * 4, s));
+    Prof *prof = render_prof(fr_in.rw);
+    if (prof) prof->open(s);
     AMG_LAUNCH(k_fm_classify, g, 256, 0, s, a);
     // active limits (morph.cpp:830-835)
     std::vector<uint32_t> cnt(sc.C), create(sc.C, 0), del(sc.C, 0);
@@ -636,12 +638,16 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
         }
     }
     AMG_LAUNCH(k_fm_update, g, 256, 0, s, a);
+    if (prof) prof->close(PROF_FLUID_MANAGE, s);
     // solver steps (morph.cpp:1052-1054)
     const double freedom = std::sqrt((double)sc.width * sc.width + (double)sc.height * sc.height) *
                            fr_in.sparseness / 4.0;
     for (uint32_t k = 0; k < fr_in.fluidsteps; ++k)
-        if ((rc = fluid_step(fl, fr_in.fluidsteps - (k + 1), freedom * (1.0 - fr.t), s, nullptr))) return rc;
-    return fluid_draw(fl, m->acc, sc.width, sc.height, fr_in.sparseness, sc.bbox, fr.t, out, s);
+        if ((rc = fluid_step(fl, fr_in.fluidsteps - (k + 1), freedom * (1.0 - fr.t), s, prof))) return rc;
+    if (prof) prof->open(s);
+    rc = fluid_draw(fl, m->acc, sc.width, sc.height, fr_in.sparseness, sc.bbox, fr.t, out, s);
+    if (prof) prof->close(PROF_FLUID_DRAW, s);
+    return rc;
 }
 
 }  // namespace amg

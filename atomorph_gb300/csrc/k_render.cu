@@ -78,6 +78,7 @@ constexpr uint64_t kPairCacheBytes = 8ull << 30;
 constexpr uint64_t kPairBytesPerAtom = 16 + 16 + 8 + 8 + 4 + 4;
 
 void render_set_prof(RenderWork *w, Prof *p) { w->prof = p; }
+Prof *render_prof(RenderWork *w) { return w ? w->prof : nullptr; }
 
 RenderWork *render_work_create() { return new RenderWork(); }
 
@@ -179,7 +180,7 @@ __device__ __forceinline__ uint32_t find_chain_r(const uint64_t *__restrict__ of
 __global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, const int *__restrict__ perm,
                                                     int4 *pa, int4 *pb, uint2 *col, float2 *ls, uint32_t *rank,
                                                     uint32_t *keys, uint32_t *vals, uint32_t tiles_x,
-                                                    uint32_t inactive_key) {
+                                                    uint32_t inactive_key, uint32_t key_shift) {
     __shared__ int sp[1024];
     for (int i = threadIdx.x; i < 1024; i += blockDim.x) sp[i] = perm ? perm[i] : 0;
     __syncthreads();
@@ -226,7 +227,12 @@ __global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, c
         int mx = ((X1 + X2) >> 9), my = ((Y1 + Y2) >> 9);
         mx = min(max(mx, 0), (int)sc.width - 1);
         my = min(max(my, 0), (int)sc.height - 1);
-        keys[i] = (uint32_t)((my / kTile) * tiles_x + (mx / kTile));
+        // tile-major, row-major inside the tile (below 2^21 tiles): where the
+        // motion is coherent a warp's atoms sit in a row of distinct columns,
+        // so the resolve's shared accumulators (banked by column) see few
+        // conflicts
+        const uint32_t tile = (uint32_t)((my / kTile) * tiles_x + (mx / kTile));
+        keys[i] = key_shift ? (tile << key_shift) | ((uint32_t)(my % kTile) << 5) | (uint32_t)(mx % kTile) : tile;
     }
 }
 
@@ -899,11 +905,14 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
     if (w->prof) w->prof->open(s);
     uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
     unsigned grid = (unsigned)std::min<uint64_t>((sc.N + 255) / 256, (uint64_t)kSMs * 8);
+    // Keys: the midpoint's tile, then its row-major place inside the tile;
+    // inactive atoms carry the largest key and sort last.
+    const uint64_t ntiles = (uint64_t)tiles_x * tiles_y;
+    const uint32_t key_shift = ntiles < (1ull << 21) ? 10u : 0u;
     AMG_LAUNCH(k_pair_prep, grid, 256, 0, s, sc, f, w->perm_set ? w->perm : nullptr, w->pa, w->pb, w->col, w->ls,
-               w->rank, w->keys, w->vals, tiles_x, tiles_x * tiles_y);
-    // Inactive atoms carry key ntiles so a sort on the tile bits orders them last.
+               w->rank, w->keys, w->vals, tiles_x, (uint32_t)(ntiles << key_shift), key_shift);
     int bits = 1;
-    while ((1ull << bits) < (uint64_t)tiles_x * tiles_y + 1) ++bits;
+    while ((1ull << bits) < (ntiles << key_shift) + 1) ++bits;
     rc = radix_sort_pairs(w->keys, w->vals, w->tkeys, w->tvals, w->hist, sc.N, bits, s);
     if (rc) return rc;
     AMG_CUDA(cudaMemsetAsync(d.d_active, 0, 4, s));

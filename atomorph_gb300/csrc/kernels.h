@@ -221,6 +221,7 @@ struct RenderWork;                // per-handle scratch (k_render.cu)
 RenderWork *render_work_create();
 void render_work_destroy(RenderWork *w);
 void render_set_prof(RenderWork *w, Prof *p);
+Prof *render_prof(RenderWork *w);  // the timer render_set_prof installed (or null)
 // Uploads the two Perlin permutations (lag map seed, slope map seed+1).
 int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope);
 // Renders the frame at normalised time `time` into out (device, width*height*4).

@@ -138,16 +138,18 @@ static __device__ __noinline__ uint32_t spl_fixed(double b0, double b1, double b
 // PERLIN / COSINE ramp of an atom depends on its lag and slope only, so its
 // parameters are prepared once per key-frame pair: fade_params gives
 // (l, pi / s) with s = (slope + 0.1) / 1.1 and l = (1 - s) lag, and the
-// frame's weight of the earlier colour is 0 before l, 1 after l + s and the
-// cosine ramp between.
+// frame's weight of the earlier colour is 0 up to l, 1 from l + s and the
+// cosine ramp between.  Octave noise below -1.2 makes s <= 0: the reference's
+// tests then give 0 up to l and 1 after it, a step, which pi / s = +inf
+// reproduces (x is +inf past l, NaN at l, -inf before).
 __device__ __forceinline__ float2 fade_params(float lag, float slope) {
     const float s = (slope + 0.1f) / 1.1f;
-    return make_float2((1.f - s) * lag, 3.14159265358f / s);
+    return make_float2((1.f - s) * lag, s > 0.f ? 3.14159265358f / s : __int_as_float(0x7f800000));
 }
 __device__ __forceinline__ uint32_t fade_colour(uint32_t fading, uint32_t c1, uint32_t c2, float2 fp, float str) {
     if (fading == AM_PERLIN || fading == AM_COSINE) {
         const float x = (str - fp.x) * fp.y;
-        if (x <= 0.f) str = 0.f;
+        if (!(x > 0.f)) str = 0.f;
         else if (x >= 3.14159265358f) str = 1.f;
         else str = (1.f - __cosf(x)) * 0.5f;  // x in (0, pi): the intrinsic's error is far below 1/255
     }

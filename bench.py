@@ -223,6 +223,9 @@ def bench_ours(args, rank, world):
                       "frac": round(frame_bytes / (frame_ms_profiled / 1e3) / 1e9 / hbm, 4)},
             "kernels_ms_per_frame": {k: round(v[0] / FRAMES_PER_STEP, 5) for k, v in per_frame.items()}}
 
+    flu = None
+    if rank == 0 and args.fluid_frames:
+        flu = fluid_bench(m, torch, stream, args)
     ttc = None
     if rank == 0 and args.time_to_cost:
         ttc = time_to_cost(capi, frames, args)
@@ -251,12 +254,69 @@ def bench_ours(args, rank, world):
         "roofline": roof,
         "clocks": clk.summary(),
     }
+    if flu is not None:
+        res["fluid"] = flu
     if ttc is not None:
         res["time_to_cost"] = ttc
     if bat is not None:
         res["batch"] = bat
     if cpu is not None:
         res["cpu_baseline"] = cpu
+    return res
+
+
+def fluid_bench(m, torch, stream, args):
+    """Fluid-on frames (the draw_fluid path the reference takes when fluid
+    steps are set, morph.cpp:1417-1418) on the same chains: every frame
+    manages the particles (step_fluid), runs `--fluid-steps` solver steps on
+    a grid of (0.5 x 1024 + 20)^2 nodes and draws them.  The simulation is
+    stateful, so frames are rendered in cycle order; timed with CUDA events
+    on the render stream.  Per-part times come from one further profiled run
+    of frames."""
+    m.set(fluid=args.fluid_steps, fluid_sparseness=0.5)
+    n_frames = FRAMES_PER_STEP
+    out = torch.empty((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    ts = [m.get_time(i, n_frames) for i in range(n_frames)]
+    cursor = [0]
+
+    def frames(k):
+        for _ in range(k):
+            m.render_device(float(ts[cursor[0] % n_frames]), out.data_ptr())
+            cursor[0] += 1
+
+    frames(max(args.warmup, 3))
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    frames(args.fluid_frames)
+    e1.record(stream)
+    stream.synchronize()
+    ms = e0.elapsed_time(e1)
+    m.profile(True)
+    m.profile_read()
+    frames(min(args.fluid_frames, 8))
+    stream.synchronize()
+    prof = m.profile_read()
+    m.profile(False)
+    m.set(fluid=0)
+    hbm, peak_kind = _peaks()
+    P = m.atoms
+    gx = gy = int(round(1024 * 0.5)) + 20
+    step_bytes = P * 96 + gx * gy * 104  # particle fields read 16 + written 8 (FP32); 13 node fields x2
+    st_ms, st_n = prof.get("fluid_step", (0.0, 0))
+    res = {"workload": WORKLOAD + " with fluid", "grid": [gx, gy], "particles": int(P),
+           "steps_per_frame": args.fluid_steps, "frames": args.fluid_frames,
+           "frames_per_s": round(args.fluid_frames / (ms / 1e3), 2),
+           "ms_per_frame": round(ms / args.fluid_frames, 4),
+           "ms_per_frame_parts": {k: round(v[0] / max(1, min(args.fluid_frames, 8)), 4) for k, v in prof.items()
+                                  if k.startswith("fluid") and v[1] > 0}}
+    if st_n:
+        achieved = step_bytes / (st_ms / st_n / 1e3) / 1e9
+        res["step_roofline"] = {"bound": "hbm", "algorithmic_bytes_per_step": int(step_bytes),
+                                "avg_step_ms": round(st_ms / st_n, 5), "achieved": round(achieved, 1),
+                                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                                "peak_kind": peak_kind}
     return res
 
 
@@ -559,6 +619,8 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=2)
     ap.add_argument("--batch-jobs", type=int, default=32)
     ap.add_argument("--batch-sweeps", type=int, default=200)
+    ap.add_argument("--fluid-frames", type=int, default=24)
+    ap.add_argument("--fluid-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -88,3 +88,62 @@ def test_render_device_output_matches_host(capi):
         m.render_device(t, buf.data_ptr())
         assert m.lib.am_device_sync(m.h) == capi.AM_OK  # device frames are left in flight
         assert np.array_equal(buf.cpu().numpy(), m.render(t))
+
+
+@pytest.mark.parametrize("resolution", [(1600, 1500), (300, 200)])
+def test_render_other_resolutions_match_oracle(capi, oracle, resolution):
+    """Outputs above 2048 tiles of 32x32 px take the separate splat / scan /
+    scatter kernels instead of the fused binning; an output smaller than the
+    key frames drops the atoms outside it.  Same parity bar."""
+    frames = synth.workload("shapes256")
+    m = capi.Morph()
+    m.load(frames, seed=3, blob_delimiter=1, motion=4, fading=6)
+    assert m.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+    m.refine(20)
+    m.set(resolution=resolution)
+    assert (m.width, m.height) == resolution
+    w, pts, order = m.export_chains()
+    from oracle.oracle import stored_frames
+    colors, present = stored_frames(frames, 1, oracle)
+    st = dict(K=len(frames), width=m.width, height=m.height, bbox=_bbox(frames), seed=3, motion=4, fading=6,
+              delimiter=1, density=1, colors=colors, present=present, widths=w, pts=pts, blob_order=order,
+              frame_keys=np.arange(len(frames), dtype=np.uint64))
+    for t in (0.1, 0.45, 0.8):
+        ref = oracle.render(st, t)
+        got = m.render(t)
+        worst, ndiff = _lsb(got, ref)
+        assert worst <= 1, f"t={t}: worst {worst}, {ndiff} channels differ"
+        assert ndiff <= max(16, ref.size // 200)
+
+
+@pytest.mark.parametrize("motion", [2, 3, 4])
+def test_render_perlin_step_ramp_matches_oracle(capi, oracle, motion):
+    """PERLIN fading where an atom's octave noise falls below -1.2: the
+    reference's ramp width s = (slope + 0.1) / 1.1 is then <= 0 and its colour
+    weight steps from 0 to 1 at l (morph.cpp:1467-1479).  This seeded case
+    (4 ellipses, HSP blobs) has such atoms in the second key-frame pair."""
+    frames = synth.workload("ellipses64")
+    m = capi.Morph()
+    m.load(frames, seed=7, blob_delimiter=capi.HSP, motion=motion, fading=capi.PERLIN)
+    assert m.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+    m.refine(50)
+    w, pts, order = m.export_chains()
+    from oracle.oracle import stored_frames
+    colors, present = stored_frames(frames, capi.HSP, oracle)
+    bbox = _bbox(frames)
+    # the case does exercise the step: some frame-1 atom has slope < -0.1
+    P = pts.reshape(2, -1)
+    x = (P & np.uint64(0xFFFF)).astype(np.float64) + ((P >> np.uint64(32)) & np.uint64(0xFF)) / 256.0
+    y = ((P >> np.uint64(16)) & np.uint64(0xFFFF)).astype(np.float64) + ((P >> np.uint64(40)) & np.uint64(0xFF)) / 256.0
+    bw, bh = bbox[2] - bbox[0] + 1.0, bbox[3] - bbox[1] + 1.0
+    px, py = (x[1] - bbox[0]) / bw * 8.0, (y[1] - bbox[1]) / bh * 8.0
+    slopes = [oracle.octave_noise(8, a, b) * 0.5 + 0.5 for a, b in zip(px, py)]
+    assert min(slopes) < -0.1
+    st = dict(K=2, width=m.width, height=m.height, bbox=bbox, seed=7, motion=motion, fading=capi.PERLIN,
+              delimiter=capi.HSP, density=1, colors=colors, present=present, widths=w, pts=pts, blob_order=order,
+              frame_keys=np.arange(2, dtype=np.uint64))
+    for t in (0.3, 0.55, 0.7, 0.9):
+        ref = oracle.render(st, t)
+        got = m.render(t)
+        worst, ndiff = _lsb(got, ref)
+        assert worst <= 1, f"t={t}: worst {worst}, {ndiff} channels differ"
