@@ -1,5 +1,6 @@
 // extern "C" entry points of the standalone fluid solver (the GB300
 // counterpart of the reference's FluidModel, fluidmodel.h:103-142).
+#include <algorithm>
 #include "engine.h"
 
 struct am_fluid {
@@ -54,8 +55,9 @@ int am_fluid_step(am_fluid *h, size_t steps_left, double freedom_radius) {
 
 int am_fluid_steps(am_fluid *h, size_t n, double freedom_radius) {
     if (!h) return AM_ERR_ARG;
-    for (size_t i = 0; i < n; ++i) {
-        int rc = amg::fluid_step(h->f, n - (i + 1), freedom_radius, h->s, nullptr);
+    for (size_t i = 0; i < n; i += 1u << 20) {
+        const uint32_t k = (uint32_t)std::min<size_t>(n - i, 1u << 20);
+        int rc = amg::fluid_run(h->f, k, n - i - k, freedom_radius, h->s, nullptr);
         if (rc) return rc;
     }
     return cudaStreamSynchronize(h->s) == cudaSuccess ? AM_OK : AM_ERR_CUDA;

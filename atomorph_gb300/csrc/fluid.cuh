@@ -15,11 +15,14 @@ enum { NM, ND, NGX, NGY, NAX, NAY, NU, NV, NW, NR, NG, NB, NA, kFlNode };
 
 struct FluidDev {
     uint32_t gsx = 0, gsy = 0, n = 0;
-    float *P = nullptr;      // [kFlFields][n]
+    float *P = nullptr;      // [kFlFields][n] in the caller's order
     uint8_t *flags = nullptr;// [n] bit0 active, bit1 mature
-    int2 *cell = nullptr;    // [n] stencil origin
     float *G = nullptr;      // [kFlNode][gsx*gsy]
     uint64_t step = 0;
+    // solver order (particles sorted by 8x8 cell block) for fluid_run
+    float *S = nullptr;      // [kFlFields][n] gathered copy
+    uint8_t *sflags = nullptr;
+    uint32_t *keys = nullptr, *ids = nullptr, *tkeys = nullptr, *tids = nullptr, *hist = nullptr;
 };
 
 

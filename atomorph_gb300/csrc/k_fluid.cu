@@ -21,6 +21,15 @@
 // the jitter is a counter hash of (step, particle) in the same range.
 // Grid clearing replaces the reference's active-node list: every node a step
 // touches is zero before the next step either way.
+//
+// Particles are kept in the caller's order (the morph's particle p is atom
+// column p, spatially random).  fluid_run sorts them by 8x8 cell block once
+// per call, runs its steps on a gathered copy in that order and scatters the
+// changed fields back.  In sorted order a CTA's 256 particles cover a compact
+// patch of the grid, so the three deposit passes accumulate into a
+// shared-memory copy of the patch's nodes and add it to the grid with one
+// atomic per node and field; a CTA whose patch exceeds kPrivNodes nodes (sparse
+// regions, block-row ends) deposits directly.
 #include "common.cuh"
 #include "fluid.cuh"
 #include "kernels.h"
@@ -55,14 +64,47 @@ __device__ __forceinline__ Stencil stencil(float x, float y, uint32_t gsx, uint3
 }
 
 struct FlArgs {
-    float *P;
+    float *P;                 // [kFlFields][n] particles in solver (sorted) order
     const uint8_t *flags;
-    int2 *cell;
+    const uint32_t *ids;      // [n] caller index of each solver slot (wall-jitter hash)
     float *G;
     uint32_t n, gsx, gsy;
     float freedom_radius, w_pull;  // w_pull = 1 / (steps_left + 1)
     uint64_t step;
 };
+
+constexpr int kFlThreads = 256;    // particles per CTA of the deposit passes (one per thread)
+constexpr int kPrivNodes = 1024;   // nodes of a CTA's shared-memory patch
+
+// Patch of the CTA's 3x3 stencils (origins (cx, cy) of its active
+// particles): box = {x0, y0, width, height} in shared memory.  True when the
+// CTA has active particles and the patch fits kPrivNodes nodes (uniform).
+__device__ bool priv_box(bool act, int cx, int cy, int *box, int *red) {
+    int mnx = act ? cx : INT_MAX, mny = act ? cy : INT_MAX, mxx = act ? cx : INT_MIN, mxy = act ? cy : INT_MIN;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[4 * w] = mnx; red[4 * w + 1] = mny; red[4 * w + 2] = mxx; red[4 * w + 3] = mxy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kFlThreads / 32; ++k) {
+            mnx = min(mnx, red[4 * k]); mny = min(mny, red[4 * k + 1]);
+            mxx = max(mxx, red[4 * k + 2]); mxy = max(mxy, red[4 * k + 3]);
+        }
+        box[0] = mnx; box[1] = mny;
+        box[2] = mnx == INT_MAX ? 0 : mxx - mnx + 3;
+        box[3] = mnx == INT_MAX ? 0 : mxy - mny + 3;
+    }
+    __syncthreads();
+    return box[2] > 0 && box[2] * box[3] <= kPrivNodes;
+}
 
 #define FL(f, i) a.P[(size_t)(f) * a.n + (i)]
 #define ND_(f, q) a.G[(size_t)(f) * ((size_t)a.gsx * a.gsy) + (q)]
@@ -70,14 +112,26 @@ struct FlArgs {
 // Grid index of node (i, j) = grid[i][j] of the reference (x-major).
 __device__ __forceinline__ size_t node(const FlArgs &a, int i, int j) { return (size_t)i * a.gsy + j; }
 
-__global__ void k_fl_p2g(FlArgs a) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
-        uint8_t fl = a.flags[p];
-        if (!(fl & 1)) continue;
-        Stencil s = stencil(FL(PX, p), FL(PY, p), a.gsx, a.gsy);
-        a.cell[p] = make_int2(s.cx, s.cy);
-        bool colour = (fl & 2) && FL(PSTR, p) > 0.f;
-        float str = FL(PSTR, p), r = FL(Pr, p), g = FL(Pg, p), b = FL(Pb, p), al = FL(Pa, p);
+// Deposit fields of k_fl_p2g's shared patch: mass (= density: material mass
+// 1), density gradient x, y, colour weight and weighted R G B A.
+enum { QM, QGX, QGY, QW, QR, QG, QB, QA, kQ };
+
+__global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
+    __shared__ float acc[kQ * kPrivNodes];
+    __shared__ int box[4], red[4 * (kFlThreads / 32)];
+    const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
+    const uint8_t fl = p < a.n ? a.flags[p] : 0;
+    const bool act = fl & 1;
+    Stencil s{};
+    float str = 0.f, r = 0.f, g = 0.f, b = 0.f, al = 0.f;
+    bool colour = false;
+    if (act) {
+        s = stencil(FL(PX, p), FL(PY, p), a.gsx, a.gsy);
+        str = FL(PSTR, p); r = FL(Pr, p); g = FL(Pg, p); b = FL(Pb, p); al = FL(Pa, p);
+        colour = (fl & 2) && str > 0.f;
+    }
+    if (!priv_box(act, s.cx, s.cy, box, red)) {
+        if (!act) return;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -96,12 +150,106 @@ __global__ void k_fl_p2g(FlArgs a) {
                     atomicAdd(&ND_(NA, q), str * al);
                 }
             }
+        return;
+    }
+    const int x0 = box[0], y0 = box[1], bh = box[3], nn = box[2] * bh;
+    for (int k = threadIdx.x; k < kQ * kPrivNodes; k += kFlThreads)
+        if ((k % kPrivNodes) < nn) acc[k] = 0.f;
+    __syncthreads();
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int q = (s.cx + i - x0) * bh + (s.cy + j - y0);
+                const float phi = s.px[i] * s.py[j];
+                atomicAdd(&acc[QM * kPrivNodes + q], phi);
+                atomicAdd(&acc[QGX * kPrivNodes + q], s.gx[i] * s.py[j]);
+                atomicAdd(&acc[QGY * kPrivNodes + q], s.px[i] * s.gy[j]);
+                if (colour) {
+                    atomicAdd(&acc[QW * kPrivNodes + q], str);
+                    atomicAdd(&acc[QR * kPrivNodes + q], str * r);
+                    atomicAdd(&acc[QG * kPrivNodes + q], str * g);
+                    atomicAdd(&acc[QB * kPrivNodes + q], str * b);
+                    atomicAdd(&acc[QA * kPrivNodes + q], str * al);
+                }
+            }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nn; q += kFlThreads) {
+        const float m = acc[QM * kPrivNodes + q], gx = acc[QGX * kPrivNodes + q], gy = acc[QGY * kPrivNodes + q];
+        const size_t n = node(a, x0 + q / bh, y0 + q % bh);
+        if (m != 0.f || gx != 0.f || gy != 0.f) {
+            atomicAdd(&ND_(NM, n), m);
+            atomicAdd(&ND_(ND, n), m);
+            atomicAdd(&ND_(NGX, n), gx);
+            atomicAdd(&ND_(NGY, n), gy);
+        }
+        const float w = acc[QW * kPrivNodes + q];
+        if (w != 0.f) {
+            atomicAdd(&ND_(NW, n), w);
+            atomicAdd(&ND_(NR, n), acc[QR * kPrivNodes + q]);
+            atomicAdd(&ND_(NG, n), acc[QG * kPrivNodes + q]);
+            atomicAdd(&ND_(NB, n), acc[QB * kPrivNodes + q]);
+            atomicAdd(&ND_(NA, n), acc[QA * kPrivNodes + q]);
+        }
     }
 }
 
-__global__ void k_fl_forces(FlArgs a) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
-        if (!(a.flags[p] & 1)) continue;
+// Adds a two-field 3x3 deposit (per-node values v1, v2 of the stencil) into
+// the grid fields f1, f2 through the CTA's shared patch when it fits.
+struct Dep2 {
+    float v1[9], v2[9];
+};
+__device__ __forceinline__ void deposit2(const FlArgs &a, bool act, const Stencil &s, const Dep2 &d, int f1, int f2,
+                                         float *acc, int *box, int *red) {
+    if (!priv_box(act, s.cx, s.cy, box, red)) {
+        if (!act) return;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const size_t q = node(a, s.cx + i, s.cy + j);
+                atomicAdd(&ND_(f1, q), d.v1[3 * i + j]);
+                atomicAdd(&ND_(f2, q), d.v2[3 * i + j]);
+            }
+        return;
+    }
+    const int x0 = box[0], y0 = box[1], bh = box[3], nn = box[2] * bh;
+    for (int q = threadIdx.x; q < nn; q += kFlThreads) {
+        acc[q] = 0.f;
+        acc[kPrivNodes + q] = 0.f;
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int q = (s.cx + i - x0) * bh + (s.cy + j - y0);
+                atomicAdd(&acc[q], d.v1[3 * i + j]);
+                atomicAdd(&acc[kPrivNodes + q], d.v2[3 * i + j]);
+            }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nn; q += kFlThreads) {
+        const float u = acc[q], v = acc[kPrivNodes + q];
+        if (u != 0.f || v != 0.f) {
+            const size_t n = node(a, x0 + q / bh, y0 + q % bh);
+            atomicAdd(&ND_(f1, n), u);
+            atomicAdd(&ND_(f2, n), v);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kFlThreads) k_fl_forces(FlArgs a) {
+    __shared__ float acc[2 * kPrivNodes];
+    __shared__ int box[4], red[4 * (kFlThreads / 32)];
+    const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
+    const bool act = p < a.n && (a.flags[p] & 1);
+    Stencil s{};
+    Dep2 d;
+    if (act) {
         float x = FL(PX, p), y = FL(PY, p);
         int cx = min(max((int)x, 0), (int)a.gsx - 2), cy = min(max((int)y, 0), (int)a.gsy - 2);
         size_t n01 = node(a, cx, cy), n02 = node(a, cx, cy + 1), n11 = node(a, cx + 1, cy),
@@ -127,17 +275,17 @@ __global__ void k_fl_forces(FlArgs a) {
         else if (x > (float)(a.gsx - 5)) fx += (float)(a.gsx - 5) - x;
         if (y < 4.f) fy += 4.f - y;
         else if (y > (float)(a.gsy - 5)) fy += (float)(a.gsy - 5) - y;
-        Stencil s = stencil(x, y, a.gsx, a.gsy);
+        s = stencil(x, y, a.gsx, a.gsy);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                size_t q = node(a, s.cx + i, s.cy + j);
                 float phi = s.px[i] * s.py[j];
-                atomicAdd(&ND_(NAX, q), -((s.gx[i] * s.py[j]) * pressure) + fx * phi);
-                atomicAdd(&ND_(NAY, q), -((s.px[i] * s.gy[j]) * pressure) + fy * phi);
+                d.v1[3 * i + j] = -((s.gx[i] * s.py[j]) * pressure) + fx * phi;
+                d.v2[3 * i + j] = -((s.px[i] * s.gy[j]) * pressure) + fy * phi;
             }
     }
+    deposit2(a, act, s, d, NAX, NAY, acc, box, red);
 }
 
 __global__ void k_fl_div(FlArgs a, int fa, int fb) {
@@ -167,12 +315,17 @@ __device__ __forceinline__ void pull(float x1, float y1, float x2, float y2, flo
     }
 }
 
-__global__ void k_fl_vel(FlArgs a) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
-        uint8_t fl = a.flags[p];
-        if (!(fl & 1)) continue;
+__global__ void __launch_bounds__(kFlThreads) k_fl_vel(FlArgs a) {
+    __shared__ float acc[2 * kPrivNodes];
+    __shared__ int box[4], red[4 * (kFlThreads / 32)];
+    const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
+    const uint8_t fl = p < a.n ? a.flags[p] : 0;
+    const bool act = fl & 1;
+    Stencil s{};
+    Dep2 d;
+    if (act) {
         float x = FL(PX, p), y = FL(PY, p);
-        Stencil s = stencil(x, y, a.gsx, a.gsy);
+        s = stencil(x, y, a.gsx, a.gsy);
         float cax, cay;
         pull(x, y, FL(PGX, p), FL(PGY, p), 0.03f, cax, cay);
         float u = FL(PU, p), v = FL(PV, p);
@@ -192,12 +345,12 @@ __global__ void k_fl_vel(FlArgs a) {
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                size_t q = node(a, s.cx + i, s.cy + j);
                 float phi = s.px[i] * s.py[j];
-                atomicAdd(&ND_(NU, q), phi * mu);
-                atomicAdd(&ND_(NV, q), phi * mv);
+                d.v1[3 * i + j] = phi * mu;
+                d.v2[3 * i + j] = phi * mv;
             }
     }
+    deposit2(a, act, s, d, NU, NV, acc, box, red);
 }
 
 __global__ void k_fl_advect(FlArgs a) {
@@ -248,13 +401,51 @@ __global__ void k_fl_advect(FlArgs a) {
             }
         }
         float u = gu, v = gv;
-        uint32_t h = mix32((uint32_t)a.step * 0x9E3779B1u ^ mix32(p));
+        uint32_t h = mix32((uint32_t)a.step * 0x9E3779B1u ^ mix32(a.ids ? a.ids[p] : p));
         float jit = (float)(h & 0xFFFFFFu) / 16777215.f * 0.01f;
         if (x < 1.f) { x = 1.f + jit; u = 0.f; }
         else if (x > (float)(a.gsx - 2)) { x = (float)(a.gsx - 2) - jit; u = 0.f; }
         if (y < 1.f) { y = 1.f + jit; v = 0.f; }
         else if (y > (float)(a.gsy - 2)) { y = (float)(a.gsy - 2) - jit; v = 0.f; }
         FL(PX, p) = x; FL(PY, p) = y; FL(PU, p) = u; FL(PV, p) = v;
+    }
+}
+
+// Sort key of a particle: its stencil cell's 8x8 block (row-major over
+// blocks), then the cell inside the block; inactive particles sort last.
+__global__ void k_fl_keys(const float *__restrict__ P, const uint8_t *__restrict__ flags, uint32_t n,
+                          uint32_t gsx, uint32_t gsy, uint32_t *keys, uint32_t *ids) {
+    const uint32_t nbx = (gsx + 7) / 8, nby = (gsy + 7) / 8;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        ids[p] = p;
+        if (!(flags[p] & 1)) {
+            keys[p] = nbx * nby * 64u;
+            continue;
+        }
+        const int cx = min(max((int)(P[(size_t)PX * n + p] - 0.5f), 0), (int)gsx - 3);
+        const int cy = min(max((int)(P[(size_t)PY * n + p] - 0.5f), 0), (int)gsy - 3);
+        keys[p] = (((uint32_t)cy >> 3) * nbx + ((uint32_t)cx >> 3)) << 6 | ((uint32_t)cy & 7u) << 3 | ((uint32_t)cx & 7u);
+    }
+}
+
+__global__ void k_fl_gather(const float *__restrict__ P, const uint8_t *__restrict__ flags,
+                            const uint32_t *__restrict__ ids, uint32_t n, float *S, uint8_t *sflags) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t p = ids[j];
+        sflags[j] = flags[p];
+#pragma unroll
+        for (int k = 0; k < kFlFields; ++k) S[(size_t)k * n + j] = P[(size_t)k * n + p];
+    }
+}
+
+// The fields a step changes (position, velocity, current colour) back to the
+// caller's order.
+__global__ void k_fl_scatter(const float *__restrict__ S, const uint32_t *__restrict__ ids, uint32_t n, float *P) {
+    const int changed[8] = {PX, PY, PU, PV, Pr, Pg, Pb, Pa};
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t p = ids[j];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) P[(size_t)changed[k] * n + p] = S[(size_t)changed[k] * n + j];
     }
 }
 
@@ -265,10 +456,13 @@ FluidDev *fluid_create(uint32_t gsx, uint32_t gsy, uint32_t n) {
     FluidDev *f = new FluidDev();
     f->gsx = gsx; f->gsy = gsy; f->n = n;
     size_t G = (size_t)gsx * gsy;
-    if (cudaMalloc(&f->P, (size_t)kFlFields * std::max<uint32_t>(n, 1) * 4) != cudaSuccess ||
-        cudaMalloc(&f->flags, std::max<uint32_t>(n, 1)) != cudaSuccess ||
-        cudaMalloc(&f->cell, sizeof(int2) * std::max<uint32_t>(n, 1)) != cudaSuccess ||
-        cudaMalloc(&f->G, (size_t)kFlNode * G * 4) != cudaSuccess) {
+    const size_t m = std::max<uint32_t>(n, 1);
+    if (cudaMalloc(&f->P, (size_t)kFlFields * m * 4) != cudaSuccess || cudaMalloc(&f->flags, m) != cudaSuccess ||
+        cudaMalloc(&f->G, (size_t)kFlNode * G * 4) != cudaSuccess ||
+        cudaMalloc(&f->S, (size_t)kFlFields * m * 4) != cudaSuccess || cudaMalloc(&f->sflags, m) != cudaSuccess ||
+        cudaMalloc(&f->keys, m * 4) != cudaSuccess || cudaMalloc(&f->ids, m * 4) != cudaSuccess ||
+        cudaMalloc(&f->tkeys, m * 4) != cudaSuccess || cudaMalloc(&f->tids, m * 4) != cudaSuccess ||
+        cudaMalloc(&f->hist, radix_hist_words(m) * 4) != cudaSuccess) {
         fluid_destroy(f);
         return nullptr;
     }
@@ -281,8 +475,9 @@ void fluid_destroy(FluidDev *f) {
     if (!f) return;
     if (f->P) cudaFree(f->P);
     if (f->flags) cudaFree(f->flags);
-    if (f->cell) cudaFree(f->cell);
-    if (f->G) cudaFree(f->G);
+    void *ps[] = {f->G, f->S, f->sflags, f->keys, f->ids, f->tkeys, f->tids, f->hist};
+    for (void *q : ps)
+        if (q) cudaFree(q);
     delete f;
 }
 
@@ -319,28 +514,57 @@ int fluid_get(FluidDev *f, double *state, cudaStream_t s) {
     return AM_OK;
 }
 
-int fluid_step(FluidDev *f, uint64_t steps_left, double freedom_radius, cudaStream_t s, Prof *prof) {
-    FlArgs a;
-    a.P = f->P; a.flags = f->flags; a.cell = f->cell; a.G = f->G; a.n = f->n; a.gsx = f->gsx; a.gsy = f->gsy;
-    a.freedom_radius = (float)freedom_radius;
-    a.w_pull = (float)(1.0 / (double)(steps_left + 1));
-    a.step = ++f->step;
-    size_t G = (size_t)f->gsx * f->gsy;
-    if (prof) prof->open(s);
-    AMG_CUDA(cudaMemsetAsync(f->G, 0, (size_t)kFlNode * G * 4, s));
-    unsigned gp = (unsigned)std::min<uint64_t>((f->n + 255) / 256, (uint64_t)kSMs * 8);
-    unsigned gg = (unsigned)std::min<uint64_t>((G + 255) / 256, (uint64_t)kSMs * 8);
-    if (f->n) {
-        AMG_LAUNCH(k_fl_p2g, gp, 256, 0, s, a);
-        AMG_LAUNCH(k_fl_forces, gp, 256, 0, s, a);
-        AMG_LAUNCH(k_fl_div, gg, 256, 0, s, a, (int)NAX, (int)NAY);
-        AMG_LAUNCH(k_fl_vel, gp, 256, 0, s, a);
-        AMG_LAUNCH(k_fl_div, gg, 256, 0, s, a, (int)NU, (int)NV);
-        AMG_LAUNCH(k_fl_advect, gp, 256, 0, s, a);
+// `nsteps` solver steps; step k runs with steps_left = last_steps_left +
+// (nsteps - 1 - k) (the freedom-radius pull weight 1 / (steps_left + 1)).
+int fluid_run(FluidDev *f, uint32_t nsteps, uint64_t last_steps_left, double freedom_radius, cudaStream_t s,
+              Prof *prof) {
+    if (!nsteps) return AM_OK;
+    const uint32_t n = f->n;
+    const size_t G = (size_t)f->gsx * f->gsy;
+    const unsigned gl = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 8);
+    const unsigned gp = (unsigned)((n + kFlThreads - 1) / kFlThreads);
+    const unsigned gg = (unsigned)std::min<uint64_t>((G + 255) / 256, (uint64_t)kSMs * 8);
+    if (n) {
+        if (prof) prof->open(s);
+        AMG_LAUNCH(k_fl_keys, gl, 256, 0, s, f->P, f->flags, n, f->gsx, f->gsy, f->keys, f->ids);
+        const uint64_t maxkey = (uint64_t)((f->gsx + 7) / 8) * ((f->gsy + 7) / 8) * 64;
+        int bits = 1;
+        while ((1ull << bits) < maxkey + 1) ++bits;
+        int rc = radix_sort_pairs(f->keys, f->ids, f->tkeys, f->tids, f->hist, n, bits, s);
+        if (rc) return rc;
+        AMG_LAUNCH(k_fl_gather, gl, 256, 0, s, f->P, f->flags, f->ids, n, f->S, f->sflags);
+        if (prof) prof->close(PROF_FLUID_MANAGE, s);
     }
-    if (prof) prof->close(PROF_FLUID, s);
+    FlArgs a;
+    a.P = f->S; a.flags = f->sflags; a.ids = f->ids; a.G = f->G; a.n = n; a.gsx = f->gsx; a.gsy = f->gsy;
+    a.freedom_radius = (float)freedom_radius;
+    for (uint32_t k = 0; k < nsteps; ++k) {
+        const uint64_t steps_left = last_steps_left + (nsteps - 1 - k);
+        a.w_pull = (float)(1.0 / (double)(steps_left + 1));
+        a.step = ++f->step;
+        if (prof) prof->open(s);
+        AMG_CUDA(cudaMemsetAsync(f->G, 0, (size_t)kFlNode * G * 4, s));
+        if (n) {
+            AMG_LAUNCH(k_fl_p2g, gp, kFlThreads, 0, s, a);
+            AMG_LAUNCH(k_fl_forces, gp, kFlThreads, 0, s, a);
+            AMG_LAUNCH(k_fl_div, gg, 256, 0, s, a, (int)NAX, (int)NAY);
+            AMG_LAUNCH(k_fl_vel, gp, kFlThreads, 0, s, a);
+            AMG_LAUNCH(k_fl_div, gg, 256, 0, s, a, (int)NU, (int)NV);
+            AMG_LAUNCH(k_fl_advect, gl, 256, 0, s, a);
+        }
+        if (prof) prof->close(PROF_FLUID, s);
+    }
+    if (n) {
+        if (prof) prof->open(s);
+        AMG_LAUNCH(k_fl_scatter, gl, 256, 0, s, f->S, f->ids, n, f->P);
+        if (prof) prof->close(PROF_FLUID_MANAGE, s);
+    }
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
+}
+
+int fluid_step(FluidDev *f, uint64_t steps_left, double freedom_radius, cudaStream_t s, Prof *prof) {
+    return fluid_run(f, 1, steps_left, freedom_radius, s, prof);
 }
 
 }  // namespace amg

@@ -642,8 +642,7 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
     // solver steps (morph.cpp:1052-1054)
     const double freedom = std::sqrt((double)sc.width * sc.width + (double)sc.height * sc.height) *
                            fr_in.sparseness / 4.0;
-    for (uint32_t k = 0; k < fr_in.fluidsteps; ++k)
-        if ((rc = fluid_step(fl, fr_in.fluidsteps - (k + 1), freedom * (1.0 - fr.t), s, prof))) return rc;
+    if ((rc = fluid_run(fl, fr_in.fluidsteps, 0, freedom * (1.0 - fr.t), s, prof))) return rc;
     if (prof) prof->open(s);
     rc = fluid_draw(fl, m->acc, sc.width, sc.height, fr_in.sparseness, sc.bbox, fr.t, out, s);
     if (prof) prof->close(PROF_FLUID_DRAW, s);

@@ -241,6 +241,9 @@ void fluid_destroy(FluidDev *f);
 int fluid_set(FluidDev *f, const double *state, cudaStream_t s);  // n x 18 doubles (oracle order)
 int fluid_get(FluidDev *f, double *state, cudaStream_t s);
 int fluid_step(FluidDev *f, uint64_t steps_left, double freedom_radius, cudaStream_t s, Prof *prof);
+// nsteps steps; step k runs with steps_left = last_steps_left + (nsteps - 1 - k).
+int fluid_run(FluidDev *f, uint32_t nsteps, uint64_t last_steps_left, double freedom_radius, cudaStream_t s,
+              Prof *prof);
 
 // ---- k_fluid_morph.cu: the morph's fluid path (step_fluid + draw_fluid)
 struct FluidMorph;
