@@ -79,31 +79,54 @@ constexpr int kPrivNodes = 1024;   // nodes of a CTA's shared-memory patch
 // Patch of the CTA's 3x3 stencils (origins (cx, cy) of its active
 // particles): box = {x0, y0, width, height} in shared memory.  True when the
 // CTA has active particles and the patch fits kPrivNodes nodes (uniform).
-__device__ bool priv_box(bool act, int cx, int cy, int *box, int *red) {
+// The patch sums are 32-bit fixed point: `bound` is the largest magnitude
+// one particle adds to one node in one field, and *scale the largest power of
+// two (at most 2^24) at which the CTA's summed bounds stay below 2^31, so no
+// node sum can overflow; integer sums are exact and order-free.  *scale is 0
+// when that power would be below 2^12 (the patch then sums in FP32).
+__device__ bool priv_box(bool act, int cx, int cy, float bound, int *box, int *red, float *scale) {
     int mnx = act ? cx : INT_MAX, mny = act ? cy : INT_MAX, mxx = act ? cx : INT_MIN, mxy = act ? cy : INT_MIN;
+    float bsum = act ? bound : 0.f;
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
         mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
         mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
         mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+        bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
     }
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        red[4 * w] = mnx; red[4 * w + 1] = mny; red[4 * w + 2] = mxx; red[4 * w + 3] = mxy;
+        red[5 * w] = mnx; red[5 * w + 1] = mny; red[5 * w + 2] = mxx; red[5 * w + 3] = mxy;
+        red[5 * w + 4] = __float_as_int(bsum);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int k = 1; k < kFlThreads / 32; ++k) {
-            mnx = min(mnx, red[4 * k]); mny = min(mny, red[4 * k + 1]);
-            mxx = max(mxx, red[4 * k + 2]); mxy = max(mxy, red[4 * k + 3]);
+            mnx = min(mnx, red[5 * k]); mny = min(mny, red[5 * k + 1]);
+            mxx = max(mxx, red[5 * k + 2]); mxy = max(mxy, red[5 * k + 3]);
+            bsum += __int_as_float(red[5 * k + 4]);
         }
         box[0] = mnx; box[1] = mny;
         box[2] = mnx == INT_MAX ? 0 : mxx - mnx + 3;
         box[3] = mnx == INT_MAX ? 0 : mxy - mny + 3;
+        // each rounded term adds at most 1/2 more: keep 2^10 of headroom
+        int e = 24;
+        while (e >= 12 && !(bsum * ldexpf(1.f, e) <= 2147483648.f - 1024.f)) --e;
+        box[4] = e >= 12 ? e : 0;
     }
     __syncthreads();
+    *scale = box[4] ? ldexpf(1.f, box[4]) : 0.f;
     return box[2] > 0 && box[2] * box[3] <= kPrivNodes;
+}
+
+// One term of a patch sum: fixed point at `scale`, or FP32 when scale is 0.
+__device__ __forceinline__ void patch_add(float *acc, int q, float v, float scale) {
+    if (scale != 0.f) atomicAdd(reinterpret_cast<int *>(acc) + q, __float2int_rn(v * scale));
+    else atomicAdd(acc + q, v);
+}
+__device__ __forceinline__ float patch_get(const float *acc, int q, float scale) {
+    return scale != 0.f ? (float)reinterpret_cast<const int *>(acc)[q] / scale : acc[q];
 }
 
 #define FL(f, i) a.P[(size_t)(f) * a.n + (i)]
@@ -118,7 +141,7 @@ enum { QM, QGX, QGY, QW, QR, QG, QB, QA, kQ };
 
 __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
     __shared__ float acc[kQ * kPrivNodes];
-    __shared__ int box[4], red[4 * (kFlThreads / 32)];
+    __shared__ int box[5], red[5 * (kFlThreads / 32)];
     const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
     const uint8_t fl = p < a.n ? a.flags[p] : 0;
     const bool act = fl & 1;
@@ -130,7 +153,13 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
         str = FL(PSTR, p); r = FL(Pr, p); g = FL(Pg, p); b = FL(Pb, p); al = FL(Pa, p);
         colour = (fl & 2) && str > 0.f;
     }
-    if (!priv_box(act, s.cx, s.cy, box, red)) {
+    // per-node term bound: phi <= 0.5625, |gradient term| <= 1.5 x 0.75,
+    // colour terms str and str x colour
+    float bound = 1.125f;
+    if (colour)
+        bound = fmaxf(bound, fmaxf(fabsf(str), fabsf(str) * fmaxf(fmaxf(fabsf(r), fabsf(g)), fmaxf(fabsf(b), fabsf(al)))));
+    float scale;
+    if (!priv_box(act, s.cx, s.cy, bound, box, red, &scale)) {
         if (!act) return;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -163,21 +192,22 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
             for (int j = 0; j < 3; ++j) {
                 const int q = (s.cx + i - x0) * bh + (s.cy + j - y0);
                 const float phi = s.px[i] * s.py[j];
-                atomicAdd(&acc[QM * kPrivNodes + q], phi);
-                atomicAdd(&acc[QGX * kPrivNodes + q], s.gx[i] * s.py[j]);
-                atomicAdd(&acc[QGY * kPrivNodes + q], s.px[i] * s.gy[j]);
+                patch_add(acc, QM * kPrivNodes + q, phi, scale);
+                patch_add(acc, QGX * kPrivNodes + q, s.gx[i] * s.py[j], scale);
+                patch_add(acc, QGY * kPrivNodes + q, s.px[i] * s.gy[j], scale);
                 if (colour) {
-                    atomicAdd(&acc[QW * kPrivNodes + q], str);
-                    atomicAdd(&acc[QR * kPrivNodes + q], str * r);
-                    atomicAdd(&acc[QG * kPrivNodes + q], str * g);
-                    atomicAdd(&acc[QB * kPrivNodes + q], str * b);
-                    atomicAdd(&acc[QA * kPrivNodes + q], str * al);
+                    patch_add(acc, QW * kPrivNodes + q, str, scale);
+                    patch_add(acc, QR * kPrivNodes + q, str * r, scale);
+                    patch_add(acc, QG * kPrivNodes + q, str * g, scale);
+                    patch_add(acc, QB * kPrivNodes + q, str * b, scale);
+                    patch_add(acc, QA * kPrivNodes + q, str * al, scale);
                 }
             }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nn; q += kFlThreads) {
-        const float m = acc[QM * kPrivNodes + q], gx = acc[QGX * kPrivNodes + q], gy = acc[QGY * kPrivNodes + q];
+        const float m = patch_get(acc, QM * kPrivNodes + q, scale), gx = patch_get(acc, QGX * kPrivNodes + q, scale),
+                    gy = patch_get(acc, QGY * kPrivNodes + q, scale);
         const size_t n = node(a, x0 + q / bh, y0 + q % bh);
         if (m != 0.f || gx != 0.f || gy != 0.f) {
             atomicAdd(&ND_(NM, n), m);
@@ -185,13 +215,13 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
             atomicAdd(&ND_(NGX, n), gx);
             atomicAdd(&ND_(NGY, n), gy);
         }
-        const float w = acc[QW * kPrivNodes + q];
+        const float w = patch_get(acc, QW * kPrivNodes + q, scale);
         if (w != 0.f) {
             atomicAdd(&ND_(NW, n), w);
-            atomicAdd(&ND_(NR, n), acc[QR * kPrivNodes + q]);
-            atomicAdd(&ND_(NG, n), acc[QG * kPrivNodes + q]);
-            atomicAdd(&ND_(NB, n), acc[QB * kPrivNodes + q]);
-            atomicAdd(&ND_(NA, n), acc[QA * kPrivNodes + q]);
+            atomicAdd(&ND_(NR, n), patch_get(acc, QR * kPrivNodes + q, scale));
+            atomicAdd(&ND_(NG, n), patch_get(acc, QG * kPrivNodes + q, scale));
+            atomicAdd(&ND_(NB, n), patch_get(acc, QB * kPrivNodes + q, scale));
+            atomicAdd(&ND_(NA, n), patch_get(acc, QA * kPrivNodes + q, scale));
         }
     }
 }
@@ -203,7 +233,12 @@ struct Dep2 {
 };
 __device__ __forceinline__ void deposit2(const FlArgs &a, bool act, const Stencil &s, const Dep2 &d, int f1, int f2,
                                          float *acc, int *box, int *red) {
-    if (!priv_box(act, s.cx, s.cy, box, red)) {
+    float bound = 0.f;
+    if (act)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) bound = fmaxf(bound, fmaxf(fabsf(d.v1[k]), fabsf(d.v2[k])));
+    float scale;
+    if (!priv_box(act, s.cx, s.cy, bound, box, red, &scale)) {
         if (!act) return;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -227,13 +262,13 @@ __device__ __forceinline__ void deposit2(const FlArgs &a, bool act, const Stenci
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 const int q = (s.cx + i - x0) * bh + (s.cy + j - y0);
-                atomicAdd(&acc[q], d.v1[3 * i + j]);
-                atomicAdd(&acc[kPrivNodes + q], d.v2[3 * i + j]);
+                patch_add(acc, q, d.v1[3 * i + j], scale);
+                patch_add(acc, kPrivNodes + q, d.v2[3 * i + j], scale);
             }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nn; q += kFlThreads) {
-        const float u = acc[q], v = acc[kPrivNodes + q];
+        const float u = patch_get(acc, q, scale), v = patch_get(acc, kPrivNodes + q, scale);
         if (u != 0.f || v != 0.f) {
             const size_t n = node(a, x0 + q / bh, y0 + q % bh);
             atomicAdd(&ND_(f1, n), u);
@@ -244,7 +279,7 @@ __device__ __forceinline__ void deposit2(const FlArgs &a, bool act, const Stenci
 
 __global__ void __launch_bounds__(kFlThreads) k_fl_forces(FlArgs a) {
     __shared__ float acc[2 * kPrivNodes];
-    __shared__ int box[4], red[4 * (kFlThreads / 32)];
+    __shared__ int box[5], red[5 * (kFlThreads / 32)];
     const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
     const bool act = p < a.n && (a.flags[p] & 1);
     Stencil s{};
@@ -317,7 +352,7 @@ __device__ __forceinline__ void pull(float x1, float y1, float x2, float y2, flo
 
 __global__ void __launch_bounds__(kFlThreads) k_fl_vel(FlArgs a) {
     __shared__ float acc[2 * kPrivNodes];
-    __shared__ int box[4], red[4 * (kFlThreads / 32)];
+    __shared__ int box[5], red[5 * (kFlThreads / 32)];
     const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
     const uint8_t fl = p < a.n ? a.flags[p] : 0;
     const bool act = fl & 1;

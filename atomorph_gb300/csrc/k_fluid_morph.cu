@@ -98,6 +98,20 @@ struct FmArgs {
 
 #define PF_(k, i) a.PF[(size_t)(k) * a.N + (i)]
 
+// Adds 1 to cnt[key] for the calling lane and returns its previous value as
+// if the lanes had added one at a time; the converged lanes naming the same
+// counter make one atomic (every particle of a one-chain morph names the
+// same per-chain counter).
+__device__ __forceinline__ uint32_t agg_add1(uint32_t *cnt, uint32_t key) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, key);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&cnt[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 __global__ void k_fm_classify(FmArgs a) {
     for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < a.N; x += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t p1 = a.P[(uint64_t)a.y * a.N + x], p2 = a.P[(uint64_t)a.yn * a.N + x];
@@ -105,7 +119,7 @@ __global__ void k_fm_classify(FmArgs a) {
         if (pt_fluid(p2)) atomicMax(&a.m.dst_map[pt_pos(p2, a.cw)], (int32_t)x);
         uint8_t fl = a.flags[x];
         if ((fl & 1u) && a.m.frame_key[x] == a.f) {
-            atomicAdd(&a.m.chain_cnt[a.chain_id[x]], 1u);
+            agg_add1(a.m.chain_cnt, a.chain_id[x]);
             const uint32_t sp = a.m.src_pos[x], dp = a.m.dst_pos[x];
             if (sp < a.cw * a.ch) {
                 atomicAdd(&a.m.src_cnt[sp], 1u);
@@ -225,7 +239,7 @@ __global__ void k_fm_assign1(FmArgs a, const uint32_t *__restrict__ raw) {
         a.flags[s] = 1u;  // active, not mature: starts at its attractor (k_fm_update)
         atomicAdd(&a.m.dst_cnt[dq], 1u);
         atomicAdd(&a.m.src_cnt[q], 1u);
-        atomicAdd(&a.m.phase1[c], 1u);
+        agg_add1(a.m.phase1, c);
     }
 }
 
@@ -238,7 +252,7 @@ __global__ void k_fm_dst_cands(FmArgs a) {
         if (!pt_fluid(p2)) continue;
         const uint32_t q = pt_pos(p2, a.cw);
         if (a.m.dst_map[q] != (int32_t)x || a.m.dst_cnt[q] != 0) continue;
-        const uint32_t k = atomicAdd(a.m.ncand, 1u);
+        const uint32_t k = agg_add1(a.m.ncand, 0u);
         a.m.ckeys[k] = q;
         a.m.cvals[k] = (uint32_t)x;
     }

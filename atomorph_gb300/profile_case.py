@@ -4,7 +4,7 @@ workload: the program per-kernel profiler captures are taken on.
     python -m atomorph_gb300.profile_case [--workload shapes1024] [--frames 3]
 
 After the pipeline (components, blob matching, chain construction) it runs
-4 plain sweeps, 4 guided sweeps, a recorded guided sweep, one training epoch
+4 plain sweeps, 4 guided sweeps, 2 recorded sweeps, one training epoch
 and 4 gated (learned) sweeps, the allocation-free cost, `--frames` atom
 frames, 2 fluid frames with 2 solver steps each on a (0.5 W + 20)^2 grid,
 and one batched refinement of 4 small jobs.  Settings match bench.py's
@@ -31,12 +31,13 @@ def run(workload: str, frames: int) -> dict:
     m.tune(guided_switch=0)
     m.refine(4, capi.PROPOSAL_LOCAL)
     m.tune(learned_adaptive=0)
-    m.record_swaps(1 << 22)
-    m.refine(1, capi.PROPOSAL_LOCAL)
+    m.record_swaps(1 << 22)  # recording sweeps run the learned form's gate with every region kept
+    m.refine(2, capi.PROPOSAL_LEARNED)
     f, y = m.recorded_swaps(1 << 22)
     m.record_swaps(0)
-    if len(y):
-        m.train_proposal(f, y, epochs=1, lr=2e-3)
+    if not len(y):
+        raise RuntimeError("no recorded samples")
+    m.train_proposal(f, y, epochs=1, lr=2e-3)
     m.refine(4, capi.PROPOSAL_LEARNED)
     v = C.c_uint64()
     rc = m.lib.am_get_cost_noalloc(m.h, C.byref(v))

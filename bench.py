@@ -50,6 +50,21 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
+    dram__bytes_write.sum) from the committed per-kernel ncu summary of the
+    same workload, or None."""
+    path = os.path.join(ROOT, "profiles", "kernels_shapes1024_profile_case.md")
+    try:
+        for line in open(path):
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cells) >= 6 and cells[0] == f"`{kernel}`":
+                return int(float(cells[5]) * 1e6)
+    except OSError:
+        pass
+    return None
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -216,7 +231,8 @@ def bench_ours(args, rank, world):
     }.get(dom_name, frame_bytes)
     achieved = kernel_bytes / (dom_avg_ms / 1e3) / 1e9
     roof = {"kernel": dom_name, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "peak_kind": peak_kind, "traffic": None,
+            "frac": round(achieved / hbm, 4), "peak_kind": peak_kind, "traffic": _profiled_traffic(dom_name),
+            "traffic_source": "profiles/kernels_shapes1024_profile_case.md (ncu, cold cache, bytes per launch)",
             "algorithmic_bytes_per_launch": int(kernel_bytes), "avg_launch_ms": round(dom_avg_ms, 5),
             "frame": {"algorithmic_bytes": int(frame_bytes), "profiled_ms": round(frame_ms_profiled, 5),
                       "achieved_gbs": round(frame_bytes / (frame_ms_profiled / 1e3) / 1e9, 1),
