@@ -108,6 +108,8 @@ _SIGS = {
     "am_fluid_steps": (C.c_int, [vp, C.c_size_t, C.c_double]),
     "am_fluid_stream": (vp, [vp]),
     "am_fluid_render": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_double, C.POINTER(C.c_uint32), C.c_double, u8p]),
+    "am_fluid_render_ex": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_double, C.POINTER(C.c_uint32), C.c_double,
+                                     C.c_size_t, u8p, u8p]),
     "am_set_fluid_sparseness": (C.c_int, [vp, C.c_double]),
     "am_get_fluid_particles": (C.c_size_t, [vp, f64p, C.c_size_t]),
     "am_set_tuning": (C.c_int, [vp, C.c_char_p, C.c_double]),
@@ -459,6 +461,16 @@ class Fluid:
         out = np.zeros((height, width, 4), np.uint8)
         bb = (C.c_uint32 * 4)(*[int(v) for v in bbox])
         _check(self.lib.am_fluid_render(self.h, width, height, sparseness, bb, t, _p(out, u8p)), "am_fluid_render")
+        return out
+
+    def render_ex(self, width: int, height: int, sparseness: float, bbox, t: float, feather: int = 0,
+                  background: np.ndarray | None = None) -> np.ndarray:
+        """draw_fluid with feather layers and keep_background over `background`."""
+        out = np.zeros((height, width, 4), np.uint8)
+        bb = (C.c_uint32 * 4)(*[int(v) for v in bbox])
+        bg = None if background is None else np.ascontiguousarray(background, np.uint8)
+        _check(self.lib.am_fluid_render_ex(self.h, width, height, sparseness, bb, t, feather,
+                                           None if bg is None else _p(bg, u8p), _p(out, u8p)), "am_fluid_render_ex")
         return out
 
 

@@ -76,21 +76,19 @@ int am_set_threads(am_morph *m, size_t t) { CHECK(m); H(m).front.threads = t; re
 int am_set_cycle_length(am_morph *m, size_t c) { CHECK(m); H(m).front.cycle_length = c; return AM_OK; }
 int am_set_feather(am_morph *m, size_t f) {
     CHECK(m);
-    if (f != 0) { amg::set_error("feather > 0 is not implemented on the GPU path"); return AM_ERR_UNSUPPORTED; }
+    if (f > amg::kMaxFeather) { amg::set_error("feather above 96 pixels is not supported"); return AM_ERR_UNSUPPORTED; }
     H(m).front.feather = f;
     return AM_OK;
 }
 int am_set_keep_background(am_morph *m, int k) {
     CHECK(m);
-    if (k) { amg::set_error("keep_background is not implemented on the GPU path"); return AM_ERR_UNSUPPORTED; }
-    H(m).front.keep_background = false;
+    H(m).front.keep_background = k != 0;
     return AM_OK;
 }
 int am_set_finite(am_morph *m, int f) { CHECK(m); H(m).front.finite = f != 0; return AM_OK; }
 int am_set_show_blobs(am_morph *m, unsigned b) {
     CHECK(m);
-    if (b != AM_TEXTURE) { amg::set_error("only TEXTURE blobs are implemented on the GPU path"); return AM_ERR_UNSUPPORTED; }
-    H(m).front.show_blobs = b;
+    H(m).front.show_blobs = b;  // values other than AVERAGE / DISTINCT draw TEXTURE, as in the reference
     return AM_OK;
 }
 // morph::set_fluid / set_density (morph.cpp:1553-1570): fluid forces density 1
@@ -255,6 +253,15 @@ double am_get_time(const am_morph *m, size_t i, size_t n) {
     }
     return double(i) / double(n);
 }
+// round(255 x mean) of a stored colour, converted HSP -> RGB when the blob
+// delimiter is HSP (morph.cpp:344-351, 366-373).
+static void store_rgba(const amg::Engine &e, double r, double g, double b, double a, uint8_t *rgba) {
+    auto cc = [](double v) { return (uint32_t)(int)std::round(255.0 * v) & 255u; };
+    uint32_t c = cc(r) | (cc(g) << 8) | (cc(b) << 16) | (cc(a) << 24);
+    if (e.front.delimiter == AM_HSP) c = amg::hsp_to_rgb_host(c);
+    for (int k = 0; k < 4; ++k) rgba[k] = (uint8_t)(c >> (8 * k));
+}
+
 int am_get_average_pixel(const am_morph *m, size_t frame, uint16_t *xy, uint8_t *rgba) {
     if (!m) return AM_ERR_ARG;
     auto it = m->e.frames.find(frame);
@@ -266,8 +273,7 @@ int am_get_average_pixel(const am_morph *m, size_t frame, uint16_t *xy, uint8_t 
         if (i >= 0 && (size_t)i < m->e.f_blobs.size())
             for (auto &bl : m->e.f_blobs[i]) { r += bl.r * bl.size; g += bl.g * bl.size; b += bl.b * bl.size; a += bl.a * bl.size; n += bl.size; }
         if (n > 0) { r /= n; g /= n; b /= n; a /= n; }
-        rgba[0] = (uint8_t)std::round(255.0 * r); rgba[1] = (uint8_t)std::round(255.0 * g);
-        rgba[2] = (uint8_t)std::round(255.0 * b); rgba[3] = (uint8_t)std::round(255.0 * a);
+        store_rgba(m->e, r, g, b, a, rgba);
     }
     return AM_OK;
 }
@@ -277,10 +283,7 @@ int am_get_blob_average(const am_morph *m, size_t frame, size_t blob, uint16_t *
     if (i < 0 || (size_t)i >= m->e.f_blobs.size() || blob >= m->e.f_blobs[i].size()) return AM_ERR_NOT_FOUND;
     const amg::Blob &b = m->e.f_blobs[i][blob];
     if (xy) { xy[0] = (uint16_t)std::round(b.x); xy[1] = (uint16_t)std::round(b.y); }
-    if (rgba) {
-        rgba[0] = (uint8_t)std::round(255.0 * b.r); rgba[1] = (uint8_t)std::round(255.0 * b.g);
-        rgba[2] = (uint8_t)std::round(255.0 * b.b); rgba[3] = (uint8_t)std::round(255.0 * b.a);
-    }
+    if (rgba) store_rgba(m->e, b.r, b.g, b.b, b.a, rgba);
     return AM_OK;
 }
 size_t am_get_atom_count(const am_morph *m) { return m ? (size_t)m->e.fN : 0; }

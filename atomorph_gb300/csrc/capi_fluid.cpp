@@ -65,19 +65,31 @@ int am_fluid_steps(am_fluid *h, size_t n, double freedom_radius) {
 
 void *am_fluid_stream(am_fluid *h) { return h ? (void *)h->s : nullptr; }
 
-int am_fluid_render(am_fluid *h, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox, double t,
-                    uint8_t *rgba_out) {
+int am_fluid_render_ex(am_fluid *h, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
+                       double t, size_t feather, const uint8_t *background, uint8_t *rgba_out) {
     if (!h || !bbox || !rgba_out || !width || !height || !(sparseness > 0.0)) return AM_ERR_ARG;
-    uint8_t *d = nullptr;
+    if (feather > amg::kMaxFeather) return AM_ERR_UNSUPPORTED;
+    uint8_t *d = nullptr, *bg = nullptr;
     const size_t bytes = (size_t)width * height * 4;
-    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    if (cudaMalloc(&d, bytes) != cudaSuccess || (background && cudaMalloc(&bg, bytes) != cudaSuccess)) {
+        cudaFree(d);
         amg::set_error("cudaMalloc failed");
         return AM_ERR_NOMEM;
     }
-    int rc = amg::fluid_render_only(h->f, width, height, sparseness, bbox, t, d, h->s);
+    int rc = AM_OK;
+    if (bg && cudaMemcpy(bg, background, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = AM_ERR_CUDA;
+    if (!rc)
+        rc = amg::fluid_render_only(h->f, width, height, sparseness, bbox, t, (uint32_t)feather,
+                                    reinterpret_cast<const uint32_t *>(bg), d, h->s);
     if (!rc && cudaMemcpy(rgba_out, d, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = AM_ERR_CUDA;
     cudaFree(d);
+    cudaFree(bg);
     return rc;
+}
+
+int am_fluid_render(am_fluid *h, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox, double t,
+                    uint8_t *rgba_out) {
+    return am_fluid_render_ex(h, width, height, sparseness, bbox, t, 0, nullptr, rgba_out);
 }
 
 }  // extern "C"

@@ -712,6 +712,30 @@ int Engine::publish_front() {
         AMG_CUDA(cudaMemcpyAsync(d_Pf.p, d_P.p, N * K * 8, cudaMemcpyDeviceToDevice, stream));
         AMG_CUDA(cudaMemcpyAsync(d_chain_off_f.p, chain_off.data(), (C + 1) * 8, cudaMemcpyHostToDevice, stream));
         AMG_CUDA(cudaMemcpyAsync(d_rank_f.p, f_rank.data(), f_rank.size() * 4, cudaMemcpyHostToDevice, stream));
+        // show_blobs colours by blob (morph.cpp:1321-1334): AVERAGE is
+        // blob2pixel (create_color of the blob's mean, HSP -> RGB when the
+        // delimiter is HSP, morph.cpp:1423-1429); DISTINCT draws three bytes
+        // from std::mt19937(group) as the reference does.
+        const size_t kc = (size_t)K * C;
+        std::vector<uint32_t> col(3 * kc, 0);
+        auto cc = [](double v) { return (uint32_t)(int)std::round(v * 255.0) & 255u; };
+        for (uint32_t k = 0; k < K; ++k)
+            for (uint32_t g = 0; g < C; ++g) {
+                const uint32_t b = (uint32_t)f_rank[(size_t)k * C + g];
+                if (b >= C) continue;
+                if (k < f_blobs.size() && b < f_blobs[k].size()) {
+                    const Blob &bl = f_blobs[k][b];
+                    const uint32_t st = cc(bl.r) | (cc(bl.g) << 8) | (cc(bl.b) << 16) | (cc(bl.a) << 24);
+                    col[(size_t)k * C + b] = st;
+                    col[kc + (size_t)k * C + b] = hsp_to_rgb_host(st);
+                }
+                std::mt19937 gen(g);
+                std::uniform_int_distribution<unsigned char> byte(0, 255);
+                const uint32_t r = byte(gen), gg = byte(gen), bb = byte(gen);
+                col[2 * kc + (size_t)k * C + b] = r | (gg << 8) | (bb << 16) | 0xFF000000u;
+            }
+        if ((rc = d_blob_col.reserve(std::max<size_t>(col.size(), 1)))) return rc;
+        AMG_CUDA(cudaMemcpyAsync(d_blob_col.p, col.data(), col.size() * 4, cudaMemcpyHostToDevice, stream));
         AMG_CUDA(cudaStreamSynchronize(stream));
     }
     if (rw) render_invalidate(rw);
@@ -777,6 +801,7 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         sc.bbox[0] = bbox_x1; sc.bbox[1] = bbox_y1; sc.bbox[2] = bbox_x2; sc.bbox[3] = bbox_y2;
         sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
         sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
+        render_options(sc);
         size_t f = (size_t)(t * fK);
         uint64_t key = f < f_keys.size() ? f_keys[f] : 0;
         rc = render_frame(rw, sc, t, key, dst, rstream);
@@ -791,6 +816,23 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         AMG_CUDA(cudaGetLastError());
     }
     return AM_OK;
+}
+
+// Render options of the front settings (feather, keep_background,
+// show_blobs) and the tables they read.
+void Engine::render_options(RenderScene &sc) const {
+    sc.feather = (uint32_t)std::min<size_t>(front.feather, kMaxFeather);
+    sc.keep_background = front.keep_background ? 1u : 0u;
+    sc.show_blobs = front.show_blobs;
+    sc.present = d_present.p;
+    sc.perm = render_perm(rw);
+    const size_t kc = (size_t)fK * fC;
+    sc.blob_col = nullptr;
+    if (d_blob_col.p && front.show_blobs == AM_AVERAGE)
+        sc.blob_col = d_blob_col.p + (front.delimiter == AM_HSP ? kc : 0);
+    else if (d_blob_col.p && front.show_blobs == AM_DISTINCT)
+        sc.blob_col = d_blob_col.p + 2 * kc;
+    if (!sc.blob_col) sc.show_blobs = AM_TEXTURE;
 }
 
 // The fluid frame (morph::get_pixels with fluid steps, morph.cpp:1417): the
@@ -831,6 +873,7 @@ int Engine::render_fluid(double t, uint8_t *dst) {
     fr.sc.bbox[0] = bbox_x1; fr.sc.bbox[1] = bbox_y1; fr.sc.bbox[2] = bbox_x2; fr.sc.bbox[3] = bbox_y2;
     fr.sc.motion = front.motion; fr.sc.fading = front.fading; fr.sc.density = front.density;
     fr.sc.P = d_Pf.p; fr.sc.chain_off = d_chain_off_f.p; fr.sc.display = d_display.p; fr.sc.rank = d_rank_f.p;
+    render_options(fr.sc);
     const size_t f = std::min<size_t>((size_t)(t * fK), fK - 1);
     fr.time = t;
     fr.frame_key = f < f_keys.size() ? f_keys[f] : f;

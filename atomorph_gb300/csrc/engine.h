@@ -155,6 +155,9 @@ class Engine {
     DBuf<int32_t> d_labels;
     DBuf<uint64_t> d_P, d_Pf, d_chain_off, d_pair_off, d_chain_off_f, d_singles;
     DBuf<int32_t> d_rank_f;
+    // [3][K][C] draw colours of the b-th blob of key frame k for show_blobs:
+    // AVERAGE as stored, AVERAGE converted HSP -> RGB, DISTINCT
+    DBuf<uint32_t> d_blob_col;
     DBuf<uint32_t> d_phase;
     DBuf<unsigned long long> d_acc;        // [0] gain, [1] accepted, [2] cost
     DBuf<unsigned long long> d_stats;
@@ -185,6 +188,7 @@ class Engine {
     DBuf<uint32_t> d_fchain_id, d_surf;
     std::vector<uint32_t> surf_host;
     int render_fluid(double t, uint8_t *dst);
+    void render_options(RenderScene &sc) const;
     BlobWork *bw = nullptr;
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_n = 0;

@@ -13,7 +13,7 @@ namespace {
 
 constexpr double kPr = 0.299, kPg = 0.587, kPb = 0.114;
 
-__device__ void rgb2hsp(double R, double G, double B, double *H, double *S, double *P) {
+__host__ __device__ void rgb2hsp(double R, double G, double B, double *H, double *S, double *P) {
     *P = sqrt(R * R * kPr + G * G * kPg + B * B * kPb);
     if (R == G && R == B) { *H = 0.; *S = 0.; return; }
     if (R >= G && R >= B) {
@@ -28,7 +28,7 @@ __device__ void rgb2hsp(double R, double G, double B, double *H, double *S, doub
     }
 }
 
-__device__ void hsp2rgb(double H, double S, double P, double *R, double *G, double *B) {
+__host__ __device__ void hsp2rgb(double H, double S, double P, double *R, double *G, double *B) {
     double part, mom = 1. - S;
     if (mom > 0.) {
         if (H < 1. / 6.) {
@@ -62,14 +62,14 @@ __device__ void hsp2rgb(double H, double S, double P, double *R, double *G, doub
 
 // Round-half-away-from-zero of a non-negative double to a byte, as
 // std::round followed by the implicit conversion to uint8_t.
-__device__ __forceinline__ uint32_t rbyte(double v) { return (uint32_t)(int)round(v) & 0xFFu; }
+__host__ __device__ __forceinline__ uint32_t rbyte(double v) { return (uint32_t)(int)round(v) & 0xFFu; }
 
-__device__ uint32_t to_hsp(uint32_t c) {
+__host__ __device__ uint32_t to_hsp(uint32_t c) {
     double h, s, p;
     rgb2hsp((c & 0xFF) / 255.0, ((c >> 8) & 0xFF) / 255.0, ((c >> 16) & 0xFF) / 255.0, &h, &s, &p);
     return rbyte(h * 255.0) | (rbyte(s * 255.0) << 8) | (rbyte(p * 255.0) << 16) | (c & 0xFF000000u);
 }
-__device__ uint32_t to_rgb(uint32_t c) {
+__host__ __device__ uint32_t to_rgb(uint32_t c) {
     double r, g, b;
     hsp2rgb((c & 0xFF) / 255.0, ((c >> 8) & 0xFF) / 255.0, ((c >> 16) & 0xFF) / 255.0, &r, &g, &b);
     return rbyte(fmin(round(r * 255.0), 255.0)) | (rbyte(fmin(round(g * 255.0), 255.0)) << 8) |
@@ -96,6 +96,8 @@ __global__ void k_hsp_probe(const uint32_t *in, uint32_t *out, size_t n, int dir
 }
 
 }  // namespace
+
+uint32_t hsp_to_rgb_host(uint32_t c) { return to_rgb(c); }
 
 int launch_colour(const uint32_t *raw, const uint8_t *present, uint32_t *stored, uint32_t *display, size_t n,
                   int display_hsp, cudaStream_t s) {

@@ -66,7 +66,19 @@ struct FluidMorph {
     uint32_t *to_create = nullptr, *to_delete = nullptr, *phase1 = nullptr;  // [C]
     uint32_t *ncand = nullptr;       // phase 2 candidates
     unsigned long long *acc = nullptr;  // [5][out_w*out_h] W, R, G, B, A sums
+    uint32_t *col[2] = {nullptr, nullptr};  // [out_w*out_h] fluid colours (feather / background passes)
+    uint8_t *mem[2] = {nullptr, nullptr};   // [out_w*out_h] 1 where the fluid image has the pixel
     uint64_t frames = 0;             // frames stepped (random key)
+};
+
+// draw_fluid options: feather layers, keep_background (the background from
+// the key frames, or a given image), scratch for the passes.
+struct FluidDrawOpts {
+    uint32_t feather = 0, keep_bg = 0;
+    BgArgs bg{};
+    const uint32_t *bg_img = nullptr;
+    uint32_t *col[2] = {nullptr, nullptr};
+    uint8_t *mem[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -459,6 +471,81 @@ __global__ void k_fm_resolve(const unsigned long long *__restrict__ acc, size_t 
     }
 }
 
+// draw_fluid's per-pixel colour (morph.cpp:1160-1201) with membership; with
+// keep_background the alpha fades by afade = 1 - t^24 and truncates, as
+// create_pixel converts the faded double.
+__global__ void k_fm_means(const unsigned long long *__restrict__ acc, size_t npx, double afade, uint32_t *col,
+                           uint8_t *mem) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < npx; q += (size_t)gridDim.x * blockDim.x) {
+        const unsigned long long W = acc[q];
+        uint32_t o = 0;
+        if (W) {
+            uint32_t a = rdiv64(acc[4 * npx + q], W);
+            if (afade != 1.0) a = (uint32_t)(int)__dmul_rn((double)a, afade);
+            o = rdiv64(acc[npx + q], W) | (rdiv64(acc[2 * npx + q], W) << 8) | (rdiv64(acc[3 * npx + q], W) << 16) |
+                (a << 24);
+        }
+        col[q] = o;
+        mem[q] = W ? 1 : 0;
+    }
+}
+
+// One outward feather layer of the fluid image (morph.cpp:1204-1251): a
+// pixel outside the image with members among its 4 neighbours joins it with
+// their mean colour (summed in the reference's position order: up, left,
+// right, down), alpha scaled by `alpha`, create_color rounding.
+__global__ void k_fm_dilate(const uint32_t *__restrict__ col, const uint8_t *__restrict__ mem, uint32_t width,
+                            uint32_t height, double alpha, uint32_t *col2, uint8_t *mem2) {
+    const size_t npx = (size_t)width * height;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < npx; q += (size_t)gridDim.x * blockDim.x) {
+        if (mem[q]) {
+            col2[q] = col[q];
+            mem2[q] = 1;
+            continue;
+        }
+        const uint32_t x = (uint32_t)(q % width), y = (uint32_t)(q / width);
+        size_t nb[4];
+        int w = 0;
+        if (y > 0 && mem[q - width]) nb[w++] = q - width;
+        if (x > 0 && mem[q - 1]) nb[w++] = q - 1;
+        if (x + 1 < width && mem[q + 1]) nb[w++] = q + 1;
+        if (y + 1 < height && mem[q + width]) nb[w++] = q + width;
+        if (!w) {
+            col2[q] = 0u;
+            mem2[q] = 0;
+            continue;
+        }
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int k = 0; k < w; ++k) {
+            const uint32_t c = col[nb[k]];
+            for (int ch = 0; ch < 4; ++ch)
+                v[ch] = __dadd_rn(v[ch], __ddiv_rn(__ddiv_rn((double)((c >> (8 * ch)) & 255u), 255.0), (double)w));
+        }
+        v[3] = __dmul_rn(v[3], alpha);
+        uint32_t o = 0;
+        for (int ch = 0; ch < 4; ++ch) o |= ((uint32_t)(int)round(__dmul_rn(v[ch], 255.0)) & 255u) << (8 * ch);
+        col2[q] = o;
+        mem2[q] = 1;
+    }
+}
+
+// The fluid image into the frame (morph.cpp:1268-1299): over the background
+// with keep_background (bg_img, or the key frames' cross-fade), else as is
+// with transparent black elsewhere.
+__global__ void k_fm_final(const uint32_t *__restrict__ col, const uint8_t *__restrict__ mem, uint32_t width,
+                           uint32_t height, uint32_t keep_bg, BgArgs bg, const uint32_t *__restrict__ bg_img,
+                           uint32_t *out) {
+    const size_t npx = (size_t)width * height;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < npx; q += (size_t)gridDim.x * blockDim.x) {
+        if (!keep_bg) {
+            out[q] = mem[q] ? col[q] : 0u;
+            continue;
+        }
+        const uint32_t b = bg_img ? bg_img[q] : bg_colour(bg, (uint32_t)(q % width), (uint32_t)(q / width));
+        out[q] = over_background(mem[q] ? 1 : 0, col[q], nullptr, b);
+    }
+}
+
 int grow(void **p, size_t bytes, size_t *cap) {
     if (bytes <= *cap) return AM_OK;
     if (*p) cudaFree(*p);
@@ -477,14 +564,15 @@ void fluid_morph_destroy(FluidMorph *m) {
     if (!m) return;
     void *ps[] = {m->frame_key, m->src_pos, m->dst_pos, m->owner, m->src_map, m->dst_map, m->src_cnt, m->dst_cnt,
                   m->src_any, m->flags_a, m->flags_b, m->slot_by_rank, m->ckeys, m->cvals, m->tk, m->tv, m->hist,
-                  m->chain_cnt, m->to_create, m->to_delete, m->phase1, m->ncand, m->acc};
+                  m->chain_cnt, m->to_create, m->to_delete, m->phase1, m->ncand, m->acc, m->col[0], m->col[1],
+                  m->mem[0], m->mem[1]};
     for (void *p : ps)
         if (p) cudaFree(p);
     delete m;
 }
 
 int fluid_draw(FluidDev *fl, unsigned long long *acc, uint32_t width, uint32_t height, double sparseness,
-               const uint32_t *bbox, double t, uint8_t *out, cudaStream_t s) {
+               const uint32_t *bbox, double t, uint8_t *out, cudaStream_t s, const FluidDrawOpts &o) {
     const size_t npx = (size_t)width * height;
     if (!npx) return AM_OK;
     AMG_CUDA(cudaMemsetAsync(acc, 0, 5 * npx * sizeof(unsigned long long), s));
@@ -497,18 +585,45 @@ int fluid_draw(FluidDev *fl, unsigned long long *acc, uint32_t width, uint32_t h
         AMG_LAUNCH(k_fm_splat, g, 256, 0, s, a);
     }
     unsigned g2 = (unsigned)std::min<size_t>((npx + 255) / 256, (size_t)kSMs * 8);
-    AMG_LAUNCH(k_fm_resolve, g2, 256, 0, s, acc, npx, (uint32_t *)out);
+    if (!o.feather && !o.keep_bg) {
+        AMG_LAUNCH(k_fm_resolve, g2, 256, 0, s, acc, npx, (uint32_t *)out);
+    } else {
+        const double afade = o.keep_bg ? 1.0 - std::pow(t, 24.0) : 1.0;
+        AMG_LAUNCH(k_fm_means, g2, 256, 0, s, acc, npx, afade, o.col[0], o.mem[0]);
+        int cur = 0;
+        for (uint32_t layer = 0; layer < o.feather; ++layer) {
+            const double alpha = 1.0 - (double(layer + 1) / double(o.feather + 1));
+            AMG_LAUNCH(k_fm_dilate, g2, 256, 0, s, o.col[cur], o.mem[cur], width, height, alpha, o.col[cur ^ 1],
+                       o.mem[cur ^ 1]);
+            cur ^= 1;
+        }
+        AMG_LAUNCH(k_fm_final, g2, 256, 0, s, o.col[cur], o.mem[cur], width, height, o.keep_bg, o.bg, o.bg_img,
+                   (uint32_t *)out);
+    }
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }
 
 int fluid_render_only(FluidDev *fl, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
-                      double t, uint8_t *out, cudaStream_t s) {
+                      double t, uint32_t feather, const uint32_t *bg_img, uint8_t *out, cudaStream_t s) {
+    const size_t npx = std::max<size_t>((size_t)width * height, 1);
     unsigned long long *acc = nullptr;
-    AMG_CUDA(cudaMalloc(&acc, 5 * std::max<size_t>((size_t)width * height, 1) * sizeof(unsigned long long)));
-    int rc = fluid_draw(fl, acc, width, height, sparseness, bbox, t, out, s);
+    uint32_t *col = nullptr;
+    uint8_t *mem = nullptr;
+    if (cudaMalloc(&acc, 5 * npx * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&col, 2 * npx * 4) != cudaSuccess || cudaMalloc(&mem, 2 * npx) != cudaSuccess) {
+        cudaFree(acc); cudaFree(col); cudaFree(mem);
+        set_error("fluid draw: out of device memory");
+        return AM_ERR_NOMEM;
+    }
+    FluidDrawOpts o;
+    o.feather = feather;
+    o.keep_bg = bg_img ? 1u : 0u;
+    o.bg_img = bg_img;
+    o.col[0] = col; o.col[1] = col + npx; o.mem[0] = mem; o.mem[1] = mem + npx;
+    int rc = fluid_draw(fl, acc, width, height, sparseness, bbox, t, out, s, o);
     cudaError_t e = cudaStreamSynchronize(s);
-    cudaFree(acc);
+    cudaFree(acc); cudaFree(col); cudaFree(mem);
     if (rc) return rc;
     AMG_CUDA(e);
     return AM_OK;
@@ -569,7 +684,8 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
                   {(void **)&m->tk, N * 4}, {(void **)&m->tv, N * 4}, {(void **)&m->hist, radix_hist_words(N) * 4},
                   {(void **)&m->chain_cnt, (size_t)sc.C * 4}, {(void **)&m->to_create, (size_t)sc.C * 4},
                   {(void **)&m->to_delete, (size_t)sc.C * 4}, {(void **)&m->phase1, (size_t)sc.C * 4},
-                  {(void **)&m->ncand, 4}, {(void **)&m->acc, npx * 40}};
+                  {(void **)&m->ncand, 4}, {(void **)&m->acc, npx * 40}, {(void **)&m->col[0], npx * 4},
+                  {(void **)&m->col[1], npx * 4}, {(void **)&m->mem[0], npx}, {(void **)&m->mem[1], npx}};
         bool fresh = m->n != N || m->C != sc.C || m->cw != sc.CW || m->ch != sc.CH || m->out_w != sc.width ||
                      m->out_h != sc.height;
         if (fresh) {
@@ -658,7 +774,12 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
                            fr_in.sparseness / 4.0;
     if ((rc = fluid_run(fl, fr_in.fluidsteps, 0, freedom * (1.0 - fr.t), s, prof))) return rc;
     if (prof) prof->open(s);
-    rc = fluid_draw(fl, m->acc, sc.width, sc.height, fr_in.sparseness, sc.bbox, fr.t, out, s);
+    FluidDrawOpts dopt;
+    dopt.feather = std::min<uint32_t>(sc.feather, kMaxFeather);
+    dopt.keep_bg = sc.keep_background && sc.present ? 1u : 0u;
+    dopt.bg = bg_args(sc, fr.f, fr.t);
+    dopt.col[0] = m->col[0]; dopt.col[1] = m->col[1]; dopt.mem[0] = m->mem[0]; dopt.mem[1] = m->mem[1];
+    rc = fluid_draw(fl, m->acc, sc.width, sc.height, fr_in.sparseness, sc.bbox, fr.t, out, s, dopt);
     if (prof) prof->close(PROF_FLUID_DRAW, s);
     return rc;
 }

@@ -682,10 +682,89 @@ __device__ __noinline__ uint32_t over_bytes(const double *st) {
     return o;
 }
 
+// Render options the resolve applies (morph.cpp:1313-1399, 625-674).
+struct ResolveOpts {
+    uint32_t show_blobs;           // AM_TEXTURE, or AM_AVERAGE / AM_DISTINCT with rank_col
+    uint32_t feather;              // TEXTURE blobs: outer layers faded
+    uint32_t keep_bg;
+    const uint32_t *rank_col;      // [C] colour of the rank-b blob of the pair's first key frame
+    uint32_t tiles_y;
+    BgArgs bg;                     // the background under the composite
+};
+
+// Feather layers of the tile's pixels in the rank-`cur` blob (morph.cpp:
+// 625-674): layer[li] = min(feather, d - 1), d the city-block distance to
+// the nearest pixel outside the blob (iterated 4-neighbour erosion peels one
+// layer per step).  Membership (any valid corner of a rank-`cur` record) is
+// gathered from the tiles within R = ceil(feather / 32) rings into a bitmap
+// of the (2R + 1) x 32 px square window; erosion runs on the bitmap.  Pixels
+// outside the window count as outside the blob: every tile pixel is more
+// than 32 R >= feather pixels from them, so no layer below feather changes.
+__device__ __noinline__ void feather_layers(const uint4 *__restrict__ rec, const uint32_t *__restrict__ tile_off,
+                               uint32_t tiles_x, uint32_t tiles_y, uint32_t tile, uint32_t cur, uint32_t F,
+                               uint32_t *bm, uint8_t *layer) {
+    const int R = (int)((F + 31) / 32), WW = 2 * R + 1, WH = 32 * WW, nw = WW * WH;
+    uint32_t *A = bm, *B = bm + nw;
+    for (int i = threadIdx.x; i < nw; i += 256) A[i] = 0u;
+    for (int i = threadIdx.x; i < 1024; i += 256) layer[i] = (uint8_t)F;
+    __syncthreads();
+    const int tx = (int)(tile % tiles_x), ty = (int)(tile / tiles_x);
+    const int x0 = (tx - R) * 32, y0 = (ty - R) * 32;
+    for (int dy = -R; dy <= R; ++dy)
+        for (int dx = -R; dx <= R; ++dx) {
+            const int ux = tx + dx, uy = ty + dy;
+            if (ux < 0 || uy < 0 || ux >= (int)tiles_x || uy >= (int)tiles_y) continue;
+            const uint32_t t2 = (uint32_t)uy * tiles_x + (uint32_t)ux;
+            const uint32_t beg = tile_off[t2], end = tile_off[t2 + 1];
+            for (uint32_t j = beg + threadIdx.x; j < end; j += 256) {
+                const uint4 s = rec[j];
+                if (s.w != cur) continue;
+                const int px = (int)(s.x & 0xFFFFu), py = (int)(s.x >> 16);
+                const uint32_t valid = (s.y >> 16) & 15u;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (!(valid & (1u << k))) continue;
+                    const int wx = px + (k & 1) - x0, wy = py + (k >> 1) - y0;
+                    if (wx < 0 || wy < 0 || wx >= 32 * WW || wy >= WH) continue;
+                    atomicOr(&A[wy * WW + (wx >> 5)], 1u << (wx & 31));
+                }
+            }
+        }
+    __syncthreads();
+    for (uint32_t step = 0; step < F; ++step) {
+        for (int i = threadIdx.x; i < nw; i += 256) {
+            const int row = i / WW, w = i % WW;
+            const uint32_t a = A[i];
+            const uint32_t left = (a << 1) | (w > 0 ? A[i - 1] >> 31 : 0u);
+            const uint32_t right = (a >> 1) | (w + 1 < WW ? A[i + 1] << 31 : 0u);
+            const uint32_t up = row > 0 ? A[i - WW] : 0u, down = row + 1 < WH ? A[i + WW] : 0u;
+            const uint32_t e = a & left & right & up & down;
+            B[i] = e;
+            uint32_t removed = a & ~e;
+            if (removed && w == R && row >= 32 * R && row < 32 * R + 32)
+                while (removed) {
+                    const int bit = __ffs(removed) - 1;
+                    removed &= removed - 1u;
+                    layer[(row - 32 * R) * 32 + bit] = (uint8_t)step;
+                }
+        }
+        __syncthreads();
+        uint32_t *t = A; A = B; B = t;
+    }
+}
+
+// Extra dynamic shared memory of the resolve for a feather: two window
+// bitmaps and the tile's layers.
+__host__ __device__ inline size_t feather_smem(uint32_t F) {
+    if (!F) return 0;
+    const size_t R = (F + 31) / 32, WW = 2 * R + 1;
+    return 2 * WW * (32 * WW) * 4 + 1024;
+}
+
 __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restrict__ rec,
                                                         const uint32_t *__restrict__ tile_off, uint32_t tiles_x,
                                                         uint32_t width, uint32_t height, uint32_t density,
-                                                        uint8_t *out) {
+                                                        uint8_t *out, const __grid_constant__ ResolveOpts o) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ uint32_t red[8];
     __shared__ int s_over;
@@ -701,6 +780,8 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
     const uint32_t tx0 = (tile % tiles_x) * kTile, ty0 = (tile / tiles_x) * kTile;
     const uint32_t beg = tile_off[tile], end = tile_off[tile + 1];
     const uint32_t nrec = end - beg;
+    const bool feathered = o.feather > 0 && o.show_blobs == AM_TEXTURE;
+    uint8_t *flayer = sm + kResolveSmem + (o.feather ? feather_smem(o.feather) - 1024 : 0);
     // thread t owns pixels t, t + 256, t + 512, t + 768 of the tile (rows
     // t/32 + 8q): a warp reads 32 consecutive accumulators and stores 32
     // consecutive output pixels
@@ -728,7 +809,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
         for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; }
         if (!cached)
             for (uint32_t j = threadIdx.x; j < nrec; j += 256) mn = min(mn, rec[beg + j].w);
-        for (int o = 16; o; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        for (int w = 16; w; w >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, w));
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
         __syncthreads();
         uint32_t cur = red[0];
@@ -771,9 +852,12 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
                     }
                 }
             }
-            for (int o = 16; o; o >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, o));
+            for (int w = 16; w; w >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, w));
             __syncthreads();
             if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nxt;
+            if (feathered)
+                feather_layers(rec, tile_off, tiles_x, o.tiles_y, tile, cur, o.feather,
+                               reinterpret_cast<uint32_t *>(sm + kResolveSmem), flayer);
             if (packed) {
                 // more than kPackMax contributions could have wrapped a 32-bit sum
 #pragma unroll
@@ -809,8 +893,12 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
                     a = cnt >= density ? round_div(sa, W)
                                        : round_div((unsigned long long)cnt * sa, (unsigned long long)density * W);
                 }
-                if (a == 0) continue;  // draw_atoms skips transparent blob pixels
+                if (feathered && flayer[li] < o.feather)
+                    a = (uint32_t)(int)round(__dmul_rn((double)a, __ddiv_rn((double)(flayer[li] + 1),
+                                                                             (double)(o.feather + 1))));
                 uint32_t cc = r | (g << 8) | (b << 16) | (a << 24);
+                if (o.show_blobs != AM_TEXTURE) cc = o.rank_col[cur];
+                if ((cc >> 24) == 0) continue;  // draw_atoms skips transparent blob pixels
                 if (n[q] == 0) c0[q] = cc;
                 else over_blob(st[q], n[q] == 1, c0[q], cc);
                 n[q]++;
@@ -827,8 +915,10 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
         const uint32_t li = threadIdx.x + 256 * q;
         const uint32_t gy = ty0 + (li >> 5), gx = tx0 + (li & 31u);
         if (gy >= height || gx >= width) continue;
-        const uint32_t o = n[q] == 0 ? 0u : (n[q] == 1 ? c0[q] : over_bytes(st[q]));
-        reinterpret_cast<uint32_t *>(out)[(size_t)gy * width + gx] = o;
+        uint32_t px;
+        if (o.keep_bg) px = over_background(n[q], c0[q], st[q], bg_colour(o.bg, gx, gy));
+        else px = n[q] == 0 ? 0u : (n[q] == 1 ? c0[q] : over_bytes(st[q]));
+        reinterpret_cast<uint32_t *>(out)[(size_t)gy * width + gx] = px;
     }
 }
 
@@ -1063,17 +1153,25 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         }
         AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));  // the fused path expects zero counts
     }
+    ResolveOpts o;
+    std::memset(&o, 0, sizeof(o));
+    o.show_blobs = sc.blob_col ? sc.show_blobs : AM_TEXTURE;
+    o.rank_col = sc.blob_col ? sc.blob_col + (size_t)f * sc.C : nullptr;
+    o.feather = std::min<uint32_t>(sc.feather, kMaxFeather);
+    o.keep_bg = sc.keep_background && sc.present;
+    o.tiles_y = tiles_y;
+    o.bg = bg_args(sc, (uint32_t)f, t);
     if (w->prof) w->prof->open(s);
     {
         static bool attr = false;
         if (!attr) {
             AMG_CUDA(cudaFuncSetAttribute(k_frame_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)kResolveSmem));
+                                          (int)(kResolveSmem + feather_smem(kMaxFeather))));
             attr = true;
         }
     }
-    AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem, s, w->rec, w->tile_off, tiles_x, sc.width, sc.height,
-               sc.density ? sc.density : 1u, out);
+    AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem + feather_smem(o.feather), s, w->rec, w->tile_off, tiles_x,
+               sc.width, sc.height, sc.density ? sc.density : 1u, out, o);
     if (w->prof) w->prof->close(PROF_RESOLVE, s);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;

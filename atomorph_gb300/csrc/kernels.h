@@ -216,7 +216,18 @@ struct RenderScene {
     const uint64_t *chain_off;    // [C+1]
     const uint32_t *display;      // [K][CH][CW] RGB colour read by get_pixel
     const int32_t *rank;          // [K][C] composite rank of group g in frame k
+    // render options (morph.h:67-70)
+    uint32_t feather = 0;         // outer layers of each blob faded (TEXTURE blobs)
+    uint32_t keep_background = 0; // key frames cross-faded under the blobs
+    uint32_t show_blobs = 0;      // AM_TEXTURE, AM_AVERAGE or AM_DISTINCT
+    const uint8_t *present = nullptr;   // [K][CH][CW] 1 where the key frame has a pixel
+    const uint32_t *blob_col = nullptr; // [K][C] AVERAGE / DISTINCT colour (RGB) of the b-th blob of frame k
+    const int *perm = nullptr;          // [2][512] Perlin permutations (lag, slope) for the background
 };
+// Largest feather the frame render supports (three 32-px tile rings).
+constexpr uint32_t kMaxFeather = 96;
+// HSP -> RGB of one stored colour on the host (color.cpp:71-178).
+uint32_t hsp_to_rgb_host(uint32_t c);
 struct RenderWork;                // per-handle scratch (k_render.cu)
 RenderWork *render_work_create();
 void render_work_destroy(RenderWork *w);
@@ -266,9 +277,11 @@ void fluid_morph_destroy(FluidMorph *m);
 // Steps the particles to the frame (management, update, solver) and draws
 // it into out (device, width * height RGBA8).
 int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr, uint8_t *out, cudaStream_t s);
-// draw_fluid of the particles as they are (tests and the standalone solver).
+// draw_fluid of the particles as they are (tests and the standalone solver):
+// `feather` outward layers; bg_img (device [height][width] RGBA8, or null)
+// turns keep_background on with that background.
 int fluid_render_only(FluidDev *fl, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
-                      double t, uint8_t *out, cudaStream_t s);
+                      double t, uint32_t feather, const uint32_t *bg_img, uint8_t *out, cudaStream_t s);
 int launch_chain_ids(const uint64_t *chain_off, uint32_t C, uint64_t N, uint32_t *out, cudaStream_t s);
 const int *render_perm(RenderWork *w);
 

@@ -163,5 +163,77 @@ __device__ __forceinline__ uint32_t fade_colour(uint32_t fading, uint32_t c1, ui
     return o;
 }
 
+// get_background (morph.cpp:1431-1465) inputs for one frame: key frames f
+// and f + 1 ([CH][CW] RGB and presence), the fading, the Perlin maps and the
+// bbox the noise coordinates are normalised by; str = 1 - t.
+struct BgArgs {
+    uint32_t fading;
+    const uint32_t *disp1, *disp2;
+    const uint8_t *pres1, *pres2;
+    uint32_t CW, CH;
+    const int *perm;  // [2][512] (lag, slope)
+    float bx1, by1, bw, bh;
+    float str;
+};
+inline BgArgs bg_args(const RenderScene &sc, uint32_t f, double t) {
+    BgArgs o;
+    const size_t fr = (size_t)sc.CW * sc.CH, fn = (f + 1) % sc.K;
+    o.fading = sc.fading;
+    o.disp1 = sc.display + f * fr;
+    o.disp2 = sc.display + fn * fr;
+    o.pres1 = sc.present ? sc.present + f * fr : nullptr;
+    o.pres2 = sc.present ? sc.present + fn * fr : nullptr;
+    o.CW = sc.CW;
+    o.CH = sc.CH;
+    o.perm = sc.perm;
+    o.bx1 = (float)sc.bbox[0];
+    o.by1 = (float)sc.bbox[1];
+    o.bw = (float)(sc.bbox[2] - sc.bbox[0] + 1);
+    o.bh = (float)(sc.bbox[3] - sc.bbox[1] + 1);
+    o.str = (float)(1.0 - t);
+    return o;
+}
+
+// The background colour at pixel (x, y): the key frames' colours (a pixel a
+// key frame lacks reads as transparent black) cross-faded, PERLIN at the
+// pixel itself in FP32.
+static __device__ __noinline__ uint32_t bg_colour(const BgArgs &o, uint32_t x, uint32_t y) {
+    uint32_t c1 = 0, c2 = 0;
+    if (x < o.CW && y < o.CH && o.pres1) {
+        const size_t i = (size_t)y * o.CW + x;
+        if (o.pres1[i]) c1 = o.disp1[i];
+        if (o.pres2[i]) c2 = o.disp2[i];
+    }
+    float2 fp = fade_params(0.5f, 0.5f);
+    if (o.fading == AM_PERLIN && o.perm) {
+        const float px = ((float)((int)x - (int)o.bx1) / o.bw) * 8.f, py = ((float)((int)y - (int)o.by1) / o.bh) * 8.f;
+        fp = fade_params(poctave(o.perm, px, py) * 0.5f + 0.5f, poctave(o.perm + 512, px, py) * 0.5f + 0.5f);
+    }
+    return fade_colour(o.fading, c1, c2, fp, o.str);
+}
+
+// The composite drawn over the background (morph.cpp:1387-1399, 1270-1296):
+// n colours (the first c0; the FP64 "over" state st for two or more), bg the
+// background colour; create_color of the result.
+static __device__ __noinline__ uint32_t over_background(int n, uint32_t c0, const double *st, uint32_t bg) {
+    if (n == 0) return bg;
+    double r, g, b, a;
+    if (n == 1) {
+        r = (c0 & 255u) / 255.0; g = ((c0 >> 8) & 255u) / 255.0; b = ((c0 >> 16) & 255u) / 255.0; a = (c0 >> 24) / 255.0;
+    } else {
+        r = st[0]; g = st[1]; b = st[2]; a = st[3];
+    }
+    const double br = (bg & 255u) / 255.0, bgg = ((bg >> 8) & 255u) / 255.0, bb = ((bg >> 16) & 255u) / 255.0,
+                 ba = (bg >> 24) / 255.0;
+    const double om = __dsub_rn(1.0, a);
+    r = __dadd_rn(__dmul_rn(a, r), __dmul_rn(om, br));
+    g = __dadd_rn(__dmul_rn(a, g), __dmul_rn(om, bgg));
+    b = __dadd_rn(__dmul_rn(a, b), __dmul_rn(om, bb));
+    a = __dadd_rn(ba, __dmul_rn(__dsub_rn(1.0, ba), a));
+    const double v[4] = {r, g, b, a};
+    uint32_t o = 0;
+    for (int k = 0; k < 4; ++k) o |= ((uint32_t)(int)round(__dmul_rn(v[k], 255.0)) & 255u) << (8 * k);
+    return o;
+}
 
 }  // namespace amg

@@ -97,9 +97,15 @@ int am_set_motion(am_morph *m, unsigned motion);             /* morph.h:63 */
 int am_set_fading(am_morph *m, unsigned fading);             /* morph.h:64 */
 int am_set_threads(am_morph *m, size_t t);                   /* morph.h:65 (accepted; GPU width is automatic) */
 int am_set_cycle_length(am_morph *m, size_t c);              /* morph.h:66 (proposals per atom step, see DESIGN) */
+/* Feather fades each blob's outer f layers (morph.cpp:625-674; the fluid
+ * path grows f layers outward, morph.cpp:1204-1266); f <= 96, larger values
+ * return AM_ERR_UNSUPPORTED. */
 int am_set_feather(am_morph *m, size_t f);                   /* morph.h:67 */
 int am_set_keep_background(am_morph *m, int k);              /* morph.h:68 */
 int am_set_finite(am_morph *m, int f);                       /* morph.h:69 */
+/* AM_TEXTURE (atom colours), AM_AVERAGE (each blob in its mean colour) or
+ * AM_DISTINCT (a colour per group from std::mt19937(group)),
+ * morph.cpp:1321-1334; other values draw TEXTURE. */
 int am_set_show_blobs(am_morph *m, unsigned b);              /* morph.h:70 */
 int am_set_fluid(am_morph *m, unsigned steps);               /* morph::set_fluid morph.cpp:1553-1560 */
 int am_set_density(am_morph *m, uint16_t d);                 /* morph::set_density morph.cpp:1562-1570 */
@@ -231,6 +237,12 @@ void *am_fluid_stream(am_fluid *f);
  * width x height RGBA8); bbox = x1, y1, x2, y2 of the key frames. */
 int  am_fluid_render(am_fluid *f, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
                      double t, uint8_t *rgba_out);
+/* The same with `feather` outward layers (morph.cpp:1204-1266) and, when
+ * `background` (host width x height RGBA8, the get_background image) is not
+ * NULL, keep_background: fluid alpha x (1 - t^24) drawn over it
+ * (morph.cpp:1187-1190, 1268-1299). */
+int  am_fluid_render_ex(am_fluid *f, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
+                        double t, size_t feather, const uint8_t *background, uint8_t *rgba_out);
 
 /* ---- batched refinement (no reference counterpart: the reference refines
  * one morph per worker thread, thread.cpp:173-206).  A batch refines many

@@ -27,6 +27,7 @@
 #include <map>
 #include <numeric>
 #include <random>
+#include <set>
 #include <thread>
 #include <vector>
 
@@ -303,6 +304,10 @@ struct orc_scene {
     const uint64_t *pts;        // [K][N]
     const int32_t *blob_order;  // [K][C] group of the b-th blob of key frame k
     const uint64_t *frame_keys; // [K] map keys of the key frames
+    uint32_t feather;           // set_feather: outer layers of each blob faded
+    uint32_t keep_background;   // set_keep_background
+    uint32_t show_blobs;        // set_show_blobs: TEXTURE 0, AVERAGE 1, DISTINCT 2
+    const uint32_t *blob_avg;   // [K][C] create_color of the b-th blob's mean colour (stored space), for AVERAGE
 };
 
 }  // extern "C"
@@ -451,6 +456,71 @@ void blob_pixels(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_
         px.c = Col{(uint8_t)r, (uint8_t)g, (uint8_t)b, (uint8_t)a};
         out.push_back(px);
     }
+    if (s.feather == 0) return;
+    // Feather (morph.cpp:625-674): peel the blob's 4-neighbour border up to
+    // `feather` times; layer l's alpha scales by (l + 1) / (feather + 1).
+    std::map<size_t, Col> blob;
+    for (const Px &p : out) blob[(size_t)p.y * 65536 + p.x] = p.c;
+    std::map<size_t, Col> peeled = blob;
+    std::vector<std::set<size_t>> layers;
+    while (!peeled.empty() && layers.size() < s.feather) {
+        std::set<size_t> border;
+        for (auto &kv : peeled) {
+            const size_t pos = kv.first;
+            const uint32_t x = (uint32_t)(pos % 65536), y = (uint32_t)(pos / 65536);
+            if (x == 0 || x == 65535 || y == 0 || y == 65535) { border.insert(pos); continue; }
+            if (!peeled.count(pos + 1) || !peeled.count(pos - 1) || !peeled.count(pos + 65536) ||
+                !peeled.count(pos - 65536))
+                border.insert(pos);
+        }
+        for (size_t pos : border) peeled.erase(pos);
+        layers.push_back(border);
+    }
+    out.clear();
+    for (size_t l = 0; l < layers.size(); ++l)
+        for (size_t pos : layers[l]) {
+            Px px;
+            px.x = (uint16_t)(pos % 65536);
+            px.y = (uint16_t)(pos / 65536);
+            px.c = blob[pos];
+            px.c.a = (uint8_t)std::round(double(px.c.a) * (double(l + 1) / double(s.feather + 1)));
+            out.push_back(px);
+        }
+    for (auto &kv : peeled) {
+        Px px;
+        px.x = (uint16_t)(kv.first % 65536);
+        px.y = (uint16_t)(kv.first / 65536);
+        px.c = kv.second;
+        out.push_back(px);
+    }
+}
+
+// morph::get_background (morph.cpp:1431-1465): the key frames' colours at
+// (x, y) cross-faded with the frame's fading (Perlin at the pixel itself).
+Col background(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_map, uint32_t x, uint32_t y, size_t f,
+               double t) {
+    const size_t fn = (f + 1) % s.K;
+    const Col c1 = read_pixel(s, (uint32_t)f, x, y), c2 = read_pixel(s, (uint32_t)fn, x, y);
+    if (s.fading == PERLIN) {
+        const double bw = s.bbox[2] - s.bbox[0] + 1.0, bh = s.bbox[3] - s.bbox[1] + 1.0;
+        const double px = ((int)x - (int)s.bbox[0]) / bw * 8.0, py = ((int)y - (int)s.bbox[1]) / bh * 8.0;
+        const double lag = lag_map.octave(px, py, 8) * 0.5 + 0.5, slope = slope_map.octave(px, py, 8) * 0.5 + 0.5;
+        return ramp_col(c1, c2, lag, slope, 1.0 - t);
+    }
+    if (s.fading == COSINE) return ramp_col(c1, c2, 0.5, 0.5, 1.0 - t);
+    return lerp_col(c1, c2, 1.0 - t);
+}
+
+// show_blobs == DISTINCT colour of a group (morph.cpp:1322-1328).
+Col distinct_colour(size_t group) {
+    std::mt19937 gen((unsigned)group);
+    std::uniform_int_distribution<unsigned char> d(0, 255);
+    Col c;
+    c.r = d(gen);
+    c.g = d(gen);
+    c.b = d(gen);
+    c.a = 255;
+    return c;
 }
 
 void render_one(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_map, double time_in, uint8_t *out) {
@@ -465,18 +535,34 @@ void render_one(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_m
     if (f >= s.K) return;
     double dt = 1.0 / double(s.K);
     double t = std::max(0.0, (time - (double)(s.frame_keys[f] * dt)) / dt);
+    if (s.keep_background)
+        for (uint32_t y = 0; y < s.height; ++y)
+            for (uint32_t x = 0; x < s.width; ++x) {
+                const Col c = background(s, lag_map, slope_map, x, y, f, t);
+                uint8_t *d = out + ((size_t)y * s.width + x) * 4;
+                d[0] = c.r; d[1] = c.g; d[2] = c.b; d[3] = c.a;
+            }
     std::map<size_t, std::vector<Col>> comp;
     std::vector<Px> pix;
     for (uint32_t b = 0; b < s.C; ++b) {
         pix.clear();
-        blob_pixels(s, lag_map, slope_map, (uint32_t)s.blob_order[(size_t)f * s.C + b], (uint32_t)f, t, time, pix);
-        // draw_atoms (morph.cpp:1313-1345), TEXTURE colours.
+        const uint32_t group = (uint32_t)s.blob_order[(size_t)f * s.C + b];
+        blob_pixels(s, lag_map, slope_map, group, (uint32_t)f, t, time, pix);
+        // draw_atoms (morph.cpp:1313-1345): TEXTURE, AVERAGE (blob2pixel,
+        // morph.cpp:1423-1429) or DISTINCT colours.
+        Col ave{0, 0, 0, 0};
+        if (s.show_blobs == 1 && s.blob_avg) {
+            ave = col_of(s.blob_avg[(size_t)f * s.C + b]);
+            if (s.delimiter == HSP) ave = to_rgb(ave);
+        }
+        const Col dis = distinct_colour(group);
         for (size_t i = pix.size(); i-- > 0;) {
             Px px = pix[i];
             size_t pos = (size_t)px.y * s.width + px.x;
             if (pos >= npx) continue;
-            if (px.c.a == 0) continue;
-            comp[pos].push_back(px.c);
+            const Col c = s.show_blobs == 2 ? dis : (s.show_blobs == 1 ? ave : px.c);
+            if (c.a == 0) continue;
+            comp[pos].push_back(c);
         }
     }
     // Ordered "over" composite (morph.cpp:1348-1402), no blend/background.
@@ -493,8 +579,16 @@ void render_one(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_m
                 a = a + (1.0 - a) * (q.a / 255.0);
             }
         }
-        Col o = make_col(r, g, b, a);
         uint8_t *d = out + kv.first * 4;
+        if (s.keep_background) {
+            // morph.cpp:1387-1399
+            const double bgr = d[0] / 255.0, bgg = d[1] / 255.0, bgb = d[2] / 255.0, bga = d[3] / 255.0;
+            r = a * r + (1.0 - a) * bgr;
+            g = a * g + (1.0 - a) * bgg;
+            b = a * b + (1.0 - a) * bgb;
+            a = bga + (1.0 - bga) * a;
+        }
+        Col o = make_col(r, g, b, a);
         d[0] = o.r; d[1] = o.g; d[2] = o.b; d[3] = o.a;
     }
 }
@@ -505,7 +599,8 @@ extern "C" {
 
 // Renders one frame at time t into width*height*4 bytes (morph.cpp:1405-1421,
 // fluid off).  Supports motion NONE/LINEAR/SPLINE, fading
-// NONE/LINEAR/COSINE/PERLIN, TEXTURE blobs, feather 0, no background.
+// NONE/LINEAR/COSINE/PERLIN, TEXTURE/AVERAGE/DISTINCT blobs, feather and
+// keep_background (blend_blobs has no setter in the reference and stays off).
 void orc_render(const orc_scene *s, double t, uint8_t *out) {
     Perlin lag(s->seed), slope(s->seed + 1);
     render_one(*s, lag, slope, t, out);
@@ -727,8 +822,21 @@ void orc_srand(unsigned s) { srand(s); }
 // height, zero where no particle lands).  feather = 0, keep_background off.
 // Corners outside the output are dropped like the GPU path (the reference
 // would wrap them into the next row).
+void orc_draw_fluid_ex(double *P, uint32_t n, uint32_t width, uint32_t height, double sparseness,
+                       const uint32_t *bbox, double t, uint32_t feather, const uint8_t *background, uint8_t *out);
 void orc_draw_fluid(double *P, uint32_t n, uint32_t width, uint32_t height, double sparseness, const uint32_t *bbox,
                     double t, uint8_t *out) {
+    orc_draw_fluid_ex(P, n, width, height, sparseness, bbox, t, 0, nullptr, out);
+}
+
+// draw_fluid with feather and keep_background (morph.cpp:1187-1300):
+// `background` (RGBA8 width x height, or null for keep_background off) is
+// the image get_background prefilled; the fluid's alpha fades by 1 - t^24,
+// `feather` layers grow outward (each new pixel the mean of its member
+// 4-neighbours, alpha scaled by 1 - (layer + 1) / (feather + 1)), and the
+// result is drawn over the background.
+void orc_draw_fluid_ex(double *P, uint32_t n, uint32_t width, uint32_t height, double sparseness,
+                       const uint32_t *bbox, double t, uint32_t feather, const uint8_t *background, uint8_t *out) {
     auto F = [&](int f, uint32_t i) -> double & { return P[(size_t)f * n + i]; };
     const size_t npx = (size_t)width * height;
     std::vector<double> W(npx, 0.0), R(npx, 0.0), G(npx, 0.0), B(npx, 0.0), A(npx, 0.0);
@@ -769,14 +877,85 @@ void orc_draw_fluid(double *P, uint32_t n, uint32_t width, uint32_t height, doub
         if ((y < bbox[3] || y + 1 < height) && w12 > 0.0) put(x, y + 1, w12);
         if (w22 > 0.0 && ((y < bbox[3] && x < bbox[2]) || (y + 1 < height && x + 1 < width))) put(x + 1, y + 1, w22);
     }
+    std::map<size_t, Col> blob;  // fluid pixels by y * 65536 + x
+    for (size_t q = 0; q < npx; ++q) {
+        if (!any[q]) continue;
+        double a = std::round(A[q] / W[q]);
+        if (background) a *= 1.0 - std::pow(t, 24.0);
+        blob[(q / width) * 65536 + q % width] =
+            Col{(uint8_t)std::round(R[q] / W[q]), (uint8_t)std::round(G[q] / W[q]), (uint8_t)std::round(B[q] / W[q]),
+                (uint8_t)a};
+    }
+    for (uint32_t layer = 0; layer < feather; ++layer) {
+        const double alpha = 1.0 - (double(layer + 1) / double(feather + 1));
+        std::set<size_t> border;
+        for (auto &kv : blob) {
+            const uint32_t x = (uint32_t)(kv.first % 65536), y = (uint32_t)(kv.first / 65536);
+            if (x + 1 < width && !blob.count(kv.first + 1)) border.insert(kv.first + 1);
+            if (y + 1 < height && !blob.count(kv.first + 65536)) border.insert(kv.first + 65536);
+            if (x > 0 && !blob.count(kv.first - 1)) border.insert(kv.first - 1);
+            if (y > 0 && !blob.count(kv.first - 65536)) border.insert(kv.first - 65536);
+        }
+        if (border.empty()) break;
+        std::map<size_t, Col> add;
+        for (size_t pos : border) {
+            const uint32_t x = (uint32_t)(pos % 65536), y = (uint32_t)(pos / 65536);
+            std::set<size_t> comps;
+            if (x + 1 < width && blob.count(pos + 1)) comps.insert(pos + 1);
+            if (y + 1 < height && blob.count(pos + 65536)) comps.insert(pos + 65536);
+            if (x > 0 && blob.count(pos - 1)) comps.insert(pos - 1);
+            if (y > 0 && blob.count(pos - 65536)) comps.insert(pos - 65536);
+            double r = 0, g = 0, b = 0, a = 0;
+            const double w = (double)comps.size();
+            for (size_t c : comps) {
+                const Col q = blob[c];
+                r += (q.r / 255.0) / w; g += (q.g / 255.0) / w; b += (q.b / 255.0) / w; a += (q.a / 255.0) / w;
+            }
+            a *= alpha;
+            add[pos] = make_col(r, g, b, a);
+        }
+        for (auto &kv : add) blob[kv.first] = kv.second;
+    }
     for (size_t q = 0; q < npx; ++q) {
         uint8_t *o = out + 4 * q;
-        if (!any[q]) { o[0] = o[1] = o[2] = o[3] = 0; continue; }
-        o[0] = (uint8_t)std::round(R[q] / W[q]);
-        o[1] = (uint8_t)std::round(G[q] / W[q]);
-        o[2] = (uint8_t)std::round(B[q] / W[q]);
-        o[3] = (uint8_t)std::round(A[q] / W[q]);
+        if (background) std::memcpy(o, background + 4 * q, 4);
+        else o[0] = o[1] = o[2] = o[3] = 0;
     }
+    for (auto &kv : blob) {
+        const size_t q = (kv.first / 65536) * width + kv.first % 65536;
+        uint8_t *o = out + 4 * q;
+        Col c = kv.second;
+        if (background) {
+            const double bgr = o[0] / 255.0, bgg = o[1] / 255.0, bgb = o[2] / 255.0, bga = o[3] / 255.0;
+            double r = c.r / 255.0, g = c.g / 255.0, b = c.b / 255.0, a = c.a / 255.0;
+            r = a * r + (1.0 - a) * bgr;
+            g = a * g + (1.0 - a) * bgg;
+            b = a * b + (1.0 - a) * bgb;
+            a = bga + (1.0 - bga) * a;
+            c = Col{(uint8_t)std::round(r * 255.0), (uint8_t)std::round(g * 255.0), (uint8_t)std::round(b * 255.0),
+                    (uint8_t)std::round(a * 255.0)};
+        }
+        o[0] = c.r; o[1] = c.g; o[2] = c.b; o[3] = c.a;
+    }
+}
+
+// The image get_background fills (morph.cpp:1405-1413) for time t.
+void orc_background(const orc_scene *s, double time_in, uint8_t *out) {
+    Perlin lag(s->seed), slope(s->seed + 1);
+    double integ;
+    double time = std::modf(time_in, &integ);
+    if (time < 0.0) time += 1.0;
+    size_t f = (size_t)(time * s->K);
+    const size_t npx = (size_t)s->width * s->height;
+    if (s->K == 0 || f >= s->K) { std::memset(out, 0, npx * 4); return; }
+    const double dt = 1.0 / double(s->K);
+    const double t = std::max(0.0, (time - (double)(s->frame_keys[f] * dt)) / dt);
+    for (uint32_t y = 0; y < s->height; ++y)
+        for (uint32_t x = 0; x < s->width; ++x) {
+            const Col c = background(*s, lag, slope, x, y, f, t);
+            uint8_t *d = out + ((size_t)y * s->width + x) * 4;
+            d[0] = c.r; d[1] = c.g; d[2] = c.b; d[3] = c.a;
+        }
 }
 
 // --------------------------------------------------------------- blobs -----

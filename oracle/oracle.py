@@ -14,6 +14,7 @@ import this module.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -53,7 +54,8 @@ class Scene(C.Structure):
         ("width", C.c_uint32), ("height", C.c_uint32), ("bbox", C.c_uint32 * 4), ("seed", C.c_uint32),
         ("motion", C.c_uint32), ("fading", C.c_uint32), ("delimiter", C.c_uint32), ("density", C.c_uint32),
         ("colors", u32p), ("present", u8p), ("widths", u64p), ("pts", u64p), ("blob_order", i32p),
-        ("frame_keys", u64p),
+        ("frame_keys", u64p), ("feather", C.c_uint32), ("keep_background", C.c_uint32), ("show_blobs", C.c_uint32),
+        ("blob_avg", u32p),
     ]
 
 
@@ -84,6 +86,13 @@ def make_scene(state: dict) -> tuple[Scene, list]:
     s.delimiter, s.density = int(state["delimiter"]), int(state["density"])
     s.colors, s.present, s.widths = _p(colors, u32p), _p(present, u8p), _p(widths, u64p)
     s.pts, s.blob_order, s.frame_keys = _p(pts, u64p), _p(order, i32p), _p(keys, u64p)
+    # render options (morph.h:67-70); blob_avg: [K][C] stored-space colour of
+    # the b-th blob of key frame k (create_color of its mean), for AVERAGE
+    s.feather = int(state.get("feather", 0))
+    s.keep_background = int(bool(state.get("keep_background", 0)))
+    s.show_blobs = int(state.get("show_blobs", 0))
+    if state.get("blob_avg") is not None:
+        s.blob_avg = _p(arr("blob_avg", np.uint32), u32p)
     return s, keep
 
 
@@ -108,6 +117,9 @@ class Oracle:
         L.orc_fluid_step.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, f64p, u8p, C.c_uint64, C.c_double]
         L.orc_srand.argtypes = [C.c_uint]
         L.orc_draw_fluid.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, u32p, C.c_double, u8p]
+        L.orc_draw_fluid_ex.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, u32p, C.c_double,
+                                        C.c_uint32, u8p, u8p]
+        L.orc_background.argtypes = [C.POINTER(Scene), C.c_double, u8p]
         L.orc_components.restype = C.c_uint32
         L.orc_components.argtypes = [u8p, u32p, C.c_uint32, C.c_uint32, i32p, f64p, C.c_uint32]
         L.orc_blob_energy.restype = C.c_double
@@ -181,13 +193,24 @@ class Oracle:
         self.lib.orc_fluid_step(_p(P, f64p), n, gsx, gsy, _p(grid, f64p), _p(touched, u8p), steps_left,
                                 freedom_radius)
 
-    def draw_fluid(self, P: np.ndarray, width: int, height: int, sparseness: float, bbox, t: float) -> np.ndarray:
+    def draw_fluid(self, P: np.ndarray, width: int, height: int, sparseness: float, bbox, t: float,
+                   feather: int = 0, background: np.ndarray | None = None) -> np.ndarray:
         """draw_fluid of particles P[18, n] (modified like the reference's:
-        colours corrected, particles matured); returns the RGBA8 frame."""
+        colours corrected, particles matured); returns the RGBA8 frame.  With
+        `background` (the get_background image) keep_background is on."""
         n = P.shape[1]
         out = np.zeros((height, width, 4), np.uint8)
         bb = np.ascontiguousarray(bbox, np.uint32)
-        self.lib.orc_draw_fluid(_p(P, f64p), n, width, height, sparseness, _p(bb, u32p), t, _p(out, u8p))
+        bg = None if background is None else np.ascontiguousarray(background, np.uint8)
+        self.lib.orc_draw_fluid_ex(_p(P, f64p), n, width, height, sparseness, _p(bb, u32p), t, feather,
+                                   None if bg is None else _p(bg, u8p), _p(out, u8p))
+        return out
+
+    def background(self, state: dict, t: float) -> np.ndarray:
+        """The get_background image at time t (morph.cpp:1405-1413, 1431-1465)."""
+        s, keep = make_scene(state)
+        out = np.zeros((int(state["height"]), int(state["width"]), 4), np.uint8)
+        self.lib.orc_background(C.byref(s), t, _p(out, u8p))
         return out
 
     def srand(self, s: int) -> None:
@@ -223,7 +246,8 @@ class Reference:
             ("ref_set_motion", [C.c_uint]), ("ref_set_fading", [C.c_uint]), ("ref_set_fluid", [C.c_uint]),
             ("ref_set_degeneration", [C.c_size_t]), ("ref_set_finite", [C.c_int]),
             ("ref_set_resolution", [C.c_uint, C.c_uint]), ("ref_set_cycle_length", [C.c_size_t]),
-            ("ref_set_threads", [C.c_size_t]),
+            ("ref_set_threads", [C.c_size_t]), ("ref_set_feather", [C.c_size_t]),
+            ("ref_set_keep_background", [C.c_int]), ("ref_set_show_blobs", [C.c_uint]),
             ("ref_add_image", [C.c_size_t, u8p, C.c_uint, C.c_uint]),
             ("ref_prepare", [C.c_size_t, C.c_size_t]), ("ref_export_points", [u64p, C.c_size_t]),
             ("ref_import_points", [u64p, C.c_size_t]), ("ref_sweeps", [C.c_size_t, C.c_uint]),
@@ -346,19 +370,35 @@ class Reference:
             out.append((g.value, s.value, xy))
         return out
 
+    def options(self, feather: int = 0, keep_background: int = 0, show_blobs: int = 0) -> None:
+        self.lib.ref_set_feather(self.h, feather)
+        self.lib.ref_set_keep_background(self.h, keep_background)
+        self.lib.ref_set_show_blobs(self.h, show_blobs)
+
     def state(self, seed: int, motion: int, fading: int, delimiter: int, density: int, frames) -> dict:
         """Morph state dict of the reference after prepare(), for the
-        oracle / GPU renderers."""
+        oracle / GPU renderers (blob_avg: create_color of each blob's mean)."""
         w, K = self.widths()
         C_ = len(w)
         order = np.zeros((K, C_), np.int32)
+        avg = np.zeros((K, C_), np.uint32)
         for f in range(K):
             for b, (g, s, xy) in enumerate(self.blobs(f)):
                 order[f, b] = g
+                c = [_round_away(v * 255.0) & 255 for v in xy[2:6]]
+                avg[f, b] = c[0] | (c[1] << 8) | (c[2] << 16) | (c[3] << 24)
         stored = stored_frames(frames, delimiter, self)
         return dict(K=K, width=self.width, height=self.height, bbox=self.bbox(), seed=seed, motion=motion,
                     fading=fading, delimiter=delimiter, density=density, colors=stored[0], present=stored[1],
-                    widths=w, pts=self.points(), blob_order=order, frame_keys=np.arange(K, dtype=np.uint64))
+                    widths=w, pts=self.points(), blob_order=order, frame_keys=np.arange(K, dtype=np.uint64),
+                    blob_avg=avg)
+
+
+def _round_away(x: float) -> int:
+    """std::round: halves away from zero (x - floor(x) is exact in double)."""
+    f = math.floor(x)
+    r = int(f) + (1 if x - f >= 0.5 else 0)
+    return r if x >= 0 else -_round_away(-x)
 
 
 def stored_frames(frames, delimiter: int, conv) -> tuple[np.ndarray, np.ndarray]:

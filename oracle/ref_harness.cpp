@@ -61,6 +61,9 @@ void ref_set_resolution(void *h, unsigned w, unsigned hh) {
     ((am::morph *)h)->set_resolution((uint16_t)w, (uint16_t)hh);
 }
 void ref_set_cycle_length(void *h, size_t c) { ((am::morph *)h)->set_cycle_length(c); }
+void ref_set_feather(void *h, size_t f) { ((am::morph *)h)->set_feather(f); }
+void ref_set_keep_background(void *h, int k) { ((am::morph *)h)->set_keep_background(k != 0); }
+void ref_set_show_blobs(void *h, unsigned b) { ((am::morph *)h)->set_show_blobs(b); }
 void ref_set_threads(void *h, size_t t) { ((am::morph *)h)->set_threads(t); }
 
 // Same ingestion as the demo's fill_morph (demo/main.cpp:96-127): every pixel

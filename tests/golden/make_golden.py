@@ -13,6 +13,11 @@ Fixtures (all small, seeded):
   spline48.npz    48x48, 3 key frames: chains and frames (SPLINE, COSINE, RGB,
                   density 2)
   fluid.npz       FluidModel::step on 300 particles for 8 steps
+  features.npz    56x56, 4 key frames (SPLINE, PERLIN, HSP): frames rendered
+                  with feather, keep_background and show_blobs AVERAGE /
+                  DISTINCT (morph.h:67-70), and the blob colours they read
+
+    python tests/golden/make_golden.py features   # that fixture only
 """
 from __future__ import annotations
 
@@ -51,9 +56,36 @@ def morph_case(R, frames, *, seed, motion, fading, delimiter, density, sweeps, s
     return out
 
 
+FEATURE_OPTIONS = [(0, 0, 0), (0, 0, 1), (0, 0, 2), (0, 1, 0), (3, 0, 0), (2, 1, 0), (1, 1, 1), (5, 0, 2)]
+FEATURE_TS = [0.05, 0.3, 0.61, 0.9]
+
+
+def features_case(R):
+    """Render options (feather, keep_background, show_blobs) on one seeded
+    case; the state the oracle needs to draw the same frames."""
+    rng = np.random.default_rng(77)
+    frames = [synth.ellipses_frame(56, 5, 3.0, 14.0, rng) for _ in range(4)]
+    R.new(frames, seed=5, motion=4, fading=6, delimiter=1, density=1)
+    R.prepare()
+    R.sweeps(4, 31)
+    st = R.state(5, 4, 6, 1, 1, frames)
+    renders = []
+    for feather, kb, sb in FEATURE_OPTIONS:
+        R.options(feather, kb, sb)
+        renders.append(np.stack([R.render(t) for t in FEATURE_TS]))
+    R.options(0, 0, 0)
+    return dict(frames=np.stack(frames), options=np.array(FEATURE_OPTIONS), ts=np.array(FEATURE_TS),
+                renders=np.stack(renders), K=st["K"], width=st["width"], height=st["height"], bbox=st["bbox"],
+                seed=5, motion=4, fading=6, delimiter=1, density=1, colors=st["colors"], present=st["present"],
+                widths=st["widths"], pts=st["pts"], blob_order=st["blob_order"], blob_avg=st["blob_avg"])
+
+
 def main():
     orc.build(with_ref=True)
     R = orc.Reference()
+    if sys.argv[1:] == ["features"]:
+        np.savez_compressed(os.path.join(HERE, "features.npz"), **features_case(R))
+        return
     L = R.lib
     rng = np.random.default_rng(2024)
     rgb = rng.integers(0, 2**32, 4096, dtype=np.uint64).astype(np.uint32)
@@ -100,6 +132,7 @@ def main():
     L.ref_fluid_free(h)
     np.savez_compressed(os.path.join(HERE, "fluid.npz"), init=P, gsx=gsx, gsy=gsy, freedom=4.0,
                         step1=steps[0], step8=steps[-1])
+    np.savez_compressed(os.path.join(HERE, "features.npz"), **features_case(R))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

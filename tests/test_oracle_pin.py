@@ -99,3 +99,34 @@ def test_live_reference_pin(oracle):
         st = R.state(5, motion, fading, delim, dens, frames)
         for t in (0.05, 0.3, 0.61, 0.9):
             assert np.array_equal(oracle.render(st, t), R.render(t))
+
+
+def test_render_options_match_reference(oracle):
+    """feather, keep_background and show_blobs AVERAGE / DISTINCT (morph.h:
+    67-70): the oracle draws the reference's frames from the reference's
+    chains and blob colours, bit-exact."""
+    g = golden("features")
+    st = golden_state(g)
+    st["blob_avg"] = g["blob_avg"]
+    for (feather, kb, sb), frames in zip(g["options"], g["renders"]):
+        st.update(feather=int(feather), keep_background=int(kb), show_blobs=int(sb))
+        for t, ref in zip(g["ts"], frames):
+            assert np.array_equal(oracle.render(st, float(t)), ref), f"options {(feather, kb, sb)} t={t}"
+
+
+@pytest.mark.skipif(not orc.have_reference(), reason="reference sources not built here")
+def test_live_reference_pin_render_options(oracle):
+    """Fresh seeded case with the render options, reference run live."""
+    from atomorph_gb300 import synth
+    R = orc.Reference()
+    r = np.random.default_rng(91)
+    frames = [synth.ellipses_frame(48, 4, 3.0, 12.0, r) for _ in range(3)]
+    R.new(frames, seed=9, motion=3, fading=5, delimiter=0, density=1)
+    R.prepare()
+    R.sweeps(3, 7)
+    for opts in [(2, 1, 0), (4, 0, 1), (0, 1, 2)]:
+        R.options(*opts)
+        st = R.state(9, 3, 5, 0, 1, frames)
+        st.update(feather=opts[0], keep_background=opts[1], show_blobs=opts[2])
+        for t in (0.2, 0.55, 0.85):
+            assert np.array_equal(oracle.render(st, t), R.render(t)), (opts, t)
