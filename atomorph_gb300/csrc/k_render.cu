@@ -1042,7 +1042,9 @@ int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, do
         int n = (int)sc.K;
         double delta_t = 1.0 / n;
         int p = (int)(time / delta_t);
-        auto wrap = [n](int i) { return i < 0 ? n - 1 : (i >= n ? i - n : i); };
+        // cyclic indices: the reference's single wrap (spline.cpp:49-52) for n >= 2; with one
+        // key frame it reads past its control points, here every index is that frame
+        auto wrap = [n](int i) { return ((i % n) + n) % n; };
         double lt = (time - delta_t * (double)p) / delta_t;
         double t2 = lt * lt, t3 = t2 * lt;
         fa.b0 = 0.5 * (-t3 + 2.0 * t2 - lt);

@@ -197,7 +197,9 @@ struct Perlin {
 void spline_eval(const double *xs, const double *ys, int n, double t, double *ox, double *oy) {
     double delta_t = 1.0 / n;
     int p = (int)(t / delta_t);
-    auto wrap = [n](int i) { return i < 0 ? n - 1 : (i >= n ? i - n : i); };
+    // cyclic indices: the reference's single wrap (spline.cpp:49-52) for n >= 2; with one
+    // key frame it reads past its control points, here every index is that frame
+    auto wrap = [n](int i) { return ((i % n) + n) % n; };
     int p0 = wrap(p - 1), p1 = wrap(p), p2 = wrap(p + 1), p3 = wrap(p + 2);
     double lt = (t - delta_t * (double)p) / delta_t;
     double t2 = lt * lt, t3 = t2 * lt;

@@ -17,7 +17,10 @@ Fixtures (all small, seeded):
                   with feather, keep_background and show_blobs AVERAGE /
                   DISTINCT (morph.h:67-70), and the blob colours they read
 
-    python tests/golden/make_golden.py features   # that fixture only
+  edges.npz       edge inputs: an all-transparent key frame, a single key
+                  frame, key frames of different sizes (counts, chains, frames)
+
+    python tests/golden/make_golden.py features   # one fixture only (or: edges)
 """
 from __future__ import annotations
 
@@ -56,6 +59,33 @@ def morph_case(R, frames, *, seed, motion, fading, delimiter, density, sweeps, s
     return out
 
 
+def edges_case(R):
+    """Edge inputs: an all-transparent key frame between two others, one key
+    frame, key frames of different sizes (LINEAR, PERLIN, RGB): reference
+    counts after matching and frames rendered from the reference's chains."""
+    rng = np.random.default_rng(3)
+    a = synth.ellipses_frame(48, 3, 4.0, 12.0, rng)
+    b = synth.ellipses_frame(48, 3, 4.0, 12.0, rng)
+    small = synth.ellipses_frame(32, 2, 3.0, 8.0, rng)
+    empty = np.zeros((48, 48, 4), np.uint8)
+    out = {}
+    for name, frames in (("empty_middle", [a, empty, b]), ("single", [a]), ("mixed_sizes", [a, small, b])):
+        R.new(frames, seed=4, motion=3, fading=6, delimiter=0, density=1)
+        R.prepare()
+        w, K = R.widths()
+        st = R.state(4, 3, 6, 0, 1, frames)
+        canvas = np.zeros((K, st["height"], st["width"], 4), np.uint8)
+        for k, f in enumerate(frames):
+            canvas[k, :f.shape[0], :f.shape[1]] = f
+        out.update({f"{name}_frames": canvas, f"{name}_sizes": np.array([f.shape[:2] for f in frames]),
+                    f"{name}_blob_counts": np.array([R.blob_count(f) for f in range(K)]),
+                    f"{name}_pixel_counts": np.array([R.pixel_count(f) for f in range(K)]),
+                    f"{name}_widths": w, f"{name}_pts": st["pts"], f"{name}_blob_order": st["blob_order"],
+                    f"{name}_renders": np.stack([R.render(t) for t in FEATURE_TS])})
+    out["ts"] = np.array(FEATURE_TS)
+    return out
+
+
 FEATURE_OPTIONS = [(0, 0, 0), (0, 0, 1), (0, 0, 2), (0, 1, 0), (3, 0, 0), (2, 1, 0), (1, 1, 1), (5, 0, 2)]
 FEATURE_TS = [0.05, 0.3, 0.61, 0.9]
 
@@ -85,6 +115,9 @@ def main():
     R = orc.Reference()
     if sys.argv[1:] == ["features"]:
         np.savez_compressed(os.path.join(HERE, "features.npz"), **features_case(R))
+        return
+    if sys.argv[1:] == ["edges"]:
+        np.savez_compressed(os.path.join(HERE, "edges.npz"), **edges_case(R))
         return
     L = R.lib
     rng = np.random.default_rng(2024)
@@ -133,6 +166,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "fluid.npz"), init=P, gsx=gsx, gsy=gsy, freedom=4.0,
                         step1=steps[0], step8=steps[-1])
     np.savez_compressed(os.path.join(HERE, "features.npz"), **features_case(R))
+    np.savez_compressed(os.path.join(HERE, "edges.npz"), **edges_case(R))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -130,3 +130,24 @@ def test_live_reference_pin_render_options(oracle):
         st.update(feather=opts[0], keep_background=opts[1], show_blobs=opts[2])
         for t in (0.2, 0.55, 0.85):
             assert np.array_equal(oracle.render(st, t), R.render(t)), (opts, t)
+
+
+@pytest.mark.parametrize("name", ["empty_middle", "single", "mixed_sizes"])
+def test_edge_inputs_render_like_reference(oracle, name):
+    """An all-transparent key frame, one key frame, key frames of different
+    sizes: the oracle draws the reference's frames from its chains."""
+    from oracle.oracle import stored_frames
+    g = golden("edges")
+    frames = [f[:h, :w] for f, (h, w) in zip(g[f"{name}_frames"], g[f"{name}_sizes"])]
+    colors, present = stored_frames(frames, 0, oracle)
+    K = len(frames)
+    H, W = g[f"{name}_frames"].shape[1:3]
+    pts = [np.nonzero(f[..., 3]) for f in frames]
+    bx = [int(p[1].min()) for p in pts if len(p[1])] + [int(p[1].max()) for p in pts if len(p[1])]
+    by = [int(p[0].min()) for p in pts if len(p[0])] + [int(p[0].max()) for p in pts if len(p[0])]
+    st = dict(K=K, width=W, height=H, bbox=np.array([min(bx), min(by), max(bx), max(by)], np.uint32), seed=4,
+              motion=3, fading=6, delimiter=0, density=1, colors=colors, present=present,
+              widths=g[f"{name}_widths"], pts=g[f"{name}_pts"], blob_order=g[f"{name}_blob_order"],
+              frame_keys=np.arange(K, dtype=np.uint64))
+    for t, ref in zip(g["ts"], g[f"{name}_renders"]):
+        assert np.array_equal(oracle.render(st, float(t)), ref), f"{name} t={t}"
