@@ -86,6 +86,7 @@ _SIGS = {
     "am_get_time": (C.c_double, [vp, C.c_size_t, C.c_size_t]),
     "am_get_average_pixel": (C.c_int, [vp, C.c_size_t, C.POINTER(C.c_uint16), u8p]),
     "am_get_blob_average": (C.c_int, [vp, C.c_size_t, C.c_size_t, C.POINTER(C.c_uint16), u8p]),
+    "am_get_blob_labels": (C.c_int, [vp, C.c_size_t, i32p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "am_get_atom_count": (C.c_size_t, [vp]),
     "am_get_chain_count": (C.c_size_t, [vp]),
     "am_render": (C.c_int, [vp, C.c_double, vp, C.c_int]),
@@ -204,6 +205,14 @@ class Morph:
             else:
                 _check(f(self.h, v), "am_set_" + k)
         return self
+
+    def blob_labels(self, frame: int) -> np.ndarray:
+        """[h, w] blob index of every canvas pixel of key frame `frame` (-1: none)."""
+        w, h = C.c_uint32(), C.c_uint32()
+        _check(self.lib.am_get_blob_labels(self.h, frame, None, C.byref(w), C.byref(h)), "am_get_blob_labels")
+        out = np.zeros((h.value, w.value), np.int32)
+        _check(self.lib.am_get_blob_labels(self.h, frame, _p(out, i32p), None, None), "am_get_blob_labels")
+        return out
 
     def fluid_particles(self) -> np.ndarray:
         """[18, n] particle fields of the morph's fluid (oracle order)."""

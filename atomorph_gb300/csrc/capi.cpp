@@ -277,6 +277,20 @@ int am_get_average_pixel(const am_morph *m, size_t frame, uint16_t *xy, uint8_t 
     }
     return AM_OK;
 }
+int am_get_blob_labels(am_morph *m, size_t frame, int32_t *labels, uint32_t *w, uint32_t *h) {
+    CHECK(m);
+    Engine &e = H(m);
+    if (e.is_busy()) return AM_ERR_BUSY;
+    const long i = frame_index(e, frame);
+    if (i < 0 || (size_t)i >= e.blobs.size()) return AM_ERR_NOT_FOUND;
+    if (w) *w = e.CW;
+    if (h) *h = e.CH;
+    if (!labels) return AM_OK;
+    const size_t fr = (size_t)e.CW * e.CH;
+    if (!e.d_labels.p || e.d_labels.n < (size_t)(i + 1) * fr) return AM_ERR_STATE;
+    AMG_CUDA(cudaMemcpy(labels, e.d_labels.p + (size_t)i * fr, fr * 4, cudaMemcpyDeviceToHost));
+    return AM_OK;
+}
 int am_get_blob_average(const am_morph *m, size_t frame, size_t blob, uint16_t *xy, uint8_t *rgba) {
     if (!m) return AM_ERR_ARG;
     long i = frame_index(m->e, frame);

@@ -354,6 +354,32 @@ int Engine::detect() {
         std::vector<unsigned long long> st((size_t)nb * 7);
         if (nb) AMG_CUDA(cudaMemcpyAsync(st.data(), d_stats.p, st.size() * 8, cudaMemcpyDeviceToHost, stream));
         AMG_CUDA(cudaStreamSynchronize(stream));
+        // The components are blobify's result when every colour distance is
+        // within the threshold, nothing is below the minimum size or above
+        // the maximum, and blob_number does not stop the merging earlier;
+        // otherwise the merge rules run (k_blobs.cu, merge_blobs).
+        unsigned long long largest = 0;
+        for (uint32_t b = 0; b < nb; ++b) largest = std::max(largest, st[(size_t)b * 7]);
+        if (!(active.threshold >= 1.0 && active.min_size <= 1 && active.blob_number <= nb &&
+              active.max_size >= largest)) {
+            BlobRules br;
+            br.threshold = active.threshold;
+            br.blob_number = active.blob_number;
+            br.min_size = active.min_size;
+            br.max_size = active.max_size;
+            br.box_samples = active.box_samples;
+            br.box_grip = active.box_grip;
+            br.seed = (uint32_t)mix64(((uint64_t)seed << 16) ^ k);
+            rc = merge_blobs(bw, d_present.p + k * fr, d_stored.p + k * fr, CW, CH, br, d_labels.p + k * fr, &nb,
+                             stream);
+            if (rc) return rc;
+            if ((rc = d_stats.reserve(std::max<size_t>((size_t)nb * 7, 7)))) return rc;
+            rc = blob_stats(bw, d_labels.p + k * fr, d_stored.p + k * fr, CW, CH, nb, d_stats.p, stream);
+            if (rc) return rc;
+            st.assign((size_t)nb * 7, 0);
+            if (nb) AMG_CUDA(cudaMemcpyAsync(st.data(), d_stats.p, st.size() * 8, cudaMemcpyDeviceToHost, stream));
+            AMG_CUDA(cudaStreamSynchronize(stream));
+        }
         std::vector<Blob> &bl = blobs[k];
         bl.resize(nb);
         for (uint32_t b = 0; b < nb; ++b) {

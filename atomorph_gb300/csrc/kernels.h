@@ -292,6 +292,18 @@ void blob_work_destroy(BlobWork *w);
 // 4-connected components of one key frame's present pixels: labels (blob
 // index by first pixel in row-major order, -1 absent) and per-blob exact sums
 // {count, sum x, sum y, sum r, sum g, sum b, sum a} of the stored colour.
+// blobify / unify settings (morph.h:53-58).
+struct BlobRules {
+    double threshold = 1.0;
+    size_t blob_number = 1, min_size = 1, max_size = SIZE_MAX, box_samples = 100;
+    uint32_t box_grip = 65535;
+    uint32_t seed = 0;
+};
+// Blobs by the reference's merge rules outside the component regime (parallel
+// agglomeration rounds, then dust unification); labels and count as
+// label_components gives them.
+int merge_blobs(BlobWork *w, const uint8_t *present, const uint32_t *stored, uint32_t CW, uint32_t CH,
+                const BlobRules &p, int32_t *labels, uint32_t *nblobs, cudaStream_t s);
 int label_components(BlobWork *w, const uint8_t *present, const uint32_t *stored, uint32_t CW, uint32_t CH,
                      int32_t *labels, uint32_t *nblobs, cudaStream_t s);
 int blob_stats(BlobWork *w, const int32_t *labels, const uint32_t *stored, uint32_t CW, uint32_t CH,

@@ -167,6 +167,11 @@ uint16_t am_get_height(const am_morph *m);                    /* morph.h:36 */
 double   am_get_time(const am_morph *m, size_t i, size_t n);  /* morph::get_time morph.cpp:1522-1538 */
 /* morph::get_average_pixel(f) morph.cpp:339-354: x, y, r, g, b, a (RGB). */
 int      am_get_average_pixel(const am_morph *m, size_t frame, uint16_t *xy, uint8_t *rgba);
+/* The blobs of key frame `frame` after detection (morph::get_blob's surface
+ * sets, morph.h:31): labels[y * w + x] = index of the blob holding pixel
+ * (x, y), -1 where the frame has no pixel; w, h = the key-frame canvas.  With
+ * labels NULL only w and h are written.  AM_ERR_BUSY while the worker runs. */
+int      am_get_blob_labels(am_morph *m, size_t frame, int32_t *labels, uint32_t *w, uint32_t *h);
 /* morph::get_average_pixel(f, b) morph.cpp:356-376. */
 int      am_get_blob_average(const am_morph *m, size_t frame, size_t blob, uint16_t *xy, uint8_t *rgba);
 size_t   am_get_atom_count(const am_morph *m);                /* total chain width (atoms per key frame) */

@@ -19,8 +19,9 @@ Fixtures (all small, seeded):
 
   edges.npz       edge inputs: an all-transparent key frame, a single key
                   frame, key frames of different sizes (counts, chains, frames)
+  blob_rules.npz  blob counts under blob_threshold / number / min / max size
 
-    python tests/golden/make_golden.py features   # one fixture only (or: edges)
+    python tests/golden/make_golden.py features   # one fixture only (or: edges, blob_rules)
 """
 from __future__ import annotations
 
@@ -86,6 +87,27 @@ def edges_case(R):
     return out
 
 
+BLOB_RULES = [(0.05, 1, 1, 2**62), (0.12, 1, 1, 2**62), (1.0, 60, 1, 2**62), (0.12, 1, 8, 2**62),
+              (1.0, 1, 1, 200), (0.08, 30, 4, 2**62)]
+
+
+def blob_rules_case(R):
+    """Blob detection outside the component regime (blob_threshold,
+    blob_number, blob_min_size, blob_max_size; thread.cpp:225-585): the
+    reference's real blob count per key frame for each setting, on two noisy
+    96x96 key frames (RGB delimiter)."""
+    rng = np.random.default_rng(12)
+    frames = [synth.shapes_frame(96, 6, 0.5, rng) for _ in range(2)]
+    counts = []
+    for thr, bn, mn, mx in BLOB_RULES:
+        R.new(frames, seed=3, motion=3, fading=3, delimiter=0, density=1, threshold=thr, blob_number=bn)
+        R.lib.ref_set_blob_min_size(R.h, mn)
+        R.lib.ref_set_blob_max_size(R.h, mx)
+        R.prepare()
+        counts.append([sum(1 for g, s, xy in R.blobs(f) if s > 0) for f in range(2)])
+    return dict(frames=np.stack(frames), rules=np.array(BLOB_RULES, dtype=np.float64), counts=np.array(counts))
+
+
 FEATURE_OPTIONS = [(0, 0, 0), (0, 0, 1), (0, 0, 2), (0, 1, 0), (3, 0, 0), (2, 1, 0), (1, 1, 1), (5, 0, 2)]
 FEATURE_TS = [0.05, 0.3, 0.61, 0.9]
 
@@ -118,6 +140,9 @@ def main():
         return
     if sys.argv[1:] == ["edges"]:
         np.savez_compressed(os.path.join(HERE, "edges.npz"), **edges_case(R))
+        return
+    if sys.argv[1:] == ["blob_rules"]:
+        np.savez_compressed(os.path.join(HERE, "blob_rules.npz"), **blob_rules_case(R))
         return
     L = R.lib
     rng = np.random.default_rng(2024)
@@ -167,6 +192,7 @@ def main():
                         step1=steps[0], step8=steps[-1])
     np.savez_compressed(os.path.join(HERE, "features.npz"), **features_case(R))
     np.savez_compressed(os.path.join(HERE, "edges.npz"), **edges_case(R))
+    np.savez_compressed(os.path.join(HERE, "blob_rules.npz"), **blob_rules_case(R))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
