@@ -65,8 +65,12 @@ struct RenderWork {
     uint64_t rec_cap = 0;
     uint32_t *tile_cnt = nullptr, *tile_off = nullptr, *tile_cur = nullptr;
     uint32_t ntiles_cap = 0;
-    unsigned *bar = nullptr;   // grid barrier of the fused splat + binning launch
-    int *err = nullptr;        // its bounded-wait failure flag
+    // tile regions of the fused binning, planned from the previous frame
+    uint32_t *p_off = nullptr, *p_cap = nullptr, *p_cnt = nullptr, *ovf_cnt = nullptr, *zero = nullptr;
+    uint32_t plan_tiles = 0;   // tiles the plan is for (0: none yet)
+    uint64_t plan_atoms = 0;   // atom capacity the record buffers were sized for
+    uint4 *ovf = nullptr;
+    uint64_t ovf_cap = 0;
     int *perm = nullptr;    // [2][512] Perlin permutations on the device
     bool perm_set = false;
     Prof *prof = nullptr;   // optional per-kernel timing
@@ -111,8 +115,9 @@ void render_work_destroy(RenderWork *w) {
     if (w->tile_off) cudaFree(w->tile_off);
     if (w->tile_cur) cudaFree(w->tile_cur);
     if (w->perm) cudaFree(w->perm);
-    if (w->bar) cudaFree(w->bar);
-    if (w->err) cudaFree(w->err);
+    void *pl[] = {w->p_off, w->p_cap, w->p_cnt, w->ovf_cnt, w->zero, w->ovf};
+    for (void *q : pl)
+        if (q) cudaFree(q);
     delete w;
 }
 
@@ -415,32 +420,30 @@ __global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs f
 }
 
 // ---------------------------------------------------------------------------
-// Fused splat + binning: one cooperative launch per frame.  Each CTA splats
-// a contiguous chunk of `per` x 256 atoms (the pair records are sorted by
-// the tile of the path midpoint, so a chunk touches few tiles), keeps the
-// records in shared memory, counts them per tile in a shared histogram and
-// reserves its share of every tile it touches with one global atomic per
-// tile (the returned count is its offset inside the tile).  After a grid
-// barrier — whose last arriving CTA turns the tile counts into tile offsets
-// and clears the counts for the next frame — every CTA writes its records
-// straight to their tiles.  No splat buffer, no separate scan kernel.
-// The barrier waits are bounded (kBinBarrierTries polls): a CTA that gives
-// up sets the error flag and the abort flag and every CTA leaves.
+// Fused splat + binning without waiting for other CTAs.  Each tile owns a
+// region of the record buffer planned from the previous frame's tile counts
+// (atoms move continuously from frame to frame, so the counts change little;
+// k_tile_plan sizes the regions with slack).  A CTA splats a contiguous chunk
+// of atoms into shared memory, counts its records per tile, reserves its
+// share of every tile it touches with one global atomic per tile and writes
+// the records straight into the tiles' regions; records past a region's
+// capacity go to the overflow list, tile in bits 20-31 of .y, which the
+// resolve also reads.  No grid barrier, no scan in the frame's path.
 constexpr int kBinThreads = 256;
 constexpr uint32_t kBinMaxTiles = 2048;
-constexpr uint32_t kBinBarrierTries = 1u << 24;
+constexpr uint32_t kBinPer = 2;        // records per thread held in shared memory
 
 struct BinArgs {
     RenderScene sc;
     FrameArgs fa;
     const uint32_t *n;      // atoms of the pair (device; the grid covers an upper bound)
-    uint32_t per;           // atoms per thread (records kept in shared memory)
     SplatIn in;
-    uint4 *rec;
-    uint32_t *tile_cnt;     // [ntiles] zero on entry, zero again on exit
-    uint32_t *tile_off;     // [ntiles + 1] out: exclusive scan of the counts
-    unsigned *bar;          // [0] arrivals, [1] generation, [2] abort
-    int *err;
+    uint4 *rec;             // tile regions
+    const uint32_t *off, *cap;  // [ntiles] region start and capacity
+    uint32_t *cnt;          // [ntiles] records reserved; zero on entry
+    uint4 *ovf;             // overflow records
+    uint32_t *ovf_cnt;      // zero on entry
+    uint32_t ovf_cap;
 };
 
 // Dynamic shared memory of k_frame_bin: records [per][256] uint4, tile
@@ -451,21 +454,20 @@ inline size_t bin_smem(uint32_t per, uint32_t ntiles) {
 
 constexpr uint32_t kNoAtom = 0xFFFFFFFFu;  // X of a record slot past the last atom
 
-__global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(BinArgs b) {
+__global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
     extern __shared__ __align__(16) unsigned char bsm[];
-    const uint32_t ntiles = b.fa.ntiles, tid = threadIdx.x, per = b.per;
+    const uint32_t ntiles = b.fa.ntiles, tid = threadIdx.x, per = kBinPer;
     uint4 *srec = reinterpret_cast<uint4 *>(bsm);
     uint32_t *hist = reinterpret_cast<uint32_t *>(bsm + (size_t)per * kBinThreads * 16);
     uint32_t *base = hist + ntiles;
     uint16_t *fix = reinterpret_cast<uint16_t *>(base + ntiles);
-    __shared__ uint32_t warp_sum[kBinThreads / 32];
     __shared__ uint32_t nfix;
-    __shared__ int s_last, s_ok;
+    const uint64_t chunk0 = (uint64_t)blockIdx.x * per * kBinThreads;
+    const uint64_t n_atoms = *b.n;
+    if (chunk0 >= n_atoms) return;  // past the pair's active atoms
     for (uint32_t t = tid; t < ntiles; t += kBinThreads) hist[t] = 0;
     if (tid == 0) nfix = 0;
     __syncthreads();
-    const uint64_t chunk0 = (uint64_t)blockIdx.x * per * kBinThreads;
-    const uint64_t n_atoms = *b.n;
     // ---- positions by the integer paths.  Axes that need the reference's
     // double formula are listed and evaluated together afterwards, so the
     // slow FP64 work runs in full warps instead of holding up every warp
@@ -516,80 +518,74 @@ __global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(BinArgs b) {
             if (m & (1u << k)) atomicAdd(&hist[tk[k]], 1u);
     }
     __syncthreads();
+    // ---- this CTA's share of every tile it touches
     for (uint32_t t = tid; t < ntiles; t += kBinThreads) {
-        uint32_t h = hist[t];
-        base[t] = h ? atomicAdd(&b.tile_cnt[t], h) : 0u;
-    }
-    // ---- grid barrier; the last CTA scans the counts into offsets
-    __syncthreads();
-    if (tid == 0) {
-        s_ok = 1;
-        __threadfence();
-        s_last = atomicAdd(b.bar, 1u) == gridDim.x - 1;
+        const uint32_t h = hist[t];
+        if (h) hist[t] = atomicAdd(&b.cnt[t], h);
     }
     __syncthreads();
-    if (s_last) {
-        __threadfence();
-        uint32_t carry = 0;
-        for (uint32_t t0 = 0; t0 <= ntiles; t0 += kBinThreads) {
-            const uint32_t t = t0 + tid;
-            const uint32_t v = t < ntiles ? *((volatile uint32_t *)b.tile_cnt + t) : 0u;
-            uint32_t x = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                if ((tid & 31) >= (uint32_t)o) x += y;
-            }
-            if ((tid & 31) == 31) warp_sum[tid >> 5] = x;
-            __syncthreads();
-            uint32_t wbase = 0;
-            for (uint32_t w = 0; w < (tid >> 5); ++w) wbase += warp_sum[w];
-            uint32_t total = 0;
-            for (uint32_t w = 0; w < kBinThreads / 32; ++w) total += warp_sum[w];
-            if (t <= ntiles) b.tile_off[t] = carry + wbase + x - v;
-            if (t < ntiles) b.tile_cnt[t] = 0u;
-            carry += total;
-            __syncthreads();
-        }
-        __threadfence();
-        __syncthreads();
-        if (tid == 0) {
-            atomicExch(b.bar, 0u);
-            __threadfence();
-            atomicAdd(b.bar + 1, 1u);
-        }
-    } else if (tid == 0) {
-        // The barrier words are zeroed before every launch and this is the
-        // launch's only barrier: wait for the generation to leave 0.
-        volatile unsigned *gen = b.bar + 1;
-        volatile int *abort_flag = (volatile int *)(b.bar + 2);
-        uint32_t tries = 0;
-        while (*gen == 0u) {
-            if (*abort_flag) { s_ok = 0; break; }
-            if (++tries > kBinBarrierTries) {
-                atomicExch(b.err, AM_ERR_TIMEOUT);
-                atomicExch((int *)(b.bar + 2), 1);
-                s_ok = 0;
-                break;
-            }
-            __nanosleep(64);
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    if (!s_ok) return;
-    // ---- records to their tiles
-    for (uint32_t t = tid; t < ntiles; t += kBinThreads)
-        if (hist[t]) hist[t] = __ldcg(b.tile_off + t) + base[t];
-    __syncthreads();
+    // ---- records into the tiles' regions (the overflow list past capacity)
     for (uint32_t r = 0; r < per; ++r) {
         const uint4 rec = srec[r * kBinThreads + tid];
         uint32_t tk[4];
         uint32_t m = record_tiles(rec, b.fa.tiles_x, tk);
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (m & (1u << k)) b.rec[atomicAdd(&hist[tk[k]], 1u)] = rec;
+        for (int k = 0; k < 4; ++k) {
+            if (!(m & (1u << k))) continue;
+            const uint32_t t = tk[k], pos = atomicAdd(&hist[t], 1u);
+            if (pos < b.cap[t]) {
+                b.rec[b.off[t] + pos] = rec;
+            } else {
+                const uint32_t o = atomicAdd(b.ovf_cnt, 1u);
+                if (o < b.ovf_cap) b.ovf[o] = make_uint4(rec.x, rec.y | (t << 20), rec.z, rec.w);
+            }
+        }
     }
+}
+
+// The next frame's tile regions from this frame's counts (one CTA): capacity
+// count + count / 4 + 32 (or, with init, the atoms spread evenly), regions in
+// tile order, clipped to the buffer; then the counters are cleared.
+__global__ void __launch_bounds__(1024) k_tile_plan(uint32_t *cnt, uint32_t *off, uint32_t *cap, uint32_t ntiles,
+                                                    uint64_t init_atoms, uint64_t rec_cap, uint32_t *ovf_cnt) {
+    __shared__ uint32_t wsum[32];
+    __shared__ unsigned long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t t0 = 0; t0 < ntiles; t0 += 1024) {
+        const uint32_t t = t0 + threadIdx.x;
+        uint32_t c = 0;
+        if (t < ntiles) {
+            const uint64_t seen = init_atoms ? (init_atoms * 5 / 4) / ntiles : cnt[t];
+            const uint64_t want = seen + seen / 4 + 32;
+            c = want < (1ull << 30) ? (uint32_t)want : (1u << 30);
+        }
+        uint32_t x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) >= (uint32_t)o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = x;
+        __syncthreads();
+        unsigned long long run = carry + x - c;
+        for (uint32_t w = 0; w < (threadIdx.x >> 5); ++w) run += wsum[w];
+        if (t < ntiles) {
+            const unsigned long long end = run + c < rec_cap ? run + c : rec_cap;
+            const unsigned long long st = run < rec_cap ? run : rec_cap;
+            off[t] = (uint32_t)st;
+            cap[t] = (uint32_t)(end - st);
+            cnt[t] = 0u;
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) {
+            unsigned long long tot = 0;
+            for (int w = 0; w < 32; ++w) tot += wsum[w];
+            carry += tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *ovf_cnt = 0u;
 }
 
 __global__ void __launch_bounds__(256) k_frame_scatter(const uint4 *__restrict__ spl, const uint32_t *n_dev,
@@ -692,6 +688,32 @@ struct ResolveOpts {
     BgArgs bg;                     // the background under the composite
 };
 
+// Where a frame's binned records are: tile t's region starts at off[t] and
+// holds min(cnt[t], cap[t]) records; records past a region's capacity went
+// to the overflow list with the tile in bits 20-31 of .y.
+struct TileRecs {
+    const uint4 *rec;
+    const uint32_t *off, *cnt, *cap;
+    const uint4 *ovf;
+    const uint32_t *ovf_cnt;
+    uint32_t ovf_cap;
+};
+__device__ __forceinline__ uint32_t ovf_tile(const uint4 &s) { return s.y >> 20; }
+__device__ __forceinline__ uint32_t ovf_total(const TileRecs &r) { return min(*r.ovf_cnt, r.ovf_cap); }
+
+// Calls f(record) for every record of tile t from global memory (its region,
+// then its overflow records), threads striding over them.
+template <class F>
+__device__ __forceinline__ void visit_tile(const TileRecs &r, uint32_t t, F &&f) {
+    const uint32_t beg = r.off[t], n = min(r.cnt[t], r.cap[t]);
+    for (uint32_t j = threadIdx.x; j < n; j += 256) f(r.rec[beg + j]);
+    const uint32_t no = ovf_total(r);
+    for (uint32_t j = threadIdx.x; j < no; j += 256) {
+        const uint4 v = r.ovf[j];
+        if (ovf_tile(v) == t) f(v);
+    }
+}
+
 // Feather layers of the tile's pixels in the rank-`cur` blob (morph.cpp:
 // 625-674): layer[li] = min(feather, d - 1), d the city-block distance to
 // the nearest pixel outside the blob (iterated 4-neighbour erosion peels one
@@ -700,9 +722,8 @@ struct ResolveOpts {
 // of the (2R + 1) x 32 px square window; erosion runs on the bitmap.  Pixels
 // outside the window count as outside the blob: every tile pixel is more
 // than 32 R >= feather pixels from them, so no layer below feather changes.
-__device__ __noinline__ void feather_layers(const uint4 *__restrict__ rec, const uint32_t *__restrict__ tile_off,
-                               uint32_t tiles_x, uint32_t tiles_y, uint32_t tile, uint32_t cur, uint32_t F,
-                               uint32_t *bm, uint8_t *layer) {
+__device__ __noinline__ void feather_layers(const TileRecs &tr, uint32_t tiles_x, uint32_t tiles_y, uint32_t tile,
+                                            uint32_t cur, uint32_t F, uint32_t *bm, uint8_t *layer) {
     const int R = (int)((F + 31) / 32), WW = 2 * R + 1, WH = 32 * WW, nw = WW * WH;
     uint32_t *A = bm, *B = bm + nw;
     for (int i = threadIdx.x; i < nw; i += 256) A[i] = 0u;
@@ -715,10 +736,8 @@ __device__ __noinline__ void feather_layers(const uint4 *__restrict__ rec, const
             const int ux = tx + dx, uy = ty + dy;
             if (ux < 0 || uy < 0 || ux >= (int)tiles_x || uy >= (int)tiles_y) continue;
             const uint32_t t2 = (uint32_t)uy * tiles_x + (uint32_t)ux;
-            const uint32_t beg = tile_off[t2], end = tile_off[t2 + 1];
-            for (uint32_t j = beg + threadIdx.x; j < end; j += 256) {
-                const uint4 s = rec[j];
-                if (s.w != cur) continue;
+            visit_tile(tr, t2, [&](const uint4 &s) {
+                if (s.w != cur) return;
                 const int px = (int)(s.x & 0xFFFFu), py = (int)(s.x >> 16);
                 const uint32_t valid = (s.y >> 16) & 15u;
 #pragma unroll
@@ -728,7 +747,7 @@ __device__ __noinline__ void feather_layers(const uint4 *__restrict__ rec, const
                     if (wx < 0 || wy < 0 || wx >= 32 * WW || wy >= WH) continue;
                     atomicOr(&A[wy * WW + (wx >> 5)], 1u << (wx & 31));
                 }
-            }
+            });
         }
     __syncthreads();
     for (uint32_t step = 0; step < F; ++step) {
@@ -761,8 +780,7 @@ __host__ __device__ inline size_t feather_smem(uint32_t F) {
     return 2 * WW * (32 * WW) * 4 + 1024;
 }
 
-__global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restrict__ rec,
-                                                        const uint32_t *__restrict__ tile_off, uint32_t tiles_x,
+__global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant__ TileRecs tr, uint32_t tiles_x,
                                                         uint32_t width, uint32_t height, uint32_t density,
                                                         uint8_t *out, const __grid_constant__ ResolveOpts o) {
     extern __shared__ __align__(16) unsigned char sm[];
@@ -778,8 +796,20 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
     uint32_t *xN = reinterpret_cast<uint32_t *>(xW + 5120);
     const uint32_t tile = blockIdx.x;
     const uint32_t tx0 = (tile % tiles_x) * kTile, ty0 = (tile / tiles_x) * kTile;
-    const uint32_t beg = tile_off[tile], end = tile_off[tile + 1];
-    const uint32_t nrec = end - beg;
+    const uint4 *__restrict__ rec = tr.rec;
+    const uint32_t beg = tr.off[tile], nmain = min(tr.cnt[tile], tr.cap[tile]);
+    // overflow records of this tile (normally none)
+    __shared__ uint32_t s_nov;
+    const uint32_t novf = ovf_total(tr);
+    if (novf) {
+        if (threadIdx.x == 0) s_nov = 0;
+        __syncthreads();
+        uint32_t c = 0;
+        for (uint32_t j = threadIdx.x; j < novf; j += 256) c += ovf_tile(tr.ovf[j]) == tile;
+        if (c) atomicAdd(&s_nov, c);
+        __syncthreads();
+    }
+    const uint32_t nrec = nmain + (novf ? s_nov : 0u);
     const bool feathered = o.feather > 0 && o.show_blobs == AM_TEXTURE;
     uint8_t *flayer = sm + kResolveSmem + (o.feather ? feather_smem(o.feather) - 1024 : 0);
     // thread t owns pixels t, t + 256, t + 512, t + 768 of the tile (rows
@@ -794,12 +824,23 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
         uint32_t mn = 0xFFFFFFFFu;
         if (packed) {
             for (int i = threadIdx.x; i < 6 * 1024; i += 256) pW[i] = 0u;
-            if (cached)
-                for (uint32_t j = threadIdx.x; j < nrec; j += 256) {
+            if (cached) {
+                for (uint32_t j = threadIdx.x; j < nmain; j += 256) {
                     const uint4 v = rec[beg + j];
                     cache[j] = v;
                     mn = min(mn, v.w);
                 }
+                if (novf) {
+                    if (threadIdx.x == 0) s_nov = nmain;
+                    __syncthreads();
+                    for (uint32_t j = threadIdx.x; j < novf; j += 256) {
+                        const uint4 v = tr.ovf[j];
+                        if (ovf_tile(v) != tile) continue;
+                        cache[atomicAdd(&s_nov, 1u)] = v;
+                        mn = min(mn, v.w);
+                    }
+                }
+            }
         } else {
             for (int i = threadIdx.x; i < 5 * 1024; i += 256) xW[i] = 0ull;
             for (int i = threadIdx.x; i < 1024; i += 256) xN[i] = 0u;
@@ -807,8 +848,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
         if (threadIdx.x == 0) s_over = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; }
-        if (!cached)
-            for (uint32_t j = threadIdx.x; j < nrec; j += 256) mn = min(mn, rec[beg + j].w);
+        if (!cached) visit_tile(tr, tile, [&](const uint4 &v) { mn = min(mn, v.w); });
         for (int w = 16; w; w >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, w));
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
         __syncthreads();
@@ -818,8 +858,19 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
         while (cur != 0xFFFFFFFFu) {
             __syncthreads();
             uint32_t nxt = 0xFFFFFFFFu;
-            for (uint32_t j = threadIdx.x; j < nrec; j += 256) {
-                uint4 s = cached ? cache[j] : rec[beg + j];
+            // cached: the tile's records in shared memory; else its region
+            // and then the overflow list (other tiles' entries skipped)
+            const uint32_t iter = cached ? nrec : nmain + novf;
+            for (uint32_t j = threadIdx.x; j < iter; j += 256) {
+                uint4 s;
+                if (cached) {
+                    s = cache[j];
+                } else if (j < nmain) {
+                    s = rec[beg + j];
+                } else {
+                    s = tr.ovf[j - nmain];
+                    if (ovf_tile(s) != tile) continue;
+                }
                 if (s.w != cur) {
                     if (s.w > cur) nxt = min(nxt, s.w);
                     continue;
@@ -856,7 +907,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const uint4 *__restric
             __syncthreads();
             if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nxt;
             if (feathered)
-                feather_layers(rec, tile_off, tiles_x, o.tiles_y, tile, cur, o.feather,
+                feather_layers(tr, tiles_x, o.tiles_y, tile, cur, o.feather,
                                reinterpret_cast<uint32_t *>(sm + kResolveSmem), flayer);
             if (packed) {
                 // more than kPackMax contributions could have wrapped a 32-bit sum
@@ -946,34 +997,6 @@ int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32
     AMG_LAUNCH(k_keyframe_copy, grid, 256, 0, s, display, present, CW, CH, width, height, (uint32_t *)out);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
-}
-
-// Atoms per thread of the fused launch: the smallest count (1..8) whose
-// co-resident grid covers n atoms; 0 when even 8 does not.
-static uint32_t bin_per(uint64_t n, uint32_t ntiles) {
-    static int occ[9];
-    static uint32_t occ_tiles = UINT32_MAX;
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
-    if (occ_tiles != ntiles) {
-        for (int p = 0; p < 9; ++p) occ[p] = -1;
-        occ_tiles = ntiles;
-    }
-    for (uint32_t p = 1; p <= 8; ++p) {
-        if (occ[p] < 0) {
-            size_t smem = bin_smem(p, ntiles);
-            cudaFuncSetAttribute(k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            int o = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_frame_bin, kBinThreads, smem) != cudaSuccess) o = 0;
-            occ[p] = o;
-        }
-        if ((uint64_t)occ[p] * sms * kBinThreads * p >= n) return p;
-    }
-    return 0;
 }
 
 // The cache slot holding pair f (prepared now when it is not there yet).
@@ -1095,16 +1118,46 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
         w->ntiles_cap = ntiles + 1;
     }
-    if (!w->bar) {
-        AMG_CUDA(cudaMalloc(&w->bar, 4 * sizeof(unsigned)));
-        AMG_CUDA(cudaMalloc(&w->err, sizeof(int)));
-        AMG_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), s));
-    }
-    uint64_t need = sc.N * 4 + 16;  // an atom has records in at most 4 tiles
+    const bool fused = ntiles <= kBinMaxTiles;
+    // records: fused, the planned tile regions (about 1.25 x the records of a
+    // frame plus slack; at most 4 records per atom) and an overflow list of
+    // 4 per atom; separate kernels, 4 per atom
+    const uint64_t need = fused ? sc.N * 5 + (uint64_t)ntiles * 64 + 16 : sc.N * 4 + 16;
     if (need > w->rec_cap) {
         if (w->rec) cudaFree(w->rec);
+        w->rec = nullptr;
         w->rec_cap = need + need / 4;
         AMG_CUDA(cudaMalloc(&w->rec, w->rec_cap * sizeof(uint4)));
+        w->plan_tiles = 0;
+    }
+    if (fused) {
+        if (!w->zero) {
+            AMG_CUDA(cudaMalloc(&w->zero, 4));
+            AMG_CUDA(cudaMemsetAsync(w->zero, 0, 4, s));
+            AMG_CUDA(cudaMalloc(&w->ovf_cnt, 4));
+        }
+        if (sc.N * 4 + 16 > w->ovf_cap) {
+            if (w->ovf) cudaFree(w->ovf);
+            w->ovf = nullptr;
+            w->ovf_cap = sc.N * 4 + 16;
+            AMG_CUDA(cudaMalloc(&w->ovf, w->ovf_cap * sizeof(uint4)));
+        }
+        if (w->plan_tiles != ntiles || w->plan_atoms != sc.N) {
+            uint32_t **arrs[] = {&w->p_off, &w->p_cap, &w->p_cnt};
+            for (uint32_t **q : arrs) {
+                if (*q) cudaFree(*q);
+                *q = nullptr;
+                AMG_CUDA(cudaMalloc(q, (size_t)ntiles * 4));
+            }
+            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, s, w->p_cnt, w->p_off, w->p_cap, ntiles, std::max<uint64_t>(sc.N, 1),
+                       w->rec_cap, w->ovf_cnt);
+            w->plan_tiles = ntiles;
+            w->plan_atoms = sc.N;
+        }
+    } else if (!w->zero) {
+        AMG_CUDA(cudaMalloc(&w->zero, 4));
+        AMG_CUDA(cudaMemsetAsync(w->zero, 0, 4, s));
+        AMG_CUDA(cudaMalloc(&w->ovf_cnt, 4));
     }
     FrameArgs fa;
     {
@@ -1116,20 +1169,23 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     // atoms of the pair: at most N; the active count stays on the device
     uint64_t n = sc.N;
     SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx};
-    uint32_t per = n && ntiles <= kBinMaxTiles ? bin_per(n, ntiles) : 0;
-    if (n && ntiles <= kBinMaxTiles && per) {
-        // fused splat + binning (one cooperative launch)
+    TileRecs tr;
+    if (fused) {
         BinArgs b;
-        b.sc = sc; b.fa = fa; b.n = pd->d_active; b.per = per; b.in = in; b.rec = w->rec;
-        b.tile_cnt = w->tile_cnt; b.tile_off = w->tile_off; b.bar = w->bar; b.err = w->err;
-        AMG_CUDA(cudaMemsetAsync(w->bar, 0, 4 * sizeof(unsigned), s));
-        unsigned grid = (unsigned)((n + (uint64_t)per * kBinThreads - 1) / ((uint64_t)per * kBinThreads));
-        void *params[] = {&b};
+        b.sc = sc; b.fa = fa; b.n = pd->d_active; b.in = in; b.rec = w->rec;
+        b.off = w->p_off; b.cap = w->p_cap; b.cnt = w->p_cnt;
+        b.ovf = w->ovf; b.ovf_cnt = w->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->ovf_cap, UINT32_MAX);
+        const unsigned grid = (unsigned)((n + (uint64_t)kBinPer * kBinThreads - 1) / ((uint64_t)kBinPer * kBinThreads));
+        static bool battr = false;
+        if (!battr) {
+            AMG_CUDA(cudaFuncSetAttribute(k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)bin_smem(kBinPer, kBinMaxTiles)));
+            battr = true;
+        }
         if (w->prof) w->prof->open(s);
-        AMG_CUDA(cudaLaunchCooperativeKernel((const void *)k_frame_bin, dim3(grid), dim3(kBinThreads), params,
-                                             bin_smem(per, ntiles), s));
-        g_launches.fetch_add(1, std::memory_order_relaxed);
+        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bin_smem(kBinPer, ntiles), s, b);
         if (w->prof) w->prof->close(PROF_BIN, s);
+        tr = TileRecs{w->rec, w->p_off, w->p_cnt, w->p_cap, w->ovf, w->ovf_cnt, b.ovf_cap};
     } else {
         AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
         if (n) {
@@ -1153,7 +1209,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
             AMG_LAUNCH(k_frame_scatter, grid, 256, 0, s, w->spl, pd->d_active, tiles_x, w->tile_cur, w->rec);
             if (w->prof) w->prof->close(PROF_SCATTER, s);
         }
-        AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));  // the fused path expects zero counts
+        tr = TileRecs{w->rec, w->tile_off, w->tile_cnt, w->tile_cnt, w->rec, w->zero, 0u};
     }
     ResolveOpts o;
     std::memset(&o, 0, sizeof(o));
@@ -1172,9 +1228,13 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
             attr = true;
         }
     }
-    AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem + feather_smem(o.feather), s, w->rec, w->tile_off, tiles_x,
-               sc.width, sc.height, sc.density ? sc.density : 1u, out, o);
+    AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem + feather_smem(o.feather), s, tr, tiles_x, sc.width,
+               sc.height, sc.density ? sc.density : 1u, out, o);
     if (w->prof) w->prof->close(PROF_RESOLVE, s);
+    // the next frame's tile regions from this frame's counts
+    if (fused)
+        AMG_LAUNCH(k_tile_plan, 1, 1024, 0, s, w->p_cnt, w->p_off, w->p_cap, ntiles, (uint64_t)0, w->rec_cap,
+                   w->ovf_cnt);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }

@@ -147,3 +147,22 @@ def test_render_perlin_step_ramp_matches_oracle(capi, oracle, motion):
         got = m.render(t)
         worst, ndiff = _lsb(got, ref)
         assert worst <= 1, f"t={t}: worst {worst}, {ndiff} channels differ"
+
+
+def test_render_independent_of_frame_order(capi):
+    """Tile regions are planned from the previous frame's counts; records past
+    a region's capacity take the overflow list.  Frames rendered in a shuffled
+    order (large jumps, so regions misfit and overflow) equal the same frames
+    rendered in time order."""
+    frames = synth.workload("shapes256")
+    m = capi.Morph()
+    m.load(frames, seed=2, blob_delimiter=1, motion=capi.SPLINE, fading=capi.PERLIN)
+    assert m.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+    m.refine(10)
+    ts = [i / 16 for i in range(16)]
+    forward = {t: m.render(t) for t in ts}
+    order = np.random.default_rng(4).permutation(len(ts))
+    for k in order:
+        t = ts[k]
+        assert np.array_equal(m.render(t), forward[t]), t
+    m.close()
