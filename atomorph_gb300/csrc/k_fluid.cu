@@ -182,8 +182,9 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
         return;
     }
     const int x0 = box[0], y0 = box[1], bh = box[3], nn = box[2] * bh;
-    for (int k = threadIdx.x; k < kQ * kPrivNodes; k += kFlThreads)
-        if ((k % kPrivNodes) < nn) acc[k] = 0.f;
+    for (int q = threadIdx.x; q < nn; q += kFlThreads)
+#pragma unroll
+        for (int f = 0; f < kQ; ++f) acc[f * kPrivNodes + q] = 0.f;
     __syncthreads();
     if (act) {
 #pragma unroll
