@@ -12,6 +12,7 @@
 #include "fluid.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -979,6 +980,7 @@ int Engine::ensure_local_index() {
     if ((rc = d_cell_start.reserve((size_t)K * (ncells + 1)))) return rc;
     if ((rc = d_chain_id.reserve(N))) return rc;
     if ((rc = d_chain_w1.reserve(std::max<uint32_t>(C, 1)))) return rc;
+    if ((rc = d_slot_ch.reserve(N * K))) return rc;
     if ((rc = d_claim.reserve(N * maxph))) return rc;
     if ((rc = d_pgain.reserve(N * maxph))) return rc;
     if ((rc = d_lprop.reserve(N * maxph))) return rc;
@@ -994,7 +996,7 @@ int Engine::ensure_local_index() {
     for (uint32_t c = 0; c < C; ++c) w1[c] = widths[c] <= 1;
     AMG_CUDA(cudaMemcpyAsync(d_chain_w1.p, w1.data(), w1.size(), cudaMemcpyHostToDevice, stream));
     lix.slot_pt = d_slot_pt.p; lix.col = d_col.p; lix.slot_of = d_slot_of.p; lix.cell_start = d_cell_start.p;
-    lix.chain_id = d_chain_id.p; lix.chain_w1 = d_chain_w1.p; lix.sv = d_sv.p;
+    lix.chain_id = d_chain_id.p; lix.chain_w1 = d_chain_w1.p; lix.slot_ch = d_slot_ch.p; lix.sv = d_sv.p;
     rc = local_index_build(lix, d_P.p, N, K, CW, CH, d_chain_off.p, C, d_lk.p, d_lv.p, d_tk.p, d_tv.p, d_hist.p,
                            stream);
     if (rc) return rc;
@@ -1007,15 +1009,14 @@ int Engine::ensure_local_index() {
 // full guided sweep, so it must keep at least that share of a full sweep's
 // gain.  The policy alternates one measured full block and one measured
 // gated block, then runs four blocks of the better one, and measures again.
-void Engine::learned_gate_next(double gain_per_sweep) {
-    constexpr double kGatedCost = 0.75;  // gated / full sweep time, measured at 1M atoms, keep 1/4
+void Engine::learned_gate_next(double gain_per_s) {
     switch (lg_state) {
     case LG_MEASURE_FULL:
-        lg_full_rate = gain_per_sweep;
+        lg_full_rate = gain_per_s;
         lg_state = LG_MEASURE_GATED;
         break;
     case LG_MEASURE_GATED:
-        lg_state = gain_per_sweep >= kGatedCost * lg_full_rate ? LG_GATED : LG_FULL;
+        lg_state = gain_per_s >= lg_full_rate ? LG_GATED : LG_FULL;
         lg_left = 4;
         break;
     default:
@@ -1049,6 +1050,7 @@ int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
         const size_t nb = std::min(kBlock, sweeps - done);
         const bool gated = learned && (recording || !active.learned_adaptive || lg_state == LG_MEASURE_GATED ||
                                        lg_state == LG_GATED);
+        const auto t_block = std::chrono::steady_clock::now();
         AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * nb * 8, stream));
         for (size_t s = 0; s < nb; ++s) {
             uint32_t pofs = 0;
@@ -1056,8 +1058,8 @@ int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
                 LocalArgs a;
                 a.P = d_P.p; a.N = N; a.K = K; a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
                 a.slot_pt = lix.slot_pt; a.col = lix.col; a.slot_of = lix.slot_of; a.cell_start = lix.cell_start;
-                a.ncx = lix.ncx; a.ncy = lix.ncy; a.ncells = lix.ncells; a.chain_id = lix.chain_id;
-                a.chain_w1 = lix.chain_w1; a.cap = active.local_target;
+                a.ncx = lix.ncx; a.ncy = lix.ncy; a.ncells = lix.ncells; a.slot_ch = lix.slot_ch;
+                a.cap = active.local_target;
                 a.self_cap = active.local_self; a.nrandom = active.local_random; a.chain_off = d_chain_off.p;
                 a.key = mix64(((uint64_t)seed << 40) ^ (sweep_counter << 4) ^ p ^ 0x5bd1e995ULL);
                 a.claim = d_claim.p; a.prop = d_lprop.p; a.pgain = d_pgain.p; a.sv = d_sv.p; a.hot = d_hot.p;
@@ -1091,7 +1093,10 @@ int Engine::refine_guided(size_t sweeps, uint64_t *gains) {
             block_gain += (double)acc[2 * s];
             if (gains) gains[done + s] = acc[2 * s];
         }
-        if (learned && !recording) learned_gate_next(block_gain / (double)nb);
+        if (learned && !recording) {
+            const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_block).count();
+            learned_gate_next(block_gain / std::max(dt, 1e-9));
+        }
         done += nb;
     }
     return AM_OK;

@@ -170,7 +170,7 @@ class Engine {
     LocalIndex lix;
     bool local_valid = false;
     DBuf<uint64_t> d_slot_pt;
-    DBuf<uint32_t> d_col, d_slot_of, d_cell_start, d_chain_id, d_lprop, d_lk, d_lv;
+    DBuf<uint32_t> d_col, d_slot_of, d_cell_start, d_chain_id, d_slot_ch, d_lprop, d_lk, d_lv;
     DBuf<uint8_t> d_chain_w1;
     DBuf<unsigned long long> d_claim, d_pgain, d_nsel;
     DBuf<uint64_t> d_sv;
@@ -215,7 +215,7 @@ class Engine {
     enum { LG_MEASURE_FULL, LG_MEASURE_GATED, LG_GATED, LG_FULL };
     int lg_state = LG_MEASURE_FULL, lg_left = 0;
     double lg_full_rate = 0.0;
-    void learned_gate_next(double gain_per_sweep);
+    void learned_gate_next(double gain_per_s);
     int copy_keyframe(size_t f, uint8_t *dst);
     unsigned active_seed_mix() const;
     int status = AM_OK;                    // first failure inside the worker

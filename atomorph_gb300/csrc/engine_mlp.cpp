@@ -87,23 +87,25 @@ int Engine::train_proposal(const float *feat, const float *gains, size_t n, size
     if ((rc = d_io_b.reserve(n))) return rc;
     AMG_CUDA(cudaMemcpyAsync(d_io_a.p, feat, n * kMlpIn * 4, cudaMemcpyHostToDevice, stream));
     AMG_CUDA(cudaMemcpyAsync(d_io_b.p, gains, n * 4, cudaMemcpyHostToDevice, stream));
-    const size_t batch = 16384;
+    const size_t batch = 16384, steps = (n + batch - 1) / batch;
+    // one loss slot per minibatch, read once per epoch
+    if ((rc = d_mlp_loss.reserve(steps))) return rc;
+    std::vector<float> losses(steps);
     double last = 0.0;
     for (size_t e = 0; e < epochs; ++e) {
-        double sum = 0.0;
-        for (size_t b = 0; b < n; b += batch) {
-            size_t m = std::min(batch, n - b);
+        for (size_t k = 0; k < steps; ++k) {
+            const size_t b = k * batch, m = std::min(batch, n - b);
             ++adam_t;
             prof.open(stream);
             rc = mlp_train_step(d_io_a.p + b * kMlpIn, d_io_b.p + b, m, d_mlp_master.p, d_mlp_dep.p, d_mlp_grad.p,
-                                d_adam_m.p, d_adam_v.p, adam_t, (float)lr, d_mlp_loss.p, d_err.p, stream);
+                                d_adam_m.p, d_adam_v.p, adam_t, (float)lr, d_mlp_loss.p + k, d_err.p, stream);
             if (rc) return rc;
             prof.close(PROF_MLP, stream);
-            float l = 0.f;
-            AMG_CUDA(cudaMemcpyAsync(&l, d_mlp_loss.p, 4, cudaMemcpyDeviceToHost, stream));
-            AMG_CUDA(cudaStreamSynchronize(stream));
-            sum += l;
         }
+        AMG_CUDA(cudaMemcpyAsync(losses.data(), d_mlp_loss.p, steps * 4, cudaMemcpyDeviceToHost, stream));
+        AMG_CUDA(cudaStreamSynchronize(stream));
+        double sum = 0.0;
+        for (float l : losses) sum += l;
         last = sum / (double)n;
         rc = check_err();
         if (rc) return rc;

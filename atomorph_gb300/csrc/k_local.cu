@@ -71,8 +71,11 @@ __global__ void k_chain_ids(const uint64_t *__restrict__ off, uint32_t C, uint64
 // index; afterwards k_local_apply keeps it current: a swap at frame y moves
 // the two columns' sums at frame y to their new slots and changes the two
 // columns' sums at frames y-1 and y+1 by the exchanged points' difference.
+// The same pass records each slot's chain (slot_ch), which no swap changes.
 __global__ void __launch_bounds__(256) k_slot_sums(const uint64_t *__restrict__ P, const uint32_t *__restrict__ col,
-                                                   uint64_t N, uint32_t K, uint64_t *sv) {
+                                                   const uint32_t *__restrict__ chain_id,
+                                                   const uint8_t *__restrict__ chain_w1, uint64_t N, uint32_t K,
+                                                   uint64_t *sv, uint32_t *slot_ch) {
     const uint64_t total = N * K;
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t y = (uint32_t)(t / N);
@@ -80,6 +83,8 @@ __global__ void __launch_bounds__(256) k_slot_sums(const uint64_t *__restrict__ 
         uint32_t x = col[t];
         uint64_t p = P[(uint64_t)yp * N + x], n = P[(uint64_t)yn * N + x];
         sv[t] = sums_pack(pt_X(p) + pt_X(n), pt_Y(p) + pt_Y(n));
+        const uint32_t ch = chain_id[x];
+        slot_ch[t] = chain_w1[ch] ? kNoChain : ch;
     }
 }
 
@@ -151,11 +156,12 @@ __device__ __forceinline__ int64_t propose_one(const LocalArgs &a, uint32_t fi, 
         const uint32_t *col = a.col + (uint64_t)y * N;
         const uint64_t *sv = a.sv + (uint64_t)y * N;
         a.prop[t] = 0xFFFFFFFFu;
-        uint32_t x1 = col[c.s1];
-        uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
-        if (a.chain_w1[ch]) return 0;  // width-1 chains do not refine (thread.cpp:1045)
+        // independent loads: the slot's chain, point, target sum and column
+        const uint32_t ch = a.slot_ch[(uint64_t)y * N + c.s1];
         c.a1 = spt[c.s1];
         c.S1 = sv[c.s1];
+        const uint32_t x1 = col[c.s1];
+        if (ch == kNoChain) return 0;  // width-1 chains do not refine (thread.cpp:1045)
         c.lo = a.single_chain ? 0ull : a.chain_off[ch];
         c.hi = a.single_chain ? N : a.chain_off[ch + 1];
         const uint32_t *cs = a.cell_start + (uint64_t)y * (a.ncells + 1);
@@ -364,7 +370,7 @@ int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K,
     }
     AMG_LAUNCH(k_chain_ids, grid, 256, 0, s, chain_off, C, N, ix.chain_id);
     unsigned g2 = (unsigned)std::min<uint64_t>((N * K + 255) / 256, (uint64_t)kSMs * 8);
-    AMG_LAUNCH(k_slot_sums, g2, 256, 0, s, P, ix.col, N, K, ix.sv);
+    AMG_LAUNCH(k_slot_sums, g2, 256, 0, s, P, ix.col, ix.chain_id, ix.chain_w1, N, K, ix.sv, ix.slot_ch);
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }

@@ -241,6 +241,37 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float *__restrict__ f
 }
 
 // ----------------------------------------------------- training kernel ---
+// Warp sums of 64 values at once (a transposed butterfly: 62 shuffles
+// instead of 320).  Lane l ends with the totals of values i and i + 1,
+// i = 32 b4 + 16 b3 + 8 b2 + 4 b1 + 2 b0 (b_k the lane's bits), returned in
+// v[0], v[1]; the other entries of v are clobbered.
+__device__ __forceinline__ int warp_sum64(float (&v)[64], int lane) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const bool up = lane & o;
+        // 2 o values stay after this level
+#pragma unroll
+        for (int j = 0; j < 2 * o; ++j) {
+            const float send = up ? v[j] : v[j + 2 * o], keep = up ? v[j + 2 * o] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return ((lane >> 4) & 1) * 32 + ((lane >> 3) & 1) * 16 + ((lane >> 2) & 1) * 8 + ((lane >> 1) & 1) * 4 +
+           (lane & 1) * 2;
+}
+// Adds a warp's 64 per-lane vectors into acc[64] (one shared atomic per lane
+// and value pair instead of 32 same-address atomics per value).
+__device__ __forceinline__ void warp_add64(float (&v)[64], float *acc) {
+    const int i = warp_sum64(v, threadIdx.x & 31);
+    atomicAdd(acc + i, v[0]);
+    atomicAdd(acc + i + 1, v[1]);
+}
+__device__ __forceinline__ float warp_sum1(float v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 struct TrainSmem {
     uint8_t A1[kTM * 16 * 2];        // X [b][16]
     uint8_t A2[kTM * 64 * 2];        // H1 [b][64]
@@ -351,17 +382,25 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float *__restrict__ fea
         for (int i = 0; i < 64; ++i) out += fmaxf(z2[i], 0.f) * s.w3[i];
         float e = valid ? out - tgt : 0.f;
         float dout = 2.f * e * inv_n;
-        atomicAdd(&s.loss, e * e);
-        atomicAdd(&s.gb3, dout);
+        {
+            const float l = warp_sum1(e * e), d = warp_sum1(dout);
+            if ((r & 31) == 0) {
+                atomicAdd(&s.loss, l);
+                atomicAdd(&s.gb3, d);
+            }
+        }
+        float acc[64];
+#pragma unroll
+        for (int i = 0; i < 64; ++i) acc[i] = dout * fmaxf(z2[i], 0.f);
+        warp_add64(acc, s.gw3);
 #pragma unroll
         for (int i = 0; i < 64; ++i) {
-            float h2 = fmaxf(z2[i], 0.f);
             float g = z2[i] > 0.f ? dout * s.w3[i] : 0.f;
-            if (h2 != 0.f) atomicAdd(&s.gw3[i], dout * h2);
-            if (g != 0.f) atomicAdd(&s.gb2[i], g);
+            acc[i] = g;
             put_bf16(s.G2, kmaj(r, i, 1024), g);
             put_bf16(s.G2T, kmaj(i, r, 2048), g);
         }
+        warp_add64(acc, s.gb2);
         // dH1 = dZ2 W2  and  dW2 += dZ2^T H1
         fence_async_smem();
         fence_before();
@@ -389,10 +428,11 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float *__restrict__ fea
                 int i = 16 * c + j;
                 float g = (act1[i >> 5] >> (i & 31)) & 1u ? v[j] : 0.f;
                 if (!valid) g = 0.f;
-                if (g != 0.f) atomicAdd(&s.gb1[i], g);
+                acc[i] = g;
                 put_bf16(s.G1T, kmaj(i, r, 2048), g);
             }
         }
+        warp_add64(acc, s.gb1);
         // dW1 += dZ1^T X
         fence_async_smem();
         fence_before();
@@ -486,75 +526,89 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, int n, floa
 //   8    fraction of slots whose target lies in their own cell
 //   9    fraction of slots that can refine (chain wider than 1)
 // Target: log1p(sum of the best gains the full scan found in the region / S^2).
-struct GroupFeat {
-    float f[kMlpIn];
-    bool elig;
+// The seven per-slot terms summed over a region (slot 7 pads to eight).
+enum { kTOk, kTLg, kTHb, kTHit, kTAx, kTAy, kTSame, kTerms = 8 };
+// Raw sums of a region as staged for its owner lane: the eight sums, then
+// the maxima of lg and hb (row padded to 11 floats against bank conflicts).
+constexpr int kRawMaxLg = 8, kRawMaxHb = 9, kRawStride = 11;
+
+// What the features read of one slot (lane = slot of the region).
+struct SlotRaw {
+    uint64_t a1, S1;  // the slot's point and its column's target sum
+    uint32_t ch, h;   // the slot's chain (kNoChain: cannot refine), gain bucket of its last scan
 };
-
-__device__ __forceinline__ float warp_sum_f(float v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ float warp_max_f(float v) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
-// Warp-collective: features of region g (every lane gets them).
-__device__ __forceinline__ GroupFeat group_features(const LocalArgs &a, uint64_t g, uint64_t total) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t t = g * 32 + lane;
-    float lg = 0.f, hb = 0.f, hit = 0.f, ax = 0.f, ay = 0.f, same = 0.f, ok = 0.f;
-    if (t < total) {
-        const uint32_t N32 = (uint32_t)a.N;
-        const uint32_t fi = (uint32_t)t / N32, s1 = (uint32_t)t - fi * N32;  // t < 2^32 (host-checked)
-        const uint32_t y = a.frames[fi];
-        const uint64_t base = (uint64_t)y * a.N + s1;
-        const uint32_t x1 = a.col[base];
-        const uint32_t ch = a.single_chain ? 0u : a.chain_id[x1];
-        if (!a.chain_w1[ch]) {
-            ok = 1.f;
-            const uint64_t a1 = a.slot_pt[base], S1 = a.sv[base];
-            const float dx = (float)pt_X(a1) - 0.5f * (float)sums_x(S1), dy = (float)pt_Y(a1) - 0.5f * (float)sums_y(S1);
-            lg = log1pf((dx * dx + dy * dy) / kS2);
-            const uint8_t h = a.hot[base];
-            hb = (float)h * (1.f / 16.f);
-            hit = h ? 1.f : 0.f;
-            ax = fabsf(dx) / kS;
-            ay = fabsf(dy) / kS;
-            const int32_t mx = sums_x(S1) >> 1, my = sums_y(S1) >> 1;
-            const uint32_t own = (min((uint32_t)pt_Y(a1) >> 9, a.ncy - 1)) * a.ncx + min((uint32_t)pt_X(a1) >> 9, a.ncx - 1);
-            const uint32_t tgt = (min((uint32_t)max(my, 0) >> 9, a.ncy - 1)) * a.ncx + min((uint32_t)max(mx, 0) >> 9, a.ncx - 1);
-            same = own == tgt ? 1.f : 0.f;
-        }
+// Four independent coalesced loads of slot s1 of phase frame fi.
+__device__ __forceinline__ SlotRaw slot_load(const LocalArgs &a, uint32_t fi, uint32_t s1, bool in) {
+    SlotRaw r{0ull, 0ull, kNoChain, 0u};
+    if (in) {
+        const uint64_t base = (uint64_t)a.frames[fi] * a.N + s1;
+        r.ch = a.slot_ch[base];
+        r.a1 = a.slot_pt[base];
+        r.S1 = a.sv[base];
+        r.h = a.hot[base];
     }
-    GroupFeat r;
-    const float n = warp_sum_f(ok);
-    const float inv = n > 0.f ? 1.f / n : 0.f;
-    r.f[0] = warp_sum_f(lg) * inv;
-    r.f[1] = warp_max_f(lg);
-    r.f[2] = warp_sum_f(hb) * inv;
-    r.f[3] = warp_max_f(hb);
-    r.f[4] = warp_sum_f(hit) * inv;
-    r.f[5] = fminf(warp_sum_f(ax) * inv, 8.f);
-    r.f[6] = fminf(warp_sum_f(ay) * inv, 8.f);
-    r.f[7] = a.cost_scale;
-    r.f[8] = warp_sum_f(same) * inv;
-    r.f[9] = n * (1.f / 32.f);
-    r.elig = n > 0.f;
     return r;
 }
+// The slot's terms of its region's features.
+__device__ __forceinline__ void slot_terms(const LocalArgs &a, const SlotRaw &r, float (&v)[kTerms]) {
+#pragma unroll
+    for (int k = 0; k < kTerms; ++k) v[k] = 0.f;
+    if (r.ch == kNoChain) return;
+    const float dx = (float)pt_X(r.a1) - 0.5f * (float)sums_x(r.S1), dy = (float)pt_Y(r.a1) - 0.5f * (float)sums_y(r.S1);
+    v[kTOk] = 1.f;
+    v[kTLg] = __logf(1.f + (dx * dx + dy * dy) * (1.f / kS2));
+    v[kTHb] = (float)r.h * (1.f / 16.f);
+    v[kTHit] = r.h ? 1.f : 0.f;
+    v[kTAx] = fabsf(dx) * (1.f / kS);
+    v[kTAy] = fabsf(dy) * (1.f / kS);
+    const int32_t mx = sums_x(r.S1) >> 1, my = sums_y(r.S1) >> 1;
+    const uint32_t own = (min((uint32_t)pt_Y(r.a1) >> 9, a.ncy - 1)) * a.ncx + min((uint32_t)pt_X(r.a1) >> 9, a.ncx - 1);
+    const uint32_t tgt = (min((uint32_t)max(my, 0) >> 9, a.ncy - 1)) * a.ncx + min((uint32_t)max(mx, 0) >> 9, a.ncx - 1);
+    v[kTSame] = own == tgt ? 1.f : 0.f;
+}
 
-// One CTA scores 128 regions per tile (one MMA tile): warp w computes the
-// features of regions 32w .. 32w+31 of the tile, lane r keeps region
-// 32w + r's row.  While recording, every eligible region is listed and its
-// features logged.
-__global__ void __launch_bounds__(128) k_learned_gate(LocalArgs a) {
+// Warp sum of eight values at once (a transposed butterfly: 9 shuffles
+// instead of 40).  Each lane ends with one total: that of value
+// 4 b4 + 2 b3 + b2, b_i the lane's bits.  Every total is the same
+// xor-butterfly tree a single-value reduction builds, so the sums are
+// bit-identical to eight separate reductions.
+__device__ __forceinline__ float warp_sum8(float (&v)[kTerms], int lane) {
+    const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float send = u16 ? v[j] : v[j + 4], keep = u16 ? v[j + 4] : v[j];
+        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const float send = u8 ? v[j] : v[j + 2], keep = u8 ? v[j + 2] : v[j];
+        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    const float send = u4 ? v[0] : v[1], keep = u4 ? v[1] : v[0];
+    float t = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    t += __shfl_xor_sync(0xffffffffu, t, 2);
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
+    return t;
+}
+// Warp maxima of two values: lanes 0-15 end with max(p), lanes 16-31 with max(q).
+__device__ __forceinline__ float warp_max2(float p, float q, int lane) {
+    const bool u16 = lane & 16;
+    float m = fmaxf(u16 ? q : p, __shfl_xor_sync(0xffffffffu, u16 ? p : q, 16));
+#pragma unroll
+    for (int o = 8; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    return m;
+}
+
+// One CTA scores 128 regions per tile (one MMA tile): warp w reduces the
+// slots of regions 32w .. 32w+31 of the tile, four regions per pass so
+// their loads overlap, and stages each region's raw sums in shared memory;
+// lane r then builds region 32w + r's features.  While recording, every
+// eligible region is listed and its features logged.
+__global__ void __launch_bounds__(128, 4) k_learned_gate(LocalArgs a) {
     extern __shared__ __align__(1024) uint8_t smraw[];
     FwdSmem &s = *reinterpret_cast<FwdSmem *>(smraw);
     __shared__ float sc[kTM];
+    __shared__ float raw[kTM * kRawStride];
     fwd_setup(s, a.mlp);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t total = a.N * a.nframes;
@@ -562,23 +616,70 @@ __global__ void __launch_bounds__(128) k_learned_gate(LocalArgs a) {
     const uint64_t ntiles = (ngroups + kTM - 1) / kTM;
     const int kk = max(1, min(kTM, (int)ceilf(a.keep * (float)kTM)));
     const bool rec = a.rec_idx != nullptr;
+    const uint32_t N32 = (uint32_t)a.N;  // total < 2^32 (host-checked)
+    float *wraw = raw + warp * 32 * kRawStride;
     uint32_t phase = 0;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        float f[kMlpIn];
+        // the warp's first region: slot gw * 32 + lane, then 32 slots further
+        // per region
+        const uint64_t gw = tile * kTM + warp * 32;
+        const uint32_t t0 = (uint32_t)(gw * 32) + lane;
+        uint32_t fi = t0 / N32, s1 = t0 - fi * N32;
+        // the loads of pass p + 1 are issued before pass p's reductions
+        SlotRaw cur[4];
 #pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
-        bool elig = false;
-        for (int r = 0; r < 32; ++r) {
-            const uint64_t g = tile * kTM + warp * 32 + r;
-            if (g >= ngroups) break;  // uniform across the warp
-            const GroupFeat gf = group_features(a, g, total);
-            if (lane == r) {
+        for (int u = 0; u < 4; ++u) {
+            cur[u] = slot_load(a, fi, s1, (gw + u) * 32 + lane < total);
+            s1 += 32;
+            while (s1 >= N32) { s1 -= N32; ++fi; }
+        }
+        for (int r0 = 0; r0 < 32; r0 += 4) {
+            const uint64_t g0 = gw + r0;
+            if (g0 >= ngroups) break;  // uniform across the warp
+            SlotRaw nxt[4];
 #pragma unroll
-                for (int k = 0; k < kMlpIn; ++k) f[k] = gf.f[k];
-                elig = gf.elig;
+            for (int u = 0; u < 4; ++u) {
+                nxt[u] = slot_load(a, fi, s1, r0 + 4 < 32 && (g0 + 4 + u) * 32 + lane < total);
+                s1 += 32;
+                while (s1 >= N32) { s1 -= N32; ++fi; }
+            }
+            float v[4][kTerms];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) slot_terms(a, cur[u], v[u]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) cur[u] = nxt[u];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float mx = warp_max2(v[u][kTLg], v[u][kTHb], lane);
+                const float sum = warp_sum8(v[u], lane);
+                float *row = wraw + (r0 + u) * kRawStride;
+                if ((lane & 3) == 0) row[((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1)] = sum;
+                if (lane == 1) row[kRawMaxLg] = mx;
+                if (lane == 17) row[kRawMaxHb] = mx;
             }
         }
+        __syncwarp();
         const uint64_t g = tile * kTM + threadIdx.x;
+        float f[kMlpIn];
+        bool elig = false;
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
+        if (g < ngroups) {
+            const float *q = wraw + lane * kRawStride;
+            const float n = q[kTOk];
+            const float inv = n > 0.f ? 1.f / n : 0.f;
+            f[0] = q[kTLg] * inv;
+            f[1] = q[kRawMaxLg];
+            f[2] = q[kTHb] * inv;
+            f[3] = q[kRawMaxHb];
+            f[4] = q[kTHit] * inv;
+            f[5] = fminf(q[kTAx] * inv, 8.f);
+            f[6] = fminf(q[kTAy] * inv, 8.f);
+            f[7] = a.cost_scale;
+            f[8] = q[kTSame] * inv;
+            f[9] = n * (1.f / 32.f);
+            elig = n > 0.f;
+        }
         write_features(s.A1, threadIdx.x, f);
         float score = forward_tile(s, phase, a.err);
         bool keep;
@@ -637,8 +738,9 @@ int mlp_deploy(const float *master, float *deployed, cudaStream_t s) {
 
 int mlp_forward(const float *feat, uint64_t n, const float *deployed, float *out, int *err, cudaStream_t s) {
     if (!n) return AM_OK;
-    // >= 56 KB of shared memory keeps at most 4 CTAs (4 x 128 TMEM columns) per SM.
-    size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 56 * 1024);
+    // 48 KB of shared memory (+1 KB the runtime reserves per CTA) lets 4 CTAs
+    // share an SM's 228 KB but not 5: 4 x 128 TMEM columns at most.
+    size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 48 * 1024);
     int rc = set_smem((const void *)k_mlp_forward, smem);
     if (rc) return rc;
     unsigned grid = (unsigned)std::min<uint64_t>((n + kTM - 1) / kTM, (uint64_t)kSMs * 4);
@@ -681,8 +783,9 @@ int launch_learned_phase(const LocalArgs &a, cudaStream_t s) {
     AMG_CUDA(cudaMemsetAsync(a.claim, 0, total * sizeof(unsigned long long), s));
     AMG_CUDA(cudaMemsetAsync(a.nsel_out, 0, sizeof(unsigned long long), s));
     int rc;
-    // >= 56 KB of shared memory keeps at most 4 CTAs (4 x 128 TMEM columns) per SM.
-    size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 56 * 1024);
+    // 44 KB dynamic + 6.1 KB static (scores, raw sums) + 1 KB reserved per
+    // CTA: 4 CTAs share an SM's 228 KB, 5 do not (4 x 128 TMEM columns at most).
+    size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 44 * 1024);
     if ((rc = set_smem((const void *)k_learned_gate, smem))) return rc;
     const uint64_t ngroups = (total + 31) / 32;
     unsigned g = (unsigned)std::min<uint64_t>((ngroups + kTM - 1) / kTM, (uint64_t)kSMs * 4);

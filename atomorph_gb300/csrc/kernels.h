@@ -85,7 +85,11 @@ struct LocalIndex {
     uint64_t *sv = nullptr;                  // [K][N] target sum p + n of the column at slot s
     uint32_t *chain_id = nullptr;            // [N]
     uint8_t *chain_w1 = nullptr;             // [C] 1 for width-1 chains
+    uint32_t *slot_ch = nullptr;             // [K][N] chain of the column at slot s, kNoChain for width-1 chains
 };
+// Swaps stay within a chain and a slot's point never moves, so the chain of
+// the column at a slot is fixed for the life of the index.
+constexpr uint32_t kNoChain = 0xFFFFFFFFu;
 struct LocalArgs {
     uint64_t *P;
     uint64_t N;
@@ -96,8 +100,7 @@ struct LocalArgs {
     uint32_t *col, *slot_of;
     const uint32_t *cell_start;
     uint32_t ncx, ncy, ncells;
-    const uint32_t *chain_id;
-    const uint8_t *chain_w1;
+    const uint32_t *slot_ch;                 // [K][N] chain of the column at each slot (kNoChain: width 1)
     uint32_t cap;                            // candidates from the target cell
     uint32_t self_cap = 12;                  // candidates from the column's own neighbourhood
     uint32_t nrandom = 2;                    // uniform random candidates of the same chain
