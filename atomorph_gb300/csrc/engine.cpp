@@ -8,6 +8,8 @@
 // them, so a paused worker never has GPU work in flight.  synchronize()
 // publishes the worker's results to the front copy that rendering reads
 // (morph.cpp:102-269), so a frame can be rendered while the worker refines.
+#include <cuda.h>
+
 #include "engine.h"
 #include "fluid.cuh"
 
@@ -796,13 +798,54 @@ int Engine::synchronize() {
     return AM_OK;
 }
 
+// Pinned host memory is mapped into the GPU's address space: the device
+// address of [p, p + bytes) when the driver reports p as mapped host memory
+// whose whole allocation covers the range, else nullptr.  Pageable memory,
+// a short pinned buffer or a failed query leave the frame on the copy path.
+static uint8_t *mapped_host_range(uint8_t *p, size_t bytes) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    using GetAttr = CUresult (*)(void *, CUpointer_attribute, CUdeviceptr);
+    static GetAttr get_attr = [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        return reinterpret_cast<GetAttr>(fn);
+    }();
+    if (!get_attr) return nullptr;
+    const CUdeviceptr dp = (CUdeviceptr)(uintptr_t)at.devicePointer;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    if (get_attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, dp) != CUDA_SUCCESS ||
+        get_attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, dp) != CUDA_SUCCESS)
+        return nullptr;
+    if (dp < start || dp - start > size || size - (dp - start) < bytes) return nullptr;
+    return static_cast<uint8_t *>(at.devicePointer);
+}
+
 int Engine::render(double time, uint8_t *out, bool out_dev) {
     int rc = ensure_streams(this);
     if (rc) return rc;
     size_t bytes = (size_t)width * height * 4;
     if (bytes == 0) return AM_OK;
     uint8_t *dst = out;
-    if (!out_dev) {
+    // An atom frame into mapped (pinned) host memory is stored there by the
+    // resolve kernel directly, over the CPU-GPU link, while it resolves.
+    bool direct = false;
+    if (!out_dev && fN && fK && front.fluidsteps == 0) {
+        if (uint8_t *d = mapped_host_range(out, bytes)) {
+            dst = d;
+            direct = true;
+        }
+    }
+    if (!out_dev && !direct) {
         if ((rc = d_frame.reserve(bytes))) return rc;
         dst = d_frame.p;
     }
@@ -835,9 +878,9 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         if (rc) return rc;
     }
     // A device frame is left in flight on the render stream (am_get_stream);
-    // a host frame is copied out and waited for.
+    // a host frame is copied out (unless stored there directly) and waited for.
     if (!out_dev) {
-        AMG_CUDA(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, rstream));
+        if (!direct) AMG_CUDA(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, rstream));
         AMG_CUDA(cudaStreamSynchronize(rstream));
     } else {
         AMG_CUDA(cudaGetLastError());

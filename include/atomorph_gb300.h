@@ -179,7 +179,10 @@ size_t   am_get_chain_count(const am_morph *m);               /* chains = blob g
 
 /* Renders the frame at time t (morph::get_pixels(t, vec) morph.cpp:1405-1421)
  * as width*height RGBA8, row-major.  out is a host pointer, or a device
- * pointer when out_on_device != 0. */
+ * pointer when out_on_device != 0.  A host frame is complete when the call
+ * returns.  When out lies in pinned (page-locked, CUDA-mapped) host memory
+ * whose allocation covers the whole frame, an atom frame is stored there by
+ * the GPU directly while it is resolved; other host memory receives a copy. */
 int am_render(am_morph *m, double t, uint8_t *out, int out_on_device);
 /* Renders n frames at times ts[0..n) into n consecutive device frames. */
 int am_render_many(am_morph *m, const double *ts, size_t n, uint8_t *out_device);

@@ -90,6 +90,24 @@ def test_render_device_output_matches_host(capi):
         assert np.array_equal(buf.cpu().numpy(), m.render(t))
 
 
+def test_render_into_pinned_host_memory_matches_pageable(capi):
+    """Pinned host buffers are mapped into the GPU's address space and the
+    resolve kernel stores the frame there directly; the frame must equal the
+    one copied into pageable memory, also at an offset inside a larger
+    pinned allocation and with the buffer dirty beforehand."""
+    torch = pytest.importorskip("torch")
+    g = golden("spline48")
+    m = morph_from_golden(capi, g)
+    fb = m.height * m.width * 4
+    pinned = torch.full((3 * fb,), 0xAB, dtype=torch.uint8).pin_memory()
+    for t in (0.1, 0.45, 0.8):
+        want = m.render(t)
+        for off in (0, fb, 2 * fb):
+            assert m.lib.am_render(m.h, t, pinned.data_ptr() + off, 0) == capi.AM_OK
+            got = pinned[off:off + fb].numpy().reshape(m.height, m.width, 4)
+            assert np.array_equal(got, want), (t, off)
+
+
 @pytest.mark.parametrize("resolution", [(1600, 1500), (300, 200)])
 def test_render_other_resolutions_match_oracle(capi, oracle, resolution):
     """Outputs above 2048 tiles of 32x32 px take the separate splat / scan /
