@@ -802,32 +802,31 @@ int Engine::synchronize() {
 // address of [p, p + bytes) when the driver reports p as mapped host memory
 // whose whole allocation covers the range, else nullptr.  Pageable memory,
 // a short pinned buffer or a failed query leave the frame on the copy path.
+// One driver query (cuPointerGetAttributes answers pointers it does not
+// know with empty attributes, not an error).
 static uint8_t *mapped_host_range(uint8_t *p, size_t bytes) {
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
-    using GetAttr = CUresult (*)(void *, CUpointer_attribute, CUdeviceptr);
-    static GetAttr get_attr = [] {
+    using GetAttrs = CUresult (*)(unsigned, CUpointer_attribute *, void **, CUdeviceptr);
+    static GetAttrs get_attrs = [] {
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) !=
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttributes", &fn, 12000, cudaEnableDefault, &q) !=
                 cudaSuccess ||
             q != cudaDriverEntryPointSuccess)
             fn = nullptr;
-        return reinterpret_cast<GetAttr>(fn);
+        return reinterpret_cast<GetAttrs>(fn);
     }();
-    if (!get_attr) return nullptr;
-    const CUdeviceptr dp = (CUdeviceptr)(uintptr_t)at.devicePointer;
-    CUdeviceptr start = 0;
+    if (!get_attrs) return nullptr;
+    CUpointer_attribute which[4] = {CU_POINTER_ATTRIBUTE_MEMORY_TYPE, CU_POINTER_ATTRIBUTE_DEVICE_POINTER,
+                                    CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, CU_POINTER_ATTRIBUTE_RANGE_SIZE};
+    unsigned int type = 0;
+    CUdeviceptr dev = 0, start = 0;
     size_t size = 0;
-    if (get_attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, dp) != CUDA_SUCCESS ||
-        get_attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, dp) != CUDA_SUCCESS)
-        return nullptr;
-    if (dp < start || dp - start > size || size - (dp - start) < bytes) return nullptr;
-    return static_cast<uint8_t *>(at.devicePointer);
+    void *data[4] = {&type, &dev, &start, &size};
+    const CUdeviceptr hp = (CUdeviceptr)(uintptr_t)p;
+    if (get_attrs(4, which, data, hp) != CUDA_SUCCESS) return nullptr;
+    if (type != CU_MEMORYTYPE_HOST || !dev || !size) return nullptr;
+    if (hp < start || hp - start > size || size - (hp - start) < bytes) return nullptr;
+    return reinterpret_cast<uint8_t *>((uintptr_t)dev);
 }
 
 int Engine::render(double time, uint8_t *out, bool out_dev) {
