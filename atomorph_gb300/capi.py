@@ -224,7 +224,8 @@ class Morph:
 
     def tune(self, **kw) -> "Morph":
         """Guided-refinement tunables (am_set_tuning): local_self,
-        local_target, local_random, learned_keep, learned_adaptive, guided_switch."""
+        local_target, local_random, learned_keep, learned_adaptive, guided_switch,
+        render_pipeline."""
         for k, v in kw.items():
             _check(self.lib.am_set_tuning(self.h, k.encode(), float(v)), "am_set_tuning " + k)
         return self

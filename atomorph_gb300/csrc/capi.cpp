@@ -124,8 +124,12 @@ int am_set_sweeps(am_morph *m, size_t s) { CHECK(m); H(m).front.sweeps = s; H(m)
 int am_set_tuning(am_morph *m, const char *name, double value) {
     CHECK(m);
     if (!name || !(value >= 0.0) || value > 1024.0) return AM_ERR_ARG;
-    amg::Params *ps[2] = {&H(m).front, &H(m).active};
     std::string n(name);
+    if (n == "render_pipeline") {
+        H(m).render_pipeline = value != 0.0;
+        return AM_OK;
+    }
+    amg::Params *ps[2] = {&H(m).front, &H(m).active};
     for (amg::Params *p : ps) {
         if (n == "local_self") p->local_self = (uint32_t)value;
         else if (n == "local_target") p->local_target = (uint32_t)value;

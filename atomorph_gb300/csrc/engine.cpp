@@ -735,6 +735,9 @@ int Engine::publish_front() {
     else f_energy = -1.0;
     if (N && K) {
         int rc;
+        // frames in flight read the front chains, ranks and colour tables
+        if (rstream) AMG_CUDA(cudaStreamSynchronize(rstream));
+        render_quiesce(rw);
         if ((rc = d_Pf.reserve(N * K))) return rc;
         if ((rc = d_chain_off_f.reserve(C + 1))) return rc;
         if ((rc = d_rank_f.reserve((size_t)K * C))) return rc;
@@ -871,6 +874,7 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
         sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
         render_options(sc);
+        sc.pipeline = render_pipeline ? 1u : 0u;
         size_t f = (size_t)(t * fK);
         uint64_t key = f < f_keys.size() ? f_keys[f] : 0;
         rc = render_frame(rw, sc, t, key, dst, rstream);

@@ -65,12 +65,25 @@ struct RenderWork {
     uint64_t rec_cap = 0;
     uint32_t *tile_cnt = nullptr, *tile_off = nullptr, *tile_cur = nullptr;
     uint32_t ntiles_cap = 0;
-    // tile regions of the fused binning, planned from the previous frame
-    uint32_t *p_off = nullptr, *p_cap = nullptr, *p_cnt = nullptr, *ovf_cnt = nullptr, *zero = nullptr;
-    uint32_t plan_tiles = 0;   // tiles the plan is for (0: none yet)
-    uint64_t plan_atoms = 0;   // atom capacity the record buffers were sized for
-    uint4 *ovf = nullptr;
-    uint64_t ovf_cap = 0;
+    uint32_t *zero = nullptr;   // a zero overflow count for the separate-kernel path
+    // Fused frames are pipelined over two record slots: the pair preparation,
+    // binning and planning of a frame run on `bs` while the previous frame
+    // resolves on the render stream.  Each slot holds its tile regions
+    // (planned from the previous frame's counts), their records and the
+    // overflow list.
+    struct Slot {
+        uint4 *rec = nullptr, *ovf = nullptr;
+        uint32_t *off = nullptr, *cap = nullptr, *cnt = nullptr, *ovf_cnt = nullptr;
+        uint32_t tiles = 0;              // tiles the plan in off / cap is for (0: none)
+        uint64_t atoms = 0;              // atom count it was planned for
+        cudaEvent_t resolved = nullptr;  // after the last resolve that read the slot
+    } slot[2];
+    int cur = 0;                         // slot of the next fused frame
+    uint64_t slot_rec_cap = 0, slot_ovf_cap = 0;
+    uint32_t slot_tiles_cap = 0;
+    cudaStream_t bs = nullptr;
+    cudaEvent_t binned = nullptr, mark = nullptr;
+    bool bs_after_s = false;             // the next fused frame orders bs after the render stream
     int *perm = nullptr;    // [2][512] Perlin permutations on the device
     bool perm_set = false;
     Prof *prof = nullptr;   // optional per-kernel timing
@@ -107,17 +120,37 @@ static void rw_free(RenderWork *w) {
     w->pairs.clear();
 }
 
+static void slot_free(RenderWork::Slot &sl) {
+    void *pl[] = {sl.rec, sl.ovf, sl.off, sl.cap, sl.cnt, sl.ovf_cnt};
+    for (void *q : pl)
+        if (q) cudaFree(q);
+    sl.rec = sl.ovf = nullptr;
+    sl.off = sl.cap = sl.cnt = sl.ovf_cnt = nullptr;
+    sl.tiles = 0;
+    sl.atoms = 0;
+}
+
+void render_quiesce(RenderWork *w) {
+    if (w && w->bs) cudaStreamSynchronize(w->bs);
+}
+
 void render_work_destroy(RenderWork *w) {
     if (!w) return;
+    render_quiesce(w);
     rw_free(w);
     if (w->rec) cudaFree(w->rec);
     if (w->tile_cnt) cudaFree(w->tile_cnt);
     if (w->tile_off) cudaFree(w->tile_off);
     if (w->tile_cur) cudaFree(w->tile_cur);
     if (w->perm) cudaFree(w->perm);
-    void *pl[] = {w->p_off, w->p_cap, w->p_cnt, w->ovf_cnt, w->zero, w->ovf};
-    for (void *q : pl)
-        if (q) cudaFree(q);
+    if (w->zero) cudaFree(w->zero);
+    for (auto &sl : w->slot) {
+        slot_free(sl);
+        if (sl.resolved) cudaEventDestroy(sl.resolved);
+    }
+    if (w->binned) cudaEventDestroy(w->binned);
+    if (w->mark) cudaEventDestroy(w->mark);
+    if (w->bs) cudaStreamDestroy(w->bs);
     delete w;
 }
 
@@ -128,6 +161,8 @@ void render_invalidate(RenderWork *w) {
 }
 
 int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope) {
+    // frames in flight may still read the permutations (a seed change is rare)
+    AMG_CUDA(cudaDeviceSynchronize());
     if (!w->perm) AMG_CUDA(cudaMalloc(&w->perm, 1024 * sizeof(int)));
     std::vector<int> h(1024);
     std::memcpy(h.data(), perm_lag, 512 * sizeof(int));
@@ -543,11 +578,14 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
     }
 }
 
-// The next frame's tile regions from this frame's counts (one CTA): capacity
-// count + count / 4 + 32 (or, with init, the atoms spread evenly), regions in
-// tile order, clipped to the buffer; then the counters are cleared.
-__global__ void __launch_bounds__(1024) k_tile_plan(uint32_t *cnt, uint32_t *off, uint32_t *cap, uint32_t ntiles,
-                                                    uint64_t init_atoms, uint64_t rec_cap, uint32_t *ovf_cnt) {
+// A frame's tile regions from the previous frame's counts src_cnt (one CTA):
+// capacity count + count / 4 + 32 (or, with init, the atoms spread evenly),
+// regions in tile order, clipped to the buffer; the destination slot's
+// counters (cnt, ovf_cnt) are cleared.  Source and destination are the two
+// record slots, so the source's counts stay intact for its resolve.
+__global__ void __launch_bounds__(1024) k_tile_plan(const uint32_t *src_cnt, uint32_t *off, uint32_t *cap,
+                                                    uint32_t *cnt, uint32_t ntiles, uint64_t init_atoms,
+                                                    uint64_t rec_cap, uint32_t *ovf_cnt) {
     __shared__ uint32_t wsum[32];
     __shared__ unsigned long long carry;
     if (threadIdx.x == 0) carry = 0;
@@ -556,7 +594,7 @@ __global__ void __launch_bounds__(1024) k_tile_plan(uint32_t *cnt, uint32_t *off
         const uint32_t t = t0 + threadIdx.x;
         uint32_t c = 0;
         if (t < ntiles) {
-            const uint64_t seen = init_atoms ? (init_atoms * 5 / 4) / ntiles : cnt[t];
+            const uint64_t seen = init_atoms ? (init_atoms * 5 / 4) / ntiles : src_cnt[t];
             const uint64_t want = seen + seen / 4 + 32;
             c = want < (1ull << 30) ? (uint32_t)want : (1u << 30);
         }
@@ -1101,67 +1139,38 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     }
     double dt = 1.0 / double(sc.K);
     double t = std::max(0.0, (time - (double)(frame_key * dt)) / dt);
-    PairData *pd = nullptr;
-    {
-        int rc = prep_pair(w, sc, (uint32_t)f, s, &pd);
-        if (rc) return rc;
-    }
     uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
     uint32_t ntiles = tiles_x * tiles_y;
-    if (ntiles + 1 > w->ntiles_cap) {
-        if (w->tile_cnt) cudaFree(w->tile_cnt);
-        if (w->tile_off) cudaFree(w->tile_off);
-        if (w->tile_cur) cudaFree(w->tile_cur);
-        AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
-        AMG_CUDA(cudaMalloc(&w->tile_off, (ntiles + 1) * 4));
-        AMG_CUDA(cudaMalloc(&w->tile_cur, (ntiles + 1) * 4));
-        AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
-        w->ntiles_cap = ntiles + 1;
-    }
     const bool fused = ntiles <= kBinMaxTiles;
-    // records: fused, the planned tile regions (about 1.25 x the records of a
-    // frame plus slack; at most 4 records per atom) and an overflow list of
-    // 4 per atom; separate kernels, 4 per atom
-    const uint64_t need = fused ? sc.N * 5 + (uint64_t)ntiles * 64 + 16 : sc.N * 4 + 16;
-    if (need > w->rec_cap) {
-        if (w->rec) cudaFree(w->rec);
-        w->rec = nullptr;
-        w->rec_cap = need + need / 4;
-        AMG_CUDA(cudaMalloc(&w->rec, w->rec_cap * sizeof(uint4)));
-        w->plan_tiles = 0;
+    if (!w->bs) {
+        AMG_CUDA(cudaStreamCreateWithFlags(&w->bs, cudaStreamNonBlocking));
+        AMG_CUDA(cudaEventCreateWithFlags(&w->binned, cudaEventDisableTiming));
+        AMG_CUDA(cudaEventCreateWithFlags(&w->mark, cudaEventDisableTiming));
+        for (auto &sl : w->slot) AMG_CUDA(cudaEventCreateWithFlags(&sl.resolved, cudaEventDisableTiming));
     }
+    // The pre-resolve work of a fused frame runs on bs, of a separate-kernel
+    // frame on the render stream; switching orders one after the other.
+    cudaStream_t ps = s;
     if (fused) {
-        if (!w->zero) {
-            AMG_CUDA(cudaMalloc(&w->zero, 4));
-            AMG_CUDA(cudaMemsetAsync(w->zero, 0, 4, s));
-            AMG_CUDA(cudaMalloc(&w->ovf_cnt, 4));
+        ps = w->bs;
+        if (w->bs_after_s || !sc.pipeline) {
+            AMG_CUDA(cudaEventRecord(w->mark, s));
+            AMG_CUDA(cudaStreamWaitEvent(w->bs, w->mark, 0));
+            w->bs_after_s = false;
         }
-        if (sc.N * 4 + 16 > w->ovf_cap) {
-            if (w->ovf) cudaFree(w->ovf);
-            w->ovf = nullptr;
-            w->ovf_cap = sc.N * 4 + 16;
-            AMG_CUDA(cudaMalloc(&w->ovf, w->ovf_cap * sizeof(uint4)));
-        }
-        if (w->plan_tiles != ntiles || w->plan_atoms != sc.N) {
-            uint32_t **arrs[] = {&w->p_off, &w->p_cap, &w->p_cnt};
-            for (uint32_t **q : arrs) {
-                if (*q) cudaFree(*q);
-                *q = nullptr;
-                AMG_CUDA(cudaMalloc(q, (size_t)ntiles * 4));
-            }
-            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, s, w->p_cnt, w->p_off, w->p_cap, ntiles, std::max<uint64_t>(sc.N, 1),
-                       w->rec_cap, w->ovf_cnt);
-            w->plan_tiles = ntiles;
-            w->plan_atoms = sc.N;
-        }
-    } else if (!w->zero) {
-        AMG_CUDA(cudaMalloc(&w->zero, 4));
-        AMG_CUDA(cudaMemsetAsync(w->zero, 0, 4, s));
-        AMG_CUDA(cudaMalloc(&w->ovf_cnt, 4));
+    } else {
+        AMG_CUDA(cudaEventRecord(w->mark, w->bs));
+        AMG_CUDA(cudaStreamWaitEvent(s, w->mark, 0));
+        w->bs_after_s = true;
+    }
+    PairData *pd = nullptr;
+    {
+        int rc = prep_pair(w, sc, (uint32_t)f, ps, &pd);
+        if (rc) return rc;
     }
     FrameArgs fa;
     {
-        int rc = frame_args(w, sc, time, (uint32_t)f, t, &fa, s);
+        int rc = frame_args(w, sc, time, (uint32_t)f, t, &fa, ps);
         if (rc) return rc;
     }
     fa.tiles_x = tiles_x;
@@ -1170,11 +1179,42 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     uint64_t n = sc.N;
     SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx};
     TileRecs tr;
+    RenderWork::Slot *A = nullptr, *B = nullptr;
     if (fused) {
+        // records: the planned tile regions (about 1.25 x the records of a
+        // frame plus slack; at most 4 records per atom) and an overflow list
+        // of 4 per atom, per slot
+        const uint64_t need = sc.N * 5 + (uint64_t)ntiles * 64 + 16, need_ovf = sc.N * 4 + 16;
+        if (need > w->slot_rec_cap || need_ovf > w->slot_ovf_cap || ntiles > w->slot_tiles_cap) {
+            // frames in flight read the old buffers
+            AMG_CUDA(cudaStreamSynchronize(w->bs));
+            AMG_CUDA(cudaStreamSynchronize(s));
+            w->slot_rec_cap = std::max(w->slot_rec_cap, need + need / 4);
+            w->slot_ovf_cap = std::max(w->slot_ovf_cap, need_ovf);
+            w->slot_tiles_cap = std::max(w->slot_tiles_cap, ntiles);
+            for (auto &sl : w->slot) {
+                slot_free(sl);
+                AMG_CUDA(cudaMalloc(&sl.rec, w->slot_rec_cap * sizeof(uint4)));
+                AMG_CUDA(cudaMalloc(&sl.ovf, w->slot_ovf_cap * sizeof(uint4)));
+                uint32_t **arrs[] = {&sl.off, &sl.cap, &sl.cnt};
+                for (uint32_t **q : arrs) AMG_CUDA(cudaMalloc(q, (size_t)w->slot_tiles_cap * 4));
+                AMG_CUDA(cudaMalloc(&sl.ovf_cnt, 4));
+            }
+        }
+        A = &w->slot[w->cur];
+        B = &w->slot[w->cur ^ 1];
+        if (A->tiles != ntiles || A->atoms != sc.N) {
+            // plan from the atom count; the slot's last resolve must be done
+            AMG_CUDA(cudaStreamWaitEvent(w->bs, A->resolved, 0));
+            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, w->bs, A->cnt, A->off, A->cap, A->cnt, ntiles,
+                       std::max<uint64_t>(sc.N, 1), w->slot_rec_cap, A->ovf_cnt);
+            A->tiles = ntiles;
+            A->atoms = sc.N;
+        }
         BinArgs b;
-        b.sc = sc; b.fa = fa; b.n = pd->d_active; b.in = in; b.rec = w->rec;
-        b.off = w->p_off; b.cap = w->p_cap; b.cnt = w->p_cnt;
-        b.ovf = w->ovf; b.ovf_cnt = w->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->ovf_cap, UINT32_MAX);
+        b.sc = sc; b.fa = fa; b.n = pd->d_active; b.in = in; b.rec = A->rec;
+        b.off = A->off; b.cap = A->cap; b.cnt = A->cnt;
+        b.ovf = A->ovf; b.ovf_cnt = A->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->slot_ovf_cap, UINT32_MAX);
         const unsigned grid = (unsigned)((n + (uint64_t)kBinPer * kBinThreads - 1) / ((uint64_t)kBinPer * kBinThreads));
         static bool battr = false;
         if (!battr) {
@@ -1182,11 +1222,34 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
                                           (int)bin_smem(kBinPer, kBinMaxTiles)));
             battr = true;
         }
-        if (w->prof) w->prof->open(s);
-        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bin_smem(kBinPer, ntiles), s, b);
-        if (w->prof) w->prof->close(PROF_BIN, s);
-        tr = TileRecs{w->rec, w->p_off, w->p_cnt, w->p_cap, w->ovf, w->ovf_cnt, b.ovf_cap};
+        if (w->prof) w->prof->open(w->bs);
+        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bin_smem(kBinPer, ntiles), w->bs, b);
+        if (w->prof) w->prof->close(PROF_BIN, w->bs);
+        AMG_CUDA(cudaEventRecord(w->binned, w->bs));
+        AMG_CUDA(cudaStreamWaitEvent(s, w->binned, 0));
+        tr = TileRecs{A->rec, A->off, A->cnt, A->cap, A->ovf, A->ovf_cnt, b.ovf_cap};
     } else {
+        if (ntiles + 1 > w->ntiles_cap) {
+            if (w->tile_cnt) cudaFree(w->tile_cnt);
+            if (w->tile_off) cudaFree(w->tile_off);
+            if (w->tile_cur) cudaFree(w->tile_cur);
+            AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
+            AMG_CUDA(cudaMalloc(&w->tile_off, (ntiles + 1) * 4));
+            AMG_CUDA(cudaMalloc(&w->tile_cur, (ntiles + 1) * 4));
+            w->ntiles_cap = ntiles + 1;
+        }
+        // records of the separate kernels: 4 per atom
+        const uint64_t need = sc.N * 4 + 16;
+        if (need > w->rec_cap) {
+            if (w->rec) cudaFree(w->rec);
+            w->rec = nullptr;
+            w->rec_cap = need + need / 4;
+            AMG_CUDA(cudaMalloc(&w->rec, w->rec_cap * sizeof(uint4)));
+        }
+        if (!w->zero) {
+            AMG_CUDA(cudaMalloc(&w->zero, 4));
+            AMG_CUDA(cudaMemsetAsync(w->zero, 0, 4, s));
+        }
         AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));
         if (n) {
             unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)kSMs * 8);
@@ -1231,10 +1294,17 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem + feather_smem(o.feather), s, tr, tiles_x, sc.width,
                sc.height, sc.density ? sc.density : 1u, out, o);
     if (w->prof) w->prof->close(PROF_RESOLVE, s);
-    // the next frame's tile regions from this frame's counts
-    if (fused)
-        AMG_LAUNCH(k_tile_plan, 1, 1024, 0, s, w->p_cnt, w->p_off, w->p_cap, ntiles, (uint64_t)0, w->rec_cap,
-                   w->ovf_cnt);
+    if (fused) {
+        AMG_CUDA(cudaEventRecord(A->resolved, s));
+        // the next frame's tile regions (the other slot) from this frame's
+        // counts, once the other slot's last resolve is done
+        AMG_CUDA(cudaStreamWaitEvent(w->bs, B->resolved, 0));
+        AMG_LAUNCH(k_tile_plan, 1, 1024, 0, w->bs, A->cnt, B->off, B->cap, B->cnt, ntiles, (uint64_t)0,
+                   w->slot_rec_cap, B->ovf_cnt);
+        B->tiles = ntiles;
+        B->atoms = sc.N;
+        w->cur ^= 1;
+    }
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }

@@ -219,6 +219,7 @@ struct RenderScene {
     const uint64_t *chain_off;    // [C+1]
     const uint32_t *display;      // [K][CH][CW] RGB colour read by get_pixel
     const int32_t *rank;          // [K][C] composite rank of group g in frame k
+    uint32_t pipeline = 1;        // a frame's binning may run beside the previous frame's resolve
     // render options (morph.h:67-70)
     uint32_t feather = 0;         // outer layers of each blob faded (TEXTURE blobs)
     uint32_t keep_background = 0; // key frames cross-faded under the blobs
@@ -247,6 +248,9 @@ int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32
                          uint32_t width, uint32_t height, uint8_t *out, cudaStream_t s);
 // Drops cached per-key-frame-pair data (chains or settings changed).
 void render_invalidate(RenderWork *w);
+// Waits for the render work's own binning stream (frames resolve on the
+// caller's render stream; their binning may still be running on it).
+void render_quiesce(RenderWork *w);
 
 // ---- k_fluid.cu: FluidModel::step in FP32
 struct FluidDev;

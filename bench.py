@@ -126,7 +126,10 @@ def setup_morph(capi, frames, refine_sweeps):
 
 def render_roofline(m, frames_ts, torch, stream):
     """Per-kernel live CUDA-event timing over one extra cycle, and the
-    algorithmic bytes of the dominant kernel."""
+    algorithmic bytes of the dominant kernel.  The cycle runs with frames one
+    after the other (render_pipeline 0), so each kernel's span is its own
+    duration rather than its share of an overlap."""
+    m.tune(render_pipeline=0)
     m.profile(True)
     buf = torch.empty((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
     for t in frames_ts:
@@ -134,6 +137,7 @@ def render_roofline(m, frames_ts, torch, stream):
     stream.synchronize()
     prof = m.profile_read()
     m.profile(False)
+    m.tune(render_pipeline=1)
     return prof
 
 
@@ -218,6 +222,10 @@ def bench_ours(args, rank, world):
     # (4 B) + original index (4 B) = 56 B read once, plus 4 B per output pixel.
     frame_bytes = N * 56 + m.width * m.height * 4
     frame_ms_profiled = sum(v[0] for v in per_frame.values() if True) / FRAMES_PER_STEP
+    # in the timed cycle frames overlap (a frame's binning runs beside the
+    # previous frame's resolve), so the whole-frame figure uses the timed
+    # milliseconds per frame; kernel_ms_sum is the one-after-the-other sum
+    frame_ms = ms / (FRAMES_PER_STEP * args.steps)
     dom_name, (dom_ms, dom_n) = dom[0], dom[1]
     dom_avg_ms = dom_ms / dom_n
     # Algorithmic bytes attributed to the dominant kernel (roofline)
@@ -234,9 +242,10 @@ def bench_ours(args, rank, world):
             "frac": round(achieved / hbm, 4), "peak_kind": peak_kind, "traffic": _profiled_traffic(dom_name),
             "traffic_source": "profiles/kernels_shapes1024_profile_case.md (ncu, cold cache, bytes per launch)",
             "algorithmic_bytes_per_launch": int(kernel_bytes), "avg_launch_ms": round(dom_avg_ms, 5),
-            "frame": {"algorithmic_bytes": int(frame_bytes), "profiled_ms": round(frame_ms_profiled, 5),
-                      "achieved_gbs": round(frame_bytes / (frame_ms_profiled / 1e3) / 1e9, 1),
-                      "frac": round(frame_bytes / (frame_ms_profiled / 1e3) / 1e9 / hbm, 4)},
+            "frame": {"algorithmic_bytes": int(frame_bytes), "ms": round(frame_ms, 5),
+                      "kernel_ms_sum": round(frame_ms_profiled, 5),
+                      "achieved_gbs": round(frame_bytes / (frame_ms / 1e3) / 1e9, 1),
+                      "frac": round(frame_bytes / (frame_ms / 1e3) / 1e9 / hbm, 4)},
             "kernels_ms_per_frame": {k: round(v[0] / FRAMES_PER_STEP, 5) for k, v in per_frame.items()}}
 
     flu = None

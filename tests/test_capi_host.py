@@ -72,6 +72,12 @@ def test_setter_validation_and_density_fluid_coupling(capi):
     m.set(fluid=10)
     m.set(density=3)  # density > 1 with fluid on turns the fluid off
     assert m.lib.am_set_fluid(m.h, 10) == capi.AM_OK
+    # tunables: known names in range, unknown names and bad values refused
+    for name, v in (("render_pipeline", 0), ("render_pipeline", 1), ("learned_keep", 0.5), ("guided_switch", 0)):
+        assert m.lib.am_set_tuning(m.h, name.encode(), float(v)) == capi.AM_OK, name
+    assert m.lib.am_set_tuning(m.h, b"no_such_knob", 1.0) == capi.AM_ERR_ARG
+    assert m.lib.am_set_tuning(m.h, b"learned_keep", 0.0) == capi.AM_ERR_ARG
+    assert m.lib.am_set_tuning(m.h, b"render_pipeline", -1.0) == capi.AM_ERR_ARG
 
 
 def test_not_busy_without_work(capi):

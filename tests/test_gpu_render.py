@@ -90,6 +90,56 @@ def test_render_device_output_matches_host(capi):
         assert np.array_equal(buf.cpu().numpy(), m.render(t))
 
 
+@pytest.mark.parametrize("pipeline", [1, 0])
+def test_back_to_back_device_frames_match_host(capi, pipeline):
+    """Device frames are left in flight, and (render_pipeline 1, the default)
+    a frame's binning runs beside the previous frame's resolve over two
+    record slots: 43 frames issued without a sync (crossing every key-frame
+    pair, repeating times, in a scrambled order) must equal the same frames
+    rendered one at a time."""
+    torch = pytest.importorskip("torch")
+    g = golden("spline48")
+    m = morph_from_golden(capi, g)
+    m.tune(render_pipeline=pipeline)
+    ts = [((i * 7) % 40) / 40.0 for i in range(40)] + [0.5, 0.5, 0.0]
+    want = [m.render(t) for t in ts]
+    buf = torch.zeros((len(ts), m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        for i, t in enumerate(ts):
+            m.render_device(t, buf[i].data_ptr())
+        assert m.lib.am_device_sync(m.h) == capi.AM_OK
+        got = buf.cpu().numpy()
+        for i, t in enumerate(ts):
+            assert np.array_equal(got[i], want[i]), (i, t)
+
+
+def test_device_frames_across_render_paths_match_host(capi):
+    """Frames in flight while the resolution switches between the fused,
+    pipelined binning (at most 2048 tiles) and the separate-kernel path
+    (1600 x 1500: 2350 tiles) and back."""
+    torch = pytest.importorskip("torch")
+    g = golden("spline48")
+    m = morph_from_golden(capi, g)
+    small = (m.width, m.height)
+    ts = [0.1, 0.6, 0.35, 0.85]
+    plan = [small, (1600, 1500), small, (1600, 1500)]
+    want, bufs = [], []
+    for res in plan:
+        m.set(resolution=res)
+        want.append([m.render(t) for t in ts])
+    for res in plan:
+        m.set(resolution=res)
+        b = torch.zeros((len(ts), res[1], res[0], 4), dtype=torch.uint8, device="cuda")
+        for i, t in enumerate(ts):
+            m.render_device(t, b[i].data_ptr())
+        bufs.append(b)
+    assert m.lib.am_device_sync(m.h) == capi.AM_OK
+    for k, b in enumerate(bufs):
+        got = b.cpu().numpy()
+        for i, t in enumerate(ts):
+            assert np.array_equal(got[i], want[k][i]), (plan[k], t)
+
+
 def test_render_into_pinned_host_memory_matches_pageable(capi):
     """Pinned host buffers are mapped into the GPU's address space and the
     resolve kernel stores the frame there directly; the frame must equal the
