@@ -668,18 +668,22 @@ __device__ __forceinline__ uint32_t round_div(unsigned long long num, unsigned l
     return (uint32_t)q;
 }
 
-// round_div for 32-bit sums: den < 2^24, quotient < 256 (packed path).
-// No 64-bit conversion or 64 x 64 multiply (both are slow on this part).
-__device__ __forceinline__ uint32_t round_div32(uint32_t num, uint32_t den) {
-    float qf = __fdividef(__uint2float_rn(num), __uint2float_rn(den)) + 0.5f;
-    uint32_t q = __float2uint_rz(qf);
-    const unsigned long long a = 2ull * num + den, b = 2ull * den;
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const unsigned long long lo = (unsigned long long)(2u * q) * den;  // 32 x 32 -> 64
-        if (a < lo) --q;
-        else if (a >= lo + b) ++q;
-    }
+// Exactly rounded (half away from zero) quotients of several 32-bit
+// numerators over one denominator (a pixel's four channel sums over its
+// weight, packed path): one IEEE reciprocal, then per numerator a
+// float estimate of num / den + 1/2 — within 1 of the exact quotient for
+// den < 2^24 and quotients below 256 — and one correction on the exact
+// 32-bit remainder (|remainder| < 1.5 den).
+struct RoundDiv {
+    float rcp;
+    uint32_t den;
+};
+__device__ __forceinline__ RoundDiv round_div_by(uint32_t den) { return RoundDiv{__frcp_rn(__uint2float_rn(den)), den}; }
+__device__ __forceinline__ uint32_t round_div(const RoundDiv &d, uint32_t num) {
+    uint32_t q = __float2uint_rz(__fmaf_rn(__uint2float_rn(num), d.rcp, 0.5f));
+    const int r2 = 2 * (int)(num - q * d.den);
+    if (r2 < -(int)d.den) --q;
+    else if (r2 >= (int)d.den) ++q;
     return q;
 }
 
@@ -972,10 +976,9 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                 if (!cnt) continue;
                 uint32_t r, g, b, a;
                 if (packed) {
-                    const uint32_t w32 = (uint32_t)W;
-                    r = round_div32((uint32_t)sr, w32); g = round_div32((uint32_t)sg, w32);
-                    b = round_div32((uint32_t)sb, w32);
-                    a = cnt >= density ? round_div32((uint32_t)sa, w32)
+                    const RoundDiv d = round_div_by((uint32_t)W);
+                    r = round_div(d, (uint32_t)sr); g = round_div(d, (uint32_t)sg); b = round_div(d, (uint32_t)sb);
+                    a = cnt >= density ? round_div(d, (uint32_t)sa)
                                        : round_div((unsigned long long)cnt * sa, (unsigned long long)density * W);
                 } else {
                     r = round_div(sr, W); g = round_div(sg, W); b = round_div(sb, W);
