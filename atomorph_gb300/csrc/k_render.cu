@@ -1219,12 +1219,10 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         b.off = A->off; b.cap = A->cap; b.cnt = A->cnt;
         b.ovf = A->ovf; b.ovf_cnt = A->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->slot_ovf_cap, UINT32_MAX);
         const unsigned grid = (unsigned)((n + (uint64_t)kBinPer * kBinThreads - 1) / ((uint64_t)kBinPer * kBinThreads));
-        static bool battr = false;
-        if (!battr) {
-            AMG_CUDA(cudaFuncSetAttribute(k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)bin_smem(kBinPer, kBinMaxTiles)));
-            battr = true;
-        }
+        // once per process (thread-safe static initialisation)
+        static const cudaError_t battr = cudaFuncSetAttribute(
+            k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bin_smem(kBinPer, kBinMaxTiles));
+        AMG_CUDA(battr);
         if (w->prof) w->prof->open(w->bs);
         if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bin_smem(kBinPer, ntiles), w->bs, b);
         if (w->prof) w->prof->close(PROF_BIN, w->bs);
@@ -1287,12 +1285,9 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     o.bg = bg_args(sc, (uint32_t)f, t);
     if (w->prof) w->prof->open(s);
     {
-        static bool attr = false;
-        if (!attr) {
-            AMG_CUDA(cudaFuncSetAttribute(k_frame_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(kResolveSmem + feather_smem(kMaxFeather))));
-            attr = true;
-        }
+        static const cudaError_t attr = cudaFuncSetAttribute(
+            k_frame_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kResolveSmem + feather_smem(kMaxFeather)));
+        AMG_CUDA(attr);
     }
     AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem + feather_smem(o.feather), s, tr, tiles_x, sc.width,
                sc.height, sc.density ? sc.density : 1u, out, o);
