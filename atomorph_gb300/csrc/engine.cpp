@@ -874,6 +874,8 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
         sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
         render_options(sc);
+        // host frames too: the tile plan for the next frame then runs on the
+        // second stream, after the resolve the caller waits for
         sc.pipeline = render_pipeline ? 1u : 0u;
         size_t f = (size_t)(t * fK);
         uint64_t key = f < f_keys.size() ? f_keys[f] : 0;

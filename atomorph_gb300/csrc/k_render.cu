@@ -83,7 +83,8 @@ struct RenderWork {
     uint32_t slot_tiles_cap = 0;
     cudaStream_t bs = nullptr;
     cudaEvent_t binned = nullptr, mark = nullptr;
-    bool bs_after_s = false;             // the next fused frame orders bs after the render stream
+    bool bs_after_s = false;             // bs must wait for the render stream before its next work
+    bool s_after_bs = false;             // the render stream must wait for bs before touching slots or pairs
     int *perm = nullptr;    // [2][512] Perlin permutations on the device
     bool perm_set = false;
     Prof *prof = nullptr;   // optional per-kernel timing
@@ -1151,21 +1152,23 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         AMG_CUDA(cudaEventCreateWithFlags(&w->mark, cudaEventDisableTiming));
         for (auto &sl : w->slot) AMG_CUDA(cudaEventCreateWithFlags(&sl.resolved, cudaEventDisableTiming));
     }
-    // The pre-resolve work of a fused frame runs on bs, of a separate-kernel
-    // frame on the render stream; switching orders one after the other.
-    cudaStream_t ps = s;
-    if (fused) {
-        ps = w->bs;
-        if (w->bs_after_s || !sc.pipeline) {
-            AMG_CUDA(cudaEventRecord(w->mark, s));
-            AMG_CUDA(cudaStreamWaitEvent(w->bs, w->mark, 0));
-            w->bs_after_s = false;
-        }
-    } else {
+    // The pre-resolve work of a pipelined fused frame runs on bs; everything
+    // else (a frame whose caller waits for it, the separate-kernel path) runs
+    // on the render stream alone, with no cross-stream events.  Switching
+    // between the two orders one stream after the other, once.
+    const bool piped = fused && sc.pipeline;
+    const cudaStream_t ps = piped ? w->bs : s;
+    if (piped && w->bs_after_s) {
+        AMG_CUDA(cudaEventRecord(w->mark, s));
+        AMG_CUDA(cudaStreamWaitEvent(w->bs, w->mark, 0));
+        w->bs_after_s = false;
+    } else if (!piped && w->s_after_bs) {
         AMG_CUDA(cudaEventRecord(w->mark, w->bs));
         AMG_CUDA(cudaStreamWaitEvent(s, w->mark, 0));
-        w->bs_after_s = true;
+        w->s_after_bs = false;
     }
+    if (piped) w->s_after_bs = true;
+    else w->bs_after_s = true;
     PairData *pd = nullptr;
     {
         int rc = prep_pair(w, sc, (uint32_t)f, ps, &pd);
@@ -1208,8 +1211,8 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         B = &w->slot[w->cur ^ 1];
         if (A->tiles != ntiles || A->atoms != sc.N) {
             // plan from the atom count; the slot's last resolve must be done
-            AMG_CUDA(cudaStreamWaitEvent(w->bs, A->resolved, 0));
-            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, w->bs, A->cnt, A->off, A->cap, A->cnt, ntiles,
+            if (piped) AMG_CUDA(cudaStreamWaitEvent(w->bs, A->resolved, 0));
+            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, A->off, A->cap, A->cnt, ntiles,
                        std::max<uint64_t>(sc.N, 1), w->slot_rec_cap, A->ovf_cnt);
             A->tiles = ntiles;
             A->atoms = sc.N;
@@ -1223,11 +1226,13 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         static const cudaError_t battr = cudaFuncSetAttribute(
             k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bin_smem(kBinPer, kBinMaxTiles));
         AMG_CUDA(battr);
-        if (w->prof) w->prof->open(w->bs);
-        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bin_smem(kBinPer, ntiles), w->bs, b);
-        if (w->prof) w->prof->close(PROF_BIN, w->bs);
-        AMG_CUDA(cudaEventRecord(w->binned, w->bs));
-        AMG_CUDA(cudaStreamWaitEvent(s, w->binned, 0));
+        if (w->prof) w->prof->open(ps);
+        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bin_smem(kBinPer, ntiles), ps, b);
+        if (w->prof) w->prof->close(PROF_BIN, ps);
+        if (piped) {
+            AMG_CUDA(cudaEventRecord(w->binned, w->bs));
+            AMG_CUDA(cudaStreamWaitEvent(s, w->binned, 0));
+        }
         tr = TileRecs{A->rec, A->off, A->cnt, A->cap, A->ovf, A->ovf_cnt, b.ovf_cap};
     } else {
         if (ntiles + 1 > w->ntiles_cap) {
@@ -1293,11 +1298,13 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
                sc.height, sc.density ? sc.density : 1u, out, o);
     if (w->prof) w->prof->close(PROF_RESOLVE, s);
     if (fused) {
-        AMG_CUDA(cudaEventRecord(A->resolved, s));
         // the next frame's tile regions (the other slot) from this frame's
         // counts, once the other slot's last resolve is done
-        AMG_CUDA(cudaStreamWaitEvent(w->bs, B->resolved, 0));
-        AMG_LAUNCH(k_tile_plan, 1, 1024, 0, w->bs, A->cnt, B->off, B->cap, B->cnt, ntiles, (uint64_t)0,
+        if (piped) {
+            AMG_CUDA(cudaEventRecord(A->resolved, s));
+            AMG_CUDA(cudaStreamWaitEvent(w->bs, B->resolved, 0));
+        }
+        AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, B->off, B->cap, B->cnt, ntiles, (uint64_t)0,
                    w->slot_rec_cap, B->ovf_cnt);
         B->tiles = ntiles;
         B->atoms = sc.N;

@@ -130,9 +130,10 @@ size_t am_get_fluid_particles(am_morph *m, double *state, size_t cap);
  * blocks of sweeps where gated sweeps keep up with full ones; 0: always) and
  * "guided_switch" (guided/learned refinement runs plain sweeps until one gains
  * less than this fraction of the cost per sweep; 0 = guided from the start).
- * Render: "render_pipeline" (1, the default: a frame's binning runs beside the
- * previous frame's resolve on a second stream; 0: frames run one after the
- * other, for timing each kernel alone). */
+ * Render: "render_pipeline" (1, the default: a frame's binning and the next
+ * frame's tile plan run on a second stream, beside the previous frame's
+ * resolve; 0: frames run one after the other on the render stream alone, for
+ * timing each kernel by itself). */
 int am_set_tuning(am_morph *m, const char *name, double value);
 
 /* ---- control (morph.h:40-49, morph.cpp:52-100, 102-269) */

@@ -113,6 +113,30 @@ def test_back_to_back_device_frames_match_host(capi, pipeline):
             assert np.array_equal(got[i], want[i]), (i, t)
 
 
+def test_interleaved_host_and_device_frames(capi):
+    """Host frames (waited for) and device frames (left in flight) share the
+    pipelined record slots: alternating them, with device frames still in
+    flight when a host frame is rendered, changes no frame."""
+    torch = pytest.importorskip("torch")
+    g = golden("spline48")
+    m = morph_from_golden(capi, g)
+    ts = [((i * 11) % 24) / 24.0 for i in range(24)]
+    want = {t: m.render(t) for t in ts}
+    buf = torch.zeros((len(ts), m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    host = {}
+    for i, t in enumerate(ts):
+        m.render_device(t, buf[i].data_ptr())
+        if i % 3 == 2:
+            u = ts[(i * 5) % len(ts)]
+            host[(i, u)] = m.render(u)
+    assert m.lib.am_device_sync(m.h) == capi.AM_OK
+    got = buf.cpu().numpy()
+    for i, t in enumerate(ts):
+        assert np.array_equal(got[i], want[t]), (i, t)
+    for (i, u), frame in host.items():
+        assert np.array_equal(frame, want[u]), (i, u)
+
+
 def test_device_frames_across_render_paths_match_host(capi):
     """Frames in flight while the resolution switches between the fused,
     pipelined binning (at most 2048 tiles) and the separate-kernel path
