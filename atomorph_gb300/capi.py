@@ -91,6 +91,7 @@ _SIGS = {
     "am_get_chain_count": (C.c_size_t, [vp]),
     "am_render": (C.c_int, [vp, C.c_double, vp, C.c_int]),
     "am_render_many": (C.c_int, [vp, f64p, C.c_size_t, vp]),
+    "am_render_many_host": (C.c_int, [vp, f64p, C.c_size_t, vp]),
     "am_export_chains": (C.c_int, [vp, u64p, u64p, i32p]),
     "am_import_chains": (C.c_int, [vp, C.c_size_t, C.c_size_t, u64p, u64p, i32p]),
     "am_refine": (C.c_int, [vp, C.c_size_t, u64p]),

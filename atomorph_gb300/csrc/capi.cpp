@@ -323,6 +323,12 @@ int am_render_many(am_morph *m, const double *ts, size_t n, uint8_t *out) {
     return AM_OK;
 }
 
+int am_render_many_host(am_morph *m, const double *ts, size_t n, uint8_t *out) {
+    CHECK(m);
+    if ((!ts || !out) && n) return AM_ERR_ARG;
+    return H(m).render_many_host(ts, n, out);
+}
+
 int am_export_chains(am_morph *m, uint64_t *w, uint64_t *pts, int32_t *order) {
     CHECK(m);
     return H(m).export_chains(w, pts, order);

@@ -893,6 +893,24 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
     return AM_OK;
 }
 
+// n frames into consecutive host frames.  A pinned buffer covering all of
+// them is mapped: every frame is resolved straight into it, the frames
+// pipelined as device frames are, and the call waits once at the end.  Other
+// host memory takes the frames one at a time (render's copy path).
+int Engine::render_many_host(const double *ts, size_t n, uint8_t *out) {
+    const size_t fsz = (size_t)width * height * 4;
+    if (n == 0 || fsz == 0) return AM_OK;
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    uint8_t *dev = (fN && fK && front.fluidsteps == 0) ? mapped_host_range(out, n * fsz) : nullptr;
+    for (size_t i = 0; i < n; ++i) {
+        rc = dev ? render(ts[i], dev + i * fsz, true) : render(ts[i], out + i * fsz, false);
+        if (rc) return rc;
+    }
+    if (dev) AMG_CUDA(cudaStreamSynchronize(rstream));
+    return AM_OK;
+}
+
 // Render options of the front settings (feather, keep_background,
 // show_blobs) and the tables they read.
 void Engine::render_options(RenderScene &sc) const {

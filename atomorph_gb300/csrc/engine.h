@@ -205,6 +205,7 @@ class Engine {
     int compute_cost_noalloc(uint64_t *exact);  // noalloc.cu: static scratch, no device allocation
     int publish_front();
     int render(double t, uint8_t *out, bool out_dev);
+    int render_many_host(const double *ts, size_t n, uint8_t *out);
     int import_chains(size_t K, size_t C, const uint64_t *w, const uint64_t *pts, const int32_t *order);
     int export_chains(uint64_t *w, uint64_t *pts, int32_t *order);
     int set_chain_layout(const std::vector<uint64_t> &w);

@@ -212,6 +212,19 @@ def bench_ours(args, rank, world):
     e2e_s = time.perf_counter() - t0
     e2e = FRAMES_PER_STEP * args.steps * world / e2e_s
 
+    # a whole cycle per call into pinned host memory (am_render_many_host):
+    # frames pipelined and stored by the GPU directly, one wait per call
+    import ctypes as C
+    seq_host = torch.empty((FRAMES_PER_STEP, m.height, m.width, 4), dtype=torch.uint8).pin_memory()
+    ts_arr = np.ascontiguousarray(np.array(ts, np.float64))
+    tp = ts_arr.ctypes.data_as(C.POINTER(C.c_double))
+    assert m.lib.am_render_many_host(m.h, tp, len(ts), seq_host.data_ptr()) == 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert m.lib.am_render_many_host(m.h, tp, len(ts), seq_host.data_ptr()) == 0
+    seq_s = time.perf_counter() - t0
+    e2e_seq = FRAMES_PER_STEP * args.steps * world / seq_s
+
     # roofline of the dominant kernel from a profiled cycle
     prof = render_roofline(m, ts, torch, stream)
     per_frame = {k: v for k, v in prof.items() if v[1] > 0}
@@ -275,6 +288,9 @@ def bench_ours(args, rank, world):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": FRAMES_PER_STEP * fb},
+        "e2e_sequence": {"value": round(e2e_seq, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                         "d2h_bytes_per_step": FRAMES_PER_STEP * fb,
+                         "call": "am_render_many_host, 240 frames per call into pinned host memory"},
         "gpu_launches": int(launches),
         "roofline": roof,
         "clocks": clk.summary(),

@@ -190,6 +190,12 @@ size_t   am_get_chain_count(const am_morph *m);               /* chains = blob g
 int am_render(am_morph *m, double t, uint8_t *out, int out_on_device);
 /* Renders n frames at times ts[0..n) into n consecutive device frames. */
 int am_render_many(am_morph *m, const double *ts, size_t n, uint8_t *out_device);
+/* Renders n frames at times ts[0..n) into n consecutive host frames, complete
+ * when the call returns.  When out lies in pinned host memory whose
+ * allocation covers all n frames, atom frames are stored there by the GPU
+ * directly and pipelined like device frames; other memory receives the frames
+ * one at a time as am_render would. */
+int am_render_many_host(am_morph *m, const double *ts, size_t n, uint8_t *out);
 
 /* ---- chains (reference chain = points[width][height], atomorph.h:286-298)
  * pts is frame-major: pts[k * N + off_c + x] = point x of chain c at key

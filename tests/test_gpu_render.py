@@ -164,6 +164,25 @@ def test_device_frames_across_render_paths_match_host(capi):
             assert np.array_equal(got[i], want[k][i]), (plan[k], t)
 
 
+def test_render_many_host_matches_single_frames(capi):
+    """am_render_many_host: into a pinned buffer covering all frames (stored
+    by the GPU directly, pipelined) and into pageable memory (copied frame by
+    frame), the frames equal single am_render frames."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    g = golden("spline48")
+    m = morph_from_golden(capi, g)
+    ts = np.array([((i * 7) % 30) / 30.0 for i in range(30)], np.float64)
+    want = np.stack([m.render(float(t)) for t in ts])
+    tp = ts.ctypes.data_as(C.POINTER(C.c_double))
+    pinned = torch.full((len(ts), m.height, m.width, 4), 0x5A, dtype=torch.uint8).pin_memory()
+    assert m.lib.am_render_many_host(m.h, tp, len(ts), pinned.data_ptr()) == capi.AM_OK
+    assert np.array_equal(pinned.numpy(), want)
+    pageable = np.zeros_like(want)
+    assert m.lib.am_render_many_host(m.h, tp, len(ts), pageable.ctypes.data) == capi.AM_OK
+    assert np.array_equal(pageable, want)
+
+
 def test_render_into_pinned_host_memory_matches_pageable(capi):
     """Pinned host buffers are mapped into the GPU's address space and the
     resolve kernel stores the frame there directly; the frame must equal the
