@@ -7,11 +7,14 @@ overlapping ellipses/rectangles (~1M atoms per key frame), SPLINE motion,
 PERLIN colour fading, HSP blob delimiter.  Setup (untimed) runs the whole
 pipeline on the GPU: blobs, matching, chains, refinement.  One step renders
 the full morph cycle, 240 output frames at t = i/240, into device memory;
-``value`` is frames/s with everything resident in HBM.  ``e2e`` renders the
-same frames through the C ABI into pinned HOST memory (device->host copy of
-every frame inside the timed region).  ``time_to_cost`` reports the
-refinement side of the metric (plain random-pair sweeps vs the guided
-proposal) on the same chains.
+``value`` is frames/s with everything resident in HBM (frames pipelined: a
+frame's binning runs beside the previous frame's resolve).  ``e2e`` renders
+the same frames through the C ABI, one waited-for ``am_render`` call per
+frame, into pinned HOST memory: every frame reaches host memory inside the
+timed region (the resolve stores it there directly over the CPU-GPU link).
+``e2e_sequence`` does the same with ``am_render_many_host``, a whole cycle per
+call.  ``time_to_cost`` reports the refinement side of the metric (plain
+random-pair sweeps vs the guided and learned proposals) on the same chains.
 
 --impl reference times the reference's CPU implementation of the render on
 this machine's host cores: the oracle restatement (the reference itself is
