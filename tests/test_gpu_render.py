@@ -164,10 +164,11 @@ def test_device_frames_across_render_paths_match_host(capi):
             assert np.array_equal(got[i], want[k][i]), (plan[k], t)
 
 
-def test_render_many_host_matches_single_frames(capi):
-    """am_render_many_host: into a pinned buffer covering all frames (stored
-    by the GPU directly, pipelined) and into pageable memory (copied frame by
-    frame), the frames equal single am_render frames."""
+def test_render_many_matches_single_frames(capi):
+    """am_render_many_host into a pinned buffer covering all frames (stored by
+    the GPU directly, pipelined) and into pageable memory (copied frame by
+    frame), and am_render_many into device memory: every frame equals the
+    single am_render frame."""
     import ctypes as C
     torch = pytest.importorskip("torch")
     g = golden("spline48")
@@ -181,6 +182,11 @@ def test_render_many_host_matches_single_frames(capi):
     pageable = np.zeros_like(want)
     assert m.lib.am_render_many_host(m.h, tp, len(ts), pageable.ctypes.data) == capi.AM_OK
     assert np.array_equal(pageable, want)
+    # am_render_many: the same frames into device memory, left in flight
+    dev = torch.zeros((len(ts), m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    assert m.lib.am_render_many(m.h, tp, len(ts), dev.data_ptr()) == capi.AM_OK
+    assert m.lib.am_device_sync(m.h) == capi.AM_OK
+    assert np.array_equal(dev.cpu().numpy(), want)
 
 
 def test_render_into_pinned_host_memory_matches_pageable(capi):
