@@ -98,6 +98,7 @@ _SIGS = {
     "am_record_swaps": (C.c_int, [vp, C.c_size_t]),
     "am_recorded_swaps": (C.c_size_t, [vp, f32p, f32p, C.c_size_t]),
     "am_train_proposal": (C.c_int, [vp, f32p, f32p, C.c_size_t, C.c_size_t, C.c_double, f32p]),
+    "am_train_recorded": (C.c_int, [vp, C.c_size_t, C.c_double, f32p]),
     "am_get_proposal_weights": (C.c_int, [vp, f32p, C.c_size_t]),
     "am_set_proposal_weights": (C.c_int, [vp, f32p, C.c_size_t]),
     "am_proposal_forward": (C.c_int, [vp, f32p, C.c_size_t, f32p]),
@@ -385,6 +386,12 @@ class Morph:
         loss = C.c_float()
         _check(self.lib.am_train_proposal(self.h, _p(feats, f32p), _p(targets, f32p), len(targets), epochs, lr,
                                           C.byref(loss)), "am_train_proposal")
+        return loss.value
+
+    def train_recorded(self, epochs: int = 3, lr: float = 1e-3) -> float:
+        """Trains on the recorded samples in device memory; recording stops."""
+        loss = C.c_float()
+        _check(self.lib.am_train_recorded(self.h, epochs, lr, C.byref(loss)), "am_train_recorded")
         return loss.value
 
     def proposal_weights(self, w=None):

@@ -351,6 +351,12 @@ int am_refine(am_morph *m, size_t sweeps, uint64_t *gains) {
 // ---- learned proposal
 int am_record_swaps(am_morph *m, size_t cap) { CHECK(m); return H(m).record_swaps(cap); }
 size_t am_recorded_swaps(am_morph *m, float *f, float *t, size_t cap) { return m ? m->e.recorded_swaps(f, t, cap) : 0; }
+int am_train_recorded(am_morph *m, size_t epochs, double lr, float *loss) {
+    CHECK(m);
+    if (H(m).is_busy()) return AM_ERR_BUSY;
+    if (epochs == 0 || !(lr > 0.0)) return AM_ERR_ARG;
+    return H(m).train_recorded(epochs, lr, loss);
+}
 int am_train_proposal(am_morph *m, const float *f, const float *t, size_t n, size_t epochs, double lr, float *loss) {
     CHECK(m);
     if (H(m).is_busy()) return AM_ERR_BUSY;

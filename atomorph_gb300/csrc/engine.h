@@ -235,6 +235,8 @@ class Engine {
     int record_swaps(size_t cap);
     size_t recorded_swaps(float *feat, float *gains, size_t cap);
     int train_proposal(const float *feat, const float *gains, size_t n, size_t epochs, double lr, float *loss_out);
+    int train_recorded(size_t epochs, double lr, float *loss_out);
+    int train_device(const float *feat, const float *gains, size_t n, size_t epochs, double lr, float *loss_out);
     int proposal_weights(float *w, size_t count, bool set);
     int proposal_forward(const float *feat, size_t n, float *out);
     int proposal_grad(const float *feat, const float *target, size_t n, float *grad, float *loss);

@@ -87,6 +87,27 @@ int Engine::train_proposal(const float *feat, const float *gains, size_t n, size
     if ((rc = d_io_b.reserve(n))) return rc;
     AMG_CUDA(cudaMemcpyAsync(d_io_a.p, feat, n * kMlpIn * 4, cudaMemcpyHostToDevice, stream));
     AMG_CUDA(cudaMemcpyAsync(d_io_b.p, gains, n * 4, cudaMemcpyHostToDevice, stream));
+    return train_device(d_io_a.p, d_io_b.p, n, epochs, lr, loss_out);
+}
+
+// Trains on the samples the recording sweeps logged, where they lie in device
+// memory (no copy to the host and back); recording stops.
+int Engine::train_recorded(size_t epochs, double lr, float *loss_out) {
+    if (!d_rec_count.p) return AM_ERR_STATE;
+    int rc = mlp_init();
+    if (rc) return rc;
+    unsigned long long cnt = 0;
+    AMG_CUDA(cudaMemcpyAsync(&cnt, d_rec_count.p, 8, cudaMemcpyDeviceToHost, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    const size_t n = std::min<size_t>((size_t)cnt, (size_t)rec_cap);
+    if (n == 0) return AM_ERR_STATE;
+    recording = false;
+    return train_device(d_rec_feat.p, d_rec_gain.p, n, epochs, lr, loss_out);
+}
+
+int Engine::train_device(const float *feat, const float *gains, size_t n, size_t epochs, double lr,
+                         float *loss_out) {
+    int rc;
     const size_t batch = 16384, steps = (n + batch - 1) / batch;
     // one loss slot per minibatch, read once per epoch
     if ((rc = d_mlp_loss.reserve(steps))) return rc;
@@ -97,7 +118,7 @@ int Engine::train_proposal(const float *feat, const float *gains, size_t n, size
             const size_t b = k * batch, m = std::min(batch, n - b);
             ++adam_t;
             prof.open(stream);
-            rc = mlp_train_step(d_io_a.p + b * kMlpIn, d_io_b.p + b, m, d_mlp_master.p, d_mlp_dep.p, d_mlp_grad.p,
+            rc = mlp_train_step(feat + b * kMlpIn, gains + b, m, d_mlp_master.p, d_mlp_dep.p, d_mlp_grad.p,
                                 d_adam_m.p, d_adam_v.p, adam_t, (float)lr, d_mlp_loss.p + k, d_err.p, stream);
             if (rc) return rc;
             prof.close(PROF_MLP, stream);

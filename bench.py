@@ -382,8 +382,9 @@ def time_to_cost(capi, frames, args):
     runs until its cost is <= 1.005 C_plain.  All forms refine in blocks of
     `block` sweeps per am_refine call (each call also publishes the chains
     for rendering).  The learned form records its first guided sweeps, trains
-    its network on them on the GPU, and continues gated; recording and
-    training are inside its wall time."""
+    its network on them on the GPU where the recording left them
+    (am_train_recorded), and continues gated; recording and training are
+    inside its wall time."""
     out = {}
     B = args.block
     m = setup_morph(capi, frames, refine_sweeps=0)
@@ -428,11 +429,11 @@ def time_to_cost(capi, frames, args):
             c -= int(g.sum())
             if kind == capi.PROPOSAL_LEARNED and recording and t.recorded_count() >= args.learned_samples // 2:
                 t1 = time.perf_counter()
-                f, y = t.recorded_swaps(args.learned_samples)
-                loss = t.train_proposal(f, y, epochs=4, lr=2e-3)
+                n_rec = min(t.recorded_count(), args.learned_samples)
+                loss = t.train_recorded(epochs=4, lr=2e-3)  # on the device-resident sample log
                 t.record_swaps(0)
                 recording = False
-                info.update(trained_at_sweep=sweeps, samples=int(len(y)),
+                info.update(trained_at_sweep=sweeps, samples=int(n_rec),
                             train_s=round(time.perf_counter() - t1, 4), loss=round(float(loss), 5))
         info.update(sweeps_to_target=sweeps, s_to_target=round(time.perf_counter() - t0, 4), cost=int(c),
                     reached=bool(c <= target))

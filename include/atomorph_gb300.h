@@ -228,6 +228,10 @@ size_t am_recorded_swaps(am_morph *m, float *features, float *targets, size_t ca
  * samples for `epochs` passes; loss_out gets the last epoch's mean loss. */
 int    am_train_proposal(am_morph *m, const float *features, const float *targets, size_t n, size_t epochs,
                          double lr, float *loss_out);
+/* The same on the samples recorded since am_record_swaps, where the
+ * recording sweeps left them in device memory (no copy through the host);
+ * recording stops.  AM_ERR_STATE when nothing was recorded. */
+int    am_train_recorded(am_morph *m, size_t epochs, double lr, float *loss_out);
 int    am_get_proposal_weights(am_morph *m, float *w, size_t count);
 int    am_set_proposal_weights(am_morph *m, const float *w, size_t count);
 /* Scores of n feature rows, and the gradient of the mean squared error of n

@@ -144,3 +144,32 @@ def test_learned_proposal_end_to_end(capi, oracle):
         t.close()
     print("cost after %d gated sweeps (keep 1/4):" % sweeps, results, "start", c0)
     assert results["trained"] < results["untrained"], results
+
+
+def test_train_recorded_trains_on_device_samples(capi):
+    """am_train_recorded trains on the sample log where the recording sweeps
+    left it: the regression error on the recorded samples falls as with
+    am_train_proposal on the same samples copied through the host, and
+    without a recording it reports AM_ERR_STATE."""
+    import ctypes as C
+    frames = synth.workload("shapes256")
+    m = _chains(capi, frames, seed=3, blob_delimiter=0, motion=capi.LINEAR, fading=capi.LINEAR)
+    loss = C.c_float()
+    assert m.lib.am_train_recorded(m.h, 2, 2e-3, C.byref(loss)) == capi.AM_ERR_STATE
+    m.tune(guided_switch=0)
+    m.record_swaps(1 << 20)
+    m.refine(20, capi.PROPOSAL_LEARNED)
+    feats, targets = m.recorded_swaps(1 << 20)
+    untrained = m.proposal_weights()
+    pred_u = m.proposal_forward(feats[:20000])
+    l_dev = m.train_recorded(epochs=6, lr=2e-3)
+    assert np.isfinite(l_dev)
+    pred_t = m.proposal_forward(feats[:20000])
+    mse_u = float(np.mean((pred_u - targets[:20000]) ** 2))
+    mse_t = float(np.mean((pred_t - targets[:20000]) ** 2))
+    assert mse_t < 0.5 * mse_u
+    # the same samples through the host, from the same starting weights
+    h = _chains(capi, frames, seed=3, blob_delimiter=0, motion=capi.LINEAR, fading=capi.LINEAR)
+    h.proposal_weights(untrained)
+    l_host = h.train_proposal(feats, targets, epochs=6, lr=2e-3)
+    assert abs(l_host - l_dev) <= 0.05 * max(l_host, l_dev) + 1e-3
