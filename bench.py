@@ -430,7 +430,7 @@ def time_to_cost(capi, frames, args):
             if kind == capi.PROPOSAL_LEARNED and recording and t.recorded_count() >= args.learned_samples // 2:
                 t1 = time.perf_counter()
                 n_rec = min(t.recorded_count(), args.learned_samples)
-                loss = t.train_recorded(epochs=4, lr=2e-3)  # on the device-resident sample log
+                loss = t.train_recorded(epochs=args.learned_epochs, lr=2e-3)  # on the device-resident log
                 t.record_swaps(0)
                 recording = False
                 info.update(trained_at_sweep=sweeps, samples=int(n_rec),
@@ -661,6 +661,7 @@ def main():
     ap.add_argument("--proposal-max-s", type=float, default=30.0)
     ap.add_argument("--learned-keep", type=float, default=0.25)
     ap.add_argument("--learned-samples", type=int, default=1_000_000)
+    ap.add_argument("--learned-epochs", type=int, default=1)
     ap.add_argument("--cpu-frames", type=int, default=2)
     ap.add_argument("--batch-jobs", type=int, default=32)
     ap.add_argument("--batch-sweeps", type=int, default=200)
