@@ -188,8 +188,7 @@ def bench_ours(args, rank, world):
     launches0 = capi.launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    with Clocks(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
-                             f"clocks_rank{rank}.csv")) as clk:
+    with Clocks(os.path.join(args.clocks_dir, f"clocks_rank{rank}.csv")) as clk:
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(args.steps):
@@ -244,7 +243,8 @@ def bench_ours(args, rank, world):
     frame_ms = ms / (FRAMES_PER_STEP * args.steps)
     dom_name, (dom_ms, dom_n) = dom[0], dom[1]
     dom_avg_ms = dom_ms / dom_n
-    # Algorithmic bytes attributed to the dominant kernel (roofline)
+    # Algorithmic bytes per launch attributed to each kernel that can dominate:
+    # inputs read once and outputs written once (records 16 B, pixels 4 B)
     kernel_bytes = {
         "k_frame_bin": N * 56 + N * 16,
         "k_frame_splat": N * 56,
@@ -668,6 +668,7 @@ def main():
     ap.add_argument("--fluid-frames", type=int, default=24)
     ap.add_argument("--fluid-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--clocks-dir", default=".", help="where the nvidia-smi clock samples of the timed region go")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
