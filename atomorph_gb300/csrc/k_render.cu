@@ -1195,17 +1195,32 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
             // frames in flight read the old buffers
             AMG_CUDA(cudaStreamSynchronize(w->bs));
             AMG_CUDA(cudaStreamSynchronize(s));
-            w->slot_rec_cap = std::max(w->slot_rec_cap, need + need / 4);
-            w->slot_ovf_cap = std::max(w->slot_ovf_cap, need_ovf);
-            w->slot_tiles_cap = std::max(w->slot_tiles_cap, ntiles);
+            const uint64_t rc_new = std::max(w->slot_rec_cap, need + need / 4);
+            const uint64_t oc_new = std::max(w->slot_ovf_cap, need_ovf);
+            const uint32_t tc_new = std::max(w->slot_tiles_cap, ntiles);
+            // capacities are recorded only once every buffer exists: after a
+            // failed allocation the slots are empty and the next frame retries
+            w->slot_rec_cap = w->slot_ovf_cap = 0;
+            w->slot_tiles_cap = 0;
+            cudaError_t e = cudaSuccess;
             for (auto &sl : w->slot) {
                 slot_free(sl);
-                AMG_CUDA(cudaMalloc(&sl.rec, w->slot_rec_cap * sizeof(uint4)));
-                AMG_CUDA(cudaMalloc(&sl.ovf, w->slot_ovf_cap * sizeof(uint4)));
-                uint32_t **arrs[] = {&sl.off, &sl.cap, &sl.cnt};
-                for (uint32_t **q : arrs) AMG_CUDA(cudaMalloc(q, (size_t)w->slot_tiles_cap * 4));
-                AMG_CUDA(cudaMalloc(&sl.ovf_cnt, 4));
+                if (e == cudaSuccess) e = cudaMalloc(&sl.rec, rc_new * sizeof(uint4));
+                if (e == cudaSuccess) e = cudaMalloc(&sl.ovf, oc_new * sizeof(uint4));
+                if (e == cudaSuccess) e = cudaMalloc(&sl.off, (size_t)tc_new * 4);
+                if (e == cudaSuccess) e = cudaMalloc(&sl.cap, (size_t)tc_new * 4);
+                if (e == cudaSuccess) e = cudaMalloc(&sl.cnt, (size_t)tc_new * 4);
+                if (e == cudaSuccess) e = cudaMalloc(&sl.ovf_cnt, 4);
             }
+            if (e != cudaSuccess) {
+                for (auto &sl : w->slot) slot_free(sl);
+                cudaGetLastError();
+                set_error(std::string("render record slots: ") + cudaGetErrorString(e));
+                return AM_ERR_NOMEM;
+            }
+            w->slot_rec_cap = rc_new;
+            w->slot_ovf_cap = oc_new;
+            w->slot_tiles_cap = tc_new;
         }
         A = &w->slot[w->cur];
         B = &w->slot[w->cur ^ 1];
@@ -1236,12 +1251,13 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         tr = TileRecs{A->rec, A->off, A->cnt, A->cap, A->ovf, A->ovf_cnt, b.ovf_cap};
     } else {
         if (ntiles + 1 > w->ntiles_cap) {
-            if (w->tile_cnt) cudaFree(w->tile_cnt);
-            if (w->tile_off) cudaFree(w->tile_off);
-            if (w->tile_cur) cudaFree(w->tile_cur);
-            AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
-            AMG_CUDA(cudaMalloc(&w->tile_off, (ntiles + 1) * 4));
-            AMG_CUDA(cudaMalloc(&w->tile_cur, (ntiles + 1) * 4));
+            uint32_t **arrs[] = {&w->tile_cnt, &w->tile_off, &w->tile_cur};
+            for (uint32_t **q : arrs) {
+                if (*q) cudaFree(*q);
+                *q = nullptr;
+            }
+            w->ntiles_cap = 0;  // recorded once all three exist
+            for (uint32_t **q : arrs) AMG_CUDA(cudaMalloc(q, (size_t)(ntiles + 1) * 4));
             w->ntiles_cap = ntiles + 1;
         }
         // records of the separate kernels: 4 per atom
@@ -1249,8 +1265,9 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         if (need > w->rec_cap) {
             if (w->rec) cudaFree(w->rec);
             w->rec = nullptr;
+            w->rec_cap = 0;  // recorded once the buffer exists
+            AMG_CUDA(cudaMalloc(&w->rec, (need + need / 4) * sizeof(uint4)));
             w->rec_cap = need + need / 4;
-            AMG_CUDA(cudaMalloc(&w->rec, w->rec_cap * sizeof(uint4)));
         }
         if (!w->zero) {
             AMG_CUDA(cudaMalloc(&w->zero, 4));
