@@ -516,11 +516,15 @@ int label_components(BlobWork *w, const uint8_t *present, const uint32_t *stored
     size_t ntiles = (n + kScanTile - 1) / kScanTile;
     if (ntiles + 1 > w->tile_cap) {
         if (w->tile_cnt) cudaFree(w->tile_cnt);
+        w->tile_cnt = nullptr;
+        w->tile_cap = 0;  // recorded once the buffer exists
         AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
         w->tile_cap = ntiles + 1;
     }
     if (n > w->px_cap) {
         if (w->root_rank) cudaFree(w->root_rank);
+        w->root_rank = nullptr;
+        w->px_cap = 0;
         AMG_CUDA(cudaMalloc(&w->root_rank, n * 4));
         w->px_cap = n;
     }
@@ -578,12 +582,14 @@ int merge_blobs(BlobWork *w, const uint8_t *present, const uint32_t *stored, uin
     if (ntiles + 1 > w->tile_cap) {
         if (w->tile_cnt) cudaFree(w->tile_cnt);
         w->tile_cnt = nullptr;
+        w->tile_cap = 0;  // recorded once the buffer exists
         AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
         w->tile_cap = ntiles + 1;
     }
     if (n > w->px_cap) {
         if (w->root_rank) cudaFree(w->root_rank);
         w->root_rank = nullptr;
+        w->px_cap = 0;
         AMG_CUDA(cudaMalloc(&w->root_rank, n * 4));
         w->px_cap = n;
     }
@@ -594,6 +600,7 @@ int merge_blobs(BlobWork *w, const uint8_t *present, const uint32_t *stored, uin
     if (bytes > w->merge_cap) {
         if (w->merge) cudaFree(w->merge);
         w->merge = nullptr;
+        w->merge_cap = 0;
         AMG_CUDA(cudaMalloc(&w->merge, bytes));
         w->merge_cap = bytes;
     }

@@ -693,6 +693,7 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
                 if (*b.p) cudaFree(*b.p);
                 *b.p = nullptr;
             }
+            m->n = 0;  // the buffers are sized for (n, C, ...) only once all exist
             for (auto &b : bs) AMG_CUDA(cudaMalloc(b.p, std::max<size_t>(b.bytes, 8)));
             m->n = (uint32_t)N; m->C = sc.C; m->cw = sc.CW; m->ch = sc.CH; m->out_w = sc.width; m->out_h = sc.height;
             fluid_init_particles(fl, m, sc.width, sc.height, fr_in.sparseness, s);
