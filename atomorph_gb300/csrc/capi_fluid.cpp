@@ -72,6 +72,7 @@ int am_fluid_render_ex(am_fluid *h, uint32_t width, uint32_t height, double spar
     uint8_t *d = nullptr, *bg = nullptr;
     const size_t bytes = (size_t)width * height * 4;
     if (cudaMalloc(&d, bytes) != cudaSuccess || (background && cudaMalloc(&bg, bytes) != cudaSuccess)) {
+        cudaGetLastError();  // the failed allocation's pending error
         cudaFree(d);
         amg::set_error("cudaMalloc failed");
         return AM_ERR_NOMEM;

@@ -23,6 +23,21 @@ extern std::atomic<uint64_t> g_launches;      // kernels launched by the library
         }                                                                           \
     } while (0)
 
+// Device allocation inside a function returning an AM_* status.  A failed
+// cudaMalloc also leaves its error pending in the runtime (what the next
+// cudaGetLastError reports); it is taken off here, so the caller's next call
+// (which retries the allocation) is not failed by this one's error.
+#define AMG_ALLOC(ptr, bytes)                                                       \
+    do {                                                                            \
+        cudaError_t e_ = cudaMalloc((ptr), (bytes));                                \
+        if (e_ != cudaSuccess) {                                                    \
+            cudaGetLastError();                                                     \
+            *(ptr) = nullptr;                                                       \
+            ::amg::set_error(std::string("cudaMalloc(" #ptr "): ") + cudaGetErrorString(e_)); \
+            return AM_ERR_NOMEM;                                                    \
+        }                                                                           \
+    } while (0)
+
 // Launch bookkeeping: every kernel launch goes through this so the process-wide
 // launch counter (am_launch_count) is exact.
 #define AMG_LAUNCH(kernel, grid, block, smem, stream, ...)                          \

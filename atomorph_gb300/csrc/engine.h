@@ -68,6 +68,7 @@ struct DBuf {
         if (count == 0) return AM_OK;
         cudaError_t e = cudaMalloc(&p, count * sizeof(T));
         if (e != cudaSuccess) {
+            cudaGetLastError();  // the failed allocation's pending error, so the caller's retry can succeed
             set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
             p = nullptr;
             return AM_ERR_NOMEM;

@@ -518,17 +518,17 @@ int label_components(BlobWork *w, const uint8_t *present, const uint32_t *stored
         if (w->tile_cnt) cudaFree(w->tile_cnt);
         w->tile_cnt = nullptr;
         w->tile_cap = 0;  // recorded once the buffer exists
-        AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
+        AMG_ALLOC(&w->tile_cnt, (ntiles + 1) * 4);
         w->tile_cap = ntiles + 1;
     }
     if (n > w->px_cap) {
         if (w->root_rank) cudaFree(w->root_rank);
         w->root_rank = nullptr;
         w->px_cap = 0;
-        AMG_CUDA(cudaMalloc(&w->root_rank, n * 4));
+        AMG_ALLOC(&w->root_rank, n * 4);
         w->px_cap = n;
     }
-    if (!w->err) AMG_CUDA(cudaMalloc(&w->err, sizeof(int)));
+    if (!w->err) AMG_ALLOC(&w->err, sizeof(int));
     AMG_CUDA(cudaMemsetAsync(w->err, 0, sizeof(int), s));
     unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)kSMs * 16);
     AMG_LAUNCH(k_cc_init, grid, 256, 0, s, present, labels, n);
@@ -583,17 +583,17 @@ int merge_blobs(BlobWork *w, const uint8_t *present, const uint32_t *stored, uin
         if (w->tile_cnt) cudaFree(w->tile_cnt);
         w->tile_cnt = nullptr;
         w->tile_cap = 0;  // recorded once the buffer exists
-        AMG_CUDA(cudaMalloc(&w->tile_cnt, (ntiles + 1) * 4));
+        AMG_ALLOC(&w->tile_cnt, (ntiles + 1) * 4);
         w->tile_cap = ntiles + 1;
     }
     if (n > w->px_cap) {
         if (w->root_rank) cudaFree(w->root_rank);
         w->root_rank = nullptr;
         w->px_cap = 0;
-        AMG_CUDA(cudaMalloc(&w->root_rank, n * 4));
+        AMG_ALLOC(&w->root_rank, n * 4);
         w->px_cap = n;
     }
-    if (!w->err) AMG_CUDA(cudaMalloc(&w->err, sizeof(int)));
+    if (!w->err) AMG_ALLOC(&w->err, sizeof(int));
     // scratch: 7 x u32 + 4 x u64 + 2 x u8 per pixel, then the counters
     const size_t per = 7 * 4 + 4 * 8 + 2;
     const size_t bytes = n * per + 64;
@@ -601,7 +601,7 @@ int merge_blobs(BlobWork *w, const uint8_t *present, const uint32_t *stored, uin
         if (w->merge) cudaFree(w->merge);
         w->merge = nullptr;
         w->merge_cap = 0;
-        AMG_CUDA(cudaMalloc(&w->merge, bytes));
+        AMG_ALLOC(&w->merge, bytes);
         w->merge_cap = bytes;
     }
     unsigned char *b = (unsigned char *)w->merge;

@@ -299,7 +299,7 @@ int launch_scan_u32(uint32_t *a, size_t n, uint32_t *total, cudaStream_t s) {
         if (sums) cudaFree(sums);
         sums = nullptr;
         sums_cap = 0;
-        AMG_CUDA(cudaMalloc(&sums, (nb + 1) * sizeof(uint32_t)));
+        AMG_ALLOC(&sums, (nb + 1) * sizeof(uint32_t));
         sums_cap = nb + 1;
     }
     AMG_LAUNCH(k_scan_sums, (unsigned)nb, 1024, 0, s, a, n, sums);

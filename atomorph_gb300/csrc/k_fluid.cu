@@ -499,6 +499,7 @@ FluidDev *fluid_create(uint32_t gsx, uint32_t gsy, uint32_t n) {
         cudaMalloc(&f->keys, m * 4) != cudaSuccess || cudaMalloc(&f->ids, m * 4) != cudaSuccess ||
         cudaMalloc(&f->tkeys, m * 4) != cudaSuccess || cudaMalloc(&f->tids, m * 4) != cudaSuccess ||
         cudaMalloc(&f->hist, radix_hist_words(m) * 4) != cudaSuccess) {
+        cudaGetLastError();  // the failed allocation's pending error
         fluid_destroy(f);
         return nullptr;
     }

@@ -551,7 +551,7 @@ int grow(void **p, size_t bytes, size_t *cap) {
     if (*p) cudaFree(*p);
     *p = nullptr;
     *cap = 0;
-    AMG_CUDA(cudaMalloc(p, bytes));
+    AMG_ALLOC(p, bytes);
     *cap = bytes;
     return AM_OK;
 }
@@ -612,6 +612,7 @@ int fluid_render_only(FluidDev *fl, uint32_t width, uint32_t height, double spar
     uint8_t *mem = nullptr;
     if (cudaMalloc(&acc, 5 * npx * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&col, 2 * npx * 4) != cudaSuccess || cudaMalloc(&mem, 2 * npx) != cudaSuccess) {
+        cudaGetLastError();  // the failed allocation's pending error
         cudaFree(acc); cudaFree(col); cudaFree(mem);
         set_error("fluid draw: out of device memory");
         return AM_ERR_NOMEM;
@@ -694,7 +695,7 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
                 *b.p = nullptr;
             }
             m->n = 0;  // the buffers are sized for (n, C, ...) only once all exist
-            for (auto &b : bs) AMG_CUDA(cudaMalloc(b.p, std::max<size_t>(b.bytes, 8)));
+            for (auto &b : bs) AMG_ALLOC(b.p, std::max<size_t>(b.bytes, 8));
             m->n = (uint32_t)N; m->C = sc.C; m->cw = sc.CW; m->ch = sc.CH; m->out_w = sc.width; m->out_h = sc.height;
             fluid_init_particles(fl, m, sc.width, sc.height, fr_in.sparseness, s);
         }

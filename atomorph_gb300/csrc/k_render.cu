@@ -164,7 +164,7 @@ void render_invalidate(RenderWork *w) {
 int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope) {
     // frames in flight may still read the permutations (a seed change is rare)
     AMG_CUDA(cudaDeviceSynchronize());
-    if (!w->perm) AMG_CUDA(cudaMalloc(&w->perm, 1024 * sizeof(int)));
+    if (!w->perm) AMG_ALLOC(&w->perm, 1024 * sizeof(int));
     std::vector<int> h(1024);
     std::memcpy(h.data(), perm_lag, 512 * sizeof(int));
     std::memcpy(h.data() + 512, perm_slope, 512 * sizeof(int));
@@ -178,17 +178,17 @@ static int rw_reserve(RenderWork *w, uint64_t n) {
     if (n <= w->cap) return AM_OK;
     rw_free(w);
     uint64_t c = n + n / 8 + 1024;
-    AMG_CUDA(cudaMalloc(&w->pa, c * sizeof(int4)));
-    AMG_CUDA(cudaMalloc(&w->pb, c * sizeof(int4)));
-    AMG_CUDA(cudaMalloc(&w->col, c * sizeof(uint2)));
-    AMG_CUDA(cudaMalloc(&w->ls, c * sizeof(float2)));
-    AMG_CUDA(cudaMalloc(&w->rank, c * 4));
-    AMG_CUDA(cudaMalloc(&w->keys, c * 4));
-    AMG_CUDA(cudaMalloc(&w->vals, c * 4));
-    AMG_CUDA(cudaMalloc(&w->tkeys, c * 4));
-    AMG_CUDA(cudaMalloc(&w->tvals, c * 4));
-    AMG_CUDA(cudaMalloc(&w->hist, radix_hist_words(c) * 4));
-    AMG_CUDA(cudaMalloc(&w->spl, c * sizeof(uint4)));
+    AMG_ALLOC(&w->pa, c * sizeof(int4));
+    AMG_ALLOC(&w->pb, c * sizeof(int4));
+    AMG_ALLOC(&w->col, c * sizeof(uint2));
+    AMG_ALLOC(&w->ls, c * sizeof(float2));
+    AMG_ALLOC(&w->rank, c * 4);
+    AMG_ALLOC(&w->keys, c * 4);
+    AMG_ALLOC(&w->vals, c * 4);
+    AMG_ALLOC(&w->tkeys, c * 4);
+    AMG_ALLOC(&w->tvals, c * 4);
+    AMG_ALLOC(&w->hist, radix_hist_words(c) * 4);
+    AMG_ALLOC(&w->spl, c * sizeof(uint4));
     w->cap = c;
     return AM_OK;
 }
@@ -196,13 +196,13 @@ static int rw_reserve(RenderWork *w, uint64_t n) {
 static int pair_reserve(PairData &d, uint64_t c) {
     if (d.cap >= c) return AM_OK;
     pair_free(d);
-    AMG_CUDA(cudaMalloc(&d.pa, c * sizeof(int4)));
-    AMG_CUDA(cudaMalloc(&d.pb, c * sizeof(int4)));
-    AMG_CUDA(cudaMalloc(&d.col, c * sizeof(uint2)));
-    AMG_CUDA(cudaMalloc(&d.ls, c * sizeof(float2)));
-    AMG_CUDA(cudaMalloc(&d.rank, c * 4));
-    AMG_CUDA(cudaMalloc(&d.idx, c * 4));
-    AMG_CUDA(cudaMalloc(&d.d_active, 4));
+    AMG_ALLOC(&d.pa, c * sizeof(int4));
+    AMG_ALLOC(&d.pb, c * sizeof(int4));
+    AMG_ALLOC(&d.col, c * sizeof(uint2));
+    AMG_ALLOC(&d.ls, c * sizeof(float2));
+    AMG_ALLOC(&d.rank, c * 4);
+    AMG_ALLOC(&d.idx, c * 4);
+    AMG_ALLOC(&d.d_active, 4);
     d.cap = c;
     return AM_OK;
 }
@@ -1257,7 +1257,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
                 *q = nullptr;
             }
             w->ntiles_cap = 0;  // recorded once all three exist
-            for (uint32_t **q : arrs) AMG_CUDA(cudaMalloc(q, (size_t)(ntiles + 1) * 4));
+            for (uint32_t **q : arrs) AMG_ALLOC(q, (size_t)(ntiles + 1) * 4);
             w->ntiles_cap = ntiles + 1;
         }
         // records of the separate kernels: 4 per atom
@@ -1266,11 +1266,11 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
             if (w->rec) cudaFree(w->rec);
             w->rec = nullptr;
             w->rec_cap = 0;  // recorded once the buffer exists
-            AMG_CUDA(cudaMalloc(&w->rec, (need + need / 4) * sizeof(uint4)));
+            AMG_ALLOC(&w->rec, (need + need / 4) * sizeof(uint4));
             w->rec_cap = need + need / 4;
         }
         if (!w->zero) {
-            AMG_CUDA(cudaMalloc(&w->zero, 4));
+            AMG_ALLOC(&w->zero, 4);
             AMG_CUDA(cudaMemsetAsync(w->zero, 0, 4, s));
         }
         AMG_CUDA(cudaMemsetAsync(w->tile_cnt, 0, (ntiles + 1) * 4, s));

@@ -22,7 +22,9 @@
 //
 // Setup: the first call on each device, with that device current, looks up
 // the array's device address once (cudaGetSymbolAddress) and caches it; make
-// that first call before any stream capture begins.
+// that first call before any stream capture begins.  Each call makes the
+// handle's device current while it runs and restores the calling thread's
+// current device before it returns.
 #include <mutex>
 
 #include "engine.h"
@@ -128,7 +130,16 @@ int Engine::compute_cost_noalloc(uint64_t *exact) {
                   std::to_string(kCostMaxColumns));
         return AM_ERR_ARG;
     }
-    AMG_CUDA(cudaSetDevice(device));
+    // The handle's device is made current for the call and the caller's
+    // current device is put back on every return path.
+    struct DeviceGuard {
+        int prev = -1;
+        ~DeviceGuard() {
+            if (prev >= 0) cudaSetDevice(prev);
+        }
+    } guard;
+    AMG_CUDA(cudaGetDevice(&guard.prev));
+    if (guard.prev != device) AMG_CUDA(cudaSetDevice(device));
     unsigned long long *scratch = nullptr;
     int rc = cost_scratch(&scratch);
     if (rc) return rc;

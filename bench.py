@@ -116,6 +116,28 @@ class Clocks:
                 "reasons": sorted(reasons)}
 
 
+def physical_gpu_index(torch, dev):
+    """nvidia-smi index of torch device `dev`: its PCI bus id matched against
+    nvidia-smi's list (CUDA_VISIBLE_DEVICES renumbers devices; nvidia-smi does
+    not).  Falls back to the visible-device list, then to `dev`."""
+    try:
+        pr = torch.cuda.get_device_properties(dev)
+        bus = f"{pr.pci_domain_id:08X}:{pr.pci_bus_id:02X}:{pr.pci_device_id:02X}.0"
+        out = subprocess.run(["nvidia-smi", "--query-gpu=index,pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=20).stdout
+        for line in out.strip().splitlines():
+            idx, b = [c.strip() for c in line.split(",")]
+            if b.upper().endswith(bus[-12:]):
+                return int(idx)
+    except Exception:
+        pass
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    ids = [v.strip() for v in vis.split(",") if v.strip()]
+    if dev < len(ids) and ids[dev].isdigit():
+        return int(ids[dev])
+    return dev
+
+
 def setup_morph(capi, frames, refine_sweeps):
     m = capi.Morph()
     m.load(frames, **SETTINGS)
@@ -165,7 +187,9 @@ def bench_ours(args, rank, world):
     import torch
     from atomorph_gb300 import capi, synth
 
-    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    dev = 0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(dev)
+    gpu_index = physical_gpu_index(torch, dev)
     frames = synth.workload(WORKLOAD)
     atoms_per_frame = int(np.mean([synth.opaque_count(f) for f in frames]))
     m = setup_morph(capi, frames, refine_sweeps=args.refine_sweeps)
@@ -296,7 +320,7 @@ def bench_ours(args, rank, world):
                          "call": "am_render_many_host, 240 frames per call into pinned host memory"},
         "gpu_launches": int(launches),
         "roofline": roof,
-        "clocks": clk.summary(),
+        "clocks": clk.summary(gpu_index),
     }
     if flu is not None:
         res["fluid"] = flu
@@ -646,6 +670,67 @@ def cpu_pipeline(O, frames):
                 frame_keys=np.arange(K, dtype=np.uint64))
 
 
+def profile_case(args):
+    """Every kernel of the morph path, a few launches each, on one seeded
+    workload: the program the per-kernel ncu captures under profiles/ run.
+    After the pipeline (components, blob matching, chain construction): 4
+    plain sweeps, 4 guided sweeps, 2 recorded sweeps, one training epoch, 4
+    gated (learned) sweeps, the allocation-free cost, `--frames` atom frames,
+    2 fluid frames with 2 solver steps each on a (0.5 W + 20)^2 grid, and one
+    batched refinement of 4 small jobs.  Settings as the benchmark's."""
+    import ctypes as C
+
+    import torch
+    from atomorph_gb300 import capi, synth
+
+    keys = synth.workload(args.workload)
+    m = capi.Morph()
+    m.load(keys, **SETTINGS)
+    if args.motion_noise:
+        m.set(motion_noise=args.motion_noise)
+    if m.run_until(capi.STATE_ATOM_MORPHING) != capi.STATE_ATOM_MORPHING:
+        raise RuntimeError("pipeline stopped early")
+    m.refine(4, capi.PROPOSAL_RANDOM)
+    m.tune(guided_switch=0)
+    m.refine(4, capi.PROPOSAL_LOCAL)
+    m.tune(learned_adaptive=0)
+    m.record_swaps(1 << 22)  # recording sweeps run the learned form's gate with every region kept
+    m.refine(2, capi.PROPOSAL_LEARNED)
+    f, y = m.recorded_swaps(1 << 22)
+    m.record_swaps(0)
+    if not len(y):
+        raise RuntimeError("no recorded samples")
+    m.train_proposal(f, y, epochs=1, lr=2e-3)
+    m.refine(4, capi.PROPOSAL_LEARNED)
+    v = C.c_uint64()
+    rc = m.lib.am_get_cost_noalloc(m.h, C.byref(v))
+    if rc:
+        raise RuntimeError(f"am_get_cost_noalloc: {rc}")
+    out = torch.empty((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    for i in range(args.frames):
+        m.render_device(m.get_time(i * 7 + 1, 240), out.data_ptr())
+    m.set(fluid=2, fluid_sparseness=0.5)
+    for i in range(2):
+        m.render_device(m.get_time(i, 240), out.data_ptr())
+    m.set(fluid=0)
+    torch.cuda.synchronize()
+    jobs = []
+    for j in range(4):
+        a = capi.Morph()
+        a.load(synth.workload("batch", j), seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+        if a.run_until(capi.STATE_ATOM_MORPHING) != capi.STATE_ATOM_MORPHING:
+            raise RuntimeError(f"batch job {j}: pipeline stopped early")
+        jobs.append(a)
+    b = capi.Batch(jobs)
+    b.refine(4)
+    b.close()
+    for a in jobs:
+        a.close()
+    res = {"profile_case": args.workload, "atoms": m.atoms, "cost": int(v.value), "samples": int(len(y))}
+    m.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -669,7 +754,16 @@ def main():
     ap.add_argument("--fluid-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--clocks-dir", default=".", help="where the nvidia-smi clock samples of the timed region go")
+    ap.add_argument("--motion-noise", type=float, default=2.0,
+                    help="Perlin motion perturbation amplitude in px (0 = spline paths alone)")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run every kernel of the path a few times on --workload (for ncu captures) and exit")
+    ap.add_argument("--workload", default=WORKLOAD, help="workload of --profile-case")
+    ap.add_argument("--frames", type=int, default=3, help="atom frames of --profile-case")
     args = ap.parse_args()
+    if args.profile_case:
+        print(json.dumps(profile_case(args)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":

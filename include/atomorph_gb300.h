@@ -159,7 +159,9 @@ int      am_get_cost(am_morph *m, uint64_t *exact, double *as_double);
  * calls that overlap in time race and must be serialised by the caller.
  * Accepts chains of at most 2^27 columns (atoms x key frames); larger ones
  * return AM_ERR_ARG.  The first call on a device looks up the array's
- * address: make it before any stream capture begins. */
+ * address: make it before any stream capture begins.  The call runs on the
+ * handle's device and leaves the calling thread's current device as it
+ * found it. */
 int      am_get_cost_noalloc(am_morph *m, uint64_t *exact);
 size_t   am_get_blob_count(const am_morph *m, size_t frame);  /* morph::get_blob_count(f) morph.cpp:399-402 */
 size_t   am_get_blob_count_total(const am_morph *m);          /* morph::get_blob_count() morph.cpp:425-434 */

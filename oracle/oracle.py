@@ -21,7 +21,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SOURCES = "/root/reference"
+# Where the reference sources are (the fixtures' generator and the live pin
+# build the unmodified reference from them); absent on machines without them.
+REF_SOURCES = os.environ.get("ATOMORPH_REFERENCE", "/root/reference")
 
 u8p = C.POINTER(C.c_uint8)
 u32p = C.POINTER(C.c_uint32)

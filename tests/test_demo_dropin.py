@@ -11,7 +11,7 @@ import subprocess
 
 import pytest
 
-REF = "/root/reference"
+REF = os.environ.get("ATOMORPH_REFERENCE", "/root/reference")  # the reference sources, where present
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
