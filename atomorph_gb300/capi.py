@@ -91,6 +91,7 @@ _SIGS = {
     "am_get_chain_count": (C.c_size_t, [vp]),
     "am_render": (C.c_int, [vp, C.c_double, vp, C.c_int]),
     "am_render_many": (C.c_int, [vp, f64p, C.c_size_t, vp]),
+    "am_get_positions": (C.c_size_t, [vp, C.c_double, i32p, C.c_size_t]),
     "am_render_many_host": (C.c_int, [vp, f64p, C.c_size_t, vp]),
     "am_export_chains": (C.c_int, [vp, u64p, u64p, i32p]),
     "am_import_chains": (C.c_int, [vp, C.c_size_t, C.c_size_t, u64p, u64p, i32p]),
@@ -337,6 +338,17 @@ class Morph:
         out = np.zeros((self.height, self.width, 4), np.uint8)
         _check(self.lib.am_render(self.h, t, out.ctypes.data, 0), "am_render")
         return out
+
+    def positions(self, t: float) -> np.ndarray:
+        """[N, 2] position words (integer pixel * 256 + fraction byte) of every
+        atom column at time t as the render places them; -1 where not drawn."""
+        n = self.lib.am_get_positions(self.h, t, None, 0)
+        out = np.zeros((max(n, 1), 2), np.int32)
+        if n:
+            got = self.lib.am_get_positions(self.h, t, _p(out, i32p), n)
+            if got != n:
+                raise AmError(AM_ERR_CUDA, "am_get_positions")
+        return out[:n]
 
     def render_device(self, t: float, dev_ptr: int) -> None:
         _check(self.lib.am_render(self.h, t, dev_ptr, 1), "am_render")

@@ -158,7 +158,7 @@ size_t am_get_fluid_particles(am_morph *m, double *state, size_t cap) {
 }
 int am_set_motion_noise(am_morph *m, double a) {
     CHECK(m);
-    if (!(a >= 0.0)) return AM_ERR_ARG;
+    if (!(a >= 0.0 && a <= 64.0)) return AM_ERR_ARG;
     H(m).front.motion_noise = a;
     return AM_OK;
 }
@@ -311,6 +311,12 @@ int am_render(am_morph *m, double t, uint8_t *out, int on_dev) {
     CHECK(m);
     if (!out) return AM_ERR_ARG;
     return H(m).render(t, out, on_dev != 0);
+}
+size_t am_get_positions(am_morph *m, double t, int32_t *xy, size_t cap) {
+    if (!m) return 0;
+    size_t n = 0;
+    if (H(m).positions(t, xy, cap, &n) != AM_OK) return 0;
+    return n;
 }
 int am_render_many(am_morph *m, const double *ts, size_t n, uint8_t *out) {
     CHECK(m);

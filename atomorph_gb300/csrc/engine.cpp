@@ -45,6 +45,9 @@ Engine::Engine() {
     // Default-constructed PerlinNoise maps use seed 1 (perlin.h:7, morph.h:136-137).
     perlin_perm(1, perm_lag);
     perlin_perm(1, perm_slope);
+    // The motion perturbation's maps: seed + 2 and seed + 3 of the morph's seed (0 until set).
+    perlin_perm(2, perm_mx);
+    perlin_perm(3, perm_my);
 }
 
 Engine::~Engine() {
@@ -76,7 +79,7 @@ static int ensure_streams(Engine *e) {
     e->rw = render_work_create();
     e->bw = blob_work_create();
     render_set_prof(e->rw, &e->prof);
-    int rc = render_set_perlin(e->rw, e->perm_lag, e->perm_slope);
+    int rc = render_set_perlin(e->rw, e->perm_lag, e->perm_slope, e->perm_mx, e->perm_my);
     return rc;
 }
 
@@ -165,7 +168,9 @@ void Engine::set_seed(unsigned s) {
     seed = s;
     perlin_perm(s, perm_lag);
     perlin_perm(s + 1, perm_slope);
-    if (rw) render_set_perlin(rw, perm_lag, perm_slope);
+    perlin_perm(s + 2, perm_mx);
+    perlin_perm(s + 3, perm_my);
+    if (rw) render_set_perlin(rw, perm_lag, perm_slope, perm_mx, perm_my);
 }
 
 int Engine::clear() {
@@ -873,6 +878,7 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         sc.bbox[0] = bbox_x1; sc.bbox[1] = bbox_y1; sc.bbox[2] = bbox_x2; sc.bbox[3] = bbox_y2;
         sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
         sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
+        sc.motion_noise = front.motion_noise;
         render_options(sc);
         // host frames too: the tile plan for the next frame then runs on the
         // second stream, after the resolve the caller waits for
@@ -890,6 +896,32 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
     } else {
         AMG_CUDA(cudaGetLastError());
     }
+    return AM_OK;
+}
+
+// Every atom's position at time `time` as the render places it (host xy,
+// 2 words per atom column); returns the atom count.
+int Engine::positions(double time, int32_t *xy, size_t cap, size_t *count) {
+    *count = fN;
+    if (!xy || cap < fN || fN == 0 || fK == 0) return AM_OK;
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    if ((rc = d_pos.reserve(2 * fN))) return rc;
+    double integ;
+    double t = std::modf(time, &integ);
+    if (t < 0.0) t += 1.0;
+    RenderScene sc;
+    sc.K = fK; sc.C = fC; sc.N = fN; sc.CW = CW; sc.CH = CH; sc.width = width; sc.height = height;
+    sc.bbox[0] = bbox_x1; sc.bbox[1] = bbox_y1; sc.bbox[2] = bbox_x2; sc.bbox[3] = bbox_y2;
+    sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
+    sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
+    sc.motion_noise = front.motion_noise;
+    render_options(sc);
+    const size_t f = (size_t)(t * fK);
+    const uint64_t key = f < f_keys.size() ? f_keys[f] : 0;
+    if ((rc = render_positions(rw, sc, t, key, d_pos.p, rstream))) return rc;
+    AMG_CUDA(cudaMemcpyAsync(xy, d_pos.p, fN * 8, cudaMemcpyDeviceToHost, rstream));
+    AMG_CUDA(cudaStreamSynchronize(rstream));
     return AM_OK;
 }
 
@@ -965,6 +997,7 @@ int Engine::render_fluid(double t, uint8_t *dst) {
     fr.sc.K = fK; fr.sc.C = fC; fr.sc.N = fN; fr.sc.CW = CW; fr.sc.CH = CH; fr.sc.width = width; fr.sc.height = height;
     fr.sc.bbox[0] = bbox_x1; fr.sc.bbox[1] = bbox_y1; fr.sc.bbox[2] = bbox_x2; fr.sc.bbox[3] = bbox_y2;
     fr.sc.motion = front.motion; fr.sc.fading = front.fading; fr.sc.density = front.density;
+    fr.sc.motion_noise = front.motion_noise;
     fr.sc.P = d_Pf.p; fr.sc.chain_off = d_chain_off_f.p; fr.sc.display = d_display.p; fr.sc.rank = d_rank_f.p;
     render_options(fr.sc);
     const size_t f = std::min<size_t>((size_t)(t * fK), fK - 1);

@@ -100,7 +100,7 @@ class Engine {
     size_t identifier = 0;
     bool skip_state = false;
     unsigned seed = 0;
-    int perm_lag[512], perm_slope[512];
+    int perm_lag[512], perm_slope[512], perm_mx[512], perm_my[512];  // Perlin maps: seed, +1, +2, +3
 
     int add_pixel(size_t f, uint16_t x, uint16_t y, uint32_t rgba);
     int add_pixels(size_t f, const uint8_t *rgba, uint32_t w, uint32_t h);
@@ -207,6 +207,8 @@ class Engine {
     int publish_front();
     int render(double t, uint8_t *out, bool out_dev);
     int render_many_host(const double *ts, size_t n, uint8_t *out);
+    int positions(double time, int32_t *xy, size_t cap, size_t *count);
+    DBuf<int32_t> d_pos;                   // position readout
     int import_chains(size_t K, size_t C, const uint64_t *w, const uint64_t *pts, const int32_t *order);
     int export_chains(uint64_t *w, uint64_t *pts, int32_t *order);
     int set_chain_layout(const std::vector<uint64_t> &w);

@@ -313,8 +313,8 @@ __global__ void k_fm_assign2(FmArgs a, uint32_t n) {
 
 // update_particle (morph.cpp:680-805) for every active particle.
 __global__ void k_fm_update(FmArgs a) {
-    __shared__ int sp[1024];
-    for (int i = threadIdx.x; i < 1024; i += blockDim.x) sp[i] = a.perm ? a.perm[i] : 0;
+    __shared__ int sp[2048];  // lag, slope, motion x, motion y permutations
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) sp[i] = a.perm ? a.perm[i] : 0;
     __syncthreads();
     const float bw = (float)(a.bbox[2] - a.bbox[0] + 1), bh = (float)(a.bbox[3] - a.bbox[1] + 1);
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < a.N; s += (uint64_t)gridDim.x * blockDim.x) {
@@ -364,6 +364,14 @@ __global__ void k_fm_update(FmArgs a) {
                 X = spl_fixed(a.fa.b0, a.fa.b1, a.fa.b2, a.fa.b3, pt_X(q0), pt_X(q1), pt_X(q2), pt_X(q3));
             if (!spl_fast(a.fa, pt_Y(q0), pt_Y(q1), pt_Y(q2), pt_Y(q3), &Y))
                 Y = spl_fixed(a.fa.b0, a.fa.b1, a.fa.b2, a.fa.b3, pt_Y(q0), pt_Y(q1), pt_Y(q2), pt_Y(q3));
+        }
+        if (a.fa.noise_s != 0.f) {
+            // the Perlin motion perturbation of the atom render, at the source point
+            const int bwi = (int)(a.bbox[2] - a.bbox[0] + 1), bhi = (int)(a.bbox[3] - a.bbox[1] + 1);
+            const float u = noise_coord_rn((int)pt_x(pt1), (int)pt_xf(pt1), (int)a.bbox[0], bwi);
+            const float v = noise_coord_rn((int)pt_y(pt1), (int)pt_yf(pt1), (int)a.bbox[1], bhi);
+            X = displace_rn(X, a.fa.noise_s, poctave_rn(sp + 1024, u, v));
+            Y = displace_rn(Y, a.fa.noise_s, poctave_rn(sp + 1536, u, v));
         }
         const float ptx = (float)(X >> 8) + (float)(X & 255u) / 256.f;
         const float pty = (float)(Y >> 8) + (float)(Y & 255u) / 256.f;

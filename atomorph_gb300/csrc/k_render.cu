@@ -44,10 +44,12 @@ constexpr uint32_t kInactive = 0xFFFFFFFFu;
 struct PairData {
     int f = -1;                          // key frame of the pair held (-1: none)
     uint32_t motion = 0, fading = 0, width = 0, height = 0;
+    bool noise = false;                  // mn holds the motion perturbation's noise values
     uint64_t cap = 0;
     int4 *pa = nullptr, *pb = nullptr;   // endpoints / spline control points
     uint2 *col = nullptr;
     float2 *ls = nullptr;
+    float2 *mn = nullptr;                // motion noise (x, y) at the atom's first point
     uint32_t *rank = nullptr, *idx = nullptr;
     uint32_t *d_active = nullptr;        // active (sorted first) atoms, on the device
 };
@@ -56,7 +58,7 @@ struct RenderWork {
     uint64_t cap = 0;       // atom capacity of the prep scratch below
     int4 *pa = nullptr, *pb = nullptr;   // unsorted prep output (scratch)
     uint2 *col = nullptr;
-    float2 *ls = nullptr;
+    float2 *ls = nullptr, *mn = nullptr;
     uint32_t *rank = nullptr;
     uint32_t *keys = nullptr, *vals = nullptr, *tkeys = nullptr, *tvals = nullptr, *hist = nullptr;
     uint4 *spl = nullptr;
@@ -85,7 +87,7 @@ struct RenderWork {
     cudaEvent_t binned = nullptr, mark = nullptr;
     bool bs_after_s = false;             // bs must wait for the render stream before its next work
     bool s_after_bs = false;             // the render stream must wait for bs before touching slots or pairs
-    int *perm = nullptr;    // [2][512] Perlin permutations on the device
+    int *perm = nullptr;    // [4][512] Perlin permutations on the device (lag, slope, motion x, motion y)
     bool perm_set = false;
     Prof *prof = nullptr;   // optional per-kernel timing
 };
@@ -93,7 +95,7 @@ struct RenderWork {
 // Device memory the pair cache may hold (beyond one pair, which is always
 // kept): all K pairs of a 1M-atom, 8-key-frame morph take 450 MB.
 constexpr uint64_t kPairCacheBytes = 8ull << 30;
-constexpr uint64_t kPairBytesPerAtom = 16 + 16 + 8 + 8 + 4 + 4;
+constexpr uint64_t kPairBytesPerAtom = 16 + 16 + 8 + 8 + 8 + 4 + 4;
 
 void render_set_prof(RenderWork *w, Prof *p) { w->prof = p; }
 Prof *render_prof(RenderWork *w) { return w ? w->prof : nullptr; }
@@ -101,19 +103,19 @@ Prof *render_prof(RenderWork *w) { return w ? w->prof : nullptr; }
 RenderWork *render_work_create() { return new RenderWork(); }
 
 static void pair_free(PairData &d) {
-    void *ps[] = {d.pa, d.pb, d.col, d.ls, d.rank, d.idx, d.d_active};
+    void *ps[] = {d.pa, d.pb, d.col, d.ls, d.mn, d.rank, d.idx, d.d_active};
     for (void *p : ps)
         if (p) cudaFree(p);
     d = PairData();
 }
 
 static void rw_free(RenderWork *w) {
-    void *ps[] = {w->pa, w->pb, w->col, w->ls, w->rank, w->keys, w->vals, w->tkeys, w->tvals, w->hist, w->spl};
+    void *ps[] = {w->pa, w->pb, w->col, w->ls, w->mn, w->rank, w->keys, w->vals, w->tkeys, w->tvals, w->hist, w->spl};
     for (void *p : ps)
         if (p) cudaFree(p);
     w->pa = w->pb = nullptr;
     w->col = nullptr;
-    w->ls = nullptr;
+    w->ls = w->mn = nullptr;
     w->rank = w->keys = w->vals = w->tkeys = w->tvals = w->hist = nullptr;
     w->spl = nullptr;
     w->cap = 0;
@@ -161,14 +163,17 @@ void render_invalidate(RenderWork *w) {
     for (auto &d : w->pairs) d.f = -1;
 }
 
-int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope) {
+int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope, const int *perm_mx,
+                      const int *perm_my) {
     // frames in flight may still read the permutations (a seed change is rare)
     AMG_CUDA(cudaDeviceSynchronize());
-    if (!w->perm) AMG_ALLOC(&w->perm, 1024 * sizeof(int));
-    std::vector<int> h(1024);
+    if (!w->perm) AMG_ALLOC(&w->perm, 2048 * sizeof(int));
+    std::vector<int> h(2048);
     std::memcpy(h.data(), perm_lag, 512 * sizeof(int));
     std::memcpy(h.data() + 512, perm_slope, 512 * sizeof(int));
-    AMG_CUDA(cudaMemcpy(w->perm, h.data(), 1024 * sizeof(int), cudaMemcpyHostToDevice));
+    std::memcpy(h.data() + 1024, perm_mx, 512 * sizeof(int));
+    std::memcpy(h.data() + 1536, perm_my, 512 * sizeof(int));
+    AMG_CUDA(cudaMemcpy(w->perm, h.data(), 2048 * sizeof(int), cudaMemcpyHostToDevice));
     w->perm_set = true;
     render_invalidate(w);
     return AM_OK;
@@ -182,6 +187,7 @@ static int rw_reserve(RenderWork *w, uint64_t n) {
     AMG_ALLOC(&w->pb, c * sizeof(int4));
     AMG_ALLOC(&w->col, c * sizeof(uint2));
     AMG_ALLOC(&w->ls, c * sizeof(float2));
+    AMG_ALLOC(&w->mn, c * sizeof(float2));
     AMG_ALLOC(&w->rank, c * 4);
     AMG_ALLOC(&w->keys, c * 4);
     AMG_ALLOC(&w->vals, c * 4);
@@ -200,6 +206,7 @@ static int pair_reserve(PairData &d, uint64_t c) {
     AMG_ALLOC(&d.pb, c * sizeof(int4));
     AMG_ALLOC(&d.col, c * sizeof(uint2));
     AMG_ALLOC(&d.ls, c * sizeof(float2));
+    AMG_ALLOC(&d.mn, c * sizeof(float2));
     AMG_ALLOC(&d.rank, c * 4);
     AMG_ALLOC(&d.idx, c * 4);
     AMG_ALLOC(&d.d_active, 4);
@@ -219,12 +226,13 @@ __device__ __forceinline__ uint32_t find_chain_r(const uint64_t *__restrict__ of
 }
 
 __global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, const int *__restrict__ perm,
-                                                    int4 *pa, int4 *pb, uint2 *col, float2 *ls, uint32_t *rank,
-                                                    uint32_t *keys, uint32_t *vals, uint32_t tiles_x,
+                                                    int4 *pa, int4 *pb, uint2 *col, float2 *ls, float2 *mn,
+                                                    uint32_t *rank, uint32_t *keys, uint32_t *vals, uint32_t tiles_x,
                                                     uint32_t inactive_key, uint32_t key_shift) {
-    __shared__ int sp[1024];
-    for (int i = threadIdx.x; i < 1024; i += blockDim.x) sp[i] = perm ? perm[i] : 0;
+    __shared__ int sp[2048];  // lag, slope, motion x, motion y permutations
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) sp[i] = perm ? perm[i] : 0;
     __syncthreads();
+    const int bwi = (int)(sc.bbox[2] - sc.bbox[0] + 1), bhi = (int)(sc.bbox[3] - sc.bbox[1] + 1);
     const uint32_t y = f, yn = (f + 1) % sc.K;
     const float bw = (float)(sc.bbox[2] - sc.bbox[0] + 1), bh = (float)(sc.bbox[3] - sc.bbox[1] + 1);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < sc.N; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -264,6 +272,12 @@ __global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, c
             slope = poctave(sp + 512, px, py) * 0.5f + 0.5f;
         }
         ls[i] = fade_params(lag, slope);
+        if (mn) {
+            // the motion perturbation's noise at pt1 (x map seed + 2, y map seed + 3)
+            const float u = noise_coord_rn((int)pt_x(w1), (int)pt_xf(w1), (int)sc.bbox[0], bwi);
+            const float v = noise_coord_rn((int)pt_y(w1), (int)pt_yf(w1), (int)sc.bbox[1], bhi);
+            mn[i] = make_float2(poctave_rn(sp + 1024, u, v), poctave_rn(sp + 1536, u, v));
+        }
         rank[i] = (uint32_t)sc.rank[(size_t)f * sc.C + c];
         int mx = ((X1 + X2) >> 9), my = ((Y1 + Y2) >> 9);
         mx = min(max(mx, 0), (int)sc.width - 1);
@@ -278,8 +292,8 @@ __global__ void __launch_bounds__(256) k_pair_prep(RenderScene sc, uint32_t f, c
 }
 
 __global__ void k_pair_gather(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ order, uint64_t n,
-                              const int4 *pa, const int4 *pb, const uint2 *col, const float2 *ls,
-                              const uint32_t *rank, int4 *pa2, int4 *pb2, uint2 *col2, float2 *ls2,
+                              const int4 *pa, const int4 *pb, const uint2 *col, const float2 *ls, const float2 *mn,
+                              const uint32_t *rank, int4 *pa2, int4 *pb2, uint2 *col2, float2 *ls2, float2 *mn2,
                               uint32_t *rank2, uint32_t *idx2, int spline, uint32_t *active) {
     for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t i = order[j];
@@ -294,6 +308,7 @@ __global__ void k_pair_gather(const uint32_t *__restrict__ keys, const uint32_t 
         if (spline) pb2[j] = pb[i];
         col2[j] = col[i];
         ls2[j] = ls[i];
+        if (mn) mn2[j] = mn[i];
         if (j + 1 == n) *active = (uint32_t)n;
     }
 }
@@ -320,6 +335,7 @@ struct SplatIn {
     const uint2 *col;
     const float2 *ls;
     const uint32_t *rank, *idx;
+    const float2 *mn;  // motion noise per atom (read when the frame's noise scale is not 0)
 };
 
 // One atom at the frame's time: exact position, faded colour and the valid
@@ -403,6 +419,11 @@ __device__ __forceinline__ uint4 splat_atom(const RenderScene &sc, const FrameAr
     uint32_t X, Y;
     if (!axis_fast(sc, fa, 0, a, b, &X)) X = axis_fixed(sc, fa, 0, a, b);
     if (!axis_fast(sc, fa, 1, a, b, &Y)) Y = axis_fixed(sc, fa, 1, a, b);
+    if (fa.noise_s != 0.f) {
+        const float2 nz = in.mn[i];
+        X = displace_rn(X, fa.noise_s, nz.x);
+        Y = displace_rn(Y, fa.noise_s, nz.y);
+    }
     uint2 c = in.col[i];
     float2 q = in.ls[i];
     return finish_record(sc, X, Y, fade_colour(sc.fading, c.x, c.y, q, fa.str), in.rank[i]);
@@ -452,6 +473,28 @@ __global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs f
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < fa.ntiles; i += blockDim.x)
             if (hist[i]) atomicAdd(&tile_cnt[i], hist[i]);
+    }
+}
+
+// Every active atom's position words at the frame's time (the readout of the
+// positions the splat uses): xy[2 idx], xy[2 idx + 1], idx the atom's column.
+__global__ void __launch_bounds__(256) k_atom_positions(RenderScene sc, FrameArgs fa, const uint32_t *n_dev,
+                                                         SplatIn in, int32_t *xy) {
+    const uint64_t n = *n_dev;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        int4 a, b;
+        atom_controls(sc, fa, in, i, a, b);
+        uint32_t X, Y;
+        if (!axis_fast(sc, fa, 0, a, b, &X)) X = axis_fixed(sc, fa, 0, a, b);
+        if (!axis_fast(sc, fa, 1, a, b, &Y)) Y = axis_fixed(sc, fa, 1, a, b);
+        if (fa.noise_s != 0.f) {
+            const float2 nz = in.mn[i];
+            X = displace_rn(X, fa.noise_s, nz.x);
+            Y = displace_rn(Y, fa.noise_s, nz.y);
+        }
+        const uint64_t o = in.idx[i];
+        xy[2 * o] = (int32_t)X;
+        xy[2 * o + 1] = (int32_t)Y;
     }
 }
 
@@ -544,7 +587,12 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
     __syncthreads();
     for (uint32_t r = 0; r < per; ++r) {
         const uint32_t slot = r * kBinThreads + tid;
-        const uint4 v = srec[slot];
+        uint4 v = srec[slot];
+        if (v.x != kNoAtom && b.fa.noise_s != 0.f) {
+            const float2 nz = b.in.mn[chunk0 + slot];
+            v.x = displace_rn(v.x, b.fa.noise_s, nz.x);
+            v.y = displace_rn(v.y, b.fa.noise_s, nz.y);
+        }
         const uint4 rec = v.x == kNoAtom ? make_uint4(0, 0, 0, 0) : finish_record(b.sc, v.x, v.y, v.z, v.w);
         srec[slot] = rec;
         uint32_t tk[4];
@@ -1053,8 +1101,9 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
     }
     PairData &d = w->pairs[f % slots];
     *out = &d;
+    const bool noise = sc.motion_noise > 0.0;
     if (d.f == (int)f && d.motion == sc.motion && d.fading == sc.fading && d.width == sc.width &&
-        d.height == sc.height)
+        d.height == sc.height && (d.noise || !noise))
         return AM_OK;
     if ((rc = pair_reserve(d, w->cap))) return rc;
     if (w->prof) w->prof->open(s);
@@ -1065,14 +1114,16 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
     const uint64_t ntiles = (uint64_t)tiles_x * tiles_y;
     const uint32_t key_shift = ntiles < (1ull << 21) ? 10u : 0u;
     AMG_LAUNCH(k_pair_prep, grid, 256, 0, s, sc, f, w->perm_set ? w->perm : nullptr, w->pa, w->pb, w->col, w->ls,
-               w->rank, w->keys, w->vals, tiles_x, (uint32_t)(ntiles << key_shift), key_shift);
+               noise ? w->mn : nullptr, w->rank, w->keys, w->vals, tiles_x, (uint32_t)(ntiles << key_shift),
+               key_shift);
     int bits = 1;
     while ((1ull << bits) < (ntiles << key_shift) + 1) ++bits;
     rc = radix_sort_pairs(w->keys, w->vals, w->tkeys, w->tvals, w->hist, sc.N, bits, s);
     if (rc) return rc;
     AMG_CUDA(cudaMemsetAsync(d.d_active, 0, 4, s));
-    AMG_LAUNCH(k_pair_gather, grid, 256, 0, s, w->keys, w->vals, sc.N, w->pa, w->pb, w->col, w->ls, w->rank, d.pa,
-               d.pb, d.col, d.ls, d.rank, d.idx, (int)(sc.motion == AM_SPLINE), d.d_active);
+    AMG_LAUNCH(k_pair_gather, grid, 256, 0, s, w->keys, w->vals, sc.N, w->pa, w->pb, w->col, w->ls,
+               noise ? w->mn : nullptr, w->rank, d.pa, d.pb, d.col, d.ls, d.mn, d.rank, d.idx,
+               (int)(sc.motion == AM_SPLINE), d.d_active);
     AMG_CUDA(cudaGetLastError());
     if (w->prof) w->prof->close(PROF_PAIR, s);
     d.f = (int)f;
@@ -1080,6 +1131,7 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
     d.fading = sc.fading;
     d.width = sc.width;
     d.height = sc.height;
+    d.noise = noise;
     return AM_OK;
 }
 
@@ -1101,6 +1153,7 @@ int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, do
     split(fa.w1q, &fa.w1h, &fa.w1l);
     fa.lin_mode = fa.w1 == 1.0 ? 1u : (fa.w1 == 0.0 ? 2u : 0u);
     fa.str = (float)(1.0 - t);
+    fa.noise_s = sc.motion_noise > 0.0 ? (float)(sc.motion_noise * 256.0 * std::sin(3.141592653589793 * t)) : 0.f;
     fa.seg_ok = 1;
     if (sc.motion == AM_SPLINE) {
         // GetInterpolatedSplinePoint(time) (spline.cpp:45-57) basis.
@@ -1126,6 +1179,29 @@ int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, do
         split(fa.bq3, &fa.bh3, &fa.bl3);
         fa.key_mode = (fa.b0 == 0.0 && fa.b1 == 1.0 && fa.b2 == 0.0 && fa.b3 == 0.0) ? 1u : 0u;
     }
+    return AM_OK;
+}
+
+int render_positions(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, int32_t *xy,
+                     cudaStream_t s) {
+    AMG_CUDA(cudaMemsetAsync(xy, 0xFF, (size_t)sc.N * 8, s));
+    if (sc.K == 0 || sc.C == 0 || sc.N == 0) return AM_OK;
+    const size_t f = (size_t)(time * sc.K);
+    if (f >= sc.K) return AM_OK;
+    const double dt = 1.0 / double(sc.K);
+    const double t = std::max(0.0, (time - (double)(frame_key * dt)) / dt);
+    // the pair cache is shared with the frames, which may run on the binning stream
+    render_quiesce(w);
+    w->bs_after_s = true;
+    PairData *pd = nullptr;
+    int rc = prep_pair(w, sc, (uint32_t)f, s, &pd);
+    if (rc) return rc;
+    FrameArgs fa;
+    if ((rc = frame_args(w, sc, time, (uint32_t)f, t, &fa, s))) return rc;
+    SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx, pd->mn};
+    const unsigned grid = (unsigned)std::min<uint64_t>((sc.N + 255) / 256, (uint64_t)kSMs * 8);
+    AMG_LAUNCH(k_atom_positions, grid, 256, 0, s, sc, fa, pd->d_active, in, xy);
+    AMG_CUDA(cudaGetLastError());
     return AM_OK;
 }
 
@@ -1183,7 +1259,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     fa.ntiles = ntiles;
     // atoms of the pair: at most N; the active count stays on the device
     uint64_t n = sc.N;
-    SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx};
+    SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx, pd->mn};
     TileRecs tr;
     RenderWork::Slot *A = nullptr, *B = nullptr;
     if (fused) {

@@ -227,6 +227,7 @@ struct RenderScene {
     const uint8_t *present = nullptr;   // [K][CH][CW] 1 where the key frame has a pixel
     const uint32_t *blob_col = nullptr; // [K][C] AVERAGE / DISTINCT colour (RGB) of the b-th blob of frame k
     const int *perm = nullptr;          // [2][512] Perlin permutations (lag, slope) for the background
+    double motion_noise = 0.0;          // Perlin motion perturbation amplitude in px (0: off)
 };
 // Largest feather the frame render supports (three 32-px tile rings).
 constexpr uint32_t kMaxFeather = 96;
@@ -237,11 +238,18 @@ RenderWork *render_work_create();
 void render_work_destroy(RenderWork *w);
 void render_set_prof(RenderWork *w, Prof *p);
 Prof *render_prof(RenderWork *w);  // the timer render_set_prof installed (or null)
-// Uploads the two Perlin permutations (lag map seed, slope map seed+1).
-int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope);
+// Uploads the Perlin permutations: lag map (seed), slope map (seed + 1) and
+// the motion perturbation's x and y maps (seed + 2, seed + 3), [4][512].
+int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope, const int *perm_mx,
+                      const int *perm_my);
 // Renders the frame at normalised time `time` into out (device, width*height*4).
 int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, uint8_t *out,
                  cudaStream_t s);
+// Every atom's position words (x, y) at normalised time `time` into xy
+// (device, 2 * N int32; -1 where the atom is not drawn), as render_frame
+// places them.
+int render_positions(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, int32_t *xy,
+                     cudaStream_t s);
 // Writes key frame colours (display[CH][CW]) of present, non-transparent
 // pixels into a width*height RGBA8 frame (rendering before chains exist).
 int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32_t CW, uint32_t CH,

@@ -38,6 +38,60 @@ static __device__ float poctave(const int *p, float x, float y) {
     return r;
 }
 
+// Perlin motion perturbation (no counterpart in the reference, whose atoms
+// move along their LINEAR / SPLINE paths only): 8-octave noise at the atom's
+// first point of the pair, normalised by the key frames' bounding box at
+// frequency 8, one map per axis (PerlinNoise(seed + 2) for x, seed + 3 for
+// y), evaluated in FP32 with every operation rounded to nearest separately
+// and in a fixed order (the _rn intrinsics keep the compiler from fusing
+// them), so a host restatement of the same operations gives the same bits.
+// A frame displaces the atom's position word (integer part * 256 + fraction
+// byte) by rint(s * n) in 1/256 px, s = A * 256 * sin(pi t) for amplitude A
+// px and local time t in the pair, clamped to the 24-bit word.
+__device__ __forceinline__ float pfade_rn(float t) {
+    const float a = __fadd_rn(__fmul_rn(t, __fsub_rn(__fmul_rn(t, 6.f), 15.f)), 10.f);
+    return __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), a);
+}
+__device__ __forceinline__ float pgrad_rn(int hash, float x, float y) {
+    const int h = hash & 15;
+    const float u = h < 8 ? x : y, v = h < 4 ? y : (h == 12 || h == 14 ? x : 0.f);
+    return __fadd_rn((h & 1) == 0 ? u : -u, (h & 2) == 0 ? v : -v);
+}
+__device__ __forceinline__ float plerp_rn(float t, float a, float b) { return __fadd_rn(a, __fmul_rn(t, __fsub_rn(b, a))); }
+static __device__ float pnoise_rn(const int *p, float x, float y) {
+    const float fx = floorf(x), fy = floorf(y);
+    const int X = (int)fx & 255, Y = (int)fy & 255;
+    x = __fsub_rn(x, fx);
+    y = __fsub_rn(y, fy);
+    const float u = pfade_rn(x), v = pfade_rn(y);
+    const int A = p[X] + Y, AA = p[A], AB = p[A + 1];
+    const int B = p[X + 1] + Y, BA = p[B], BB = p[B + 1];
+    const float x1 = __fsub_rn(x, 1.f), y1 = __fsub_rn(y, 1.f);
+    const float l1 = plerp_rn(u, pgrad_rn(p[AA], x, y), pgrad_rn(p[BA], x1, y));
+    const float l2 = plerp_rn(u, pgrad_rn(p[AB], x, y1), pgrad_rn(p[BB], x1, y1));
+    return plerp_rn(v, l1, l2);
+}
+static __device__ float poctave_rn(const int *p, float x, float y) {
+    float r = 0.f, amp = 1.f;
+#pragma unroll 1
+    for (int i = 0; i < 8; ++i) {
+        r = __fadd_rn(r, __fmul_rn(pnoise_rn(p, x, y), amp));
+        x = __fmul_rn(x, 2.f);
+        y = __fmul_rn(y, 2.f);
+        amp = __fmul_rn(amp, 0.5f);
+    }
+    return r;
+}
+// ((v - b1) * 256 + vf) / (bw * 256) * 8 of one axis of point (v, vf).
+__device__ __forceinline__ float noise_coord_rn(int v, int vf, int b1, int bw) {
+    return __fmul_rn(__fdiv_rn((float)((v - b1) * 256 + vf), (float)(bw * 256)), 8.f);
+}
+// Position word w displaced by rint(s * n), clamped to [0, 2^24 - 1].
+__device__ __forceinline__ uint32_t displace_rn(uint32_t w, float s, float n) {
+    const int d = __float2int_rn(__fmul_rn(s, n));
+    return (uint32_t)min(max((int)w + d, 0), 0xFFFFFF);
+}
+
 struct FrameArgs {
     double w1, w2;          // LINEAR: weight of pt1 and 1 - that weight
     double b0, b1, b2, b3;  // SPLINE basis at the frame's local time
@@ -52,6 +106,7 @@ struct FrameArgs {
     uint32_t seg_ok;        // 1 when the spline segment is the prepared one
     int32_t seg[4];         // control frames when seg_ok == 0
     float str;              // colour weight of the earlier key frame, 1 - t
+    float noise_s;          // motion perturbation scale A * 256 * sin(pi t) (0: none this frame)
     uint32_t tiles_x, ntiles;
 };
 

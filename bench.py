@@ -3,8 +3,9 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Workload (N=1): ``shapes1024`` — 8 seeded 1024x1024 RGBA8 key frames of 40-80
-overlapping ellipses/rectangles (~1M atoms per key frame), SPLINE motion,
-PERLIN colour fading, HSP blob delimiter.  Setup (untimed) runs the whole
+overlapping ellipses/rectangles (~1M atoms per key frame), SPLINE motion plus
+the Perlin motion perturbation at 2 px amplitude, PERLIN colour fading, HSP
+blob delimiter.  Setup (untimed) runs the whole
 pipeline on the GPU: blobs, matching, chains, refinement.  One step renders
 the full morph cycle, 240 output frames at t = i/240, into device memory;
 ``value`` is frames/s with everything resident in HBM (frames pipelined: a
@@ -138,9 +139,11 @@ def physical_gpu_index(torch, dev):
     return dev
 
 
-def setup_morph(capi, frames, refine_sweeps):
+def setup_morph(capi, frames, refine_sweeps, motion_noise=0.0):
     m = capi.Morph()
     m.load(frames, **SETTINGS)
+    if motion_noise:
+        m.set(motion_noise=motion_noise)
     st = m.run_until(capi.STATE_ATOM_MORPHING)
     if st != capi.STATE_ATOM_MORPHING:
         raise RuntimeError(f"pipeline stopped in state {st}")
@@ -192,7 +195,7 @@ def bench_ours(args, rank, world):
     gpu_index = physical_gpu_index(torch, dev)
     frames = synth.workload(WORKLOAD)
     atoms_per_frame = int(np.mean([synth.opaque_count(f) for f in frames]))
-    m = setup_morph(capi, frames, refine_sweeps=args.refine_sweeps)
+    m = setup_morph(capi, frames, refine_sweeps=args.refine_sweeps, motion_noise=args.motion_noise)
     N, K = m.atoms, len(frames)
     stream = torch.cuda.ExternalStream(m.stream)
     ts = [m.get_time(i, FRAMES_PER_STEP) for i in range(FRAMES_PER_STEP)]
@@ -258,8 +261,10 @@ def bench_ours(args, rank, world):
     hbm, peak_kind = _peaks()
     # Algorithmic bytes per frame (spline path): per active atom the four
     # control points (32 B) + two colours (8 B) + lag/slope (8 B) + chain rank
-    # (4 B) + original index (4 B) = 56 B read once, plus 4 B per output pixel.
-    frame_bytes = N * 56 + m.width * m.height * 4
+    # (4 B) + original index (4 B) = 56 B read once, plus the motion noise
+    # pair (8 B) when the perturbation is on, plus 4 B per output pixel.
+    atom_bytes = 56 + (8 if args.motion_noise else 0)
+    frame_bytes = N * atom_bytes + m.width * m.height * 4
     frame_ms_profiled = sum(v[0] for v in per_frame.values() if True) / FRAMES_PER_STEP
     # in the timed cycle frames overlap (a frame's binning runs beside the
     # previous frame's resolve), so the whole-frame figure uses the timed
@@ -267,11 +272,13 @@ def bench_ours(args, rank, world):
     frame_ms = ms / (FRAMES_PER_STEP * args.steps)
     dom_name, (dom_ms, dom_n) = dom[0], dom[1]
     dom_avg_ms = dom_ms / dom_n
-    # Algorithmic bytes per launch attributed to each kernel that can dominate:
-    # inputs read once and outputs written once (records 16 B, pixels 4 B)
+    # Algorithmic bytes per launch attributed to each kernel that can dominate,
+    # as the per-frame bytes are counted: the atoms' inputs read once (the
+    # binning's 16-byte intermediate records are not algorithmic bytes: they
+    # are reported beside as record_bytes) and 4 B per output pixel
     kernel_bytes = {
-        "k_frame_bin": N * 56 + N * 16,
-        "k_frame_splat": N * 56,
+        "k_frame_bin": N * atom_bytes,
+        "k_frame_splat": N * atom_bytes,
         "k_frame_scatter": N * 16 * 2,
         "k_frame_resolve": N * 16 + m.width * m.height * 4,
         "pair_prep": N * 8 * 4,
@@ -282,6 +289,7 @@ def bench_ours(args, rank, world):
             "frac": round(achieved / hbm, 4), "peak_kind": peak_kind, "traffic": _profiled_traffic(dom_name),
             "traffic_source": "profiles/kernels_shapes1024_profile_case.md (ncu, cold cache, bytes per launch)",
             "algorithmic_bytes_per_launch": int(kernel_bytes), "avg_launch_ms": round(dom_avg_ms, 5),
+            "record_bytes": "16 B per binned record written by k_frame_bin and read by k_frame_resolve (not counted)",
             "frame": {"algorithmic_bytes": int(frame_bytes), "ms": round(frame_ms, 5),
                       "kernel_ms_sum": round(frame_ms_profiled, 5),
                       "achieved_gbs": round(frame_bytes / (frame_ms / 1e3) / 1e9, 1),
@@ -310,6 +318,7 @@ def bench_ours(args, rank, world):
         "config": {"workload": WORKLOAD, "key_frames": K, "resolution": [m.width, m.height],
                    "atoms_per_key_frame": atoms_per_frame, "chain_atoms": N, "chains": m.chains,
                    "frames_per_step": FRAMES_PER_STEP, "motion": "spline", "fading": "perlin",
+                   "motion_noise_px": args.motion_noise,
                    "refine_sweeps_before_render": args.refine_sweeps,
                    "l2": "per-step working set > L2 (240 output frames, 960 MB, written each step)",
                    "parallelism": f"replicas x{world}"},
@@ -529,6 +538,7 @@ def cpu_baseline(m, frames, ts, args):
     O = orc.Oracle()
     w, pts, order = m.export_chains()
     st = _oracle_state(O, m, frames, w, pts, order)
+    st["motion_noise"] = args.motion_noise
     sample = [ts[i] for i in (37, 150)][: args.cpu_frames]
     t0 = time.perf_counter()
     O.render_many(st, sample, threads=1)
@@ -563,6 +573,7 @@ def bench_reference(args, rank, world):
     frames = synth.workload(WORKLOAD)
     K = len(frames)
     st = cpu_pipeline(O, frames)
+    st["motion_noise"] = args.motion_noise
     threads = os.cpu_count() or 1
     ts = [i / FRAMES_PER_STEP for i in range(FRAMES_PER_STEP)]
     per_step = threads
@@ -587,6 +598,7 @@ def bench_reference(args, rank, world):
         "data": "synthetic seeded key frames",
         "config": {"workload": WORKLOAD, "key_frames": K, "resolution": [1024, 1024],
                    "chain_atoms": int(np.sum(st["widths"])), "frames_per_step": per_step,
+                   "motion": "spline", "fading": "perlin", "motion_noise_px": args.motion_noise,
                    "parallelism": f"{threads} host threads, one frame each"},
         "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{per_step} frames per step of {WORKLOAD}, one per host thread"},
@@ -595,79 +607,11 @@ def bench_reference(args, rank, world):
 
 
 def cpu_pipeline(O, frames):
-    """CPU restatement of the reference pipeline up to chains: components,
-    blob matching, chain construction (oracle/oracle.cpp)."""
-    import ctypes as C
+    """CPU restatement of the reference pipeline up to chains (components,
+    blob matching, chain construction; oracle/oracle.cpp)."""
     from oracle import oracle as orc
-    K = len(frames)
-    delim = SETTINGS["blob_delimiter"]
-    colors, present = orc.stored_frames(frames, delim, O)
-    descs, labels_all = [], []
-    for k, img in enumerate(frames):
-        st_img = colors[k].view(np.uint8).reshape(img.shape)
-        lab, stats = O.components(img, st_img)
-        labels_all.append(lab)
-        d = np.zeros((len(stats), 7))
-        d[:, 0] = stats[:, 0]
-        d[:, 1:3] = stats[:, 1:3] / stats[:, :1]
-        d[:, 3:7] = stats[:, 3:7] / stats[:, :1] / 255.0
-        descs.append(d)
-    Wb = max(len(d) for d in descs)
-    desc = np.zeros((K, Wb, 7))
-    for k, d in enumerate(descs):
-        desc[k, :len(d)] = d
-        desc[k, len(d):, 1:3] = d[:, 1:3].mean(0) if len(d) else 0
-    perm = np.tile(np.arange(Wb, dtype=np.int32), (K, 1))
-    xs, ys = [], []
-    for f in frames:
-        y, x = np.nonzero(f[..., 3])
-        xs += [int(x.min()), int(x.max())]
-        ys += [int(y.min()), int(y.max())]
-    bbox = np.array([min(xs), min(ys), max(xs), max(ys)])
-    bbox_d = float((bbox[2] - bbox[0]) ** 2 + (bbox[3] - bbox[1]) ** 2)
-    wr, ws, wx = orc.blob_weights(1, 1, 1)
-    O.lib.orc_blob_match(desc.ctypes.data_as(orc.f64p), perm.ctypes.data_as(orc.i32p), Wb, K, 20000, 1, bbox_d,
-                         wr, ws, wx)
-    widths, chains = [], []
-    for g in range(Wb):
-        surfs, keep = [], []
-        cnt = np.zeros(K, np.uint64)
-        cx = np.zeros(K)
-        cy = np.zeros(K)
-        colk = np.zeros((K, 7))
-        for k in range(K):
-            b = perm[k, g]
-            colk[k] = desc[k, b]
-            if b < len(descs[k]):
-                ys_, xs_ = np.nonzero(labels_all[k] == b)
-                pos = (ys_.astype(np.uint64) * 65536 + xs_.astype(np.uint64))
-                pos.sort()
-            else:
-                pos = np.zeros(0, np.uint64)
-            keep.append(pos)
-            cnt[k] = len(pos)
-        O.lib.orc_fix_volatiles(colk.ctypes.data_as(orc.f64p), K)
-        cx[:] = colk[:, 1]
-        cy[:] = colk[:, 2]
-        ptrs = (orc.u64p * K)(*[p.ctypes.data_as(orc.u64p) for p in keep])
-        wdt = O.lib.orc_chain_build(ptrs, cnt.ctypes.data_as(orc.u64p), cx.ctypes.data_as(orc.f64p),
-                                    cy.ctypes.data_as(orc.f64p), K, SETTINGS["density"], g, None, 0)
-        buf = np.zeros(int(wdt) * K, np.uint64)
-        O.lib.orc_chain_build(ptrs, cnt.ctypes.data_as(orc.u64p), cx.ctypes.data_as(orc.f64p),
-                              cy.ctypes.data_as(orc.f64p), K, SETTINGS["density"], g,
-                              buf.ctypes.data_as(orc.u64p), int(wdt))
-        widths.append(int(wdt))
-        chains.append(buf.reshape(K, int(wdt)))
-    widths = np.array(widths, np.uint64)
-    pts = np.concatenate(chains, axis=1).reshape(-1)
-    order = np.zeros((K, Wb), np.int32)
-    for k in range(K):
-        for g in range(Wb):
-            order[k, perm[k, g]] = g
-    return dict(K=K, width=1024, height=1024, bbox=bbox, seed=SETTINGS["seed"], motion=SETTINGS["motion"],
-                fading=SETTINGS["fading"], delimiter=delim, density=SETTINGS["density"], colors=colors,
-                present=present, widths=widths, pts=pts, blob_order=order,
-                frame_keys=np.arange(K, dtype=np.uint64))
+    return orc.pipeline(O, frames, delimiter=SETTINGS["blob_delimiter"], density=SETTINGS["density"],
+                        seed=SETTINGS["seed"], motion=SETTINGS["motion"], fading=SETTINGS["fading"])
 
 
 def profile_case(args):

@@ -110,10 +110,19 @@ int am_set_show_blobs(am_morph *m, unsigned b);              /* morph.h:70 */
 int am_set_fluid(am_morph *m, unsigned steps);               /* morph::set_fluid morph.cpp:1553-1560 */
 int am_set_density(am_morph *m, uint16_t d);                 /* morph::set_density morph.cpp:1562-1570 */
 int am_set_resolution(am_morph *m, uint16_t w, uint16_t h);  /* morph::set_resolution morph.cpp:1517-1520 */
-/* New knobs (no reference counterpart): swap proposal kind, sweeps per
- * atom-morphing step, and the Perlin motion amplitude in pixels (0 = off). */
+/* New knobs (no reference counterpart): swap proposal kind and sweeps per
+ * atom-morphing step. */
 int am_set_proposal(am_morph *m, unsigned kind);
 int am_set_sweeps(am_morph *m, size_t sweeps_per_step);
+/* Perlin motion perturbation (no reference counterpart: the reference moves
+ * atoms along their LINEAR / SPLINE paths, morph.cpp:523-531).  Amplitude A
+ * in pixels, 0 (the default) = off, at most 64.  An atom drawn at local time
+ * t of a key-frame pair is displaced by rint(s * n) in 1/256 px per axis,
+ * s = A * 256 * sin(pi t) (zero at key frames), n the 8-octave Perlin noise
+ * (perlin.cpp:57-69) of maps seeded seed + 2 (x) and seed + 3 (y) at the
+ * atom's first point of the pair, normalised by the key frames' bounding box
+ * at frequency 8 as the colour fade's lag map is (morph.cpp:540-545); the
+ * noise is evaluated in FP32, every operation rounded to nearest. */
 int am_set_motion_noise(am_morph *m, double amplitude_px);
 /* Fluid solver grid units per pixel (the reference's sparseness, fixed at 1
  * there): the grid is (width * s + 20) x (height * s + 20). */
@@ -190,6 +199,14 @@ size_t   am_get_chain_count(const am_morph *m);               /* chains = blob g
  * whose allocation covers the whole frame, an atom frame is stored there by
  * the GPU directly while it is resolved; other host memory receives a copy. */
 int am_render(am_morph *m, double t, uint8_t *out, int out_on_device);
+/* Every atom's position at time t, as the render draws it (motion path plus
+ * the motion perturbation): xy[2i], xy[2i + 1] = x and y position words
+ * (integer pixel * 256 + fraction byte, the point layout of atomorph.h:275-
+ * 284) of atom column i (chain order, as am_export_chains), -1, -1 where the
+ * atom is drawn at neither key frame of its pair.  Returns the atom count
+ * and writes when cap >= it (0 when the readout failed: am_last_error).
+ * Readout of get_pixels(blob, t)'s positions, morph.cpp:523-531. */
+size_t am_get_positions(am_morph *m, double t, int32_t *xy, size_t cap);
 /* Renders n frames at times ts[0..n) into n consecutive device frames. */
 int am_render_many(am_morph *m, const double *ts, size_t n, uint8_t *out_device);
 /* Renders n frames at times ts[0..n) into n consecutive host frames, complete

@@ -291,6 +291,102 @@ void orc_sweeps(uint64_t *pts, const uint64_t *widths, uint32_t C, uint32_t K, u
     }
 }
 
+// ---------------------------------------------------------- motion noise ---
+// Perlin motion perturbation (no counterpart in the reference, which moves
+// atoms along their LINEAR / SPLINE paths only).  Definition:
+//   * two noise maps, PerlinNoise(seed + 2) for x and PerlinNoise(seed + 3)
+//     for y (the morph's seed; the colour fade's lag and slope maps use seed
+//     and seed + 1, morph.h:136-137, morph.cpp:436-444);
+//   * sampled at the atom's point pt1 at the pair's first key frame,
+//     normalised by the key frames' bounding box at frequency 8, as the lag
+//     map is (morph.cpp:540-545);
+//   * 8-octave noise (perlin.cpp:57-69) evaluated in IEEE single precision,
+//     every operation separately rounded to nearest in the order written
+//     below (the GPU evaluates the same operations, so both give the same
+//     bits); its FP64 form is the accuracy reference;
+//   * displacement D = rint(s * n) in 1/256 px, s = (float)(A * 256 *
+//     sin(pi * t)), A the amplitude in px, t the local time in the key-frame
+//     pair (zero at key frames, so paths stay continuous);
+//   * added to the position word the motion gives (integer part * 256 +
+//     fraction byte, morph.cpp:523-531), clamped to [0, 2^24 - 1].
+struct Perm {
+    int p[512];
+    explicit Perm(unsigned seed) {
+        if (seed == 0) seed = std::mt19937::default_seed;
+        std::iota(p, p + 256, 0);
+        std::shuffle(p, p + 256, std::mt19937(seed));
+        for (int i = 0; i < 256; ++i) p[256 + i] = p[i];
+    }
+};
+inline float fade_f(float t) {
+    const float a = t * (t * 6.0f - 15.0f) + 10.0f;
+    return t * t * t * a;
+}
+inline float grad_f(int hash, float x, float y) {
+    const int h = hash & 15;
+    const float u = h < 8 ? x : y, v = h < 4 ? y : (h == 12 || h == 14 ? x : 0.0f);
+    return ((h & 1) == 0 ? u : -u) + ((h & 2) == 0 ? v : -v);
+}
+inline float lerp_f(float t, float a, float b) { return a + t * (b - a); }
+float noise_f(const int *p, float x, float y) {
+    const float fx = std::floor(x), fy = std::floor(y);
+    const int X = (int)fx & 255, Y = (int)fy & 255;
+    x = x - fx;
+    y = y - fy;
+    const float u = fade_f(x), v = fade_f(y);
+    const int A = p[X] + Y, AA = p[A], AB = p[A + 1];
+    const int B = p[X + 1] + Y, BA = p[B], BB = p[B + 1];
+    const float l1 = lerp_f(u, grad_f(p[AA], x, y), grad_f(p[BA], x - 1.0f, y));
+    const float l2 = lerp_f(u, grad_f(p[AB], x, y - 1.0f), grad_f(p[BB], x - 1.0f, y - 1.0f));
+    return lerp_f(v, l1, l2);
+}
+float octave_f(const int *p, float x, float y) {
+    float r = 0.0f, amp = 1.0f;
+    for (int i = 0; i < 8; ++i) {
+        r = r + noise_f(p, x, y) * amp;
+        x = x * 2.0f;
+        y = y * 2.0f;
+        amp = amp * 0.5f;
+    }
+    return r;
+}
+// The noise coordinates of point (x, xf) on one axis: the bbox-normalised
+// position at frequency 8, (((x - b1) * 256 + xf) / (bw * 256)) * 8.
+inline float noise_coord_f(int x, int xf, int b1, int bw) {
+    return ((float)((x - b1) * 256 + xf) / (float)(bw * 256)) * 8.0f;
+}
+inline double noise_coord_d(int x, int xf, int b1, int bw) {
+    return (((double)(x - b1) * 256 + xf) / double(bw * 256.0)) * 8.0;
+}
+// Displacement (dx, dy) in 1/256 px of an atom whose pair's first point is
+// pt1; fp64 selects the FP64 accuracy reference instead of the definition.
+void motion_offset(const Perm &mx, const Perm &my, const Perlin &nx64, const Perlin &ny64, const uint32_t *bbox,
+                   double amplitude, double t, Pt pt1, bool fp64, int32_t *dx, int32_t *dy) {
+    const int bw = (int)bbox[2] - (int)bbox[0] + 1, bh = (int)bbox[3] - (int)bbox[1] + 1;
+    const double sd = amplitude * 256.0 * std::sin(3.141592653589793 * t);
+    if (fp64) {
+        const double u = noise_coord_d(pt1.x, pt1.xf, (int)bbox[0], bw), v = noise_coord_d(pt1.y, pt1.yf, (int)bbox[1], bh);
+        *dx = (int32_t)std::nearbyint(sd * nx64.octave(u, v, 8));
+        *dy = (int32_t)std::nearbyint(sd * ny64.octave(u, v, 8));
+        return;
+    }
+    const float sf = (float)sd;
+    const float u = noise_coord_f(pt1.x, pt1.xf, (int)bbox[0], bw), v = noise_coord_f(pt1.y, pt1.yf, (int)bbox[1], bh);
+    *dx = (int32_t)std::nearbyint(sf * octave_f(mx.p, u, v));
+    *dy = (int32_t)std::nearbyint(sf * octave_f(my.p, u, v));
+}
+// Position word plus displacement, clamped to the 24-bit word.
+inline int32_t displaced(int32_t w, int32_t d) {
+    const int64_t v = (int64_t)w + d;
+    return (int32_t)std::min<int64_t>(std::max<int64_t>(v, 0), 0xFFFFFF);
+}
+// The four maps of a scene's seed.
+struct NoiseMaps {
+    Perm mx, my;
+    Perlin mx64, my64;
+    explicit NoiseMaps(unsigned seed) : mx(seed + 2), my(seed + 3), mx64(seed + 2), my64(seed + 3) {}
+};
+
 // ------------------------------------------------------------ rendering ---
 // Scene handed to the renderer: what morph::get_pixels(t) reads.
 struct orc_scene {
@@ -310,6 +406,7 @@ struct orc_scene {
     uint32_t keep_background;   // set_keep_background
     uint32_t show_blobs;        // set_show_blobs: TEXTURE 0, AVERAGE 1, DISTINCT 2
     const uint32_t *blob_avg;   // [K][C] create_color of the b-th blob's mean colour (stored space), for AVERAGE
+    double motion_noise;        // Perlin motion perturbation amplitude in px (0: off); not in the reference
 };
 
 }  // extern "C"
@@ -352,9 +449,52 @@ inline Col ramp_col(Col c1, Col c2, double lag, double slope, double str) {
     return lerp_col(c1, c2, str);
 }
 
+// The atom's point at local time t of pair y (global time `time`): the
+// motion's position (LINEAR morph.cpp:1501-1515, SPLINE morph.cpp:526-531,
+// NONE the first point) plus the motion perturbation when it is on (FP64
+// noise when fp64, for the accuracy comparison).  col = the atom's column in
+// the frame-major point array.
+Pt atom_point(const orc_scene &s, const NoiseMaps &nm, uint32_t y, uint64_t N, uint64_t col, double t, double time,
+              bool fp64, std::vector<double> &sx, std::vector<double> &sy) {
+    const uint32_t h = s.K, yn = (y + 1) % h;
+    const Pt pt1 = unpack(s.pts[(uint64_t)y * N + col]);
+    const Pt pt2 = unpack(s.pts[(uint64_t)yn * N + col]);
+    Pt pt = pt1;
+    if (s.motion == LINEAR) {
+        // morph::interpolate(point, point, w), morph.cpp:1501-1515.
+        double w1 = 1.0 - t;
+        double x1 = (double(256) * pt1.x + pt1.xf), y1 = (double(256) * pt1.y + pt1.yf);
+        double x2 = (double(256) * pt2.x + pt2.xf), y2 = (double(256) * pt2.y + pt2.yf);
+        double xx = (w1 * x1 + (1.0 - w1) * x2), yy = (w1 * y1 + (1.0 - w1) * y2);
+        pt.x = (uint16_t)(xx / double(256)); pt.xf = (uint8_t)(xx - (pt.x * 256));
+        pt.y = (uint16_t)(yy / double(256)); pt.yf = (uint8_t)(yy - (pt.y * 256));
+    } else if (s.motion == SPLINE) {
+        // Spline through all key frames at global time, morph.cpp:526-531.
+        for (uint32_t j = 0; j < h; ++j) {
+            Pt q = unpack(s.pts[(uint64_t)j * N + col]);
+            sx[j] = q.x + q.xf / double(256);
+            sy[j] = q.y + q.yf / double(256);
+        }
+        double vx, vy, ix, iy;
+        spline_eval(sx.data(), sy.data(), (int)h, time, &vx, &vy);
+        double fx = std::modf(vx, &ix), fy = std::modf(vy, &iy);
+        // double -> uint16/uint8 as the x86 build converts: via int.
+        pt.x = (uint16_t)(int)ix; pt.xf = (uint8_t)(int)std::round(fx * 255);
+        pt.y = (uint16_t)(int)iy; pt.yf = (uint8_t)(int)std::round(fy * 255);
+    }
+    if (s.motion_noise > 0.0) {
+        int32_t dx, dy;
+        motion_offset(nm.mx, nm.my, nm.mx64, nm.my64, s.bbox, s.motion_noise, t, pt1, fp64, &dx, &dy);
+        const int32_t X = displaced((int32_t)pt.x * 256 + pt.xf, dx), Y = displaced((int32_t)pt.y * 256 + pt.yf, dy);
+        pt.x = (uint16_t)(X >> 8); pt.xf = (uint8_t)(X & 255);
+        pt.y = (uint16_t)(Y >> 8); pt.yf = (uint8_t)(Y & 255);
+    }
+    return pt;
+}
+
 // Per-blob pixel list at local time t (morph.cpp:452-623, feather 0).
-void blob_pixels(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_map, uint32_t group, uint32_t y,
-                 double t, double time, std::vector<Px> &out) {
+void blob_pixels(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_map, const NoiseMaps &nm,
+                 uint32_t group, uint32_t y, double t, double time, std::vector<Px> &out) {
     uint64_t N = 0, off = 0;
     for (uint32_t c = 0; c < s.C; ++c) {
         if (c == group) off = N;
@@ -377,29 +517,7 @@ void blob_pixels(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_
         else if (h2 && !h1) { c2 = read_pixel(s, yn, pt2.x, pt2.y); c1 = c2; c1.a = 0; }
         else { c1 = read_pixel(s, y, pt1.x, pt1.y); c2 = read_pixel(s, yn, pt2.x, pt2.y); }
 
-        Pt pt = pt1;
-        if (s.motion == LINEAR) {
-            // morph::interpolate(point, point, w), morph.cpp:1501-1515.
-            double w1 = 1.0 - t;
-            double x1 = (double(256) * pt1.x + pt1.xf), y1 = (double(256) * pt1.y + pt1.yf);
-            double x2 = (double(256) * pt2.x + pt2.xf), y2 = (double(256) * pt2.y + pt2.yf);
-            double xx = (w1 * x1 + (1.0 - w1) * x2), yy = (w1 * y1 + (1.0 - w1) * y2);
-            pt.x = (uint16_t)(xx / double(256)); pt.xf = (uint8_t)(xx - (pt.x * 256));
-            pt.y = (uint16_t)(yy / double(256)); pt.yf = (uint8_t)(yy - (pt.y * 256));
-        } else if (s.motion == SPLINE) {
-            // Spline through all key frames at global time, morph.cpp:526-531.
-            for (uint32_t j = 0; j < h; ++j) {
-                Pt q = unpack(s.pts[(uint64_t)j * N + off + x]);
-                sx[j] = q.x + q.xf / double(256);
-                sy[j] = q.y + q.yf / double(256);
-            }
-            double vx, vy, ix, iy;
-            spline_eval(sx.data(), sy.data(), (int)h, time, &vx, &vy);
-            double fx = std::modf(vx, &ix), fy = std::modf(vy, &iy);
-            // double -> uint16/uint8 as the x86 build converts: via int.
-            pt.x = (uint16_t)(int)ix; pt.xf = (uint8_t)(int)std::round(fx * 255);
-            pt.y = (uint16_t)(int)iy; pt.yf = (uint8_t)(int)std::round(fy * 255);
-        }
+        Pt pt = atom_point(s, nm, y, N, off + x, t, time, false, sx, sy);
         Px px;
         px.x = pt.x;
         px.y = pt.y;
@@ -525,7 +643,8 @@ Col distinct_colour(size_t group) {
     return c;
 }
 
-void render_one(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_map, double time_in, uint8_t *out) {
+void render_one(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_map, const NoiseMaps &nm,
+                double time_in, uint8_t *out) {
     size_t npx = (size_t)s.width * s.height;
     std::memset(out, 0, npx * 4);
     if (s.K == 0 || s.C == 0) return;
@@ -549,7 +668,7 @@ void render_one(const orc_scene &s, const Perlin &lag_map, const Perlin &slope_m
     for (uint32_t b = 0; b < s.C; ++b) {
         pix.clear();
         const uint32_t group = (uint32_t)s.blob_order[(size_t)f * s.C + b];
-        blob_pixels(s, lag_map, slope_map, group, (uint32_t)f, t, time, pix);
+        blob_pixels(s, lag_map, slope_map, nm, group, (uint32_t)f, t, time, pix);
         // draw_atoms (morph.cpp:1313-1345): TEXTURE, AVERAGE (blob2pixel,
         // morph.cpp:1423-1429) or DISTINCT colours.
         Col ave{0, 0, 0, 0};
@@ -605,24 +724,57 @@ extern "C" {
 // keep_background (blend_blobs has no setter in the reference and stays off).
 void orc_render(const orc_scene *s, double t, uint8_t *out) {
     Perlin lag(s->seed), slope(s->seed + 1);
-    render_one(*s, lag, slope, t, out);
+    const NoiseMaps nm(s->seed);
+    render_one(*s, lag, slope, nm, t, out);
 }
 
 // Renders n frames with up to `threads` host threads (frames are
 // independent); out holds n consecutive frames.
 void orc_render_many(const orc_scene *s, const double *ts, uint32_t n, uint8_t *out, uint32_t threads) {
     Perlin lag(s->seed), slope(s->seed + 1);
+    const NoiseMaps nm(s->seed);
     size_t fsz = (size_t)s->width * s->height * 4;
     if (threads <= 1) {
-        for (uint32_t i = 0; i < n; ++i) render_one(*s, lag, slope, ts[i], out + i * fsz);
+        for (uint32_t i = 0; i < n; ++i) render_one(*s, lag, slope, nm, ts[i], out + i * fsz);
         return;
     }
     std::vector<std::thread> pool;
     for (uint32_t w = 0; w < threads; ++w)
         pool.emplace_back([&, w]() {
-            for (uint32_t i = w; i < n; i += threads) render_one(*s, lag, slope, ts[i], out + i * fsz);
+            for (uint32_t i = w; i < n; i += threads) render_one(*s, lag, slope, nm, ts[i], out + i * fsz);
         });
     for (auto &th : pool) th.join();
+}
+
+// Every atom's point at time t (global time, as orc_render takes it) as two
+// position words (integer part * 256 + fraction byte) per column of the
+// frame-major point array; -1, -1 where the atom is drawn at neither key
+// frame of its pair.  fp64 selects the FP64 noise (the accuracy reference of
+// the motion perturbation) instead of its FP32 definition.
+void orc_positions(const orc_scene *sp, double time_in, int fp64, int32_t *xy) {
+    const orc_scene &s = *sp;
+    uint64_t N = 0;
+    for (uint32_t c = 0; c < s.C; ++c) N += s.widths[c];
+    if (s.K == 0 || N == 0) return;
+    double integ;
+    double time = std::modf(time_in, &integ);
+    if (time < 0.0) time += 1.0;
+    const size_t f = std::min<size_t>((size_t)(time * s.K), s.K - 1);
+    const double dt = 1.0 / double(s.K);
+    const double t = std::max(0.0, (time - (double)(s.frame_keys[f] * dt)) / dt);
+    const NoiseMaps nm(s.seed);
+    std::vector<double> sx(s.K), sy(s.K);
+    const uint32_t y = (uint32_t)f, yn = (y + 1) % s.K;
+    for (uint64_t col = 0; col < N; ++col) {
+        const Pt p1 = unpack(s.pts[(uint64_t)y * N + col]), p2 = unpack(s.pts[(uint64_t)yn * N + col]);
+        if (!(p1.flags & HAS_PIXEL) && !(p2.flags & HAS_PIXEL)) {
+            xy[2 * col] = xy[2 * col + 1] = -1;
+            continue;
+        }
+        const Pt pt = atom_point(s, nm, y, N, col, t, time, fp64 != 0, sx, sy);
+        xy[2 * col] = (int32_t)pt.x * 256 + pt.xf;
+        xy[2 * col + 1] = (int32_t)pt.y * 256 + pt.yf;
+    }
 }
 
 // ------------------------------------------------------------ fluid step ---

@@ -57,7 +57,7 @@ class Scene(C.Structure):
         ("motion", C.c_uint32), ("fading", C.c_uint32), ("delimiter", C.c_uint32), ("density", C.c_uint32),
         ("colors", u32p), ("present", u8p), ("widths", u64p), ("pts", u64p), ("blob_order", i32p),
         ("frame_keys", u64p), ("feather", C.c_uint32), ("keep_background", C.c_uint32), ("show_blobs", C.c_uint32),
-        ("blob_avg", u32p),
+        ("blob_avg", u32p), ("motion_noise", C.c_double),
     ]
 
 
@@ -95,6 +95,8 @@ def make_scene(state: dict) -> tuple[Scene, list]:
     s.show_blobs = int(state.get("show_blobs", 0))
     if state.get("blob_avg") is not None:
         s.blob_avg = _p(arr("blob_avg", np.uint32), u32p)
+    # Perlin motion perturbation amplitude in px (not in the reference)
+    s.motion_noise = float(state.get("motion_noise", 0.0))
     return s, keep
 
 
@@ -116,6 +118,7 @@ class Oracle:
         L.orc_sweeps.argtypes = [u64p, u64p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint]
         L.orc_render.argtypes = [C.POINTER(Scene), C.c_double, u8p]
         L.orc_render_many.argtypes = [C.POINTER(Scene), f64p, C.c_uint32, u8p, C.c_uint32]
+        L.orc_positions.argtypes = [C.POINTER(Scene), C.c_double, C.c_int, i32p]
         L.orc_fluid_step.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, f64p, u8p, C.c_uint64, C.c_double]
         L.orc_srand.argtypes = [C.c_uint]
         L.orc_draw_fluid.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, u32p, C.c_double, u8p]
@@ -175,6 +178,16 @@ class Oracle:
         self.lib.orc_render_many(C.byref(s), _p(ts, f64p), len(ts), _p(out, u8p), threads)
         return out
 
+    def positions(self, state: dict, t: float, fp64: bool = False) -> np.ndarray:
+        """[N, 2] position words (integer part * 256 + fraction byte) of every
+        atom column at time t, -1 where the atom is not drawn; fp64 gives the
+        motion perturbation's FP64 accuracy reference."""
+        s, keep = make_scene(state)
+        N = int(np.sum(state["widths"]))
+        out = np.zeros((max(N, 1), 2), np.int32)
+        self.lib.orc_positions(C.byref(s), t, int(fp64), _p(out, i32p))
+        return out[:N]
+
     def components(self, img: np.ndarray, stored: np.ndarray | None = None):
         """4-connected components of img's opaque pixels: (labels, stats)."""
         h, w = img.shape[:2]
@@ -223,6 +236,41 @@ class Oracle:
         wr, ws, wx = blob_weights(*weights)
         d = np.ascontiguousarray(desc, np.float64)
         return self.lib.orc_blob_energy(_p(d, f64p), d.shape[0], d.shape[1], bbox_d, wr, ws, wx)
+
+
+def group_desc(colors: np.ndarray, glabels: np.ndarray, groups: int) -> np.ndarray:
+    """Blob descriptors by group, [groups, K, 7] = (size, mean x, mean y,
+    mean stored r, g, b, a in 0..1), from each key frame's group-label image
+    glabels[k] (-1 where no blob) and stored colours colors[k] (uint32 RGBA);
+    exact means.  A group without a blob in a frame has size 0 (its other
+    fields do not enter blob_distance, thread.cpp:1163-1170)."""
+    K = len(glabels)
+    d = np.zeros((groups, K, 7))
+    for k in range(K):
+        lab = glabels[k]
+        ys, xs = np.nonzero(lab >= 0)
+        g = lab[ys, xs]
+        c = colors[k][ys, xs]
+        cnt = np.bincount(g, minlength=groups).astype(np.float64)
+        nz = cnt > 0
+        d[:, k, 0] = cnt
+        for j, v in enumerate((xs, ys)):
+            d[nz, k, 1 + j] = np.bincount(g, weights=v, minlength=groups)[nz] / cnt[nz]
+        for j in range(4):
+            ch = ((c >> np.uint32(8 * j)) & np.uint32(255)).astype(np.float64)
+            d[nz, k, 3 + j] = np.bincount(g, weights=ch, minlength=groups)[nz] / cnt[nz] / 255.0
+    return d
+
+
+def bbox_diag2(frames) -> float:
+    """Squared diagonal of the key frames' pixel bounding box (thread.cpp:1127-1139)."""
+    xs, ys = [], []
+    for f in frames:
+        y, x = np.nonzero(f[..., 3])
+        if len(x):
+            xs += [int(x.min()), int(x.max())]
+            ys += [int(y.min()), int(y.max())]
+    return float((max(xs) - min(xs)) ** 2 + (max(ys) - min(ys)) ** 2)
 
 
 def blob_weights(rgba: int, size: int, xy: int) -> tuple[float, float, float]:
@@ -276,6 +324,8 @@ class Reference:
         L.ref_pixel_count.restype = C.c_size_t
         L.ref_pixel_count.argtypes = [C.c_void_p, C.c_size_t]
         L.ref_blob_surface.restype = C.c_size_t
+        L.ref_synchronize.restype = C.c_int
+        L.ref_synchronize.argtypes = [C.c_void_p]
         L.ref_state.restype = C.c_uint
         L.ref_state.argtypes = [C.c_void_p]
         L.ref_get_time.restype = C.c_double
@@ -297,7 +347,14 @@ class Reference:
 
     # -- morph handle ------------------------------------------------------
     def new(self, frames, *, seed=0, delimiter=1, density=1, blob_number=1, motion=3, fading=6,
-            threshold=1.0, fluid=0):
+            threshold=1.0, fluid=0, resync=False):
+        """A reference morph of `frames`.  resync: synchronize once before
+        prepare(), as the demo's loop does (demo/main.cpp:231-233).  The first
+        synchronize after ingestion sets the worker's bounding box and then
+        clears it (morph.cpp:119-125, thread.cpp:75-80); blob matching run
+        before a second synchronize sees a zero bbox diagonal, every blob
+        distance is infinite or NaN (thread.cpp:1167), no swap registers as
+        a new best and the groups stay at their initial shuffle."""
         if self.h:
             self.lib.ref_free(self.h)
         h = self.h = self.lib.ref_new()
@@ -317,6 +374,8 @@ class Reference:
             mw, mh = max(mw, img.shape[1]), max(mh, img.shape[0])
         L.ref_set_resolution(h, mw, mh)
         self.width, self.height, self.K = mw, mh, len(frames)
+        if resync:
+            L.ref_synchronize(h)
         return self
 
     def prepare(self, max_match_steps=20000, max_detect_steps=10**9) -> int:
@@ -361,6 +420,21 @@ class Reference:
 
     def pixel_count(self, f: int) -> int:
         return self.lib.ref_pixel_count(self.h, f)
+
+    def blob_energy(self) -> float:
+        """The worker's best blob-map energy (thread.cpp:713-716)."""
+        return self.lib.ref_blob_energy(self.h)
+
+    def group_labels(self, f: int) -> np.ndarray:
+        """[H, W] group of the blob holding each pixel of key frame f (-1: none)."""
+        out = np.full((self.height, self.width), -1, np.int32)
+        for b, (g, s, xy) in enumerate(self.blobs(f)):
+            if not s:
+                continue
+            pos = np.zeros(s, np.uint64)
+            self.lib.ref_blob_surface(self.h, f, b, _p(pos, u64p))
+            out[(pos // 65536).astype(np.int64), (pos % 65536).astype(np.int64)] = g
+        return out
 
     def blobs(self, f: int):
         """List of (group, surface, [x,y,r,g,b,a]) in blob-vector order."""
@@ -429,3 +503,82 @@ def stored_frames(frames, delimiter: int, conv) -> tuple[np.ndarray, np.ndarray]
         else:
             colors[k, :h, :w] = np.where(m, c, 0)
     return colors, present
+
+
+def pipeline(O, frames, *, delimiter: int, density: int, seed: int, motion: int, fading: int,
+             match_steps: int = 20000) -> dict:
+    """The reference pipeline up to chains restated on the CPU (components,
+    blob matching, chain construction; oracle.cpp): the morph-state dict of
+    the chains it builds for `frames` (blob_number 1 regime: one blob per
+    4-connected component).  Deterministic for given inputs on any machine."""
+    K = len(frames)
+    delim = delimiter
+    colors, present = stored_frames(frames, delim, O)
+    descs, labels_all = [], []
+    for k, img in enumerate(frames):
+        st_img = colors[k].view(np.uint8).reshape(img.shape)
+        lab, stats = O.components(img, st_img)
+        labels_all.append(lab)
+        d = np.zeros((len(stats), 7))
+        d[:, 0] = stats[:, 0]
+        d[:, 1:3] = stats[:, 1:3] / stats[:, :1]
+        d[:, 3:7] = stats[:, 3:7] / stats[:, :1] / 255.0
+        descs.append(d)
+    Wb = max(len(d) for d in descs)
+    desc = np.zeros((K, Wb, 7))
+    for k, d in enumerate(descs):
+        desc[k, :len(d)] = d
+        desc[k, len(d):, 1:3] = d[:, 1:3].mean(0) if len(d) else 0
+    perm = np.tile(np.arange(Wb, dtype=np.int32), (K, 1))
+    xs, ys = [], []
+    for f in frames:
+        y, x = np.nonzero(f[..., 3])
+        xs += [int(x.min()), int(x.max())]
+        ys += [int(y.min()), int(y.max())]
+    bbox = np.array([min(xs), min(ys), max(xs), max(ys)])
+    bbox_d = float((bbox[2] - bbox[0]) ** 2 + (bbox[3] - bbox[1]) ** 2)
+    wr, ws, wx = blob_weights(1, 1, 1)
+    O.lib.orc_blob_match(desc.ctypes.data_as(f64p), perm.ctypes.data_as(i32p), Wb, K, match_steps, 1, bbox_d,
+                         wr, ws, wx)
+    widths, chains = [], []
+    for g in range(Wb):
+        keep = []
+        cnt = np.zeros(K, np.uint64)
+        cx = np.zeros(K)
+        cy = np.zeros(K)
+        colk = np.zeros((K, 7))
+        for k in range(K):
+            b = perm[k, g]
+            colk[k] = desc[k, b]
+            if b < len(descs[k]):
+                ys_, xs_ = np.nonzero(labels_all[k] == b)
+                pos = (ys_.astype(np.uint64) * 65536 + xs_.astype(np.uint64))
+                pos.sort()
+            else:
+                pos = np.zeros(0, np.uint64)
+            keep.append(pos)
+            cnt[k] = len(pos)
+        O.lib.orc_fix_volatiles(colk.ctypes.data_as(f64p), K)
+        cx[:] = colk[:, 1]
+        cy[:] = colk[:, 2]
+        ptrs = (u64p * K)(*[p.ctypes.data_as(u64p) for p in keep])
+        wdt = O.lib.orc_chain_build(ptrs, cnt.ctypes.data_as(u64p), cx.ctypes.data_as(f64p),
+                                    cy.ctypes.data_as(f64p), K, density, g, None, 0)
+        buf = np.zeros(int(wdt) * K, np.uint64)
+        O.lib.orc_chain_build(ptrs, cnt.ctypes.data_as(u64p), cx.ctypes.data_as(f64p),
+                              cy.ctypes.data_as(f64p), K, density, g,
+                              buf.ctypes.data_as(u64p), int(wdt))
+        widths.append(int(wdt))
+        chains.append(buf.reshape(K, int(wdt)))
+    widths = np.array(widths, np.uint64)
+    pts = np.concatenate(chains, axis=1).reshape(-1)
+    order = np.zeros((K, Wb), np.int32)
+    for k in range(K):
+        for g in range(Wb):
+            order[k, perm[k, g]] = g
+    H = max(f.shape[0] for f in frames)
+    W = max(f.shape[1] for f in frames)
+    return dict(K=K, width=W, height=H, bbox=bbox, seed=seed, motion=motion,
+                fading=fading, delimiter=delim, density=density, colors=colors,
+                present=present, widths=widths, pts=pts, blob_order=order,
+                frame_keys=np.arange(K, dtype=np.uint64))

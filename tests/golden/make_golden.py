@@ -20,8 +20,12 @@ Fixtures (all small, seeded):
   edges.npz       edge inputs: an all-transparent key frame, a single key
                   frame, key frames of different sizes (counts, chains, frames)
   blob_rules.npz  blob counts under blob_threshold / number / min / max size
+  converge256.npz the reference's converged cost (its own morph_asynch to a
+                  plateau) on the CPU pipeline's chains of shapes256
+  matching.npz    blob matching results (groups per pixel, best blob-map
+                  energy, descriptors) on four cases of 2-4 key frames
 
-    python tests/golden/make_golden.py features   # one fixture only (or: edges, blob_rules)
+    python tests/golden/make_golden.py features   # one fixture only (or: edges, blob_rules, converge, matching)
 """
 from __future__ import annotations
 
@@ -132,9 +136,95 @@ def features_case(R):
                 widths=st["widths"], pts=st["pts"], blob_order=st["blob_order"], blob_avg=st["blob_avg"])
 
 
+def converge_case(R, window=10000, rel=2e-5, max_sweeps=200000):
+    """C2-style convergence target: the chains the CPU pipeline builds for
+    shapes256 (2 key frames of 256x256, about 40k atoms, HSP), refined by the
+    reference's own morph_asynch (the unmodified library, ref_sweeps) until a
+    window of `window` sweeps gains less than `rel` of the cost.  The chains
+    are rebuilt at test time by the same deterministic CPU pipeline; their
+    checksum is stored to prove it."""
+    O = orc.Oracle()
+    frames = synth.workload("shapes256")
+    st = orc.pipeline(O, frames, delimiter=1, density=1, seed=5, motion=4, fading=6)
+    w, pts, K = st["widths"], st["pts"], st["K"]
+    R.new(frames, seed=5, motion=4, fading=6, delimiter=1, density=1, resync=True)
+    R.prepare()
+    rw, rK = R.widths()
+    assert rK == K and np.array_equal(np.sort(rw), np.sort(w)) and np.array_equal(rw, w), (rw, w)
+    R.set_points(pts)
+    e0 = O.energy(pts, w, K)[1]
+    assert int(R.energy()) == e0
+    # the first 50 sweeps of the reference and of the oracle's restatement agree bit for bit
+    R.sweeps(50, 1)
+    assert np.array_equal(R.points(), O.sweeps(pts, w, K, 50, 1))
+    done, seed, trace = 50, 2, [(50, int(R.energy()))]
+    while done < max_sweeps:
+        R.sweeps(window, seed)
+        seed += 1
+        done += window
+        trace.append((done, int(R.energy())))
+        if trace[-2][1] - trace[-1][1] < rel * trace[-1][1]:
+            break
+    cost = trace[-1][1]
+    assert O.energy(R.points(), w, K)[1] == cost
+    return dict(initial_cost=e0, converged_cost=cost, converged_sweeps=done, trace=np.array(trace, np.int64),
+                widths=w, pts_checksum=np.uint64(int(np.bitwise_xor.reduce(pts * np.uint64(0x9E3779B97F4A7C15)))))
+
+
+MATCH_CASES = [("ellipses64", 7, 1), ("spline48", 3, 0), ("features", 5, 1), ("many96", 11, 0)]
+
+
+def matching_frames(name):
+    if name == "ellipses64":
+        return synth.workload("ellipses64")
+    if name == "spline48":
+        r3 = np.random.default_rng(48)
+        return [synth.ellipses_frame(48, 3, 4.0, 12.0, r3) for _ in range(3)]
+    if name == "features":
+        rng = np.random.default_rng(77)
+        return [synth.ellipses_frame(56, 5, 3.0, 14.0, rng) for _ in range(4)]
+    rng = np.random.default_rng(96)
+    return [synth.ellipses_frame(96, 10, 3.0, 10.0, rng) for _ in range(4)]
+
+
+def matching_case(R):
+    """Blob matching (thread::match, thread.cpp:598-738) of the reference,
+    run with a valid bounding box (one synchronize before prepare, as the
+    demo's loop gives it): per case the group of every key-frame pixel's
+    blob, the reference's best blob-map energy and its blob descriptors
+    (running means, stored colour space) by group."""
+    O = orc.Oracle()
+    out = {}
+    for name, seed, delim in MATCH_CASES:
+        frames = matching_frames(name)
+        R.new(frames, seed=seed, motion=3, fading=6, delimiter=delim, density=1, resync=True)
+        R.prepare()
+        K = len(frames)
+        glab = np.stack([R.group_labels(f) for f in range(K)])
+        groups = max(R.blob_count(f) for f in range(K))
+        desc = np.zeros((groups, K, 7))
+        for f in range(K):
+            for g, sz, xy in R.blobs(f):
+                desc[g, f, 0] = sz
+                desc[g, f, 1:] = xy
+        bd = orc.bbox_diag2(frames)
+        e = R.blob_energy()
+        assert abs(O.blob_energy(desc, bd) - e) <= 1e-9 * max(e, 1.0), (name, O.blob_energy(desc, bd), e)
+        out.update({f"{name}_frames": np.stack(frames), f"{name}_group_labels": glab.astype(np.int16),
+                    f"{name}_energy": e, f"{name}_desc": desc, f"{name}_delimiter": delim, f"{name}_seed": seed})
+    out["cases"] = np.array([c[0] for c in MATCH_CASES])
+    return out
+
+
 def main():
     orc.build(with_ref=True)
     R = orc.Reference()
+    if sys.argv[1:] == ["matching"]:
+        np.savez_compressed(os.path.join(HERE, "matching.npz"), **matching_case(R))
+        return
+    if sys.argv[1:] == ["converge"]:
+        np.savez_compressed(os.path.join(HERE, "converge256.npz"), **converge_case(R))
+        return
     if sys.argv[1:] == ["features"]:
         np.savez_compressed(os.path.join(HERE, "features.npz"), **features_case(R))
         return
@@ -193,6 +283,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "features.npz"), **features_case(R))
     np.savez_compressed(os.path.join(HERE, "edges.npz"), **edges_case(R))
     np.savez_compressed(os.path.join(HERE, "blob_rules.npz"), **blob_rules_case(R))
+    np.savez_compressed(os.path.join(HERE, "converge256.npz"), **converge_case(R))
+    np.savez_compressed(os.path.join(HERE, "matching.npz"), **matching_case(R))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
