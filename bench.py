@@ -346,11 +346,13 @@ def fluid_bench(m, torch, stream, args):
     """Fluid-on frames (the draw_fluid path the reference takes when fluid
     steps are set, morph.cpp:1417-1418) on the same chains: every frame
     manages the particles (step_fluid), runs `--fluid-steps` solver steps on
-    a grid of (0.5 x 1024 + 20)^2 nodes and draws them.  The simulation is
+    a 512 x 512 grid (sparseness 492/1024: 1024 * s + 20 = 512 nodes per
+    axis) and draws them.  The simulation is
     stateful, so frames are rendered in cycle order; timed with CUDA events
     on the render stream.  Per-part times come from one further profiled run
     of frames."""
-    m.set(fluid=args.fluid_steps, fluid_sparseness=0.5)
+    sparseness = 492.0 / 1024.0
+    m.set(fluid=args.fluid_steps, fluid_sparseness=sparseness)
     n_frames = FRAMES_PER_STEP
     out = torch.empty((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
     ts = [m.get_time(i, n_frames) for i in range(n_frames)]
@@ -379,7 +381,7 @@ def fluid_bench(m, torch, stream, args):
     m.set(fluid=0)
     hbm, peak_kind = _peaks()
     P = m.atoms
-    gx = gy = int(round(1024 * 0.5)) + 20
+    gx = gy = int(round(1024 * sparseness)) + 20
     step_bytes = P * 96 + gx * gy * 104  # particle fields read 16 + written 8 (FP32); 13 node fields x2
     st_ms, st_n = prof.get("fluid_step", (0.0, 0))
     res = {"workload": WORKLOAD + " with fluid", "grid": [gx, gy], "particles": int(P),
@@ -617,8 +619,9 @@ def cpu_pipeline(O, frames):
 def profile_case(args):
     """Every kernel of the morph path, a few launches each, on one seeded
     workload: the program the per-kernel ncu captures under profiles/ run.
-    After the pipeline (components, blob matching, chain construction): 4
-    plain sweeps, 4 guided sweeps, 2 recorded sweeps, one training epoch, 4
+    After the pipeline (components, blob matching, chain construction):
+    `--refine-sweeps` plain sweeps (as the benchmark refines before it
+    renders), 4 guided sweeps, 2 recorded sweeps, one training epoch, 4
     gated (learned) sweeps, the allocation-free cost, `--frames` atom frames,
     2 fluid frames with 2 solver steps each on a (0.5 W + 20)^2 grid, and one
     batched refinement of 4 small jobs.  Settings as the benchmark's."""
@@ -634,7 +637,7 @@ def profile_case(args):
         m.set(motion_noise=args.motion_noise)
     if m.run_until(capi.STATE_ATOM_MORPHING) != capi.STATE_ATOM_MORPHING:
         raise RuntimeError("pipeline stopped early")
-    m.refine(4, capi.PROPOSAL_RANDOM)
+    m.refine(max(args.refine_sweeps, 1), capi.PROPOSAL_RANDOM)
     m.tune(guided_switch=0)
     m.refine(4, capi.PROPOSAL_LOCAL)
     m.tune(learned_adaptive=0)
