@@ -431,21 +431,24 @@ __device__ __forceinline__ uint4 splat_atom(const RenderScene &sc, const FrameAr
 
 // Tiles of the valid corners of a splat record, each distinct tile once:
 // bit k of the returned mask marks corner k as the first valid corner in its
-// tile; tk[k] is that corner's tile.  Registers only.
+// tile; tk[k] is that corner's tile.  The four corners span at most 2 x 2
+// tiles: corner k is in the base pixel's tile moved one tile right when k is
+// a right corner and the base pixel is the last column of its tile, one down
+// likewise.  Registers only.
 __device__ __forceinline__ uint32_t record_tiles(uint4 s, uint32_t tiles_x, uint32_t *tk) {
     const uint32_t px = s.x & 0xFFFFu, py = s.x >> 16, valid = (s.y >> 16) & 15u;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) tk[k] = ((py + (k >> 1)) / kTile) * tiles_x + (px + (k & 1)) / kTile;
-    uint32_t m = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        if (!(valid & (1u << k))) continue;
-        bool dup = false;
-#pragma unroll
-        for (int j = 0; j < k; ++j) dup |= (valid & (1u << j)) && tk[j] == tk[k];
-        if (!dup) m |= 1u << k;
-    }
-    return m;
+    const uint32_t t00 = (py / kTile) * tiles_x + px / kTile;
+    const bool cx = (px % kTile) == kTile - 1, cy = (py % kTile) == kTile - 1;
+    const uint32_t dx = cx ? 1u : 0u, dy = cy ? tiles_x : 0u;
+    tk[0] = t00;
+    tk[1] = t00 + dx;
+    tk[2] = t00 + dy;
+    tk[3] = t00 + dx + dy;
+    uint32_t m = valid;
+    if (!cx && !cy) return m & (0u - m);                                 // one tile: its lowest valid corner
+    if (!cx) return (m & 0x5u) | (m & 0xAu & ~((m & 0x5u) << 1));        // corners 0,1 and 2,3 share tiles
+    if (!cy) return (m & 0x3u) | (m & 0xCu & ~((m & 0x3u) << 2));        // corners 0,2 and 1,3 share tiles
+    return m;                                                            // four tiles
 }
 
 __global__ void __launch_bounds__(256) k_frame_splat(RenderScene sc, FrameArgs fa, const uint32_t *n_dev,
@@ -602,10 +605,15 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
             if (m & (1u << k)) atomicAdd(&hist[tk[k]], 1u);
     }
     __syncthreads();
-    // ---- this CTA's share of every tile it touches
+    // ---- this CTA's share of every tile it touches: hist becomes the CTA's
+    // write cursor in the record buffer, base the end of the tile's region
     for (uint32_t t = tid; t < ntiles; t += kBinThreads) {
         const uint32_t h = hist[t];
-        if (h) hist[t] = atomicAdd(&b.cnt[t], h);
+        if (h) {
+            const uint32_t o = b.off[t];
+            hist[t] = o + atomicAdd(&b.cnt[t], h);
+            base[t] = o + b.cap[t];
+        }
     }
     __syncthreads();
     // ---- records into the tiles' regions (the overflow list past capacity)
@@ -617,8 +625,8 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
         for (int k = 0; k < 4; ++k) {
             if (!(m & (1u << k))) continue;
             const uint32_t t = tk[k], pos = atomicAdd(&hist[t], 1u);
-            if (pos < b.cap[t]) {
-                b.rec[b.off[t] + pos] = rec;
+            if (pos < base[t]) {
+                b.rec[pos] = rec;
             } else {
                 const uint32_t o = atomicAdd(b.ovf_cnt, 1u);
                 if (o < b.ovf_cap) b.ovf[o] = make_uint4(rec.x, rec.y | (t << 20), rec.z, rec.w);
@@ -738,6 +746,12 @@ __device__ __forceinline__ uint32_t round_div(const RoundDiv &d, uint32_t num) {
 
 constexpr int kRecCache = 1920;   // records of a tile kept in shared memory (30 KB; 4 CTAs per SM fit)
 constexpr uint32_t kPackMax = 258; // contributions per pixel for which packed 32-bit sums cannot overflow
+// Without per-pixel counts (density 1) the packed sums are checked through
+// the weight sum W: every channel sum is at most 255 W, so W <= kPackW keeps
+// them below 2^32; W itself cannot wrap while the tile holds fewer than
+// kPackRec records (each contributes at most 65025 to a pixel).
+constexpr uint32_t kPackW = 0xFFFFFFFFu / 255u;
+constexpr uint32_t kPackRec = 0xFFFFFFFFu / 65025u;
 
 // Shared memory of the resolve kernel, two layouts over one buffer:
 //  packed: W, N, R, G, B, A as 32-bit sums [1024] each (exact while a pixel
@@ -909,7 +923,10 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
     int n[4];
     uint32_t c0[4];
     double st[4][4];  // FP64 "over" state (R, G, B, A) of pixels with 2+ blobs; local memory, rarely touched
-    for (int mode = 0; mode < 2; ++mode) {
+    // density 1: a pixel's alpha needs no count, so the packed mode keeps
+    // five sums per pixel and checks the weight sum instead of the count
+    const bool counted = density > 1;
+    for (int mode = (!counted && nrec >= kPackRec) ? 1 : 0; mode < 2; ++mode) {
         const bool packed = mode == 0;
         const bool cached = packed && nrec <= (uint32_t)kRecCache;
         uint32_t mn = 0xFFFFFFFFu;
@@ -979,7 +996,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                     uint32_t W = wx[k & 1] * wy[k >> 1];
                     if (packed) {
                         atomicAdd(&pW[li], W);
-                        atomicAdd(&pN[li], 1u);
+                        if (counted) atomicAdd(&pN[li], 1u);
                         atomicAdd(&pR[li], W * cr);
                         atomicAdd(&pG[li], W * cg);
                         atomicAdd(&pB[li], W * cb);
@@ -1001,10 +1018,13 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                 feather_layers(tr, tiles_x, o.tiles_y, tile, cur, o.feather,
                                reinterpret_cast<uint32_t *>(sm + kResolveSmem), flayer);
             if (packed) {
-                // more than kPackMax contributions could have wrapped a 32-bit sum
+                // more than kPackMax contributions (a weight sum above kPackW
+                // without counts) could have wrapped a 32-bit sum
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (pN[threadIdx.x + 256 * q] > kPackMax) s_over = 1;
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t li = threadIdx.x + 256 * q;
+                    if (counted ? pN[li] > kPackMax : pW[li] > kPackW) s_over = 1;
+                }
                 __syncthreads();
                 if (s_over) { over = true; break; }
             }
@@ -1014,8 +1034,8 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                 unsigned long long W, sr, sg, sb, sa;
                 uint32_t cnt;
                 if (packed) {
-                    cnt = pN[li];
                     W = pW[li]; sr = pR[li]; sg = pG[li]; sb = pB[li]; sa = pA[li];
+                    cnt = counted ? pN[li] : (W ? 1u : 0u);  // valid corners have positive weights
                     pW[li] = 0u; pN[li] = 0u; pR[li] = 0u; pG[li] = 0u; pB[li] = 0u; pA[li] = 0u;
                 } else {
                     cnt = xN[li];
@@ -1145,12 +1165,7 @@ int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, do
     std::memset(&fa, 0, sizeof(fa));
     fa.w1 = 1.0 - t;
     fa.w2 = 1.0 - fa.w1;
-    fa.w1q = llround(std::ldexp(fa.w1, 38));
-    auto split = [](long long q, int32_t *h, int32_t *l) {
-        *h = (int32_t)(q >> 19);  // arithmetic shift: floor division
-        *l = (int32_t)(q & ((1ll << 19) - 1));
-    };
-    split(fa.w1q, &fa.w1h, &fa.w1l);
+    fa.w1q = (int32_t)llround(std::ldexp(fa.w1, 30));
     fa.lin_mode = fa.w1 == 1.0 ? 1u : (fa.w1 == 0.0 ? 2u : 0u);
     fa.str = (float)(1.0 - t);
     fa.noise_s = sc.motion_noise > 0.0 ? (float)(sc.motion_noise * 256.0 * std::sin(3.141592653589793 * t)) : 0.f;
@@ -1171,12 +1186,9 @@ int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, do
         fa.b3 = 0.5 * (t3 - t2);
         fa.seg[0] = wrap(p - 1); fa.seg[1] = wrap(p); fa.seg[2] = wrap(p + 1); fa.seg[3] = wrap(p + 2);
         fa.seg_ok = (p == (int)f) ? 1u : 0u;
-        fa.bq0 = llround(std::ldexp(fa.b0, 38));
-        fa.bq2 = llround(std::ldexp(fa.b2, 38));
-        fa.bq3 = llround(std::ldexp(fa.b3, 38));
-        split(fa.bq0, &fa.bh0, &fa.bl0);
-        split(fa.bq2, &fa.bh2, &fa.bl2);
-        split(fa.bq3, &fa.bh3, &fa.bl3);
+        fa.bq0 = (int32_t)llround(std::ldexp(fa.b0, 30));
+        fa.bq2 = (int32_t)llround(std::ldexp(fa.b2, 30));
+        fa.bq3 = (int32_t)llround(std::ldexp(fa.b3, 30));
         fa.key_mode = (fa.b0 == 0.0 && fa.b1 == 1.0 && fa.b2 == 0.0 && fa.b3 == 0.0) ? 1u : 0u;
     }
     return AM_OK;

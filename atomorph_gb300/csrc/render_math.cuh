@@ -95,12 +95,11 @@ __device__ __forceinline__ uint32_t displace_rn(uint32_t w, float s, float n) {
 struct FrameArgs {
     double w1, w2;          // LINEAR: weight of pt1 and 1 - that weight
     double b0, b1, b2, b3;  // SPLINE basis at the frame's local time
-    long long w1q;          // round(w1 * 2^38)
-    long long bq0, bq2, bq3;// round(b_i * 2^38) (b1 enters through the q1 term)
-    // The same weights split as hi * 2^19 + lo (lo in [0, 2^19)), so every
-    // product with a 32-bit coordinate difference is a 32 x 32 -> 64-bit
-    // multiply: 64 x 64-bit integer multiplies are slow on this part.
-    int32_t w1h, w1l, bh0, bl0, bh2, bl2, bh3, bl3;
+    // The weights as round(w * 2^30) in 32 bits (every one lies in
+    // (-0.08, 1], so it fits), so each product with a 32-bit coordinate
+    // difference is one 32 x 32 -> 64-bit multiply-add; b1 enters through
+    // the q1 term.
+    int32_t w1q, bq0, bq2, bq3;
     uint32_t lin_mode;      // 0 general, 1 w1 == 1 (X = X1), 2 w1 == 0 (X = X2)
     uint32_t key_mode;      // 1 when the spline basis is exactly (0, 1, 0, 0)
     uint32_t seg_ok;        // 1 when the spline segment is the prepared one
@@ -117,50 +116,59 @@ int frame_args(RenderWork *w, const RenderScene &sc, double time, uint32_t f, do
 
 // Fast exact positions.  The reference evaluates its interpolation in
 // double.  The kernels evaluate the same formula's real value in 64-bit fixed
-// point (weights quantised to 2^-38) and take its floor / rounded fraction,
+// point (weights quantised to 2^-30) and take its floor / rounded fraction,
 // which equals the reference's unless the value lies within the combined
-// error bound of a rounding boundary; those rare atoms re-run the reference's
-// own double formula (lin_fixed / spl_fixed below).  The bound is per atom:
-// quantising a weight moves the value by at most half a unit of 2^-38 per
-// unit of the coordinate difference it multiplies, i.e. |d| / 2 fixed-point
-// units in total, and the reference's double rounding (a handful of
+// error bound of a rounding boundary; those rare atoms (and the rarer ones
+// with a negative value or a coordinate difference of 2^22 units or more)
+// re-run the reference's own double formula (lin_fixed / spl_fixed below).
+// The bound is per atom: quantising a weight moves the value by at most half
+// a fixed-point unit per unit of the coordinate difference it multiplies,
+// i.e. sum |d| / 2 units, and the reference's double rounding (a handful of
 // operations on values below 2^16 px, plus its weights summing to 1 only
-// within a few ulps) stays below 2^13 units of 2^-46 px.  Returns false when
-// the fallback is needed.
+// within a few ulps) stays below 2^-33 px.  Returns false when the fallback
+// is needed.
+//
+// LINEAR: X = floor(w1 a + (1 - w1) b) in 1/256 px (morph.cpp:1501-1515).
+// V = b 2^30 + round(w1 2^30) (a - b), units of 2^-30 / 256 px.
 __device__ __forceinline__ bool lin_fast(const FrameArgs &fa, int32_t a, int32_t b, int32_t *out) {
     if (fa.lin_mode == 1) { *out = a; return true; }
     if (fa.lin_mode == 2) { *out = b; return true; }
     const int32_t d = a - b;
-    long long V = ((long long)b << 38) + (long long)fa.w1h * d * (1ll << 19) + (long long)fa.w1l * d;  // 2^-38 (1/256 px)
-    const long long one = 1ll << 38;
-    const long long tol = (long long)((uint32_t)abs(d) >> 1) + (1ll << 13);
-    long long r = V & (one - 1);
-    if (r < tol || one - r < tol) return false;
-    *out = (int32_t)(V >> 38);
+    const long long V = (long long)fa.w1q * d + ((long long)b << 30);
+    const uint32_t r = (uint32_t)V & ((1u << 30) - 1u);
+    const uint32_t tol = ((uint32_t)abs(d) >> 1) + 64u;  // 64 units = 2^-32 px, above the reference's error
+    if (r < tol || (1u << 30) - r < tol) return false;
+    *out = (int32_t)(V >> 30);
     return true;
 }
+// SPLINE: the Catmull-Rom value v of the prepared basis (morph.cpp:526-531,
+// spline.cpp:45-57), then the reference's split into integer pixel trunc(v)
+// and fraction byte round(frac * 255), packed (integer << 8) | byte.
+// V = q1 2^30 + sum_i round(b_i 2^30) (q_i - q1), units of 2^-38 px; its top
+// 32 fraction bits f (units of 2^-32 px) give both roundings in 32-bit
+// arithmetic: the integer boundary is f near 0 or 2^32, the byte is the high
+// word of f * 255 + 2^31 and its boundary the low word near 0 or 2^32.
 __device__ __forceinline__ bool spl_fast(const FrameArgs &fa, int32_t q0, int32_t q1, int32_t q2, int32_t q3,
                                          uint32_t *out) {
-    if ((abs(q0 - q1) | abs(q2 - q1) | abs(q3 - q1)) >= (1 << 22)) return false;  // keeps V in 63 bits
     const int32_t d0 = q0 - q1, d2 = q2 - q1, d3 = q3 - q1;
-    long long V = ((long long)q1 << 38) +
-                  ((long long)fa.bh0 * d0 + (long long)fa.bh2 * d2 + (long long)fa.bh3 * d3) * (1ll << 19) +
-                  (long long)fa.bl0 * d0 + (long long)fa.bl2 * d2 + (long long)fa.bl3 * d3;  // units of 2^-46 px
-    unsigned long long A = V >= 0 ? (unsigned long long)V : (unsigned long long)(-V);
-    const unsigned long long one = 1ull << 46;
-    unsigned long long I = A >> 46, F = A & (one - 1);
+    const uint32_t a0 = (uint32_t)abs(d0), a2 = (uint32_t)abs(d2), a3 = (uint32_t)abs(d3);
+    if ((a0 | a2 | a3) >= (1u << 22)) return false;  // keeps V in 63 bits and the bounds in 32
+    long long V = (long long)q1 << 30;
+    V += (long long)fa.bq0 * d0;
+    V += (long long)fa.bq2 * d2;
+    V += (long long)fa.bq3 * d3;
+    if (V < 0) return false;  // left of the canvas origin: the reference's signed split decides
+    const uint32_t I = (uint32_t)(V >> 38), f = (uint32_t)(V >> 6);
+    const unsigned long long p = (unsigned long long)f * 255ull + 0x80000000ull;
     if (!fa.key_mode) {
-        const unsigned long long tol =
-            (unsigned long long)(((uint32_t)abs(d0) + (uint32_t)abs(d2) + (uint32_t)abs(d3)) >> 1) + (1ull << 14);
-        if (F < tol || one - F < tol) return false;
-        unsigned long long h = ((F << 8) - F) & (one - 1);  // F * 255 mod one
-        unsigned long long dd = h > (one >> 1) ? h - (one >> 1) : (one >> 1) - h;
-        if (dd < 255ull * tol) return false;
+        // sum |d| / 2 units of 2^-38 px quantisation + 2^-33 px reference error
+        // + the 2^-32 px truncation of f, in units of 2^-32 px
+        const uint32_t tol = ((a0 + a2 + a3) >> 7) + 4u;
+        if (f < tol || f > ~tol) return false;
+        const uint32_t lo = (uint32_t)p, t255 = tol * 255u + 255u;
+        if (lo < t255 || lo > ~t255) return false;
     }
-    unsigned long long xf = ((F << 8) - F + (one >> 1)) >> 46;  // round(F * 255), half away on |fraction|
-    uint32_t xi = (uint32_t)I & 0xFFFFu, xb = (uint32_t)xf & 0xFFu;
-    if (V < 0) { xi = (0u - xi) & 0xFFFFu; xb = (0u - xb) & 0xFFu; }
-    *out = (xi << 8) | xb;
+    *out = ((I & 0xFFFFu) << 8) | ((uint32_t)(p >> 32) & 0xFFu);
     return true;
 }
 
