@@ -389,8 +389,14 @@ __device__ __forceinline__ uint32_t axis_fixed(const RenderScene &sc, const Fram
 // rules (morph.cpp:552-588), packed as
 // {px | py << 16, xf | yf << 8 | valid << 16, colour, rank}.
 __device__ __forceinline__ uint4 finish_record(const RenderScene &sc, uint32_t X, uint32_t Y, uint32_t colour,
-                                               uint32_t r) {
+                                               uint32_t rr) {
     uint32_t px = X >> 8, py = Y >> 8, xf = X & 255u, yf = Y & 255u;
+    if (px + 1 < sc.width && py + 1 < sc.height) {
+        // every corner inside the output: the rules reduce to positive weights
+        const uint32_t l = xf < 255u, r = xf > 0u, t = yf < 255u, d = yf > 0u;
+        const uint32_t valid = (l & t) | ((r & t) << 1) | ((l & d) << 2) | ((r & d) << 3);
+        return make_uint4(px | (py << 16), xf | (yf << 8) | (valid << 16), colour, rr);
+    }
     uint32_t valid = 0;
     const uint32_t bx1 = sc.bbox[0], by1 = sc.bbox[1], bx2 = sc.bbox[2], by2 = sc.bbox[3];
     bool skip = (px >= sc.width || py >= sc.height) && (px > bx2 || px < bx1 || py > by2 || py < by1);
@@ -407,7 +413,7 @@ __device__ __forceinline__ uint4 finish_record(const RenderScene &sc, uint32_t X
         if (px >= sc.width || py + 1 >= sc.height) valid &= ~4u;
         if (px + 1 >= sc.width || py + 1 >= sc.height) valid &= ~8u;
     }
-    return make_uint4(px | (py << 16), xf | (yf << 8) | (valid << 16), colour, r);
+    return make_uint4(px | (py << 16), xf | (yf << 8) | (valid << 16), colour, rr);
 }
 
 // One atom at the frame's time: exact position, faded colour (morph.cpp:
@@ -536,6 +542,23 @@ inline size_t bin_smem(uint32_t per, uint32_t ntiles) {
 
 constexpr uint32_t kNoAtom = 0xFFFFFFFFu;  // X of a record slot past the last atom
 
+// One atom's inputs for a frame: its control coordinates, colours, fade
+// ramp, composite rank and (with the motion perturbation) noise pair.
+struct AtomIn {
+    int4 a, c;
+    uint2 col;
+    float2 q;
+    uint32_t rank;
+    float2 nz;
+};
+__device__ __forceinline__ void load_atom(const BinArgs &b, uint64_t i, bool noise, AtomIn &x) {
+    atom_controls(b.sc, b.fa, b.in, i, x.a, x.c);
+    x.col = b.in.col[i];
+    x.q = b.in.ls[i];
+    x.rank = b.in.rank[i];
+    x.nz = noise ? b.in.mn[i] : make_float2(0.f, 0.f);
+}
+
 __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
     extern __shared__ __align__(16) unsigned char bsm[];
     const uint32_t ntiles = b.fa.ntiles, tid = threadIdx.x, per = kBinPer;
@@ -554,20 +577,27 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
     // double formula are listed and evaluated together afterwards, so the
     // slow FP64 work runs in full warps instead of holding up every warp
     // that contains one such atom.
-    for (uint32_t r = 0; r < per; ++r) {
+    const bool noise = b.fa.noise_s != 0.f;
+    for (uint32_t r = 0; r < kBinPer; ++r) {
         const uint32_t slot = r * kBinThreads + tid;
         const uint64_t i = chunk0 + slot;
         uint4 v = make_uint4(kNoAtom, 0, 0, 0);
         uint32_t need = 0;
         if (i < n_atoms) {
-            int4 a, c;
-            atom_controls(b.sc, b.fa, b.in, i, a, c);
-            if (!axis_fast(b.sc, b.fa, 0, a, c, &v.x)) need |= 1u;
-            if (!axis_fast(b.sc, b.fa, 1, a, c, &v.y)) need |= 2u;
-            const uint2 col = b.in.col[i];
-            const float2 q = b.in.ls[i];
-            v.z = fade_colour(b.sc.fading, col.x, col.y, q, b.fa.str);
-            v.w = b.in.rank[i];
+            AtomIn x;
+            load_atom(b, i, noise, x);
+            if (axis_fast(b.sc, b.fa, 0, x.a, x.c, &v.x)) {
+                if (noise) v.x = displace_rn(v.x, b.fa.noise_s, x.nz.x);
+            } else {
+                need |= 1u;
+            }
+            if (axis_fast(b.sc, b.fa, 1, x.a, x.c, &v.y)) {
+                if (noise) v.y = displace_rn(v.y, b.fa.noise_s, x.nz.y);
+            } else {
+                need |= 2u;
+            }
+            v.z = fade_colour(b.sc.fading, x.col.x, x.col.y, x.q, b.fa.str);
+            v.w = x.rank;
         }
         srec[slot] = v;
         const uint32_t k = __popc(need);
@@ -583,19 +613,18 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
         const uint32_t e = fix[j], slot = e >> 1, axis = e & 1u;
         int4 a, c;
         atom_controls(b.sc, b.fa, b.in, chunk0 + slot, a, c);
-        const uint32_t v = axis_fixed(b.sc, b.fa, (int)axis, a, c);
+        uint32_t v = axis_fixed(b.sc, b.fa, (int)axis, a, c);
+        if (noise) {
+            const float2 nz = b.in.mn[chunk0 + slot];
+            v = displace_rn(v, b.fa.noise_s, axis ? nz.y : nz.x);
+        }
         if (axis) srec[slot].y = v;
         else srec[slot].x = v;
     }
     __syncthreads();
     for (uint32_t r = 0; r < per; ++r) {
         const uint32_t slot = r * kBinThreads + tid;
-        uint4 v = srec[slot];
-        if (v.x != kNoAtom && b.fa.noise_s != 0.f) {
-            const float2 nz = b.in.mn[chunk0 + slot];
-            v.x = displace_rn(v.x, b.fa.noise_s, nz.x);
-            v.y = displace_rn(v.y, b.fa.noise_s, nz.y);
-        }
+        const uint4 v = srec[slot];
         const uint4 rec = v.x == kNoAtom ? make_uint4(0, 0, 0, 0) : finish_record(b.sc, v.x, v.y, v.z, v.w);
         srec[slot] = rec;
         uint32_t tk[4];
@@ -1028,6 +1057,13 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                 __syncthreads();
                 if (s_over) { over = true; break; }
             }
+            // after the last blob rank the accumulators are not read again
+            bool more = true;
+            if (packed) {
+                uint32_t nx = red[0];
+                for (int k = 1; k < 8; ++k) nx = min(nx, red[k]);
+                more = nx != 0xFFFFFFFFu;
+            }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const uint32_t li = threadIdx.x + 256 * q;
@@ -1036,7 +1072,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                 if (packed) {
                     W = pW[li]; sr = pR[li]; sg = pG[li]; sb = pB[li]; sa = pA[li];
                     cnt = counted ? pN[li] : (W ? 1u : 0u);  // valid corners have positive weights
-                    pW[li] = 0u; pN[li] = 0u; pR[li] = 0u; pG[li] = 0u; pB[li] = 0u; pA[li] = 0u;
+                    if (more) { pW[li] = 0u; pN[li] = 0u; pR[li] = 0u; pG[li] = 0u; pB[li] = 0u; pA[li] = 0u; }
                 } else {
                     cnt = xN[li];
                     W = xW[li]; sr = xR[li]; sg = xG[li]; sb = xB[li]; sa = xA[li];
