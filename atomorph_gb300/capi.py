@@ -20,7 +20,7 @@ AM_OK, AM_ERR_BUSY, AM_ERR_NOMEM, AM_ERR_CUDA, AM_ERR_TIMEOUT, AM_ERR_ARG, AM_ER
     AM_ERR_NOT_FOUND = range(9)
 RGB, HSP, NONE, LINEAR, SPLINE, COSINE, PERLIN = range(7)
 STATE_BLOB_DETECTION, STATE_BLOB_UNIFICATION, STATE_BLOB_MATCHING, STATE_ATOM_MORPHING, STATE_DONE = range(5)
-PROPOSAL_RANDOM, PROPOSAL_LOCAL, PROPOSAL_LEARNED = range(3)
+PROPOSAL_RANDOM, PROPOSAL_LOCAL, PROPOSAL_LEARNED, PROPOSAL_SCORED = range(4)
 
 u8p = C.POINTER(C.c_uint8)
 u64p = C.POINTER(C.c_uint64)
@@ -97,6 +97,7 @@ _SIGS = {
     "am_import_chains": (C.c_int, [vp, C.c_size_t, C.c_size_t, u64p, u64p, i32p]),
     "am_refine": (C.c_int, [vp, C.c_size_t, u64p]),
     "am_record_swaps": (C.c_int, [vp, C.c_size_t]),
+    "am_record_outcomes": (C.c_int, [vp, C.c_size_t, C.c_uint32]),
     "am_recorded_swaps": (C.c_size_t, [vp, f32p, f32p, C.c_size_t]),
     "am_train_proposal": (C.c_int, [vp, f32p, f32p, C.c_size_t, C.c_size_t, C.c_double, f32p]),
     "am_train_recorded": (C.c_int, [vp, C.c_size_t, C.c_double, f32p]),
@@ -382,6 +383,11 @@ class Morph:
     # -- learned proposal -----------------------------------------------------
     def record_swaps(self, cap: int) -> None:
         _check(self.lib.am_record_swaps(self.h, cap), "am_record_swaps")
+
+    def record_outcomes(self, cap: int, every: int = 1) -> None:
+        """Plain sweeps log 1 in `every` proposals (pair features, accept 1 /
+        reject 0) for the learned pair proposal; cap 0 stops."""
+        _check(self.lib.am_record_outcomes(self.h, cap, every), "am_record_outcomes")
 
     def recorded_count(self) -> int:
         return int(self.lib.am_recorded_swaps(self.h, None, None, 1 << 62))

@@ -115,7 +115,7 @@ int am_set_density(am_morph *m, uint16_t d) {
 int am_set_resolution(am_morph *m, uint16_t w, uint16_t h) { CHECK(m); H(m).width = w; H(m).height = h; return AM_OK; }
 int am_set_proposal(am_morph *m, unsigned k) {
     CHECK(m);
-    if (k > AM_PROPOSAL_LEARNED) return AM_ERR_ARG;
+    if (k > AM_PROPOSAL_SCORED) return AM_ERR_ARG;
     H(m).front.proposal = k;
     H(m).active.proposal = k;
     return AM_OK;
@@ -356,6 +356,11 @@ int am_refine(am_morph *m, size_t sweeps, uint64_t *gains) {
 
 // ---- learned proposal
 int am_record_swaps(am_morph *m, size_t cap) { CHECK(m); return H(m).record_swaps(cap); }
+int am_record_outcomes(am_morph *m, size_t cap, uint32_t every) {
+    CHECK(m);
+    if (H(m).is_busy()) return AM_ERR_BUSY;
+    return H(m).record_outcomes(cap, every);
+}
 size_t am_recorded_swaps(am_morph *m, float *f, float *t, size_t cap) { return m ? m->e.recorded_swaps(f, t, cap) : 0; }
 int am_train_recorded(am_morph *m, size_t epochs, double lr, float *loss) {
     CHECK(m);

@@ -670,6 +670,31 @@ int Engine::compute_cost(uint64_t *exact) {
 int Engine::refine(size_t sweeps, uint64_t *gains) {
     if (N == 0 || K == 0 || sweeps == 0) return AM_OK;
     if (active.proposal == AM_PROPOSAL_RANDOM) return refine_plain(sweeps, gains);
+    if (active.proposal == AM_PROPOSAL_SCORED) {
+        // The pair proposal falls back to plain sweeps until its network is
+        // trained, and afterwards whenever plain sweeps gain more cost per
+        // second: one call of each is timed, the better runs the next four
+        // calls, then both are measured again.
+        if (!mlp_trained) return refine_plain(sweeps, gains);
+        const bool scored = ps_state == PS_MEASURE_SCORED || (ps_state == PS_RUN && ps_scored);
+        const uint64_t before = cost_exact;
+        const auto t0 = std::chrono::steady_clock::now();
+        int rc = scored ? refine_scored(sweeps, gains) : refine_plain(sweeps, gains);
+        if (rc) return rc;
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        const double rate = (double)(before - cost_exact) / std::max(secs, 1e-9);
+        if (ps_state == PS_MEASURE_SCORED) {
+            ps_rate = rate;
+            ps_state = PS_MEASURE_PLAIN;
+        } else if (ps_state == PS_MEASURE_PLAIN) {
+            ps_scored = ps_rate > rate;
+            ps_state = PS_RUN;
+            ps_left = 4;
+        } else if (--ps_left <= 0) {
+            ps_state = PS_MEASURE_SCORED;
+        }
+        return AM_OK;
+    }
     size_t done = 0;
     if (active.guided_switch <= 0.0) guided_on = true;
     while (!guided_on && done < sweeps) {
@@ -699,6 +724,11 @@ int Engine::refine_plain(size_t sweeps, uint64_t *gains) {
             a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
             a.key = sweep_key(seed, sweep_counter, (uint32_t)p);
             a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
+            if (recording_outcomes) {
+                a.log_feat = d_rec_feat.p; a.log_label = d_rec_gain.p; a.log_count = d_rec_count.p;
+                a.log_cap = rec_cap; a.log_every = outcome_every;
+                a.display = d_display.p; a.CW = CW; a.CH = CH;
+            }
             if (pair_off[C] > 0) {
                 prof.open(stream);
                 rc = launch_sweep_random(a, stream);
@@ -717,6 +747,54 @@ int Engine::refine_plain(size_t sweeps, uint64_t *gains) {
         if (gains) gains[s] = acc[2 * s];
     }
     return AM_OK;
+}
+
+// Sweeps of the learned pair proposal: per phase the network scores four
+// random partners of every column and mutually best-scored pairs are swapped
+// when the exact criterion holds; the gains are exact, as in plain sweeps.
+int Engine::refine_scored(size_t sweeps, uint64_t *gains) {
+    local_valid = false;
+    int rc;
+    size_t maxph = 0;
+    for (auto &p : phases_for(K)) maxph = std::max(maxph, p.size());
+    if (scored_layout != layout_version) {
+        if ((rc = d_scored_chain.reserve(std::max<uint64_t>(N, 1)))) return rc;
+        if ((rc = launch_chain_ids(d_chain_off.p, C, N, d_scored_chain.p, stream))) return rc;
+        scored_layout = layout_version;
+    }
+    if ((rc = d_sclaim.reserve(std::max<size_t>(N * maxph, 1)))) return rc;
+    if ((rc = d_acc.reserve(std::max<size_t>(8, 2 * sweeps + 4)))) return rc;
+    AMG_CUDA(cudaMemsetAsync(d_acc.p + 4, 0, 2 * sweeps * 8, stream));
+    auto ph = phases_for(K);
+    for (size_t s = 0; s < sweeps; ++s) {
+        uint32_t pofs = 0;
+        for (size_t p = 0; p < ph.size(); ++p) {
+            ScoredArgs a;
+            a.P = d_P.p; a.N = N; a.K = K; a.C = C; a.chain_off = d_chain_off.p; a.chain_id = d_scored_chain.p;
+            a.frames = d_phase.p + pofs; a.nframes = (uint32_t)ph[p].size();
+            a.key = sweep_key(seed, sweep_counter, (uint32_t)p) ^ 0x73636f726564ull;
+            a.display = d_display.p; a.CW = CW; a.CH = CH;
+            a.mlp = d_mlp_dep.p; a.claim = d_sclaim.p;
+            a.gain = d_acc.p + 4 + 2 * s; a.accepted = d_acc.p + 5 + 2 * s;
+            a.err = d_err.p;
+            if (pair_off[C] > 0) {
+                prof.open(stream);
+                rc = launch_scored_sweep(a, stream);
+                if (rc) return rc;
+                prof.close(PROF_MLP, stream);
+            }
+            pofs += (uint32_t)ph[p].size();
+        }
+        ++sweep_counter;
+    }
+    std::vector<unsigned long long> acc(2 * sweeps);
+    AMG_CUDA(cudaMemcpyAsync(acc.data(), d_acc.p + 4, acc.size() * 8, cudaMemcpyDeviceToHost, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    for (size_t s = 0; s < sweeps; ++s) {
+        cost_exact -= acc[2 * s];
+        if (gains) gains[s] = acc[2 * s];
+    }
+    return check_err();
 }
 
 int Engine::publish_front() {

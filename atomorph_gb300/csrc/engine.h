@@ -214,6 +214,19 @@ class Engine {
     int set_chain_layout(const std::vector<uint64_t> &w);
     int refine_guided(size_t sweeps, uint64_t *gains);
     int refine_plain(size_t sweeps, uint64_t *gains);
+    // learned pair proposal (AM_PROPOSAL_SCORED): outcome log of the plain
+    // sweeps, per-column chain ids and claims of the scored sweeps
+    int refine_scored(size_t sweeps, uint64_t *gains);
+    int record_outcomes(size_t cap, uint32_t every);
+    bool recording_outcomes = false;
+    enum { PS_MEASURE_SCORED, PS_MEASURE_PLAIN, PS_RUN };
+    int ps_state = PS_MEASURE_SCORED, ps_left = 0;
+    bool ps_scored = true;
+    double ps_rate = 0.0;
+    uint32_t outcome_every = 1;
+    DBuf<uint32_t> d_scored_chain;
+    DBuf<unsigned long long> d_sclaim;
+    uint64_t scored_layout = UINT64_MAX;
     bool guided_on = false;                // the guided phase of the current chains has started
     // learned form: when its gate runs (learned_gate_next)
     enum { LG_MEASURE_FULL, LG_MEASURE_GATED, LG_GATED, LG_FULL };

@@ -64,6 +64,26 @@ int Engine::record_swaps(size_t cap) {
     AMG_CUDA(cudaStreamSynchronize(stream));
     rec_cap = cap;
     recording = cap > 0;
+    recording_outcomes = false;
+    return AM_OK;
+}
+
+// Makes the next plain sweeps log 1 in `every` of their proposals: pair
+// features and the exact criterion's accept (1) / reject (0), the training
+// data of the learned pair proposal.  cap 0 stops logging.
+int Engine::record_outcomes(size_t cap, uint32_t every) {
+    if (every == 0) return AM_ERR_ARG;
+    int rc = mlp_init();
+    if (rc) return rc;
+    if ((rc = d_rec_feat.reserve(std::max<size_t>(cap, 1) * kMlpIn))) return rc;
+    if ((rc = d_rec_gain.reserve(std::max<size_t>(cap, 1)))) return rc;
+    if ((rc = d_rec_count.reserve(1))) return rc;
+    AMG_CUDA(cudaMemsetAsync(d_rec_count.p, 0, 8, stream));
+    AMG_CUDA(cudaStreamSynchronize(stream));
+    rec_cap = cap;
+    recording = false;
+    recording_outcomes = cap > 0;
+    outcome_every = every;
     return AM_OK;
 }
 
@@ -102,6 +122,7 @@ int Engine::train_recorded(size_t epochs, double lr, float *loss_out) {
     const size_t n = std::min<size_t>((size_t)cnt, (size_t)rec_cap);
     if (n == 0) return AM_ERR_STATE;
     recording = false;
+    recording_outcomes = false;
     return train_device(d_rec_feat.p, d_rec_gain.p, n, epochs, lr, loss_out);
 }
 

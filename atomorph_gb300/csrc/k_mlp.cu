@@ -22,6 +22,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "sweep.cuh"
 
 namespace amg {
 namespace {
@@ -723,6 +724,105 @@ __global__ void __launch_bounds__(128, 4) k_learned_gate(LocalArgs a) {
     fwd_teardown(s);
 }
 
+// ----------------------------------------------- learned pair proposal --
+// A score as an unsigned key whose order is the float order.
+__device__ __forceinline__ uint32_t score_key(float v) {
+    const uint32_t u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Proposals: one 128-row network tile scores 32 columns x 4 candidate
+// partners (row 4c + k = candidate k of column c, drawn uniformly from the
+// column's chain without the column itself); each column claims its
+// best-scored partner on both claim words with one 64-bit atomicMax of
+// (score key, partner + 1).
+__global__ void __launch_bounds__(128, 4) k_scored_propose(ScoredArgs a) {
+    extern __shared__ __align__(1024) uint8_t smraw[];
+    FwdSmem &s = *reinterpret_cast<FwdSmem *>(smraw);
+    fwd_setup(s, a.mlp);
+    uint32_t phase = 0;
+    const uint64_t total = (uint64_t)a.nframes * a.N;
+    const uint32_t t = threadIdx.x, cand = t & 3u;
+    for (uint64_t base = (uint64_t)blockIdx.x * 32; base < total; base += (uint64_t)gridDim.x * 32) {
+        const uint64_t item = base + (t >> 2);
+        bool live = item < total;
+        uint32_t fi = 0;
+        uint64_t i = 0, j = 0;
+        float f[kMlpIn];
+#pragma unroll
+        for (int q = 0; q < kMlpIn; ++q) f[q] = 0.f;
+        if (live) {
+            fi = (uint32_t)(item / a.N);
+            i = item - (uint64_t)fi * a.N;
+            const uint32_t c = a.C == 1 ? 0u : __ldg(a.chain_id + i);
+            const uint64_t off = __ldg(a.chain_off + c), w = __ldg(a.chain_off + c + 1) - off;
+            live = w >= 2;
+            if (live) {
+                const uint64_t h = mix64(a.key ^ mix64(item * kScoredCandidates + cand));
+                const uint64_t il = i - off, jl = h % (w - 1);
+                j = off + (jl >= il ? jl + 1 : jl);
+                const uint32_t y = __ldg(a.frames + fi), yn = y + 1 == a.K ? 0 : y + 1, yp = y == 0 ? a.K - 1 : y - 1;
+                const uint64_t *Py = a.P + (uint64_t)y * a.N, *Pp = a.P + (uint64_t)yp * a.N,
+                               *Pn = a.P + (uint64_t)yn * a.N;
+                const uint64_t a1 = Py[i], a2 = Py[j], p1 = Pp[i], p2 = Pp[j], n1 = Pn[i], n2 = Pn[j];
+                pair_features(a1, a2, p1, n1, p2, n2, atom_colour(a.display, a.CW, a.CH, y, a1),
+                              atom_colour(a.display, a.CW, a.CH, y, a2), f);
+            }
+        }
+        write_features(s.A1, t, f);
+        const float score = forward_tile(s, phase, a.err);
+        uint32_t key = live ? score_key(score) : 0u;
+        uint32_t part = (uint32_t)j;
+#pragma unroll
+        for (int o = 1; o < kScoredCandidates; o <<= 1) {
+            const uint32_t k2 = __shfl_xor_sync(0xffffffffu, key, o), p2 = __shfl_xor_sync(0xffffffffu, part, o);
+            if (k2 > key || (k2 == key && p2 > part)) { key = k2; part = p2; }
+        }
+        if (live && cand == 0 && key) {
+            const uint64_t row = (uint64_t)fi * a.N;
+            atomicMax(&a.claim[row + i], ((unsigned long long)key << 32) | (unsigned long long)(part + 1u));
+            atomicMax(&a.claim[row + part], ((unsigned long long)key << 32) | (unsigned long long)(i + 1u));
+        }
+    }
+    fwd_teardown(s);
+}
+
+// Mutually claimed pairs (column i's claim names j and j's names i with the
+// same score) are disjoint; the lower column checks the reference's
+// criterion exactly and swaps.
+__global__ void __launch_bounds__(256) k_scored_apply(ScoredArgs a) {
+    const uint64_t total = (uint64_t)a.nframes * a.N;
+    unsigned long long gain = 0, acc = 0;
+    for (uint64_t item = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; item < total;
+         item += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long c = a.claim[item];
+        if (!c) continue;
+        const uint32_t fi = (uint32_t)(item / a.N);
+        const uint64_t i = item - (uint64_t)fi * a.N, row = (uint64_t)fi * a.N;
+        const uint64_t j = (uint64_t)(uint32_t)c - 1u;
+        if (j <= i) continue;
+        if (a.claim[row + j] != ((c & 0xFFFFFFFF00000000ull) | (unsigned long long)(i + 1u))) continue;
+        const uint32_t y = __ldg(a.frames + fi), yn = y + 1 == a.K ? 0 : y + 1, yp = y == 0 ? a.K - 1 : y - 1;
+        uint64_t *Py = a.P + (uint64_t)y * a.N;
+        const uint64_t *Pp = a.P + (uint64_t)yp * a.N, *Pn = a.P + (uint64_t)yn * a.N;
+        const uint64_t a1 = Py[i], a2 = Py[j], p1 = Pp[i], p2 = Pp[j], n1 = Pn[i], n2 = Pn[j];
+        const uint64_t c1 = pt_dist(p1, a1) + pt_dist(a1, n1) + pt_dist(p2, a2) + pt_dist(a2, n2);
+        const uint64_t c2 = pt_dist(p2, a1) + pt_dist(a1, n2) + pt_dist(p1, a2) + pt_dist(a2, n1);
+        if (c1 >= c2) {
+            Py[i] = a2;
+            Py[j] = a1;
+            gain += c1 - c2;
+            acc += 1;
+        }
+    }
+    gain = warp_sum_u64(gain);
+    acc = warp_sum_u64(acc);
+    if ((threadIdx.x & 31) == 0) {
+        if (gain) atomicAdd(a.gain, gain);
+        if (acc) atomicAdd(a.accepted, acc);
+    }
+}
+
 }  // namespace
 
 static int set_smem(const void *fn, size_t bytes) {
@@ -796,6 +896,26 @@ int launch_learned_phase(const LocalArgs &a, cudaStream_t s) {
     b.sel_groups = true;
     if ((rc = launch_local_propose(b, s))) return rc;
     return launch_local_apply(b, s);
+}
+
+int launch_scored_sweep(const ScoredArgs &a, cudaStream_t s) {
+    const uint64_t total = a.N * a.nframes;
+    if (!total) return AM_OK;
+    if (a.N >= 0xFFFFFFFFull) {
+        set_error("the learned pair proposal names partners as 32-bit columns: too many atoms");
+        return AM_ERR_ARG;
+    }
+    AMG_CUDA(cudaMemsetAsync(a.claim, 0, total * sizeof(unsigned long long), s));
+    // 48 KB per CTA keeps 4 CTAs on an SM: 4 x 128 TMEM columns at most
+    const size_t smem = std::max<size_t>(sizeof(FwdSmem) + 1024, 48 * 1024);
+    int rc = set_smem((const void *)k_scored_propose, smem);
+    if (rc) return rc;
+    unsigned g = (unsigned)std::min<uint64_t>((total + 31) / 32, (uint64_t)kSMs * 4);
+    AMG_LAUNCH(k_scored_propose, g, 128, smem, s, a);
+    g = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)kSMs * 8);
+    AMG_LAUNCH(k_scored_apply, g, 256, 0, s, a);
+    AMG_CUDA(cudaGetLastError());
+    return AM_OK;
 }
 
 }  // namespace amg

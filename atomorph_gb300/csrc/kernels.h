@@ -38,12 +38,45 @@ struct SweepArgs {
     uint64_t key;                // random key of this (sweep, phase)
     unsigned long long *gain;    // += exact cost decrease
     unsigned long long *accepted;
+    // Optional outcome log for the learned pair proposal: a hashed sample of
+    // 1 in log_every proposals writes its pair features ([cap][10]) and
+    // whether the exact criterion accepted it (1 or 0).
+    float *log_feat = nullptr, *log_label = nullptr;
+    unsigned long long *log_count = nullptr;
+    uint64_t log_cap = 0;
+    uint32_t log_every = 1;
+    const uint32_t *display = nullptr;  // [K][CH][CW] colours the features read
+    uint32_t CW = 0, CH = 0;
 };
 // One phase of the plain refinement: for every chain and every frame of the
 // phase, a uniformly random perfect matching of the chain's columns; each pair
 // is swapped when the reference's criterion c1 >= c2 holds
 // (thread.cpp:1014-1039).
 int launch_sweep_random(const SweepArgs &a, cudaStream_t s);
+
+// ---- the learned pair proposal (k_mlp.cu): every column of the phase's
+// frames draws kScoredCandidates random partners in its chain, the network
+// scores the pairs, each column claims its best-scored partner, and mutually
+// claimed pairs are swapped when the exact criterion holds (c1 >= c2,
+// thread.cpp:1014-1022).
+constexpr int kScoredCandidates = 4;
+struct ScoredArgs {
+    uint64_t *P;
+    uint64_t N;
+    uint32_t K, C;
+    const uint64_t *chain_off;          // [C+1]
+    const uint32_t *chain_id;           // [N] chain of each column
+    const uint32_t *frames;
+    uint32_t nframes;
+    uint64_t key;
+    const uint32_t *display;
+    uint32_t CW, CH;
+    const float *mlp;                   // deployed network
+    unsigned long long *claim;          // [nframes][N], zero on entry
+    unsigned long long *gain, *accepted;
+    int *err;
+};
+int launch_scored_sweep(const ScoredArgs &a, cudaStream_t s);
 
 // ---- k_batch.cu: many jobs' plain sweeps in one persistent launch
 struct BatchJob {

@@ -305,6 +305,9 @@ def bench_ours(args, rank, world):
     bat = None
     if rank == 0 and args.batch_jobs:
         bat = batch_bench(capi, args)
+    c4 = None
+    if rank == 0 and args.c4:
+        c4 = pair_proposal(capi, args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -337,6 +340,8 @@ def bench_ours(args, rank, world):
         res["time_to_cost"] = ttc
     if bat is not None:
         res["batch"] = bat
+    if c4 is not None:
+        res["learned_pairs_c4"] = c4
     if cpu is not None:
         res["cpu_baseline"] = cpu
     return res
@@ -476,6 +481,100 @@ def time_to_cost(capi, frames, args):
         t.close()
     for name in ("local", "learned"):
         if out[name].get("reached"):
+            out[f"speedup_{name}_vs_plain"] = round(out["plain"]["s_to_target"] / max(out[name]["s_to_target"], 1e-9), 2)
+    return out
+
+
+def _to_target(t, kind, target, B, max_s):
+    """Refines handle t with `kind` in blocks of B sweeps until its exact cost
+    is <= target (or max_s seconds); returns (sweeps, seconds, cost)."""
+    c = t.cost()
+    sweeps = 0
+    t0 = time.perf_counter()
+    while c > target and time.perf_counter() - t0 < max_s:
+        g = t.refine(B, kind)
+        sweeps += B
+        c -= int(g.sum())
+    return sweeps, time.perf_counter() - t0, c
+
+
+def pair_proposal(capi, args):
+    """The learned pair proposal on the C4 configuration.  Training: plain
+    sweeps of a seeded 256x256 job (shapes256, job 1, about 42k atoms) log
+    the outcome of every proposal (am_record_outcomes) until `--c4-samples`
+    are logged, and the network trains on them where they lie
+    (am_train_recorded).  Evaluation: a 512x512 job (shapes512, about 200k
+    atoms): plain refinement to its converged cost C (a 2000-sweep window
+    gaining < 2e-5), then every form from the same initial chains until its
+    cost is <= 1.005 C: plain, guided, and the pair proposal with the network
+    trained at 256x256 (training outside its time; its calls alternate with
+    plain sweeps by measured gain per second).  scored_block: one block of
+    scored sweeps alone from the same chains against the same number of plain
+    sweeps (cost reached, milliseconds per sweep)."""
+    from atomorph_gb300 import synth
+    out = {"train_workload": "shapes256 (job 1)", "eval_workload": "shapes512"}
+    tr = setup_morph(capi, synth.workload("shapes256", 1), 0)
+    out["train_atoms"] = tr.atoms
+    tr.record_outcomes(args.c4_samples, 1)
+    t0 = time.perf_counter()
+    sweeps = 0
+    while tr.recorded_count() < args.c4_samples:
+        tr.refine(50, capi.PROPOSAL_RANDOM)
+        sweeps += 50
+    out["log_sweeps"] = sweeps
+    out["log_s"] = round(time.perf_counter() - t0, 3)
+    f, y = tr.recorded_swaps(min(tr.recorded_count(), 1_000_000))
+    out["accept_rate_first_1M"] = round(float(y.mean()), 4)
+    t0 = time.perf_counter()
+    loss = tr.train_recorded(epochs=args.c4_epochs, lr=2e-3)
+    out["train_s"] = round(time.perf_counter() - t0, 3)
+    out["samples"] = int(min(tr.recorded_count(), args.c4_samples))
+    out["loss"] = round(float(loss), 5)
+    weights = tr.proposal_weights()
+    tr.close()
+    frames = synth.workload("shapes512")
+    m = setup_morph(capi, frames, 0)
+    w, pts0, order = m.export_chains()
+    out["eval_atoms"] = m.atoms
+    c0 = m.cost()
+    trace = [(0, 0.0, c0)]
+    sweeps, c = 0, c0
+    t0 = time.perf_counter()
+    while True:
+        g = m.refine(args.block, capi.PROPOSAL_RANDOM)
+        sweeps += args.block
+        c -= int(g.sum())
+        trace.append((sweeps, time.perf_counter() - t0, c))
+        back = next((tr_ for tr_ in reversed(trace) if tr_[0] <= sweeps - args.plain_window), None)
+        if (back is not None and back[2] - c < args.plain_conv * c) or trace[-1][1] > args.plain_max_s:
+            break
+    m.close()
+    target = 1.005 * c
+    hit = next(tr_ for tr_ in trace if tr_[2] <= target)
+    out["plain"] = {"converged_cost": int(c), "converged_sweeps": sweeps, "sweeps_to_target": hit[0],
+                    "s_to_target": round(hit[1], 4)}
+    out["initial_cost"] = int(c0)
+    out["target_cost"] = int(target)
+    for kind, name in ((capi.PROPOSAL_LOCAL, "guided"), (capi.PROPOSAL_SCORED, "pair_proposal")):
+        t = _twin(capi, frames, w, pts0, order)
+        if kind == capi.PROPOSAL_SCORED:
+            t.proposal_weights(weights)
+        sw, secs, cost = _to_target(t, kind, target, args.block, args.proposal_max_s)
+        out[name] = {"sweeps_to_target": sw, "s_to_target": round(secs, 4), "cost": int(cost),
+                     "reached": bool(cost <= target)}
+        t.close()
+    blk = {}
+    for kind, name in ((capi.PROPOSAL_SCORED, "scored"), (capi.PROPOSAL_RANDOM, "plain")):
+        t = _twin(capi, frames, w, pts0, order)
+        if kind == capi.PROPOSAL_SCORED:
+            t.proposal_weights(weights)
+        t1 = time.perf_counter()
+        g = t.refine(200, kind)
+        blk[name] = {"cost": int(c0 - int(g.sum())), "ms_per_sweep": round(1e3 * (time.perf_counter() - t1) / 200, 4)}
+        t.close()
+    out["scored_block"] = dict(blk, sweeps=200)
+    for name in ("guided", "pair_proposal"):
+        if out[name]["reached"]:
             out[f"speedup_{name}_vs_plain"] = round(out["plain"]["s_to_target"] / max(out[name]["s_to_target"], 1e-9), 2)
     return out
 
@@ -695,6 +794,9 @@ def main():
     ap.add_argument("--learned-samples", type=int, default=1_000_000)
     ap.add_argument("--learned-epochs", type=int, default=1)
     ap.add_argument("--cpu-frames", type=int, default=2)
+    ap.add_argument("--c4", type=int, default=1, help="run the learned pair proposal's C4 measurement")
+    ap.add_argument("--c4-samples", type=int, default=20_000_000)
+    ap.add_argument("--c4-epochs", type=int, default=1)
     ap.add_argument("--batch-jobs", type=int, default=32)
     ap.add_argument("--batch-sweeps", type=int, default=200)
     ap.add_argument("--fluid-frames", type=int, default=24)

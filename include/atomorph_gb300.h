@@ -59,6 +59,8 @@ extern "C" {
 #define AM_PROPOSAL_RANDOM  0  /* disjoint uniform random pairs: the plain method */
 #define AM_PROPOSAL_LOCAL   1  /* spatially local candidates, exact gain, greedy disjoint matching */
 #define AM_PROPOSAL_LEARNED 2  /* the trained MLP picks which columns run the local scan */
+#define AM_PROPOSAL_SCORED  3  /* the trained MLP ranks random partners; the best-ranked is checked exactly
+                                * (calls alternate with plain sweeps by measured cost gain per second) */
 
 typedef struct am_morph am_morph;
 
@@ -251,6 +253,18 @@ int    am_train_proposal(am_morph *m, const float *features, const float *target
  * recording sweeps left them in device memory (no copy through the host);
  * recording stops.  AM_ERR_STATE when nothing was recorded. */
 int    am_train_recorded(am_morph *m, size_t epochs, double lr, float *loss_out);
+/* Training data of the learned pair proposal (AM_PROPOSAL_SCORED): makes the
+ * next plain (AM_PROPOSAL_RANDOM) sweeps log 1 in `every` of their proposals,
+ * up to cap, as 10 pair features (position difference and distance over
+ * 16 px, colour difference of the two atoms' key-frame pixels, each column's
+ * current cost log1p(d / (16 px)^2), HAS_PIXEL parity) and the outcome of the
+ * reference's criterion c1 >= c2 (thread.cpp:1014-1022): 1 accepted, 0
+ * rejected.  am_recorded_swaps reads them (targets = outcomes) and
+ * am_train_recorded trains the network on them where they lie.  cap 0 stops.
+ * The learned gate and the pair proposal share one network: train it for
+ * the proposal kind it serves.  Until it is trained, AM_PROPOSAL_SCORED runs
+ * plain sweeps. */
+int    am_record_outcomes(am_morph *m, size_t cap, uint32_t every);
 int    am_get_proposal_weights(am_morph *m, float *w, size_t count);
 int    am_set_proposal_weights(am_morph *m, const float *w, size_t count);
 /* Scores of n feature rows, and the gradient of the mean squared error of n
