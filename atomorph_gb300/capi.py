@@ -88,6 +88,9 @@ _SIGS = {
     "am_get_blob_average": (C.c_int, [vp, C.c_size_t, C.c_size_t, C.POINTER(C.c_uint16), u8p]),
     "am_get_blob_labels": (C.c_int, [vp, C.c_size_t, i32p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "am_get_atom_count": (C.c_size_t, [vp]),
+    "am_get_blob_info": (C.c_int, [vp, C.c_size_t, C.c_size_t, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), f64p]),
+    "am_get_blob_pixels": (C.c_int, [vp, C.c_size_t, C.c_double, C.POINTER(C.c_uint16), u8p, C.c_size_t,
+                                     C.POINTER(C.c_size_t)]),
     "am_get_chain_count": (C.c_size_t, [vp]),
     "am_render": (C.c_int, [vp, C.c_double, vp, C.c_int]),
     "am_render_many": (C.c_int, [vp, f64p, C.c_size_t, vp]),
@@ -117,6 +120,7 @@ _SIGS = {
                                      C.c_size_t, u8p, u8p]),
     "am_set_fluid_sparseness": (C.c_int, [vp, C.c_double]),
     "am_get_fluid_particles": (C.c_size_t, [vp, f64p, C.c_size_t]),
+    "am_get_fluid_links": (C.c_size_t, [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_size_t]),
     "am_set_tuning": (C.c_int, [vp, C.c_char_p, C.c_double]),
     "am_batch_create": (C.c_int, [C.POINTER(vp), C.POINTER(vp), C.c_size_t]),
     "am_batch_destroy": (None, [vp]),
@@ -225,6 +229,16 @@ class Morph:
         if n:
             self.lib.am_get_fluid_particles(self.h, _p(q, f64p), n)
         return q[:n].T.copy()
+
+    def fluid_links(self):
+        """(source, destination) column of every particle's last update."""
+        n = self.lib.am_get_fluid_links(self.h, None, None, 0)
+        s = np.zeros(max(n, 1), np.uint32)
+        d = np.zeros(max(n, 1), np.uint32)
+        if n:
+            self.lib.am_get_fluid_links(self.h, s.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                        d.ctypes.data_as(C.POINTER(C.c_uint32)), n)
+        return s[:n], d[:n]
 
     def tune(self, **kw) -> "Morph":
         """Guided-refinement tunables (am_set_tuning): local_self,
@@ -339,6 +353,17 @@ class Morph:
         out = np.zeros((self.height, self.width, 4), np.uint8)
         _check(self.lib.am_render(self.h, t, out.ctypes.data, 0), "am_render")
         return out
+
+    def blob_pixels(self, blob: int, t: float):
+        """morph::get_pixels(blob, t): ([n, 2] x, y and [n, 4] RGBA) in the
+        reference's order."""
+        n = C.c_size_t()
+        _check(self.lib.am_get_blob_pixels(self.h, blob, t, None, None, 0, C.byref(n)), "am_get_blob_pixels")
+        xy = np.zeros((max(n.value, 1), 2), np.uint16)
+        rgba = np.zeros((max(n.value, 1), 4), np.uint8)
+        _check(self.lib.am_get_blob_pixels(self.h, blob, t, xy.ctypes.data_as(C.POINTER(C.c_uint16)), _p(rgba, u8p),
+                                           n.value, C.byref(n)), "am_get_blob_pixels")
+        return xy[:n.value], rgba[:n.value]
 
     def positions(self, t: float) -> np.ndarray:
         """[N, 2] position words (integer pixel * 256 + fraction byte) of every

@@ -150,6 +150,17 @@ int am_set_fluid_sparseness(am_morph *m, double v) {
     H(m).front.fluid_sparseness = v;
     return AM_OK;
 }
+size_t am_get_fluid_links(am_morph *m, uint32_t *src_col, uint32_t *dst_col, size_t cap) {
+    if (!m || !m->e.fluid || !m->e.fmorph) return 0;
+    const size_t n = m->e.fluid->n;
+    if (src_col && dst_col && cap >= n) {
+        std::vector<uint32_t> v(2 * n);
+        if (amg::fluid_morph_links(m->e.fmorph, v.data(), n, m->e.rstream) != AM_OK) return 0;
+        std::copy(v.begin(), v.begin() + n, src_col);
+        std::copy(v.begin() + n, v.end(), dst_col);
+    }
+    return n;
+}
 size_t am_get_fluid_particles(am_morph *m, double *state, size_t cap) {
     if (!m || !m->e.fluid) return 0;
     const size_t n = m->e.fluid->n;
@@ -302,6 +313,32 @@ int am_get_blob_average(const am_morph *m, size_t frame, size_t blob, uint16_t *
     const amg::Blob &b = m->e.f_blobs[i][blob];
     if (xy) { xy[0] = (uint16_t)std::round(b.x); xy[1] = (uint16_t)std::round(b.y); }
     if (rgba) store_rgba(m->e, b.r, b.g, b.b, b.a, rgba);
+    return AM_OK;
+}
+int am_get_blob_info(const am_morph *m, size_t frame, size_t blob, size_t *group, size_t *surface, double *xyrgba) {
+    if (!m) return AM_ERR_ARG;
+    const long i = frame_index(m->e, frame);
+    if (i < 0 || (size_t)i >= m->e.f_blobs.size() || blob >= m->e.f_blobs[i].size()) return AM_ERR_NOT_FOUND;
+    const amg::Blob &b = m->e.f_blobs[i][blob];
+    if (group) *group = (size_t)i < m->e.f_group.size() && blob < m->e.f_group[i].size() ? (size_t)m->e.f_group[i][blob] : 0;
+    if (surface) *surface = (size_t)b.size;
+    if (xyrgba) {
+        xyrgba[0] = b.x; xyrgba[1] = b.y; xyrgba[2] = b.r; xyrgba[3] = b.g; xyrgba[4] = b.b; xyrgba[5] = b.a;
+    }
+    return AM_OK;
+}
+int am_get_blob_pixels(am_morph *m, size_t blob, double t, uint16_t *xy, uint8_t *rgba, size_t cap, size_t *count) {
+    CHECK(m);
+    if (H(m).is_busy()) return AM_ERR_BUSY;
+    std::vector<std::pair<uint32_t, uint32_t>> px;
+    const int rc = H(m).blob_pixels(blob, t, px);
+    if (rc) return rc;
+    if (count) *count = px.size();
+    const size_t n = std::min(cap, px.size());
+    for (size_t k = 0; k < n; ++k) {
+        if (xy) { xy[2 * k] = (uint16_t)(px[k].first & 0xFFFFu); xy[2 * k + 1] = (uint16_t)(px[k].first >> 16); }
+        if (rgba) for (int c = 0; c < 4; ++c) rgba[4 * k + c] = (uint8_t)(px[k].second >> (8 * c));
+    }
     return AM_OK;
 }
 size_t am_get_atom_count(const am_morph *m) { return m ? (size_t)m->e.fN : 0; }

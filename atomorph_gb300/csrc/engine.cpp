@@ -977,6 +977,61 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
     return AM_OK;
 }
 
+// The pixels of blob `blob` of the key frame at `time` drawn alone
+// (morph::get_pixels(blob, t), morph.cpp:452-678), in the reference's order:
+// ascending position, or with a feather its outer layers one by one and then
+// the rest.  Before chains exist, the blob's own key-frame pixels.
+int Engine::blob_pixels(size_t blob, double time, std::vector<std::pair<uint32_t, uint32_t>> &out) {
+    out.clear();
+    int rc = ensure_streams(this);
+    if (rc) return rc;
+    double integ;
+    double t = std::modf(time, &integ);
+    if (t < 0.0) t += 1.0;
+    const size_t nk = frames.size();
+    if (nk == 0) return AM_ERR_NOT_FOUND;
+    const size_t f = std::min<size_t>((size_t)(t * nk), nk - 1);
+    if (f >= f_blobs.size() || blob >= f_blobs[f].size()) return AM_ERR_NOT_FOUND;
+    if (fN == 0 || fK == 0) {
+        const size_t fr = (size_t)CW * CH;
+        if (!d_labels.p || d_labels.n < (f + 1) * fr) return AM_ERR_STATE;
+        std::vector<int32_t> lab(fr);
+        std::vector<uint32_t> disp(fr);
+        AMG_CUDA(cudaMemcpy(lab.data(), d_labels.p + f * fr, fr * 4, cudaMemcpyDeviceToHost));
+        AMG_CUDA(cudaMemcpy(disp.data(), d_display.p + f * fr, fr * 4, cudaMemcpyDeviceToHost));
+        for (size_t q = 0; q < fr; ++q)
+            if (lab[q] == (int32_t)blob) out.emplace_back((uint32_t)((q / CW) << 16 | (q % CW)), disp[q]);
+        return AM_OK;
+    }
+    const size_t npx = (size_t)width * height;
+    if (npx == 0) return AM_OK;
+    if ((rc = d_frame.reserve(npx * 4))) return rc;
+    if ((rc = d_aux.reserve(npx))) return rc;
+    RenderScene sc;
+    sc.K = fK; sc.C = fC; sc.N = fN; sc.CW = CW; sc.CH = CH; sc.width = width; sc.height = height;
+    sc.bbox[0] = bbox_x1; sc.bbox[1] = bbox_y1; sc.bbox[2] = bbox_x2; sc.bbox[3] = bbox_y2;
+    sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
+    sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
+    sc.motion_noise = front.motion_noise;
+    render_options(sc);
+    sc.pipeline = 0;
+    sc.only_rank = (uint32_t)blob;
+    sc.aux = d_aux.p;
+    const uint64_t key = f < f_keys.size() ? f_keys[f] : 0;
+    if ((rc = render_frame(rw, sc, t, key, d_frame.p, rstream))) return rc;
+    std::vector<uint32_t> rgba(npx);
+    std::vector<uint8_t> aux(npx);
+    AMG_CUDA(cudaMemcpyAsync(rgba.data(), d_frame.p, npx * 4, cudaMemcpyDeviceToHost, rstream));
+    AMG_CUDA(cudaMemcpyAsync(aux.data(), d_aux.p, npx, cudaMemcpyDeviceToHost, rstream));
+    AMG_CUDA(cudaStreamSynchronize(rstream));
+    const uint32_t F = sc.feather;
+    for (uint32_t code = 1; code <= F + 1; ++code)
+        for (size_t q = 0; q < npx; ++q)
+            if (aux[q] == code || (F == 0 && aux[q]))
+                out.emplace_back((uint32_t)((q / width) << 16 | (q % width)), rgba[q]);
+    return AM_OK;
+}
+
 // Every atom's position at time `time` as the render places it (host xy,
 // 2 words per atom column); returns the atom count.
 int Engine::positions(double time, int32_t *xy, size_t cap, size_t *count) {

@@ -209,6 +209,9 @@ class Engine {
     int render_many_host(const double *ts, size_t n, uint8_t *out);
     int positions(double time, int32_t *xy, size_t cap, size_t *count);
     DBuf<int32_t> d_pos;                   // position readout
+    // morph::get_pixels(blob, t): (y << 16 | x, RGBA) in the reference's order
+    int blob_pixels(size_t blob, double time, std::vector<std::pair<uint32_t, uint32_t>> &out);
+    DBuf<uint8_t> d_aux;                   // per-pixel layer codes of a blob drawn alone
     int import_chains(size_t K, size_t C, const uint64_t *w, const uint64_t *pts, const int32_t *order);
     int export_chains(uint64_t *w, uint64_t *pts, int32_t *order);
     int set_chain_layout(const std::vector<uint64_t> &w);

@@ -69,6 +69,7 @@ struct FluidMorph {
     uint32_t *col[2] = {nullptr, nullptr};  // [out_w*out_h] fluid colours (feather / background passes)
     uint8_t *mem[2] = {nullptr, nullptr};   // [out_w*out_h] 1 where the fluid image has the pixel
     uint64_t frames = 0;             // frames stepped (random key)
+    uint32_t *link = nullptr;        // [2][n] source and destination column of each particle's last update
 };
 
 // draw_fluid options: feather layers, keep_background (the background from
@@ -379,6 +380,8 @@ __global__ void k_fm_update(FmArgs a) {
         const float gy = fminf(fmaxf(pty * a.sp + 10.f, 1.f), (float)a.height * a.sp + 10.f);
         PF_(PGX, s) = gx;
         PF_(PGY, s) = gy;
+        a.m.link[s] = (uint32_t)src_x;
+        a.m.link[a.N + s] = (uint32_t)dst_x;
         const float R = (float)(col & 255u) / 255.f, G = (float)((col >> 8) & 255u) / 255.f,
                     B = (float)((col >> 16) & 255u) / 255.f, A = (float)(col >> 24) / 255.f;
         PF_(PR_, s) = R; PF_(PG_, s) = G; PF_(PB_, s) = B; PF_(PA_, s) = A;
@@ -573,10 +576,20 @@ void fluid_morph_destroy(FluidMorph *m) {
     void *ps[] = {m->frame_key, m->src_pos, m->dst_pos, m->owner, m->src_map, m->dst_map, m->src_cnt, m->dst_cnt,
                   m->src_any, m->flags_a, m->flags_b, m->slot_by_rank, m->ckeys, m->cvals, m->tk, m->tv, m->hist,
                   m->chain_cnt, m->to_create, m->to_delete, m->phase1, m->ncand, m->acc, m->col[0], m->col[1],
-                  m->mem[0], m->mem[1]};
+                  m->mem[0], m->mem[1], m->link};
     for (void *p : ps)
         if (p) cudaFree(p);
     delete m;
+}
+
+// The source and destination column each particle's last update read
+// (update_particle's src_x after the growing-area rule and dst_x,
+// morph.cpp:687-695), n particles: out[0..n) sources, out[n..2n) destinations.
+int fluid_morph_links(FluidMorph *m, uint32_t *out, size_t n, cudaStream_t s) {
+    if (!m || !m->link || n != m->n) return AM_ERR_STATE;
+    AMG_CUDA(cudaMemcpyAsync(out, m->link, 2 * n * 4, cudaMemcpyDeviceToHost, s));
+    AMG_CUDA(cudaStreamSynchronize(s));
+    return AM_OK;
 }
 
 int fluid_draw(FluidDev *fl, unsigned long long *acc, uint32_t width, uint32_t height, double sparseness,
@@ -694,7 +707,8 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
                   {(void **)&m->chain_cnt, (size_t)sc.C * 4}, {(void **)&m->to_create, (size_t)sc.C * 4},
                   {(void **)&m->to_delete, (size_t)sc.C * 4}, {(void **)&m->phase1, (size_t)sc.C * 4},
                   {(void **)&m->ncand, 4}, {(void **)&m->acc, npx * 40}, {(void **)&m->col[0], npx * 4},
-                  {(void **)&m->col[1], npx * 4}, {(void **)&m->mem[0], npx}, {(void **)&m->mem[1], npx}};
+                  {(void **)&m->col[1], npx * 4}, {(void **)&m->mem[0], npx}, {(void **)&m->mem[1], npx},
+                  {(void **)&m->link, N * 8}};
         bool fresh = m->n != N || m->C != sc.C || m->cw != sc.CW || m->ch != sc.CH || m->out_w != sc.width ||
                      m->out_h != sc.height;
         if (fresh) {

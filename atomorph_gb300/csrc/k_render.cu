@@ -820,6 +820,8 @@ struct ResolveOpts {
     const uint32_t *rank_col;      // [C] colour of the rank-b blob of the pair's first key frame
     uint32_t tiles_y;
     BgArgs bg;                     // the background under the composite
+    uint32_t only_rank;            // one blob alone (0xFFFFFFFF: the composite of all)
+    uint8_t *aux;                  //   and its per-pixel coverage / feather layer code
 };
 
 // Where a frame's binned records are: tile t's region starts at off[t] and
@@ -856,6 +858,12 @@ __device__ __forceinline__ void visit_tile(const TileRecs &r, uint32_t t, F &&f)
 // of the (2R + 1) x 32 px square window; erosion runs on the bitmap.  Pixels
 // outside the window count as outside the blob: every tile pixel is more
 // than 32 R >= feather pixels from them, so no layer below feather changes.
+// The composite rank a record takes part in: its own, or none when one other
+// blob is drawn alone.
+__device__ __forceinline__ uint32_t rank_of(const ResolveOpts &o, const uint4 &s) {
+    return (o.only_rank == 0xFFFFFFFFu || s.w == o.only_rank) ? s.w : 0xFFFFFFFFu;
+}
+
 __device__ __noinline__ void feather_layers(const TileRecs &tr, uint32_t tiles_x, uint32_t tiles_y, uint32_t tile,
                                             uint32_t cur, uint32_t F, uint32_t *bm, uint8_t *layer) {
     const int R = (int)((F + 31) / 32), WW = 2 * R + 1, WH = 32 * WW, nw = WW * WH;
@@ -951,6 +959,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
     // consecutive output pixels
     int n[4];
     uint32_t c0[4];
+    uint8_t lay[4] = {0, 0, 0, 0};  // one blob alone: 1 + feather layer of each pixel it reaches
     double st[4][4];  // FP64 "over" state (R, G, B, A) of pixels with 2+ blobs; local memory, rarely touched
     // density 1: a pixel's alpha needs no count, so the packed mode keeps
     // five sums per pixel and checks the weight sum instead of the count
@@ -965,7 +974,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                 for (uint32_t j = threadIdx.x; j < nmain; j += 256) {
                     const uint4 v = rec[beg + j];
                     cache[j] = v;
-                    mn = min(mn, v.w);
+                    mn = min(mn, rank_of(o, v));
                 }
                 if (novf) {
                     if (threadIdx.x == 0) s_nov = nmain;
@@ -974,7 +983,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                         const uint4 v = tr.ovf[j];
                         if (ovf_tile(v) != tile) continue;
                         cache[atomicAdd(&s_nov, 1u)] = v;
-                        mn = min(mn, v.w);
+                        mn = min(mn, rank_of(o, v));
                     }
                 }
             }
@@ -985,7 +994,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
         if (threadIdx.x == 0) s_over = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; }
-        if (!cached) visit_tile(tr, tile, [&](const uint4 &v) { mn = min(mn, v.w); });
+        if (!cached) visit_tile(tr, tile, [&](const uint4 &v) { mn = min(mn, rank_of(o, v)); });
         for (int w = 16; w; w >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, w));
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
         __syncthreads();
@@ -1009,7 +1018,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                     if (ovf_tile(s) != tile) continue;
                 }
                 if (s.w != cur) {
-                    if (s.w > cur) nxt = min(nxt, s.w);
+                    if (s.w > cur) nxt = min(nxt, rank_of(o, s));
                     continue;
                 }
                 uint32_t px = s.x & 0xFFFFu, py = s.x >> 16;
@@ -1094,6 +1103,13 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                     a = (uint32_t)(int)round(__dmul_rn((double)a, __ddiv_rn((double)(flayer[li] + 1),
                                                                              (double)(o.feather + 1))));
                 uint32_t cc = r | (g << 8) | (b << 16) | (a << 24);
+                if (o.only_rank != 0xFFFFFFFFu) {
+                    // one blob alone: every pixel it reaches, transparent ones too
+                    n[q] = 1;
+                    c0[q] = cc;
+                    lay[q] = feathered ? (uint8_t)(flayer[li] + 1) : (uint8_t)1;
+                    continue;
+                }
                 if (o.show_blobs != AM_TEXTURE) cc = o.rank_col[cur];
                 if ((cc >> 24) == 0) continue;  // draw_atoms skips transparent blob pixels
                 if (n[q] == 0) c0[q] = cc;
@@ -1116,6 +1132,7 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
         if (o.keep_bg) px = over_background(n[q], c0[q], st[q], bg_colour(o.bg, gx, gy));
         else px = n[q] == 0 ? 0u : (n[q] == 1 ? c0[q] : over_bytes(st[q]));
         reinterpret_cast<uint32_t *>(out)[(size_t)gy * width + gx] = px;
+        if (o.aux) o.aux[(size_t)gy * width + gx] = lay[q];
     }
 }
 
@@ -1429,6 +1446,12 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     o.keep_bg = sc.keep_background && sc.present;
     o.tiles_y = tiles_y;
     o.bg = bg_args(sc, (uint32_t)f, t);
+    o.only_rank = sc.only_rank;
+    o.aux = sc.aux;
+    if (sc.only_rank != 0xFFFFFFFFu) {
+        o.show_blobs = AM_TEXTURE;
+        o.keep_bg = 0;
+    }
     if (w->prof) w->prof->open(s);
     {
         static const cudaError_t attr = cudaFuncSetAttribute(

@@ -261,6 +261,12 @@ struct RenderScene {
     const uint32_t *blob_col = nullptr; // [K][C] AVERAGE / DISTINCT colour (RGB) of the b-th blob of frame k
     const int *perm = nullptr;          // [2][512] Perlin permutations (lag, slope) for the background
     double motion_noise = 0.0;          // Perlin motion perturbation amplitude in px (0: off)
+    // One blob alone (morph::get_pixels(blob, t), morph.cpp:452-678): only
+    // records of this composite rank are drawn, every pixel they reach keeps
+    // its mean colour (alpha 0 included) and aux[pixel] gets 1 + its feather
+    // layer (feather + 1 inside, 0 where the blob has no pixel).
+    uint32_t only_rank = 0xFFFFFFFFu;
+    uint8_t *aux = nullptr;             // device, width * height
 };
 // Largest feather the frame render supports (three 32-px tile rings).
 constexpr uint32_t kMaxFeather = 96;
@@ -299,6 +305,9 @@ FluidDev *fluid_create(uint32_t gsx, uint32_t gsy, uint32_t n);
 void fluid_destroy(FluidDev *f);
 int fluid_set(FluidDev *f, const double *state, cudaStream_t s);  // n x 18 doubles (oracle order)
 int fluid_get(FluidDev *f, double *state, cudaStream_t s);
+struct FluidMorph;
+// Source and destination columns of every particle's last update (host, 2n).
+int fluid_morph_links(FluidMorph *m, uint32_t *out, size_t n, cudaStream_t s);
 int fluid_step(FluidDev *f, uint64_t steps_left, double freedom_radius, cudaStream_t s, Prof *prof);
 // nsteps steps; step k runs with steps_left = last_steps_left + (nsteps - 1 - k).
 int fluid_run(FluidDev *f, uint32_t nsteps, uint64_t last_steps_left, double freedom_radius, cudaStream_t s,

@@ -132,6 +132,12 @@ int am_set_fluid_sparseness(am_morph *m, double s);
 /* The morph's fluid particles (fields as am_fluid_get_particles) after the
  * last fluid frame; returns the particle count, writes when cap >= it. */
 size_t am_get_fluid_particles(am_morph *m, double *state, size_t cap);
+/* The columns each particle's last update_particle read (morph.cpp:687-695):
+ * its source column (after the growing-area rule) and destination column,
+ * whose trajectory and colours gave its gravity target and ideal colour;
+ * meaningful for the active particles.  Returns the particle count, writes
+ * when cap >= it. */
+size_t am_get_fluid_links(am_morph *m, uint32_t *src_col, uint32_t *dst_col, size_t cap);
 /* Guided-refinement tunables (the autotuner sets these): "local_self",
  * "local_target", "local_random" (candidates per column from the column's own
  * neighbourhood, its target cell, and uniform random columns),
@@ -191,6 +197,23 @@ int      am_get_average_pixel(const am_morph *m, size_t frame, uint16_t *xy, uin
 int      am_get_blob_labels(am_morph *m, size_t frame, int32_t *labels, uint32_t *w, uint32_t *h);
 /* morph::get_average_pixel(f, b) morph.cpp:356-376. */
 int      am_get_blob_average(const am_morph *m, size_t frame, size_t blob, uint16_t *xy, uint8_t *rgba);
+/* morph::get_blob(f, b) (morph.h:40; blob, atomorph.h:256-263) as values:
+ * the blob's group (its chain), surface size and means x, y, r, g, b, a
+ * (colours in the stored colour space, 0..1).  AM_ERR_NOT_FOUND when the
+ * frame or blob does not exist. */
+int      am_get_blob_info(const am_morph *m, size_t frame, size_t blob, size_t *group, size_t *surface,
+                          double *xyrgba);
+/* morph::get_pixels(blob, t, to) (morph.h:29, morph.cpp:452-678): the pixels
+ * of the blob-th blob of the key frame at time t drawn alone, every pixel its
+ * atoms reach with its mean colour (transparent ones included), in the
+ * reference's order (ascending position y * 65536 + x; with a feather the
+ * outer layers first, layer by layer, then the rest).  Before chains exist,
+ * the blob's own key-frame pixels.  xy (2 per pixel) and rgba (4 per pixel)
+ * receive up to cap pixels, *count the number; pixels outside the morph's
+ * resolution are not returned.  AM_ERR_NOT_FOUND when the blob does not
+ * exist, AM_ERR_BUSY while the worker runs. */
+int      am_get_blob_pixels(am_morph *m, size_t blob, double t, uint16_t *xy, uint8_t *rgba, size_t cap,
+                            size_t *count);
 size_t   am_get_atom_count(const am_morph *m);                /* total chain width (atoms per key frame) */
 size_t   am_get_chain_count(const am_morph *m);               /* chains = blob groups */
 

@@ -8,16 +8,21 @@
 // synchronize() returns false while busy (morph.cpp:103), getters return 0 or
 // an all-zero pixel for missing frames/blobs.  get_energy() returns the true
 // atom cost (the reference's running value for atoms is not maintained
-// correctly, thread.cpp:869-870).  Blob surfaces (get_blob) are not exposed:
-// the GPU keeps blobs as labels in device memory; use get_blob_count and
-// get_average_pixel(frame, blob).
+// correctly, thread.cpp:869-870).  get_blob returns a blob the class builds
+// from the GPU's blob labels and descriptors (surface positions, 4-connected
+// border, group, means); like the reference's pointer it stays valid until
+// the next synchronize() or clear().  Blob means are exact means (the
+// reference keeps running means, which can differ in the last bits).
 #ifndef ATOMORPH_GB300_HPP
 #define ATOMORPH_GB300_HPP
 
 #include <cstddef>
 #include <cstdint>
 #include <iostream>  // callers of the reference rely on its header pulling in the iostreams
+#include <map>
+#include <set>
 #include <stdexcept>
+#include <utility>
 #include <vector>
 
 #include "atomorph_gb300.h"
@@ -71,6 +76,16 @@ typedef union key_point {
     uint64_t word;
 } point;
 
+// atomorph.h:256-263
+typedef struct blob {
+    size_t index;              // position in the key frame's blob vector
+    std::set<size_t> surface;  // pixel positions y * 65536 + x of the blob
+    std::set<size_t> border;   // 4-neighbours of the surface outside it
+    size_t group = 0;          // the chain (blob group) the blob belongs to
+    bool unified = false;      // a volatile (empty) blob added by matching
+    double x, y, r, g, b, a;   // means; colours in the stored colour space, 0..1
+} blob;
+
 inline size_t get_warning() {
     size_t flags = 0;
     if (sizeof(void *) < 8) flags |= WARN_POINTER_SIZE;
@@ -89,7 +104,10 @@ class morph {
     morph(const morph &) = delete;
     morph &operator=(const morph &) = delete;
 
-    void clear() { am_clear(h_); }
+    void clear() {
+        blobs_.clear();
+        am_clear(h_);
+    }
     bool add_pixel(size_t frame, pixel px) {
         return am_add_pixel(h_, frame, px.x, px.y, px.c.r, px.c.g, px.c.b, px.c.a) == AM_OK;
     }
@@ -126,6 +144,49 @@ class morph {
             to->push_back(create_pixel((uint16_t)(i % w), (uint16_t)(i / w), rgba[4 * i], rgba[4 * i + 1],
                                        rgba[4 * i + 2], rgba[4 * i + 3]));
     }
+    // morph::get_pixels(blob, t, to) (morph.cpp:452-678): the blob-th blob of
+    // the key frame at t drawn alone, appended to *to in the reference's
+    // order; returns the blob, or nullptr when it does not exist.
+    const blob *get_pixels(size_t blob_index, double t, std::vector<pixel> *to) {
+        size_t n = 0;
+        if (am_get_blob_pixels(h_, blob_index, t, nullptr, nullptr, 0, &n) != AM_OK) return nullptr;
+        std::vector<uint16_t> xy(2 * n + 2);
+        std::vector<uint8_t> c(4 * n + 4);
+        if (am_get_blob_pixels(h_, blob_index, t, xy.data(), c.data(), n, &n) != AM_OK) return nullptr;
+        for (size_t i = 0; i < n; ++i)
+            to->push_back(create_pixel(xy[2 * i], xy[2 * i + 1], c[4 * i], c[4 * i + 1], c[4 * i + 2], c[4 * i + 3]));
+        return get_blob(get_frame_key(t), blob_index);
+    }
+    // morph::get_blob(f, b) (morph.h:40): nullptr when it does not exist.
+    const blob *get_blob(size_t f, size_t b) {
+        auto key = std::make_pair(f, b);
+        auto it = blobs_.find(key);
+        if (it != blobs_.end()) return &it->second;
+        size_t group = 0, surface = 0;
+        double v[6];
+        if (am_get_blob_info(h_, f, b, &group, &surface, v) != AM_OK) return nullptr;
+        am::blob bl;
+        bl.index = b;
+        bl.group = group;
+        bl.unified = surface == 0;
+        bl.x = v[0]; bl.y = v[1]; bl.r = v[2]; bl.g = v[3]; bl.b = v[4]; bl.a = v[5];
+        uint32_t w = 0, h = 0;
+        if (surface && am_get_blob_labels(h_, f, nullptr, &w, &h) == AM_OK && w && h) {
+            std::vector<int32_t> lab((size_t)w * h);
+            if (am_get_blob_labels(h_, f, lab.data(), nullptr, nullptr) == AM_OK) {
+                for (size_t q = 0; q < lab.size(); ++q)
+                    if (lab[q] == (int32_t)b) bl.surface.insert(xy2pos((uint16_t)(q % w), (uint16_t)(q / w)));
+                for (size_t p : bl.surface) {
+                    const uint16_t x = (uint16_t)(p % (UINT16_MAX + 1)), y = (uint16_t)(p / (UINT16_MAX + 1));
+                    const size_t nb[4] = {x > 0 ? xy2pos(x - 1, y) : SIZE_MAX, x < UINT16_MAX ? xy2pos(x + 1, y) : SIZE_MAX,
+                                          y > 0 ? xy2pos(x, y - 1) : SIZE_MAX, y < UINT16_MAX ? xy2pos(x, y + 1) : SIZE_MAX};
+                    for (size_t q : nb)
+                        if (q != SIZE_MAX && !bl.surface.count(q)) bl.border.insert(q);
+                }
+            }
+        }
+        return &blobs_.emplace(key, std::move(bl)).first->second;
+    }
     // The same frame straight into an RGBA8 buffer (host, or device when on_device).
     bool get_frame(double t, uint8_t *rgba, bool on_device = false) {
         return am_render(h_, t, rgba, on_device ? 1 : 0) == AM_OK;
@@ -145,7 +206,11 @@ class morph {
     void suspend() { am_suspend(h_); }
     bool suspend(double timeout) { return am_suspend_timeout(h_, timeout) == AM_OK; }
     bool is_busy() const { return am_is_busy(h_) != 0; }
-    bool synchronize() { return am_synchronize(h_) == AM_OK; }
+    bool synchronize() {
+        if (am_synchronize(h_) != AM_OK) return false;
+        blobs_.clear();  // blobs returned by get_blob are valid until here
+        return true;
+    }
 
     void set_blob_delimiter(unsigned char d) { am_set_blob_delimiter(h_, d); }
     void set_blob_threshold(double t) { am_set_blob_threshold(h_, t); }
@@ -177,6 +242,7 @@ class morph {
 
   private:
     am_morph *h_ = nullptr;
+    std::map<std::pair<size_t, size_t>, am::blob> blobs_;
 };
 
 }  // namespace am

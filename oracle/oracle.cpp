@@ -454,42 +454,61 @@ inline Col ramp_col(Col c1, Col c2, double lag, double slope, double str) {
 // NONE the first point) plus the motion perturbation when it is on (FP64
 // noise when fp64, for the accuracy comparison).  col = the atom's column in
 // the frame-major point array.
+// morph::interpolate(point, point, w) (morph.cpp:1501-1515) at w = 1 - t.
+Pt lin_point(Pt pt1, Pt pt2, double t) {
+    Pt pt = pt1;
+    double w1 = 1.0 - t;
+    double x1 = (double(256) * pt1.x + pt1.xf), y1 = (double(256) * pt1.y + pt1.yf);
+    double x2 = (double(256) * pt2.x + pt2.xf), y2 = (double(256) * pt2.y + pt2.yf);
+    double xx = (w1 * x1 + (1.0 - w1) * x2), yy = (w1 * y1 + (1.0 - w1) * y2);
+    pt.x = (uint16_t)(xx / double(256)); pt.xf = (uint8_t)(xx - (pt.x * 256));
+    pt.y = (uint16_t)(yy / double(256)); pt.yf = (uint8_t)(yy - (pt.y * 256));
+    return pt;
+}
+// The cyclic spline of column col through every key frame at global time
+// (morph.cpp:526-531, spline.cpp:45-57), split as the reference splits it.
+Pt spline_point(const orc_scene &s, uint64_t N, uint64_t col, double time, Pt pt, std::vector<double> &sx,
+                std::vector<double> &sy) {
+    const uint32_t h = s.K;
+    for (uint32_t j = 0; j < h; ++j) {
+        Pt q = unpack(s.pts[(uint64_t)j * N + col]);
+        sx[j] = q.x + q.xf / double(256);
+        sy[j] = q.y + q.yf / double(256);
+    }
+    double vx, vy, ix, iy;
+    spline_eval(sx.data(), sy.data(), (int)h, time, &vx, &vy);
+    double fx = std::modf(vx, &ix), fy = std::modf(vy, &iy);
+    // double -> uint16/uint8 as the x86 build converts: via int.
+    pt.x = (uint16_t)(int)ix; pt.xf = (uint8_t)(int)std::round(fx * 255);
+    pt.y = (uint16_t)(int)iy; pt.yf = (uint8_t)(int)std::round(fy * 255);
+    return pt;
+}
+// pt displaced by the motion perturbation of an atom whose pair's first
+// point is pt1 (FP64 noise when fp64).
+Pt perturbed(const orc_scene &s, const NoiseMaps &nm, Pt pt, Pt pt1, double t, bool fp64) {
+    if (!(s.motion_noise > 0.0)) return pt;
+    int32_t dx, dy;
+    motion_offset(nm.mx, nm.my, nm.mx64, nm.my64, s.bbox, s.motion_noise, t, pt1, fp64, &dx, &dy);
+    const int32_t X = displaced((int32_t)pt.x * 256 + pt.xf, dx), Y = displaced((int32_t)pt.y * 256 + pt.yf, dy);
+    pt.x = (uint16_t)(X >> 8); pt.xf = (uint8_t)(X & 255);
+    pt.y = (uint16_t)(Y >> 8); pt.yf = (uint8_t)(Y & 255);
+    return pt;
+}
+
+// The atom's point at local time t of pair y (global time `time`): the
+// motion's position (LINEAR morph.cpp:1501-1515, SPLINE morph.cpp:526-531,
+// NONE the first point) plus the motion perturbation when it is on (FP64
+// noise when fp64, for the accuracy comparison).  col = the atom's column in
+// the frame-major point array.
 Pt atom_point(const orc_scene &s, const NoiseMaps &nm, uint32_t y, uint64_t N, uint64_t col, double t, double time,
               bool fp64, std::vector<double> &sx, std::vector<double> &sy) {
-    const uint32_t h = s.K, yn = (y + 1) % h;
+    const uint32_t yn = (y + 1) % s.K;
     const Pt pt1 = unpack(s.pts[(uint64_t)y * N + col]);
     const Pt pt2 = unpack(s.pts[(uint64_t)yn * N + col]);
     Pt pt = pt1;
-    if (s.motion == LINEAR) {
-        // morph::interpolate(point, point, w), morph.cpp:1501-1515.
-        double w1 = 1.0 - t;
-        double x1 = (double(256) * pt1.x + pt1.xf), y1 = (double(256) * pt1.y + pt1.yf);
-        double x2 = (double(256) * pt2.x + pt2.xf), y2 = (double(256) * pt2.y + pt2.yf);
-        double xx = (w1 * x1 + (1.0 - w1) * x2), yy = (w1 * y1 + (1.0 - w1) * y2);
-        pt.x = (uint16_t)(xx / double(256)); pt.xf = (uint8_t)(xx - (pt.x * 256));
-        pt.y = (uint16_t)(yy / double(256)); pt.yf = (uint8_t)(yy - (pt.y * 256));
-    } else if (s.motion == SPLINE) {
-        // Spline through all key frames at global time, morph.cpp:526-531.
-        for (uint32_t j = 0; j < h; ++j) {
-            Pt q = unpack(s.pts[(uint64_t)j * N + col]);
-            sx[j] = q.x + q.xf / double(256);
-            sy[j] = q.y + q.yf / double(256);
-        }
-        double vx, vy, ix, iy;
-        spline_eval(sx.data(), sy.data(), (int)h, time, &vx, &vy);
-        double fx = std::modf(vx, &ix), fy = std::modf(vy, &iy);
-        // double -> uint16/uint8 as the x86 build converts: via int.
-        pt.x = (uint16_t)(int)ix; pt.xf = (uint8_t)(int)std::round(fx * 255);
-        pt.y = (uint16_t)(int)iy; pt.yf = (uint8_t)(int)std::round(fy * 255);
-    }
-    if (s.motion_noise > 0.0) {
-        int32_t dx, dy;
-        motion_offset(nm.mx, nm.my, nm.mx64, nm.my64, s.bbox, s.motion_noise, t, pt1, fp64, &dx, &dy);
-        const int32_t X = displaced((int32_t)pt.x * 256 + pt.xf, dx), Y = displaced((int32_t)pt.y * 256 + pt.yf, dy);
-        pt.x = (uint16_t)(X >> 8); pt.xf = (uint8_t)(X & 255);
-        pt.y = (uint16_t)(Y >> 8); pt.yf = (uint8_t)(Y & 255);
-    }
-    return pt;
+    if (s.motion == LINEAR) pt = lin_point(pt1, pt2, t);
+    else if (s.motion == SPLINE) pt = spline_point(s, N, col, time, pt1, sx, sy);
+    return perturbed(s, nm, pt, pt1, t, fp64);
 }
 
 // Per-blob pixel list at local time t (morph.cpp:452-623, feather 0).
@@ -774,6 +793,95 @@ void orc_positions(const orc_scene *sp, double time_in, int fp64, int32_t *xy) {
         const Pt pt = atom_point(s, nm, y, N, col, t, time, fp64 != 0, sx, sy);
         xy[2 * col] = (int32_t)pt.x * 256 + pt.xf;
         xy[2 * col + 1] = (int32_t)pt.y * 256 + pt.yf;
+    }
+}
+
+// morph::get_pixels(blob, t, to) (morph.cpp:452-678) of the blob-th blob of
+// the key frame at time t (global time, as orc_render takes it): up to cap
+// pixels into xy / rgba in the reference's order; returns the list's length
+// (SIZE_MAX when the blob does not exist).
+size_t orc_blob_pixels(const orc_scene *sp, size_t blob, double time_in, uint16_t *xy, uint8_t *rgba, size_t cap) {
+    const orc_scene &s = *sp;
+    if (s.K == 0 || s.C == 0 || blob >= s.C) return SIZE_MAX;
+    double integ;
+    double time = std::modf(time_in, &integ);
+    if (time < 0.0) time += 1.0;
+    const size_t f = std::min<size_t>((size_t)(time * s.K), s.K - 1);
+    const double dt = 1.0 / double(s.K);
+    const double t = std::max(0.0, (time - (double)(s.frame_keys[f] * dt)) / dt);
+    Perlin lag(s.seed), slope(s.seed + 1);
+    const NoiseMaps nm(s.seed);
+    std::vector<Px> pix;
+    blob_pixels(s, lag, slope, nm, (uint32_t)s.blob_order[f * s.C + blob], (uint32_t)f, t, time, pix);
+    for (size_t i = 0; i < pix.size() && i < cap; ++i) {
+        xy[2 * i] = pix[i].x;
+        xy[2 * i + 1] = pix[i].y;
+        rgba[4 * i] = pix[i].c.r; rgba[4 * i + 1] = pix[i].c.g; rgba[4 * i + 2] = pix[i].c.b; rgba[4 * i + 3] = pix[i].c.a;
+    }
+    return pix.size();
+}
+
+// update_particle's gravity target and ideal colour (morph.cpp:697-767,
+// TEXTURE blobs) of n particles of the fluid frame at time `time` (global),
+// given the source and destination column each one read (src_x after the
+// growing-area rule, dst_x) and the surfaces s0, s1 of its chain's blobs at
+// the pair's two key frames: out[6 i ..] = gravity x, y in grid units
+// (sparseness grid units per pixel, 10 of margin), R, G, B, A in 0..1.
+void orc_fluid_targets(const orc_scene *sp, double time_in, double sparseness, uint32_t n, const uint32_t *src,
+                       const uint32_t *dst, const double *s0, const double *s1, double *out) {
+    const orc_scene &s = *sp;
+    uint64_t N = 0;
+    for (uint32_t c = 0; c < s.C; ++c) N += s.widths[c];
+    double integ;
+    double time = std::modf(time_in, &integ);
+    if (time < 0.0) time += 1.0;
+    const size_t f = std::min<size_t>((size_t)(time * s.K), s.K - 1);
+    const double dt = 1.0 / double(s.K);
+    const double t = std::max(0.0, (time - (double)(s.frame_keys[f] * dt)) / dt);
+    const uint32_t y = (uint32_t)f, yn = (y + 1) % s.K;
+    Perlin lag_map(s.seed), slope_map(s.seed + 1);
+    const NoiseMaps nm(s.seed);
+    std::vector<double> sx(s.K), sy(s.K);
+    const double bx1 = s.bbox[0], by1 = s.bbox[1], bw = s.bbox[2] - s.bbox[0] + 1.0, bh = s.bbox[3] - s.bbox[1] + 1.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const Pt pt1 = unpack(s.pts[(uint64_t)y * N + src[i]]), pt2 = unpack(s.pts[(uint64_t)yn * N + dst[i]]);
+        const bool h1 = pt1.flags & HAS_PIXEL, h2 = pt2.flags & HAS_PIXEL;
+        Col c1, c2;
+        if (h1 && !h2) {
+            c1 = read_pixel(s, y, pt1.x, pt1.y);
+            c2 = c1;
+            if (s1[i] > 0.0) c2.a = 0;
+        } else if (h2 && !h1) {
+            c2 = read_pixel(s, yn, pt2.x, pt2.y);
+            c1 = c2;
+            if (s0[i] > 0.0) c1.a = 0;
+        } else {
+            c1 = read_pixel(s, y, pt1.x, pt1.y);
+            c2 = read_pixel(s, yn, pt2.x, pt2.y);
+        }
+        Col c;
+        if (s.fading == PERLIN) {
+            const double px = (((pt1.x - bx1) * 256 + pt1.xf) / double(bw * 256)) * 8.0;
+            const double py = (((pt1.y - by1) * 256 + pt1.yf) / double(bh * 256)) * 8.0;
+            c = ramp_col(c1, c2, lag_map.octave(px, py, 8) * 0.5 + 0.5, slope_map.octave(px, py, 8) * 0.5 + 0.5, 1.0 - t);
+        } else if (s.fading == COSINE) {
+            c = ramp_col(c1, c2, 0.5, 0.5, 1.0 - t);
+        } else {
+            c = lerp_col(c1, c2, 1.0 - t);
+        }
+        Pt pt = pt1;
+        if (s.motion == LINEAR) pt = lin_point(pt1, pt2, t);
+        else if (s.motion == SPLINE) pt = spline_point(s, N, src[i], time, pt1, sx, sy);
+        pt = perturbed(s, nm, pt, pt1, t, false);
+        // point2xy (atomorph.h:315-318) in float
+        const float ptx = pt.x + pt.xf / float(256), pty = pt.y + pt.yf / float(256);
+        double *o = out + 6 * (size_t)i;
+        o[0] = std::min(std::max((ptx * sparseness) + 10.0, 1.0), double(s.width * sparseness + 10.0));
+        o[1] = std::min(std::max((pty * sparseness) + 10.0, 1.0), double(s.height * sparseness + 10.0));
+        o[2] = c.r / 255.0;
+        o[3] = c.g / 255.0;
+        o[4] = c.b / 255.0;
+        o[5] = c.a / 255.0;
     }
 }
 

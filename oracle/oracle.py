@@ -119,6 +119,11 @@ class Oracle:
         L.orc_render.argtypes = [C.POINTER(Scene), C.c_double, u8p]
         L.orc_render_many.argtypes = [C.POINTER(Scene), f64p, C.c_uint32, u8p, C.c_uint32]
         L.orc_positions.argtypes = [C.POINTER(Scene), C.c_double, C.c_int, i32p]
+        L.orc_fluid_targets.argtypes = [C.POINTER(Scene), C.c_double, C.c_double, C.c_uint32, u32p, u32p, f64p, f64p,
+                                        f64p]
+        L.orc_blob_pixels.restype = C.c_size_t
+        L.orc_blob_pixels.argtypes = [C.POINTER(Scene), C.c_size_t, C.c_double, C.POINTER(C.c_uint16), u8p,
+                                      C.c_size_t]
         L.orc_fluid_step.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, f64p, u8p, C.c_uint64, C.c_double]
         L.orc_srand.argtypes = [C.c_uint]
         L.orc_draw_fluid.argtypes = [f64p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double, u32p, C.c_double, u8p]
@@ -187,6 +192,31 @@ class Oracle:
         out = np.zeros((max(N, 1), 2), np.int32)
         self.lib.orc_positions(C.byref(s), t, int(fp64), _p(out, i32p))
         return out[:N]
+
+    def fluid_targets(self, state: dict, t: float, sparseness: float, src, dst, s0, s1) -> np.ndarray:
+        """update_particle's gravity target (x, y) and ideal colour (R, G, B, A)
+        for particles reading columns src / dst with blob surfaces s0 / s1:
+        [n, 6] (morph.cpp:697-767)."""
+        s, keep = make_scene(state)
+        src = np.ascontiguousarray(src, np.uint32)
+        dst = np.ascontiguousarray(dst, np.uint32)
+        s0 = np.ascontiguousarray(s0, np.float64)
+        s1 = np.ascontiguousarray(s1, np.float64)
+        out = np.zeros((len(src), 6))
+        self.lib.orc_fluid_targets(C.byref(s), t, sparseness, len(src), _p(src, u32p), _p(dst, u32p), _p(s0, f64p),
+                                   _p(s1, f64p), _p(out, f64p))
+        return out
+
+    def blob_pixels(self, state: dict, blob: int, t: float):
+        """morph::get_pixels(blob, t): ([n, 2] x, y, [n, 4] RGBA) or None."""
+        s, keep = make_scene(state)
+        n = self.lib.orc_blob_pixels(C.byref(s), blob, t, None, None, 0)
+        if n == (1 << 64) - 1:
+            return None
+        xy = np.zeros((max(n, 1), 2), np.uint16)
+        rgba = np.zeros((max(n, 1), 4), np.uint8)
+        self.lib.orc_blob_pixels(C.byref(s), blob, t, xy.ctypes.data_as(C.POINTER(C.c_uint16)), _p(rgba, u8p), n)
+        return xy[:n], rgba[:n]
 
     def components(self, img: np.ndarray, stored: np.ndarray | None = None):
         """4-connected components of img's opaque pixels: (labels, stats)."""
@@ -324,6 +354,8 @@ class Reference:
         L.ref_pixel_count.restype = C.c_size_t
         L.ref_pixel_count.argtypes = [C.c_void_p, C.c_size_t]
         L.ref_blob_surface.restype = C.c_size_t
+        L.ref_blob_pixels.restype = C.c_size_t
+        L.ref_blob_pixels.argtypes = [C.c_void_p, C.c_size_t, C.c_double, C.POINTER(C.c_uint16), u8p, C.c_size_t]
         L.ref_synchronize.restype = C.c_int
         L.ref_synchronize.argtypes = [C.c_void_p]
         L.ref_state.restype = C.c_uint
@@ -424,6 +456,16 @@ class Reference:
     def blob_energy(self) -> float:
         """The worker's best blob-map energy (thread.cpp:713-716)."""
         return self.lib.ref_blob_energy(self.h)
+
+    def blob_pixels(self, blob: int, t: float):
+        """morph::get_pixels(blob, t): ([n, 2] x, y, [n, 4] RGBA) or None."""
+        n = self.lib.ref_blob_pixels(self.h, blob, t, None, None, 0)
+        if n == (1 << 64) - 1:
+            return None
+        xy = np.zeros((max(n, 1), 2), np.uint16)
+        rgba = np.zeros((max(n, 1), 4), np.uint8)
+        self.lib.ref_blob_pixels(self.h, blob, t, xy.ctypes.data_as(C.POINTER(C.c_uint16)), _p(rgba, u8p), n)
+        return xy[:n], rgba[:n]
 
     def group_labels(self, f: int) -> np.ndarray:
         """[H, W] group of the blob holding each pixel of key frame f (-1: none)."""

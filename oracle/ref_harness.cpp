@@ -247,6 +247,22 @@ void ref_render(void *h, double t, uint8_t *out) {
 }
 
 double ref_get_time(void *h, size_t i, size_t n) { return ((am::morph *)h)->get_time(i, n); }
+// morph::get_pixels(blob, t, to) (morph.cpp:452-678): the pixel list of the
+// blob-th blob of the key frame at t; up to cap pixels into xy / rgba.
+// Returns the list's length, or SIZE_MAX when the reference returns nullptr.
+size_t ref_blob_pixels(void *h, size_t blob, double t, uint16_t *xy, uint8_t *rgba, size_t cap) {
+    std::vector<am::pixel> v;
+    if (!((am::morph *)h)->get_pixels(blob, t, &v)) return SIZE_MAX;
+    for (size_t i = 0; i < v.size() && i < cap; ++i) {
+        xy[2 * i] = v[i].x;
+        xy[2 * i + 1] = v[i].y;
+        rgba[4 * i] = v[i].c.r;
+        rgba[4 * i + 1] = v[i].c.g;
+        rgba[4 * i + 2] = v[i].c.b;
+        rgba[4 * i + 3] = v[i].c.a;
+    }
+    return v.size();
+}
 void ref_bbox(void *h, unsigned *b4) {
     am::morph *m = (am::morph *)h;
     b4[0] = m->bbox_x1; b4[1] = m->bbox_y1; b4[2] = m->bbox_x2; b4[3] = m->bbox_y2;

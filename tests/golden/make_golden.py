@@ -24,8 +24,10 @@ Fixtures (all small, seeded):
                   plateau) on the CPU pipeline's chains of shapes256
   matching.npz    blob matching results (groups per pixel, best blob-map
                   energy, descriptors) on four cases of 2-4 key frames
+  blob_pixels.npz morph::get_pixels(blob, t) lists of every blob at four
+                  times, feather 0 and 3, on the features case's chains
 
-    python tests/golden/make_golden.py features   # one fixture only (or: edges, blob_rules, converge, matching)
+    python tests/golden/make_golden.py features   # one fixture only (or: edges, blob_rules, converge, matching, blob_pixels)
 """
 from __future__ import annotations
 
@@ -216,9 +218,41 @@ def matching_case(R):
     return out
 
 
+BLOB_TS = [0.05, 0.3, 0.61, 0.9]
+
+
+def blob_pixels_case(R):
+    """morph::get_pixels(blob, t) of the reference (morph.cpp:452-678) for
+    every blob of the key frame at each time in BLOB_TS, on the features
+    case's chains, with feather 0 and 3: pixel lists concatenated, offsets per
+    (feather, t, blob)."""
+    rng = np.random.default_rng(77)
+    frames = [synth.ellipses_frame(56, 5, 3.0, 14.0, rng) for _ in range(4)]
+    R.new(frames, seed=5, motion=4, fading=6, delimiter=1, density=1)
+    R.prepare()
+    R.sweeps(4, 31)
+    xy, rgba, index = [], [], []
+    for feather in (0, 3):
+        R.options(feather, 0, 0)
+        for ti, t in enumerate(BLOB_TS):
+            f = int(t * 4)
+            for b in range(R.blob_count(f)):
+                got = R.blob_pixels(b, t)
+                n = 0 if got is None else len(got[0])
+                index.append((feather, ti, b, sum(len(a) for a in xy), n))
+                if got is not None:
+                    xy.append(got[0]); rgba.append(got[1])
+    R.options(0, 0, 0)
+    return dict(ts=np.array(BLOB_TS), index=np.array(index, np.int64), xy=np.concatenate(xy),
+                rgba=np.concatenate(rgba))
+
+
 def main():
     orc.build(with_ref=True)
     R = orc.Reference()
+    if sys.argv[1:] == ["blob_pixels"]:
+        np.savez_compressed(os.path.join(HERE, "blob_pixels.npz"), **blob_pixels_case(R))
+        return
     if sys.argv[1:] == ["matching"]:
         np.savez_compressed(os.path.join(HERE, "matching.npz"), **matching_case(R))
         return
@@ -285,6 +319,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "blob_rules.npz"), **blob_rules_case(R))
     np.savez_compressed(os.path.join(HERE, "converge256.npz"), **converge_case(R))
     np.savez_compressed(os.path.join(HERE, "matching.npz"), **matching_case(R))
+    np.savez_compressed(os.path.join(HERE, "blob_pixels.npz"), **blob_pixels_case(R))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -86,3 +86,41 @@ def test_fluid_morph_counts_over_a_cycle(capi):
         assert np.isfinite(P[:, act]).all()
         assert img[..., 3].any()
     m.close()
+
+
+@pytest.mark.parametrize("case,noise", [("spline48", 0.0), ("ellipses64", 0.0), ("spline48", 3.0)])
+def test_update_particle_targets_match_oracle(capi, oracle, case, noise):
+    """update_particle's gravity target and ideal colour (morph.cpp:697-767)
+    of every active particle after fluid frames, against the oracle's FP64
+    restatement given the columns the particle read: gravity within
+    GRAVITY_TOL grid units (FP32 attractor arithmetic), colour channels within
+    1/255 + COLOUR_TOL (the FP32 fade is within 1 LSB)."""
+    from conftest import golden, golden_state, morph_from_golden
+    GRAVITY_TOL, COLOUR_TOL = 1e-3, 1e-6
+    g = golden(case)
+    m = morph_from_golden(capi, g)
+    sp = 1.0
+    m.set(fluid=2, fluid_sparseness=sp, motion_noise=noise)
+    st = dict(golden_state(g), motion_noise=noise)
+    K = int(g["K"])
+    w, pts, order = m.export_chains()
+    surf, off = _surfaces(pts, w, K)
+    col_of = np.repeat(np.arange(len(w)), w.astype(np.int64))
+    checked = 0
+    for i, t in enumerate([0.1, 0.12, 0.4, 0.42, 0.77]):
+        m.render(t)
+        P = m.fluid_particles()
+        src, dst = m.fluid_links()
+        act = np.nonzero(P[7] != 0)[0]
+        f = min(int(t * K), K - 1)
+        c = col_of[src[act]]
+        assert np.array_equal(c, col_of[dst[act]])  # a particle reads columns of its own chain
+        ref = oracle.fluid_targets(st, t, sp, src[act], dst[act], surf[f][c], surf[(f + 1) % K][c])
+        dg = np.abs(P[4:6, act].T - ref[:, 0:2])
+        dc = np.abs(P[10:14, act].T - ref[:, 2:6])
+        print(f"{case} A={noise} t={t}: {len(act)} particles, gravity max {dg.max():.2e}, colour max {dc.max():.2e}")
+        assert dg.max() <= GRAVITY_TOL
+        assert dc.max() <= 1 / 255 + COLOUR_TOL
+        checked += len(act)
+    assert checked > 0
+    m.close()
