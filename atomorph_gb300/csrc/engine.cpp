@@ -1173,6 +1173,23 @@ int Engine::import_chains(size_t k_, size_t c_, const uint64_t *w, const uint64_
     match_started = true;
     rc = set_chain_layout(std::vector<uint64_t>(w, w + c_));
     if (rc) return rc;
+    // The blobs behind the imported chains: a chain's blob at key frame k is
+    // its original points there (HAS_PIXEL | HAS_FLUID, thread.cpp:800-830),
+    // whose count is the blob's surface and whose mean is its position.
+    for (uint32_t k = 0; k < K; ++k)
+        for (uint32_t g = 0; g < Wb && g < C; ++g) {
+            Blob &b = blobs[k][perm[(size_t)k * Wb + g]];
+            b = Blob();
+            double sx = 0.0, sy = 0.0;
+            for (uint64_t x = chain_off[g]; x < chain_off[g + 1]; ++x) {
+                const uint64_t p = pts[(uint64_t)k * N + x];
+                if (((p >> 48) & 3u) != 3u) continue;
+                ++b.size;
+                sx += (double)(p & 0xFFFFu);
+                sy += (double)((p >> 16) & 0xFFFFu);
+            }
+            if (b.size) { b.x = sx / (double)b.size; b.y = sy / (double)b.size; }
+        }
     if (N * K) AMG_CUDA(cudaMemcpyAsync(d_P.p, pts, N * K * 8, cudaMemcpyHostToDevice, stream));
     uint64_t ex = 0;
     rc = compute_cost(&ex);

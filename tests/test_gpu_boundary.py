@@ -60,7 +60,8 @@ def test_blob_pixels_before_chains_are_the_key_frame_pixels(capi, oracle):
         xy, rgba = m.blob_pixels(b, 0.0)
         ys, xs = np.nonzero(lab == b)
         assert np.array_equal(xy[:, 0], xs) and np.array_equal(xy[:, 1], ys)  # ascending position order
-        want = frames[0][ys, xs]
+        # get_pixel reads the stored HSP colour back as RGB (morph.cpp:378-392)
+        want = np.array([oracle.hsp_to_rgb(int(c)) for c in colors[0][ys, xs]], np.uint32).view(np.uint8).reshape(-1, 4)
         assert np.array_equal(rgba, want)
     m.close()
 

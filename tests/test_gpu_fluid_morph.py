@@ -88,7 +88,7 @@ def test_fluid_morph_counts_over_a_cycle(capi):
     m.close()
 
 
-@pytest.mark.parametrize("case,noise", [("spline48", 0.0), ("ellipses64", 0.0), ("spline48", 3.0)])
+@pytest.mark.parametrize("case,noise", [("ellipses64", 0.0), ("features", 0.0), ("features", 3.0)])
 def test_update_particle_targets_match_oracle(capi, oracle, case, noise):
     """update_particle's gravity target and ideal colour (morph.cpp:697-767)
     of every active particle after fluid frames, against the oracle's FP64
