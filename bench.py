@@ -20,8 +20,10 @@ random-pair sweeps vs the guided and learned proposals) on the same chains.
 --impl reference times the reference's CPU implementation of the render on
 this machine's host cores: the oracle restatement (the reference itself is
 not built on this machine), every host thread rendering its own frames.
-Under torchrun every rank renders its own cycle (replicas, weak scaling, no
-collective on the data path).
+Under torchrun (N ranks) a step renders a cycle of 240 N frames, split
+round-robin across the ranks (240 frames each: weak scaling, every rank's
+frames span the whole morph); frames are independent, so there is no
+collective on the data path, only the max over ranks of the timed region.
 """
 from __future__ import annotations
 
@@ -171,7 +173,7 @@ def render_roofline(m, frames_ts, torch, stream):
 
 def max_over_ranks(ms, world, device="cuda"):
     """Slowest rank's timed region: the whole job's throughput is measured
-    against it (replicas render their own cycles, so this is the only
+    against it (ranks render their own share of the frames, so this is the only
     collective of a multi-GPU run)."""
     if world == 1:
         return float(ms)
@@ -198,7 +200,8 @@ def bench_ours(args, rank, world):
     m = setup_morph(capi, frames, refine_sweeps=args.refine_sweeps, motion_noise=args.motion_noise)
     N, K = m.atoms, len(frames)
     stream = torch.cuda.ExternalStream(m.stream)
-    ts = [m.get_time(i, FRAMES_PER_STEP) for i in range(FRAMES_PER_STEP)]
+    from atomorph_gb300 import shard
+    ts = [m.get_time(i, FRAMES_PER_STEP * world) for i in shard.frame_indices(rank, world, FRAMES_PER_STEP)]
     out = torch.empty((FRAMES_PER_STEP, m.height, m.width, 4), dtype=torch.uint8, device="cuda")
     fb = m.height * m.width * 4
 
@@ -324,7 +327,8 @@ def bench_ours(args, rank, world):
                    "motion_noise_px": args.motion_noise,
                    "refine_sweeps_before_render": args.refine_sweeps,
                    "l2": "per-step working set > L2 (240 output frames, 960 MB, written each step)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": (f"frames split x{world}: a cycle of {FRAMES_PER_STEP * world} frames, "
+                                   f"{FRAMES_PER_STEP} per rank round-robin") if world > 1 else "1 GPU"},
         "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": FRAMES_PER_STEP * fb},
         "e2e_sequence": {"value": round(e2e_seq, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
