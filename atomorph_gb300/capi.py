@@ -126,6 +126,9 @@ _SIGS = {
     "am_batch_destroy": (None, [vp]),
     "am_batch_refine": (C.c_int, [vp, C.c_size_t, u64p]),
     "am_batch_tune": (C.c_int, [vp, C.c_size_t]),
+    "am_batch_refine_guided": (C.c_int, [vp, C.c_size_t, u64p]),
+    "am_batch_refine_schedule": (C.c_int, [vp, C.c_size_t, u64p]),
+    "am_batch_tune_schedule": (C.c_int, [vp, C.c_size_t, C.POINTER(C.c_size_t)]),
     "am_batch_get_tuning": (C.c_int, [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_uint32)]),
     "am_batch_set_tuning": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
@@ -410,8 +413,8 @@ class Morph:
         _check(self.lib.am_record_swaps(self.h, cap), "am_record_swaps")
 
     def record_outcomes(self, cap: int, every: int = 1) -> None:
-        """Plain sweeps log 1 in `every` proposals (pair features, accept 1 /
-        reject 0) for the learned pair proposal; cap 0 stops."""
+        """Plain sweeps log 1 in `every` proposals (pair features, 1 when the swap lowers the cost,
+        else 0) for the learned pair proposal; cap 0 stops."""
         _check(self.lib.am_record_outcomes(self.h, cap, every), "am_record_outcomes")
 
     def recorded_count(self) -> int:
@@ -561,6 +564,23 @@ class Batch:
         """Runs `sweeps` plain sweeps of every job; returns gains [jobs, sweeps]."""
         g = np.zeros((len(self.jobs), sweeps), np.uint64)
         _check(self.lib.am_batch_refine(self.h, sweeps, _p(g, u64p)), "am_batch_refine")
+        return g
+
+    def refine_guided(self, sweeps: int) -> np.ndarray:
+        """`sweeps` guided sweeps of every job; returns gains [jobs, sweeps]."""
+        g = np.zeros((len(self.jobs), sweeps), np.uint64)
+        _check(self.lib.am_batch_refine_guided(self.h, sweeps, _p(g, u64p)), "am_batch_refine_guided")
+        return g
+
+    def tune_schedule(self, sweeps: int) -> int:
+        """Plain sweeps before the guided ones the autotuner picks for a budget."""
+        n = C.c_size_t()
+        _check(self.lib.am_batch_tune_schedule(self.h, sweeps, C.byref(n)), "am_batch_tune_schedule")
+        return n.value
+
+    def refine_schedule(self, sweeps: int) -> np.ndarray:
+        g = np.zeros((len(self.jobs), sweeps), np.uint64)
+        _check(self.lib.am_batch_refine_schedule(self.h, sweeps, _p(g, u64p)), "am_batch_refine_schedule")
         return g
 
     def tune(self, trial_sweeps: int = 3) -> dict:

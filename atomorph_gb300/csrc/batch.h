@@ -16,6 +16,7 @@ struct BatchTuning {
     uint32_t ctas_per_sm = 4;    // co-resident CTAs per SM (<= occupancy limit)
     uint32_t chunk = 4096;       // pairs per chunk (a CTA's unit of work)
     uint32_t order = 0;          // 0: each job's chunks together; 1: jobs interleaved chunk by chunk
+    uint64_t plain_sweeps = 0;   // schedule: plain sweeps before the guided ones (refine_schedule)
 };
 
 class Batch {
@@ -24,13 +25,20 @@ class Batch {
     ~Batch();
     int init();
     int refine(size_t sweeps, uint64_t *gains);  // gains: [njobs][sweeps] or null
+    int refine_guided(size_t sweeps, uint64_t *gains);
+    int refine_schedule(size_t sweeps, uint64_t *gains);  // tuning.plain_sweeps plain, then guided
     int tune(size_t trial_sweeps);
+    int tune_schedule(size_t sweeps);
     BatchTuning tuning;
     size_t njobs() const { return jobs_.size(); }
 
   private:
     int sync_layout();                 // rebuild chunks when any job's chain layout changed
     int run(size_t sweeps, const BatchTuning &t, bool graph, float *ms);
+    int run_local(size_t sweeps, const BatchTuning &t, bool graph, float *ms);
+    int sync_slot_layout();            // slot chunks of the guided sweeps
+    int prepare_guided(uint64_t sweep_offset);
+    int apply_gains(size_t sweeps, uint64_t *gains, bool guided);
     void drop_graphs();
     std::vector<Engine *> jobs_;
     std::vector<uint64_t> versions_;
@@ -51,6 +59,15 @@ class Batch {
     uint32_t chunk_built_ = 0, order_built_ = UINT32_MAX;
     struct Graph { cudaGraphExec_t exec = nullptr; BatchTuning t; };
     std::map<size_t, Graph> graphs_;   // by sweeps per call
+    // batched guided sweeps
+    DBuf<BatchLocalJob> d_ljobs_;
+    BatchLocalJob *h_ljobs_ = nullptr; // pinned mirror
+    DBuf<uint32_t> d_sch_job_, d_sch_count_, d_sch_fi_;
+    DBuf<uint64_t> d_sch_start_;
+    uint32_t sch_off_[4] = {};
+    uint32_t slot_chunk_built_ = 0;
+    std::vector<uint64_t> sversions_;
+    std::map<size_t, Graph> lgraphs_;
 };
 
 }  // namespace amg

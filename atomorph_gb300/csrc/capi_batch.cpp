@@ -44,6 +44,23 @@ int am_batch_refine(am_batch *b, size_t sweeps, uint64_t *gains) {
     return b->b->refine(sweeps, gains);
 }
 
+int am_batch_refine_guided(am_batch *b, size_t sweeps, uint64_t *gains) {
+    if (!b) return AM_ERR_ARG;
+    return b->b->refine_guided(sweeps, gains);
+}
+
+int am_batch_refine_schedule(am_batch *b, size_t sweeps, uint64_t *gains) {
+    if (!b) return AM_ERR_ARG;
+    return b->b->refine_schedule(sweeps, gains);
+}
+
+int am_batch_tune_schedule(am_batch *b, size_t sweeps, size_t *plain_sweeps) {
+    if (!b) return AM_ERR_ARG;
+    int rc = b->b->tune_schedule(sweeps);
+    if (!rc && plain_sweeps) *plain_sweeps = (size_t)b->b->tuning.plain_sweeps;
+    return rc;
+}
+
 int am_batch_tune(am_batch *b, size_t trial_sweeps) {
     if (!b) return AM_ERR_ARG;
     return b->b->tune(trial_sweeps);
@@ -64,7 +81,11 @@ int am_batch_set_tuning(am_batch *b, uint32_t threads, uint32_t ctas_per_sm, uin
     if ((threads != 128 && threads != 256 && threads != 512 && threads != 1024) || ctas_per_sm == 0 ||
         ctas_per_sm > 32 || chunk == 0 || order > 1)
         return AM_ERR_ARG;
-    b->b->tuning = amg::BatchTuning{threads, ctas_per_sm, chunk, order};
+    amg::BatchTuning &t = b->b->tuning;
+    t.threads = threads;
+    t.ctas_per_sm = ctas_per_sm;
+    t.chunk = chunk;
+    t.order = order;
     return AM_OK;
 }
 

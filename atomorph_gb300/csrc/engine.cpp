@@ -673,8 +673,8 @@ int Engine::refine(size_t sweeps, uint64_t *gains) {
     if (active.proposal == AM_PROPOSAL_SCORED) {
         // The pair proposal falls back to plain sweeps until its network is
         // trained, and afterwards whenever plain sweeps gain more cost per
-        // second: one call of each is timed, the better runs the next four
-        // calls, then both are measured again.
+        // second: one call of each is timed, the better runs the next calls
+        // (4 when scored won, 16 when plain did), then both are measured again.
         if (!mlp_trained) return refine_plain(sweeps, gains);
         const bool scored = ps_state == PS_MEASURE_SCORED || (ps_state == PS_RUN && ps_scored);
         const uint64_t before = cost_exact;
@@ -689,7 +689,7 @@ int Engine::refine(size_t sweeps, uint64_t *gains) {
         } else if (ps_state == PS_MEASURE_PLAIN) {
             ps_scored = ps_rate > rate;
             ps_state = PS_RUN;
-            ps_left = 4;
+            ps_left = ps_scored ? 4 : 16;
         } else if (--ps_left <= 0) {
             ps_state = PS_MEASURE_SCORED;
         }

@@ -11,51 +11,14 @@
 // pair runs sweep_pair with the job's own key, so the result is bit-identical
 // to refining each job on its own, whatever the launch shape.
 //
-// The barrier is bounded: a CTA that waits longer than kBarrierTries polls
-// sets the error flag and the abort flag, and every CTA leaves at its next
-// barrier; the host reports AM_ERR_TIMEOUT.  The launch is cooperative, so
-// all CTAs are co-resident and the barrier cannot wait on a CTA that has not
-// started.
+// The grid barrier (gridbar.cuh) is bounded, and the launch cooperative.
 #include "common.cuh"
 #include "kernels.h"
+#include "gridbar.cuh"
 #include "sweep.cuh"
 
 namespace amg {
 namespace {
-
-constexpr uint32_t kBarrierTries = 1u << 24;  // x ~64 ns sleep: about a second
-
-__device__ __forceinline__ bool grid_barrier(const BatchArgs &b) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        ok = 1;
-        volatile unsigned *gen = b.bar + 1;
-        volatile int *abort_flag = (volatile int *)(b.bar + 2);
-        unsigned g = *gen;
-        __threadfence();
-        if (atomicAdd(b.bar, 1u) == gridDim.x - 1) {
-            atomicExch(b.bar, 0u);
-            __threadfence();
-            atomicAdd(b.bar + 1, 1u);
-        } else {
-            uint32_t tries = 0;
-            while (*gen == g) {
-                if (*abort_flag) { ok = 0; break; }
-                if (++tries > kBarrierTries) {
-                    atomicExch(b.err, AM_ERR_TIMEOUT);
-                    atomicExch((int *)(b.bar + 2), 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok;
-}
 
 __global__ void k_batch_sweeps(BatchArgs b) {
     __shared__ unsigned long long red[32];
@@ -88,7 +51,7 @@ __global__ void k_batch_sweeps(BatchArgs b) {
                 __syncthreads();
             }
             const bool last = s + 1 == b.sweeps && p + 1 == nphase;
-            if (!last && !grid_barrier(b)) return;
+            if (!last && !grid_barrier(b.bar, b.err)) return;
         }
     }
 }

@@ -24,6 +24,7 @@
 // both slots, so applied swaps are disjoint and every applied gain is exact.
 #include "common.cuh"
 #include "kernels.h"
+#include "gridbar.cuh"
 
 namespace amg {
 namespace {
@@ -345,7 +346,76 @@ __global__ void __launch_bounds__(256) k_local_apply(LocalArgs a) {
     }
 }
 
+// Every job's guided sweeps in one persistent cooperative launch.  Per sweep
+// and phase, three stages over chunks of (job, frame, slot range) separated
+// by grid barriers: clear the claims, propose (propose_one), apply
+// (apply_one).  The job's LocalArgs are those its own guided sweeps use, with
+// the same keys, so every job ends bit-identical to refining it alone.
+__global__ void __launch_bounds__(256) k_batch_local(BatchLocalArgs b) {
+    __shared__ unsigned long long red[8];
+    const int nphase = (int)b.nphase;
+    for (uint32_t s = 0; s < b.sweeps; ++s) {
+        for (int p = 0; p < nphase; ++p) {
+            const uint32_t lo = p == 0 ? b.ch_off[0] : (p == 1 ? b.ch_off[1] : b.ch_off[2]);
+            const uint32_t hi = p == 0 ? b.ch_off[1] : (p == 1 ? b.ch_off[2] : b.ch_off[3]);
+            for (int stage = 0; stage < 3; ++stage) {
+                for (uint32_t ch = lo + blockIdx.x; ch < hi; ch += gridDim.x) {
+                    const uint32_t j = b.ch_job[ch], fi = b.ch_fi[ch];
+                    const BatchLocalJob &J = b.jobs[j];
+                    const uint64_t start = b.ch_start[ch], end = start + b.ch_count[ch];
+                    if (stage == 0) {
+                        for (uint64_t r = start + threadIdx.x; r < end; r += blockDim.x)
+                            J.a.claim[(uint64_t)fi * J.a.N + r] = 0ull;
+                        continue;
+                    }
+                    LocalArgs a = J.a;
+                    a.frames = J.frames + (p == 0 ? J.ph_off[0] : (p == 1 ? J.ph_off[1] : J.ph_off[2]));
+                    a.nframes = p == 0 ? J.ph_n[0] : (p == 1 ? J.ph_n[1] : J.ph_n[2]);
+                    a.key = mix64(((uint64_t)J.seed << 40) ^ ((J.sweep0 + s) << 4) ^ (uint64_t)p ^ 0x5bd1e995ULL);
+                    if (stage == 1) {
+                        for (uint64_t r = start + threadIdx.x; r < end; r += blockDim.x) propose_one(a, fi, (uint32_t)r);
+                        continue;
+                    }
+                    unsigned long long gain = 0, acc = 0;
+                    for (uint64_t r = start + threadIdx.x; r < end; r += blockDim.x) apply_one(a, fi, (uint32_t)r, gain, acc);
+                    gain = warp_sum_u64(gain);
+                    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = gain;
+                    __syncthreads();
+                    if (threadIdx.x < 32) {
+                        unsigned long long v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0ull;
+                        v = warp_sum_u64(v);
+                        if (threadIdx.x == 0 && v) atomicAdd(b.gains + (uint64_t)j * b.sweeps + s, v);
+                    }
+                    __syncthreads();
+                }
+                const bool last = stage == 2 && s + 1 == b.sweeps && p + 1 == nphase;
+                if (!last && !grid_barrier(b.bar, b.err)) return;
+            }
+        }
+    }
+}
+
 }  // namespace
+
+int batch_local_max_ctas_per_sm(uint32_t threads, int *out) {
+    int n = 0;
+    AMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_local, (int)threads, 0));
+    *out = n;
+    return AM_OK;
+}
+
+int launch_batch_local(const BatchLocalArgs &b, uint32_t grid, uint32_t threads, cudaStream_t s) {
+    if (b.sweeps == 0 || b.nphase == 0) return AM_OK;
+    if (threads > 256) {
+        set_error("am_batch: the batched guided kernel runs at most 256 threads per CTA");
+        return AM_ERR_ARG;
+    }
+    BatchLocalArgs arg = b;
+    void *params[] = {&arg};
+    AMG_CUDA(cudaLaunchCooperativeKernel((const void *)k_batch_local, dim3(grid), dim3(threads), params, 0, s));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return AM_OK;
+}
 
 int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K, uint32_t CW, uint32_t CH,
                       const uint64_t *chain_off, uint32_t C, uint32_t *keys, uint32_t *vals, uint32_t *tk,

@@ -40,7 +40,7 @@ struct SweepArgs {
     unsigned long long *accepted;
     // Optional outcome log for the learned pair proposal: a hashed sample of
     // 1 in log_every proposals writes its pair features ([cap][10]) and
-    // whether the exact criterion accepted it (1 or 0).
+    // whether the swap lowers the cost (1 when c1 > c2, else 0).
     float *log_feat = nullptr, *log_label = nullptr;
     unsigned long long *log_count = nullptr;
     uint64_t log_cap = 0;
@@ -197,6 +197,32 @@ int mlp_forward(const float *feat, uint64_t n, const float *deployed, float *out
 // Gradient of the mean squared error over n samples (no update).
 int mlp_grad(const float *feat, const float *target, uint64_t n, const float *deployed, float *grad,
              float *loss_sum, int *err, cudaStream_t s);
+// ---- batched guided refinement (k_local.cu): every job's guided sweeps in
+// one persistent cooperative launch; per phase the claims of all jobs are
+// cleared, all proposals made, all winners applied, with grid barriers
+// between the stages.  Each job uses its own keys and index, so the result
+// is bit-identical to its own guided sweeps (refine with AM_PROPOSAL_LOCAL
+// once the guided phase has started).
+struct BatchLocalJob {
+    LocalArgs a;                 // the job's guided index and arrays (frames, key, gain set per phase)
+    const uint32_t *frames;      // the job's phase frames, phases concatenated
+    uint32_t ph_off[3], ph_n[3];
+    unsigned seed;
+    uint64_t sweep0;
+};
+struct BatchLocalArgs {
+    const BatchLocalJob *jobs;
+    const uint32_t *ch_job, *ch_fi, *ch_count;  // chunk -> job, frame within the phase, slots
+    const uint64_t *ch_start;    // first slot of the chunk
+    uint32_t ch_off[4];
+    uint32_t nphase, sweeps;
+    unsigned long long *gains;   // [njobs][sweeps], zeroed before the launch
+    unsigned *bar;
+    int *err;
+};
+int launch_batch_local(const BatchLocalArgs &b, uint32_t grid, uint32_t threads, cudaStream_t s);
+int batch_local_max_ctas_per_sm(uint32_t threads, int *out);
+
 int local_index_build(LocalIndex &ix, const uint64_t *P, uint64_t N, uint32_t K, uint32_t CW, uint32_t CH,
                       const uint64_t *chain_off, uint32_t C, uint32_t *keys, uint32_t *vals, uint32_t *tk,
                       uint32_t *tv, uint32_t *hist, cudaStream_t s);

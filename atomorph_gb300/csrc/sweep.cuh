@@ -78,7 +78,9 @@ __device__ __forceinline__ void sweep_pair(const SweepArgs &a, uint32_t fi, uint
                           atom_colour(a.display, a.CW, a.CH, y, a2), f);
 #pragma unroll
             for (int k = 0; k < kMlpIn; ++k) a.log_feat[at * kMlpIn + k] = f[k];
-            a.log_label[at] = c1 >= c2 ? 1.f : 0.f;
+            // the reference's criterion also accepts ties (c1 == c2), which gain
+            // nothing; the label marks the swaps that lower the cost
+            a.log_label[at] = c1 > c2 ? 1.f : 0.f;
         }
     }
     if (c1 >= c2) {

@@ -281,8 +281,9 @@ int    am_train_recorded(am_morph *m, size_t epochs, double lr, float *loss_out)
  * up to cap, as 10 pair features (position difference and distance over
  * 16 px, colour difference of the two atoms' key-frame pixels, each column's
  * current cost log1p(d / (16 px)^2), HAS_PIXEL parity) and the outcome of the
- * reference's criterion c1 >= c2 (thread.cpp:1014-1022): 1 accepted, 0
- * rejected.  am_recorded_swaps reads them (targets = outcomes) and
+ * swap under the reference's costs (thread.cpp:1014-1022): 1 when it lowers
+ * the cost (c1 > c2), 0 otherwise (the criterion c1 >= c2 also accepts ties,
+ * which gain nothing).  am_recorded_swaps reads them (targets = outcomes) and
  * am_train_recorded trains the network on them where they lie.  cap 0 stops.
  * The learned gate and the pair proposal share one network: train it for
  * the proposal kind it serves.  Until it is trained, AM_PROPOSAL_SCORED runs
@@ -337,6 +338,22 @@ void am_batch_destroy(am_batch *b);
 /* n plain sweeps of every job; gains (optional, [jobs][sweeps]) receive the
  * exact cost decrease of each job's sweeps. */
 int  am_batch_refine(am_batch *b, size_t sweeps, uint64_t *gains);
+/* n guided sweeps (AM_PROPOSAL_LOCAL) of every job in one persistent
+ * cooperative launch, captured into a CUDA graph and replayed: per phase the
+ * claims of all jobs are cleared, every column proposes, the winners are
+ * applied, with grid barriers between.  Each job's result is bit-identical
+ * to its own am_refine with AM_PROPOSAL_LOCAL once its guided phase has
+ * started (guided_switch 0); gains as am_batch_refine. */
+int  am_batch_refine_guided(am_batch *b, size_t sweeps, uint64_t *gains);
+/* Schedule autotuner: for a budget of `sweeps` per job, tries 0, 1/8, 1/4
+ * and 1/2 of the budget as plain sweeps followed by guided ones, from the
+ * jobs' chains as they are (restored after each trial), and keeps the split
+ * whose summed final cost is lowest; *plain_sweeps receives it.  The chains
+ * are left as they were. */
+int  am_batch_tune_schedule(am_batch *b, size_t sweeps, size_t *plain_sweeps);
+/* The tuned schedule: plain sweeps (am_batch_refine), then guided ones
+ * (am_batch_refine_guided), `sweeps` in all; gains [jobs][sweeps]. */
+int  am_batch_refine_schedule(am_batch *b, size_t sweeps, uint64_t *gains);
 /* Autotuner: times trial_sweeps real sweeps of all jobs under each candidate
  * launch shape (threads per CTA, CTAs per SM) and work schedule (pairs per
  * chunk, job-major or interleaved chunk order) on a snapshot of the jobs'
