@@ -129,6 +129,11 @@ int am_set_tuning(am_morph *m, const char *name, double value) {
         H(m).render_pipeline = value != 0.0;
         return AM_OK;
     }
+    if (n == "render_bin_ctas" || n == "render_resolve_ctas") {
+        if (value > 8.0 || value != (double)(uint32_t)value) return AM_ERR_ARG;
+        (n == "render_bin_ctas" ? H(m).render_bin_ctas : H(m).render_resolve_ctas) = (uint32_t)value;
+        return AM_OK;
+    }
     amg::Params *ps[2] = {&H(m).front, &H(m).active};
     for (amg::Params *p : ps) {
         if (n == "local_self") p->local_self = (uint32_t)value;

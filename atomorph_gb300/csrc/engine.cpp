@@ -961,6 +961,8 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         // host frames too: the tile plan for the next frame then runs on the
         // second stream, after the resolve the caller waits for
         sc.pipeline = render_pipeline ? 1u : 0u;
+        sc.bin_ctas = render_bin_ctas;
+        sc.resolve_ctas = render_resolve_ctas;
         size_t f = (size_t)(t * fK);
         uint64_t key = f < f_keys.size() ? f_keys[f] : 0;
         rc = render_frame(rw, sc, t, key, dst, rstream);

@@ -235,6 +235,7 @@ class Engine {
     enum { LG_MEASURE_FULL, LG_MEASURE_GATED, LG_GATED, LG_FULL };
     int lg_state = LG_MEASURE_FULL, lg_left = 0;
     bool render_pipeline = true;           // render tuning "render_pipeline"
+    uint32_t render_bin_ctas = 0, render_resolve_ctas = 0;  // "render_bin_ctas", "render_resolve_ctas" (0: all that fit)
     double lg_full_rate = 0.0;
     void learned_gate_next(double gain_per_s);
     int copy_keyframe(size_t f, uint8_t *dst);

@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(256) k_local_apply(LocalArgs a) {
 // by grid barriers: clear the claims, propose (propose_one), apply
 // (apply_one).  The job's LocalArgs are those its own guided sweeps use, with
 // the same keys, so every job ends bit-identical to refining it alone.
-__global__ void __launch_bounds__(256) k_batch_local(BatchLocalArgs b) {
+__global__ void __launch_bounds__(256, 4) k_batch_local(BatchLocalArgs b) {
     __shared__ unsigned long long red[8];
     const int nphase = (int)b.nphase;
     for (uint32_t s = 0; s < b.sweeps; ++s) {

@@ -518,6 +518,9 @@ __global__ void __launch_bounds__(256) k_atom_positions(RenderScene sc, FrameArg
 // capacity go to the overflow list, tile in bits 20-31 of .y, which the
 // resolve also reads.  No grid barrier, no scan in the frame's path.
 constexpr int kBinThreads = 256;
+// Dynamic shared memory that lets at most n CTAs share an SM (227 KB per SM
+// for CTAs, 1 KB of it reserved per CTA, a little static shared memory each).
+inline size_t occupancy_smem(uint32_t n) { return (size_t)(227 * 1024) / std::max<uint32_t>(n, 1) - 2048; }
 constexpr uint32_t kBinMaxTiles = 2048;
 constexpr uint32_t kBinPer = 2;        // records per thread held in shared memory
 
@@ -1379,11 +1382,12 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         b.ovf = A->ovf; b.ovf_cnt = A->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->slot_ovf_cap, UINT32_MAX);
         const unsigned grid = (unsigned)((n + (uint64_t)kBinPer * kBinThreads - 1) / ((uint64_t)kBinPer * kBinThreads));
         // once per process (thread-safe static initialisation)
-        static const cudaError_t battr = cudaFuncSetAttribute(
-            k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bin_smem(kBinPer, kBinMaxTiles));
+        static const cudaError_t battr = cudaFuncSetAttribute(k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                              (int)occupancy_smem(1));
         AMG_CUDA(battr);
         if (w->prof) w->prof->open(ps);
-        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bin_smem(kBinPer, ntiles), ps, b);
+        const size_t bsm = std::max(bin_smem(kBinPer, ntiles), sc.bin_ctas ? occupancy_smem(sc.bin_ctas) : (size_t)0);
+        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bsm, ps, b);
         if (w->prof) w->prof->close(PROF_BIN, ps);
         if (piped) {
             AMG_CUDA(cudaEventRecord(w->binned, w->bs));
@@ -1455,11 +1459,14 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     if (w->prof) w->prof->open(s);
     {
         static const cudaError_t attr = cudaFuncSetAttribute(
-            k_frame_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kResolveSmem + feather_smem(kMaxFeather)));
+            k_frame_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (int)std::max(kResolveSmem + feather_smem(kMaxFeather), occupancy_smem(1)));
         AMG_CUDA(attr);
     }
-    AMG_LAUNCH(k_frame_resolve, ntiles, 256, kResolveSmem + feather_smem(o.feather), s, tr, tiles_x, sc.width,
-               sc.height, sc.density ? sc.density : 1u, out, o);
+    const size_t rsm = std::max(kResolveSmem + feather_smem(o.feather),
+                                sc.resolve_ctas ? occupancy_smem(sc.resolve_ctas) : (size_t)0);
+    AMG_LAUNCH(k_frame_resolve, ntiles, 256, rsm, s, tr, tiles_x, sc.width, sc.height,
+               sc.density ? sc.density : 1u, out, o);
     if (w->prof) w->prof->close(PROF_RESOLVE, s);
     if (fused) {
         // the next frame's tile regions (the other slot) from this frame's

@@ -293,6 +293,10 @@ struct RenderScene {
     // layer (feather + 1 inside, 0 where the blob has no pixel).
     uint32_t only_rank = 0xFFFFFFFFu;
     uint8_t *aux = nullptr;             // device, width * height
+    // Co-resident CTAs per SM the binning and the resolve may take (0: as
+    // many as fit): capping one leaves room on every SM for the other
+    // kernel of the pipelined frames.
+    uint32_t bin_ctas = 0, resolve_ctas = 0;
 };
 // Largest feather the frame render supports (three 32-px tile rings).
 constexpr uint32_t kMaxFeather = 96;

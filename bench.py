@@ -589,10 +589,16 @@ def batch_bench(capi, args):
     once job by job (one am_refine per job) and once as one batch (one
     persistent launch in a replayed CUDA graph, autotuned); both start from
     the same chains with the same sweep counters, so every job's cost must
-    come out identical.  Each form runs twice; the second run is timed."""
+    come out identical.  Each form runs twice; the second run is timed.
+    schedule: from the same initial chains, the plain/guided split the
+    schedule autotuner picks for the same budget, run batched (plain sweeps
+    and guided sweeps each one persistent launch per call), against the
+    summed cost 200 plain sweeps reach.  Atom counts: per key frame (opaque
+    pixels, C3's 2k-200k) and per chain layout (widths summed: the larger
+    blob of each matched group, so up to about twice a key frame's)."""
     from atomorph_gb300 import synth
     n, S = args.batch_jobs, args.batch_sweeps
-    solo, twin = [], []
+    solo, twin, init = [], [], []
     t0 = time.perf_counter()
     for j in range(n):
         frames = synth.workload("batch", j)
@@ -602,11 +608,14 @@ def batch_bench(capi, args):
             raise RuntimeError(f"batch job {j}: pipeline stopped early")
         b = capi.Morph()
         b.load(frames, seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
-        b.import_chains(*a.export_chains())
+        ch = a.export_chains()
+        b.import_chains(*ch)
         solo.append(a)
         twin.append(b)
+        init.append((frames, j, ch))
     setup_s = time.perf_counter() - t0
     atoms = [a.atoms for a in solo]
+    kf_atoms = [synth.opaque_count(f) for fr, _, _ in init for f in fr]
     keys = [a.export_chains()[2].shape[0] for a in solo]
     seq_s = []
     for _ in range(2):
@@ -614,6 +623,8 @@ def batch_bench(capi, args):
         for a in solo:
             a.refine(S, capi.PROPOSAL_RANDOM)
         seq_s.append(time.perf_counter() - t0)
+        if len(seq_s) == 1:
+            cost_plain = sum(a.cost() for a in solo)
     batch = capi.Batch(twin)
     t0 = time.perf_counter()
     tuning = batch.tune(3)
@@ -624,12 +635,54 @@ def batch_bench(capi, args):
         batch.refine(S)
         bat_s.append(time.perf_counter() - t0)
     equal = all(a.cost() == b.cost() for a, b in zip(solo, twin))
-    out = {"workload": f"batch ({n} jobs)", "atoms_min": min(atoms), "atoms_max": max(atoms),
+    third = []
+    for frames, j, ch in init:
+        c = capi.Morph()
+        c.load(frames, seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+        c.import_chains(*ch)
+        third.append(c)
+    cost0 = sum(c.cost() for c in third)
+    sb = capi.Batch(third)
+    sb.set_tuning(**{k: v for k, v in tuning.items()})
+    t0 = time.perf_counter()
+    n_plain = sb.tune_schedule(S)
+    stune_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sb.refine_schedule(S)
+    sched_s = time.perf_counter() - t0
+    cost_sched = sum(c.cost() for c in third)
+    sb.close()
+    # the same schedule job by job (plain sweeps, then guided from the first)
+    fourth = []
+    for frames, j, ch in init:
+        d = capi.Morph()
+        d.load(frames, seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+        d.import_chains(*ch)
+        d.tune(guided_switch=0)
+        fourth.append(d)
+    t0 = time.perf_counter()
+    for d in fourth:
+        if n_plain:
+            d.refine(int(n_plain), capi.PROPOSAL_RANDOM)
+        d.refine(int(S - n_plain), capi.PROPOSAL_LOCAL)
+    sched_seq_s = time.perf_counter() - t0
+    sched_equal = all(c.cost() == d.cost() for c, d in zip(third, fourth))
+    for c in third + fourth:
+        c.close()
+    out = {"workload": f"batch ({n} jobs)", "atoms_per_key_frame_min": min(kf_atoms),
+           "atoms_per_key_frame_max": max(kf_atoms), "chain_atoms_min": min(atoms), "chain_atoms_max": max(atoms),
            "atoms_total": int(sum(atoms)), "key_frames": sorted(set(keys)), "sweeps_per_job": S,
            "setup_s": round(setup_s, 2), "sequential_s": round(seq_s[1], 4), "batched_s": round(bat_s[1], 4),
            "first_batched_call_s": round(bat_s[0], 4), "tune_s": round(tune_s, 3), "tuning": tuning,
            "jobs_per_s_sequential": round(n / seq_s[1], 2), "jobs_per_s_batched": round(n / bat_s[1], 2),
-           "speedup": round(seq_s[1] / bat_s[1], 2), "per_job_cost_identical": bool(equal)}
+           "speedup": round(seq_s[1] / bat_s[1], 2), "per_job_cost_identical": bool(equal),
+           "schedule": {"plain_sweeps": int(n_plain), "guided_sweeps": int(S - n_plain), "tune_s": round(stune_s, 3),
+                        "batched_s": round(sched_s, 4), "jobs_per_s": round(n / sched_s, 2),
+                        "sequential_s": round(sched_seq_s, 4), "jobs_per_s_sequential": round(n / sched_seq_s, 2),
+                        "per_job_cost_identical": bool(sched_equal),
+                        "initial_cost_sum": int(cost0), "cost_sum": int(cost_sched),
+                        "cost_sum_after_plain_sweeps": int(cost_plain),
+                        "vs_plain": round(cost_sched / max(cost_plain, 1), 4)}}
     batch.close()
     for m in solo + twin:
         m.close()

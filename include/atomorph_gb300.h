@@ -150,7 +150,10 @@ size_t am_get_fluid_links(am_morph *m, uint32_t *src_col, uint32_t *dst_col, siz
  * Render: "render_pipeline" (1, the default: a frame's binning and the next
  * frame's tile plan run on a second stream, beside the previous frame's
  * resolve; 0: frames run one after the other on the render stream alone, for
- * timing each kernel by itself). */
+ * timing each kernel by itself).  "render_bin_ctas" / "render_resolve_ctas"
+ * (0, the default: as many as fit; 1-8): co-resident CTAs per SM the frame's
+ * binning / resolve kernel may take, so the pipelined frames' two kernels can
+ * share every SM. */
 int am_set_tuning(am_morph *m, const char *name, double value);
 
 /* ---- control (morph.h:40-49, morph.cpp:52-100, 102-269) */
