@@ -58,15 +58,15 @@ def _peaks():
 
 def _profiled_traffic(kernel):
     """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
-    dram__bytes_write.sum) from the committed per-kernel ncu summary of the
-    same workload, or None."""
-    path = os.path.join(ROOT, "profiles", "kernels_shapes1024_profile_case.md")
+    dram__bytes_write.sum) from the committed ncu summary of the render
+    kernels on the same workload (its per-kernel traffic table), or None."""
+    path = os.path.join(ROOT, "profiles", "render_shapes1024_full.md")
     try:
         for line in open(path):
             cells = [c.strip() for c in line.strip().strip("|").split("|")]
-            if len(cells) >= 6 and cells[0] == f"`{kernel}`":
-                return int(float(cells[5]) * 1e6)
-    except OSError:
+            if len(cells) == 2 and cells[0] == f"`{kernel}`":
+                return int(float(cells[1]) * 1e6)
+    except (OSError, ValueError):
         pass
     return None
 
@@ -290,7 +290,7 @@ def bench_ours(args, rank, world):
     achieved = kernel_bytes / (dom_avg_ms / 1e3) / 1e9
     roof = {"kernel": dom_name, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "peak_kind": peak_kind, "traffic": _profiled_traffic(dom_name),
-            "traffic_source": "profiles/kernels_shapes1024_profile_case.md (ncu, cold cache, bytes per launch)",
+            "traffic_source": "profiles/render_shapes1024_full.md (ncu, cold cache, bytes per launch)",
             "algorithmic_bytes_per_launch": int(kernel_bytes), "avg_launch_ms": round(dom_avg_ms, 5),
             "record_bytes": "16 B per binned record written by k_frame_bin and read by k_frame_resolve (not counted)",
             "frame": {"algorithmic_bytes": int(frame_bytes), "ms": round(frame_ms, 5),
