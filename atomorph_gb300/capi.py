@@ -129,6 +129,7 @@ _SIGS = {
     "am_batch_refine_guided": (C.c_int, [vp, C.c_size_t, u64p]),
     "am_batch_refine_schedule": (C.c_int, [vp, C.c_size_t, u64p]),
     "am_batch_tune_schedule": (C.c_int, [vp, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "am_batch_render": (C.c_int, [vp, f64p, C.c_size_t, C.POINTER(vp), C.c_int]),
     "am_batch_get_tuning": (C.c_int, [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_uint32)]),
     "am_batch_set_tuning": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
@@ -539,7 +540,7 @@ class Fluid:
 
 
 class Batch:
-    """Batched refinement of many morph jobs (am_batch_*)."""
+    """Batched refinement and rendering of many morph jobs (am_batch_*)."""
 
     def __init__(self, jobs):
         self.lib = load()
@@ -582,6 +583,22 @@ class Batch:
         g = np.zeros((len(self.jobs), sweeps), np.uint64)
         _check(self.lib.am_batch_refine_schedule(self.h, sweeps, _p(g, u64p)), "am_batch_refine_schedule")
         return g
+
+    def render(self, ts) -> list:
+        """Frames of every job at the times ts, batched; one [n, H, W, 4]
+        uint8 array per job."""
+        ts = np.ascontiguousarray(ts, np.float64)
+        outs = [np.zeros((len(ts), j.height, j.width, 4), np.uint8) for j in self.jobs]
+        arr = (vp * len(outs))(*[o.ctypes.data for o in outs])
+        _check(self.lib.am_batch_render(self.h, _p(ts, f64p), len(ts), arr, 0), "am_batch_render")
+        return outs
+
+    def render_device(self, ts, dev_ptrs) -> None:
+        """Frames of every job at the times ts into device buffers
+        (dev_ptrs[j]: n frames of job j)."""
+        ts = np.ascontiguousarray(ts, np.float64)
+        arr = (vp * len(dev_ptrs))(*[int(d) for d in dev_ptrs])
+        _check(self.lib.am_batch_render(self.h, _p(ts, f64p), len(ts), arr, 1), "am_batch_render")
 
     def tune(self, trial_sweeps: int = 3) -> dict:
         _check(self.lib.am_batch_tune(self.h, trial_sweeps), "am_batch_tune")

@@ -29,6 +29,9 @@ class Batch {
     int refine_schedule(size_t sweeps, uint64_t *gains);  // tuning.plain_sweeps plain, then guided
     int tune(size_t trial_sweeps);
     int tune_schedule(size_t sweeps);
+    // frames of every job at times ts[0..n): job j's into outs[j] (n frames of
+    // its width * height * 4 bytes, consecutive), device or host memory
+    int render(const double *ts, size_t n, uint8_t *const *outs, bool on_device);
     BatchTuning tuning;
     size_t njobs() const { return jobs_.size(); }
 
@@ -68,6 +71,8 @@ class Batch {
     uint32_t slot_chunk_built_ = 0;
     std::vector<uint64_t> sversions_;
     std::map<size_t, Graph> lgraphs_;
+    // batched frames: staging for host memory the GPU cannot store into
+    DBuf<uint8_t> stage_;
 };
 
 }  // namespace amg

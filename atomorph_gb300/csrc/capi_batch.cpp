@@ -61,6 +61,11 @@ int am_batch_tune_schedule(am_batch *b, size_t sweeps, size_t *plain_sweeps) {
     return rc;
 }
 
+int am_batch_render(am_batch *b, const double *ts, size_t n, uint8_t *const *outs, int outs_on_device) {
+    if (!b) return AM_ERR_ARG;
+    return b->b->render(ts, n, outs, outs_on_device != 0);
+}
+
 int am_batch_tune(am_batch *b, size_t trial_sweeps) {
     if (!b) return AM_ERR_ARG;
     return b->b->tune(trial_sweeps);

@@ -890,7 +890,7 @@ int Engine::synchronize() {
 // a short pinned buffer or a failed query leave the frame on the copy path.
 // One driver query (cuPointerGetAttributes answers pointers it does not
 // know with empty attributes, not an error).
-static uint8_t *mapped_host_range(uint8_t *p, size_t bytes) {
+uint8_t *mapped_host_range(uint8_t *p, size_t bytes) {
     using GetAttrs = CUresult (*)(unsigned, CUpointer_attribute *, void **, CUdeviceptr);
     static GetAttrs get_attrs = [] {
         void *fn = nullptr;
@@ -952,19 +952,8 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         if (rc) return rc;
     } else {
         RenderScene sc;
-        sc.K = fK; sc.C = fC; sc.N = fN; sc.CW = CW; sc.CH = CH; sc.width = width; sc.height = height;
-        sc.bbox[0] = bbox_x1; sc.bbox[1] = bbox_y1; sc.bbox[2] = bbox_x2; sc.bbox[3] = bbox_y2;
-        sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
-        sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
-        sc.motion_noise = front.motion_noise;
-        render_options(sc);
-        // host frames too: the tile plan for the next frame then runs on the
-        // second stream, after the resolve the caller waits for
-        sc.pipeline = render_pipeline ? 1u : 0u;
-        sc.bin_ctas = render_bin_ctas;
-        sc.resolve_ctas = render_resolve_ctas;
-        size_t f = (size_t)(t * fK);
-        uint64_t key = f < f_keys.size() ? f_keys[f] : 0;
+        uint64_t key = 0;
+        frame_scene(t, sc, &key);
         rc = render_frame(rw, sc, t, key, dst, rstream);
         if (rc) return rc;
     }
@@ -1076,6 +1065,24 @@ int Engine::render_many_host(const double *ts, size_t n, uint8_t *out) {
     }
     if (dev) AMG_CUDA(cudaStreamSynchronize(rstream));
     return AM_OK;
+}
+
+// The published chains' scene for an atom frame at normalised time t in
+// [0, 1), and the key frame of its pair.
+void Engine::frame_scene(double t, RenderScene &sc, uint64_t *key) const {
+    sc.K = fK; sc.C = fC; sc.N = fN; sc.CW = CW; sc.CH = CH; sc.width = width; sc.height = height;
+    sc.bbox[0] = bbox_x1; sc.bbox[1] = bbox_y1; sc.bbox[2] = bbox_x2; sc.bbox[3] = bbox_y2;
+    sc.motion = front.motion; sc.fading = front.fading; sc.density = front.density;
+    sc.P = d_Pf.p; sc.chain_off = d_chain_off_f.p; sc.display = d_display.p; sc.rank = d_rank_f.p;
+    sc.motion_noise = front.motion_noise;
+    render_options(sc);
+    // host frames too: the tile plan for the next frame then runs on the
+    // second stream, after the resolve the caller waits for
+    sc.pipeline = render_pipeline ? 1u : 0u;
+    sc.bin_ctas = render_bin_ctas;
+    sc.resolve_ctas = render_resolve_ctas;
+    const size_t f = (size_t)(t * fK);
+    *key = f < f_keys.size() ? f_keys[f] : 0;
 }
 
 // Render options of the front settings (feather, keep_background,

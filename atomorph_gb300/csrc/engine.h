@@ -16,6 +16,10 @@
 
 namespace amg {
 
+// The device address of pinned, CUDA-mapped host memory [p, p + bytes) when
+// one allocation covers it, else null.
+uint8_t *mapped_host_range(uint8_t *p, size_t bytes);
+
 struct Params {  // defaults of morph.h:97-119
     unsigned delimiter = AM_HSP;
     double threshold = 1.0;
@@ -190,6 +194,7 @@ class Engine {
     std::vector<uint32_t> surf_host;
     int render_fluid(double t, uint8_t *dst);
     void render_options(RenderScene &sc) const;
+    void frame_scene(double t, RenderScene &sc, uint64_t *key) const;  // atom frame at t in [0, 1)
     BlobWork *bw = nullptr;
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_n = 0;

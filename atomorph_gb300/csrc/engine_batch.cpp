@@ -4,6 +4,7 @@
 #include "batch.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 namespace amg {
@@ -39,6 +40,12 @@ int Batch::init() {
         return AM_ERR_ARG;
     }
     device_ = jobs_[0]->device;
+    std::vector<Engine *> sorted(jobs_);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) {
+        set_error("am_batch_create: a job appears twice");
+        return AM_ERR_ARG;
+    }
     for (Engine *e : jobs_) {
         if (!e) { set_error("am_batch_create: null job"); return AM_ERR_ARG; }
         if (e->device != device_) { set_error("am_batch_create: jobs on different devices"); return AM_ERR_ARG; }
@@ -584,6 +591,84 @@ int Batch::tune(size_t trial_sweeps) {
     tuning = best;
     drop_graphs();
     return sync_layout();
+}
+
+}  // namespace amg
+
+namespace amg {
+
+// Frames of every job at the times ts: per time, the atom frames of all jobs
+// through render_frames_batch (one binning, one resolve and one tile-plan
+// launch for up to 32 jobs), fluid frames and frames before chains through
+// each job's own render.  Host destinations the GPU can store into (pinned,
+// mapped) are written directly; others receive a copy from a staging frame.
+int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_device) {
+    if (n == 0) return AM_OK;
+    if (!ts || !outs) return AM_ERR_ARG;
+    for (size_t j = 0; j < jobs_.size(); ++j) {
+        if (!outs[j]) return AM_ERR_ARG;
+        if (jobs_[j]->is_busy()) return AM_ERR_BUSY;
+    }
+    AMG_CUDA(cudaSetDevice(device_));
+    const size_t nj = jobs_.size();
+    std::vector<size_t> fsz(nj), stage_off(nj, SIZE_MAX);
+    std::vector<uint8_t *> base(nj);
+    size_t stage_bytes = 0;
+    int rc;
+    for (size_t j = 0; j < nj; ++j) {
+        Engine *e = jobs_[j];
+        if ((rc = e->ensure_streams_public())) return rc;
+        // the job's own frames in flight read the slots and pairs reused here
+        AMG_CUDA(cudaStreamSynchronize(e->rstream));
+        render_quiesce(e->rw);
+        fsz[j] = (size_t)e->width * e->height * 4;
+        base[j] = outs[j];
+        if (!on_device) {
+            uint8_t *d = mapped_host_range(outs[j], n * fsz[j]);
+            if (d) {
+                base[j] = d;
+            } else {
+                stage_off[j] = stage_bytes;
+                stage_bytes += (fsz[j] + 255) / 256 * 256;
+            }
+        }
+    }
+    if (stage_bytes && (rc = stage_.reserve(stage_bytes))) return rc;
+    std::vector<RenderJob> rj;
+    rj.reserve(nj);
+    std::vector<char> batched(nj);
+    for (size_t i = 0; i < n; ++i) {
+        double integ;
+        double t = std::modf(ts[i], &integ);
+        if (t < 0.0) t += 1.0;
+        rj.clear();
+        for (size_t j = 0; j < nj; ++j) {
+            Engine *e = jobs_[j];
+            batched[j] = 0;
+            if (fsz[j] == 0) continue;
+            if (e->fN == 0 || e->fK == 0 || e->front.fluidsteps > 0) {
+                // the job's own render on its render stream, waited for
+                if ((rc = e->render(ts[i], outs[j] + i * fsz[j], on_device))) return rc;
+                AMG_CUDA(cudaStreamSynchronize(e->rstream));
+            } else {
+                uint8_t *dst = stage_off[j] != SIZE_MAX ? stage_.p + stage_off[j] : base[j] + i * fsz[j];
+                RenderJob r;
+                r.w = e->rw;
+                e->frame_scene(t, r.sc, &r.frame_key);
+                r.time = t;
+                r.out = dst;
+                rj.push_back(r);
+                batched[j] = 1;
+            }
+        }
+        if ((rc = render_frames_batch(rj.data(), rj.size(), stream_))) return rc;
+        for (size_t j = 0; j < nj; ++j)
+            if (batched[j] && stage_off[j] != SIZE_MAX)
+                AMG_CUDA(cudaMemcpyAsync(outs[j] + i * fsz[j], stage_.p + stage_off[j], fsz[j], cudaMemcpyDeviceToHost,
+                                         stream_));
+    }
+    AMG_CUDA(cudaStreamSynchronize(stream_));
+    return AM_OK;
 }
 
 }  // namespace amg

@@ -31,6 +31,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <vector>
 
 namespace amg {
@@ -562,7 +563,8 @@ __device__ __forceinline__ void load_atom(const BinArgs &b, uint64_t i, bool noi
     x.nz = noise ? b.in.mn[i] : make_float2(0.f, 0.f);
 }
 
-__global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
+// The binning of one frame's atom chunk `cta` (kBinPer * kBinThreads atoms).
+__device__ __forceinline__ void frame_bin(const BinArgs &b, uint32_t cta) {
     extern __shared__ __align__(16) unsigned char bsm[];
     const uint32_t ntiles = b.fa.ntiles, tid = threadIdx.x, per = kBinPer;
     uint4 *srec = reinterpret_cast<uint4 *>(bsm);
@@ -570,7 +572,7 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
     uint32_t *base = hist + ntiles;
     uint16_t *fix = reinterpret_cast<uint16_t *>(base + ntiles);
     __shared__ uint32_t nfix;
-    const uint64_t chunk0 = (uint64_t)blockIdx.x * per * kBinThreads;
+    const uint64_t chunk0 = (uint64_t)cta * per * kBinThreads;
     const uint64_t n_atoms = *b.n;
     if (chunk0 >= n_atoms) return;  // past the pair's active atoms
     for (uint32_t t = tid; t < ntiles; t += kBinThreads) hist[t] = 0;
@@ -667,14 +669,50 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin(BinArgs b) {
     }
 }
 
+__global__ void __launch_bounds__(kBinThreads, 8) k_frame_bin(const __grid_constant__ BinArgs b) {
+    frame_bin(b, blockIdx.x);
+}
+
+// Frames of several morphs rendered by one launch per kernel (am_batch_render):
+// the jobs' CTAs (atom chunks, tiles, plans) follow one another in the grid,
+// job j's from start[j]; every CTA runs the single-frame code on its own
+// job's arguments, so each job's frame is the one its own launches give.
+// The arguments travel as kernel parameters (constant bank, read uniformly).
+constexpr uint32_t kBatchFrames = 32;
+__device__ __forceinline__ uint32_t batch_job(const uint32_t *start, uint32_t n, uint32_t cta) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (start[mid] <= cta) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+struct BinBatch {
+    uint32_t n;
+    uint32_t start[kBatchFrames + 1];
+    BinArgs job[kBatchFrames];
+};
+__global__ void __launch_bounds__(kBinThreads) k_frame_bin_batch(const __grid_constant__ BinBatch bb) {
+    const uint32_t j = batch_job(bb.start, bb.n, blockIdx.x);
+    frame_bin(bb.job[j], blockIdx.x - bb.start[j]);
+}
+
 // A frame's tile regions from the previous frame's counts src_cnt (one CTA):
 // capacity count + count / 4 + 32 (or, with init, the atoms spread evenly),
 // regions in tile order, clipped to the buffer; the destination slot's
 // counters (cnt, ovf_cnt) are cleared.  Source and destination are the two
 // record slots, so the source's counts stay intact for its resolve.
-__global__ void __launch_bounds__(1024) k_tile_plan(const uint32_t *src_cnt, uint32_t *off, uint32_t *cap,
-                                                    uint32_t *cnt, uint32_t ntiles, uint64_t init_atoms,
-                                                    uint64_t rec_cap, uint32_t *ovf_cnt) {
+struct PlanArgs {
+    const uint32_t *src_cnt;
+    uint32_t *off, *cap, *cnt;
+    uint32_t ntiles;
+    uint64_t init_atoms, rec_cap;
+    uint32_t *ovf_cnt;
+};
+__device__ __forceinline__ void tile_plan(const uint32_t *src_cnt, uint32_t *off, uint32_t *cap, uint32_t *cnt,
+                                          uint32_t ntiles, uint64_t init_atoms, uint64_t rec_cap,
+                                          uint32_t *ovf_cnt) {
     __shared__ uint32_t wsum[32];
     __shared__ unsigned long long carry;
     if (threadIdx.x == 0) carry = 0;
@@ -713,6 +751,22 @@ __global__ void __launch_bounds__(1024) k_tile_plan(const uint32_t *src_cnt, uin
         __syncthreads();
     }
     if (threadIdx.x == 0) *ovf_cnt = 0u;
+}
+__global__ void __launch_bounds__(1024) k_tile_plan(const uint32_t *src_cnt, uint32_t *off, uint32_t *cap,
+                                                    uint32_t *cnt, uint32_t ntiles, uint64_t init_atoms,
+                                                    uint64_t rec_cap, uint32_t *ovf_cnt) {
+    tile_plan(src_cnt, off, cap, cnt, ntiles, init_atoms, rec_cap, ovf_cnt);
+}
+struct PlanBatch {
+    uint32_t n;
+    PlanArgs job[kBatchFrames];
+};
+// Kernel parameters may take up to 32,764 bytes (sm_70 and later, CUDA 12.1 and later).
+static_assert(sizeof(BinBatch) < 32000, "batched binning arguments exceed the kernel parameter space");
+static_assert(sizeof(PlanBatch) < 32000, "batched plan arguments exceed the kernel parameter space");
+__global__ void __launch_bounds__(1024) k_tile_plan_batch(const __grid_constant__ PlanBatch pb) {
+    const PlanArgs &a = pb.job[blockIdx.x];
+    tile_plan(a.src_cnt, a.off, a.cap, a.cnt, a.ntiles, a.init_atoms, a.rec_cap, a.ovf_cnt);
 }
 
 __global__ void __launch_bounds__(256) k_frame_scatter(const uint4 *__restrict__ spl, const uint32_t *n_dev,
@@ -925,9 +979,16 @@ __host__ __device__ inline size_t feather_smem(uint32_t F) {
     return 2 * WW * (32 * WW) * 4 + 1024;
 }
 
-__global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant__ TileRecs tr, uint32_t tiles_x,
-                                                        uint32_t width, uint32_t height, uint32_t density,
-                                                        uint8_t *out, const __grid_constant__ ResolveOpts o) {
+
+// Stacked records of an uncached tile are reduced in the warp when at least
+// kStackMin of a warp's 32 share a base pixel (the accumulation in
+// frame_resolve).
+constexpr bool kStackReduce = true;
+constexpr uint32_t kStackMin = 4;
+
+// The resolve of one 32 x 32 tile of a frame.
+__device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles_x, uint32_t width, uint32_t height,
+                                              uint32_t density, uint8_t *out, const ResolveOpts &o, uint32_t tile) {
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ uint32_t red[8];
     __shared__ int s_over;
@@ -939,7 +1000,6 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
     unsigned long long *xW = reinterpret_cast<unsigned long long *>(sm), *xR = xW + 1024, *xG = xW + 2048,
                        *xB = xW + 3072, *xA = xW + 4096;
     uint32_t *xN = reinterpret_cast<uint32_t *>(xW + 5120);
-    const uint32_t tile = blockIdx.x;
     const uint32_t tx0 = (tile % tiles_x) * kTile, ty0 = (tile / tiles_x) * kTile;
     const uint4 *__restrict__ rec = tr.rec;
     const uint32_t beg = tr.off[tile], nmain = min(tr.cnt[tile], tr.cap[tile]);
@@ -1010,24 +1070,12 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
             // cached: the tile's records in shared memory; else its region
             // and then the overflow list (other tiles' entries skipped)
             const uint32_t iter = cached ? nrec : nmain + novf;
-            for (uint32_t j = threadIdx.x; j < iter; j += 256) {
-                uint4 s;
-                if (cached) {
-                    s = cache[j];
-                } else if (j < nmain) {
-                    s = rec[beg + j];
-                } else {
-                    s = tr.ovf[j - nmain];
-                    if (ovf_tile(s) != tile) continue;
-                }
-                if (s.w != cur) {
-                    if (s.w > cur) nxt = min(nxt, rank_of(o, s));
-                    continue;
-                }
-                uint32_t px = s.x & 0xFFFFu, py = s.x >> 16;
-                uint32_t xf = s.y & 255u, yf = (s.y >> 8) & 255u, valid = (s.y >> 16) & 15u;
-                uint32_t wx[2] = {255u - xf, xf}, wy[2] = {255u - yf, yf};
-                uint32_t cr = s.z & 255u, cg = (s.z >> 8) & 255u, cb = (s.z >> 16) & 255u, ca = s.z >> 24;
+            // one record's valid corners into the accumulators
+            auto add_corners = [&](const uint4 &s) {
+                const uint32_t px = s.x & 0xFFFFu, py = s.x >> 16;
+                const uint32_t xf = s.y & 255u, yf = (s.y >> 8) & 255u, valid = (s.y >> 16) & 15u;
+                const uint32_t wx[2] = {255u - xf, xf}, wy[2] = {255u - yf, yf};
+                const uint32_t cr = s.z & 255u, cg = (s.z >> 8) & 255u, cb = (s.z >> 16) & 255u, ca = s.z >> 24;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     if (!(valid & (1u << k))) continue;
@@ -1050,6 +1098,97 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
                         atomicAdd(&xA[li], (unsigned long long)(W * ca));
                         atomicAdd(&xN[li], 1u);
                     }
+                }
+            };
+            if (kStackReduce && !cached) {
+                // A tile too full for the record cache usually holds atoms
+                // stacked on one pixel (a chain much wider than a key frame's
+                // blob collapses onto that blob's pixels).  The records of a
+                // warp that share the first used record's base pixel are summed
+                // in the warp per corner, and each corner takes one atomic per
+                // sum instead of one per record on the same address.  The trip
+                // count is uniform per warp, so every lane reaches the votes.
+                const uint32_t lane = threadIdx.x & 31u;
+                for (uint32_t jb = threadIdx.x & ~31u; jb < iter; jb += 256) {
+                    const uint32_t j = jb + lane;
+                    uint4 s = make_uint4(0u, 0u, 0u, 0u);
+                    bool use = false;
+                    if (j < iter) {
+                        bool mine = true;
+                        if (j < nmain) {
+                            s = rec[beg + j];
+                        } else {
+                            s = tr.ovf[j - nmain];
+                            mine = ovf_tile(s) == tile;
+                        }
+                        if (mine) {
+                            if (s.w == cur) use = true;
+                            else if (s.w > cur) nxt = min(nxt, rank_of(o, s));
+                        }
+                    }
+                    const unsigned um = __ballot_sync(0xffffffffu, use);
+                    if (um) {
+                        const int L = __ffs(um) - 1;
+                        const uint32_t x0 = __shfl_sync(0xffffffffu, s.x, L);
+                        const bool same = use && s.x == x0;
+                        if ((uint32_t)__popc(__ballot_sync(0xffffffffu, same)) >= kStackMin) {
+                            const uint32_t xf = s.y & 255u, yf = (s.y >> 8) & 255u, valid = (s.y >> 16) & 15u;
+                            const uint32_t cr = s.z & 255u, cg = (s.z >> 8) & 255u, cb = (s.z >> 16) & 255u,
+                                           ca = s.z >> 24;
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) {
+                                const uint32_t cx = (x0 & 0xFFFFu) + (k & 1) - tx0, cy = (x0 >> 16) + (k >> 1) - ty0;
+                                if (cx >= (uint32_t)kTile || cy >= (uint32_t)kTile) continue;  // uniform
+                                const bool a = same && ((valid >> k) & 1u);
+                                // at most 32 records: 32 W and 32 W c stay below 2^32
+                                const uint32_t W = a ? ((k & 1) ? xf : 255u - xf) * ((k >> 1) ? yf : 255u - yf) : 0u;
+                                const uint32_t n = (uint32_t)__popc(__ballot_sync(0xffffffffu, a));
+                                if (n == 0) continue;  // uniform
+                                const uint32_t sW = __reduce_add_sync(0xffffffffu, W);
+                                const uint32_t sR = __reduce_add_sync(0xffffffffu, W * cr);
+                                const uint32_t sG = __reduce_add_sync(0xffffffffu, W * cg);
+                                const uint32_t sB = __reduce_add_sync(0xffffffffu, W * cb);
+                                const uint32_t sA = __reduce_add_sync(0xffffffffu, W * ca);
+                                if ((int)lane == L) {
+                                    const uint32_t li = cy * kTile + cx;
+                                    if (packed) {
+                                        atomicAdd(&pW[li], sW);
+                                        if (counted) atomicAdd(&pN[li], n);
+                                        atomicAdd(&pR[li], sR);
+                                        atomicAdd(&pG[li], sG);
+                                        atomicAdd(&pB[li], sB);
+                                        atomicAdd(&pA[li], sA);
+                                    } else {
+                                        atomicAdd(&xW[li], (unsigned long long)sW);
+                                        atomicAdd(&xR[li], (unsigned long long)sR);
+                                        atomicAdd(&xG[li], (unsigned long long)sG);
+                                        atomicAdd(&xB[li], (unsigned long long)sB);
+                                        atomicAdd(&xA[li], (unsigned long long)sA);
+                                        atomicAdd(&xN[li], n);
+                                    }
+                                }
+                            }
+                            if (same) use = false;
+                        }
+                    }
+                    if (use) add_corners(s);
+                }
+            } else {
+                for (uint32_t j = threadIdx.x; j < iter; j += 256) {
+                    uint4 s;
+                    if (cached) {
+                        s = cache[j];
+                    } else if (j < nmain) {
+                        s = rec[beg + j];
+                    } else {
+                        s = tr.ovf[j - nmain];
+                        if (ovf_tile(s) != tile) continue;
+                    }
+                    if (s.w != cur) {
+                        if (s.w > cur) nxt = min(nxt, rank_of(o, s));
+                        continue;
+                    }
+                    add_corners(s);
                 }
             }
             for (int w = 16; w; w >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, w));
@@ -1139,6 +1278,29 @@ __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant_
     }
 }
 
+__global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant__ TileRecs tr, uint32_t tiles_x,
+                                                        uint32_t width, uint32_t height, uint32_t density,
+                                                        uint8_t *out, const __grid_constant__ ResolveOpts o) {
+    frame_resolve(tr, tiles_x, width, height, density, out, o, blockIdx.x);
+}
+struct ResolveJob {
+    TileRecs tr;
+    ResolveOpts o;
+    uint8_t *out;
+    uint32_t tiles_x, width, height, density;
+};
+struct ResolveBatch {
+    uint32_t n;
+    uint32_t start[kBatchFrames + 1];
+    ResolveJob job[kBatchFrames];
+};
+static_assert(sizeof(ResolveBatch) < 32000, "batched resolve arguments exceed the kernel parameter space");
+__global__ void __launch_bounds__(256, 4) k_frame_resolve_batch(const __grid_constant__ ResolveBatch rb) {
+    const uint32_t j = batch_job(rb.start, rb.n, blockIdx.x);
+    const ResolveJob &a = rb.job[j];
+    frame_resolve(a.tr, a.tiles_x, a.width, a.height, a.density, a.out, a.o, blockIdx.x - rb.start[j]);
+}
+
 __global__ void k_keyframe_copy(const uint32_t *__restrict__ display, const uint8_t *__restrict__ present,
                                 uint32_t CW, uint32_t CH, uint32_t width, uint32_t height, uint32_t *out) {
     size_t n = (size_t)width * height;
@@ -1209,6 +1371,64 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
     d.height = sc.height;
     d.noise = noise;
     return AM_OK;
+}
+
+// Record slots large enough for a fused frame of n atoms over ntiles tiles:
+// the planned tile regions (about 1.25 x the records of a frame plus slack;
+// at most 4 records per atom) and an overflow list of 4 per atom, per slot.
+static int ensure_slots(RenderWork *w, uint64_t n, uint32_t ntiles, cudaStream_t s) {
+    const uint64_t need = n * 5 + (uint64_t)ntiles * 64 + 16, need_ovf = n * 4 + 16;
+    if (need > w->slot_rec_cap || need_ovf > w->slot_ovf_cap || ntiles > w->slot_tiles_cap) {
+        // frames in flight read the old buffers
+        if (w->bs) AMG_CUDA(cudaStreamSynchronize(w->bs));
+        AMG_CUDA(cudaStreamSynchronize(s));
+        const uint64_t rc_new = std::max(w->slot_rec_cap, need + need / 4);
+        const uint64_t oc_new = std::max(w->slot_ovf_cap, need_ovf);
+        const uint32_t tc_new = std::max(w->slot_tiles_cap, ntiles);
+        // capacities are recorded only once every buffer exists: after a
+        // failed allocation the slots are empty and the next frame retries
+        w->slot_rec_cap = w->slot_ovf_cap = 0;
+        w->slot_tiles_cap = 0;
+        cudaError_t e = cudaSuccess;
+        for (auto &sl : w->slot) {
+            slot_free(sl);
+            if (e == cudaSuccess) e = cudaMalloc(&sl.rec, rc_new * sizeof(uint4));
+            if (e == cudaSuccess) e = cudaMalloc(&sl.ovf, oc_new * sizeof(uint4));
+            if (e == cudaSuccess) e = cudaMalloc(&sl.off, (size_t)tc_new * 4);
+            if (e == cudaSuccess) e = cudaMalloc(&sl.cap, (size_t)tc_new * 4);
+            if (e == cudaSuccess) e = cudaMalloc(&sl.cnt, (size_t)tc_new * 4);
+            if (e == cudaSuccess) e = cudaMalloc(&sl.ovf_cnt, 4);
+        }
+        if (e != cudaSuccess) {
+            for (auto &sl : w->slot) slot_free(sl);
+            cudaGetLastError();
+            set_error(std::string("render record slots: ") + cudaGetErrorString(e));
+            return AM_ERR_NOMEM;
+        }
+        w->slot_rec_cap = rc_new;
+        w->slot_ovf_cap = oc_new;
+        w->slot_tiles_cap = tc_new;
+    }
+    return AM_OK;
+}
+
+// The resolve's render options for a frame of pair f at local time t.
+static ResolveOpts resolve_opts(const RenderScene &sc, uint32_t f, double t, uint32_t tiles_y) {
+    ResolveOpts o;
+    std::memset(&o, 0, sizeof(o));
+    o.show_blobs = sc.blob_col ? sc.show_blobs : AM_TEXTURE;
+    o.rank_col = sc.blob_col ? sc.blob_col + (size_t)f * sc.C : nullptr;
+    o.feather = std::min<uint32_t>(sc.feather, kMaxFeather);
+    o.keep_bg = sc.keep_background && sc.present;
+    o.tiles_y = tiles_y;
+    o.bg = bg_args(sc, f, t);
+    o.only_rank = sc.only_rank;
+    o.aux = sc.aux;
+    if (sc.only_rank != 0xFFFFFFFFu) {
+        o.show_blobs = AM_TEXTURE;
+        o.keep_bg = 0;
+    }
+    return o;
 }
 
 // Position / colour arithmetic of the frame at global time `time` (local
@@ -1331,40 +1551,9 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     TileRecs tr;
     RenderWork::Slot *A = nullptr, *B = nullptr;
     if (fused) {
-        // records: the planned tile regions (about 1.25 x the records of a
-        // frame plus slack; at most 4 records per atom) and an overflow list
-        // of 4 per atom, per slot
-        const uint64_t need = sc.N * 5 + (uint64_t)ntiles * 64 + 16, need_ovf = sc.N * 4 + 16;
-        if (need > w->slot_rec_cap || need_ovf > w->slot_ovf_cap || ntiles > w->slot_tiles_cap) {
-            // frames in flight read the old buffers
-            AMG_CUDA(cudaStreamSynchronize(w->bs));
-            AMG_CUDA(cudaStreamSynchronize(s));
-            const uint64_t rc_new = std::max(w->slot_rec_cap, need + need / 4);
-            const uint64_t oc_new = std::max(w->slot_ovf_cap, need_ovf);
-            const uint32_t tc_new = std::max(w->slot_tiles_cap, ntiles);
-            // capacities are recorded only once every buffer exists: after a
-            // failed allocation the slots are empty and the next frame retries
-            w->slot_rec_cap = w->slot_ovf_cap = 0;
-            w->slot_tiles_cap = 0;
-            cudaError_t e = cudaSuccess;
-            for (auto &sl : w->slot) {
-                slot_free(sl);
-                if (e == cudaSuccess) e = cudaMalloc(&sl.rec, rc_new * sizeof(uint4));
-                if (e == cudaSuccess) e = cudaMalloc(&sl.ovf, oc_new * sizeof(uint4));
-                if (e == cudaSuccess) e = cudaMalloc(&sl.off, (size_t)tc_new * 4);
-                if (e == cudaSuccess) e = cudaMalloc(&sl.cap, (size_t)tc_new * 4);
-                if (e == cudaSuccess) e = cudaMalloc(&sl.cnt, (size_t)tc_new * 4);
-                if (e == cudaSuccess) e = cudaMalloc(&sl.ovf_cnt, 4);
-            }
-            if (e != cudaSuccess) {
-                for (auto &sl : w->slot) slot_free(sl);
-                cudaGetLastError();
-                set_error(std::string("render record slots: ") + cudaGetErrorString(e));
-                return AM_ERR_NOMEM;
-            }
-            w->slot_rec_cap = rc_new;
-            w->slot_ovf_cap = oc_new;
-            w->slot_tiles_cap = tc_new;
+        {
+            int rc = ensure_slots(w, sc.N, ntiles, s);
+            if (rc) return rc;
         }
         A = &w->slot[w->cur];
         B = &w->slot[w->cur ^ 1];
@@ -1442,20 +1631,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         }
         tr = TileRecs{w->rec, w->tile_off, w->tile_cnt, w->tile_cnt, w->rec, w->zero, 0u};
     }
-    ResolveOpts o;
-    std::memset(&o, 0, sizeof(o));
-    o.show_blobs = sc.blob_col ? sc.show_blobs : AM_TEXTURE;
-    o.rank_col = sc.blob_col ? sc.blob_col + (size_t)f * sc.C : nullptr;
-    o.feather = std::min<uint32_t>(sc.feather, kMaxFeather);
-    o.keep_bg = sc.keep_background && sc.present;
-    o.tiles_y = tiles_y;
-    o.bg = bg_args(sc, (uint32_t)f, t);
-    o.only_rank = sc.only_rank;
-    o.aux = sc.aux;
-    if (sc.only_rank != 0xFFFFFFFFu) {
-        o.show_blobs = AM_TEXTURE;
-        o.keep_bg = 0;
-    }
+    const ResolveOpts o = resolve_opts(sc, (uint32_t)f, t, tiles_y);
     if (w->prof) w->prof->open(s);
     {
         static const cudaError_t attr = cudaFuncSetAttribute(
@@ -1483,6 +1659,123 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     }
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
+}
+
+
+int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s) {
+    static const cudaError_t battr = cudaFuncSetAttribute(
+        k_frame_bin_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)occupancy_smem(1));
+    static const cudaError_t rattr = cudaFuncSetAttribute(
+        k_frame_resolve_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)std::max(kResolveSmem + feather_smem(kMaxFeather), occupancy_smem(1)));
+    AMG_CUDA(battr);
+    AMG_CUDA(rattr);
+    // about 20 KB of launch arguments: on the heap
+    std::vector<unsigned char> store(sizeof(BinBatch) + sizeof(ResolveBatch) + sizeof(PlanBatch) + 64);
+    BinBatch &bb = *new (store.data()) BinBatch();
+    ResolveBatch &rb = *new (store.data() + sizeof(BinBatch)) ResolveBatch();
+    PlanBatch &pb = *new (store.data() + sizeof(BinBatch) + sizeof(ResolveBatch)) PlanBatch();
+    struct Flip {
+        RenderWork *w;
+        RenderWork::Slot *B;
+        uint32_t ntiles;
+        uint64_t atoms;
+    };
+    std::vector<Flip> flips;
+    uint32_t bin_ctas = 0, tiles = 0;
+    size_t bsm = 0, rsm = 0;
+    auto flush = [&]() -> int {
+        if (pb.n == 0) return AM_OK;
+        bb.n = rb.n = pb.n;
+        bb.start[bb.n] = bin_ctas;
+        rb.start[rb.n] = tiles;
+        if (bin_ctas) AMG_LAUNCH(k_frame_bin_batch, bin_ctas, kBinThreads, bsm, s, bb);
+        AMG_LAUNCH(k_frame_resolve_batch, tiles, 256, rsm, s, rb);
+        AMG_LAUNCH(k_tile_plan_batch, pb.n, 1024, 0, s, pb);
+        AMG_CUDA(cudaGetLastError());
+        for (const Flip &fl : flips) {
+            fl.B->tiles = fl.ntiles;
+            fl.B->atoms = fl.atoms;
+            fl.w->cur ^= 1;
+        }
+        flips.clear();
+        pb.n = 0;
+        bin_ctas = tiles = 0;
+        bsm = rsm = 0;
+        return AM_OK;
+    };
+    for (size_t i = 0; i < n; ++i) {
+        const RenderJob &J = jobs[i];
+        const RenderScene &sc = J.sc;
+        RenderWork *w = J.w;
+        const size_t bytes = (size_t)sc.width * sc.height * 4;
+        const size_t f = (sc.K && sc.C && sc.N) ? (size_t)(J.time * sc.K) : 0;
+        if (sc.K == 0 || sc.C == 0 || sc.N == 0 || f >= sc.K) {
+            AMG_CUDA(cudaMemsetAsync(J.out, 0, bytes, s));
+            continue;
+        }
+        const uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
+        const uint32_t ntiles = tiles_x * tiles_y;
+        // a second frame of a job already in this launch would plan the slot
+        // the first one bins into: launch what is gathered first
+        bool again = false;
+        for (const Flip &fl : flips) again |= fl.w == w;
+        if (again || ntiles > kBinMaxTiles || sc.only_rank != 0xFFFFFFFFu) {
+            int rc = flush();
+            if (rc) return rc;
+        }
+        if (ntiles > kBinMaxTiles || sc.only_rank != 0xFFFFFFFFu) {
+            RenderScene one = sc;
+            one.pipeline = 0;  // everything on s
+            int rc = render_frame(w, one, J.time, J.frame_key, J.out, s);
+            if (rc) return rc;
+            continue;
+        }
+        const double dt = 1.0 / double(sc.K);
+        const double t = std::max(0.0, (J.time - (double)(J.frame_key * dt)) / dt);
+        PairData *pd = nullptr;
+        int rc = prep_pair(w, sc, (uint32_t)f, s, &pd);
+        if (rc) return rc;
+        const uint32_t k = pb.n;
+        BinArgs &b = bb.job[k];
+        if ((rc = frame_args(w, sc, J.time, (uint32_t)f, t, &b.fa, s))) return rc;
+        b.fa.tiles_x = tiles_x;
+        b.fa.ntiles = ntiles;
+        if ((rc = ensure_slots(w, sc.N, ntiles, s))) return rc;
+        RenderWork::Slot *A = &w->slot[w->cur], *B = &w->slot[w->cur ^ 1];
+        if (A->tiles != ntiles || A->atoms != sc.N) {
+            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, s, A->cnt, A->off, A->cap, A->cnt, ntiles,
+                       std::max<uint64_t>(sc.N, 1), w->slot_rec_cap, A->ovf_cnt);
+            A->tiles = ntiles;
+            A->atoms = sc.N;
+        }
+        b.sc = sc;
+        b.n = pd->d_active;
+        b.in = SplatIn{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx, pd->mn};
+        b.rec = A->rec;
+        b.off = A->off; b.cap = A->cap; b.cnt = A->cnt;
+        b.ovf = A->ovf; b.ovf_cnt = A->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->slot_ovf_cap, UINT32_MAX);
+        bb.start[k] = bin_ctas;
+        bin_ctas += (uint32_t)((sc.N + (uint64_t)kBinPer * kBinThreads - 1) / ((uint64_t)kBinPer * kBinThreads));
+        bsm = std::max({bsm, bin_smem(kBinPer, ntiles), sc.bin_ctas ? occupancy_smem(sc.bin_ctas) : (size_t)0});
+        ResolveJob &r = rb.job[k];
+        r.tr = TileRecs{A->rec, A->off, A->cnt, A->cap, A->ovf, A->ovf_cnt, b.ovf_cap};
+        r.o = resolve_opts(sc, (uint32_t)f, t, tiles_y);
+        r.out = J.out;
+        r.tiles_x = tiles_x;
+        r.width = sc.width;
+        r.height = sc.height;
+        r.density = sc.density ? sc.density : 1u;
+        rb.start[k] = tiles;
+        tiles += ntiles;
+        rsm = std::max({rsm, kResolveSmem + feather_smem(r.o.feather),
+                        sc.resolve_ctas ? occupancy_smem(sc.resolve_ctas) : (size_t)0});
+        pb.job[k] = PlanArgs{A->cnt, B->off, B->cap, B->cnt, ntiles, 0, w->slot_rec_cap, B->ovf_cnt};
+        flips.push_back(Flip{w, B, ntiles, sc.N});
+        pb.n = k + 1;
+        if (pb.n == kBatchFrames && (rc = flush())) return rc;
+    }
+    return flush();
 }
 
 }  // namespace amg

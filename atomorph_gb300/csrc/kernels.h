@@ -328,6 +328,20 @@ void render_invalidate(RenderWork *w);
 // Waits for the render work's own binning stream (frames resolve on the
 // caller's render stream; their binning may still be running on it).
 void render_quiesce(RenderWork *w);
+// One morph's frame in a batched render (render_frames_batch).
+struct RenderJob {
+    RenderWork *w;
+    RenderScene sc;
+    double time;          // normalised time in [0, 1)
+    uint64_t frame_key;   // key frame of the pair at `time`
+    uint8_t *out;         // device, width * height * 4
+};
+// Frames of several morphs on stream s: the binning, the resolve and the next
+// tile plan of up to 32 frames each run as one launch; frames that cannot
+// (no chains, tile grids above the fused limit, one blob alone) are rendered
+// one by one on s.  Every frame equals render_frame's for its morph.  Each
+// morph's own render streams must be idle.
+int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s);
 
 // ---- k_fluid.cu: FluidModel::step in FP32
 struct FluidDev;

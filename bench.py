@@ -595,7 +595,8 @@ def batch_bench(capi, args):
     and guided sweeps each one persistent launch per call), against the
     summed cost 200 plain sweeps reach.  Atom counts: per key frame (opaque
     pixels, C3's 2k-200k) and per chain layout (widths summed: the larger
-    blob of each matched group, so up to about twice a key frame's)."""
+    blob of each matched group, so up to about twice a key frame's).
+    render: `batch_frames` frames per job, job by job vs batched."""
     from atomorph_gb300 import synth
     n, S = args.batch_jobs, args.batch_sweeps
     solo, twin, init = [], [], []
@@ -669,6 +670,53 @@ def batch_bench(capi, args):
     sched_equal = all(c.cost() == d.cost() for c, d in zip(third, fourth))
     for c in third + fourth:
         c.close()
+    # frames: F per job at t = i / F from the refined chains (identical in
+    # both sets), job by job (each job's own pipelined am_render into device
+    # memory, then one device synchronisation) and batched (am_batch_render:
+    # per time one binning, one resolve and one plan launch for all jobs);
+    # the same into pageable host memory (am_render per frame vs one batched
+    # call).  Each form runs twice; the second run is timed.
+    import torch
+    F = args.batch_frames
+    ts = [i / F for i in range(F)]
+    dev_solo = [torch.empty((F, a.height, a.width, 4), dtype=torch.uint8, device="cuda") for a in solo]
+    dev_twin = [torch.empty_like(d) for d in dev_solo]
+    rs_s, rb_s, hs_s, hb_s = [], [], [], []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for a, d in zip(solo, dev_solo):
+            step = a.width * a.height * 4
+            for i, t in enumerate(ts):
+                a.render_device(t, d.data_ptr() + i * step)
+        torch.cuda.synchronize()
+        rs_s.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        batch.render_device(ts, [d.data_ptr() for d in dev_twin])
+        rb_s.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        host_solo = [np.stack([a.render(t) for t in ts]) for a in solo]
+        hs_s.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        host_twin = batch.render(ts)
+        hb_s.append(time.perf_counter() - t0)
+    same_dev = [bool(torch.equal(x, y)) for x, y in zip(dev_solo, dev_twin)]
+    same_host = [bool(np.array_equal(x, y)) for x, y in zip(host_solo, host_twin)]
+    same_dh = [bool(np.array_equal(x.cpu().numpy(), y)) for x, y in zip(dev_solo, host_solo)]
+    frames_equal = all(same_dev) and all(same_host) and all(same_dh)
+    pixels = sum(a.width * a.height for a in solo) * F
+    render = {"frames_per_job": F, "frames": n * F, "pixels": int(pixels),
+              "sequential_s": round(rs_s[1], 4), "batched_s": round(rb_s[1], 4),
+              "frames_per_s_sequential": round(n * F / rs_s[1], 1), "frames_per_s_batched": round(n * F / rb_s[1], 1),
+              "speedup": round(rs_s[1] / rb_s[1], 2),
+              "host_sequential_s": round(hs_s[1], 4), "host_batched_s": round(hb_s[1], 4),
+              "host_speedup": round(hs_s[1] / hb_s[1], 2),
+              "per_job_frames_identical": bool(frames_equal)}
+    if not frames_equal:
+        render["jobs_differing"] = {"device": [j for j, v in enumerate(same_dev) if not v],
+                                    "host": [j for j, v in enumerate(same_host) if not v],
+                                    "device_vs_host": [j for j, v in enumerate(same_dh) if not v]}
+    del dev_solo, dev_twin, host_solo, host_twin
     out = {"workload": f"batch ({n} jobs)", "atoms_per_key_frame_min": min(kf_atoms),
            "atoms_per_key_frame_max": max(kf_atoms), "chain_atoms_min": min(atoms), "chain_atoms_max": max(atoms),
            "atoms_total": int(sum(atoms)), "key_frames": sorted(set(keys)), "sweeps_per_job": S,
@@ -682,7 +730,10 @@ def batch_bench(capi, args):
                         "per_job_cost_identical": bool(sched_equal),
                         "initial_cost_sum": int(cost0), "cost_sum": int(cost_sched),
                         "cost_sum_after_plain_sweeps": int(cost_plain),
-                        "vs_plain": round(cost_sched / max(cost_plain, 1), 4)}}
+                        "vs_plain": round(cost_sched / max(cost_plain, 1), 4)},
+           "render": render,
+           "jobs_per_s_refine_and_render_sequential": round(n / (seq_s[1] + rs_s[1]), 2),
+           "jobs_per_s_refine_and_render_batched": round(n / (bat_s[1] + rb_s[1]), 2)}
     batch.close()
     for m in solo + twin:
         m.close()
@@ -856,6 +907,7 @@ def main():
     ap.add_argument("--c4-epochs", type=int, default=1)
     ap.add_argument("--batch-jobs", type=int, default=32)
     ap.add_argument("--batch-sweeps", type=int, default=200)
+    ap.add_argument("--batch-frames", type=int, default=16, help="frames per job in the batched render")
     ap.add_argument("--fluid-frames", type=int, default=24)
     ap.add_argument("--fluid-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -334,7 +334,8 @@ int  am_fluid_render_ex(am_fluid *f, uint32_t width, uint32_t height, double spa
  * am_refine with AM_PROPOSAL_RANDOM would, so results are bit-identical to
  * refining the jobs one by one, and each job's cost, sweep counter and
  * rendered front copy advance as after am_refine.  All jobs must be on one
- * device and idle (not computing) during batch calls. */
+ * device and idle (not computing) during batch calls; a job may appear only
+ * once (AM_ERR_ARG otherwise). */
 typedef struct am_batch am_batch;
 int  am_batch_create(am_batch **out, am_morph *const *jobs, size_t n);
 void am_batch_destroy(am_batch *b);
@@ -357,6 +358,17 @@ int  am_batch_tune_schedule(am_batch *b, size_t sweeps, size_t *plain_sweeps);
 /* The tuned schedule: plain sweeps (am_batch_refine), then guided ones
  * (am_batch_refine_guided), `sweeps` in all; gains [jobs][sweeps]. */
 int  am_batch_refine_schedule(am_batch *b, size_t sweeps, uint64_t *gains);
+/* Frames of every job at the n normalised times ts (morph::get_pixels(t),
+ * morph.cpp:452-678, per job): outs[j] receives job j's n frames, each its
+ * width * height * 4 RGBA8 bytes, one after the other, in device memory when
+ * outs_on_device != 0, else in host memory (pinned, mapped host memory is
+ * stored into by the GPU directly).  Per time, the atom frames of all jobs
+ * are binned by one launch, resolved by one launch and their next tile plans
+ * made by one launch (up to 32 jobs per launch); fluid frames and frames
+ * before chains exist run through each job's own render.  Every frame equals
+ * the job's own am_render at the same time.  The jobs must be idle; the
+ * frames are complete when the call returns. */
+int  am_batch_render(am_batch *b, const double *ts, size_t n, uint8_t *const *outs, int outs_on_device);
 /* Autotuner: times trial_sweeps real sweeps of all jobs under each candidate
  * launch shape (threads per CTA, CTAs per SM) and work schedule (pairs per
  * chunk, job-major or interleaved chunk order) on a snapshot of the jobs'
