@@ -990,7 +990,7 @@ constexpr uint32_t kStackMin = 4;
 __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles_x, uint32_t width, uint32_t height,
                                               uint32_t density, uint8_t *out, const ResolveOpts &o, uint32_t tile) {
     extern __shared__ __align__(16) unsigned char sm[];
-    __shared__ uint32_t red[8];
+    __shared__ uint32_t red[2][8];  // per-warp rank minima, alternating between blob ranks
     __shared__ int s_over;
     // packed mode: six 32-bit accumulators per pixel (a warp's 32-bit
     // atomics spread over 32 banks); exact mode: 64-bit sums and a count
@@ -1056,16 +1056,21 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
         }
         if (threadIdx.x == 0) s_over = 0;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; }
+        for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; lay[q] = 0; }
         if (!cached) visit_tile(tr, tile, [&](const uint4 &v) { mn = min(mn, rank_of(o, v)); });
         for (int w = 16; w; w >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, w));
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mn;
+        if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = mn;
         __syncthreads();
-        uint32_t cur = red[0];
-        for (int k = 1; k < 8; ++k) cur = min(cur, red[k]);
+        uint32_t cur = red[0][0];
+        for (int k = 1; k < 8; ++k) cur = min(cur, red[0][k]);
         bool over = false;
+        uint32_t par = 0;
+        // Two barriers per blob rank: after the accumulation (its sums and the
+        // next rank's per-warp minima complete) and after the pixel pass (the
+        // sums read and cleared).  The minima alternate between two arrays, so
+        // a rank's writes never meet the previous rank's reads.
         while (cur != 0xFFFFFFFFu) {
-            __syncthreads();
+            par ^= 1u;
             uint32_t nxt = 0xFFFFFFFFu;
             // cached: the tile's records in shared memory; else its region
             // and then the overflow list (other tiles' entries skipped)
@@ -1192,29 +1197,15 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                 }
             }
             for (int w = 16; w; w >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, w));
+            if ((threadIdx.x & 31) == 0) red[par][threadIdx.x >> 5] = nxt;
             __syncthreads();
-            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nxt;
             if (feathered)
                 feather_layers(tr, tiles_x, o.tiles_y, tile, cur, o.feather,
                                reinterpret_cast<uint32_t *>(sm + kResolveSmem), flayer);
-            if (packed) {
-                // more than kPackMax contributions (a weight sum above kPackW
-                // without counts) could have wrapped a 32-bit sum
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const uint32_t li = threadIdx.x + 256 * q;
-                    if (counted ? pN[li] > kPackMax : pW[li] > kPackW) s_over = 1;
-                }
-                __syncthreads();
-                if (s_over) { over = true; break; }
-            }
+            uint32_t nx = red[par][0];
+            for (int k = 1; k < 8; ++k) nx = min(nx, red[par][k]);
             // after the last blob rank the accumulators are not read again
-            bool more = true;
-            if (packed) {
-                uint32_t nx = red[0];
-                for (int k = 1; k < 8; ++k) nx = min(nx, red[k]);
-                more = nx != 0xFFFFFFFFu;
-            }
+            const bool more = !packed || nx != 0xFFFFFFFFu;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const uint32_t li = threadIdx.x + 256 * q;
@@ -1223,6 +1214,11 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                 if (packed) {
                     W = pW[li]; sr = pR[li]; sg = pG[li]; sb = pB[li]; sa = pA[li];
                     cnt = counted ? pN[li] : (W ? 1u : 0u);  // valid corners have positive weights
+                    // more than kPackMax contributions (a weight sum above kPackW
+                    // without counts) could have wrapped a 32-bit sum: this rank's
+                    // pixels are drawn anyway and the tile starts over with 64-bit
+                    // sums after the barrier below
+                    if (counted ? cnt > kPackMax : W > kPackW) s_over = 1;
                     if (more) { pW[li] = 0u; pN[li] = 0u; pR[li] = 0u; pG[li] = 0u; pB[li] = 0u; pA[li] = 0u; }
                 } else {
                     cnt = xN[li];
@@ -1259,8 +1255,8 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                 n[q]++;
             }
             __syncthreads();
-            cur = red[0];
-            for (int k = 1; k < 8; ++k) cur = min(cur, red[k]);
+            if (packed && s_over) { over = true; break; }
+            cur = nx;
         }
         if (!over) break;
         __syncthreads();
