@@ -171,6 +171,24 @@ def render_roofline(m, frames_ts, torch, stream):
     return prof
 
 
+def render_records(m, frames_ts, samples=4):
+    """Binned 16-byte records per frame, averaged over `samples` frames of
+    the cycle: one per atom and distinct 32 x 32 tile its positive-weight
+    bilinear corners fall in (from the atoms' exact positions)."""
+    total = 0
+    picks = [frames_ts[(i * len(frames_ts)) // samples] for i in range(samples)]
+    for t in picks:
+        xy = m.positions(float(t)).astype(np.int64)
+        xy = xy[xy[:, 0] >= 0]
+        px, py, xf, yf = xy[:, 0] >> 8, xy[:, 1] >> 8, xy[:, 0] & 255, xy[:, 1] & 255
+        n = np.ones(len(xy), np.int64)
+        cx = (px % 32 == 31) & (xf > 0)   # a right corner in the next tile
+        cy = (py % 32 == 31) & (yf > 0)   # a lower corner in the next tile
+        n += cx.astype(np.int64) + cy.astype(np.int64) + (cx & cy).astype(np.int64)
+        total += int(n.sum())
+    return total // samples
+
+
 def max_over_ranks(ms, world, device="cuda"):
     """Slowest rank's timed region: the whole job's throughput is measured
     against it (ranks render their own share of the frames, so this is the only
@@ -275,28 +293,43 @@ def bench_ours(args, rank, world):
     frame_ms = ms / (FRAMES_PER_STEP * args.steps)
     dom_name, (dom_ms, dom_n) = dom[0], dom[1]
     dom_avg_ms = dom_ms / dom_n
-    # Algorithmic bytes per launch attributed to each kernel that can dominate,
-    # as the per-frame bytes are counted: the atoms' inputs read once (the
-    # binning's 16-byte intermediate records are not algorithmic bytes: they
-    # are reported beside as record_bytes) and 4 B per output pixel
+    # Algorithmic bytes per launch of each frame kernel, split as the frame's
+    # are counted: the binning reads the atoms' inputs once, the resolve
+    # writes 4 B per output pixel.  The 16-byte records the binning writes
+    # and the resolve reads are intermediate: each kernel's figure with them
+    # is given beside ("with_records", records counted from the atoms' tile
+    # crossings as the live frames bin them).
+    recs = render_records(m, ts)
     kernel_bytes = {
         "k_frame_bin": N * atom_bytes,
-        "k_frame_splat": N * atom_bytes,
-        "k_frame_scatter": N * 16 * 2,
-        "k_frame_resolve": N * 16 + m.width * m.height * 4,
-        "pair_prep": N * 8 * 4,
-        "k_scan_u32": 4 * 1024 * 2,
-    }.get(dom_name, frame_bytes)
-    achieved = kernel_bytes / (dom_avg_ms / 1e3) / 1e9
-    roof = {"kernel": dom_name, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "peak_kind": peak_kind, "traffic": _profiled_traffic(dom_name),
+        "k_frame_resolve": m.width * m.height * 4,
+    }
+    with_records = {"k_frame_bin": N * atom_bytes + recs * 16, "k_frame_resolve": recs * 16 + m.width * m.height * 4}
+
+    def kernel_roof(name):
+        n_l = per_frame[name][1]
+        avg = per_frame[name][0] / n_l
+        kb = kernel_bytes.get(name, frame_bytes)
+        out = {"algorithmic_bytes_per_launch": int(kb), "avg_launch_ms": round(avg, 5),
+               "achieved": round(kb / (avg / 1e3) / 1e9, 1), "frac": round(kb / (avg / 1e3) / 1e9 / hbm, 4),
+               "traffic": _profiled_traffic(name)}
+        if name in with_records:
+            wr = with_records[name]
+            out["with_records"] = {"bytes": int(wr), "achieved": round(wr / (avg / 1e3) / 1e9, 1),
+                                   "frac": round(wr / (avg / 1e3) / 1e9 / hbm, 4)}
+        return out
+
+    dk = kernel_roof(dom_name)
+    roof = {"kernel": dom_name, "bound": "hbm", "achieved": dk["achieved"], "peak": hbm, "unit": "GB/s",
+            "frac": dk["frac"], "peak_kind": peak_kind, "traffic": dk["traffic"],
             "traffic_source": "profiles/render_shapes1024_full.md (ncu, cold cache, bytes per launch)",
-            "algorithmic_bytes_per_launch": int(kernel_bytes), "avg_launch_ms": round(dom_avg_ms, 5),
-            "record_bytes": "16 B per binned record written by k_frame_bin and read by k_frame_resolve (not counted)",
+            "algorithmic_bytes_per_launch": dk["algorithmic_bytes_per_launch"], "avg_launch_ms": dk["avg_launch_ms"],
+            "record_bytes": f"16 B per binned record, {recs} records per frame (intermediate; see per_kernel)",
             "frame": {"algorithmic_bytes": int(frame_bytes), "ms": round(frame_ms, 5),
                       "kernel_ms_sum": round(frame_ms_profiled, 5),
                       "achieved_gbs": round(frame_bytes / (frame_ms / 1e3) / 1e9, 1),
                       "frac": round(frame_bytes / (frame_ms / 1e3) / 1e9 / hbm, 4)},
+            "per_kernel": {k: kernel_roof(k) for k in ("k_frame_bin", "k_frame_resolve") if k in per_frame},
             "kernels_ms_per_frame": {k: round(v[0] / FRAMES_PER_STEP, 5) for k, v in per_frame.items()}}
 
     flu = None
@@ -831,7 +864,8 @@ def profile_case(args):
     renders), 4 guided sweeps, 2 recorded sweeps, one training epoch, 4
     gated (learned) sweeps, the allocation-free cost, `--frames` atom frames,
     2 fluid frames with 2 solver steps each on a (0.5 W + 20)^2 grid, and one
-    batched refinement of 4 small jobs.  Settings as the benchmark's."""
+    batched refinement and two batched frames of 4 small jobs.  Settings as
+    the benchmark's."""
     import ctypes as C
 
     import torch
@@ -877,6 +911,7 @@ def profile_case(args):
         jobs.append(a)
     b = capi.Batch(jobs)
     b.refine(4)
+    b.render([0.1, 0.6])
     b.close()
     for a in jobs:
         a.close()
