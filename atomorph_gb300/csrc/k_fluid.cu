@@ -128,6 +128,24 @@ __device__ __forceinline__ void patch_add(float *acc, int q, float v, float scal
 __device__ __forceinline__ float patch_get(const float *acc, int q, float scale) {
     return scale != 0.f ? (float)reinterpret_cast<const int *>(acc)[q] / scale : acc[q];
 }
+// Sum of a per-cell field over the 3x3 cells whose stencils reach patch node
+// (lx, ly): cells (lx - 2 .. lx, ly - 2 .. ly) inside the patch's cell range
+// [0, bw - 2) x [0, bh - 2).  In fixed point the integer terms are added
+// first, so the node sum is the one the nine per-node deposits would give.
+__device__ __forceinline__ float cell_sum(const float *acc, int lx, int ly, int bw, int bh, float scale) {
+    int isum = 0;
+    float fsum = 0.f;
+#pragma unroll
+    for (int di = 0; di < 3; ++di)
+#pragma unroll
+        for (int dj = 0; dj < 3; ++dj) {
+            const int cx = lx - di, cy = ly - dj;
+            if (cx < 0 || cy < 0 || cx >= bw - 2 || cy >= bh - 2) continue;
+            if (scale != 0.f) isum += reinterpret_cast<const int *>(acc)[cx * bh + cy];
+            else fsum += acc[cx * bh + cy];
+        }
+    return scale != 0.f ? (float)isum / scale : fsum;
+}
 
 #define FL(f, i) a.P[(size_t)(f) * a.n + (i)]
 #define ND_(f, q) a.G[(size_t)(f) * ((size_t)a.gsx * a.gsy) + (q)]
@@ -181,7 +199,7 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
             }
         return;
     }
-    const int x0 = box[0], y0 = box[1], bh = box[3], nn = box[2] * bh;
+    const int x0 = box[0], y0 = box[1], bw = box[2], bh = box[3], nn = bw * bh;
     for (int q = threadIdx.x; q < nn; q += kFlThreads)
 #pragma unroll
         for (int f = 0; f < kQ; ++f) acc[f * kPrivNodes + q] = 0.f;
@@ -196,33 +214,39 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
                 patch_add(acc, QM * kPrivNodes + q, phi, scale);
                 patch_add(acc, QGX * kPrivNodes + q, s.gx[i] * s.py[j], scale);
                 patch_add(acc, QGY * kPrivNodes + q, s.px[i] * s.gy[j], scale);
-                if (colour) {
-                    patch_add(acc, QW * kPrivNodes + q, str, scale);
-                    patch_add(acc, QR * kPrivNodes + q, str * r, scale);
-                    patch_add(acc, QG * kPrivNodes + q, str * g, scale);
-                    patch_add(acc, QB * kPrivNodes + q, str * b, scale);
-                    patch_add(acc, QA * kPrivNodes + q, str * al, scale);
-                }
             }
+        if (colour) {
+            // The colour terms are the same at all nine nodes of the stencil:
+            // one term per particle into its stencil cell, spread over the
+            // nodes when the patch is added to the grid (5 shared atomics per
+            // particle instead of 45).
+            const int c = (s.cx - x0) * bh + (s.cy - y0);
+            patch_add(acc, QW * kPrivNodes + c, str, scale);
+            patch_add(acc, QR * kPrivNodes + c, str * r, scale);
+            patch_add(acc, QG * kPrivNodes + c, str * g, scale);
+            patch_add(acc, QB * kPrivNodes + c, str * b, scale);
+            patch_add(acc, QA * kPrivNodes + c, str * al, scale);
+        }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nn; q += kFlThreads) {
         const float m = patch_get(acc, QM * kPrivNodes + q, scale), gx = patch_get(acc, QGX * kPrivNodes + q, scale),
                     gy = patch_get(acc, QGY * kPrivNodes + q, scale);
-        const size_t n = node(a, x0 + q / bh, y0 + q % bh);
+        const int lx = q / bh, ly = q % bh;
+        const size_t n = node(a, x0 + lx, y0 + ly);
         if (m != 0.f || gx != 0.f || gy != 0.f) {
             atomicAdd(&ND_(NM, n), m);
             atomicAdd(&ND_(ND, n), m);
             atomicAdd(&ND_(NGX, n), gx);
             atomicAdd(&ND_(NGY, n), gy);
         }
-        const float w = patch_get(acc, QW * kPrivNodes + q, scale);
+        const float w = cell_sum(acc + QW * kPrivNodes, lx, ly, bw, bh, scale);
         if (w != 0.f) {
             atomicAdd(&ND_(NW, n), w);
-            atomicAdd(&ND_(NR, n), patch_get(acc, QR * kPrivNodes + q, scale));
-            atomicAdd(&ND_(NG, n), patch_get(acc, QG * kPrivNodes + q, scale));
-            atomicAdd(&ND_(NB, n), patch_get(acc, QB * kPrivNodes + q, scale));
-            atomicAdd(&ND_(NA, n), patch_get(acc, QA * kPrivNodes + q, scale));
+            atomicAdd(&ND_(NR, n), cell_sum(acc + QR * kPrivNodes, lx, ly, bw, bh, scale));
+            atomicAdd(&ND_(NG, n), cell_sum(acc + QG * kPrivNodes, lx, ly, bw, bh, scale));
+            atomicAdd(&ND_(NB, n), cell_sum(acc + QB * kPrivNodes, lx, ly, bw, bh, scale));
+            atomicAdd(&ND_(NA, n), cell_sum(acc + QA * kPrivNodes, lx, ly, bw, bh, scale));
         }
     }
 }
@@ -353,15 +377,32 @@ __device__ __forceinline__ void pull(float x1, float y1, float x2, float y2, flo
 
 __global__ void __launch_bounds__(kFlThreads) k_fl_vel(FlArgs a) {
     __shared__ float acc[2 * kPrivNodes];
+    __shared__ float pg[2 * kPrivNodes];  // the patch's node accelerations (gathered as in k_fl_advect)
     __shared__ int box[5], red[5 * (kFlThreads / 32)];
     const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
     const uint8_t fl = p < a.n ? a.flags[p] : 0;
     const bool act = fl & 1;
     Stencil s{};
     Dep2 d;
+    float x = 0.f, y = 0.f;
     if (act) {
-        float x = FL(PX, p), y = FL(PY, p);
+        x = FL(PX, p);
+        y = FL(PY, p);
         s = stencil(x, y, a.gsx, a.gsy);
+    }
+    float unused;
+    const bool patch = priv_box(act, s.cx, s.cy, 0.f, box, red, &unused);
+    const int x0 = box[0], y0 = box[1], bh = box[3];
+    if (patch) {
+        const int nn = box[2] * bh;
+        for (int q = threadIdx.x; q < nn; q += kFlThreads) {
+            const size_t n = node(a, x0 + q / bh, y0 + q % bh);
+            pg[q] = ND_(NAX, n);
+            pg[kPrivNodes + q] = ND_(NAY, n);
+        }
+        __syncthreads();
+    }
+    if (act) {
         float cax, cay;
         pull(x, y, FL(PGX, p), FL(PGY, p), 0.03f, cax, cay);
         float u = FL(PU, p), v = FL(PV, p);
@@ -369,10 +410,19 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_vel(FlArgs a) {
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                size_t q = node(a, s.cx + i, s.cy + j);
+                float ax, ay;
+                if (patch) {
+                    const int q = (s.cx + i - x0) * bh + (s.cy + j - y0);
+                    ax = pg[q];
+                    ay = pg[kPrivNodes + q];
+                } else {
+                    const size_t q = node(a, s.cx + i, s.cy + j);
+                    ax = ND_(NAX, q);
+                    ay = ND_(NAY, q);
+                }
                 float phi = s.px[i] * s.py[j];
-                u += phi * (ND_(NAX, q) + cax);
-                v += phi * (ND_(NAY, q) + cay);
+                u += phi * (ax + cax);
+                v += phi * (ay + cay);
             }
         FL(PU, p) = u;
         FL(PV, p) = v;
@@ -389,25 +439,57 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_vel(FlArgs a) {
     deposit2(a, act, s, d, NU, NV, acc, box, red);
 }
 
-__global__ void k_fl_advect(FlArgs a) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
-        uint8_t fl = a.flags[p];
-        if (!(fl & 1)) continue;
-        float x = FL(PX, p), y = FL(PY, p);
-        Stencil s = stencil(x, y, a.gsx, a.gsy);
+// The node fields advect reads, in the order of its shared-memory patch.
+__host__ __device__ constexpr int advect_field(int f) {
+    return f == 0 ? NU : f == 1 ? NV : f == 2 ? NW : f == 3 ? NR : f == 4 ? NG : f == 5 ? NB : NA;
+}
+
+__global__ void __launch_bounds__(kFlThreads) k_fl_advect(FlArgs a) {
+    // The CTA's particles are neighbours in solver order, so their stencils
+    // cover a compact patch: its node fields are read once into shared
+    // memory and every particle gathers its 3x3 nodes from there (the grid
+    // itself when the patch exceeds kPrivNodes nodes).
+    __shared__ float pg[7 * kPrivNodes];
+    __shared__ int box[5], red[5 * (kFlThreads / 32)];
+    const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
+    const uint8_t fl = p < a.n ? a.flags[p] : 0;
+    const bool act = fl & 1;
+    float x = 0.f, y = 0.f;
+    Stencil s{};
+    if (act) {
+        x = FL(PX, p);
+        y = FL(PY, p);
+        s = stencil(x, y, a.gsx, a.gsy);
+    }
+    float unused;
+    const bool patch = priv_box(act, s.cx, s.cy, 0.f, box, red, &unused);
+    const int x0 = box[0], y0 = box[1], bh = box[3];
+    if (patch) {
+        const int nn = box[2] * bh;
+        for (int q = threadIdx.x; q < nn; q += kFlThreads) {
+            const size_t n = node(a, x0 + q / bh, y0 + q % bh);
+#pragma unroll
+            for (int f = 0; f < 7; ++f) pg[f * kPrivNodes + q] = ND_(advect_field(f), n);
+        }
+        __syncthreads();
+    }
+    if (act) {
+        auto nd = [&](int f, int i, int j) -> float {
+            return patch ? pg[f * kPrivNodes + (s.cx + i - x0) * bh + (s.cy + j - y0)]
+                         : ND_(advect_field(f), node(a, s.cx + i, s.cy + j));
+        };
         float gu = 0.f, gv = 0.f, w = 0.f, nR = 0.f, nG = 0.f, nB = 0.f, nA = 0.f;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                size_t q = node(a, s.cx + i, s.cy + j);
                 float phi = s.px[i] * s.py[j];
-                gu += phi * ND_(NU, q);
-                gv += phi * ND_(NV, q);
-                float nw = ND_(NW, q);
+                gu += phi * nd(0, i, j);
+                gv += phi * nd(1, i, j);
+                float nw = nd(2, i, j);
                 if (nw > 0.f) {
                     w += nw;
-                    nR += ND_(NR, q); nG += ND_(NG, q); nB += ND_(NB, q); nA += ND_(NA, q);
+                    nR += nd(3, i, j); nG += nd(4, i, j); nB += nd(5, i, j); nA += nd(6, i, j);
                 }
             }
         if (w > 0.f) {
@@ -587,7 +669,7 @@ int fluid_run(FluidDev *f, uint32_t nsteps, uint64_t last_steps_left, double fre
             AMG_LAUNCH(k_fl_div, gg, 256, 0, s, a, (int)NAX, (int)NAY);
             AMG_LAUNCH(k_fl_vel, gp, kFlThreads, 0, s, a);
             AMG_LAUNCH(k_fl_div, gg, 256, 0, s, a, (int)NU, (int)NV);
-            AMG_LAUNCH(k_fl_advect, gl, 256, 0, s, a);
+            AMG_LAUNCH(k_fl_advect, gp, kFlThreads, 0, s, a);
         }
         if (prof) prof->close(PROF_FLUID, s);
     }
