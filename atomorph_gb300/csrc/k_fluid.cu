@@ -76,6 +76,16 @@ struct FlArgs {
 constexpr int kFlThreads = 256;    // particles per CTA of the deposit passes (one per thread)
 constexpr int kPrivNodes = 1024;   // nodes of a CTA's shared-memory patch
 
+// The particle of this thread within its CTA's 256 (a bijection): lane l of
+// warp w takes particle 8 l + w.  Particles are sorted by cell, about four
+// to a cell, so consecutive particles share their stencil nodes; spread this
+// way, the 32 lanes of a warp lie in different cells and each shared-memory
+// atomic of a deposit goes to 32 different nodes instead of queueing on a
+// few.  The patch sums are integers, so the order changes nothing.
+__device__ __forceinline__ uint32_t spread_lane() {
+    return (threadIdx.x & 31u) * (kFlThreads / 32) + (threadIdx.x >> 5);
+}
+
 // Patch of the CTA's 3x3 stencils (origins (cx, cy) of its active
 // particles): box = {x0, y0, width, height} in shared memory.  True when the
 // CTA has active particles and the patch fits kPrivNodes nodes (uniform).
@@ -160,7 +170,7 @@ enum { QM, QGX, QGY, QW, QR, QG, QB, QA, kQ };
 __global__ void __launch_bounds__(kFlThreads) k_fl_p2g(FlArgs a) {
     __shared__ float acc[kQ * kPrivNodes];
     __shared__ int box[5], red[5 * (kFlThreads / 32)];
-    const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
+    const uint32_t p = blockIdx.x * kFlThreads + spread_lane();
     const uint8_t fl = p < a.n ? a.flags[p] : 0;
     const bool act = fl & 1;
     Stencil s{};
@@ -305,7 +315,7 @@ __device__ __forceinline__ void deposit2(const FlArgs &a, bool act, const Stenci
 __global__ void __launch_bounds__(kFlThreads) k_fl_forces(FlArgs a) {
     __shared__ float acc[2 * kPrivNodes];
     __shared__ int box[5], red[5 * (kFlThreads / 32)];
-    const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
+    const uint32_t p = blockIdx.x * kFlThreads + spread_lane();
     const bool act = p < a.n && (a.flags[p] & 1);
     Stencil s{};
     Dep2 d;
@@ -379,7 +389,7 @@ __global__ void __launch_bounds__(kFlThreads) k_fl_vel(FlArgs a) {
     __shared__ float acc[2 * kPrivNodes];
     __shared__ float pg[2 * kPrivNodes];  // the patch's node accelerations (gathered as in k_fl_advect)
     __shared__ int box[5], red[5 * (kFlThreads / 32)];
-    const uint32_t p = blockIdx.x * kFlThreads + threadIdx.x;
+    const uint32_t p = blockIdx.x * kFlThreads + spread_lane();
     const uint8_t fl = p < a.n ? a.flags[p] : 0;
     const bool act = fl & 1;
     Stencil s{};
