@@ -954,7 +954,16 @@ int Engine::render(double time, uint8_t *out, bool out_dev) {
         RenderScene sc;
         uint64_t key = 0;
         frame_scene(t, sc, &key);
-        rc = render_frame(rw, sc, t, key, dst, rstream);
+        // a host frame of a sequence played in order: the next frame is
+        // binned beside this one's resolve, ready when the caller asks for it
+        FrameAhead nx;
+        double tn = 0.0;
+        const bool ahead = !out_dev && next_time(t, &tn);
+        if (ahead) {
+            nx.time = tn;
+            frame_scene(tn, nx.sc, &nx.frame_key);
+        }
+        rc = render_frame(rw, sc, t, key, dst, rstream, ahead ? &nx : nullptr);
         if (rc) return rc;
     }
     // A device frame is left in flight on the render stream (am_get_stream);
@@ -1065,6 +1074,40 @@ int Engine::render_many_host(const double *ts, size_t n, uint8_t *out) {
     }
     if (dev) AMG_CUDA(cudaStreamSynchronize(rstream));
     return AM_OK;
+}
+
+// The frame after t in a sequence of host frames t_i = get_time(i, n)
+// (morph.cpp:1522-1538; without `finite` i / n, with it i / (n - 1) scaled
+// by 1 - 1/F), when the previous host frame was t_(i-1) of the same
+// sequence: the order the reference's demo writes frames in
+// (demo/main.cpp:177-190).  The prediction is exact or absent: the time is
+// recomputed with get_time's own arithmetic and both known terms are
+// checked bit for bit.
+bool Engine::next_time(double t, double *tn) {
+    const double prev = last_host_t;
+    last_host_t = t;
+    if (!(t > prev)) return false;  // the first frame, a repeat, a jump back or the cycle's wrap
+    const size_t F = frames.size();
+    const bool fin = front.finite;
+    if (fin && F == 0) return false;
+    const double scale = fin ? 1.0 - 1.0 / double(F) : 1.0;
+    const double steps = std::round(scale / (t - prev));  // n (or n - 1 with finite)
+    if (!(steps >= 2.0 && steps <= 1e9)) return false;
+    const double di = std::round(t / scale * steps);
+    if (!(di >= 1.0 && di <= steps)) return false;
+    const size_t i = (size_t)di, n = (size_t)steps + (fin ? 1 : 0);
+    auto at = [&](size_t k) {
+        if (!fin) return double(k) / double(n);
+        double v = double(k) / double(n - 1);
+        v *= 1.0 - (1.0 / double(F));
+        return v;
+    };
+    if (at(i) != t || at(i - 1) != prev) return false;
+    if (fin && i + 1 > n - 1) return false;  // a finite sequence ends
+    double nxt = at(i + 1), integ;
+    nxt = std::modf(nxt, &integ);  // i + 1 == n wraps to the cycle's start
+    *tn = nxt;
+    return true;
 }
 
 // The published chains' scene for an atom frame at normalised time t in

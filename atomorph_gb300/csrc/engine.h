@@ -195,6 +195,8 @@ class Engine {
     int render_fluid(double t, uint8_t *dst);
     void render_options(RenderScene &sc) const;
     void frame_scene(double t, RenderScene &sc, uint64_t *key) const;  // atom frame at t in [0, 1)
+    bool next_time(double t, double *tn);  // the next host frame of a get_time sequence
+    double last_host_t = -1.0;             // time of the last host frame (next_time)
     BlobWork *bw = nullptr;
     uint8_t *h_pinned = nullptr;
     size_t h_pinned_n = 0;

@@ -91,7 +91,37 @@ struct RenderWork {
     int *perm = nullptr;    // [4][512] Perlin permutations on the device (lag, slope, motion x, motion y)
     bool perm_set = false;
     Prof *prof = nullptr;   // optional per-kernel timing
+    // A frame binned before its call (render_frame's `ahead`): its records
+    // are in slot[cur] and w->binned marks their end on bs.  The next fused
+    // frame uses them when it is exactly that time and scene, and plans the
+    // slot afresh otherwise.
+    struct Ahead {
+        bool valid = false;
+        double time = 0.0;
+        uint64_t key = 0;
+        RenderScene sc;
+    } ahead;
 };
+
+// Drops a frame binned ahead: the slot it filled is planned afresh by the
+// next fused frame (stream order puts that plan after the binning).
+static void drop_ahead(RenderWork *w) {
+    if (!w->ahead.valid) return;
+    w->slot[w->cur].tiles = 0;
+    w->ahead.valid = false;
+}
+
+// Every scene field a fused frame's binning and resolve read.
+static bool same_scene(const RenderScene &a, const RenderScene &b) {
+    return a.K == b.K && a.C == b.C && a.N == b.N && a.CW == b.CW && a.CH == b.CH && a.width == b.width &&
+           a.height == b.height && a.bbox[0] == b.bbox[0] && a.bbox[1] == b.bbox[1] && a.bbox[2] == b.bbox[2] &&
+           a.bbox[3] == b.bbox[3] && a.motion == b.motion && a.fading == b.fading && a.density == b.density &&
+           a.P == b.P && a.chain_off == b.chain_off && a.display == b.display && a.rank == b.rank &&
+           a.pipeline == b.pipeline && a.feather == b.feather && a.keep_background == b.keep_background &&
+           a.show_blobs == b.show_blobs && a.present == b.present && a.blob_col == b.blob_col && a.perm == b.perm &&
+           a.motion_noise == b.motion_noise && a.only_rank == b.only_rank && a.aux == b.aux &&
+           a.bin_ctas == b.bin_ctas && a.resolve_ctas == b.resolve_ctas;
+}
 
 // Device memory the pair cache may hold (beyond one pair, which is always
 // kept): all K pairs of a 1M-atom, 8-key-frame morph take 450 MB.
@@ -162,6 +192,7 @@ const int *render_perm(RenderWork *w) { return w->perm_set ? w->perm : nullptr; 
 
 void render_invalidate(RenderWork *w) {
     for (auto &d : w->pairs) d.f = -1;
+    drop_ahead(w);
 }
 
 int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope, const int *perm_mx,
@@ -1489,8 +1520,73 @@ int render_positions(RenderWork *w, const RenderScene &sc, double time, uint64_t
     return AM_OK;
 }
 
+// The binning of a fused frame into slot[cur] on stream ps: a plan from the
+// atom count when the slot has none for this frame's shape, then k_frame_bin;
+// when piped, w->binned marks its end on bs.
+static int fused_bin(RenderWork *w, const RenderScene &sc, const FrameArgs &fa, PairData *pd, uint32_t ntiles,
+                     bool piped, cudaStream_t ps, cudaStream_t s) {
+    int rc = ensure_slots(w, sc.N, ntiles, s);
+    if (rc) return rc;
+    RenderWork::Slot *A = &w->slot[w->cur];
+    if (A->tiles != ntiles || A->atoms != sc.N) {
+        // plan from the atom count; the slot's last resolve must be done
+        if (piped) AMG_CUDA(cudaStreamWaitEvent(w->bs, A->resolved, 0));
+        AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, A->off, A->cap, A->cnt, ntiles, std::max<uint64_t>(sc.N, 1),
+                   w->slot_rec_cap, A->ovf_cnt);
+        A->tiles = ntiles;
+        A->atoms = sc.N;
+    }
+    // atoms of the pair: at most N; the active count stays on the device
+    const uint64_t n = sc.N;
+    BinArgs b;
+    b.sc = sc; b.fa = fa; b.n = pd->d_active;
+    b.in = SplatIn{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx, pd->mn};
+    b.rec = A->rec;
+    b.off = A->off; b.cap = A->cap; b.cnt = A->cnt;
+    b.ovf = A->ovf; b.ovf_cnt = A->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->slot_ovf_cap, UINT32_MAX);
+    const unsigned grid = (unsigned)((n + (uint64_t)kBinPer * kBinThreads - 1) / ((uint64_t)kBinPer * kBinThreads));
+    // once per process (thread-safe static initialisation)
+    static const cudaError_t battr = cudaFuncSetAttribute(k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)occupancy_smem(1));
+    AMG_CUDA(battr);
+    if (w->prof) w->prof->open(ps);
+    const size_t bsm = std::max(bin_smem(kBinPer, ntiles), sc.bin_ctas ? occupancy_smem(sc.bin_ctas) : (size_t)0);
+    if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bsm, ps, b);
+    if (w->prof) w->prof->close(PROF_BIN, ps);
+    if (piped) AMG_CUDA(cudaEventRecord(w->binned, w->bs));
+    return AM_OK;
+}
+
+// Bins the frame `nx` ahead of its call, on bs into the slot its tile plan
+// was just made for, when it is a pipelined fused frame of the same tile
+// grid; remembered in w->ahead.
+static int bin_ahead(RenderWork *w, const FrameAhead &nx, uint32_t ntiles_now, cudaStream_t s) {
+    const RenderScene &sc = nx.sc;
+    if (sc.K == 0 || sc.C == 0 || sc.N == 0 || !sc.pipeline || sc.only_rank != 0xFFFFFFFFu) return AM_OK;
+    const size_t f = (size_t)(nx.time * sc.K);
+    if (f >= sc.K) return AM_OK;
+    const uint32_t tiles_x = (sc.width + kTile - 1) / kTile, tiles_y = (sc.height + kTile - 1) / kTile;
+    const uint32_t ntiles = tiles_x * tiles_y;
+    if (ntiles != ntiles_now || ntiles > kBinMaxTiles) return AM_OK;
+    const double dt = 1.0 / double(sc.K);
+    const double t = std::max(0.0, (nx.time - (double)(nx.frame_key * dt)) / dt);
+    PairData *pd = nullptr;
+    int rc = prep_pair(w, sc, (uint32_t)f, w->bs, &pd);
+    if (rc) return rc;
+    FrameArgs fa;
+    if ((rc = frame_args(w, sc, nx.time, (uint32_t)f, t, &fa, w->bs))) return rc;
+    fa.tiles_x = tiles_x;
+    fa.ntiles = ntiles;
+    if ((rc = fused_bin(w, sc, fa, pd, ntiles, true, w->bs, s))) return rc;
+    w->ahead.valid = true;
+    w->ahead.time = nx.time;
+    w->ahead.key = nx.frame_key;
+    w->ahead.sc = sc;
+    return AM_OK;
+}
+
 int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, uint8_t *out,
-                 cudaStream_t s) {
+                 cudaStream_t s, const FrameAhead *ahead) {
     const size_t bytes = (size_t)sc.width * sc.height * 4;
     if (sc.K == 0 || sc.C == 0 || sc.N == 0) {
         AMG_CUDA(cudaMemsetAsync(out, 0, bytes, s));
@@ -1529,57 +1625,38 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
     }
     if (piped) w->s_after_bs = true;
     else w->bs_after_s = true;
+    // a frame binned ahead of this call: its records, when it is this frame
+    bool binned_ahead = false;
+    if (w->ahead.valid) {
+        binned_ahead = piped && time == w->ahead.time && frame_key == w->ahead.key && same_scene(sc, w->ahead.sc);
+        if (binned_ahead) w->ahead.valid = false;
+        else drop_ahead(w);
+    }
     PairData *pd = nullptr;
-    {
+    FrameArgs fa;
+    if (!binned_ahead) {
         int rc = prep_pair(w, sc, (uint32_t)f, ps, &pd);
         if (rc) return rc;
+        if ((rc = frame_args(w, sc, time, (uint32_t)f, t, &fa, ps))) return rc;
+        fa.tiles_x = tiles_x;
+        fa.ntiles = ntiles;
     }
-    FrameArgs fa;
-    {
-        int rc = frame_args(w, sc, time, (uint32_t)f, t, &fa, ps);
-        if (rc) return rc;
-    }
-    fa.tiles_x = tiles_x;
-    fa.ntiles = ntiles;
     // atoms of the pair: at most N; the active count stays on the device
     uint64_t n = sc.N;
-    SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx, pd->mn};
     TileRecs tr;
     RenderWork::Slot *A = nullptr, *B = nullptr;
     if (fused) {
-        {
-            int rc = ensure_slots(w, sc.N, ntiles, s);
+        if (!binned_ahead) {
+            int rc = fused_bin(w, sc, fa, pd, ntiles, piped, ps, s);
             if (rc) return rc;
         }
+        if (piped) AMG_CUDA(cudaStreamWaitEvent(s, w->binned, 0));
         A = &w->slot[w->cur];
         B = &w->slot[w->cur ^ 1];
-        if (A->tiles != ntiles || A->atoms != sc.N) {
-            // plan from the atom count; the slot's last resolve must be done
-            if (piped) AMG_CUDA(cudaStreamWaitEvent(w->bs, A->resolved, 0));
-            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, A->off, A->cap, A->cnt, ntiles,
-                       std::max<uint64_t>(sc.N, 1), w->slot_rec_cap, A->ovf_cnt);
-            A->tiles = ntiles;
-            A->atoms = sc.N;
-        }
-        BinArgs b;
-        b.sc = sc; b.fa = fa; b.n = pd->d_active; b.in = in; b.rec = A->rec;
-        b.off = A->off; b.cap = A->cap; b.cnt = A->cnt;
-        b.ovf = A->ovf; b.ovf_cnt = A->ovf_cnt; b.ovf_cap = (uint32_t)std::min<uint64_t>(w->slot_ovf_cap, UINT32_MAX);
-        const unsigned grid = (unsigned)((n + (uint64_t)kBinPer * kBinThreads - 1) / ((uint64_t)kBinPer * kBinThreads));
-        // once per process (thread-safe static initialisation)
-        static const cudaError_t battr = cudaFuncSetAttribute(k_frame_bin, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                              (int)occupancy_smem(1));
-        AMG_CUDA(battr);
-        if (w->prof) w->prof->open(ps);
-        const size_t bsm = std::max(bin_smem(kBinPer, ntiles), sc.bin_ctas ? occupancy_smem(sc.bin_ctas) : (size_t)0);
-        if (n) AMG_LAUNCH(k_frame_bin, grid, kBinThreads, bsm, ps, b);
-        if (w->prof) w->prof->close(PROF_BIN, ps);
-        if (piped) {
-            AMG_CUDA(cudaEventRecord(w->binned, w->bs));
-            AMG_CUDA(cudaStreamWaitEvent(s, w->binned, 0));
-        }
-        tr = TileRecs{A->rec, A->off, A->cnt, A->cap, A->ovf, A->ovf_cnt, b.ovf_cap};
+        tr = TileRecs{A->rec, A->off, A->cnt, A->cap, A->ovf, A->ovf_cnt,
+                      (uint32_t)std::min<uint64_t>(w->slot_ovf_cap, UINT32_MAX)};
     } else {
+        SplatIn in{pd->pa, pd->pb, pd->col, pd->ls, pd->rank, pd->idx, pd->mn};
         if (ntiles + 1 > w->ntiles_cap) {
             uint32_t **arrs[] = {&w->tile_cnt, &w->tile_off, &w->tile_cur};
             for (uint32_t **q : arrs) {
@@ -1652,6 +1729,11 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         B->tiles = ntiles;
         B->atoms = sc.N;
         w->cur ^= 1;
+        // the frame expected next, binned beside this frame's resolve
+        if (piped && ahead) {
+            int rc = bin_ahead(w, *ahead, ntiles, s);
+            if (rc) return rc;
+        }
     }
     AMG_CUDA(cudaGetLastError());
     return AM_OK;
@@ -1704,6 +1786,7 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s) {
         const RenderJob &J = jobs[i];
         const RenderScene &sc = J.sc;
         RenderWork *w = J.w;
+        drop_ahead(w);  // the caller has waited for the job's own streams
         const size_t bytes = (size_t)sc.width * sc.height * 4;
         const size_t f = (sc.K && sc.C && sc.N) ? (size_t)(J.time * sc.K) : 0;
         if (sc.K == 0 || sc.C == 0 || sc.N == 0 || f >= sc.K) {

@@ -312,8 +312,16 @@ Prof *render_prof(RenderWork *w);  // the timer render_set_prof installed (or nu
 int render_set_perlin(RenderWork *w, const int *perm_lag, const int *perm_slope, const int *perm_mx,
                       const int *perm_my);
 // Renders the frame at normalised time `time` into out (device, width*height*4).
+// A frame render_frame may bin after the frame it renders, beside that
+// frame's resolve, for the call expected next (frames played in order); the
+// next call uses it when it asks for exactly that time and scene.
+struct FrameAhead {
+    RenderScene sc;
+    double time;
+    uint64_t frame_key;
+};
 int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t frame_key, uint8_t *out,
-                 cudaStream_t s);
+                 cudaStream_t s, const FrameAhead *ahead = nullptr);
 // Every atom's position words (x, y) at normalised time `time` into xy
 // (device, 2 * N int32; -1 where the atom is not drawn), as render_frame
 // places them.
