@@ -16,7 +16,7 @@ from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-BAR = 1.005          # the benchmark spec: within 0.5% of the reference's converged cost
+BAR = 1.005          # within 0.5% of the reference's converged cost
 WINDOW = 4000        # sweeps per plateau check
 REL = 2e-5
 MAX_SWEEPS = 120000
