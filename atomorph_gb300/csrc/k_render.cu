@@ -1035,7 +1035,10 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
     const uint4 *__restrict__ rec = tr.rec;
     const uint32_t beg = tr.off[tile], nmain = min(tr.cnt[tile], tr.cap[tile]);
     // overflow records of this tile (normally none)
-    __shared__ uint32_t s_nov;
+    // s_nov: this tile's overflow records (read by every thread below);
+    // s_app: the cache cursor they are appended at (a separate word, so the
+    // append never overwrites the count while a warp may still read it)
+    __shared__ uint32_t s_nov, s_app;
     const uint32_t novf = ovf_total(tr);
     if (novf) {
         if (threadIdx.x == 0) s_nov = 0;
@@ -1071,12 +1074,12 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                     mn = min(mn, rank_of(o, v));
                 }
                 if (novf) {
-                    if (threadIdx.x == 0) s_nov = nmain;
+                    if (threadIdx.x == 0) s_app = nmain;
                     __syncthreads();
                     for (uint32_t j = threadIdx.x; j < novf; j += 256) {
                         const uint4 v = tr.ovf[j];
                         if (ovf_tile(v) != tile) continue;
-                        cache[atomicAdd(&s_nov, 1u)] = v;
+                        cache[atomicAdd(&s_app, 1u)] = v;
                         mn = min(mn, rank_of(o, v));
                     }
                 }

@@ -112,3 +112,38 @@ def test_batch_rejects_a_job_twice(capi, jobs):
     arr = (C.c_void_p * 2)(jobs[0].h, jobs[0].h)
     h = C.c_void_p()
     assert lib.am_batch_create(C.byref(h), arr, 2) == capi.AM_ERR_ARG and not h.value
+
+
+def test_batch_workload_frames_repeatably_equal(capi):
+    """The benchmark's batch workload (32 jobs of 2k-200k atoms, 3-8 key
+    frames, 16 frames each at t = i/16: large jumps, so tile regions planned
+    from the previous frame overflow often): job-by-job device frames and
+    batched frames agree over repeated rounds."""
+    torch = pytest.importorskip("torch")
+    solo, twin = [], []
+    for j in range(32):
+        frames = synth.workload("batch", j)
+        a = capi.Morph()
+        a.load(frames, seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+        assert a.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+        a.refine(20, capi.PROPOSAL_RANDOM)
+        b = capi.Morph()
+        b.load(frames, seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+        b.import_chains(*a.export_chains())
+        solo.append(a)
+        twin.append(b)
+    ts = [i / 16 for i in range(16)]
+    ds = [torch.empty((16, a.height, a.width, 4), dtype=torch.uint8, device="cuda") for a in solo]
+    dt = [torch.empty_like(d) for d in ds]
+    batch = capi.Batch(twin)
+    for rep in range(5):
+        for a, d in zip(solo, ds):
+            for i, t in enumerate(ts):
+                a.render_device(t, d.data_ptr() + i * a.width * a.height * 4)
+        torch.cuda.synchronize()
+        batch.render_device(ts, [d.data_ptr() for d in dt])
+        for j in range(32):
+            assert torch.equal(ds[j], dt[j]), (rep, j)
+    batch.close()
+    for m in solo + twin:
+        m.close()
