@@ -1196,6 +1196,7 @@ int Engine::render_fluid(double t, uint8_t *dst) {
     fr.perm = render_perm(rw);
     fr.fluidsteps = front.fluidsteps;
     fr.seed_key = mix64((uint64_t)seed << 24 ^ 0x666c7569ull);
+    fr.version = publish_count;
     fr.rw = rw;
     return fluid_morph_frame(fmorph, fluid, fr, dst, rstream);
 }

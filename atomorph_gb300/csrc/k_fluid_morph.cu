@@ -70,6 +70,18 @@ struct FluidMorph {
     uint8_t *mem[2] = {nullptr, nullptr};   // [out_w*out_h] 1 where the fluid image has the pixel
     uint64_t frames = 0;             // frames stepped (random key)
     uint32_t *link = nullptr;        // [2][n] source and destination column of each particle's last update
+    // Per column: the Perlin lag, slope and motion-noise pair at its point
+    // of the pair's first key frame (a particle's values are its source
+    // column's), built once per pair and chain state (k_fm_noise).
+    float4 *ntab = nullptr;
+    uint64_t ntab_n = 0;
+    struct {
+        bool valid = false;
+        uint64_t version = 0, seed_key = 0;
+        uint32_t y = 0, fading = 0;
+        bool noise = false;
+        const uint64_t *P = nullptr;
+    } ntab_key;
 };
 
 // draw_fluid options: feather layers, keep_background (the background from
@@ -104,6 +116,7 @@ struct FmArgs {
     float t;                    // local time in the pair
     float sp;                   // sparseness (grid units per pixel)
     uint64_t key;               // random key of this frame
+    const float4 *ntab;         // [N] lag, slope, motion noise x, y per column (k_fm_noise)
     float *PF;                  // particle fields [kFlFields][N]
     uint8_t *flags;             // bit0 active, bit1 mature
     FluidMorph m;
@@ -312,12 +325,36 @@ __global__ void k_fm_assign2(FmArgs a, uint32_t n) {
     }
 }
 
-// update_particle (morph.cpp:680-805) for every active particle.
-__global__ void k_fm_update(FmArgs a) {
+// The per-column table k_fm_update reads: Perlin lag and slope at the
+// column's point of key frame y (morph.cpp:537-545; 0.5 without PERLIN
+// fading) and the motion perturbation's noise pair there (the atom path's).
+__global__ void k_fm_noise(FmArgs a, float4 *tab, int noise) {
     __shared__ int sp[2048];  // lag, slope, motion x, motion y permutations
     for (int i = threadIdx.x; i < 2048; i += blockDim.x) sp[i] = a.perm ? a.perm[i] : 0;
     __syncthreads();
     const float bw = (float)(a.bbox[2] - a.bbox[0] + 1), bh = (float)(a.bbox[3] - a.bbox[1] + 1);
+    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < a.N; x += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t pt1 = a.P[(uint64_t)a.y * a.N + x];
+        float lag = 0.5f, slope = 0.5f, nx = 0.f, ny = 0.f;
+        if (a.fading == AM_PERLIN) {
+            float px = ((float)((int)pt_x(pt1) - (int)a.bbox[0]) * 256.f + (float)pt_xf(pt1)) / (bw * 256.f) * 8.f;
+            float py = ((float)((int)pt_y(pt1) - (int)a.bbox[1]) * 256.f + (float)pt_yf(pt1)) / (bh * 256.f) * 8.f;
+            lag = poctave(sp, px, py) * 0.5f + 0.5f;
+            slope = poctave(sp + 512, px, py) * 0.5f + 0.5f;
+        }
+        if (noise) {
+            const int bwi = (int)(a.bbox[2] - a.bbox[0] + 1), bhi = (int)(a.bbox[3] - a.bbox[1] + 1);
+            const float u = noise_coord_rn((int)pt_x(pt1), (int)pt_xf(pt1), (int)a.bbox[0], bwi);
+            const float v = noise_coord_rn((int)pt_y(pt1), (int)pt_yf(pt1), (int)a.bbox[1], bhi);
+            nx = poctave_rn(sp + 1024, u, v);
+            ny = poctave_rn(sp + 1536, u, v);
+        }
+        tab[x] = make_float4(lag, slope, nx, ny);
+    }
+}
+
+// update_particle (morph.cpp:680-805) for every active particle.
+__global__ void k_fm_update(FmArgs a) {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < a.N; s += (uint64_t)gridDim.x * blockDim.x) {
         const uint8_t fl = a.flags[s];
         if (!(fl & 1u)) continue;
@@ -344,14 +381,8 @@ __global__ void k_fm_update(FmArgs a) {
             c1 = c2;
             if (S0 > 0.f) c1 &= 0x00FFFFFFu;
         }
-        float lag = 0.5f, slope = 0.5f;
-        if (a.fading == AM_PERLIN) {
-            float px = ((float)((int)pt_x(pt1) - (int)a.bbox[0]) * 256.f + (float)pt_xf(pt1)) / (bw * 256.f) * 8.f;
-            float py = ((float)((int)pt_y(pt1) - (int)a.bbox[1]) * 256.f + (float)pt_yf(pt1)) / (bh * 256.f) * 8.f;
-            lag = poctave(sp, px, py) * 0.5f + 0.5f;
-            slope = poctave(sp + 512, px, py) * 0.5f + 0.5f;
-        }
-        const uint32_t col = fade_colour(a.fading, c1, c2, fade_params(lag, slope), 1.f - a.t);
+        const float4 nt = a.ntab[src_x];  // lag, slope, motion noise at the source column's point
+        const uint32_t col = fade_colour(a.fading, c1, c2, fade_params(nt.x, nt.y), 1.f - a.t);
         // attractor: the source column's trajectory point at this time
         uint32_t X = (uint32_t)pt_X(pt1), Y = (uint32_t)pt_Y(pt1);
         if (a.motion == AM_LINEAR) {
@@ -368,11 +399,8 @@ __global__ void k_fm_update(FmArgs a) {
         }
         if (a.fa.noise_s != 0.f) {
             // the Perlin motion perturbation of the atom render, at the source point
-            const int bwi = (int)(a.bbox[2] - a.bbox[0] + 1), bhi = (int)(a.bbox[3] - a.bbox[1] + 1);
-            const float u = noise_coord_rn((int)pt_x(pt1), (int)pt_xf(pt1), (int)a.bbox[0], bwi);
-            const float v = noise_coord_rn((int)pt_y(pt1), (int)pt_yf(pt1), (int)a.bbox[1], bhi);
-            X = displace_rn(X, a.fa.noise_s, poctave_rn(sp + 1024, u, v));
-            Y = displace_rn(Y, a.fa.noise_s, poctave_rn(sp + 1536, u, v));
+            X = displace_rn(X, a.fa.noise_s, nt.z);
+            Y = displace_rn(Y, a.fa.noise_s, nt.w);
         }
         const float ptx = (float)(X >> 8) + (float)(X & 255u) / 256.f;
         const float pty = (float)(Y >> 8) + (float)(Y & 255u) / 256.f;
@@ -576,7 +604,7 @@ void fluid_morph_destroy(FluidMorph *m) {
     void *ps[] = {m->frame_key, m->src_pos, m->dst_pos, m->owner, m->src_map, m->dst_map, m->src_cnt, m->dst_cnt,
                   m->src_any, m->flags_a, m->flags_b, m->slot_by_rank, m->ckeys, m->cvals, m->tk, m->tv, m->hist,
                   m->chain_cnt, m->to_create, m->to_delete, m->phase1, m->ncand, m->acc, m->col[0], m->col[1],
-                  m->mem[0], m->mem[1], m->link};
+                  m->mem[0], m->mem[1], m->link, m->ntab};
     for (void *p : ps)
         if (p) cudaFree(p);
     delete m;
@@ -790,6 +818,31 @@ int fluid_morph_frame(FluidMorph *m, FluidDev *fl, const FluidFrame &fr_in, uint
             if ((rc = radix_sort_pairs(m->ckeys, m->cvals, m->tk, m->tv, m->hist, nc, cbits, s))) return rc;
             AMG_LAUNCH(k_fm_assign2, g2, 256, 0, s, a, nc);
         }
+    }
+    {
+        // the per-column noise table of this pair and chain state
+        const bool noise = sc.motion_noise > 0.0;
+        auto &k = m->ntab_key;
+        if (!k.valid || k.version != fr_in.version || k.seed_key != fr_in.seed_key || k.y != a.y ||
+            k.fading != sc.fading || k.noise != noise || k.P != sc.P || m->ntab_n < N) {
+            if (m->ntab_n < N) {
+                if (m->ntab) cudaFree(m->ntab);
+                m->ntab = nullptr;
+                m->ntab_n = 0;
+                k.valid = false;
+                AMG_ALLOC(&m->ntab, std::max<uint64_t>(N, 1) * sizeof(float4));
+                m->ntab_n = N;
+            }
+            AMG_LAUNCH(k_fm_noise, g, 256, 0, s, a, m->ntab, noise ? 1 : 0);
+            k.valid = true;
+            k.version = fr_in.version;
+            k.seed_key = fr_in.seed_key;
+            k.y = a.y;
+            k.fading = sc.fading;
+            k.noise = noise;
+            k.P = sc.P;
+        }
+        a.ntab = m->ntab;
     }
     AMG_LAUNCH(k_fm_update, g, 256, 0, s, a);
     if (prof) prof->close(PROF_FLUID_MANAGE, s);

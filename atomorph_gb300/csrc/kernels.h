@@ -379,6 +379,7 @@ struct FluidFrame {
     const int *perm;                  // Perlin lag / slope permutations (device)
     uint32_t fluidsteps;
     uint64_t seed_key;
+    uint64_t version;                 // changes whenever the published chains change
     RenderWork *rw;                   // frame arithmetic tables
 };
 FluidMorph *fluid_morph_create();
