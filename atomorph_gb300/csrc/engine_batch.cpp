@@ -13,6 +13,15 @@ Batch::Batch(std::vector<Engine *> jobs) : jobs_(std::move(jobs)) {}
 
 Batch::~Batch() {
     drop_graphs();
+    for (cudaEvent_t e : ev_bin_) cudaEventDestroy(e);
+    for (auto &v : ev_res_)
+        for (cudaEvent_t e : v) cudaEventDestroy(e);
+    for (int k = 0; k < 2; ++k) {
+        if (ev_time_[k]) cudaEventDestroy(ev_time_[k]);
+        if (ev_copied_[k]) cudaEventDestroy(ev_copied_[k]);
+    }
+    if (bstream_) cudaStreamDestroy(bstream_);
+    if (cstream_) cudaStreamDestroy(cstream_);
     if (h_jobs_) cudaFreeHost(h_jobs_);
     if (h_ljobs_) cudaFreeHost(h_ljobs_);
     if (h_gains_) cudaFreeHost(h_gains_);
@@ -597,11 +606,33 @@ int Batch::tune(size_t trial_sweeps) {
 
 namespace amg {
 
-// Frames of every job at the times ts: per time, the atom frames of all jobs
-// through render_frames_batch (one binning, one resolve and one tile-plan
-// launch for up to 32 jobs), fluid frames and frames before chains through
-// each job's own render.  Host destinations the GPU can store into (pinned,
-// mapped) are written directly; others receive a copy from a staging frame.
+// Streams and events of the pipelined batched frames, for `groups` launch
+// groups of up to 32 jobs.
+int Batch::ensure_render_streams(uint32_t groups) {
+    if (!bstream_) AMG_CUDA(cudaStreamCreateWithFlags(&bstream_, cudaStreamNonBlocking));
+    if (!cstream_) AMG_CUDA(cudaStreamCreateWithFlags(&cstream_, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+        if (!ev_time_[k]) AMG_CUDA(cudaEventCreateWithFlags(&ev_time_[k], cudaEventDisableTiming));
+        if (!ev_copied_[k]) AMG_CUDA(cudaEventCreateWithFlags(&ev_copied_[k], cudaEventDisableTiming));
+    }
+    while (ev_bin_.size() < groups) {
+        cudaEvent_t e[3];
+        for (auto &x : e) AMG_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+        ev_bin_.push_back(e[0]);
+        ev_res_[0].push_back(e[1]);
+        ev_res_[1].push_back(e[2]);
+    }
+    return AM_OK;
+}
+
+// Frames of every job at the times ts, pipelined over the times: the atom
+// frames of all jobs per time through render_frames_batch (one binning, one
+// resolve and one tile-plan launch per group of up to 32 jobs), time i's
+// binning on a second stream beside time i-1's resolve; fluid frames and
+// frames before chains through each job's own render.  Host destinations
+// the GPU can store into (pinned, mapped) are written directly; others get a
+// copy from one of two staging frames per job, issued on a copy stream after
+// the next time's launches so the pipeline keeps running.
 int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_device) {
     if (n == 0) return AM_OK;
     if (!ts || !outs) return AM_ERR_ARG;
@@ -613,7 +644,7 @@ int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_devi
     const size_t nj = jobs_.size();
     std::vector<size_t> fsz(nj), stage_off(nj, SIZE_MAX);
     std::vector<uint8_t *> base(nj);
-    size_t stage_bytes = 0;
+    size_t half = 0;
     int rc;
     for (size_t j = 0; j < nj; ++j) {
         Engine *e = jobs_[j];
@@ -628,20 +659,39 @@ int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_devi
             if (d) {
                 base[j] = d;
             } else {
-                stage_off[j] = stage_bytes;
-                stage_bytes += (fsz[j] + 255) / 256 * 256;
+                stage_off[j] = half;
+                half += (fsz[j] + 255) / 256 * 256;
             }
         }
     }
-    if (stage_bytes && (rc = stage_.reserve(stage_bytes))) return rc;
+    if (half && (rc = stage_.reserve(2 * half))) return rc;
+    const uint32_t groups = (uint32_t)(nj + 2);  // launch groups per time: at most one per job
+    if ((rc = ensure_render_streams(groups))) return rc;
+    // bstream_ starts after the work already on stream_ (earlier calls)
+    AMG_CUDA(cudaEventRecord(ev_time_[1], stream_));
+    AMG_CUDA(cudaStreamWaitEvent(bstream_, ev_time_[1], 0));
     std::vector<RenderJob> rj;
     rj.reserve(nj);
-    std::vector<char> batched(nj);
+    std::vector<char> batched(nj), was_batched(nj);
+    auto copy_out = [&](size_t i) -> int {
+        // time i's staged frames, once its resolves are done
+        bool any = false;
+        for (size_t j = 0; j < nj; ++j) any |= was_batched[j] && stage_off[j] != SIZE_MAX;
+        if (!any) return AM_OK;
+        AMG_CUDA(cudaStreamWaitEvent(cstream_, ev_time_[i & 1], 0));
+        for (size_t j = 0; j < nj; ++j)
+            if (was_batched[j] && stage_off[j] != SIZE_MAX)
+                AMG_CUDA(cudaMemcpyAsync(outs[j] + i * fsz[j], stage_.p + (i & 1) * half + stage_off[j], fsz[j],
+                                         cudaMemcpyDeviceToHost, cstream_));
+        AMG_CUDA(cudaEventRecord(ev_copied_[i & 1], cstream_));
+        return AM_OK;
+    };
     for (size_t i = 0; i < n; ++i) {
         double integ;
         double t = std::modf(ts[i], &integ);
         if (t < 0.0) t += 1.0;
         rj.clear();
+        bool staged = false;
         for (size_t j = 0; j < nj; ++j) {
             Engine *e = jobs_[j];
             batched[j] = 0;
@@ -651,7 +701,11 @@ int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_devi
                 if ((rc = e->render(ts[i], outs[j] + i * fsz[j], on_device))) return rc;
                 AMG_CUDA(cudaStreamSynchronize(e->rstream));
             } else {
-                uint8_t *dst = stage_off[j] != SIZE_MAX ? stage_.p + stage_off[j] : base[j] + i * fsz[j];
+                uint8_t *dst = base[j] + i * fsz[j];
+                if (stage_off[j] != SIZE_MAX) {
+                    dst = stage_.p + (i & 1) * half + stage_off[j];
+                    staged = true;
+                }
                 RenderJob r;
                 r.w = e->rw;
                 e->frame_scene(t, r.sc, &r.frame_key);
@@ -661,13 +715,18 @@ int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_devi
                 batched[j] = 1;
             }
         }
-        if ((rc = render_frames_batch(rj.data(), rj.size(), stream_))) return rc;
-        for (size_t j = 0; j < nj; ++j)
-            if (batched[j] && stage_off[j] != SIZE_MAX)
-                AMG_CUDA(cudaMemcpyAsync(outs[j] + i * fsz[j], stage_.p + stage_off[j], fsz[j], cudaMemcpyDeviceToHost,
-                                         stream_));
+        // this staging half was last copied out two times ago
+        if (staged && i >= 2) AMG_CUDA(cudaStreamWaitEvent(stream_, ev_copied_[i & 1], 0));
+        BatchPipe bp{bstream_, ev_bin_.data(), {ev_res_[0].data(), ev_res_[1].data()}, groups, (int)(i & 1), i > 0};
+        if ((rc = render_frames_batch(rj.data(), rj.size(), stream_, &bp))) return rc;
+        AMG_CUDA(cudaEventRecord(ev_time_[i & 1], stream_));
+        if (i > 0 && (rc = copy_out(i - 1))) return rc;
+        was_batched = batched;
     }
+    if ((rc = copy_out(n - 1))) return rc;
+    AMG_CUDA(cudaStreamSynchronize(bstream_));
     AMG_CUDA(cudaStreamSynchronize(stream_));
+    AMG_CUDA(cudaStreamSynchronize(cstream_));
     return AM_OK;
 }
 

@@ -1406,9 +1406,13 @@ static int prep_pair(RenderWork *w, const RenderScene &sc, uint32_t f, cudaStrea
 // Record slots large enough for a fused frame of n atoms over ntiles tiles:
 // the planned tile regions (about 1.25 x the records of a frame plus slack;
 // at most 4 records per atom) and an overflow list of 4 per atom, per slot.
+static bool slots_fit(const RenderWork *w, uint64_t n, uint32_t ntiles) {
+    const uint64_t need = n * 5 + (uint64_t)ntiles * 64 + 16, need_ovf = n * 4 + 16;
+    return need <= w->slot_rec_cap && need_ovf <= w->slot_ovf_cap && ntiles <= w->slot_tiles_cap;
+}
 static int ensure_slots(RenderWork *w, uint64_t n, uint32_t ntiles, cudaStream_t s) {
     const uint64_t need = n * 5 + (uint64_t)ntiles * 64 + 16, need_ovf = n * 4 + 16;
-    if (need > w->slot_rec_cap || need_ovf > w->slot_ovf_cap || ntiles > w->slot_tiles_cap) {
+    if (!slots_fit(w, n, ntiles)) {
         // frames in flight read the old buffers
         if (w->bs) AMG_CUDA(cudaStreamSynchronize(w->bs));
         AMG_CUDA(cudaStreamSynchronize(s));
@@ -1743,7 +1747,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
 }
 
 
-int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s) {
+int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const BatchPipe *pipe) {
     static const cudaError_t battr = cudaFuncSetAttribute(
         k_frame_bin_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)occupancy_smem(1));
     static const cudaError_t rattr = cudaFuncSetAttribute(
@@ -1765,15 +1769,34 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s) {
     std::vector<Flip> flips;
     uint32_t bin_ctas = 0, tiles = 0;
     size_t bsm = 0, rsm = 0;
+    // Pipelined (pipe given): pair preparation, binning and the next tile
+    // plans of launch group c run on pipe->bs, its resolve on s; the plans
+    // wait for the group's previous resolve, which last read the slots they
+    // fill, so a time's binning runs beside the previous time's resolve.
+    const cudaStream_t ps = pipe ? pipe->bs : s;
+    uint32_t group = 0;
     auto flush = [&]() -> int {
         if (pb.n == 0) return AM_OK;
         bb.n = rb.n = pb.n;
         bb.start[bb.n] = bin_ctas;
         rb.start[rb.n] = tiles;
-        if (bin_ctas) AMG_LAUNCH(k_frame_bin_batch, bin_ctas, kBinThreads, bsm, s, bb);
+        if (pipe && group >= pipe->groups) {
+            set_error("render_frames_batch: more launch groups than events");
+            return AM_ERR_ARG;
+        }
+        if (bin_ctas) AMG_LAUNCH(k_frame_bin_batch, bin_ctas, kBinThreads, bsm, ps, bb);
+        if (pipe) {
+            AMG_CUDA(cudaEventRecord(pipe->binned[group], ps));
+            AMG_CUDA(cudaStreamWaitEvent(s, pipe->binned[group], 0));
+        }
         AMG_LAUNCH(k_frame_resolve_batch, tiles, 256, rsm, s, rb);
-        AMG_LAUNCH(k_tile_plan_batch, pb.n, 1024, 0, s, pb);
+        if (pipe) {
+            AMG_CUDA(cudaEventRecord(pipe->resolved[pipe->parity][group], s));
+            if (pipe->has_prev) AMG_CUDA(cudaStreamWaitEvent(ps, pipe->resolved[pipe->parity ^ 1][group], 0));
+        }
+        AMG_LAUNCH(k_tile_plan_batch, pb.n, 1024, 0, ps, pb);
         AMG_CUDA(cudaGetLastError());
+        ++group;
         for (const Flip &fl : flips) {
             fl.B->tiles = fl.ntiles;
             fl.B->atoms = fl.atoms;
@@ -1816,17 +1839,19 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s) {
         const double dt = 1.0 / double(sc.K);
         const double t = std::max(0.0, (J.time - (double)(J.frame_key * dt)) / dt);
         PairData *pd = nullptr;
-        int rc = prep_pair(w, sc, (uint32_t)f, s, &pd);
+        int rc = prep_pair(w, sc, (uint32_t)f, ps, &pd);
         if (rc) return rc;
         const uint32_t k = pb.n;
         BinArgs &b = bb.job[k];
-        if ((rc = frame_args(w, sc, J.time, (uint32_t)f, t, &b.fa, s))) return rc;
+        if ((rc = frame_args(w, sc, J.time, (uint32_t)f, t, &b.fa, ps))) return rc;
         b.fa.tiles_x = tiles_x;
         b.fa.ntiles = ntiles;
+        // slots too small are reallocated: nothing in flight may still use them
+        if (pipe && !slots_fit(w, sc.N, ntiles)) AMG_CUDA(cudaStreamSynchronize(pipe->bs));
         if ((rc = ensure_slots(w, sc.N, ntiles, s))) return rc;
         RenderWork::Slot *A = &w->slot[w->cur], *B = &w->slot[w->cur ^ 1];
         if (A->tiles != ntiles || A->atoms != sc.N) {
-            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, s, A->cnt, A->off, A->cap, A->cnt, ntiles,
+            AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, A->off, A->cap, A->cnt, ntiles,
                        std::max<uint64_t>(sc.N, 1), w->slot_rec_cap, A->ovf_cnt);
             A->tiles = ntiles;
             A->atoms = sc.N;

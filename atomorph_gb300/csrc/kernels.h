@@ -349,7 +349,20 @@ struct RenderJob {
 // (no chains, tile grids above the fused limit, one blob alone) are rendered
 // one by one on s.  Every frame equals render_frame's for its morph.  Each
 // morph's own render streams must be idle.
-int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s);
+// Two-stream form of render_frames_batch for consecutive times: bs runs the
+// pair preparation, binning and next tile plans, s the resolves; binned[g]
+// and resolved[parity][g] order launch group g (up to 32 frames) between
+// them, parity alternating with the time, has_prev when the previous time
+// of the same groups was rendered this way (its resolves gate the plans).
+struct BatchPipe {
+    cudaStream_t bs;
+    const cudaEvent_t *binned;
+    const cudaEvent_t *resolved[2];
+    uint32_t groups;
+    int parity;
+    bool has_prev;
+};
+int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const BatchPipe *pipe = nullptr);
 
 // ---- k_fluid.cu: FluidModel::step in FP32
 struct FluidDev;
