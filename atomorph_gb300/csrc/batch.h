@@ -73,10 +73,11 @@ class Batch {
     std::map<size_t, Graph> lgraphs_;
     // batched frames: staging for host memory the GPU cannot store into
     // (two halves, alternating with the time), the binning stream, the copy
-    // stream and their events (per launch group, per time parity)
+    // stream and their events (binned per launch group; a time's resolves
+    // done and its copies done, per time parity)
     DBuf<uint8_t> stage_;
     cudaStream_t bstream_ = nullptr, cstream_ = nullptr;
-    std::vector<cudaEvent_t> ev_bin_, ev_res_[2];
+    std::vector<cudaEvent_t> ev_bin_;
     cudaEvent_t ev_time_[2] = {nullptr, nullptr}, ev_copied_[2] = {nullptr, nullptr};
     int ensure_render_streams(uint32_t groups);
 };

@@ -14,8 +14,6 @@ Batch::Batch(std::vector<Engine *> jobs) : jobs_(std::move(jobs)) {}
 Batch::~Batch() {
     drop_graphs();
     for (cudaEvent_t e : ev_bin_) cudaEventDestroy(e);
-    for (auto &v : ev_res_)
-        for (cudaEvent_t e : v) cudaEventDestroy(e);
     for (int k = 0; k < 2; ++k) {
         if (ev_time_[k]) cudaEventDestroy(ev_time_[k]);
         if (ev_copied_[k]) cudaEventDestroy(ev_copied_[k]);
@@ -616,11 +614,9 @@ int Batch::ensure_render_streams(uint32_t groups) {
         if (!ev_copied_[k]) AMG_CUDA(cudaEventCreateWithFlags(&ev_copied_[k], cudaEventDisableTiming));
     }
     while (ev_bin_.size() < groups) {
-        cudaEvent_t e[3];
-        for (auto &x : e) AMG_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
-        ev_bin_.push_back(e[0]);
-        ev_res_[0].push_back(e[1]);
-        ev_res_[1].push_back(e[2]);
+        cudaEvent_t e;
+        AMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ev_bin_.push_back(e);
     }
     return AM_OK;
 }
@@ -717,7 +713,7 @@ int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_devi
         }
         // this staging half was last copied out two times ago
         if (staged && i >= 2) AMG_CUDA(cudaStreamWaitEvent(stream_, ev_copied_[i & 1], 0));
-        BatchPipe bp{bstream_, ev_bin_.data(), {ev_res_[0].data(), ev_res_[1].data()}, groups, (int)(i & 1), i > 0};
+        BatchPipe bp{bstream_, ev_bin_.data(), groups, i > 0 ? ev_time_[(i - 1) & 1] : nullptr};
         if ((rc = render_frames_batch(rj.data(), rj.size(), stream_, &bp))) return rc;
         AMG_CUDA(cudaEventRecord(ev_time_[i & 1], stream_));
         if (i > 0 && (rc = copy_out(i - 1))) return rc;

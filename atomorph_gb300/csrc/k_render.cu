@@ -1770,9 +1770,9 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
     uint32_t bin_ctas = 0, tiles = 0;
     size_t bsm = 0, rsm = 0;
     // Pipelined (pipe given): pair preparation, binning and the next tile
-    // plans of launch group c run on pipe->bs, its resolve on s; the plans
-    // wait for the group's previous resolve, which last read the slots they
-    // fill, so a time's binning runs beside the previous time's resolve.
+    // plans run on pipe->bs, the resolves on s; the plans wait for the
+    // previous time's resolves, which last read the slots they fill, so a
+    // time's binning runs beside the previous time's resolve.
     const cudaStream_t ps = pipe ? pipe->bs : s;
     uint32_t group = 0;
     auto flush = [&]() -> int {
@@ -1790,10 +1790,7 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
             AMG_CUDA(cudaStreamWaitEvent(s, pipe->binned[group], 0));
         }
         AMG_LAUNCH(k_frame_resolve_batch, tiles, 256, rsm, s, rb);
-        if (pipe) {
-            AMG_CUDA(cudaEventRecord(pipe->resolved[pipe->parity][group], s));
-            if (pipe->has_prev) AMG_CUDA(cudaStreamWaitEvent(ps, pipe->resolved[pipe->parity ^ 1][group], 0));
-        }
+        if (pipe && pipe->prev_resolved && group == 0) AMG_CUDA(cudaStreamWaitEvent(ps, pipe->prev_resolved, 0));
         AMG_LAUNCH(k_tile_plan_batch, pb.n, 1024, 0, ps, pb);
         AMG_CUDA(cudaGetLastError());
         ++group;

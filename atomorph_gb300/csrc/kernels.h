@@ -351,16 +351,14 @@ struct RenderJob {
 // morph's own render streams must be idle.
 // Two-stream form of render_frames_batch for consecutive times: bs runs the
 // pair preparation, binning and next tile plans, s the resolves; binned[g]
-// and resolved[parity][g] order launch group g (up to 32 frames) between
-// them, parity alternating with the time, has_prev when the previous time
-// of the same groups was rendered this way (its resolves gate the plans).
+// orders launch group g (up to 32 frames) between them, and the plans wait
+// for prev_resolved (recorded on s after the previous time's resolves, the
+// last readers of the slots the plans fill; null for the first time).
 struct BatchPipe {
     cudaStream_t bs;
     const cudaEvent_t *binned;
-    const cudaEvent_t *resolved[2];
     uint32_t groups;
-    int parity;
-    bool has_prev;
+    cudaEvent_t prev_resolved;
 };
 int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const BatchPipe *pipe = nullptr);
 
