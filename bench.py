@@ -72,27 +72,39 @@ def _profiled_traffic(kernel):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling around the timed region: sampling starts before
+    it (nvidia-smi takes a moment to start) every 20 ms with timestamps, the
+    region's wall-clock bounds are marked, and the summary keeps the samples
+    taken inside it (the nearest one when none falls inside)."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, path):
         self.path = path
         self.p = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "20"], stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)  # let the sampler start before the region
         except Exception:
             self.p = None
         return self
 
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
+
     def __exit__(self, *a):
         if self.p:
+            time.sleep(0.1)
             self.p.terminate()
             try:
                 self.p.wait(timeout=5)
@@ -101,21 +113,35 @@ class Clocks:
             self.f.close()
 
     def summary(self, gpu_index=0):
+        import datetime
         try:
             rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
         except Exception:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        rows = [r for r in rows if len(r) >= 9 and r[0].strip() == str(gpu_index)]
+        rows = [r for r in rows if len(r) >= 10 and r[1].strip() == str(gpu_index)]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in rows]
+
+        def when(r):
+            try:
+                return datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                return None
+        inside = rows
+        if self.t0 is not None and self.t1 is not None:
+            stamped = [(when(r), r) for r in rows]
+            inside = [r for w, r in stamped if w is not None and self.t0 <= w <= self.t1]
+            if not inside:
+                later = [(w, r) for w, r in stamped if w is not None and w >= self.t0]
+                inside = [min(later, key=lambda x: x[0])[1]] if later else rows[-1:]
+        sm = [float(r[2]) for r in inside]
         reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            for n, v in zip(names, r[5:9]):
+        for r in inside:
+            for n, v in zip(names, r[6:10]):
                 if v.strip().lower() == "active":
                     reasons.add(n)
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "samples": len(rows),
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(inside[0][3]), "samples": len(inside),
                 "reasons": sorted(reasons)}
 
 
@@ -238,12 +264,14 @@ def bench_ours(args, rank, world):
     e1 = torch.cuda.Event(enable_timing=True)
     with Clocks(os.path.join(args.clocks_dir, f"clocks_rank{rank}.csv")) as clk:
         torch.cuda.synchronize()
+        clk.mark_start()
         e0.record(stream)
         for _ in range(args.steps):
             step()
         e1.record(stream)
         stream.synchronize()
         torch.cuda.synchronize()
+        clk.mark_end()
     ms = e0.elapsed_time(e1)
     launches = capi.launch_count() - launches0
     ms = max_over_ranks(ms, world)
@@ -923,7 +951,7 @@ def profile_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--refine-sweeps", type=int, default=100)
