@@ -98,7 +98,7 @@ int am_set_degeneration(am_morph *m, size_t d);              /* morph.h:62 */
 int am_set_motion(am_morph *m, unsigned motion);             /* morph.h:63 */
 int am_set_fading(am_morph *m, unsigned fading);             /* morph.h:64 */
 int am_set_threads(am_morph *m, size_t t);                   /* morph.h:65 (accepted; GPU width is automatic) */
-int am_set_cycle_length(am_morph *m, size_t c);              /* morph.h:66 (proposals per atom step, see DESIGN) */
+int am_set_cycle_length(am_morph *m, size_t c);              /* morph.h:66: stored; a worker step here runs am_set_sweeps whole sweeps instead of cycle_length random proposals */
 /* Feather fades each blob's outer f layers (morph.cpp:625-674; the fluid
  * path grows f layers outward, morph.cpp:1204-1266); f <= 96, larger values
  * return AM_ERR_UNSUPPORTED. */
