@@ -637,6 +637,10 @@ int Batch::render(const double *ts, size_t n, uint8_t *const *outs, bool on_devi
         if (jobs_[j]->is_busy()) return AM_ERR_BUSY;
     }
     AMG_CUDA(cudaSetDevice(device_));
+    // work a failed earlier call may have left on the batch's own streams
+    if (bstream_) AMG_CUDA(cudaStreamSynchronize(bstream_));
+    if (cstream_) AMG_CUDA(cudaStreamSynchronize(cstream_));
+    AMG_CUDA(cudaStreamSynchronize(stream_));
     const size_t nj = jobs_.size();
     std::vector<size_t> fsz(nj), stage_off(nj, SIZE_MAX);
     std::vector<uint8_t *> base(nj);
