@@ -207,7 +207,7 @@ def test_render_into_pinned_host_memory_matches_pageable(capi):
             assert np.array_equal(got, want), (t, off)
 
 
-@pytest.mark.parametrize("resolution", [(1600, 1500), (300, 200)])
+@pytest.mark.parametrize("resolution", [(1600, 1500), (300, 200), (302, 199)])
 def test_render_other_resolutions_match_oracle(capi, oracle, resolution):
     """Outputs above 2048 tiles of 32x32 px take the separate splat / scan /
     scatter kernels instead of the fused binning; an output smaller than the
@@ -231,6 +231,31 @@ def test_render_other_resolutions_match_oracle(capi, oracle, resolution):
         worst, ndiff = _lsb(got, ref)
         assert worst <= 1, f"t={t}: worst {worst}, {ndiff} channels differ"
         assert ndiff <= max(16, ref.size // 200)
+
+
+@pytest.mark.parametrize("offset", [4, 8, 12, 16])
+def test_device_frames_at_unaligned_offsets(capi, offset):
+    """Device destinations that start off a 16-byte boundary, in a frame whose
+    width and height are no multiples of 4 or of the 32-pixel tile (302 x 199)
+    and in a square one: the same pixels as the host frame, and nothing
+    written outside the destination."""
+    torch = pytest.importorskip("torch")
+    frames = synth.workload("shapes256")
+    m = capi.Morph()
+    m.load(frames, seed=3, blob_delimiter=1, motion=4, fading=6)
+    assert m.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+    m.refine(20)
+    for res in ((302, 199), (256, 256)):
+        m.set(resolution=res)
+        fb = m.width * m.height * 4
+        buf = torch.zeros(offset + fb + 64, dtype=torch.uint8, device="cuda")
+        for t in (0.2, 0.7):
+            want = m.render(t)
+            m.render_device(t, buf.data_ptr() + offset)
+            assert m.lib.am_device_sync(m.h) == capi.AM_OK
+            got = buf.cpu().numpy()
+            assert not got[:offset].any() and not got[offset + fb:].any(), (res, t)
+            assert np.array_equal(got[offset:offset + fb].reshape(m.height, m.width, 4), want), (res, t)
 
 
 @pytest.mark.parametrize("motion", [2, 3, 4])
