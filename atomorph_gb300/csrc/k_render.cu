@@ -1014,7 +1014,6 @@ __host__ __device__ inline size_t feather_smem(uint32_t F) {
 // Stacked records of an uncached tile are reduced in the warp when at least
 // kStackMin of a warp's 32 share a base pixel (the accumulation in
 // frame_resolve).
-constexpr bool kStackReduce = true;
 constexpr uint32_t kStackMin = 4;
 
 // The resolve of one 32 x 32 tile of a frame.
@@ -1139,7 +1138,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                     }
                 }
             };
-            if (kStackReduce && !cached) {
+            if (!cached) {
                 // A tile too full for the record cache usually holds atoms
                 // stacked on one pixel (a chain much wider than a key frame's
                 // blob collapses onto that blob's pixels).  The records of a
