@@ -25,6 +25,7 @@ PROPOSAL_RANDOM, PROPOSAL_LOCAL, PROPOSAL_LEARNED, PROPOSAL_SCORED = range(4)
 u8p = C.POINTER(C.c_uint8)
 u64p = C.POINTER(C.c_uint64)
 i32p = C.POINTER(C.c_int32)
+u32p = C.POINTER(C.c_uint32)
 f64p = C.POINTER(C.c_double)
 f32p = C.POINTER(C.c_float)
 vp = C.c_void_p
@@ -137,6 +138,7 @@ _SIGS = {
     "am_profile_enable": (C.c_int, [vp, C.c_int]),
     "am_profile_read": (C.c_size_t, [vp, C.POINTER(C.c_char_p), f64p, u64p, C.c_size_t]),
     "am_launch_count": (C.c_uint64, []),
+    "am_get_heavy_tiles": (C.c_int, [vp, u32p, u32p]),
     "am_device_sync": (C.c_int, [vp]),
 }
 
@@ -474,6 +476,13 @@ class Morph:
         n = np.zeros(16, np.uint64)
         k = self.lib.am_profile_read(self.h, names, _p(ms, f64p), _p(n, u64p), 16)
         return {names[i].decode(): (float(ms[i]), int(n[i])) for i in range(k)}
+
+    def heavy_tiles(self) -> tuple:
+        """(heavy tiles of the last frame that had any, helper CTAs of the last
+        resolve): tiles resolved in row bands by helper CTAs."""
+        tiles, helpers = C.c_uint32(0), C.c_uint32(0)
+        _check(self.lib.am_get_heavy_tiles(self.h, C.byref(tiles), C.byref(helpers)), "am_get_heavy_tiles")
+        return tiles.value, helpers.value
 
     @property
     def stream(self) -> int:

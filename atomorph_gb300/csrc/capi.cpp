@@ -454,6 +454,11 @@ size_t am_profile_read(am_morph *m, const char **names, double *ms, uint64_t *la
 }
 void *am_get_stream(am_morph *m) { return m ? (void *)m->e.rstream : nullptr; }
 uint64_t am_launch_count(void) { return amg::g_launches.load(); }
+int am_get_heavy_tiles(am_morph *m, uint32_t *tiles, uint32_t *helpers) {
+    if (!m) return AM_ERR_ARG;
+    amg::render_heavy_tiles(H(m).rw, tiles, helpers);
+    return AM_OK;
+}
 int am_device_sync(am_morph *m) {
     CHECK(m);
     if (m->e.stream) { cudaError_t x = cudaStreamSynchronize(m->e.stream); if (x) return AM_ERR_CUDA; }

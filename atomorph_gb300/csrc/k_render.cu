@@ -101,6 +101,11 @@ struct RenderWork {
         uint64_t key = 0;
         RenderScene sc;
     } ahead;
+    // Heavy tiles: the resolves' count of this morph's frames and the note
+    // its heavy tiles leave (host-mapped: frame number << 32 | heavy tiles).
+    uint32_t frame_no = 0, last_helpers = 0;
+    unsigned long long *note_host = nullptr, *note_dev = nullptr;
+    bool note_tried = false;
 };
 
 // Drops a frame binned ahead: the slot it filled is planned afresh by the
@@ -185,6 +190,7 @@ void render_work_destroy(RenderWork *w) {
     if (w->binned) cudaEventDestroy(w->binned);
     if (w->mark) cudaEventDestroy(w->mark);
     if (w->bs) cudaStreamDestroy(w->bs);
+    if (w->note_host) cudaFreeHost(w->note_host);
     delete w;
 }
 
@@ -729,21 +735,48 @@ __global__ void __launch_bounds__(kBinThreads) k_frame_bin_batch(const __grid_co
     frame_bin(bb.job[j], blockIdx.x - bb.start[j]);
 }
 
+// Heavy tiles: a tile with more than kHeavyRec binned records (atoms crowded
+// or stacked by a chain much wider than a key frame's blob) would keep one
+// CTA busy for milliseconds while the rest of the frame is done, its warps
+// waiting on shared-memory atomics with nothing else to run.  The tile plan
+// after a frame's binning counts the frame's heavy tiles and notes the frame
+// and the count in host-mapped memory; from that note the host launches the
+// morph's next frames (for kHeavyMemory frames after the last heavy one)
+// with the heavy resolve: its grid ends with `helpers` extra CTAs, and the
+// first helpers / (kBands - 1) heavy tiles in tile order are resolved by
+// kBands CTAs each, the tile's own CTA taking row band 0 and the helpers
+// bands 1 .. kBands - 1.  Every CTA of a tile reads all its records and
+// accumulates, composites and writes only the rows of its band, so no CTA
+// waits for another and the pixels are the ones a single CTA gives.  Frames
+// of morphs without heavy tiles use the plain resolve.
+constexpr uint32_t kHeavyRec = 8192;
+constexpr uint32_t kBands = 32;       // one row each
+constexpr uint32_t kHeavyMaxTiles = 64;
+__device__ __forceinline__ uint32_t band_rows(uint32_t b) {
+    constexpr uint32_t rpb = 32 / kBands;
+    return (rpb >= 32 ? 0xFFFFFFFFu : ((1u << rpb) - 1u)) << (b * rpb);
+}
+
 // A frame's tile regions from the previous frame's counts src_cnt (one CTA):
 // capacity count + count / 4 + 32 (or, with init, the atoms spread evenly),
 // regions in tile order, clipped to the buffer; the destination slot's
 // counters (cnt, ovf_cnt) are cleared.  Source and destination are the two
-// record slots, so the source's counts stay intact for its resolve.
+// record slots, so the source's counts stay intact for its resolve.  With a
+// note (host-mapped), a source frame with heavy tiles is noted as
+// frame_no << 32 | heavy tiles.
 struct PlanArgs {
     const uint32_t *src_cnt;
     uint32_t *off, *cap, *cnt;
     uint32_t ntiles;
     uint64_t init_atoms, rec_cap;
     uint32_t *ovf_cnt;
+    unsigned long long *note;
+    uint32_t frame_no;
 };
 __device__ __forceinline__ void tile_plan(const uint32_t *src_cnt, uint32_t *off, uint32_t *cap, uint32_t *cnt,
                                           uint32_t ntiles, uint64_t init_atoms, uint64_t rec_cap,
-                                          uint32_t *ovf_cnt) {
+                                          uint32_t *ovf_cnt, unsigned long long *note, uint32_t frame_no) {
+    uint32_t nheavy = 0;
     __shared__ uint32_t wsum[32];
     __shared__ unsigned long long carry;
     if (threadIdx.x == 0) carry = 0;
@@ -751,8 +784,10 @@ __device__ __forceinline__ void tile_plan(const uint32_t *src_cnt, uint32_t *off
     for (uint32_t t0 = 0; t0 < ntiles; t0 += 1024) {
         const uint32_t t = t0 + threadIdx.x;
         uint32_t c = 0;
+        bool heavy = false;
         if (t < ntiles) {
             const uint64_t seen = init_atoms ? (init_atoms * 5 / 4) / ntiles : src_cnt[t];
+            heavy = !init_atoms && seen > kHeavyRec;
             const uint64_t want = seen + seen / 4 + 32;
             c = want < (1ull << 30) ? (uint32_t)want : (1u << 30);
         }
@@ -773,7 +808,7 @@ __device__ __forceinline__ void tile_plan(const uint32_t *src_cnt, uint32_t *off
             cap[t] = (uint32_t)(end - st);
             cnt[t] = 0u;
         }
-        __syncthreads();
+        nheavy += (uint32_t)__syncthreads_count(heavy);
         if (threadIdx.x == 1023) {
             unsigned long long tot = 0;
             for (int w = 0; w < 32; ++w) tot += wsum[w];
@@ -781,12 +816,17 @@ __device__ __forceinline__ void tile_plan(const uint32_t *src_cnt, uint32_t *off
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) *ovf_cnt = 0u;
+    if (threadIdx.x == 0) {
+        *ovf_cnt = 0u;
+        if (note && nheavy)
+            *reinterpret_cast<volatile unsigned long long *>(note) = ((unsigned long long)frame_no << 32) | nheavy;
+    }
 }
 __global__ void __launch_bounds__(1024) k_tile_plan(const uint32_t *src_cnt, uint32_t *off, uint32_t *cap,
                                                     uint32_t *cnt, uint32_t ntiles, uint64_t init_atoms,
-                                                    uint64_t rec_cap, uint32_t *ovf_cnt) {
-    tile_plan(src_cnt, off, cap, cnt, ntiles, init_atoms, rec_cap, ovf_cnt);
+                                                    uint64_t rec_cap, uint32_t *ovf_cnt, unsigned long long *note,
+                                                    uint32_t frame_no) {
+    tile_plan(src_cnt, off, cap, cnt, ntiles, init_atoms, rec_cap, ovf_cnt, note, frame_no);
 }
 struct PlanBatch {
     uint32_t n;
@@ -797,7 +837,7 @@ static_assert(sizeof(BinBatch) < 32000, "batched binning arguments exceed the ke
 static_assert(sizeof(PlanBatch) < 32000, "batched plan arguments exceed the kernel parameter space");
 __global__ void __launch_bounds__(1024) k_tile_plan_batch(const __grid_constant__ PlanBatch pb) {
     const PlanArgs &a = pb.job[blockIdx.x];
-    tile_plan(a.src_cnt, a.off, a.cap, a.cnt, a.ntiles, a.init_atoms, a.rec_cap, a.ovf_cnt);
+    tile_plan(a.src_cnt, a.off, a.cap, a.cnt, a.ntiles, a.init_atoms, a.rec_cap, a.ovf_cnt, a.note, a.frame_no);
 }
 
 __global__ void __launch_bounds__(256) k_frame_scatter(const uint4 *__restrict__ spl, const uint32_t *n_dev,
@@ -910,6 +950,7 @@ struct ResolveOpts {
     BgArgs bg;                     // the background under the composite
     uint32_t only_rank;            // one blob alone (0xFFFFFFFF: the composite of all)
     uint8_t *aux;                  //   and its per-pixel coverage / feather layer code
+    uint32_t helpers;              // heavy resolve: CTAs after the tiles' own, row-band helpers of heavy tiles
 };
 
 // Where a frame's binned records are: tile t's region starts at off[t] and
@@ -946,6 +987,73 @@ __device__ __forceinline__ void visit_tile(const TileRecs &r, uint32_t t, F &&f)
 // of the (2R + 1) x 32 px square window; erosion runs on the bitmap.  Pixels
 // outside the window count as outside the blob: every tile pixel is more
 // than 32 R >= feather pixels from them, so no layer below feather changes.
+// The rows of the tile (bit r: row ty0 + r) that a record's valid corners reach.
+__device__ __forceinline__ uint32_t record_rows(const uint4 &s, uint32_t ty0) {
+    const uint32_t r0 = (s.x >> 16) - ty0, valid = (s.y >> 16) & 15u;
+    uint32_t m = 0;
+    if (r0 < 32u && (valid & 3u)) m |= 1u << r0;
+    if (r0 + 1u < 32u && (valid & 12u)) m |= 1u << (r0 + 1u);
+    return m;
+}
+// Which tile and rows CTA `cta` of a heavy resolve grid takes when it is a
+// helper (cta >= ntiles) or the own CTA of a heavy tile; false for a helper
+// without a heavy tile.  Block-wide (every thread calls it); heavy tiles
+// counted in tile order from cnt.  Out of line.
+__device__ __noinline__ bool heavy_assign(const TileRecs &tr, uint32_t ntiles, const ResolveOpts &o, uint32_t cta,
+                                          uint32_t *tile, uint32_t *rows) {
+    __shared__ uint32_t wsum[8], s_kth;
+    const uint32_t per = kBands - 1, served = min(o.helpers / per, kHeavyMaxTiles);
+    const bool helper = cta >= ntiles;
+    const uint32_t k = helper ? (cta - ntiles) / per : 0u, lim = helper ? 0u : cta;
+    // thread t counts the heavy tiles of its chunk of the tile range
+    const uint32_t chunk = (ntiles + 255u) / 256u, t0 = threadIdx.x * chunk, t1 = min(t0 + chunk, ntiles);
+    uint32_t c = 0, before = 0;
+    for (uint32_t t = t0; t < t1; ++t)
+        if (tr.cnt[t] > kHeavyRec) {
+            ++c;
+            before += t < lim;
+        }
+    // exclusive prefix of c over the block, the total and the count before lim
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    uint32_t x = c;
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= (uint32_t)d) x += y;
+    }
+    if (threadIdx.x == 0) s_kth = 0xFFFFFFFFu;
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    uint32_t pre = x - c, total = 0;
+    for (uint32_t w = 0; w < 8; ++w) {
+        if (w < wid) pre += wsum[w];
+        total += wsum[w];
+    }
+    for (int d = 16; d; d >>= 1) before += __shfl_xor_sync(0xffffffffu, before, d);
+    __syncthreads();
+    if (lane == 0) wsum[wid] = before;
+    __syncthreads();
+    before = 0;
+    for (uint32_t w = 0; w < 8; ++w) before += wsum[w];
+    if (helper && k >= pre && k < pre + c) {
+        uint32_t left = k - pre;
+        for (uint32_t t = t0; t < t1; ++t)
+            if (tr.cnt[t] > kHeavyRec && left-- == 0) {
+                s_kth = t;
+                break;
+            }
+    }
+    __syncthreads();
+    if (!helper) {
+        *tile = cta;
+        *rows = before < served ? band_rows(0) : 0xFFFFFFFFu;
+        return true;
+    }
+    if (k >= min(total, served) || s_kth == 0xFFFFFFFFu) return false;
+    *tile = s_kth;
+    *rows = band_rows(1u + (cta - ntiles) % per);
+    return true;
+}
+
 // The composite rank a record takes part in: its own, or none when one other
 // blob is drawn alone.
 __device__ __forceinline__ uint32_t rank_of(const ResolveOpts &o, const uint4 &s) {
@@ -1016,10 +1124,14 @@ __host__ __device__ inline size_t feather_smem(uint32_t F) {
 // frame_resolve).
 constexpr uint32_t kStackMin = 4;
 
-// The resolve of one 32 x 32 tile of a frame.
-__device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles_x, uint32_t width, uint32_t height,
-                                              uint32_t density, uint8_t *out, const ResolveOpts &o, uint32_t tile) {
+// The resolve of one 32 x 32 tile of a frame; Banded: only the tile's rows
+// in `rows` (bit r: row r), the rest left to the tile's other CTAs.
+template <bool Banded>
+__device__ __forceinline__ void resolve_tile(const TileRecs &tr, uint32_t tiles_x, uint32_t width, uint32_t height,
+                                             uint32_t density, uint8_t *out, const ResolveOpts &o, uint32_t tile,
+                                             uint32_t rows) {
     extern __shared__ __align__(16) unsigned char sm[];
+    constexpr bool banded = Banded;
     __shared__ uint32_t red[2][8];  // per-warp rank minima, alternating between blob ranks
     __shared__ int s_over;
     // packed mode: six 32-bit accumulators per pixel (a warp's 32-bit
@@ -1062,7 +1174,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
     const bool counted = density > 1;
     for (int mode = (!counted && nrec >= kPackRec) ? 1 : 0; mode < 2; ++mode) {
         const bool packed = mode == 0;
-        const bool cached = packed && nrec <= (uint32_t)kRecCache;
+        const bool cached = packed && nrec <= (uint32_t)kRecCache && !banded;
         uint32_t mn = 0xFFFFFFFFu;
         if (packed) {
             for (int i = threadIdx.x; i < 6 * 1024; i += 256) pW[i] = 0u;
@@ -1090,7 +1202,10 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
         if (threadIdx.x == 0) s_over = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) { n[q] = 0; c0[q] = 0; lay[q] = 0; }
-        if (!cached) visit_tile(tr, tile, [&](const uint4 &v) { mn = min(mn, rank_of(o, v)); });
+        if (!cached)
+            visit_tile(tr, tile, [&](const uint4 &v) {
+                if (!banded || (record_rows(v, ty0) & rows)) mn = min(mn, rank_of(o, v));
+            });
         for (int w = 16; w; w >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, w));
         if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = mn;
         __syncthreads();
@@ -1109,7 +1224,8 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
             // and then the overflow list (other tiles' entries skipped)
             const uint32_t iter = cached ? nrec : nmain + novf;
             // one record's valid corners into the accumulators
-            auto add_corners = [&](const uint4 &s) {
+            // (rows of the tile this call may add to: band, constant on the cached path)
+            auto add_corners = [&](const uint4 &s, uint32_t band) {
                 const uint32_t px = s.x & 0xFFFFu, py = s.x >> 16;
                 const uint32_t xf = s.y & 255u, yf = (s.y >> 8) & 255u, valid = (s.y >> 16) & 15u;
                 const uint32_t wx[2] = {255u - xf, xf}, wy[2] = {255u - yf, yf};
@@ -1118,7 +1234,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                 for (int k = 0; k < 4; ++k) {
                     if (!(valid & (1u << k))) continue;
                     uint32_t cx = px + (k & 1) - tx0, cy = py + (k >> 1) - ty0;
-                    if (cx >= (uint32_t)kTile || cy >= (uint32_t)kTile) continue;
+                    if (cx >= (uint32_t)kTile || cy >= (uint32_t)kTile || !((band >> cy) & 1u)) continue;
                     uint32_t li = cy * kTile + cx;
                     uint32_t W = wx[k & 1] * wy[k >> 1];
                     if (packed) {
@@ -1159,6 +1275,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                             s = tr.ovf[j - nmain];
                             mine = ovf_tile(s) == tile;
                         }
+                        if (banded && mine) mine = (record_rows(s, ty0) & rows) != 0;
                         if (mine) {
                             if (s.w == cur) use = true;
                             else if (s.w > cur) nxt = min(nxt, rank_of(o, s));
@@ -1177,6 +1294,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                             for (int k = 0; k < 4; ++k) {
                                 const uint32_t cx = (x0 & 0xFFFFu) + (k & 1) - tx0, cy = (x0 >> 16) + (k >> 1) - ty0;
                                 if (cx >= (uint32_t)kTile || cy >= (uint32_t)kTile) continue;  // uniform
+                                if (banded && !((rows >> cy) & 1u)) continue;                  // uniform
                                 const bool a = same && ((valid >> k) & 1u);
                                 // at most 32 records: 32 W and 32 W c stay below 2^32
                                 const uint32_t W = a ? ((k & 1) ? xf : 255u - xf) * ((k >> 1) ? yf : 255u - yf) : 0u;
@@ -1209,7 +1327,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                             if (same) use = false;
                         }
                     }
-                    if (use) add_corners(s);
+                    if (use) add_corners(s, banded ? rows : 0xFFFFFFFFu);
                 }
             } else {
                 for (uint32_t j = threadIdx.x; j < iter; j += 256) {
@@ -1226,7 +1344,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
                         if (s.w > cur) nxt = min(nxt, rank_of(o, s));
                         continue;
                     }
-                    add_corners(s);
+                    add_corners(s, 0xFFFFFFFFu);
                 }
             }
             for (int w = 16; w; w >>= 1) nxt = min(nxt, __shfl_xor_sync(0xffffffffu, nxt, w));
@@ -1242,6 +1360,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const uint32_t li = threadIdx.x + 256 * q;
+                if (banded && !((rows >> (li >> 5)) & 1u)) continue;  // another CTA's band
                 unsigned long long W, sr, sg, sb, sa;
                 uint32_t cnt;
                 if (packed) {
@@ -1298,7 +1417,7 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
     for (int q = 0; q < 4; ++q) {
         const uint32_t li = threadIdx.x + 256 * q;
         const uint32_t gy = ty0 + (li >> 5), gx = tx0 + (li & 31u);
-        if (gy >= height || gx >= width) continue;
+        if (gy >= height || gx >= width || (banded && !((rows >> (li >> 5)) & 1u))) continue;
         uint32_t px;
         if (o.keep_bg) px = over_background(n[q], c0[q], st[q], bg_colour(o.bg, gx, gy));
         else px = n[q] == 0 ? 0u : (n[q] == 1 ? c0[q] : over_bytes(st[q]));
@@ -1307,10 +1426,43 @@ __device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles
     }
 }
 
+// A row band of a heavy tile (out of line: the common path keeps its registers).
+__device__ __noinline__ void resolve_band(const TileRecs &tr, uint32_t tiles_x, uint32_t width, uint32_t height,
+                                          uint32_t density, uint8_t *out, const ResolveOpts &o, uint32_t tile,
+                                          uint32_t rows) {
+    resolve_tile<true>(tr, tiles_x, width, height, density, out, o, tile, rows);
+}
+// CTA `cta` of a frame's resolve grid: its own tile, or (Heavy) a row band
+// of a heavy tile (helpers past the tiles' own CTAs).
+template <bool Heavy>
+__device__ __forceinline__ void frame_resolve(const TileRecs &tr, uint32_t tiles_x, uint32_t width, uint32_t height,
+                                              uint32_t density, uint8_t *out, const ResolveOpts &o, uint32_t cta) {
+    if (Heavy) {
+        const uint32_t ntiles = tiles_x * o.tiles_y;
+        if (cta >= ntiles || tr.cnt[cta] > kHeavyRec) {  // uniform
+            uint32_t tile = cta, rows = 0xFFFFFFFFu;
+            if (!heavy_assign(tr, ntiles, o, cta, &tile, &rows)) return;
+            if (rows != 0xFFFFFFFFu) {
+                resolve_band(tr, tiles_x, width, height, density, out, o, tile, rows);
+                return;
+            }
+        }
+    }
+    resolve_tile<false>(tr, tiles_x, width, height, density, out, o, cta, 0xFFFFFFFFu);
+}
+
 __global__ void __launch_bounds__(256, 4) k_frame_resolve(const __grid_constant__ TileRecs tr, uint32_t tiles_x,
                                                         uint32_t width, uint32_t height, uint32_t density,
                                                         uint8_t *out, const __grid_constant__ ResolveOpts o) {
-    frame_resolve(tr, tiles_x, width, height, density, out, o, blockIdx.x);
+    frame_resolve<false>(tr, tiles_x, width, height, density, out, o, blockIdx.x);
+}
+// The resolve of a frame whose morph has had heavy tiles (o.helpers CTAs
+// after the tiles' own).
+__global__ void __launch_bounds__(256, 4) k_frame_resolve_heavy(const __grid_constant__ TileRecs tr,
+                                                              uint32_t tiles_x, uint32_t width, uint32_t height,
+                                                              uint32_t density, uint8_t *out,
+                                                              const __grid_constant__ ResolveOpts o) {
+    frame_resolve<true>(tr, tiles_x, width, height, density, out, o, blockIdx.x);
 }
 struct ResolveJob {
     TileRecs tr;
@@ -1327,7 +1479,13 @@ static_assert(sizeof(ResolveBatch) < 32000, "batched resolve arguments exceed th
 __global__ void __launch_bounds__(256, 4) k_frame_resolve_batch(const __grid_constant__ ResolveBatch rb) {
     const uint32_t j = batch_job(rb.start, rb.n, blockIdx.x);
     const ResolveJob &a = rb.job[j];
-    frame_resolve(a.tr, a.tiles_x, a.width, a.height, a.density, a.out, a.o, blockIdx.x - rb.start[j]);
+    frame_resolve<false>(a.tr, a.tiles_x, a.width, a.height, a.density, a.out, a.o, blockIdx.x - rb.start[j]);
+}
+// The same when a job of the launch has had heavy tiles.
+__global__ void __launch_bounds__(256, 4) k_frame_resolve_batch_heavy(const __grid_constant__ ResolveBatch rb) {
+    const uint32_t j = batch_job(rb.start, rb.n, blockIdx.x);
+    const ResolveJob &a = rb.job[j];
+    frame_resolve<true>(a.tr, a.tiles_x, a.width, a.height, a.density, a.out, a.o, blockIdx.x - rb.start[j]);
 }
 
 __global__ void k_keyframe_copy(const uint32_t *__restrict__ display, const uint8_t *__restrict__ present,
@@ -1445,6 +1603,48 @@ static int ensure_slots(RenderWork *w, uint64_t n, uint32_t ntiles, cudaStream_t
     return AM_OK;
 }
 
+// Row-band helper CTAs for the next frame's heavy tiles, sized from the note
+// the morph's recent frames left: none while they have had no heavy tiles
+// (or when the note could not be allocated), so such frames launch exactly
+// their tiles.  The note is read without waiting; the frames in flight may
+// not have written theirs yet.
+constexpr uint32_t kHeavyMemory = 240;  // frames a heavy-tile note stays in force
+static uint32_t heavy_helpers(RenderWork *w) {
+    if (!w->note_tried) {
+        w->note_tried = true;
+        void *h = nullptr, *d = nullptr;
+        if (cudaHostAlloc(&h, sizeof(unsigned long long), cudaHostAllocMapped) == cudaSuccess) {
+            *static_cast<unsigned long long *>(h) = 0;
+            if (cudaHostGetDevicePointer(&d, h, 0) == cudaSuccess) {
+                w->note_host = static_cast<unsigned long long *>(h);
+                w->note_dev = static_cast<unsigned long long *>(d);
+            } else {
+                cudaFreeHost(h);
+            }
+        }
+        cudaGetLastError();  // a failed allocation only leaves the helpers off
+    }
+    if (!w->note_host) return 0;
+    const unsigned long long v = *reinterpret_cast<volatile unsigned long long *>(w->note_host);
+    const uint32_t seen = (uint32_t)(v >> 32), count = (uint32_t)v;
+    if (count == 0 || w->frame_no - seen > kHeavyMemory) return 0;
+    return std::min(count, kHeavyMaxTiles) * (kBands - 1);
+}
+// The heavy-tile field of a frame's resolve options; counts the frame (its
+// plan notes heavy tiles under this number).
+static void resolve_heavy(RenderWork *w, ResolveOpts &o) {
+    o.helpers = heavy_helpers(w);
+    ++w->frame_no;
+    w->last_helpers = o.helpers;
+}
+
+void render_heavy_tiles(RenderWork *w, uint32_t *tiles, uint32_t *helpers) {
+    render_quiesce(w);  // the plans that note heavy tiles run on the binning stream
+    const unsigned long long v = w->note_host ? *reinterpret_cast<volatile unsigned long long *>(w->note_host) : 0ull;
+    if (tiles) *tiles = (uint32_t)v;
+    if (helpers) *helpers = w->last_helpers;
+}
+
 // The resolve's render options for a frame of pair f at local time t.
 static ResolveOpts resolve_opts(const RenderScene &sc, uint32_t f, double t, uint32_t tiles_y) {
     ResolveOpts o;
@@ -1538,7 +1738,7 @@ static int fused_bin(RenderWork *w, const RenderScene &sc, const FrameArgs &fa, 
         // plan from the atom count; the slot's last resolve must be done
         if (piped) AMG_CUDA(cudaStreamWaitEvent(w->bs, A->resolved, 0));
         AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, A->off, A->cap, A->cnt, ntiles, std::max<uint64_t>(sc.N, 1),
-                   w->slot_rec_cap, A->ovf_cnt);
+                   w->slot_rec_cap, A->ovf_cnt, (unsigned long long *)nullptr, 0u);
         A->tiles = ntiles;
         A->atoms = sc.N;
     }
@@ -1710,18 +1910,27 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
         }
         tr = TileRecs{w->rec, w->tile_off, w->tile_cnt, w->tile_cnt, w->rec, w->zero, 0u};
     }
-    const ResolveOpts o = resolve_opts(sc, (uint32_t)f, t, tiles_y);
+    ResolveOpts o = resolve_opts(sc, (uint32_t)f, t, tiles_y);
+    resolve_heavy(w, o);
     if (w->prof) w->prof->open(s);
     {
         static const cudaError_t attr = cudaFuncSetAttribute(
             k_frame_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
             (int)std::max(kResolveSmem + feather_smem(kMaxFeather), occupancy_smem(1)));
+        static const cudaError_t hattr = cudaFuncSetAttribute(
+            k_frame_resolve_heavy, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (int)std::max(kResolveSmem + feather_smem(kMaxFeather), occupancy_smem(1)));
         AMG_CUDA(attr);
+        AMG_CUDA(hattr);
     }
     const size_t rsm = std::max(kResolveSmem + feather_smem(o.feather),
                                 sc.resolve_ctas ? occupancy_smem(sc.resolve_ctas) : (size_t)0);
-    AMG_LAUNCH(k_frame_resolve, ntiles, 256, rsm, s, tr, tiles_x, sc.width, sc.height,
-               sc.density ? sc.density : 1u, out, o);
+    if (o.helpers)
+        AMG_LAUNCH(k_frame_resolve_heavy, ntiles + o.helpers, 256, rsm, s, tr, tiles_x, sc.width, sc.height,
+                   sc.density ? sc.density : 1u, out, o);
+    else
+        AMG_LAUNCH(k_frame_resolve, ntiles, 256, rsm, s, tr, tiles_x, sc.width, sc.height,
+                   sc.density ? sc.density : 1u, out, o);
     if (w->prof) w->prof->close(PROF_RESOLVE, s);
     if (fused) {
         // the next frame's tile regions (the other slot) from this frame's
@@ -1731,7 +1940,7 @@ int render_frame(RenderWork *w, const RenderScene &sc, double time, uint64_t fra
             AMG_CUDA(cudaStreamWaitEvent(w->bs, B->resolved, 0));
         }
         AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, B->off, B->cap, B->cnt, ntiles, (uint64_t)0,
-                   w->slot_rec_cap, B->ovf_cnt);
+                   w->slot_rec_cap, B->ovf_cnt, w->note_dev, w->frame_no);
         B->tiles = ntiles;
         B->atoms = sc.N;
         w->cur ^= 1;
@@ -1752,8 +1961,12 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
     static const cudaError_t rattr = cudaFuncSetAttribute(
         k_frame_resolve_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
         (int)std::max(kResolveSmem + feather_smem(kMaxFeather), occupancy_smem(1)));
+    static const cudaError_t hattr = cudaFuncSetAttribute(
+        k_frame_resolve_batch_heavy, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)std::max(kResolveSmem + feather_smem(kMaxFeather), occupancy_smem(1)));
     AMG_CUDA(battr);
     AMG_CUDA(rattr);
+    AMG_CUDA(hattr);
     // about 20 KB of launch arguments: on the heap
     std::vector<unsigned char> store(sizeof(BinBatch) + sizeof(ResolveBatch) + sizeof(PlanBatch) + 64);
     BinBatch &bb = *new (store.data()) BinBatch();
@@ -1767,6 +1980,7 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
     };
     std::vector<Flip> flips;
     uint32_t bin_ctas = 0, tiles = 0;
+    bool heavy = false;  // a job of the launch gets row-band helpers
     size_t bsm = 0, rsm = 0;
     // Pipelined (pipe given): pair preparation, binning and the next tile
     // plans run on pipe->bs, the resolves on s; the plans wait for the
@@ -1788,7 +2002,8 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
             AMG_CUDA(cudaEventRecord(pipe->binned[group], ps));
             AMG_CUDA(cudaStreamWaitEvent(s, pipe->binned[group], 0));
         }
-        AMG_LAUNCH(k_frame_resolve_batch, tiles, 256, rsm, s, rb);
+        if (heavy) AMG_LAUNCH(k_frame_resolve_batch_heavy, tiles, 256, rsm, s, rb);
+        else AMG_LAUNCH(k_frame_resolve_batch, tiles, 256, rsm, s, rb);
         if (pipe && pipe->prev_resolved && group == 0) AMG_CUDA(cudaStreamWaitEvent(ps, pipe->prev_resolved, 0));
         AMG_LAUNCH(k_tile_plan_batch, pb.n, 1024, 0, ps, pb);
         AMG_CUDA(cudaGetLastError());
@@ -1801,6 +2016,7 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
         flips.clear();
         pb.n = 0;
         bin_ctas = tiles = 0;
+        heavy = false;
         bsm = rsm = 0;
         return AM_OK;
     };
@@ -1848,7 +2064,7 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
         RenderWork::Slot *A = &w->slot[w->cur], *B = &w->slot[w->cur ^ 1];
         if (A->tiles != ntiles || A->atoms != sc.N) {
             AMG_LAUNCH(k_tile_plan, 1, 1024, 0, ps, A->cnt, A->off, A->cap, A->cnt, ntiles,
-                       std::max<uint64_t>(sc.N, 1), w->slot_rec_cap, A->ovf_cnt);
+                       std::max<uint64_t>(sc.N, 1), w->slot_rec_cap, A->ovf_cnt, (unsigned long long *)nullptr, 0u);
             A->tiles = ntiles;
             A->atoms = sc.N;
         }
@@ -1864,16 +2080,19 @@ int render_frames_batch(const RenderJob *jobs, size_t n, cudaStream_t s, const B
         ResolveJob &r = rb.job[k];
         r.tr = TileRecs{A->rec, A->off, A->cnt, A->cap, A->ovf, A->ovf_cnt, b.ovf_cap};
         r.o = resolve_opts(sc, (uint32_t)f, t, tiles_y);
+        resolve_heavy(w, r.o);
         r.out = J.out;
         r.tiles_x = tiles_x;
         r.width = sc.width;
         r.height = sc.height;
         r.density = sc.density ? sc.density : 1u;
         rb.start[k] = tiles;
-        tiles += ntiles;
+        tiles += ntiles + r.o.helpers;
+        heavy |= r.o.helpers != 0;
         rsm = std::max({rsm, kResolveSmem + feather_smem(r.o.feather),
                         sc.resolve_ctas ? occupancy_smem(sc.resolve_ctas) : (size_t)0});
-        pb.job[k] = PlanArgs{A->cnt, B->off, B->cap, B->cnt, ntiles, 0, w->slot_rec_cap, B->ovf_cnt};
+        pb.job[k] = PlanArgs{A->cnt, B->off, B->cap, B->cnt, ntiles, 0, w->slot_rec_cap, B->ovf_cnt, w->note_dev,
+                             w->frame_no};
         flips.push_back(Flip{w, B, ntiles, sc.N});
         pb.n = k + 1;
         if (pb.n == kBatchFrames && (rc = flush())) return rc;

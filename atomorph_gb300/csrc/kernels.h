@@ -333,6 +333,11 @@ int launch_keyframe_copy(const uint32_t *display, const uint8_t *present, uint32
                          uint32_t width, uint32_t height, uint8_t *out, cudaStream_t s);
 // Drops cached per-key-frame-pair data (chains or settings changed).
 void render_invalidate(RenderWork *w);
+// Heavy tiles of the morph's recent frames (tiles resolved in row bands by
+// helper CTAs): the count the last frame that had any recorded (0: none
+// yet) and the helper CTAs of the last resolve launched.  Waits for the
+// binning stream, whose tile plans record the counts.
+void render_heavy_tiles(RenderWork *w, uint32_t *tiles, uint32_t *helpers);
 // Waits for the render work's own binning stream (frames resolve on the
 // caller's render stream; their binning may still be running on it).
 void render_quiesce(RenderWork *w);

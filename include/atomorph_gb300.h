@@ -386,6 +386,14 @@ void    *am_get_stream(am_morph *m);        /* cudaStream_t that renders run on 
 int      am_profile_enable(am_morph *m, int on);
 size_t   am_profile_read(am_morph *m, const char **names, double *ms, uint64_t *launches, size_t cap);
 uint64_t am_launch_count(void);             /* kernels launched by this library, process-wide */
+/* Heavy tiles: output tiles holding more than 8192 binned atom records
+ * (atoms crowded or stacked by a chain much wider than a key frame's blob)
+ * are resolved in 32 row bands by helper CTAs in the frames after one of the
+ * morph's frames had them.  *tiles = the heavy tiles of the last frame that
+ * had any (0 when none yet), *helpers = the helper CTAs of the last resolve
+ * launched.  Waits for the morph's binning work, so every frame rendered so
+ * far has reported.  Either pointer may be null. */
+int      am_get_heavy_tiles(am_morph *m, uint32_t *tiles, uint32_t *helpers);
 int      am_device_sync(am_morph *m);       /* waits for the handle's stream */
 
 #ifdef __cplusplus

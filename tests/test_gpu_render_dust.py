@@ -79,3 +79,45 @@ def test_stacked_atoms_match_the_oracle(capi, oracle):
         ref = oracle.render(st, t).astype(np.int32)
         assert int(np.abs(got - ref).max()) <= 1, t
     m.close()
+
+
+@pytest.mark.parametrize("density", [1, 2])
+def test_heavy_tiles_resolved_in_row_bands(capi, oracle, density):
+    """A 96 x 96 blob and a 16 x 16 square matched to a 3 x 3 dot and a
+    12 x 12 square in one 32 x 32 tile: near the second key frame that tile
+    holds over 9,000 atoms of two blob ranks (a heavy tile).  The first
+    frames resolve it with one CTA and note it; the same frames again are
+    resolved with 31 helper CTAs, one row band each.  Both within 1 LSB of
+    the oracle and equal byte for byte."""
+    rng = np.random.default_rng(11)
+    a = np.zeros((128, 128, 4), np.uint8)
+    a[4:100, 4:100] = (200, 40, 90, 255)
+    a[4:100, 4:100, :3] += rng.integers(0, 40, (96, 96, 3)).astype(np.uint8)
+    a[108:124, 108:124] = (30, 90, 220, 255)
+    b = np.zeros((128, 128, 4), np.uint8)
+    b[60:63, 60:63] = (210, 50, 80, 255)
+    b[40:52, 40:52] = (40, 100, 210, 255)
+    frames = [a, b]
+    m = capi.Morph()
+    m.load(frames, seed=5, blob_delimiter=0, motion=capi.LINEAR, fading=capi.PERLIN, density=density)
+    assert m.run_until(capi.STATE_ATOM_MORPHING) == capi.STATE_ATOM_MORPHING
+    w, pts, order = m.export_chains()
+    assert m.chains == 2 and int(w.max()) >= 96 * 96 * density
+    colors, present = orc.stored_frames(frames, 0, oracle)
+    st = dict(K=2, width=m.width, height=m.height, bbox=_bbox(frames), seed=5, motion=capi.LINEAR,
+              fading=capi.PERLIN, delimiter=0, density=density, colors=colors, present=present, widths=w,
+              pts=pts, blob_order=order, frame_keys=np.arange(2, dtype=np.uint64))
+    ts = (0.5, 0.47, 0.53, 0.2)
+    assert m.heavy_tiles() == (0, 0)
+    solo = m.render(ts[0])  # nothing noted yet: one CTA per tile
+    tiles, helpers = m.heavy_tiles()
+    assert tiles >= 1 and helpers == 0
+    banded = [m.render(t) for t in ts]
+    tiles2, helpers = m.heavy_tiles()
+    assert tiles2 >= 1 and helpers == 31 * tiles2
+    assert np.array_equal(solo, banded[0])
+    for t, f in zip(ts, banded):
+        ref = oracle.render(st, t).astype(np.int32)
+        assert int(np.abs(f.astype(np.int32) - ref).max()) <= 1, t
+        assert f[..., 3].any()
+    m.close()
