@@ -948,6 +948,33 @@ def profile_case(args):
     return res
 
 
+def profile_heavy(args):
+    """A frame with a heavy tile (more than 8192 binned records): batch job
+    19 (398,786 atoms, 512^2, 7 key frames) at t = 0.1875, where one tile
+    holds 181,428 records, after 200 plain sweeps.  The first render resolves
+    the tile with one CTA (k_frame_resolve); the plan notes it, and the next
+    renders resolve it in 32 row bands (k_frame_resolve_heavy).  Serialised
+    frames (render_pipeline 0).  The program of the heavy-tile ncu capture."""
+    import torch
+    from atomorph_gb300 import capi, synth
+
+    j, t = 19, 0.1875
+    m = capi.Morph()
+    m.load(synth.workload("batch", j), seed=j + 1, blob_delimiter=0, motion=capi.SPLINE)
+    if m.run_until(capi.STATE_ATOM_MORPHING) != capi.STATE_ATOM_MORPHING:
+        raise RuntimeError("pipeline stopped early")
+    m.refine(200, capi.PROPOSAL_RANDOM)
+    m.tune(render_pipeline=0)
+    out = torch.empty((m.height, m.width, 4), dtype=torch.uint8, device="cuda")
+    for _ in range(args.frames):
+        m.render_device(t, out.data_ptr())
+    torch.cuda.synchronize()
+    tiles, helpers = m.heavy_tiles()
+    res = {"profile_heavy": f"batch job {j} at t={t}", "atoms": m.atoms, "heavy_tiles": tiles, "helpers": helpers}
+    m.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -980,10 +1007,15 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="run every kernel of the path a few times on --workload (for ncu captures) and exit")
     ap.add_argument("--workload", default=WORKLOAD, help="workload of --profile-case")
-    ap.add_argument("--frames", type=int, default=3, help="atom frames of --profile-case")
+    ap.add_argument("--frames", type=int, default=3, help="atom frames of --profile-case / --profile-heavy")
+    ap.add_argument("--profile-heavy", action="store_true",
+                    help="render a frame with a heavy tile --frames times (for ncu captures) and exit")
     args = ap.parse_args()
     if args.profile_case:
         print(json.dumps(profile_case(args)))
+        return
+    if args.profile_heavy:
+        print(json.dumps(profile_heavy(args)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
