@@ -1639,10 +1639,12 @@ static void resolve_heavy(RenderWork *w, ResolveOpts &o) {
 }
 
 void render_heavy_tiles(RenderWork *w, uint32_t *tiles, uint32_t *helpers) {
+    // (no render work yet: the morph has used no GPU, so no frame either)
     render_quiesce(w);  // the plans that note heavy tiles run on the binning stream
-    const unsigned long long v = w->note_host ? *reinterpret_cast<volatile unsigned long long *>(w->note_host) : 0ull;
+    const unsigned long long v =
+        (w && w->note_host) ? *reinterpret_cast<volatile unsigned long long *>(w->note_host) : 0ull;
     if (tiles) *tiles = (uint32_t)v;
-    if (helpers) *helpers = w->last_helpers;
+    if (helpers) *helpers = w ? w->last_helpers : 0u;
 }
 
 // The resolve's render options for a frame of pair f at local time t.

@@ -336,7 +336,8 @@ void render_invalidate(RenderWork *w);
 // Heavy tiles of the morph's recent frames (tiles resolved in row bands by
 // helper CTAs): the count the last frame that had any recorded (0: none
 // yet) and the helper CTAs of the last resolve launched.  Waits for the
-// binning stream, whose tile plans record the counts.
+// binning stream, whose tile plans record the counts.  w may be null (no
+// GPU work yet): zeros.
 void render_heavy_tiles(RenderWork *w, uint32_t *tiles, uint32_t *helpers);
 // Waits for the render work's own binning stream (frames resolve on the
 // caller's render stream; their binning may still be running on it).

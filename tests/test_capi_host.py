@@ -85,3 +85,13 @@ def test_not_busy_without_work(capi):
     assert m.lib.am_is_busy(m.h) == 0
     assert m.suspend(0.01) == capi.AM_OK
     assert m.state == capi.STATE_BLOB_DETECTION
+
+
+def test_heavy_tiles_before_any_frame(capi):
+    """No frame rendered: no heavy tiles noted, no helper CTAs launched; a
+    null handle is rejected."""
+    m = capi.Morph()
+    assert m.heavy_tiles() == (0, 0)
+    tiles, helpers = C.c_uint32(7), C.c_uint32(7)
+    assert m.lib.am_get_heavy_tiles(None, C.byref(tiles), C.byref(helpers)) == capi.AM_ERR_ARG
+    assert m.lib.am_get_heavy_tiles(m.h, None, None) == capi.AM_OK
